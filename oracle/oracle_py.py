@@ -1,0 +1,180 @@
+"""ctypes binding of the C oracle (oracle/sv_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as
+the checker and by bench.py's CPU-baseline leg.  Never by the product path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libsv_oracle.so")
+
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+
+_lib = None
+
+
+def build():
+    subprocess.check_call(["make", "-s", "-C", HERE, "lib"])
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        for name in ("orc_k_const", "orc_e_over_amu", "orc_coulomb_ke", "orc_elem_charge", "orc_amu"):
+            getattr(L, name).restype = C.c_double
+            getattr(L, name).argtypes = []
+        L.orc_species_mass.restype = C.c_double
+        L.orc_species_mass.argtypes = [C.c_int]
+        L.orc_direct_ref32.argtypes = [_f32p, _f32p, _f32p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                       C.c_double, C.c_int]
+        L.orc_direct_rot4_ref32.argtypes = L.orc_direct_ref32.argtypes
+        L.orc_direct_trans_ref32.argtypes = [_f32p, _f32p, _f32p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                             C.c_double, C.c_int, _i32p, _f32p, C.c_int]
+        L.orc_trans_images.restype = C.c_int
+        L.orc_trans_images.argtypes = [C.c_int, _i32p, C.c_void_p, C.c_int, _i32p, C.c_int]
+        L.orc_direct_f64.argtypes = [C.c_int64, _f64p, _f64p, _f64p, _i32p, C.c_void_p, C.c_int64,
+                                     C.c_double, C.c_double, C.c_int, C.c_int, C.c_void_p, _f64p, C.c_int]
+        L.orc_potential_f64.argtypes = [C.c_int64, _f64p, _f64p, _i32p, C.c_void_p, C.c_int64,
+                                        C.c_double, _f64p, C.c_int]
+        L.orc_leapfrog_ref32.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_int, C.c_float,
+                                         C.c_double, _f32p, C.c_int, C.c_int, C.c_void_p, _f32p, C.c_int]
+        L.orc_leapfrog_f64.argtypes = [C.c_int64, _f64p, _f64p, _f64p, _f64p, _i32p, _f64p, C.c_int,
+                                       C.c_double, C.c_double, C.c_double, C.c_double, _f64p, C.c_int,
+                                       C.c_int, C.c_void_p, C.c_void_p, C.c_int]
+        L.orc_energy_f64.argtypes = [C.c_int64, _f64p, _f64p, _f64p, _f64p, C.c_double,
+                                     C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int]
+        L.orc_rel_l2.argtypes = [C.c_int64, _f64p, _f64p, C.c_void_p, C.POINTER(C.c_double),
+                                 C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_double)]
+        _lib = L
+    return _lib
+
+
+def k_const():
+    return lib().orc_k_const()
+
+
+def e_over_amu():
+    return lib().orc_e_over_amu()
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def direct_ref32(pos4, vel4, acc4, eps, sym=0, images=None, domain_size=(2e-6, 2e-6, 0.0),
+                 threads=0, i_range=None, j_range=None):
+    """Reference-arithmetic direct sum on FP32 vec4 state; returns a new acc4."""
+    n = pos4.shape[0]
+    acc = np.ascontiguousarray(acc4, np.float32).copy()
+    i0, i1 = i_range or (0, n)
+    j0, j1 = j_range or (0, n)
+    p = np.ascontiguousarray(pos4, np.float32)
+    v = np.ascontiguousarray(vel4, np.float32)
+    if sym == 0:
+        lib().orc_direct_ref32(p, v, acc, i0, i1, j0, j1, eps, threads)
+    elif sym == 1:
+        lib().orc_direct_rot4_ref32(p, v, acc, i0, i1, j0, j1, eps, threads)
+    else:
+        img = np.ascontiguousarray(images, np.int32).reshape(-1)
+        dom = np.asarray(domain_size, np.float32)
+        lib().orc_direct_trans_ref32(p, v, acc, i0, i1, j0, j1, eps, img.size // 3, img, dom, threads)
+    return acc
+
+
+def trans_images(levels=2, axes=(1, 1, 0), lattice=None):
+    """Expanded image list (k, 3) of the reference's periodic Grid."""
+    box = 3 ** levels
+    ax = np.asarray(axes, np.int32)
+    cap = box ** 3 * 8 + 8
+    out = np.zeros(3 * cap, np.int32)
+    if lattice is not None:
+        lat = np.ascontiguousarray(lattice, np.int32).reshape(-1)
+        cnt = lib().orc_trans_images(box, ax, lat.ctypes.data_as(C.c_void_p), lat.size // 3, out, cap)
+    else:
+        cnt = lib().orc_trans_images(box, ax, None, 0, out, cap)
+    return out[: 3 * cnt].reshape(cnt, 3).copy()
+
+
+def direct_f64(state, eps2, sym=0, img_off=None, targets=None, threads=0, kconst=None):
+    """FP64 direct-sum acceleration (ntargets, 3) in m/s^2."""
+    x = np.ascontiguousarray(state["x"], np.float64).reshape(-1)
+    n = x.size // 3
+    q = np.ascontiguousarray(state["q"], np.float64)
+    m = np.ascontiguousarray(state["m"], np.float64)
+    st = np.ascontiguousarray(state["status"], np.int32)
+    t = None if targets is None else np.ascontiguousarray(targets, np.int64)
+    nt = n if t is None else t.size
+    out = np.zeros(3 * nt, np.float64)
+    io = None if img_off is None else np.ascontiguousarray(img_off, np.float64).reshape(-1)
+    nimg = 0 if io is None else io.size // 3
+    lib().orc_direct_f64(n, x, q, m, st, _ptr(t), nt, eps2, k_const() if kconst is None else kconst,
+                         sym, nimg, _ptr(io), out, threads)
+    return out.reshape(nt, 3)
+
+
+def leapfrog_ref32(pos4, vel4, acc4, t_inj, nsteps, dt, eps, efield=(0.0, 0.0, 0.0), sym=0,
+                   images=None, domain_size=(2e-6, 2e-6, 0.0), threads=0):
+    p = np.ascontiguousarray(pos4, np.float32).copy()
+    v = np.ascontiguousarray(vel4, np.float32).copy()
+    a = np.ascontiguousarray(acc4, np.float32).copy()
+    t = np.ascontiguousarray(t_inj, np.float32)
+    e = np.asarray(efield, np.float32)
+    img = None if images is None else np.ascontiguousarray(images, np.int32).reshape(-1)
+    nimg = 0 if img is None else img.size // 3
+    lib().orc_leapfrog_ref32(p.shape[0], p, v, a, t, nsteps, dt, eps, e, sym, nimg, _ptr(img),
+                             np.asarray(domain_size, np.float32), threads)
+    return p, v, a
+
+
+def leapfrog_f64(state, nsteps, dt, eps2, efield=(0.0, 0.0, 0.0), t0=0.0, sym=0, img_off=None,
+                 threads=0):
+    """FP64 DKD; returns (x, v, a_last) as (n, 3) arrays."""
+    x = np.ascontiguousarray(state["x"], np.float64).reshape(-1).copy()
+    v = np.ascontiguousarray(state["v"], np.float64).reshape(-1).copy()
+    n = x.size // 3
+    st = np.ascontiguousarray(state["status"], np.int32).copy()
+    a = np.zeros(3 * n, np.float64)
+    io = None if img_off is None else np.ascontiguousarray(img_off, np.float64).reshape(-1)
+    nimg = 0 if io is None else io.size // 3
+    lib().orc_leapfrog_f64(n, x, v, np.ascontiguousarray(state["q"], np.float64),
+                           np.ascontiguousarray(state["m"], np.float64), st,
+                           np.ascontiguousarray(state["t_inj"], np.float64), nsteps, dt, t0, eps2,
+                           k_const(), np.asarray(efield, np.float64), sym, nimg, _ptr(io), _ptr(a),
+                           threads)
+    return x.reshape(n, 3), v.reshape(n, 3), a.reshape(n, 3)
+
+
+def energy_f64(state, eps2, threads=0):
+    ke = C.c_double()
+    pe = C.c_double()
+    lib().orc_energy_f64(state["x"].shape[0], np.ascontiguousarray(state["x"], np.float64).reshape(-1),
+                         np.ascontiguousarray(state["v"], np.float64).reshape(-1),
+                         np.ascontiguousarray(state["q"], np.float64),
+                         np.ascontiguousarray(state["m"], np.float64), eps2, C.byref(ke), C.byref(pe),
+                         threads)
+    return ke.value, pe.value
+
+
+def rel_l2(a, ref, status=None):
+    """Reference accuracy metric: (per-particle rel-L2, max, argmax, global rel-L2)."""
+    a = np.ascontiguousarray(a, np.float64).reshape(-1)
+    r = np.ascontiguousarray(ref, np.float64).reshape(-1)
+    st = None if status is None else np.ascontiguousarray(status, np.int32)
+    l2 = C.c_double()
+    mx = C.c_double()
+    am = C.c_int64()
+    g = C.c_double()
+    lib().orc_rel_l2(a.size // 3, a, r, _ptr(st), C.byref(l2), C.byref(mx), C.byref(am), C.byref(g))
+    return l2.value, mx.value, am.value, g.value

@@ -1,0 +1,175 @@
+// ref_harness.cpp -- drives the reference SOLVEiT force methods headlessly.
+//
+// TEST INFRASTRUCTURE ONLY.  Linked against the reference sources as they
+// lie in the reference tree (see oracle/Makefile, target `ref`); the resulting binary
+// lives in oracle/_ref/ and is used to generate golden fixtures and to pin
+// the oracle restatement.  It fills a ChargedParticles instance by hand (the
+// shipped driver needs data files the reference does not ship) and calls the
+// reference's own updateAcceleration() / propagate*New() methods.
+//
+// usage: ref_harness <mode> <in.bin> <out.bin> [key=value ...]
+//   modes: direct | bh | fmm | dkd | grid
+//   keys : threads, sym (0 none, 1 rotational, 2 translational), levels,
+//          axes (e.g. 110), dom (domain size x,y,z in metres), theta, p,
+//          maxlevel, steps, dt, ez
+// in.bin : int32 n, float pos4[4n], float vel4[4n], float acc4[4n], float tinj[n]
+// out.bin: float pos4[4n], float vel4[4n], float acc4[4n]
+//          (grid mode: int32 count, int32 points[3*count] in the Grid's order)
+#include "force_calculation_methods.h"
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+static std::map<std::string, std::string> parse_kv(int argc, char **argv, int first) {
+    std::map<std::string, std::string> kv;
+    for (int i = first; i < argc; i++) {
+        const char *eq = std::strchr(argv[i], '=');
+        if (!eq) continue;
+        kv[std::string(argv[i], eq - argv[i])] = std::string(eq + 1);
+    }
+    return kv;
+}
+
+static double getd(std::map<std::string, std::string> &kv, const char *k, double d) {
+    auto it = kv.find(k);
+    return it == kv.end() ? d : std::atof(it->second.c_str());
+}
+
+int main(int argc, char **argv) {
+    if (argc < 4) {
+        std::fprintf(stderr, "usage: %s mode in.bin out.bin [k=v ...]\n", argv[0]);
+        return 2;
+    }
+    std::string mode = argv[1];
+    auto kv = parse_kv(argc, argv, 4);
+    const int threads = (int)getd(kv, "threads", 1);
+    const int sym = (int)getd(kv, "sym", 0);
+    const int levels = (int)getd(kv, "levels", 2);
+    std::string axes_s = kv.count("axes") ? kv["axes"] : "110";
+    vec3<int> axes(axes_s[0] - '0', axes_s[1] - '0', axes_s[2] - '0');
+
+    if (mode == "grid") {
+        int box_length = 1;
+        for (int l = 0; l < levels; l++) box_length *= 3;
+        Grid grid(box_length, axes);
+        FILE *fo = std::fopen(argv[3], "wb");
+        if (!fo) return 3;
+        int32_t cnt = grid.numLattice;
+        std::fwrite(&cnt, 4, 1, fo);
+        for (int i = 0; i < grid.numLattice; i++) {
+            int32_t p[3] = {grid.lattice[i].point.x, grid.lattice[i].point.y, grid.lattice[i].point.z};
+            std::fwrite(p, 4, 3, fo);
+        }
+        std::fclose(fo);
+        return 0;
+    }
+
+    FILE *fi = std::fopen(argv[2], "rb");
+    if (!fi) return 3;
+    int32_t n = 0;
+    if (std::fread(&n, 4, 1, fi) != 1 || n <= 0) return 4;
+    ParticleSystem ps;
+    ChargedParticles &cp = ps.chargedParticles;
+    cp.allocateMemory(n);
+    bool ok = std::fread(cp.position, 16, n, fi) == (size_t)n &&
+              std::fread(cp.velocity, 16, n, fi) == (size_t)n &&
+              std::fread(cp.acceleration, 16, n, fi) == (size_t)n &&
+              std::fread(cp.timeInjected, 4, n, fi) == (size_t)n;
+    std::fclose(fi);
+    if (!ok) return 4;
+    for (int i = 0; i < n; i++) {
+        cp.Efield1[i] = 0.0f;
+        cp.Efield2[i] = 0.0f;
+    }
+    cp.firstParticle = 0;
+    cp.lastParticle = n;
+
+    ps.params.numThreads = threads;
+    ps.params.symType = sym == 1 ? SymmetryType::rotational
+                      : sym == 2 ? SymmetryType::translational : SymmetryType::none;
+    ps.params.symmetryAxes = axes;
+    ps.params.numSymmetryLevels = levels;
+    std::string dom = kv.count("dom") ? kv["dom"] : "2e-6,2e-6,0";
+    float d[3] = {0, 0, 0};
+    std::sscanf(dom.c_str(), "%f,%f,%f", &d[0], &d[1], &d[2]);
+    ps.params.domainSize = vec3<float>(d[0], d[1], d[2]);
+
+    int box_length = 1;
+    for (int l = 0; l < levels; l++) box_length *= 3;
+    Grid grid(box_length, axes);
+
+    MultipoleMethodConstants mc;
+    MultipoleMethodVariables mv;
+    ForceCalculationMethod *fm = nullptr;
+    DirectForceCalculation *df = nullptr;
+    BarnesHutForceCalculation *bh = nullptr;
+    MultipoleMethodForceCalculation *fmm = nullptr;
+    if (mode == "direct" || mode == "dkd") {
+        df = new DirectForceCalculation(&ps);
+        fm = df;
+    } else if (mode == "bh") {
+        bh = new BarnesHutForceCalculation(&ps);
+        bh->setTheta((float)getd(kv, "theta", 0.5));
+        fm = bh;
+    } else if (mode == "fmm") {
+        fmm = new MultipoleMethodForceCalculation(&ps, &mc, &mv, FmmType::fmm);
+        fmm->setNumExpansions((int)getd(kv, "p", 8));
+        if (kv.count("maxlevel")) fmm->setMaxLevel((int)getd(kv, "maxlevel", 0));
+        fm = fmm;
+    } else {
+        std::fprintf(stderr, "unknown mode %s\n", mode.c_str());
+        return 2;
+    }
+    fm->setFirstParticle(0);
+    fm->setLastParticle(n);
+    fm->setGrid(&grid);
+
+    if (mode == "dkd") {
+        // LeapfrogDKD::runSimulation step structure (integration_schemes.cpp:
+        // 867-888) on the reference's own propagate*New methods; the uniform
+        // background field is added as computeBackgroundAcceleration adds the
+        // interpolated one (particles.cpp:496-520).
+        const int steps = (int)getd(kv, "steps", 1);
+        const float dt = (float)getd(kv, "dt", 1e-13);
+        const float ez = (float)getd(kv, "ez", 0.0);
+        const float inbound = 1.0f;
+        const double factor = PhysicalConstant::ELEM_CHARGE / PhysicalConstant::AMU;
+        for (int it = 1; it <= steps; it++) {
+            float tpos = dt * (it - 1);
+            float tvel = dt * (it - 1);
+            cp.propagatePositionNew(tpos, dt / 2, ps.params.crashParameters, nullptr);
+            tpos += dt / 2;
+            cp.zeroAcceleration();
+            fm->updateAcceleration();
+            for (int i = 0; i < n; i++) {
+                if (cp.acceleration[i].w != inbound) continue;
+                float efactor = factor * cp.position[i].w / cp.getMass(i);
+                vec3<float> e(0.0f, 0.0f, ez);
+                e *= efactor;
+                cp.acceleration[i].x += e.x;
+                cp.acceleration[i].y += e.y;
+                cp.acceleration[i].z += e.z;
+            }
+            cp.propagateVelocityNew(tvel, dt);
+            cp.propagatePositionNew(tpos, dt / 2, ps.params.crashParameters, nullptr);
+        }
+    } else {
+        fm->updateAcceleration();
+    }
+
+    FILE *fo = std::fopen(argv[3], "wb");
+    if (!fo) return 3;
+    std::fwrite(cp.position, 16, n, fo);
+    std::fwrite(cp.velocity, 16, n, fo);
+    std::fwrite(cp.acceleration, 16, n, fo);
+    std::fclose(fo);
+    // SimulationParameters' destructor releases members the headless set-up
+    // never initialised (file handles, storage arrays); leave without running
+    // destructors once the outputs are on disk.
+    std::fflush(nullptr);
+    std::_Exit(0);
+}

@@ -1,0 +1,587 @@
+/*
+ * sv_oracle.c -- CPU restatement of the SOLVEiT force-evaluation hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker that the CUDA path is compared with
+ * (parity tests, smoke check, bench.py cpu_baseline leg).  The product
+ * library never links or calls it.
+ *
+ * Build with -ffp-contract=off so that no multiply-add is fused: the
+ * reference is compiled for plain x86-64 (no FMA), and the *_ref32
+ * functions reproduce its rounding step by step.  Each function cites the
+ * reference file:line it restates (paths inside the SOLVEiT-Code project).
+ */
+#include "sv_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+/* ---- constants (constants.h:28-47) ----------------------------------- */
+
+static const long double REF_PI = 3.14159265358979323846264338328L;
+static const float REF_ELEM_CHARGE = 1.6021766e-19f;
+static const float REF_AMU = 1.66053904e-27f;
+static const float REF_EPS0 = 8.85419e-12f;
+
+double orc_k_const(void) {
+    /* K_CONST = (ELEM_CHARGE * ELEM_CHARGE) / (4 * PI * FREE_SPACE_PERMITTIVITY * AMU):
+     * float*float in float, the denominator in long double (constants.h:46). */
+    float e2 = REF_ELEM_CHARGE * REF_ELEM_CHARGE;
+    long double den = 4 * REF_PI * REF_EPS0 * REF_AMU;
+    return (double)((long double)e2 / den);
+}
+
+double orc_e_over_amu(void) {
+    /* factor = ELEM_CHARGE / AMU, float division (particles.cpp:500). */
+    float f = REF_ELEM_CHARGE / REF_AMU;
+    return (double)f;
+}
+
+double orc_coulomb_ke(void) {
+    /* ke = 1 / (4 pi eps0) stored as float (particles.cpp:565). */
+    float ke = (float)(1 / (4.0 * REF_PI * REF_EPS0));
+    return (double)ke;
+}
+
+double orc_elem_charge(void) { return (double)REF_ELEM_CHARGE; }
+double orc_amu(void) { return (double)REF_AMU; }
+
+/* ParticleSpeciesFunction::getMass (particles.h:65-87), EMI 111, BF4 87. */
+static long double species_mass_ld(int s) {
+    switch (s) {
+    case 0: return 111.0L;                 /* monomerPositive */
+    case 1: return 2 * 111.0 + 87.0;       /* dimerPositive */
+    case 2: return 3 * 111.0 + 2 * 87.0;   /* trimerPositive */
+    case 3: return 0.0L;                   /* droplet: unsupported -> 0 */
+    case 4: return 111.0 + 87.0;           /* neutral */
+    case 5: return 87.0;                   /* monomerNegative */
+    case 6: return 111.0 + 2 * 87.0;       /* dimerNegative */
+    case 7: return 2 * 111.0 + 3 * 87.0;   /* trimerNegative */
+    default: return 0.0L;
+    }
+}
+
+double orc_species_mass(int species) { return (double)species_mass_ld(species); }
+
+static int nthreads_or_default(int nthreads) {
+#ifdef _OPENMP
+    return nthreads > 0 ? nthreads : omp_get_max_threads();
+#else
+    (void)nthreads;
+    return 1;
+#endif
+}
+
+/* accel_const = K_const * q / getMass(i): double * float, then divided by a
+ * long double mass, rounded to double (direct_force_method.cpp:183). */
+static double accel_const_ref(const float *pos4, const float *vel4, int i) {
+    long double m = species_mass_ld((int)vel4[4 * i + 3]);
+    double kq = orc_k_const() * (double)pos4[4 * i + 3];
+    return (double)((long double)kq / m);
+}
+
+/* ---- reference direct, no symmetry ------------------------------------ */
+
+void orc_direct_ref32(const float *pos4, const float *vel4, float *acc4,
+                      int i0, int i1, int j0, int j1, double eps, int nthreads) {
+    /* DirectForceFunction::direct (direct_force_method.cpp:153-190). */
+    const int nt = nthreads_or_default(nthreads);
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nt)
+    for (int i = i0; i < i1; i++) {
+        if (acc4[4 * i + 3] != 1.0f) continue;
+        double ax = 0, ay = 0, az = 0;
+        for (int j = j0; j < j1; j++) {
+            float wj = acc4[4 * j + 3];
+            if (!(wj == 1.0f || wj == 2.0f) || j == i) continue;
+            double dx = (float)(pos4[4 * i + 0] - pos4[4 * j + 0]);
+            double dy = (float)(pos4[4 * i + 1] - pos4[4 * j + 1]);
+            double dz = (float)(pos4[4 * i + 2] - pos4[4 * j + 2]);
+            double inv = 1.0 / sqrt(dx * dx + dy * dy + dz * dz + eps);
+            double inv3 = (double)pos4[4 * j + 3] * inv * inv * inv;
+            ax += dx * inv3;
+            ay += dy * inv3;
+            az += dz * inv3;
+        }
+        double c = accel_const_ref(pos4, vel4, i);
+        ax *= c; ay *= c; az *= c;
+        acc4[4 * i + 0] = (float)((double)acc4[4 * i + 0] + ax);
+        acc4[4 * i + 1] = (float)((double)acc4[4 * i + 1] + ay);
+        acc4[4 * i + 2] = (float)((double)acc4[4 * i + 2] + az);
+    }
+}
+
+/* quadrantRotationFunction (auxiliary_functions.h:55-57): cos/sin of k*pi/2
+ * as integers. */
+static int quadrant_rot(int n) {
+    if ((n & 1) == 0) return 0;
+    return (((n - 1) >> 1) & 1) ? -1 : 1;
+}
+
+void orc_direct_rot4_ref32(const float *pos4, const float *vel4, float *acc4,
+                           int i0, int i1, int j0, int j1, double eps,
+                           int nthreads) {
+    /* directKernelRotationCalculation + direct_rotational
+     * (direct_force_method_rotational.cpp:28-94): for each quadrant the
+     * source is rotated by k*pi/2 in FP32, no j != i test, and each
+     * quadrant's sum is added to the FP32 acceleration in turn. */
+    const int nt = nthreads_or_default(nthreads);
+    for (int k = 0; k < 4; k++) {
+        const int ck = quadrant_rot(k + 1);
+        const int sk = quadrant_rot(k);
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nt)
+        for (int i = i0; i < i1; i++) {
+            if (acc4[4 * i + 3] != 1.0f) continue;
+            double ax = 0, ay = 0, az = 0;
+            const float xi = pos4[4 * i + 0], yi = pos4[4 * i + 1], zi = pos4[4 * i + 2];
+            for (int j = j0; j < j1; j++) {
+                float wj = acc4[4 * j + 3];
+                if (!(wj == 1.0f || wj == 2.0f)) continue;
+                const float xj = pos4[4 * j + 0], yj = pos4[4 * j + 1];
+                double dz = (float)(zi - pos4[4 * j + 2]);
+                double dz2 = dz * dz;
+                float rx = (float)ck * xj - (float)sk * yj;
+                float ry = (float)sk * xj + (float)ck * yj;
+                double dx = (float)(xi - rx);
+                double dy = (float)(yi - ry);
+                double inv = 1.0 / sqrt(dx * dx + dy * dy + dz2 + eps);
+                double inv3 = (double)pos4[4 * j + 3] * inv * inv * inv;
+                ax += dx * inv3;
+                ay += dy * inv3;
+                az += dz * inv3;
+            }
+            double c = accel_const_ref(pos4, vel4, i);
+            ax *= c; ay *= c; az *= c;
+            acc4[4 * i + 0] = (float)((double)acc4[4 * i + 0] + ax);
+            acc4[4 * i + 1] = (float)((double)acc4[4 * i + 1] + ay);
+            acc4[4 * i + 2] = (float)((double)acc4[4 * i + 2] + az);
+        }
+    }
+}
+
+void orc_direct_trans_ref32(const float *pos4, const float *vel4, float *acc4,
+                            int i0, int i1, int j0, int j1, double eps,
+                            int nimg, const int *images,
+                            const float domain_size[3], int nthreads) {
+    /* direct_translational (direct_force_method_translational.cpp:320-367),
+     * called once per image in the order of the image list. */
+    const int nt = nthreads_or_default(nthreads);
+    for (int g = 0; g < nimg; g++) {
+        const float ox = (float)images[3 * g + 0] * domain_size[0];
+        const float oy = (float)images[3 * g + 1] * domain_size[1];
+        const float oz = (float)images[3 * g + 2] * domain_size[2];
+#pragma omp parallel for schedule(dynamic, 16) num_threads(nt)
+        for (int i = i0; i < i1; i++) {
+            if (acc4[4 * i + 3] != 1.0f) continue;
+            double ax = 0, ay = 0, az = 0;
+            const float xi = pos4[4 * i + 0] - ox;
+            const float yi = pos4[4 * i + 1] - oy;
+            const float zi = pos4[4 * i + 2] - oz;
+            for (int j = j0; j < j1; j++) {
+                float wj = acc4[4 * j + 3];
+                if (!(wj == 1.0f || wj == 2.0f)) continue;
+                double dx = (float)(xi - pos4[4 * j + 0]);
+                double dy = (float)(yi - pos4[4 * j + 1]);
+                double dz = (float)(zi - pos4[4 * j + 2]);
+                double inv = 1.0 / sqrt(dx * dx + dy * dy + dz * dz + eps);
+                double inv3 = (double)pos4[4 * j + 3] * inv * inv * inv;
+                ax += dx * inv3;
+                ay += dy * inv3;
+                az += dz * inv3;
+            }
+            double c = accel_const_ref(pos4, vel4, i);
+            ax *= c; ay *= c; az *= c;
+            acc4[4 * i + 0] = (float)((double)acc4[4 * i + 0] + ax);
+            acc4[4 * i + 1] = (float)((double)acc4[4 * i + 1] + ay);
+            acc4[4 * i + 2] = (float)((double)acc4[4 * i + 2] + az);
+        }
+    }
+}
+
+/* ---- periodic image list (lattice_point.h:65-131 and
+ *      direct_force_method_translational.cpp:35-306) ------------------- */
+
+static int oe(int i) { return (i & 1) ? -1 : 1; } /* ODDEVEN */
+
+static int emit(int *out, int cnt, int max_out, int x, int y, int z) {
+    if (cnt < max_out) {
+        out[3 * cnt + 0] = x;
+        out[3 * cnt + 1] = y;
+        out[3 * cnt + 2] = z;
+    }
+    return cnt + 1;
+}
+
+int orc_trans_images(int box_length, const int axes[3], const int *lattice,
+                     int nlat, int *out, int max_out) {
+    const int n = box_length / 2;
+    const int dsum = (axes[0] != 0) + (axes[1] != 0) + (axes[2] != 0);
+    int *pts = NULL;
+    if (lattice == NULL) {
+        int cap = (2 * n + 1) * (2 * n + 1) * (2 * n + 1) + 1;
+        pts = (int *)malloc(sizeof(int) * 3 * (size_t)cap);
+        int cnt = 0;
+        int t[3] = {axes[0] != 0, axes[1] != 0, axes[2] != 0};
+        for (int pass = 0; pass < dsum; pass++) {
+            int i = t[0];
+            do {
+                int j = t[1];
+                do {
+                    int k = t[2];
+                    do {
+                        pts[3 * cnt + 0] = i; pts[3 * cnt + 1] = j; pts[3 * cnt + 2] = k;
+                        cnt++;
+                        k++;
+                    } while (t[2] != 0 && k <= n);
+                    j++;
+                } while (t[1] != 0 && j <= n);
+                i++;
+            } while (t[0] != 0 && i <= n);
+            if (t[0] == 0) {
+                if (t[1] == 0) t[2] = 0; else t[1] = 0;
+            } else {
+                t[0] = 0;
+            }
+        }
+        pts[3 * cnt + 0] = 0; pts[3 * cnt + 1] = 0; pts[3 * cnt + 2] = 0;
+        cnt++;
+        /* descending norm; insertion sort keeps ties in generation order */
+        for (int a = 1; a < cnt; a++) {
+            int p0 = pts[3 * a], p1 = pts[3 * a + 1], p2 = pts[3 * a + 2];
+            int na = p0 * p0 + p1 * p1 + p2 * p2;
+            int b = a - 1;
+            while (b >= 0) {
+                int nb = pts[3 * b] * pts[3 * b] + pts[3 * b + 1] * pts[3 * b + 1] +
+                         pts[3 * b + 2] * pts[3 * b + 2];
+                if (nb >= na) break;
+                memcpy(&pts[3 * (b + 1)], &pts[3 * b], sizeof(int) * 3);
+                b--;
+            }
+            pts[3 * (b + 1)] = p0; pts[3 * (b + 1) + 1] = p1; pts[3 * (b + 1) + 2] = p2;
+        }
+        lattice = pts;
+        nlat = cnt;
+    }
+    int cnt = 0;
+    for (int ii = 0; ii < nlat; ii++) {
+        const int px = lattice[3 * ii], py = lattice[3 * ii + 1], pz = lattice[3 * ii + 2];
+        const int nz = (px != 0) + (py != 0) + (pz != 0);
+        const int ni = 1 + (px != 0), nj = 1 + (py != 0), nk = 1 + (pz != 0);
+        if (dsum == 3) {
+            if (nz == 3) {
+                for (int i = 0; i < 2; i++)
+                    for (int j = 0; j < 2; j++)
+                        for (int k = 0; k < 2; k++)
+                            cnt = emit(out, cnt, max_out, oe(i) * px, oe(j) * py, oe(k) * pz);
+            } else if (nz == 2) {
+                for (int jj = 0; jj < 3; jj++)
+                    for (int i = 0; i < ni; i++)
+                        for (int j = 0; j < nj; j++)
+                            for (int k = 0; k < nk; k++) {
+                                int tx = (jj != 0) * oe(i) * px +
+                                         (px == 0) * ((jj == 1) * oe(j) * py + (jj == 2) * oe(k) * pz);
+                                int ty = (jj != 1) * oe(j) * py +
+                                         (py == 0) * ((jj == 0) * oe(i) * px + (jj == 2) * oe(k) * pz);
+                                int tz = (jj != 2) * oe(k) * pz +
+                                         (pz == 0) * ((jj == 0) * oe(i) * px + (jj == 1) * oe(j) * py);
+                                cnt = emit(out, cnt, max_out, tx, ty, tz);
+                            }
+            } else if (nz == 1) {
+                for (int jj = 0; jj < 3; jj++)
+                    for (int i = 0; i < ni; i++)
+                        for (int j = 0; j < nj; j++)
+                            for (int k = 0; k < nk; k++) {
+                                int tx = (jj == 0) * oe(i) * px + (jj == 1) * oe(j) * py + (jj == 2) * oe(k) * pz;
+                                int ty = (jj == 0) * oe(j) * py + (jj == 1) * oe(k) * pz + (jj == 2) * oe(i) * px;
+                                int tz = (jj == 0) * oe(k) * pz + (jj == 1) * oe(i) * px + (jj == 2) * oe(j) * py;
+                                cnt = emit(out, cnt, max_out, tx, ty, tz);
+                            }
+            } else {
+                cnt = emit(out, cnt, max_out, 0, 0, 0);
+            }
+        } else if (dsum == 2) {
+            if (nz == 2) {
+                for (int i = 0; i < ni; i++)
+                    for (int j = 0; j < nj; j++)
+                        for (int k = 0; k < nk; k++)
+                            cnt = emit(out, cnt, max_out, oe(i) * px, oe(j) * py, oe(k) * pz);
+            } else if (nz == 1) {
+                const int ax = axes[0] != 0, ay = axes[1] != 0, az = axes[2] != 0;
+                for (int jj = 0; jj < 2; jj++)
+                    for (int i = 0; i < ni; i++)
+                        for (int j = 0; j < nj; j++)
+                            for (int k = 0; k < nk; k++) {
+                                int tx = ax * ((jj == 0) * oe(i) * px + (jj == 1) * (oe(j) * py + oe(k) * pz));
+                                int ty = ay * ((jj == 0) * oe(j) * py + (jj == 1) * (oe(i) * px + oe(k) * pz));
+                                int tz = az * ((jj == 0) * oe(k) * pz + (jj == 1) * (oe(i) * px + oe(j) * py));
+                                cnt = emit(out, cnt, max_out, tx, ty, tz);
+                            }
+            } else {
+                cnt = emit(out, cnt, max_out, 0, 0, 0);
+            }
+        } else if (dsum == 1) {
+            if (nz == 1) {
+                for (int i = 0; i < ni; i++)
+                    for (int j = 0; j < nj; j++)
+                        for (int k = 0; k < nk; k++)
+                            cnt = emit(out, cnt, max_out, oe(i) * px, oe(j) * py, oe(k) * pz);
+            } else {
+                cnt = emit(out, cnt, max_out, 0, 0, 0);
+            }
+        }
+    }
+    free(pts);
+    return cnt;
+}
+
+/* ---- FP64 ground truth ------------------------------------------------- */
+
+void orc_direct_f64(int64_t n, const double *x, const double *q,
+                    const double *m, const int32_t *status,
+                    const int64_t *targets, int64_t ntargets, double eps2,
+                    double kconst, int sym, int nimg, const double *img_off,
+                    double *a_out, int nthreads) {
+    /* Same pair law as direct_force_method.cpp:163-189 (and the rotational /
+     * translational variants), all in FP64. */
+    const int nt = nthreads_or_default(nthreads);
+    const int64_t nt_count = targets ? ntargets : n;
+    static const double rc[4] = {1, 0, -1, 0}, rs[4] = {0, 1, 0, -1};
+#pragma omp parallel for schedule(dynamic, 8) num_threads(nt)
+    for (int64_t t = 0; t < nt_count; t++) {
+        const int64_t i = targets ? targets[t] : t;
+        double *ao = a_out + 3 * t;
+        ao[0] = ao[1] = ao[2] = 0.0;
+        if (status[i] != 1) continue;
+        double ax = 0, ay = 0, az = 0;
+        const double xi = x[3 * i], yi = x[3 * i + 1], zi = x[3 * i + 2];
+        if (sym == 0) {
+            for (int64_t j = 0; j < n; j++) {
+                if (!(status[j] == 1 || status[j] == 2) || j == i) continue;
+                double dx = xi - x[3 * j], dy = yi - x[3 * j + 1], dz = zi - x[3 * j + 2];
+                double inv = 1.0 / sqrt(dx * dx + dy * dy + dz * dz + eps2);
+                double w = q[j] * inv * inv * inv;
+                ax += dx * w; ay += dy * w; az += dz * w;
+            }
+        } else if (sym == 1) {
+            for (int k = 0; k < 4; k++) {
+                double bx = 0, by = 0, bz = 0;
+                for (int64_t j = 0; j < n; j++) {
+                    if (!(status[j] == 1 || status[j] == 2)) continue;
+                    double sx = rc[k] * x[3 * j] - rs[k] * x[3 * j + 1];
+                    double sy = rs[k] * x[3 * j] + rc[k] * x[3 * j + 1];
+                    double dx = xi - sx, dy = yi - sy, dz = zi - x[3 * j + 2];
+                    double inv = 1.0 / sqrt(dx * dx + dy * dy + dz * dz + eps2);
+                    double w = q[j] * inv * inv * inv;
+                    bx += dx * w; by += dy * w; bz += dz * w;
+                }
+                ax += bx; ay += by; az += bz;
+            }
+        } else {
+            for (int g = 0; g < nimg; g++) {
+                const double tx = xi - img_off[3 * g], ty = yi - img_off[3 * g + 1],
+                             tz = zi - img_off[3 * g + 2];
+                double bx = 0, by = 0, bz = 0;
+                for (int64_t j = 0; j < n; j++) {
+                    if (!(status[j] == 1 || status[j] == 2)) continue;
+                    double dx = tx - x[3 * j], dy = ty - x[3 * j + 1], dz = tz - x[3 * j + 2];
+                    double inv = 1.0 / sqrt(dx * dx + dy * dy + dz * dz + eps2);
+                    double w = q[j] * inv * inv * inv;
+                    bx += dx * w; by += dy * w; bz += dz * w;
+                }
+                ax += bx; ay += by; az += bz;
+            }
+        }
+        const double c = kconst * q[i] / m[i];
+        ao[0] = ax * c; ao[1] = ay * c; ao[2] = az * c;
+    }
+}
+
+void orc_potential_f64(int64_t n, const double *x, const double *q,
+                       const int32_t *status, const int64_t *targets,
+                       int64_t ntargets, double eps2, double *phi_out,
+                       int nthreads) {
+    const int nt = nthreads_or_default(nthreads);
+    const int64_t nt_count = targets ? ntargets : n;
+#pragma omp parallel for schedule(dynamic, 8) num_threads(nt)
+    for (int64_t t = 0; t < nt_count; t++) {
+        const int64_t i = targets ? targets[t] : t;
+        double phi = 0;
+        for (int64_t j = 0; j < n; j++) {
+            if (!(status[j] == 1 || status[j] == 2) || j == i) continue;
+            double dx = x[3 * i] - x[3 * j], dy = x[3 * i + 1] - x[3 * j + 1],
+                   dz = x[3 * i + 2] - x[3 * j + 2];
+            phi += q[j] / sqrt(dx * dx + dy * dy + dz * dz + eps2);
+        }
+        phi_out[t] = phi;
+    }
+}
+
+/* ---- leapfrog DKD ------------------------------------------------------ */
+
+static float clampf_dt(float v, float dt) {
+    /* std::min(std::max(v, 0.0f), dt) */
+    float a = v > 0.0f ? v : 0.0f;
+    return dt < a ? dt : a;
+}
+
+static void drift_ref32(int n, float *pos4, const float *vel4, const float *acc4,
+                        const float *t_inj, float tstart, float dt) {
+    /* ChargedParticles::propagatePositionNew (particles.cpp:693-739), crash
+     * checks disabled (CrashConditionOptions::none). */
+    const float tend = tstart + dt;
+    for (int i = 0; i < n; i++) {
+        float w = acc4[4 * i + 3];
+        if (!(w == 1.0f || w == 2.0f)) continue;
+        float s = clampf_dt(tend - t_inj[i], dt);
+        pos4[4 * i + 0] += vel4[4 * i + 0] * s;
+        pos4[4 * i + 1] += vel4[4 * i + 1] * s;
+        pos4[4 * i + 2] += vel4[4 * i + 2] * s;
+    }
+}
+
+void orc_leapfrog_ref32(int n, float *pos4, float *vel4, float *acc4,
+                        const float *t_inj, int nsteps, float dt, double eps,
+                        const float efield[3], int sym, int nimg,
+                        const int *images, const float domain_size[3],
+                        int nthreads) {
+    /* LeapfrogDKD::runSimulation (integration_schemes.cpp:856-891):
+     * driftNew(dt/2), kick(dt), driftNew(dt/2) per step. */
+    const float factor = REF_ELEM_CHARGE / REF_AMU;
+    for (int it = 1; it <= nsteps; it++) {
+        float tpos = dt * (float)(it - 1);
+        float tvel = dt * (float)(it - 1);
+        drift_ref32(n, pos4, vel4, acc4, t_inj, tpos, dt / 2);
+        tpos += dt / 2;
+        /* kick: zeroAcceleration (particles.cpp:1031-1044) + force */
+        for (int i = 0; i < n; i++)
+            if (acc4[4 * i + 3] == 1.0f) acc4[4 * i] = acc4[4 * i + 1] = acc4[4 * i + 2] = 0.0f;
+        if (sym == 0)
+            orc_direct_ref32(pos4, vel4, acc4, 0, n, 0, n, eps, nthreads);
+        else if (sym == 1)
+            orc_direct_rot4_ref32(pos4, vel4, acc4, 0, n, 0, n, eps, nthreads);
+        else
+            orc_direct_trans_ref32(pos4, vel4, acc4, 0, n, 0, n, eps, nimg, images,
+                                   domain_size, nthreads);
+        /* computeBackgroundAcceleration with a uniform field
+         * (particles.cpp:496-520): Efactor in float, E*Efactor per axis. */
+        for (int i = 0; i < n; i++) {
+            if (acc4[4 * i + 3] != 1.0f) continue;
+            long double m = species_mass_ld((int)vel4[4 * i + 3]);
+            float ef = (float)((double)factor * (double)pos4[4 * i + 3] / m);
+            for (int d = 0; d < 3; d++) {
+                float e = (float)((double)efield[d] * (double)ef);
+                acc4[4 * i + d] += e;
+            }
+        }
+        /* propagateVelocityNew (particles.cpp:763-786) */
+        {
+            const float tend = tvel + dt;
+            for (int i = 0; i < n; i++) {
+                if (acc4[4 * i + 3] != 1.0f) continue;
+                float s = clampf_dt(tend - t_inj[i], dt);
+                vel4[4 * i + 0] += acc4[4 * i + 0] * s;
+                vel4[4 * i + 1] += acc4[4 * i + 1] * s;
+                vel4[4 * i + 2] += acc4[4 * i + 2] * s;
+            }
+        }
+        drift_ref32(n, pos4, vel4, acc4, t_inj, tpos, dt / 2);
+    }
+}
+
+void orc_leapfrog_f64(int64_t n, double *x, double *v, const double *q,
+                      const double *m, int32_t *status, const double *t_inj,
+                      int nsteps, double dt, double t0, double eps2,
+                      double kconst, const double efield[3], int sym, int nimg,
+                      const double *img_off, double *a_out, int nthreads) {
+    double *a = (double *)malloc(sizeof(double) * 3 * (size_t)(n > 0 ? n : 1));
+    const double eoa = orc_e_over_amu();
+    const double h = 0.5 * dt;
+    for (int it = 0; it < nsteps; it++) {
+        const double ts = t0 + dt * it;
+        for (int half = 0; half < 2; half++) {
+            const double t_start = ts + (half ? h : 0.0);
+            if (half == 1) {
+                /* kick over [ts, ts+dt] */
+                orc_direct_f64(n, x, q, m, status, NULL, 0, eps2, kconst, sym, nimg,
+                               img_off, a, nthreads);
+                for (int64_t i = 0; i < n; i++) {
+                    if (status[i] != 1) continue;
+                    const double ef = eoa * q[i] / m[i];
+                    double s = ts + dt - t_inj[i];
+                    s = s < 0 ? 0 : (s > dt ? dt : s);
+                    for (int d = 0; d < 3; d++) {
+                        a[3 * i + d] += efield[d] * ef;
+                        v[3 * i + d] += a[3 * i + d] * s;
+                    }
+                }
+            }
+            /* drift over [t_start, t_start + dt/2] */
+            for (int64_t i = 0; i < n; i++) {
+                if (!(status[i] == 1 || status[i] == 2)) continue;
+                double s = t_start + h - t_inj[i];
+                s = s < 0 ? 0 : (s > h ? h : s);
+                for (int d = 0; d < 3; d++) x[3 * i + d] += v[3 * i + d] * s;
+            }
+        }
+    }
+    if (a_out) memcpy(a_out, a, sizeof(double) * 3 * (size_t)n);
+    free(a);
+}
+
+/* ---- energy ------------------------------------------------------------ */
+
+void orc_energy_f64(int64_t n, const double *x, const double *v,
+                    const double *q, const double *m, double eps2,
+                    double *ke, double *pe, int nthreads) {
+    /* computeChargedKineticEnergy / computeChargedElectricPotentialEnergy
+     * (particles.cpp:535-578) and the halving in updateEnergyIntervalData
+     * (integration_schemes.cpp:815). */
+    const int nt = nthreads_or_default(nthreads);
+    const double amu = orc_amu(), e = orc_elem_charge(), kc = orc_coulomb_ke();
+    double k_sum = 0, p_sum = 0;
+#pragma omp parallel for schedule(dynamic, 16) reduction(+ : k_sum, p_sum) num_threads(nt)
+    for (int64_t i = 0; i < n; i++) {
+        const double v2 = v[3 * i] * v[3 * i] + v[3 * i + 1] * v[3 * i + 1] + v[3 * i + 2] * v[3 * i + 2];
+        k_sum += 0.5 * amu * m[i] * v2;
+        double s = 0;
+        for (int64_t j = 0; j < n; j++) {
+            if (j == i) continue;
+            double dx = x[3 * i] - x[3 * j], dy = x[3 * i + 1] - x[3 * j + 1],
+                   dz = x[3 * i + 2] - x[3 * j + 2];
+            s += q[i] * q[j] / sqrt(dx * dx + dy * dy + dz * dz + eps2);
+        }
+        p_sum += s;
+    }
+    *ke = k_sum;
+    *pe = 0.5 * p_sum * e * e * kc;
+}
+
+/* ---- accuracy metric --------------------------------------------------- */
+
+void orc_rel_l2(int64_t n, const double *a, const double *r,
+                const int32_t *status, double *l2, double *maxl2,
+                int64_t *argmax, double *global_l2) {
+    double s = 0, mx = 0, num = 0, den = 0;
+    int64_t cnt = 0, arg = 0;
+    for (int64_t k = 0; k < n; k++) {
+        if (status && status[k] != 1) continue;
+        cnt++;
+        double d = 0, nr = 0;
+        for (int c = 0; c < 3; c++) {
+            double e = a[3 * k + c] - r[3 * k + c];
+            d += e * e;
+            nr += r[3 * k + c] * r[3 * k + c];
+        }
+        num += d;
+        den += nr;
+        double ratio = (nr == 0 && d == 0) ? 0.0 : d / nr;
+        s += ratio;
+        if (ratio > mx) { mx = ratio; arg = k; }
+    }
+    *l2 = cnt ? sqrt(s / (double)cnt) : 0.0;
+    *maxl2 = sqrt(mx);
+    *argmax = arg;
+    *global_l2 = den > 0 ? sqrt(num / den) : 0.0;
+}

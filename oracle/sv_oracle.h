@@ -1,0 +1,122 @@
+/*
+ * sv_oracle.h -- CPU restatement of the SOLVEiT force-evaluation hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker: the parity tests,
+ * the smoke check and the CPU-baseline leg of bench.py call it to produce the
+ * numbers the CUDA path is compared against.  Nothing in the product path
+ * (libsolveit_gpu.so, the host adapter) links or calls it.
+ *
+ * Two families of functions:
+ *   *_ref32  restate the reference arithmetic on its own FP32 vec4 state
+ *            (position = x,y,z,q; velocity = vx,vy,vz,species;
+ *            acceleration = ax,ay,az,status), operation by operation, so that
+ *            they reproduce the reference's outputs bit for bit on the same
+ *            machine (pinned against fixtures generated by running the
+ *            reference itself, see tests/golden/make_golden.py).
+ *   *_f64    are the FP64 ground truth (FP64 positions, FP64 accumulation)
+ *            that the GPU results are measured against.
+ */
+#ifndef SV_ORACLE_H
+#define SV_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Physical constants exactly as the reference evaluates them
+ * (constants.h:28-47): K = e^2 / (4 pi eps0 amu), e/amu, 1/(4 pi eps0). */
+double orc_k_const(void);
+double orc_e_over_amu(void);
+double orc_coulomb_ke(void);
+double orc_elem_charge(void);
+double orc_amu(void);
+/* Species code (velocity.w) -> mass in amu (particles.h:65-87). */
+double orc_species_mass(int species);
+
+/* Reference direct sum, no symmetry (direct_force_method.cpp:153-190).
+ * Adds into acc4[i].xyz for i in [i0,i1) with acc4[i].w == 1, sources
+ * j in [j0,j1) with w in {1,2}, j != i. eps = softening squared (m^2). */
+void orc_direct_ref32(const float *pos4, const float *vel4, float *acc4,
+                      int i0, int i1, int j0, int j1, double eps, int nthreads);
+
+/* Reference 4-fold rotational direct sum
+ * (direct_force_method_rotational.cpp:28-94): quadrant k = 0..3 added in turn. */
+void orc_direct_rot4_ref32(const float *pos4, const float *vel4, float *acc4,
+                           int i0, int i1, int j0, int j1, double eps,
+                           int nthreads);
+
+/* Reference translational image sum
+ * (direct_force_method_translational.cpp:28-367): images[3*k..3*k+2] are the
+ * integer lattice offsets in summation order; the target is shifted by
+ * -image*domain_size (FP32) before the pair loop. */
+void orc_direct_trans_ref32(const float *pos4, const float *vel4, float *acc4,
+                            int i0, int i1, int j0, int j1, double eps,
+                            int nimg, const int *images,
+                            const float domain_size[3], int nthreads);
+
+/* Image list of the reference's periodic Grid (lattice_point.h:65-131)
+ * expanded by the sign/permutation loops of
+ * direct_force_method_translational.cpp:35-306.  lattice (3*nlat ints) is the
+ * Grid's canonical point list in its stored order; pass NULL to build it here
+ * (points sorted by descending norm, ties kept in generation order).
+ * Returns the number of images written to out (capacity max_out). */
+int orc_trans_images(int box_length, const int axes[3], const int *lattice,
+                     int nlat, int *out, int max_out);
+
+/* FP64 ground truth.  x: 3n interleaved metres; q: charge in e; m: mass in
+ * amu; status: 1 inbound, 2 source-only, 0/-1 ignored.  Computes a (m/s^2)
+ * for the given targets (NULL = all n) into a_out[3*ntargets].
+ * sym 0: none (j != i);  1: 4-fold rotation about z;  2: images
+ * (img_off = 3*nimg metres, target shifted by -offset, no j != i test,
+ * matching the reference). */
+void orc_direct_f64(int64_t n, const double *x, const double *q,
+                    const double *m, const int32_t *status,
+                    const int64_t *targets, int64_t ntargets, double eps2,
+                    double kconst, int sym, int nimg, const double *img_off,
+                    double *a_out, int nthreads);
+
+/* Same sum with the potential (sum q_j / sqrt(r^2+eps2)) per target, FP64. */
+void orc_potential_f64(int64_t n, const double *x, const double *q,
+                       const int32_t *status, const int64_t *targets,
+                       int64_t ntargets, double eps2, double *phi_out,
+                       int nthreads);
+
+/* Reference leapfrog DKD with the direct force (integration_schemes.cpp:
+ * 856-891, 705-751; particles.cpp:693-786) and a uniform background field
+ * E (V/m) added as computeBackgroundAcceleration does (particles.cpp:496-520).
+ * sym as in orc_direct_f64 (images/domain used for sym 2). */
+void orc_leapfrog_ref32(int n, float *pos4, float *vel4, float *acc4,
+                        const float *t_inj, int nsteps, float dt, double eps,
+                        const float efield[3], int sym, int nimg,
+                        const int *images, const float domain_size[3],
+                        int nthreads);
+
+/* FP64 leapfrog DKD: x, v (3n interleaved) updated in place; a_out (3n,
+ * nullable) receives the last kick's acceleration (force + field). */
+void orc_leapfrog_f64(int64_t n, double *x, double *v, const double *q,
+                      const double *m, int32_t *status, const double *t_inj,
+                      int nsteps, double dt, double t0, double eps2,
+                      double kconst, const double efield[3], int sym, int nimg,
+                      const double *img_off, double *a_out, int nthreads);
+
+/* Energy diagnostic in FP64 (particles.cpp:535-578): kinetic
+ * 0.5*amu*m*|v|^2 and potential 0.5*sum_{i!=j} q_i q_j e^2 ke/sqrt(r^2+eps2),
+ * over all particles in [0,n) as the reference does (no status test). */
+void orc_energy_f64(int64_t n, const double *x, const double *v,
+                    const double *q, const double *m, double eps2,
+                    double *ke, double *pe, int nthreads);
+
+/* Accuracy metric of compareAcceleration (integration_schemes.cpp:411-461):
+ * l2 = sqrt(mean_i |a_i - r_i|^2 / |r_i|^2) over status==1 particles (NULL
+ * status = all), max = sqrt(max ratio), argmax its index. Also returns the
+ * global form sqrt(sum|a-r|^2 / sum|r|^2). FP64. */
+void orc_rel_l2(int64_t n, const double *a, const double *r,
+                const int32_t *status, double *l2, double *maxl2,
+                int64_t *argmax, double *global_l2);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

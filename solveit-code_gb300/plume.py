@@ -1,0 +1,89 @@
+"""Seeded synthetic electrospray plumes (the workloads' input generator).
+
+A plume is a cylinder of singly charged ions: radius 20 nm, length L along z,
+positions uniform in the cylinder, species 50/50 monomer (EMI+, 111 amu,
+species code 0) and dimer ((EMI)2BF4+, 309 amu, code 1), axial velocity
+N(2e4, 2e3) m/s, transverse N(0, 500) m/s, all inbound and injected at t=0.
+The species codes, masses and status values are those of the reference's
+ParticleSpecies / ParticleStatus enums (structures.h:206-221, particles.h:65-87).
+
+Seeds follow seed = 1000*workload + realisation with numpy's PCG64, so every
+test, fixture and benchmark draws the same particles for the same workload.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+MONOMER_AMU = 111.0
+DIMER_AMU = 309.0
+
+# name -> (N, plume length in metres)
+WORKLOADS = {
+    "direct_n4096": (4096, 1e-6),
+    "bh_n65536": (65536, 10e-6),
+    "fmm_n1m": (1 << 20, 50e-6),
+    "adjoint_n16384": (16384, 1e-6),
+}
+
+
+def make_plume(n: int, length: float, seed: int, radius: float = 20e-9,
+               vz_mean: float = 2e4, vz_std: float = 2e3, vt_std: float = 500.0):
+    """Return a dict of float64 state arrays for n ions.
+
+    x, v: (n, 3) metres and m/s; q: charge in e; m: mass in amu;
+    species: int32 code; status: int32 (1 = inbound); t_inj: seconds.
+    """
+    rng = np.random.Generator(np.random.PCG64(seed))
+    r = radius * np.sqrt(rng.random(n))
+    phi = 2.0 * np.pi * rng.random(n)
+    z = length * rng.random(n)
+    species = (rng.random(n) < 0.5).astype(np.int32)
+    vz = rng.normal(vz_mean, vz_std, n)
+    vx = rng.normal(0.0, vt_std, n)
+    vy = rng.normal(0.0, vt_std, n)
+    x = np.stack([r * np.cos(phi), r * np.sin(phi), z], axis=1)
+    v = np.stack([vx, vy, vz], axis=1)
+    m = np.where(species == 1, DIMER_AMU, MONOMER_AMU)
+    return {
+        "x": np.ascontiguousarray(x, dtype=np.float64),
+        "v": np.ascontiguousarray(v, dtype=np.float64),
+        "q": np.ones(n, dtype=np.float64),
+        "m": m.astype(np.float64),
+        "species": species,
+        "status": np.ones(n, dtype=np.int32),
+        "t_inj": np.zeros(n, dtype=np.float64),
+    }
+
+
+def to_ref32(state):
+    """Pack a plume into the reference's FP32 vec4 arrays.
+
+    position = (x, y, z, q), velocity = (vx, vy, vz, species),
+    acceleration = (0, 0, 0, status), plus timeInjected (particles.h:99-105).
+    """
+    n = state["x"].shape[0]
+    pos4 = np.zeros((n, 4), np.float32)
+    vel4 = np.zeros((n, 4), np.float32)
+    acc4 = np.zeros((n, 4), np.float32)
+    pos4[:, :3] = state["x"]
+    pos4[:, 3] = state["q"]
+    vel4[:, :3] = state["v"]
+    vel4[:, 3] = state["species"]
+    acc4[:, 3] = state["status"]
+    t_inj = state["t_inj"].astype(np.float32)
+    return pos4, vel4, acc4, t_inj
+
+
+def from_ref32(pos4, vel4, acc4, t_inj=None):
+    """Widen the reference's FP32 vec4 arrays into FP64 state arrays."""
+    n = pos4.shape[0]
+    species = vel4[:, 3].astype(np.int32)
+    return {
+        "x": pos4[:, :3].astype(np.float64),
+        "v": vel4[:, :3].astype(np.float64),
+        "q": pos4[:, 3].astype(np.float64),
+        "m": np.where(species == 1, DIMER_AMU, MONOMER_AMU).astype(np.float64),
+        "species": species,
+        "status": acc4[:, 3].astype(np.int32),
+        "t_inj": (np.zeros(n) if t_inj is None else t_inj.astype(np.float64)),
+    }

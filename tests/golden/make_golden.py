@@ -1,0 +1,97 @@
+"""Generate the golden fixtures in this directory by running the reference.
+
+The reference SOLVEiT code is compiled from its own sources by
+``make -C oracle ref`` (one-line header fix, see oracle/Makefile) into
+oracle/_ref/{stock,eps20}/ref_harness, which fills the reference's
+ChargedParticles by hand and calls its own updateAcceleration() /
+propagate*New() methods.  This script feeds it seeded plumes and stores the
+inputs and the reference's outputs as compressed .npz files, so the tests
+can pin the oracle and the GPU path to the reference without the reference
+being present.
+
+    make -C oracle ref && python tests/golden/make_golden.py
+
+Fixtures (all FP32 vec4 arrays in the reference layout):
+  direct_n512.npz   direct sum, symmetry none / rotational / translational
+                    (x,y periodic, 2 levels = 81 images), reference softening
+                    6.4e-19 m^2; includes status 2 / 0 / -1 particles and the
+                    Grid's lattice order.
+  dkd_n256.npz      10 LeapfrogDKD steps (dt 1e-13 s, E_z 1e8 V/m, softening
+                    1e-20 m^2, direct force).
+  bh_n4096.npz      Barnes-Hut theta 0.5 (reference tree: 1 particle/leaf).
+  fmm_n4096.npz     FMM p = 8 (reference uniform-depth rotation FMM).
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "solveit-code_gb300"))
+import plume  # noqa: E402
+
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "{}", "ref_harness")
+
+
+def run_ref(variant, mode, pos4, vel4, acc4, tinj, **kw):
+    n = pos4.shape[0]
+    with tempfile.TemporaryDirectory() as td:
+        fin = os.path.join(td, "in.bin")
+        fout = os.path.join(td, "out.bin")
+        with open(fin, "wb") as f:
+            np.array([n], np.int32).tofile(f)
+            for a in (pos4, vel4, acc4, tinj):
+                np.ascontiguousarray(a).tofile(f)
+        args = [HARNESS.format(variant), mode, fin, fout] + [f"{k}={v}" for k, v in kw.items()]
+        subprocess.check_call(args)
+        if mode == "grid":
+            raw = np.fromfile(fout, np.int32)
+            return raw[1:].reshape(raw[0], 3)
+        out = np.fromfile(fout, np.float32).reshape(3, n, 4)
+    return out[0].copy(), out[1].copy(), out[2].copy()
+
+
+def main():
+    # direct, three symmetry variants
+    st = plume.make_plume(512, 1e-6, 9001)
+    pos4, vel4, acc4, tinj = plume.to_ref32(st)
+    acc4[5, 3] = 2.0   # affectsAcceleration: source only
+    acc4[7, 3] = 0.0   # outOfBounds: ignored
+    acc4[9, 3] = -1.0  # crashed: ignored
+    lattice = run_ref("stock", "grid", pos4, vel4, acc4, tinj, levels=2, axes="110")
+    outs = {}
+    for sym in (0, 1, 2):
+        _, _, a = run_ref("stock", "direct", pos4, vel4, acc4, tinj, threads=4, sym=sym,
+                          levels=2, axes="110", dom="2e-6,2e-6,0")
+        outs[f"acc_sym{sym}"] = a
+    np.savez_compressed(os.path.join(HERE, "direct_n512.npz"), pos4=pos4, vel4=vel4, acc4=acc4,
+                        tinj=tinj, lattice=lattice.astype(np.int32), eps=np.float64(6.4e-19),
+                        domain=np.array([2e-6, 2e-6, 0.0], np.float32), **outs)
+
+    # leapfrog DKD
+    st = plume.make_plume(256, 1e-6, 9002)
+    pos4, vel4, acc4, tinj = plume.to_ref32(st)
+    p, v, a = run_ref("eps20", "dkd", pos4, vel4, acc4, tinj, threads=4, steps=10, dt=1e-13, ez=1e8)
+    np.savez_compressed(os.path.join(HERE, "dkd_n256.npz"), pos4=pos4, vel4=vel4, acc4=acc4,
+                        tinj=tinj, pos4_out=p, vel4_out=v, acc4_out=a, steps=np.int32(10),
+                        dt=np.float32(1e-13), ez=np.float32(1e8), eps=np.float64(1e-20))
+
+    # Barnes-Hut and FMM, reference softening
+    st = plume.make_plume(4096, 1e-6, 9003)
+    pos4, vel4, acc4, tinj = plume.to_ref32(st)
+    _, _, ab = run_ref("stock", "bh", pos4, vel4, acc4, tinj, threads=4, theta=0.5)
+    np.savez_compressed(os.path.join(HERE, "bh_n4096.npz"), pos4=pos4, vel4=vel4, acc4=acc4,
+                        tinj=tinj, acc_bh=ab, theta=np.float32(0.5), eps=np.float64(6.4e-19))
+    _, _, af = run_ref("stock", "fmm", pos4, vel4, acc4, tinj, threads=4, p=8)
+    np.savez_compressed(os.path.join(HERE, "fmm_n4096.npz"), pos4=pos4, vel4=vel4, acc4=acc4,
+                        tinj=tinj, acc_fmm=af, p=np.int32(8), eps=np.float64(6.4e-19))
+    print("fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()
