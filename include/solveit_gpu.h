@@ -1,0 +1,169 @@
+/*
+ * solveit_gpu.h -- C ABI of the GB300 force-evaluation engine for SOLVEiT.
+ *
+ * One context (sv_ctx) owns one plume's particle state in GPU memory, a CUDA
+ * stream and all method workspaces.  Host buffers belong to the caller.
+ * Every call returns an sv_status; on failure sv_last_error() describes it.
+ * Calls on one context are issued from one host thread and are ordered on the
+ * context's stream; only the download / readback calls block.
+ *
+ * Each entry point names the reference interface it stands in for (paths are
+ * inside the SOLVEiT-Code project).  The reference's force methods are
+ * ForceCalculationMethod subclasses (force_calculation_methods.h:28-87) that
+ * ADD acceleration (m/s^2) into ChargedParticles::acceleration[i].xyz for
+ * inbound targets (w == 1) from sources with w in {1, 2}; the integrator
+ * zeroes inbound accelerations first (integration_schemes.cpp:344).
+ */
+#ifndef SOLVEIT_GPU_H
+#define SOLVEIT_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SV_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define SV_API __attribute__((visibility("default")))
+#else
+#define SV_API
+#endif
+
+typedef struct sv_ctx sv_ctx;
+
+typedef enum {
+    SV_OK = 0,
+    SV_ERR_INVALID = 1,     /* bad argument (null pointer, n < 0, bad enum) */
+    SV_ERR_CUDA = 2,        /* a CUDA call failed; see sv_last_error */
+    SV_ERR_ALLOC = 3,       /* device or pinned allocation failed */
+    SV_ERR_STATE = 4,       /* call out of order (e.g. compute before upload) */
+    SV_ERR_CAPACITY = 5,    /* a fixed-capacity structure overflowed */
+    SV_ERR_TIMEOUT = 6,     /* a bounded device wait gave up */
+    SV_ERR_UNSUPPORTED = 7  /* method/symmetry/precision combination not built */
+} sv_status;
+
+/* Force method (the ForceCalculationMethod subclass it replaces). */
+typedef enum {
+    SV_METHOD_DIRECT = 0,      /* DirectForceCalculation, direct_force_method.cpp:347 */
+    SV_METHOD_BARNES_HUT = 1,  /* BarnesHutForceCalculation, barnes_hut_force_calculation.cpp:574 */
+    SV_METHOD_FMM = 2          /* MultipoleMethodForceCalculation, multipole_method_force_calculation.cpp:148 */
+} sv_method;
+
+/* SimulationParameters::symType (simulation_parameters.h:139, structures.h:200-204). */
+typedef enum {
+    SV_SYM_NONE = 0,
+    SV_SYM_ROTATIONAL = 1,     /* 4-fold images about z (direct_force_method_rotational.cpp:48-94) */
+    SV_SYM_TRANSLATIONAL = 2   /* finite periodic image lattice (lattice_point.h:65-131) */
+} sv_symmetry;
+
+/* Arithmetic of the pair / expansion work.  MIXED: FP32 pair and expansion
+ * arithmetic on coordinates taken relative to a nearby FP64 origin, FP64
+ * accumulation across tiles; FP64: every operation in FP64. */
+typedef enum {
+    SV_PREC_MIXED = 0,
+    SV_PREC_FP64 = 1
+} sv_precision;
+
+typedef struct {
+    double softening2;       /* eps^2 in m^2 (constants.h:31 SOFTENING) */
+    double k_const;          /* e^2/(4 pi eps0 amu) (constants.h:46 K_CONST) */
+    double e_over_amu;       /* ELEM_CHARGE/AMU (particles.cpp:500) */
+    double efield[3];        /* uniform background field in V/m, added in the kick */
+    int32_t method;          /* sv_method */
+    int32_t precision;       /* sv_precision */
+    int32_t symmetry;        /* sv_symmetry */
+    float theta;             /* BH opening parameter (setTheta, barnes_hut_force_calculation.cpp:110) */
+    int32_t leaf_size;       /* BH leaf bucket size (reference: 1 particle per leaf) */
+    int32_t fmm_order;       /* expansion order p (setNumExpansions), 1..10 */
+    int32_t fmm_ws;          /* FMM well-separation in boxes (reference: 1) */
+    int32_t fmm_leaf_target; /* mean particles per occupied leaf box when choosing the depth */
+    int32_t sym_axes[3];     /* periodic axes (SimulationParameters::symmetryAxes) */
+    int32_t sym_levels;      /* numSymmetryLevels: 3^levels cells per periodic axis */
+    double domain_size[3];   /* periodic cell size in m (SimulationParameters::domainSize) */
+    int32_t device;          /* CUDA device ordinal */
+    int32_t reserved[7];
+} sv_params;
+
+/* Per-call statistics of the last force evaluation. */
+typedef struct {
+    double pair_interactions;     /* particle-particle pairs evaluated */
+    double cell_interactions;     /* BH accepted cells / FMM M2L translations */
+    double flops_algorithmic;     /* 20 flop/pair + expansion flops (method's count) */
+    double ms_total;              /* device time of the whole evaluation */
+    double ms_phase[8];           /* sort, tree, upward, m2l, downward, near, other, spare */
+    int32_t levels;               /* FMM leaf level / BH max depth */
+    int32_t boxes;                /* occupied leaf boxes / BH nodes */
+    int32_t reserved[6];
+} sv_stats;
+
+/* Fill p with the defaults of the reference configuration: softening
+ * 6.4e-19 m^2, K and e/amu as constants.h evaluates them, direct method,
+ * mixed precision, no symmetry, theta 0.5, leaf 16, p 8, ws 1. */
+SV_API sv_status sv_default_params(sv_params *p);
+
+/* Stands in for constructing a ForceCalculationMethod on a ParticleSystem
+ * (force_calculation_methods.h:33-35). */
+SV_API sv_status sv_create(const sv_params *p, sv_ctx **out);
+SV_API void sv_destroy(sv_ctx *ctx);
+/* setTheta / setNumExpansions / symType etc. in one call. */
+SV_API sv_status sv_set_params(sv_ctx *ctx, const sv_params *p);
+SV_API sv_status sv_get_params(const sv_ctx *ctx, sv_params *p);
+
+/* Load a plume.  x3, v3: 3n interleaved (m, m/s); q in e; m_amu in amu;
+ * status as ParticleStatus (1 inbound, 2 source only, 0 / -1 ignored);
+ * t_inj: injection time in s (timeInjected).  Null v3 / t_inj mean zero. */
+SV_API sv_status sv_upload(sv_ctx *ctx, int64_t n, const double *x3, const double *v3,
+                    const double *q, const double *m_amu, const int32_t *status,
+                    const double *t_inj);
+/* Same from the reference's own arrays (particles.h:99-105): position =
+ * (x,y,z,q), velocity = (vx,vy,vz,species), acceleration.w = status;
+ * masses come from the species code (particles.h:65-87). */
+SV_API sv_status sv_upload_ref32(sv_ctx *ctx, int64_t n, const float *pos4,
+                          const float *vel4, const float *acc4,
+                          const float *t_inj);
+SV_API sv_status sv_download(sv_ctx *ctx, double *x3, double *v3, int32_t *status);
+SV_API sv_status sv_download_ref32(sv_ctx *ctx, float *pos4, float *vel4);
+
+/* One force evaluation with the context's method: the body of
+ * updateAcceleration() (direct_force_method.cpp:347-428,
+ * barnes_hut_force_calculation.cpp:574-715,
+ * multipole_method_force_calculation.cpp:148-522).  Targets are inbound
+ * particles with index in [first, last); sources are all particles with
+ * status 1 or 2.  The result (m/s^2, FP64) stays on the device; a3_out, if
+ * not null, receives a copy (3n interleaved, zero for non-targets). */
+SV_API sv_status sv_compute_accel(sv_ctx *ctx, int64_t first, int64_t last, double *a3_out);
+/* acceleration[i].xyz += a_i for inbound i, i.e. the += contract of
+ * ForceCalculationMethod::updateAcceleration on the reference's vec4 array. */
+SV_API sv_status sv_add_accel_ref32(sv_ctx *ctx, float *acc4);
+
+/* nsteps of LeapfrogDKD (integration_schemes.cpp:856-891): drift dt/2,
+ * kick dt (force + uniform field), drift dt/2, with the reference's
+ * injection-time clamps (particles.cpp:693-786).  t0 is the time at the start
+ * of the first step. */
+SV_API sv_status sv_leapfrog(sv_ctx *ctx, int32_t nsteps, double dt, double t0);
+
+/* Kinetic and softened potential energy in J, FP64, over all particles
+ * (particles.cpp:535-578 with the halving of integration_schemes.cpp:815). */
+SV_API sv_status sv_energy(sv_ctx *ctx, double *ke, double *pe);
+
+/* Per-particle relative-L2 accuracy metric (integration_schemes.cpp:411-461)
+ * of the device acceleration against a host reference (3n, m/s^2). */
+SV_API sv_status sv_compare_accel(sv_ctx *ctx, const double *ref3, double *l2, double *maxl2,
+                           int64_t *argmax);
+
+SV_API sv_status sv_get_stats(const sv_ctx *ctx, sv_stats *out);
+SV_API sv_status sv_sync(sv_ctx *ctx);
+/* The context's cudaStream_t, for callers that time or order work on it. */
+SV_API void *sv_stream(sv_ctx *ctx);
+/* Kernels this context has launched since creation. */
+SV_API uint64_t sv_launch_count(const sv_ctx *ctx);
+SV_API const char *sv_last_error(const sv_ctx *ctx);
+SV_API int32_t sv_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SOLVEIT_GPU_H */

@@ -1,0 +1,597 @@
+// api.cu -- the C ABI (include/solveit_gpu.h): context, state transfer,
+// dispatch of force methods, leapfrog, diagnostics.
+#include <cmath>
+#include <cstdarg>
+#include <vector>
+#include <algorithm>
+
+#include "sv_internal.cuh"
+
+namespace sv {
+
+sv_status set_error(sv_ctx *c, sv_status s, const char *fmt, ...) {
+    if (c) {
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(c->err, sizeof(c->err), fmt, ap);
+        va_end(ap);
+    }
+    return s;
+}
+
+sv_status cuda_error(sv_ctx *c, cudaError_t e, const char *what, const char *file, int line) {
+    return set_error(c, e == cudaErrorMemoryAllocation ? SV_ERR_ALLOC : SV_ERR_CUDA, "%s failed: %s (%s:%d)",
+                     what, cudaGetErrorString(e), file, line);
+}
+
+// Image offsets of the reference's finite periodic lattice: the Grid's
+// canonical points (lattice_point.h:65-131: generated pass by pass, sorted by
+// descending norm) expanded by the sign / axis-permutation loops of
+// directKernelTranslationCalculation (direct_force_method_translational.cpp:
+// 35-306).  Returned in that summation order, as metres.
+int trans_images(const sv_params &P, double *out, int max_out) {
+    int box = 1;
+    for (int l = 0; l < P.sym_levels; l++) box *= 3;
+    const int n = box / 2;
+    const int ax[3] = {P.sym_axes[0] != 0, P.sym_axes[1] != 0, P.sym_axes[2] != 0};
+    const int dsum = ax[0] + ax[1] + ax[2];
+    struct Pt { int v[3]; int norm() const { return v[0] * v[0] + v[1] * v[1] + v[2] * v[2]; } };
+    std::vector<Pt> pts;
+    int t[3] = {ax[0], ax[1], ax[2]};
+    for (int pass = 0; pass < dsum; pass++) {
+        for (int i = t[0];; i++) {
+            for (int j = t[1];; j++) {
+                for (int k = t[2];; k++) {
+                    pts.push_back(Pt{{i, j, k}});
+                    if (!(t[2] != 0 && k + 1 <= n)) break;
+                }
+                if (!(t[1] != 0 && j + 1 <= n)) break;
+            }
+            if (!(t[0] != 0 && i + 1 <= n)) break;
+        }
+        if (t[0] == 0) {
+            if (t[1] == 0) t[2] = 0; else t[1] = 0;
+        } else {
+            t[0] = 0;
+        }
+    }
+    pts.push_back(Pt{{0, 0, 0}});
+    std::stable_sort(pts.begin(), pts.end(), [](const Pt &a, const Pt &b) { return a.norm() > b.norm(); });
+    auto oe = [](int i) { return (i & 1) ? -1 : 1; };
+    int cnt = 0;
+    auto emit = [&](int x, int y, int z) {
+        if (cnt < max_out) {
+            out[3 * cnt + 0] = x * P.domain_size[0];
+            out[3 * cnt + 1] = y * P.domain_size[1];
+            out[3 * cnt + 2] = z * P.domain_size[2];
+        }
+        cnt++;
+    };
+    for (const Pt &p : pts) {
+        const int px = p.v[0], py = p.v[1], pz = p.v[2];
+        const int nz = (px != 0) + (py != 0) + (pz != 0);
+        const int ni = 1 + (px != 0), nj = 1 + (py != 0), nk = 1 + (pz != 0);
+        if (dsum == 3 && nz == 3) {
+            for (int i = 0; i < 2; i++)
+                for (int j = 0; j < 2; j++)
+                    for (int k = 0; k < 2; k++) emit(oe(i) * px, oe(j) * py, oe(k) * pz);
+        } else if (dsum == 3 && nz == 2) {
+            for (int jj = 0; jj < 3; jj++)
+                for (int i = 0; i < ni; i++)
+                    for (int j = 0; j < nj; j++)
+                        for (int k = 0; k < nk; k++)
+                            emit((jj != 0) * oe(i) * px + (px == 0) * ((jj == 1) * oe(j) * py + (jj == 2) * oe(k) * pz),
+                                 (jj != 1) * oe(j) * py + (py == 0) * ((jj == 0) * oe(i) * px + (jj == 2) * oe(k) * pz),
+                                 (jj != 2) * oe(k) * pz + (pz == 0) * ((jj == 0) * oe(i) * px + (jj == 1) * oe(j) * py));
+        } else if (dsum == 3 && nz == 1) {
+            for (int jj = 0; jj < 3; jj++)
+                for (int i = 0; i < ni; i++)
+                    for (int j = 0; j < nj; j++)
+                        for (int k = 0; k < nk; k++)
+                            emit((jj == 0) * oe(i) * px + (jj == 1) * oe(j) * py + (jj == 2) * oe(k) * pz,
+                                 (jj == 0) * oe(j) * py + (jj == 1) * oe(k) * pz + (jj == 2) * oe(i) * px,
+                                 (jj == 0) * oe(k) * pz + (jj == 1) * oe(i) * px + (jj == 2) * oe(j) * py);
+        } else if (dsum == 2 && nz == 2) {
+            for (int i = 0; i < ni; i++)
+                for (int j = 0; j < nj; j++)
+                    for (int k = 0; k < nk; k++) emit(oe(i) * px, oe(j) * py, oe(k) * pz);
+        } else if (dsum == 2 && nz == 1) {
+            for (int jj = 0; jj < 2; jj++)
+                for (int i = 0; i < ni; i++)
+                    for (int j = 0; j < nj; j++)
+                        for (int k = 0; k < nk; k++)
+                            emit(ax[0] * ((jj == 0) * oe(i) * px + (jj == 1) * (oe(j) * py + oe(k) * pz)),
+                                 ax[1] * ((jj == 0) * oe(j) * py + (jj == 1) * (oe(i) * px + oe(k) * pz)),
+                                 ax[2] * ((jj == 0) * oe(k) * pz + (jj == 1) * (oe(i) * px + oe(j) * py)));
+        } else if (dsum == 1 && nz == 1) {
+            for (int i = 0; i < ni; i++)
+                for (int j = 0; j < nj; j++)
+                    for (int k = 0; k < nk; k++) emit(oe(i) * px, oe(j) * py, oe(k) * pz);
+        } else {
+            emit(0, 0, 0);
+        }
+    }
+    return cnt;
+}
+
+namespace {
+
+template <typename T>
+sv_status dev_alloc(sv_ctx *c, T **p, int64_t count) {
+    cudaFree(*p);
+    *p = nullptr;
+    SV_CK(c, cudaMalloc(p, sizeof(T) * (size_t)(count > 0 ? count : 1)));
+    return SV_OK;
+}
+
+void free_state(sv_ctx *c) {
+    cudaFree(c->x); cudaFree(c->y); cudaFree(c->z);
+    cudaFree(c->vx); cudaFree(c->vy); cudaFree(c->vz);
+    cudaFree(c->q); cudaFree(c->m); cudaFree(c->t_inj); cudaFree(c->status);
+    cudaFree(c->ax); cudaFree(c->ay); cudaFree(c->az);
+    c->x = c->y = c->z = c->vx = c->vy = c->vz = c->q = c->m = c->t_inj = nullptr;
+    c->ax = c->ay = c->az = nullptr;
+    c->status = nullptr;
+    c->cap = 0;
+}
+
+sv_status ensure_capacity(sv_ctx *c, int64_t n) {
+    if (n <= c->cap && c->x) return SV_OK;
+    free_state(c);
+    const int64_t cap = std::max<int64_t>(n, 1024);
+    SV_TRY(dev_alloc(c, &c->x, cap)); SV_TRY(dev_alloc(c, &c->y, cap)); SV_TRY(dev_alloc(c, &c->z, cap));
+    SV_TRY(dev_alloc(c, &c->vx, cap)); SV_TRY(dev_alloc(c, &c->vy, cap)); SV_TRY(dev_alloc(c, &c->vz, cap));
+    SV_TRY(dev_alloc(c, &c->q, cap)); SV_TRY(dev_alloc(c, &c->m, cap)); SV_TRY(dev_alloc(c, &c->t_inj, cap));
+    SV_TRY(dev_alloc(c, &c->status, cap));
+    SV_TRY(dev_alloc(c, &c->ax, cap)); SV_TRY(dev_alloc(c, &c->ay, cap)); SV_TRY(dev_alloc(c, &c->az, cap));
+    c->cap = cap;
+    return SV_OK;
+}
+
+__global__ void unpack_fp64(const double *__restrict__ x3, const double *__restrict__ v3,
+                            const double *__restrict__ q, const double *__restrict__ m,
+                            const int32_t *__restrict__ st, const double *__restrict__ tinj, int64_t n,
+                            int has_v, int has_t, double *__restrict__ x, double *__restrict__ y,
+                            double *__restrict__ z, double *__restrict__ vx, double *__restrict__ vy,
+                            double *__restrict__ vz, double *__restrict__ qo, double *__restrict__ mo,
+                            int32_t *__restrict__ so, double *__restrict__ to) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    x[i] = x3[3 * i]; y[i] = x3[3 * i + 1]; z[i] = x3[3 * i + 2];
+    vx[i] = has_v ? v3[3 * i] : 0.0; vy[i] = has_v ? v3[3 * i + 1] : 0.0; vz[i] = has_v ? v3[3 * i + 2] : 0.0;
+    qo[i] = q[i]; mo[i] = m[i]; so[i] = st[i];
+    to[i] = has_t ? tinj[i] : 0.0;
+}
+
+// ParticleSpeciesFunction::getMass (particles.h:65-87): EMI 111, BF4 87 amu
+__device__ double species_mass(int s) {
+    switch (s) {
+    case 0: return 111.0;
+    case 1: return 2 * 111.0 + 87.0;
+    case 2: return 3 * 111.0 + 2 * 87.0;
+    case 4: return 111.0 + 87.0;
+    case 5: return 87.0;
+    case 6: return 111.0 + 2 * 87.0;
+    case 7: return 2 * 111.0 + 3 * 87.0;
+    default: return 0.0;  // droplet (3): unsupported in the reference, mass 0
+    }
+}
+
+__global__ void unpack_ref32(const float4 *__restrict__ pos4, const float4 *__restrict__ vel4,
+                             const float4 *__restrict__ acc4, const float *__restrict__ tinj, int64_t n,
+                             int has_t, double *__restrict__ x, double *__restrict__ y,
+                             double *__restrict__ z, double *__restrict__ vx, double *__restrict__ vy,
+                             double *__restrict__ vz, double *__restrict__ qo, double *__restrict__ mo,
+                             int32_t *__restrict__ so, double *__restrict__ to) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = pos4[i], v = vel4[i], a = acc4[i];
+    x[i] = p.x; y[i] = p.y; z[i] = p.z; qo[i] = p.w;
+    vx[i] = v.x; vy[i] = v.y; vz[i] = v.z;
+    mo[i] = species_mass((int)v.w);
+    so[i] = (int32_t)a.w;
+    to[i] = has_t ? (double)tinj[i] : 0.0;
+}
+
+__global__ void pack_fp64(const double *__restrict__ x, const double *__restrict__ y,
+                          const double *__restrict__ z, const double *__restrict__ vx,
+                          const double *__restrict__ vy, const double *__restrict__ vz, int64_t n,
+                          double *__restrict__ x3, double *__restrict__ v3) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    x3[3 * i] = x[i]; x3[3 * i + 1] = y[i]; x3[3 * i + 2] = z[i];
+    v3[3 * i] = vx[i]; v3[3 * i + 1] = vy[i]; v3[3 * i + 2] = vz[i];
+}
+
+__global__ void pack_accel(const double *__restrict__ ax, const double *__restrict__ ay,
+                           const double *__restrict__ az, const int32_t *__restrict__ st,
+                           int64_t first, int64_t last, int64_t n, double *__restrict__ a3) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const bool t = st[i] == 1 && i >= first && i < last;
+    a3[3 * i] = t ? ax[i] : 0.0;
+    a3[3 * i + 1] = t ? ay[i] : 0.0;
+    a3[3 * i + 2] = t ? az[i] : 0.0;
+}
+
+__global__ void zero_nontargets(double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az,
+                                const int32_t *__restrict__ st, int64_t first, int64_t last, int64_t n) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (!(st[i] == 1 && i >= first && i < last)) ax[i] = ay[i] = az[i] = 0.0;
+}
+
+sv_status stage_bytes(sv_ctx *c, size_t bytes, void **p) {
+    if (c->d_stage_bytes < bytes) {
+        cudaFree(c->d_stage);
+        c->d_stage = nullptr;
+        c->d_stage_bytes = 0;
+        SV_CK(c, cudaMalloc(&c->d_stage, bytes));
+        c->d_stage_bytes = bytes;
+    }
+    *p = c->d_stage;
+    return SV_OK;
+}
+
+sv_status check_params(sv_ctx *c, const sv_params *p) {
+    if (!p) return set_error(c, SV_ERR_INVALID, "params is null");
+    if (p->method < SV_METHOD_DIRECT || p->method > SV_METHOD_FMM)
+        return set_error(c, SV_ERR_INVALID, "unknown method %d", p->method);
+    if (p->precision < SV_PREC_MIXED || p->precision > SV_PREC_FP64)
+        return set_error(c, SV_ERR_INVALID, "unknown precision %d", p->precision);
+    if (p->symmetry < SV_SYM_NONE || p->symmetry > SV_SYM_TRANSLATIONAL)
+        return set_error(c, SV_ERR_INVALID, "unknown symmetry %d", p->symmetry);
+    if (!(p->softening2 >= 0.0) || !std::isfinite(p->softening2))
+        return set_error(c, SV_ERR_INVALID, "softening2 must be finite and >= 0");
+    if (p->fmm_order < 1 || p->fmm_order > 10)
+        return set_error(c, SV_ERR_INVALID, "fmm_order %d outside 1..10", p->fmm_order);
+    if (p->fmm_ws < 1 || p->fmm_ws > 2) return set_error(c, SV_ERR_INVALID, "fmm_ws must be 1 or 2");
+    if (p->leaf_size < 1 || p->leaf_size > 64) return set_error(c, SV_ERR_INVALID, "leaf_size outside 1..64");
+    if (!(p->theta >= 0.0f) || p->theta > 1.0f) return set_error(c, SV_ERR_INVALID, "theta outside [0, 1]");
+    if (p->fmm_leaf_target < 1 || p->fmm_leaf_target > 4096)
+        return set_error(c, SV_ERR_INVALID, "fmm_leaf_target outside 1..4096");
+    if (p->symmetry == SV_SYM_TRANSLATIONAL) {
+        if (p->sym_levels < 0 || p->sym_levels > 4) return set_error(c, SV_ERR_INVALID, "sym_levels outside 0..4");
+        for (int d = 0; d < 3; d++)
+            if (p->sym_axes[d] && !(p->domain_size[d] > 0.0))
+                return set_error(c, SV_ERR_INVALID, "periodic axis %d needs domain_size > 0", d);
+    }
+    return SV_OK;
+}
+
+int grid_of(int64_t n) { return (int)((n + 255) / 256 > 0 ? (n + 255) / 256 : 1); }
+
+}  // namespace
+}  // namespace sv
+
+using namespace sv;
+
+extern "C" {
+
+int32_t sv_abi_version(void) { return SV_ABI_VERSION; }
+
+sv_status sv_default_params(sv_params *p) {
+    if (!p) return SV_ERR_INVALID;
+    memset(p, 0, sizeof(*p));
+    p->softening2 = 6.4e-19;
+    {
+        // constants.h:46, evaluated as the reference does (float e^2, long double denominator)
+        const float e = 1.6021766e-19f, amu = 1.66053904e-27f, eps0 = 8.85419e-12f;
+        const long double pi = 3.14159265358979323846264338328L;
+        const float e2 = e * e;
+        p->k_const = (double)((long double)e2 / (4 * pi * eps0 * amu));
+        const float eoa = e / amu;
+        p->e_over_amu = (double)eoa;
+    }
+    p->method = SV_METHOD_DIRECT;
+    p->precision = SV_PREC_MIXED;
+    p->symmetry = SV_SYM_NONE;
+    p->theta = 0.5f;
+    p->leaf_size = 16;
+    p->fmm_order = 8;
+    p->fmm_ws = 1;
+    p->fmm_leaf_target = 32;
+    p->sym_axes[0] = p->sym_axes[1] = 1;
+    p->sym_levels = 2;
+    p->domain_size[0] = p->domain_size[1] = 2e-6;
+    p->device = 0;
+    return SV_OK;
+}
+
+sv_status sv_create(const sv_params *p, sv_ctx **out) {
+    if (!out) return SV_ERR_INVALID;
+    *out = nullptr;
+    sv_ctx *c = new (std::nothrow) sv_ctx();
+    if (!c) return SV_ERR_ALLOC;
+    sv_status s = check_params(c, p);
+    if (s != SV_OK) {
+        delete c;
+        return s;
+    }
+    c->P = *p;
+    c->device = p->device;
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d_scalar, 64 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMallocHost(&c->h_scalar, 64 * sizeof(double));
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev_begin);
+    if (e == cudaSuccess) e = cudaEventCreate(&c->ev_end);
+    if (e != cudaSuccess) {
+        sv_destroy(c);
+        return e == cudaErrorMemoryAllocation ? SV_ERR_ALLOC : SV_ERR_CUDA;
+    }
+    *out = c;
+    return SV_OK;
+}
+
+void sv_destroy(sv_ctx *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    tree_free(c);
+    fmm_free(c);
+    free_state(c);
+    Sorted &S = c->S;
+    cudaFree(S.x); cudaFree(S.y); cudaFree(S.z); cudaFree(S.q); cudaFree(S.qm);
+    cudaFree(S.idx); cudaFree(S.keys); cudaFree(S.keys_alt); cudaFree(S.idx_alt);
+    cudaFree(S.ax); cudaFree(S.ay); cudaFree(S.az); cudaFree(S.cub_tmp);
+    cudaFree(S.root); cudaFree(S.red);
+    cudaFree(c->d_stage);
+    cudaFree(c->d_scalar);
+    if (c->h_scalar) cudaFreeHost(c->h_scalar);
+    if (c->ev_begin) cudaEventDestroy(c->ev_begin);
+    if (c->ev_end) cudaEventDestroy(c->ev_end);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+sv_status sv_set_params(sv_ctx *c, const sv_params *p) {
+    if (!c) return SV_ERR_INVALID;
+    SV_TRY(check_params(c, p));
+    if (p->device != c->device) return set_error(c, SV_ERR_INVALID, "device cannot change on a context");
+    c->P = *p;
+    return SV_OK;
+}
+
+sv_status sv_get_params(const sv_ctx *c, sv_params *p) {
+    if (!c || !p) return SV_ERR_INVALID;
+    *p = c->P;
+    return SV_OK;
+}
+
+sv_status sv_upload(sv_ctx *c, int64_t n, const double *x3, const double *v3, const double *q,
+                    const double *m_amu, const int32_t *status, const double *t_inj) {
+    if (!c) return SV_ERR_INVALID;
+    if (n < 0 || n > (int64_t)INT32_MAX) return set_error(c, SV_ERR_INVALID, "n=%lld out of range", (long long)n);
+    if (n > 0 && (!x3 || !q || !m_amu || !status)) return set_error(c, SV_ERR_INVALID, "null state array");
+    SV_CK(c, cudaSetDevice(c->device));
+    SV_TRY(ensure_capacity(c, n));
+    c->n = n;
+    c->have_state = true;
+    c->have_accel = false;
+    if (n == 0) return SV_OK;
+    const size_t b3 = sizeof(double) * 3 * (size_t)n, b1 = sizeof(double) * (size_t)n;
+    void *stg = nullptr;
+    SV_TRY(stage_bytes(c, 2 * b3 + 3 * b1 + sizeof(int32_t) * (size_t)n, &stg));
+    char *p = (char *)stg;
+    double *dx3 = (double *)p; p += b3;
+    double *dv3 = (double *)p; p += b3;
+    double *dq = (double *)p; p += b1;
+    double *dm = (double *)p; p += b1;
+    double *dt = (double *)p; p += b1;
+    int32_t *ds = (int32_t *)p;
+    SV_CK(c, cudaMemcpyAsync(dx3, x3, b3, cudaMemcpyHostToDevice, c->stream));
+    if (v3) SV_CK(c, cudaMemcpyAsync(dv3, v3, b3, cudaMemcpyHostToDevice, c->stream));
+    SV_CK(c, cudaMemcpyAsync(dq, q, b1, cudaMemcpyHostToDevice, c->stream));
+    SV_CK(c, cudaMemcpyAsync(dm, m_amu, b1, cudaMemcpyHostToDevice, c->stream));
+    if (t_inj) SV_CK(c, cudaMemcpyAsync(dt, t_inj, b1, cudaMemcpyHostToDevice, c->stream));
+    SV_CK(c, cudaMemcpyAsync(ds, status, sizeof(int32_t) * n, cudaMemcpyHostToDevice, c->stream));
+    unpack_fp64<<<grid_of(n), 256, 0, c->stream>>>(dx3, dv3, dq, dm, ds, dt, n, v3 != nullptr, t_inj != nullptr,
+                                                   c->x, c->y, c->z, c->vx, c->vy, c->vz, c->q, c->m,
+                                                   c->status, c->t_inj);
+    SV_LAUNCHED(c);
+    return SV_OK;
+}
+
+sv_status sv_upload_ref32(sv_ctx *c, int64_t n, const float *pos4, const float *vel4, const float *acc4,
+                          const float *t_inj) {
+    if (!c) return SV_ERR_INVALID;
+    if (n < 0 || n > (int64_t)INT32_MAX) return set_error(c, SV_ERR_INVALID, "n=%lld out of range", (long long)n);
+    if (n > 0 && (!pos4 || !vel4 || !acc4)) return set_error(c, SV_ERR_INVALID, "null state array");
+    SV_CK(c, cudaSetDevice(c->device));
+    SV_TRY(ensure_capacity(c, n));
+    c->n = n;
+    c->have_state = true;
+    c->have_accel = false;
+    if (n == 0) return SV_OK;
+    const size_t b4 = 16 * (size_t)n;
+    void *stg = nullptr;
+    SV_TRY(stage_bytes(c, 3 * b4 + 4 * (size_t)n, &stg));
+    char *p = (char *)stg;
+    float4 *dp = (float4 *)p; p += b4;
+    float4 *dv = (float4 *)p; p += b4;
+    float4 *da = (float4 *)p; p += b4;
+    float *dt = (float *)p;
+    SV_CK(c, cudaMemcpyAsync(dp, pos4, b4, cudaMemcpyHostToDevice, c->stream));
+    SV_CK(c, cudaMemcpyAsync(dv, vel4, b4, cudaMemcpyHostToDevice, c->stream));
+    SV_CK(c, cudaMemcpyAsync(da, acc4, b4, cudaMemcpyHostToDevice, c->stream));
+    if (t_inj) SV_CK(c, cudaMemcpyAsync(dt, t_inj, 4 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+    unpack_ref32<<<grid_of(n), 256, 0, c->stream>>>(dp, dv, da, dt, n, t_inj != nullptr, c->x, c->y, c->z,
+                                                    c->vx, c->vy, c->vz, c->q, c->m, c->status, c->t_inj);
+    SV_LAUNCHED(c);
+    return SV_OK;
+}
+
+sv_status sv_download(sv_ctx *c, double *x3, double *v3, int32_t *status) {
+    if (!c) return SV_ERR_INVALID;
+    if (!c->have_state) return set_error(c, SV_ERR_STATE, "no state uploaded");
+    const int64_t n = c->n;
+    if (n == 0) return SV_OK;
+    SV_CK(c, cudaSetDevice(c->device));
+    const size_t b3 = sizeof(double) * 3 * (size_t)n;
+    void *stg = nullptr;
+    SV_TRY(stage_bytes(c, 2 * b3, &stg));
+    double *dx3 = (double *)stg, *dv3 = dx3 + 3 * n;
+    pack_fp64<<<grid_of(n), 256, 0, c->stream>>>(c->x, c->y, c->z, c->vx, c->vy, c->vz, n, dx3, dv3);
+    SV_LAUNCHED(c);
+    if (x3) SV_CK(c, cudaMemcpyAsync(x3, dx3, b3, cudaMemcpyDeviceToHost, c->stream));
+    if (v3) SV_CK(c, cudaMemcpyAsync(v3, dv3, b3, cudaMemcpyDeviceToHost, c->stream));
+    if (status) SV_CK(c, cudaMemcpyAsync(status, c->status, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, c->stream));
+    SV_CK(c, cudaStreamSynchronize(c->stream));
+    return SV_OK;
+}
+
+sv_status sv_download_ref32(sv_ctx *c, float *pos4, float *vel4) {
+    if (!c) return SV_ERR_INVALID;
+    const int64_t n = c->n;
+    std::vector<double> x(3 * n), v(3 * n);
+    SV_TRY(sv_download(c, x.data(), v.data(), nullptr));
+    for (int64_t i = 0; i < n; i++) {
+        for (int d = 0; d < 3; d++) {
+            if (pos4) pos4[4 * i + d] = (float)x[3 * i + d];
+            if (vel4) vel4[4 * i + d] = (float)v[3 * i + d];
+        }
+    }
+    return SV_OK;
+}
+
+static sv_status compute_accel_device(sv_ctx *c, int64_t first, int64_t last) {
+    if (!c->have_state) return set_error(c, SV_ERR_STATE, "no state uploaded");
+    if (first < 0) first = 0;
+    if (last > c->n || last < 0) last = c->n;
+    const int64_t n = c->n;
+    memset(&c->stats, 0, sizeof(c->stats));
+    SV_CK(c, cudaEventRecord(c->ev_begin, c->stream));
+    if (n > 0) {
+        SV_TRY(sort_state(c, first, last));
+        switch (c->P.method) {
+        case SV_METHOD_DIRECT: SV_TRY(direct_accel(c)); break;
+        case SV_METHOD_BARNES_HUT: SV_TRY(bh_accel(c)); break;
+        case SV_METHOD_FMM: SV_TRY(fmm_accel(c)); break;
+        default: return set_error(c, SV_ERR_INVALID, "unknown method");
+        }
+        SV_TRY(unsort_accel(c));
+        zero_nontargets<<<grid_of(n), 256, 0, c->stream>>>(c->ax, c->ay, c->az, c->status, first, last, n);
+        SV_LAUNCHED(c);
+    }
+    SV_CK(c, cudaEventRecord(c->ev_end, c->stream));
+    c->have_accel = true;
+    return SV_OK;
+}
+
+sv_status sv_compute_accel(sv_ctx *c, int64_t first, int64_t last, double *a3_out) {
+    if (!c) return SV_ERR_INVALID;
+    SV_CK(c, cudaSetDevice(c->device));
+    SV_TRY(compute_accel_device(c, first, last));
+    if (a3_out && c->n > 0) {
+        const int64_t n = c->n;
+        void *stg = nullptr;
+        SV_TRY(stage_bytes(c, sizeof(double) * 3 * n, &stg));
+        pack_accel<<<grid_of(n), 256, 0, c->stream>>>(c->ax, c->ay, c->az, c->status, 0, n, n, (double *)stg);
+        SV_LAUNCHED(c);
+        SV_CK(c, cudaMemcpyAsync(a3_out, stg, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c->stream));
+        SV_CK(c, cudaStreamSynchronize(c->stream));
+    }
+    return SV_OK;
+}
+
+sv_status sv_add_accel_ref32(sv_ctx *c, float *acc4) {
+    if (!c || !acc4) return SV_ERR_INVALID;
+    if (!c->have_accel) return set_error(c, SV_ERR_STATE, "no acceleration computed");
+    const int64_t n = c->n;
+    std::vector<double> a(3 * n);
+    void *stg = nullptr;
+    SV_TRY(stage_bytes(c, sizeof(double) * 3 * n, &stg));
+    pack_accel<<<grid_of(n), 256, 0, c->stream>>>(c->ax, c->ay, c->az, c->status, 0, n, n, (double *)stg);
+    SV_LAUNCHED(c);
+    SV_CK(c, cudaMemcpyAsync(a.data(), stg, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c->stream));
+    SV_CK(c, cudaStreamSynchronize(c->stream));
+    for (int64_t i = 0; i < n; i++) {
+        if (acc4[4 * i + 3] != 1.0f) continue;
+        for (int d = 0; d < 3; d++) acc4[4 * i + d] = (float)((double)acc4[4 * i + d] + a[3 * i + d]);
+    }
+    return SV_OK;
+}
+
+sv_status sv_leapfrog(sv_ctx *c, int32_t nsteps, double dt, double t0) {
+    if (!c) return SV_ERR_INVALID;
+    if (!c->have_state) return set_error(c, SV_ERR_STATE, "no state uploaded");
+    if (nsteps < 0 || !(dt > 0.0)) return set_error(c, SV_ERR_INVALID, "nsteps >= 0 and dt > 0 required");
+    SV_CK(c, cudaSetDevice(c->device));
+    const double h = 0.5 * dt;
+    for (int it = 0; it < nsteps; it++) {
+        const double ts = t0 + dt * it;
+        SV_TRY(drift(c, ts, h));
+        SV_TRY(compute_accel_device(c, 0, c->n));
+        SV_TRY(kick(c, ts, dt));
+        SV_TRY(drift(c, ts + h, h));
+    }
+    return SV_OK;
+}
+
+sv_status sv_energy(sv_ctx *c, double *ke, double *pe) {
+    if (!c || !ke || !pe) return SV_ERR_INVALID;
+    if (!c->have_state) return set_error(c, SV_ERR_STATE, "no state uploaded");
+    SV_CK(c, cudaSetDevice(c->device));
+    if (c->n == 0) {
+        *ke = *pe = 0.0;
+        return SV_OK;
+    }
+    return energy(c, ke, pe);
+}
+
+sv_status sv_compare_accel(sv_ctx *c, const double *ref3, double *l2, double *maxl2, int64_t *argmax) {
+    if (!c || !ref3 || !l2) return SV_ERR_INVALID;
+    if (!c->have_accel) return set_error(c, SV_ERR_STATE, "no acceleration computed");
+    const int64_t n = c->n;
+    std::vector<double> a(3 * n);
+    std::vector<int32_t> st(n);
+    void *stg = nullptr;
+    SV_TRY(stage_bytes(c, sizeof(double) * 3 * n, &stg));
+    pack_accel<<<grid_of(n), 256, 0, c->stream>>>(c->ax, c->ay, c->az, c->status, 0, n, n, (double *)stg);
+    SV_LAUNCHED(c);
+    SV_CK(c, cudaMemcpyAsync(a.data(), stg, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c->stream));
+    SV_CK(c, cudaMemcpyAsync(st.data(), c->status, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, c->stream));
+    SV_CK(c, cudaStreamSynchronize(c->stream));
+    double s = 0, mx = 0;
+    int64_t cnt = 0, am = 0;
+    for (int64_t k = 0; k < n; k++) {
+        if (st[k] != 1) continue;
+        cnt++;
+        double d = 0, nr = 0;
+        for (int e = 0; e < 3; e++) {
+            const double df = a[3 * k + e] - ref3[3 * k + e];
+            d += df * df;
+            nr += ref3[3 * k + e] * ref3[3 * k + e];
+        }
+        const double r = (nr == 0 && d == 0) ? 0.0 : d / nr;
+        s += r;
+        if (r > mx) { mx = r; am = k; }
+    }
+    *l2 = cnt ? std::sqrt(s / cnt) : 0.0;
+    if (maxl2) *maxl2 = std::sqrt(mx);
+    if (argmax) *argmax = am;
+    return SV_OK;
+}
+
+sv_status sv_get_stats(const sv_ctx *c, sv_stats *out) {
+    if (!c || !out) return SV_ERR_INVALID;
+    *out = c->stats;
+    float ms = 0.f;
+    if (c->have_accel && cudaEventQuery(c->ev_end) == cudaSuccess &&
+        cudaEventElapsedTime(&ms, c->ev_begin, c->ev_end) == cudaSuccess)
+        out->ms_total = ms;
+    return SV_OK;
+}
+
+sv_status sv_sync(sv_ctx *c) {
+    if (!c) return SV_ERR_INVALID;
+    SV_CK(c, cudaStreamSynchronize(c->stream));
+    return SV_OK;
+}
+
+void *sv_stream(sv_ctx *c) { return c ? (void *)c->stream : nullptr; }
+uint64_t sv_launch_count(const sv_ctx *c) { return c ? c->launches : 0; }
+const char *sv_last_error(const sv_ctx *c) { return c ? c->err : "null context"; }
+
+}  // extern "C"

@@ -1,0 +1,246 @@
+// sort.cu -- Morton ordering of the plume shared by every force method.
+//
+// The reference sorts particles by Morton index only inside the FMM
+// (multipole_method_force_calculation.cpp:883-1083 presortMorton / sort /
+// sortParticles, unsortParticles :1184).  Here every method works on a
+// Morton-sorted copy so that consecutive targets are close in space; the
+// caller's array order is untouched (results are scattered back), as the
+// reference requires of updateAcceleration.
+#include <cub/device/device_radix_sort.cuh>
+
+#include "sv_internal.cuh"
+
+namespace sv {
+namespace {
+
+constexpr int kRedThreads = 256;
+
+__device__ __forceinline__ bool is_source(int32_t s) { return s == 1 || s == 2; }
+
+// Per-block min/max of source positions (status 1 or 2).
+__global__ void bbox_partial(const double *__restrict__ x, const double *__restrict__ y,
+                             const double *__restrict__ z, const int32_t *__restrict__ st,
+                             int64_t n, double *__restrict__ out) {
+    double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        if (!is_source(st[i])) continue;
+        double p[3] = {x[i], y[i], z[i]};
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            mn[d] = fmin(mn[d], p[d]);
+            mx[d] = fmax(mx[d], p[d]);
+        }
+    }
+    __shared__ double sh[6][kRedThreads / 32];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        for (int o = 16; o > 0; o >>= 1) {
+            mn[d] = fmin(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
+            mx[d] = fmax(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
+        }
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) {
+        for (int d = 0; d < 3; d++) {
+            sh[d][w] = mn[d];
+            sh[3 + d][w] = mx[d];
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int d = threadIdx.x;
+        double v = d < 3 ? 1e300 : -1e300;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) v = d < 3 ? fmin(v, sh[d][k]) : fmax(v, sh[d][k]);
+        out[blockIdx.x * 6 + d] = v;
+    }
+}
+
+// Final reduction; root = origin (bbox min), cube side S = smallest power of
+// two >= the largest extent (so every box side and every box-centre offset
+// S/2^l * k is exact in binary floating point), then the bbox max.
+__global__ void bbox_final(const double *__restrict__ part, int nblocks, double *__restrict__ root) {
+    __shared__ double sh[6];
+    if (threadIdx.x < 6) {
+        const int d = threadIdx.x;
+        double v = d < 3 ? 1e300 : -1e300;
+        for (int k = 0; k < nblocks; k++) v = d < 3 ? fmin(v, part[k * 6 + d]) : fmax(v, part[k * 6 + d]);
+        sh[d] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double ext = 0.0;
+        bool empty = sh[0] > sh[3];
+        for (int d = 0; d < 3; d++) ext = fmax(ext, sh[3 + d] - sh[d]);
+        if (empty) {
+            for (int d = 0; d < 6; d++) sh[d] = 0.0;
+            ext = 0.0;
+        }
+        // guard against a zero extent (single particle) and keep the maximum
+        // strictly inside the last cell: S > ext.
+        double S = 1e-300;
+        if (ext > 0.0) {
+            int e;
+            frexp(ext, &e);            // ext = f * 2^e, f in [0.5, 1)
+            S = ldexp(1.0, e);         // 2^e > ext
+        } else {
+            S = 1e-12;
+        }
+        root[0] = sh[0];
+        root[1] = sh[1];
+        root[2] = sh[2];
+        root[3] = S;
+        root[4] = sh[3];
+        root[5] = sh[4];
+        root[6] = sh[5];
+        root[7] = empty ? 1.0 : 0.0;
+    }
+}
+
+__device__ __forceinline__ uint64_t spread3(uint32_t v) {
+    uint64_t x = v & 0x1fffffull;
+    x = (x | (x << 32)) & 0x1f00000000ffffull;
+    x = (x | (x << 16)) & 0x1f0000ff0000ffull;
+    x = (x | (x << 8)) & 0x100f00f00f00f00full;
+    x = (x | (x << 4)) & 0x10c30c30c30c30c3ull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
+    return x;
+}
+
+__global__ void morton_keys(const double *__restrict__ x, const double *__restrict__ y,
+                            const double *__restrict__ z, const int32_t *__restrict__ st,
+                            int64_t n, const double *__restrict__ root,
+                            uint64_t *__restrict__ keys, uint32_t *__restrict__ idx) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    idx[i] = (uint32_t)i;
+    if (!is_source(st[i])) {
+        keys[i] = kInactiveKey;
+        return;
+    }
+    const double inv = (double)(1u << kMortonBits) / root[3];
+    const double p[3] = {x[i] - root[0], y[i] - root[1], z[i] - root[2]};
+    uint32_t c[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        double f = floor(p[d] * inv);
+        f = fmin(fmax(f, 0.0), (double)((1u << kMortonBits) - 1));
+        c[d] = (uint32_t)f;
+    }
+    // bit order within a level: x lowest, then y, then z
+    keys[i] = spread3(c[0]) | (spread3(c[1]) << 1) | (spread3(c[2]) << 2);
+}
+
+__global__ void gather_sorted(const uint32_t *__restrict__ idx, int64_t n,
+                              const double *__restrict__ x, const double *__restrict__ y,
+                              const double *__restrict__ z, const double *__restrict__ q,
+                              const double *__restrict__ m, const int32_t *__restrict__ st,
+                              int64_t first, int64_t last, double kconst,
+                              double *__restrict__ xs, double *__restrict__ ys,
+                              double *__restrict__ zs, float *__restrict__ qs,
+                              double *__restrict__ qm) {
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const uint32_t i = idx[s];
+    xs[s] = x[i];
+    ys[s] = y[i];
+    zs[s] = z[i];
+    const int32_t w = st[i];
+    qs[s] = is_source(w) ? (float)q[i] : 0.0f;
+    const bool tgt = (w == 1) && (int64_t)i >= first && (int64_t)i < last && m[i] > 0.0;
+    qm[s] = tgt ? kconst * q[i] / m[i] : 0.0;
+}
+
+__global__ void scatter_accel(const uint32_t *__restrict__ idx, int64_t n,
+                              const double *__restrict__ axs, const double *__restrict__ ays,
+                              const double *__restrict__ azs, double *__restrict__ ax,
+                              double *__restrict__ ay, double *__restrict__ az) {
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const uint32_t i = idx[s];
+    ax[i] = axs[s];
+    ay[i] = ays[s];
+    az[i] = azs[s];
+}
+
+}  // namespace
+
+sv_status ensure_sorted_capacity(sv_ctx *c, int64_t n) {
+    Sorted &S = c->S;
+    if (S.cap >= n && S.x) return SV_OK;
+    cudaFree(S.x); cudaFree(S.y); cudaFree(S.z); cudaFree(S.q); cudaFree(S.qm);
+    cudaFree(S.idx); cudaFree(S.keys); cudaFree(S.keys_alt); cudaFree(S.idx_alt);
+    cudaFree(S.ax); cudaFree(S.ay); cudaFree(S.az); cudaFree(S.cub_tmp);
+    cudaFree(S.root); cudaFree(S.red);
+    S = Sorted();
+    const int64_t cap = n < 1024 ? 1024 : n;
+    SV_CK(c, cudaMalloc(&S.x, cap * sizeof(double)));
+    SV_CK(c, cudaMalloc(&S.y, cap * sizeof(double)));
+    SV_CK(c, cudaMalloc(&S.z, cap * sizeof(double)));
+    SV_CK(c, cudaMalloc(&S.q, cap * sizeof(float)));
+    SV_CK(c, cudaMalloc(&S.qm, cap * sizeof(double)));
+    SV_CK(c, cudaMalloc(&S.idx, cap * sizeof(uint32_t)));
+    SV_CK(c, cudaMalloc(&S.idx_alt, cap * sizeof(uint32_t)));
+    SV_CK(c, cudaMalloc(&S.keys, cap * sizeof(uint64_t)));
+    SV_CK(c, cudaMalloc(&S.keys_alt, cap * sizeof(uint64_t)));
+    SV_CK(c, cudaMalloc(&S.ax, cap * sizeof(double)));
+    SV_CK(c, cudaMalloc(&S.ay, cap * sizeof(double)));
+    SV_CK(c, cudaMalloc(&S.az, cap * sizeof(double)));
+    size_t bytes = 0;
+    cub::DoubleBuffer<uint64_t> kb(S.keys, S.keys_alt);
+    cub::DoubleBuffer<uint32_t> vb(S.idx, S.idx_alt);
+    SV_CK(c, cub::DeviceRadixSort::SortPairs(nullptr, bytes, kb, vb, (int)cap, 0, 64, c->stream));
+    S.cub_bytes = bytes;
+    SV_CK(c, cudaMalloc(&S.cub_tmp, bytes));
+    S.red_blocks = 2 * kNumSMs;
+    SV_CK(c, cudaMalloc(&S.red, (size_t)S.red_blocks * 6 * sizeof(double)));
+    SV_CK(c, cudaMalloc(&S.root, 8 * sizeof(double)));
+    S.cap = cap;
+    return SV_OK;
+}
+
+sv_status sort_state(sv_ctx *c, int64_t first, int64_t last) {
+    const int64_t n = c->n;
+    SV_TRY(ensure_sorted_capacity(c, n));
+    Sorted &S = c->S;
+    const int nb = div_up(n, 256);
+    bbox_partial<<<S.red_blocks, kRedThreads, 0, c->stream>>>(c->x, c->y, c->z, c->status, n, S.red);
+    SV_LAUNCHED(c);
+    bbox_final<<<1, 32, 0, c->stream>>>(S.red, S.red_blocks, S.root);
+    SV_LAUNCHED(c);
+    morton_keys<<<nb, 256, 0, c->stream>>>(c->x, c->y, c->z, c->status, n, S.root, S.keys, S.idx);
+    SV_LAUNCHED(c);
+    cub::DoubleBuffer<uint64_t> kb(S.keys, S.keys_alt);
+    cub::DoubleBuffer<uint32_t> vb(S.idx, S.idx_alt);
+    size_t bytes = S.cub_bytes;
+    SV_CK(c, cub::DeviceRadixSort::SortPairs(S.cub_tmp, bytes, kb, vb, (int)n, 0, 3 * kMortonBits + 1,
+                                             c->stream));
+    c->launches += 2 * ((3 * kMortonBits + 1 + 7) / 8);  // CUB onesweep: histogram + passes
+    if (kb.Current() != S.keys) {
+        std::swap(S.keys, S.keys_alt);
+    }
+    if (vb.Current() != S.idx) {
+        std::swap(S.idx, S.idx_alt);
+    }
+    gather_sorted<<<nb, 256, 0, c->stream>>>(S.idx, n, c->x, c->y, c->z, c->q, c->m, c->status, first,
+                                             last, c->P.k_const, S.x, S.y, S.z, S.q, S.qm);
+    SV_LAUNCHED(c);
+    return SV_OK;
+}
+
+sv_status unsort_accel(sv_ctx *c) {
+    const int64_t n = c->n;
+    scatter_accel<<<div_up(n, 256), 256, 0, c->stream>>>(c->S.idx, n, c->S.ax, c->S.ay, c->S.az, c->ax,
+                                                         c->ay, c->az);
+    SV_LAUNCHED(c);
+    return SV_OK;
+}
+
+sv_status read_root(sv_ctx *c, double root[8]) {
+    SV_CK(c, cudaMemcpyAsync(c->h_scalar, c->S.root, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    SV_CK(c, cudaStreamSynchronize(c->stream));
+    memcpy(root, c->h_scalar, 8 * sizeof(double));
+    return SV_OK;
+}
+
+}  // namespace sv

@@ -1,0 +1,131 @@
+// sv_internal.cuh -- shared definitions of the GB300 engine (not part of the ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+
+#include "solveit_gpu.h"
+
+namespace sv {
+
+constexpr int kNumSMs = 152;          // GB300: 2 dies x 76 SMs
+constexpr int kMortonBits = 21;       // bits per axis of the Morton key (63-bit keys)
+constexpr uint64_t kInactiveKey = ~0ull;
+
+// Morton-sorted working copy of the plume, rebuilt at every force evaluation.
+// Sorting makes every block of consecutive targets spatially compact, which is
+// what lets the mixed-precision kernels take FP32 coordinates relative to an
+// FP64 origin per block (or per box) without losing the close pairs.
+struct Sorted {
+    double *x = nullptr, *y = nullptr, *z = nullptr;  // FP64 positions, sorted
+    float *q = nullptr;        // source charge (0 when the particle is no source)
+    double *qm = nullptr;      // K q / m for targets (0 when not a target)
+    uint32_t *idx = nullptr;   // sorted slot -> caller's particle index
+    uint64_t *keys = nullptr, *keys_alt = nullptr;
+    uint32_t *idx_alt = nullptr;
+    double *ax = nullptr, *ay = nullptr, *az = nullptr;  // acceleration, sorted order
+    void *cub_tmp = nullptr;
+    size_t cub_bytes = 0;
+    double *root = nullptr;    // device [8]: origin xyz, cube side S, bbox max xyz, spare
+    double *red = nullptr;     // device reduction scratch
+    int red_blocks = 0;
+    int64_t cap = 0;
+};
+
+struct Fmm;   // fmm.cu
+struct Tree;  // tree.cu
+
+}  // namespace sv
+
+struct sv_ctx {
+    sv_params P{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int64_t n = 0, cap = 0;
+    // caller-order state, FP64 SoA
+    double *x = nullptr, *y = nullptr, *z = nullptr;
+    double *vx = nullptr, *vy = nullptr, *vz = nullptr;
+    double *q = nullptr, *m = nullptr, *t_inj = nullptr;
+    int32_t *status = nullptr;
+    // last acceleration (force only), caller order, FP64
+    double *ax = nullptr, *ay = nullptr, *az = nullptr;
+    bool have_state = false, have_accel = false;
+    sv::Sorted S;
+    sv::Tree *tree = nullptr;
+    sv::Fmm *fmm = nullptr;
+    // device staging for interleaved <-> SoA transfers
+    void *d_stage = nullptr;
+    size_t d_stage_bytes = 0;
+    double *d_scalar = nullptr;   // device scratch for small reductions
+    double *h_scalar = nullptr;   // pinned mirror
+    cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+    unsigned long long launches = 0;
+    sv_stats stats{};
+    char err[512] = {0};
+};
+
+namespace sv {
+
+sv_status set_error(sv_ctx *c, sv_status s, const char *fmt, ...);
+sv_status cuda_error(sv_ctx *c, cudaError_t e, const char *what, const char *file, int line);
+
+#define SV_CK(ctx, call)                                                    \
+    do {                                                                    \
+        cudaError_t _e = (call);                                            \
+        if (_e != cudaSuccess) return ::sv::cuda_error((ctx), _e, #call, __FILE__, __LINE__); \
+    } while (0)
+
+#define SV_LAUNCHED(ctx)                                                    \
+    do {                                                                    \
+        (ctx)->launches++;                                                  \
+        cudaError_t _e = cudaGetLastError();                                \
+        if (_e != cudaSuccess) return ::sv::cuda_error((ctx), _e, "kernel launch", __FILE__, __LINE__); \
+    } while (0)
+
+#define SV_TRY(expr)                                                        \
+    do {                                                                    \
+        sv_status _s = (expr);                                              \
+        if (_s != SV_OK) return _s;                                         \
+    } while (0)
+
+// 32-byte aligned quadruple of doubles (one shared-memory source record)
+struct alignas(32) dbl4_t {
+    double x, y, z, w;
+};
+__host__ __device__ inline dbl4_t dbl4(double x, double y, double z, double w) { return dbl4_t{x, y, z, w}; }
+
+inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+// sort.cu
+sv_status ensure_sorted_capacity(sv_ctx *c, int64_t n);
+// Morton-sort the live plume into c->S (targets: inbound with index in [first,last)).
+sv_status sort_state(sv_ctx *c, int64_t first, int64_t last);
+// Scatter c->S.a{x,y,z} back to caller order into c->a{x,y,z}.
+sv_status unsort_accel(sv_ctx *c);
+// Read root box (origin, side) to the host (blocking).
+sv_status read_root(sv_ctx *c, double root[8]);
+
+// direct.cu
+sv_status direct_accel(sv_ctx *c);  // sorted -> c->S.a*
+
+// tree.cu / bh.cu / fmm.cu
+sv_status bh_accel(sv_ctx *c);
+sv_status fmm_accel(sv_ctx *c);
+void tree_free(sv_ctx *c);
+void fmm_free(sv_ctx *c);
+
+// integrate.cu
+sv_status drift(sv_ctx *c, double t_start, double h);
+sv_status kick(sv_ctx *c, double t_start, double dt);
+sv_status energy(sv_ctx *c, double *ke, double *pe);
+
+// image offsets (metres) of the translational lattice, in summation order
+int trans_images(const sv_params &P, double *out, int max_out);
+
+// constant memory copies per context are not used: parameters travel as
+// kernel arguments so that several contexts can share a device.
+
+}  // namespace sv

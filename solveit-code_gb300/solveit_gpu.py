@@ -1,0 +1,232 @@
+"""Python binding of the C ABI (include/solveit_gpu.h) via ctypes.
+
+This is the host-side mirror of the reference's ForceCalculationMethod use:
+a ForceMethod object owns one GPU context (one plume), uploads the particle
+state, runs updateAcceleration-equivalent evaluations and leapfrog steps, and
+reads results back.  It loads the in-tree libsolveit_gpu.so and raises if the
+library or a GPU is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_build", "libsolveit_gpu.so")
+
+DIRECT, BARNES_HUT, FMM = 0, 1, 2
+SYM_NONE, SYM_ROTATIONAL, SYM_TRANSLATIONAL = 0, 1, 2
+MIXED, FP64 = 0, 1
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "allocation failed", 4: "bad state",
+          5: "capacity exceeded", 6: "device wait timed out", 7: "unsupported"}
+
+# names exported by the library, one per declaration in include/solveit_gpu.h
+ABI_SYMBOLS = (
+    "sv_default_params", "sv_create", "sv_destroy", "sv_set_params", "sv_get_params", "sv_upload",
+    "sv_upload_ref32", "sv_download", "sv_download_ref32", "sv_compute_accel", "sv_add_accel_ref32",
+    "sv_leapfrog", "sv_energy", "sv_compare_accel", "sv_get_stats", "sv_sync", "sv_stream",
+    "sv_launch_count", "sv_last_error", "sv_abi_version",
+)
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("softening2", C.c_double), ("k_const", C.c_double), ("e_over_amu", C.c_double),
+        ("efield", C.c_double * 3), ("method", C.c_int32), ("precision", C.c_int32),
+        ("symmetry", C.c_int32), ("theta", C.c_float), ("leaf_size", C.c_int32),
+        ("fmm_order", C.c_int32), ("fmm_ws", C.c_int32), ("fmm_leaf_target", C.c_int32),
+        ("sym_axes", C.c_int32 * 3), ("sym_levels", C.c_int32), ("domain_size", C.c_double * 3),
+        ("device", C.c_int32), ("reserved", C.c_int32 * 7),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("pair_interactions", C.c_double), ("cell_interactions", C.c_double),
+        ("flops_algorithmic", C.c_double), ("ms_total", C.c_double), ("ms_phase", C.c_double * 8),
+        ("levels", C.c_int32), ("boxes", C.c_int32), ("reserved", C.c_int32 * 6),
+    ]
+
+
+class SolveitError(RuntimeError):
+    pass
+
+
+_lib = None
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+
+
+def load(path: str = LIB_PATH):
+    """Load the native library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise SolveitError(f"{path} not built: run __graft_entry__.build() or solveit-code_gb300/build_ext.py")
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.sv_default_params.argtypes = [C.POINTER(Params)]
+    L.sv_create.argtypes = [C.POINTER(Params), C.POINTER(vp)]
+    L.sv_destroy.argtypes = [vp]
+    L.sv_destroy.restype = None
+    L.sv_set_params.argtypes = [vp, C.POINTER(Params)]
+    L.sv_get_params.argtypes = [vp, C.POINTER(Params)]
+    L.sv_upload.argtypes = [vp, C.c_int64, vp, vp, vp, vp, vp, vp]
+    L.sv_upload_ref32.argtypes = [vp, C.c_int64, vp, vp, vp, vp]
+    L.sv_download.argtypes = [vp, vp, vp, vp]
+    L.sv_download_ref32.argtypes = [vp, vp, vp]
+    L.sv_compute_accel.argtypes = [vp, C.c_int64, C.c_int64, vp]
+    L.sv_add_accel_ref32.argtypes = [vp, vp]
+    L.sv_leapfrog.argtypes = [vp, C.c_int32, C.c_double, C.c_double]
+    L.sv_energy.argtypes = [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.sv_compare_accel.argtypes = [vp, vp, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                   C.POINTER(C.c_int64)]
+    L.sv_get_stats.argtypes = [vp, C.POINTER(Stats)]
+    L.sv_sync.argtypes = [vp]
+    L.sv_stream.argtypes = [vp]
+    L.sv_stream.restype = vp
+    L.sv_launch_count.argtypes = [vp]
+    L.sv_launch_count.restype = C.c_uint64
+    L.sv_last_error.argtypes = [vp]
+    L.sv_last_error.restype = C.c_char_p
+    L.sv_abi_version.restype = C.c_int32
+    for name in ABI_SYMBOLS:
+        if name not in ("sv_destroy", "sv_stream", "sv_launch_count", "sv_last_error", "sv_abi_version"):
+            getattr(L, name).restype = C.c_int
+    _lib = L
+    return L
+
+
+def default_params(**kw) -> Params:
+    p = Params()
+    load().sv_default_params(C.byref(p))
+    for k, v in kw.items():
+        if k in ("efield", "sym_axes", "domain_size"):
+            arr = getattr(p, k)
+            for i, x in enumerate(v):
+                arr[i] = x
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class ForceMethod:
+    """One GPU context: the plume state plus a configured force method."""
+
+    def __init__(self, params: Params | None = None, **kw):
+        self.L = load()
+        self.params = params if params is not None else default_params(**kw)
+        h = C.c_void_p()
+        self._check(self.L.sv_create(C.byref(self.params), C.byref(h)), ctx=None)
+        self.h = h
+        self.n = 0
+
+    def _check(self, rc, ctx="self"):
+        if rc != 0:
+            msg = "" if ctx is None else self.L.sv_last_error(self.h).decode()
+            raise SolveitError(f"{STATUS.get(rc, rc)}: {msg}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.sv_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_params(self, **kw):
+        for k, v in kw.items():
+            if k in ("efield", "sym_axes", "domain_size"):
+                arr = getattr(self.params, k)
+                for i, x in enumerate(v):
+                    arr[i] = x
+            else:
+                setattr(self.params, k, v)
+        self._check(self.L.sv_set_params(self.h, C.byref(self.params)))
+
+    # -- state ---------------------------------------------------------------
+    def upload(self, state):
+        x = np.ascontiguousarray(state["x"], np.float64)
+        v = np.ascontiguousarray(state["v"], np.float64) if state.get("v") is not None else None
+        q = np.ascontiguousarray(state["q"], np.float64)
+        m = np.ascontiguousarray(state["m"], np.float64)
+        st = np.ascontiguousarray(state["status"], np.int32)
+        t = np.ascontiguousarray(state["t_inj"], np.float64) if state.get("t_inj") is not None else None
+        self.n = x.shape[0]
+        self._check(self.L.sv_upload(self.h, self.n, _p(x), _p(v), _p(q), _p(m), _p(st), _p(t)))
+
+    def upload_ref32(self, pos4, vel4, acc4, t_inj=None):
+        p = np.ascontiguousarray(pos4, np.float32)
+        v = np.ascontiguousarray(vel4, np.float32)
+        a = np.ascontiguousarray(acc4, np.float32)
+        t = None if t_inj is None else np.ascontiguousarray(t_inj, np.float32)
+        self.n = p.shape[0]
+        self._check(self.L.sv_upload_ref32(self.h, self.n, _p(p), _p(v), _p(a), _p(t)))
+
+    def download(self):
+        x = np.zeros((self.n, 3), np.float64)
+        v = np.zeros((self.n, 3), np.float64)
+        st = np.zeros(self.n, np.int32)
+        self._check(self.L.sv_download(self.h, _p(x), _p(v), _p(st)))
+        return x, v, st
+
+    # -- force / integration ---------------------------------------------------
+    def accel(self, first=0, last=-1, out=True):
+        a = np.zeros((self.n, 3), np.float64) if out else None
+        self._check(self.L.sv_compute_accel(self.h, first, last, _p(a)))
+        return a
+
+    def add_accel_ref32(self, acc4):
+        self._check(self.L.sv_add_accel_ref32(self.h, _p(acc4)))
+        return acc4
+
+    def leapfrog(self, nsteps, dt, t0=0.0):
+        self._check(self.L.sv_leapfrog(self.h, nsteps, dt, t0))
+
+    def energy(self):
+        ke = C.c_double()
+        pe = C.c_double()
+        self._check(self.L.sv_energy(self.h, C.byref(ke), C.byref(pe)))
+        return ke.value, pe.value
+
+    def compare(self, ref):
+        r = np.ascontiguousarray(ref, np.float64)
+        l2 = C.c_double()
+        mx = C.c_double()
+        am = C.c_int64()
+        self._check(self.L.sv_compare_accel(self.h, _p(r), C.byref(l2), C.byref(mx), C.byref(am)))
+        return l2.value, mx.value, am.value
+
+    def stats(self) -> Stats:
+        s = Stats()
+        self._check(self.L.sv_get_stats(self.h, C.byref(s)))
+        return s
+
+    def sync(self):
+        self._check(self.L.sv_sync(self.h))
+
+    @property
+    def stream(self):
+        return self.L.sv_stream(self.h)
+
+    @property
+    def launches(self):
+        return int(self.L.sv_launch_count(self.h))
