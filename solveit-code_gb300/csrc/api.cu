@@ -574,8 +574,24 @@ sv_status sv_compare_accel(sv_ctx *c, const double *ref3, double *l2, double *ma
     return SV_OK;
 }
 
-sv_status sv_get_stats(const sv_ctx *c, sv_stats *out) {
-    if (!c || !out) return SV_ERR_INVALID;
+sv_status sv_get_stats(const sv_ctx *cc, sv_stats *out) {
+    if (!cc || !out) return SV_ERR_INVALID;
+    sv_ctx *c = const_cast<sv_ctx *>(cc);
+    if (c->have_accel && c->P.method == SV_METHOD_FMM) {
+        double m2l = 0, pairs = 0;
+        SV_TRY(fmm_counts(c, &m2l, &pairs));
+        const int p = c->P.fmm_order;
+        double rot = 0, zt = 0;
+        for (int n = 0; n < p; n++) rot += (n + 1) * (2 * n + 1);
+        for (int j = 0; j < p; j++)
+            for (int k = 0; k <= j; k++) zt += p - k;
+        c->stats.pair_interactions = pairs;
+        c->stats.cell_interactions = m2l;
+        // 20 flop per pair; 8 flop per complex multiply-add of the M2L
+        // rotations and z-translation; P2M + L2P (1 + 3 terms per coefficient)
+        c->stats.flops_algorithmic = 20.0 * pairs + m2l * 8.0 * (2.0 * rot + zt) +
+                                     (double)c->n * 8.0 * (p * (p + 1) / 2) * 4.0;
+    }
     *out = c->stats;
     float ms = 0.f;
     if (c->have_accel && cudaEventQuery(c->ev_end) == cudaSuccess &&

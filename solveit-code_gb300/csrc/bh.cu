@@ -3,5 +3,4 @@
 
 namespace sv {
 sv_status bh_accel(sv_ctx *c) { return set_error(c, SV_ERR_UNSUPPORTED, "Barnes-Hut not built yet"); }
-void tree_free(sv_ctx *) {}
 }  // namespace sv

@@ -1,7 +1,713 @@
-// fmm.cu -- fast multipole method on GB300 (pending).
+// fmm.cu -- rotation-based fast multipole method on GB300.
+//
+// Restates MultipoleMethodForceCalculation::updateAccelerationNoSym
+// (multipole_method_force_calculation.cpp:184-522) and its kernels
+// (fmm_cpukernel.cpp: p2m_kernel :281-384, m2m_kernel :513-619, m2l_kernel
+// :742-909 with rotation() :10-32, l2l_kernel :1050-1126, l2p_kernel
+// :1188-1317, p2p_kernel :194-219) on the level-by-level octree of tree.cu:
+//
+//   P2M   leaf boxes, one warp per box, lanes over particles, then over
+//         coefficients (shared-memory transpose).
+//   M2M   one warp per parent, lanes over the parent's coefficients, children
+//         added in turn (no mutex: one writer per parent).
+//   lists per level, one thread per box: the children of the parent's
+//         neighbours split into near boxes (|offset| <= ws) and the M2L list
+//         (offset class = integer offset target - source).
+//   down  one warp per box and level: L2L from the parent, then every M2L of
+//         the box's list (phase, folded y-rotation, z-translation, inverse
+//         rotation, inverse phase), accumulated in registers, written once.
+//   L2P   leaf boxes, lanes over particles: gradient of the local expansion.
+//   P2P   leaf boxes, lanes over targets, source chunks staged in shared
+//         memory as FP32 offsets from the target box centre (FP64 subtraction
+//         once per staged source); per-source-box FP32 partial sums are added
+//         into FP64 accumulators.
+//
+// Expansions are kept in box units (coordinates divided by the box side h),
+// so the M2L tables depend on the integer offset only; the softened M2L
+// distance rho^2 = |offset|^2 + eps^2/h^2 follows fmm_cpukernel.cpp:832.
+// ws (well-separation) 1 is the reference's interaction list
+// (multipole_method_force_calculation.cpp:2021-2114); ws 2 widens the near
+// field to 5x5x5 boxes, which is what brings p = 8 under 1e-5 force error.
+#include <cfloat>
+
+#include <string>
+
+#include "fmm_tables.h"
 #include "sv_internal.cuh"
+#include "tree.cuh"
 
 namespace sv {
-sv_status fmm_accel(sv_ctx *c) { return set_error(c, SV_ERR_UNSUPPORTED, "FMM not built yet"); }
-void fmm_free(sv_ctx *) {}
+
+struct Fmm {
+    int p = 0, ws = 0;
+    FmmTables H;
+    int *cls_theta = nullptr;
+    float2 *cls_phase = nullptr;
+    float *cls_rho2 = nullptr;
+    float *dmat = nullptr;
+    float *zc = nullptr;
+    float *nrm = nullptr;
+    float2 *oct = nullptr;
+    void *arena = nullptr;
+    size_t arena_bytes = 0;
+    unsigned long long *d_counts = nullptr;  // [0] M2L translations, [1] P2P pairs
+    unsigned long long *h_counts = nullptr;
+};
+
+namespace {
+
+constexpr int kWarps = 4;  // warps per CTA in the per-box kernels
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+
+__host__ __device__ constexpr int ncoef(int P) { return P * (P + 1) / 2; }
+__device__ __forceinline__ int cidx(int n, int m) { return n * (n + 1) / 2 + m; }
+__device__ __forceinline__ void cnm(int c, int &n, int &m) {
+    n = 0;
+    while ((n + 1) * (n + 2) / 2 <= c) n++;
+    m = c - n * (n + 1) / 2;
+}
+
+// Regular solid harmonics R_n^m(x), m >= 0, n < P (Cartesian recurrences):
+// R_m^m = (x+iy)/(2m) R_{m-1}^{m-1}; R_{m+1}^m = z R_m^m;
+// R_n^m = ((2n-1) z R_{n-1}^m - r^2 R_{n-2}^m) / ((n+m)(n-m)).
+template <int P>
+__device__ __forceinline__ void solid_harmonics(float x, float y, float z, float2 *R) {
+    const float r2 = x * x + y * y + z * z;
+    R[0] = make_float2(1.f, 0.f);
+#pragma unroll
+    for (int m = 0; m < P; m++) {
+        if (m > 0) {
+            const float2 prev = R[cidx(m - 1, m - 1)];
+            const float s = 1.f / (2.f * m);
+            R[cidx(m, m)] = make_float2((x * prev.x - y * prev.y) * s, (x * prev.y + y * prev.x) * s);
+        }
+        if (m + 1 < P) R[cidx(m + 1, m)] = cscale(R[cidx(m, m)], z);
+#pragma unroll
+        for (int n = m + 2; n < P; n++) {
+            const float a = (2.f * n - 1.f) * z, d = 1.f / ((n + m) * (n - m));
+            const float2 r1 = R[cidx(n - 1, m)], r0 = R[cidx(n - 2, m)];
+            R[cidx(n, m)] = make_float2((a * r1.x - r2 * r0.x) * d, (a * r1.y - r2 * r0.y) * d);
+        }
+    }
+}
+
+// R_n^m for any order from the m >= 0 half: R_n^-m = (-1)^m conj(R_n^m)
+__device__ __forceinline__ float2 half_get(const float2 *C, int n, int m) {
+    if (m >= 0) return C[cidx(n, m)];
+    const float2 v = C[cidx(n, -m)];
+    return (m & 1) ? make_float2(-v.x, v.y) : make_float2(v.x, -v.y);
+}
+
+// ---------------------------------------------------------------- lists --
+template <int WS>
+__global__ void build_lists_kernel(int nbox, const int *__restrict__ parent, const int4 *__restrict__ coord,
+                                   const int *__restrict__ pnbr, const int *__restrict__ pchild0,
+                                   int *__restrict__ nbr, int2 *__restrict__ m2l, int *__restrict__ m2l_cnt,
+                                   int cap, unsigned long long *__restrict__ counts) {
+    constexpr int NS1 = 2 * WS + 1, NS = NS1 * NS1 * NS1, R = 2 * WS + 1, SIDE = 2 * R + 1;
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    int cnt = 0;
+    if (b < nbox) {
+        const int4 cb = coord[b];
+        const int par = parent[b];
+        for (int s = 0; s < NS; s++) {
+            const int Q = pnbr[par * NS + s];
+            if (Q < 0) continue;
+            const int c1 = pchild0[Q + 1];
+            for (int ch = pchild0[Q]; ch < c1; ch++) {
+                const int4 cc = coord[ch];
+                const int ox = cb.x - cc.x, oy = cb.y - cc.y, oz = cb.z - cc.z;
+                const int am = max(abs(ox), max(abs(oy), abs(oz)));
+                if (am <= WS) {
+                    nbr[b * NS + ((ox + WS) * NS1 + (oy + WS)) * NS1 + (oz + WS)] = ch;
+                } else if (cnt < cap) {
+                    m2l[(size_t)b * cap + cnt] = make_int2(ch, ((ox + R) * SIDE + (oy + R)) * SIDE + (oz + R));
+                    cnt++;
+                }
+            }
+        }
+        m2l_cnt[b] = cnt;
+    }
+    // warp-aggregated statistics
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(&counts[0], (unsigned long long)cnt);
+}
+
+__global__ void root_nbr_kernel(int *nbr, int ns) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) nbr[ns / 2] = 0;
+}
+
+// ------------------------------------------------------------------ P2M --
+template <int P>
+constexpr int p2m_warps() { return P >= 9 ? 2 : 4; }
+
+template <int P>
+__global__ void __launch_bounds__(p2m_warps<P>() * 32)
+p2m_kernel(int nbox, const int *__restrict__ start, const int4 *__restrict__ coord,
+           const double *__restrict__ xs, const double *__restrict__ ys, const double *__restrict__ zs,
+           const float *__restrict__ qs, const double *__restrict__ root, int level,
+           const float *__restrict__ nrm, float2 *__restrict__ M) {
+    constexpr int NC = ncoef(P), WP = p2m_warps<P>();
+    __shared__ float2 buf[WP][32][NC + 1];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int b = blockIdx.x * WP + wid;
+    if (b >= nbox) return;
+    const double h = root[3] / (double)(1 << level);
+    const int4 cb = coord[b];
+    const double cx = root[0] + (cb.x + 0.5) * h, cy = root[1] + (cb.y + 0.5) * h, cz = root[2] + (cb.z + 0.5) * h;
+    const double ih = 1.0 / h;
+    float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
+    const int s0 = start[b], s1 = start[b + 1];
+    for (int base = s0; base < s1; base += 32) {
+        const int i = base + lane;
+        float2 R[NC];
+        if (i < s1) {
+            solid_harmonics<P>((float)((xs[i] - cx) * ih), (float)((ys[i] - cy) * ih), (float)((zs[i] - cz) * ih), R);
+            const float q = qs[i];
+#pragma unroll
+            for (int c = 0; c < NC; c++) buf[wid][lane][c] = make_float2(q * R[c].x, -q * R[c].y);
+        } else {
+#pragma unroll
+            for (int c = 0; c < NC; c++) buf[wid][lane][c] = make_float2(0.f, 0.f);
+        }
+        __syncwarp();
+        const int rows = min(32, s1 - base);
+        for (int r = 0; r < rows && lane < NC; r++) {
+            a0 = cadd(a0, buf[wid][r][lane]);
+            if (lane + 32 < NC) a1 = cadd(a1, buf[wid][r][lane + 32]);
+        }
+        __syncwarp();
+    }
+    if (lane < NC) {
+        int n, m;
+        cnm(lane, n, m);
+        M[(size_t)b * NC + lane] = cscale(a0, nrm[n * P + m]);
+        if (lane + 32 < NC) {
+            cnm(lane + 32, n, m);
+            M[(size_t)b * NC + lane + 32] = cscale(a1, nrm[n * P + m]);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ M2M --
+template <int P>
+__global__ void __launch_bounds__(kWarps * 32)
+m2m_kernel(int nbox, const int *__restrict__ child0, const int4 *__restrict__ ccoord,
+           const float2 *__restrict__ Mc, float2 *__restrict__ Mp, const float *__restrict__ nrm,
+           const float2 *__restrict__ oct) {
+    constexpr int NC = ncoef(P), W = 2 * P - 1;
+    __shared__ float2 mu[kWarps][NC];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int b = blockIdx.x * kWarps + wid;
+    if (b >= nbox) return;
+    float2 acc[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+    const int ch1 = child0[b + 1];
+    for (int ch = child0[b]; ch < ch1; ch++) {
+        const int4 cc = ccoord[ch];
+        const int oc = (cc.x & 1) | ((cc.y & 1) << 1) | ((cc.z & 1) << 2);
+        const float2 *Rd = oct + (size_t)oc * P * W;
+        for (int c = lane; c < NC; c += 32) {
+            int n, m;
+            cnm(c, n, m);
+            mu[wid][c] = cscale(Mc[(size_t)ch * NC + c], 1.f / nrm[n * P + m]);
+        }
+        __syncwarp();
+#pragma unroll
+        for (int t = 0; t < 2; t++) {
+            const int c = lane + 32 * t;
+            if (c >= NC) break;
+            int n, m;
+            cnm(c, n, m);
+            float2 s = make_float2(0.f, 0.f);
+            for (int k = 0; k <= n; k++) {
+                const int nk = n - k;
+                for (int l = -k; l <= k; l++) {
+                    const int ml = m - l;
+                    if (ml > nk || ml < -nk) continue;
+                    s = cadd(s, cmul(half_get(mu[wid], k, l), cconj(Rd[nk * W + ml + P - 1])));
+                }
+            }
+            acc[t] = cadd(acc[t], s);
+        }
+        __syncwarp();
+    }
+#pragma unroll
+    for (int t = 0; t < 2; t++) {
+        const int c = lane + 32 * t;
+        if (c >= NC) break;
+        int n, m;
+        cnm(c, n, m);
+        // back to G-R normalisation, from child to parent box units (x 2^-n)
+        Mp[(size_t)b * NC + c] = cscale(acc[t], nrm[n * P + m] * ldexpf(1.f, -n));
+    }
+}
+
+// ----------------------------------------------------------- downward --
+struct DownArgs {
+    int nbox, level, cap, esz, osz, dsz, has_parent;
+    const int *parent;
+    const int4 *coord;
+    const float2 *Lp;      // parent locals (level-1) or null
+    const float2 *Ml;      // multipoles of this level
+    const int2 *m2l;
+    const int *m2l_cnt;
+    const int *cls_theta;
+    const float2 *cls_phase;
+    const float *cls_rho2;
+    const float *dmat;
+    const float *zc;
+    const float *nrm;
+    const float2 *oct;
+    const double *root;
+    double eps2;
+    float2 *Lout;
+};
+
+template <int P>
+__global__ void __launch_bounds__(kWarps * 32) down_kernel(DownArgs a) {
+    constexpr int NC = ncoef(P), W = 2 * P - 1;
+    __shared__ float2 A[kWarps][NC], B[kWarps][NC];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int b = blockIdx.x * kWarps + wid;
+    if (b >= a.nbox) return;
+    // lane slots: coefficient lane and lane + 32, valid while < NC
+    int cn[2], cm[2];
+    cnm(min(lane, NC - 1), cn[0], cm[0]);
+    cnm(min(lane + 32, NC - 1), cn[1], cm[1]);
+    const bool has[2] = {lane < NC, lane + 32 < NC};
+    float2 acc[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+    // ---- L2L from the parent (parent box units -> child box units)
+    if (a.has_parent) {
+        const int par = a.parent[b];
+        const int4 cb = a.coord[b];
+        const int oc = (cb.x & 1) | ((cb.y & 1) << 1) | ((cb.z & 1) << 2);
+        const float2 *Rd = a.oct + (size_t)oc * P * W;
+        for (int c = lane; c < NC; c += 32) {
+            int n, m;
+            cnm(c, n, m);
+            A[wid][c] = cscale(a.Lp[(size_t)par * NC + c], a.nrm[n * P + m] * ldexpf(1.f, -(n + 1)));
+        }
+        __syncwarp();
+#pragma unroll
+        for (int t = 0; t < 2; t++) {
+            if (!has[t]) break;
+            const int k = cn[t], l = cm[t];
+            float2 s = make_float2(0.f, 0.f);
+            for (int n = k; n < P; n++) {
+                const int nk = n - k;
+                for (int m = -n; m <= n; m++) {
+                    const int ml = m - l;
+                    if (ml > nk || ml < -nk) continue;
+                    s = cadd(s, cmul(half_get(A[wid], n, m), Rd[nk * W + ml + P - 1]));
+                }
+            }
+            acc[t] = cscale(s, 1.f / a.nrm[k * P + l]);
+        }
+        __syncwarp();
+    }
+    // ---- M2L list
+    const double h = a.root[3] / (double)(1 << a.level);
+    const float eh2 = (float)(a.eps2 / (h * h));
+    const int cnt = a.m2l_cnt[b];
+    const int2 *lst = a.m2l + (size_t)b * a.cap;
+    for (int e = 0; e < cnt; e++) {
+        const int2 ent = lst[e];
+        const int src = ent.x, cls = ent.y;
+        const float2 *ph = a.cls_phase + (size_t)cls * P;
+        const float *D = a.dmat + (size_t)a.cls_theta[cls] * a.dsz;
+        const float inv_rho = rsqrtf(a.cls_rho2[cls] + eh2);
+        // phase e^{i m phi}
+#pragma unroll
+        for (int t = 0; t < 2; t++) {
+            if (!has[t]) break;
+            const int c = lane + 32 * t;
+            A[wid][c] = cmul(a.Ml[(size_t)src * NC + c], ph[cm[t]]);
+        }
+        __syncwarp();
+        // forward y-rotation (folded real matrices)
+#pragma unroll
+        for (int t = 0; t < 2; t++) {
+            if (!has[t]) break;
+            const int n = cn[t], mp = cm[t];
+            const float *E = D + (n * (n + 1) * (2 * n + 1)) / 6 + mp * (n + 1);
+            float re = 0.f, im = 0.f;
+            const float2 *An = &A[wid][cidx(n, 0)];
+            for (int m = 0; m <= n; m++) re = fmaf(E[m], An[m].x, re);
+            if (mp > 0) {
+                const float *O = D + a.esz + ((n - 1) * n * (2 * n - 1)) / 6 + (mp - 1) * n;
+                for (int m = 1; m <= n; m++) im = fmaf(O[m - 1], An[m].y, im);
+            }
+            B[wid][lane + 32 * t] = make_float2(re, im);
+        }
+        __syncwarp();
+        // translation along z: L'_j^k = sum_n C[k][j][n] rho^-(j+n+1) M'_n^k
+#pragma unroll
+        for (int t = 0; t < 2; t++) {
+            if (!has[t]) break;
+            const int j = cn[t], k = cm[t];
+            const float *Z = a.zc + ((size_t)k * P + j) * P;
+            float ip = inv_rho;
+            for (int q = 0; q < j + k; q++) ip *= inv_rho;  // rho^-(j+k+1)
+            float re = 0.f, im = 0.f;
+            for (int n = k; n < P; n++) {
+                const float2 v = B[wid][cidx(n, k)];
+                const float f = Z[n] * ip;
+                re = fmaf(f, v.x, re);
+                im = fmaf(f, v.y, im);
+                ip *= inv_rho;
+            }
+            A[wid][lane + 32 * t] = make_float2(re, im);
+        }
+        __syncwarp();
+        // backward y-rotation and phase e^{-i k phi}
+#pragma unroll
+        for (int t = 0; t < 2; t++) {
+            if (!has[t]) break;
+            const int n = cn[t], mp = cm[t];
+            const float *E = D + a.esz + a.osz + (n * (n + 1) * (2 * n + 1)) / 6 + mp * (n + 1);
+            float re = 0.f, im = 0.f;
+            const float2 *An = &A[wid][cidx(n, 0)];
+            for (int m = 0; m <= n; m++) re = fmaf(E[m], An[m].x, re);
+            if (mp > 0) {
+                const float *O = D + 2 * a.esz + a.osz + ((n - 1) * n * (2 * n - 1)) / 6 + (mp - 1) * n;
+                for (int m = 1; m <= n; m++) im = fmaf(O[m - 1], An[m].y, im);
+            }
+            acc[t] = cadd(acc[t], cmul(make_float2(re, im), cconj(ph[mp])));
+        }
+        __syncwarp();
+    }
+    if (has[0]) a.Lout[(size_t)b * NC + lane] = acc[0];
+    if (has[1]) a.Lout[(size_t)b * NC + lane + 32] = acc[1];
+}
+
+// ------------------------------------------------------------------ L2P --
+template <int P>
+__global__ void __launch_bounds__(kWarps * 32)
+l2p_kernel(int nbox, const int *__restrict__ start, const int4 *__restrict__ coord,
+           const double *__restrict__ xs, const double *__restrict__ ys, const double *__restrict__ zs,
+           const double *__restrict__ qm, const double *__restrict__ root, int level,
+           const float *__restrict__ nrm, const float2 *__restrict__ Lc, double *__restrict__ ax,
+           double *__restrict__ ay, double *__restrict__ az) {
+    constexpr int NC = ncoef(P);
+    __shared__ float2 lam[kWarps][NC];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int b = blockIdx.x * kWarps + wid;
+    if (b >= nbox) return;
+    for (int c = lane; c < NC; c += 32) {
+        int n, m;
+        cnm(c, n, m);
+        lam[wid][c] = cscale(Lc[(size_t)b * NC + c], nrm[n * P + m]);
+    }
+    __syncwarp();
+    const double h = root[3] / (double)(1 << level);
+    const int4 cb = coord[b];
+    const double cx = root[0] + (cb.x + 0.5) * h, cy = root[1] + (cb.y + 0.5) * h, cz = root[2] + (cb.z + 0.5) * h;
+    const double ih = 1.0 / h;
+    const int s1 = start[b + 1];
+    for (int i = start[b] + lane; i < s1; i += 32) {
+        float2 R[ncoef(P - 1) > 0 ? ncoef(P - 1) : 1];
+        solid_harmonics<P - 1>((float)((xs[i] - cx) * ih), (float)((ys[i] - cy) * ih), (float)((zs[i] - cz) * ih), R);
+        float gz = 0.f;
+        float2 gm = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int n = 1; n < P; n++) {
+            const float2 *ln = &lam[wid][cidx(n, 0)];
+            gz = fmaf(ln[0].x, R[cidx(n - 1, 0)].x, gz);
+#pragma unroll
+            for (int m = 1; m < n; m++) {
+                const float2 v = cmul(ln[m], R[cidx(n - 1, m)]);
+                gz = fmaf(2.f, v.x, gz);
+            }
+#pragma unroll
+            for (int m = 1; m <= n; m++) gm = cadd(gm, cmul(ln[m], R[cidx(n - 1, m - 1)]));
+#pragma unroll
+            for (int t = 0; t + 1 < n; t++) gm = cadd(gm, cscale(cconj(cmul(ln[t], R[cidx(n - 1, t + 1)])), -1.f));
+        }
+        // a = -grad(phi) * K q / m, grad in box units / h^2
+        const double f = -qm[i] * ih * ih;
+        ax[i] = f * (double)gm.x;
+        ay[i] = f * (double)(-gm.y);
+        az[i] = f * (double)gz;
+    }
+}
+
+// ------------------------------------------------------------------ P2P --
+template <int WS>
+__global__ void __launch_bounds__(kWarps * 32)
+p2p_kernel(int nbox, const int *__restrict__ start, const int4 *__restrict__ coord, const int *__restrict__ nbr,
+           const double *__restrict__ xs, const double *__restrict__ ys, const double *__restrict__ zs,
+           const float *__restrict__ qs, const double *__restrict__ qm, const double *__restrict__ root,
+           int level, float eps2, double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az,
+           unsigned long long *__restrict__ counts) {
+    constexpr int NS1 = 2 * WS + 1, NS = NS1 * NS1 * NS1;
+    __shared__ float4 src[kWarps][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int b = blockIdx.x * kWarps + wid;
+    if (b >= nbox) return;
+    const double h = root[3] / (double)(1 << level);
+    const int4 cb = coord[b];
+    const double cx = root[0] + (cb.x + 0.5) * h, cy = root[1] + (cb.y + 0.5) * h, cz = root[2] + (cb.z + 0.5) * h;
+    const int t0 = start[b], t1 = start[b + 1];
+    unsigned long long pairs = 0;
+    for (int tb = t0; tb < t1; tb += 32) {
+        const int i = tb + lane;
+        const bool valid = i < t1;
+        const int ii = valid ? i : t0;
+        const float tx = (float)(xs[ii] - cx), ty = (float)(ys[ii] - cy), tz = (float)(zs[ii] - cz);
+        double sx = 0.0, sy = 0.0, sz = 0.0;
+        for (int s = 0; s < NS; s++) {
+            const int Q = nbr[b * NS + s];
+            if (Q < 0) continue;
+            const int j0 = start[Q], j1 = start[Q + 1];
+            if (lane == 0) pairs += (unsigned long long)(j1 - j0) * (unsigned long long)min(32, t1 - tb);
+            float fx = 0.f, fy = 0.f, fz = 0.f;
+            for (int jb = j0; jb < j1; jb += 32) {
+                const int j = jb + lane;
+                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (j < j1) v = make_float4((float)(xs[j] - cx), (float)(ys[j] - cy), (float)(zs[j] - cz), qs[j]);
+                src[wid][lane] = v;
+                __syncwarp();
+                const int cnt = min(32, j1 - jb);
+                for (int k = 0; k < cnt; k++) {
+                    const float4 u = src[wid][k];
+                    const float dx = tx - u.x, dy = ty - u.y, dz = tz - u.z;
+                    float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+                    r2 = fmaxf(r2, FLT_MIN);
+                    const float inv = rsqrtf(r2);
+                    const float w = u.w * inv * inv * inv;
+                    fx = fmaf(dx, w, fx);
+                    fy = fmaf(dy, w, fy);
+                    fz = fmaf(dz, w, fz);
+                }
+                __syncwarp();
+            }
+            sx += fx;
+            sy += fy;
+            sz += fz;
+        }
+        if (valid) {
+            const double c = qm[i];
+            ax[i] += sx * c;
+            ay[i] += sy * c;
+            az[i] += sz * c;
+        }
+    }
+    if (lane == 0 && pairs) atomicAdd(&counts[1], pairs);
+}
+
+template <int P>
+sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
+    constexpr int NC = ncoef(P);
+    const int L = T.deepest;
+    const int ws = F.ws;
+    const int ns1 = 2 * ws + 1, ns = ns1 * ns1 * ns1;
+    const int cap = ns * 8 - ns;
+    Sorted &S = c->S;
+    // arena: per level M, Loc, nbr, m2l, cnt
+    auto rounded = [](size_t sz) { return (sz + 255) & ~(size_t)255; };
+    size_t bytes = 0;
+    for (int l = 0; l <= L; l++) {
+        const size_t nb = T.lv[l].nbox;
+        bytes += 2 * rounded(nb * NC * sizeof(float2)) + rounded(nb * ns * sizeof(int)) +
+                 rounded(nb * cap * sizeof(int2)) + rounded(nb * sizeof(int));
+    }
+    if (F.arena_bytes < bytes) {
+        cudaFree(F.arena);
+        F.arena = nullptr;
+        F.arena_bytes = 0;
+        const size_t want = bytes + bytes / 4;
+        SV_CK(c, cudaMalloc(&F.arena, want));
+        F.arena_bytes = want;
+    }
+    char *p = (char *)F.arena;
+    auto carve = [&](size_t sz) {
+        char *r = p;
+        p += (sz + 255) & ~(size_t)255;
+        return (void *)r;
+    };
+    float2 *Mv[kMortonBits + 1], *Lv[kMortonBits + 1];
+    int *nbr[kMortonBits + 1], *cnt[kMortonBits + 1];
+    int2 *lst[kMortonBits + 1];
+    for (int l = 0; l <= L; l++) {
+        const size_t nb = T.lv[l].nbox;
+        Mv[l] = (float2 *)carve(nb * NC * sizeof(float2));
+        Lv[l] = (float2 *)carve(nb * NC * sizeof(float2));
+        nbr[l] = (int *)carve(nb * ns * sizeof(int));
+        lst[l] = (int2 *)carve(nb * cap * sizeof(int2));
+        cnt[l] = (int *)carve(nb * sizeof(int));
+        SV_CK(c, cudaMemsetAsync(nbr[l], 0xff, nb * ns * sizeof(int), c->stream));
+    }
+    SV_CK(c, cudaMemsetAsync(F.d_counts, 0, 2 * sizeof(unsigned long long), c->stream));
+    root_nbr_kernel<<<1, 32, 0, c->stream>>>(nbr[0], ns);
+    SV_LAUNCHED(c);
+    for (int l = 1; l <= L; l++) {
+        const Level &V = T.lv[l];
+        const Level &U = T.lv[l - 1];
+        if (ws == 1)
+            build_lists_kernel<1><<<div_up(V.nbox, 128), 128, 0, c->stream>>>(
+                V.nbox, V.parent, V.coord, nbr[l - 1], U.child0, nbr[l], lst[l], cnt[l], cap, F.d_counts);
+        else
+            build_lists_kernel<2><<<div_up(V.nbox, 128), 128, 0, c->stream>>>(
+                V.nbox, V.parent, V.coord, nbr[l - 1], U.child0, nbr[l], lst[l], cnt[l], cap, F.d_counts);
+        SV_LAUNCHED(c);
+    }
+    // upward pass
+    {
+        const Level &V = T.lv[L];
+        p2m_kernel<P><<<div_up(V.nbox, p2m_warps<P>()), p2m_warps<P>() * 32, 0, c->stream>>>(
+            V.nbox, V.start, V.coord, S.x, S.y, S.z, S.q, S.root, L, F.nrm, Mv[L]);
+        SV_LAUNCHED(c);
+    }
+    for (int l = L - 1; l >= 2; l--) {
+        const Level &V = T.lv[l];
+        m2m_kernel<P><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(V.nbox, V.child0, T.lv[l + 1].coord,
+                                                                              Mv[l + 1], Mv[l], F.nrm, F.oct);
+        SV_LAUNCHED(c);
+    }
+    // downward pass: L2L + M2L per level
+    for (int l = 2; l <= L; l++) {
+        const Level &V = T.lv[l];
+        DownArgs a;
+        a.nbox = V.nbox;
+        a.level = l;
+        a.cap = cap;
+        a.esz = F.H.esz;
+        a.osz = F.H.osz;
+        a.dsz = F.H.dsz;
+        a.has_parent = l > 2;
+        a.parent = V.parent;
+        a.coord = V.coord;
+        a.Lp = l > 2 ? Lv[l - 1] : nullptr;
+        a.Ml = Mv[l];
+        a.m2l = lst[l];
+        a.m2l_cnt = cnt[l];
+        a.cls_theta = F.cls_theta;
+        a.cls_phase = F.cls_phase;
+        a.cls_rho2 = F.cls_rho2;
+        a.dmat = F.dmat;
+        a.zc = F.zc;
+        a.nrm = F.nrm;
+        a.oct = F.oct;
+        a.root = S.root;
+        a.eps2 = c->P.softening2;
+        a.Lout = Lv[l];
+        down_kernel<P><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(a);
+        SV_LAUNCHED(c);
+    }
+    // far field then near field, written in sorted order
+    {
+        const Level &V = T.lv[L];
+        if (L >= 2) {
+            l2p_kernel<P><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
+                V.nbox, V.start, V.coord, S.x, S.y, S.z, S.qm, S.root, L, F.nrm, Lv[L], S.ax, S.ay, S.az);
+            SV_LAUNCHED(c);
+        } else {
+            SV_CK(c, cudaMemsetAsync(S.ax, 0, sizeof(double) * c->n, c->stream));
+            SV_CK(c, cudaMemsetAsync(S.ay, 0, sizeof(double) * c->n, c->stream));
+            SV_CK(c, cudaMemsetAsync(S.az, 0, sizeof(double) * c->n, c->stream));
+        }
+        if (ws == 1)
+            p2p_kernel<1><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
+                V.nbox, V.start, V.coord, nbr[L], S.x, S.y, S.z, S.q, S.qm, S.root, L, (float)c->P.softening2,
+                S.ax, S.ay, S.az, F.d_counts);
+        else
+            p2p_kernel<2><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
+                V.nbox, V.start, V.coord, nbr[L], S.x, S.y, S.z, S.q, S.qm, S.root, L, (float)c->P.softening2,
+                S.ax, S.ay, S.az, F.d_counts);
+        SV_LAUNCHED(c);
+    }
+    SV_CK(c, cudaMemcpyAsync(F.h_counts, F.d_counts, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                             c->stream));
+    c->stats.levels = L;
+    c->stats.boxes = T.lv[L].nbox;
+    return SV_OK;
+}
+
+sv_status ensure_tables(sv_ctx *c, Fmm &F, int p, int ws) {
+    if (F.p == p && F.ws == ws && F.dmat) return SV_OK;
+    std::string err;
+    if (!build_fmm_tables(p, ws, F.H, err)) return set_error(c, SV_ERR_INVALID, "FMM tables: %s", err.c_str());
+    cudaFree(F.cls_theta); cudaFree(F.cls_phase); cudaFree(F.cls_rho2); cudaFree(F.dmat);
+    cudaFree(F.zc); cudaFree(F.nrm); cudaFree(F.oct);
+    const FmmTables &H = F.H;
+    SV_CK(c, cudaMalloc(&F.cls_theta, sizeof(int) * H.cls_theta.size()));
+    SV_CK(c, cudaMalloc(&F.cls_phase, sizeof(float) * H.cls_phase.size()));
+    SV_CK(c, cudaMalloc(&F.cls_rho2, sizeof(float) * H.cls_rho2.size()));
+    SV_CK(c, cudaMalloc(&F.dmat, sizeof(float) * H.dmat.size()));
+    SV_CK(c, cudaMalloc(&F.zc, sizeof(float) * H.zc.size()));
+    SV_CK(c, cudaMalloc(&F.nrm, sizeof(float) * H.nrm.size()));
+    SV_CK(c, cudaMalloc(&F.oct, sizeof(float) * H.oct.size()));
+    SV_CK(c, cudaMemcpy(F.cls_theta, H.cls_theta.data(), sizeof(int) * H.cls_theta.size(), cudaMemcpyHostToDevice));
+    SV_CK(c, cudaMemcpy(F.cls_phase, H.cls_phase.data(), sizeof(float) * H.cls_phase.size(), cudaMemcpyHostToDevice));
+    SV_CK(c, cudaMemcpy(F.cls_rho2, H.cls_rho2.data(), sizeof(float) * H.cls_rho2.size(), cudaMemcpyHostToDevice));
+    SV_CK(c, cudaMemcpy(F.dmat, H.dmat.data(), sizeof(float) * H.dmat.size(), cudaMemcpyHostToDevice));
+    SV_CK(c, cudaMemcpy(F.zc, H.zc.data(), sizeof(float) * H.zc.size(), cudaMemcpyHostToDevice));
+    SV_CK(c, cudaMemcpy(F.nrm, H.nrm.data(), sizeof(float) * H.nrm.size(), cudaMemcpyHostToDevice));
+    SV_CK(c, cudaMemcpy(F.oct, H.oct.data(), sizeof(float) * H.oct.size(), cudaMemcpyHostToDevice));
+    F.p = p;
+    F.ws = ws;
+    return SV_OK;
+}
+
+}  // namespace
+
+void fmm_free(sv_ctx *c) {
+    if (!c->fmm) return;
+    Fmm &F = *c->fmm;
+    cudaFree(F.cls_theta); cudaFree(F.cls_phase); cudaFree(F.cls_rho2); cudaFree(F.dmat);
+    cudaFree(F.zc); cudaFree(F.nrm); cudaFree(F.oct); cudaFree(F.arena); cudaFree(F.d_counts);
+    cudaFreeHost(F.h_counts);
+    delete c->fmm;
+    c->fmm = nullptr;
+}
+
+sv_status fmm_accel(sv_ctx *c) {
+    if (c->P.symmetry != SV_SYM_NONE)
+        return set_error(c, SV_ERR_UNSUPPORTED, "FMM with symmetry images is not built yet");
+    if (c->P.precision != SV_PREC_MIXED)
+        return set_error(c, SV_ERR_UNSUPPORTED, "FMM runs in mixed precision only");
+    const int p = c->P.fmm_order;
+    if (p != 4 && p != 6 && p != 8 && p != 10)
+        return set_error(c, SV_ERR_UNSUPPORTED, "FMM order %d not instantiated (4, 6, 8, 10)", p);
+    if (!c->fmm) {
+        c->fmm = new Fmm();
+        SV_CK(c, cudaMalloc(&c->fmm->d_counts, 2 * sizeof(unsigned long long)));
+        SV_CK(c, cudaMallocHost(&c->fmm->h_counts, 2 * sizeof(unsigned long long)));
+    }
+    Fmm &F = *c->fmm;
+    SV_TRY(ensure_tables(c, F, p, c->P.fmm_ws));
+    Tree *T = nullptr;
+    SV_TRY(tree_build(c, kDepthMeanOccupancy, c->P.fmm_leaf_target, &T));
+    if (T->n_act == 0) {
+        SV_CK(c, cudaMemsetAsync(c->S.ax, 0, sizeof(double) * c->n, c->stream));
+        SV_CK(c, cudaMemsetAsync(c->S.ay, 0, sizeof(double) * c->n, c->stream));
+        SV_CK(c, cudaMemsetAsync(c->S.az, 0, sizeof(double) * c->n, c->stream));
+        return SV_OK;
+    }
+    switch (p) {
+    case 4: SV_TRY(run_fmm<4>(c, F, *T)); break;
+    case 6: SV_TRY(run_fmm<6>(c, F, *T)); break;
+    case 8: SV_TRY(run_fmm<8>(c, F, *T)); break;
+    default: SV_TRY(run_fmm<10>(c, F, *T)); break;
+    }
+    return SV_OK;
+}
+
+sv_status fmm_counts(sv_ctx *c, double *m2l, double *pairs) {
+    if (!c->fmm) {
+        *m2l = *pairs = 0;
+        return SV_OK;
+    }
+    SV_CK(c, cudaStreamSynchronize(c->stream));
+    *m2l = (double)c->fmm->h_counts[0];
+    *pairs = (double)c->fmm->h_counts[1];
+    return SV_OK;
+}
+
 }  // namespace sv

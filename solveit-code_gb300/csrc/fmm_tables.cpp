@@ -1,0 +1,235 @@
+// fmm_tables.cpp -- host precompute of the FMM translation tables.
+//
+// Plays the role of MultipoleMethodConstants::precalc
+// (multipole_method_constants.cpp:40-226: factorials, Anm, Ynm at theta = 0,
+// Wigner rotation matrices Dnm for the primitive directions).  Conventions:
+//   Y_n^m(t, f) = sqrt((n-|m|)!/(n+|m|)!) P_n^|m|(cos t) e^{imf}, P without
+//   the Condon-Shortley phase;  multipole M_n^m = sum q r^n Y_n^-m,
+//   potential sum M_n^m Y_n^m / r^{n+1};  local potential sum L_j^k Y_j^k r^j.
+// An M2L from a source box to a target box at offset d (target - source, in
+// box units) is done as: phase e^{imf}, rotation about y by -theta (d -> +z),
+// translation along z, rotation about y by +theta, phase e^{-imf}.  The two
+// y-rotation matrices of every polar angle are computed by exact quadrature on
+// the sphere (Gauss-Legendre x trapezoid), so no sign convention of a Wigner
+// formula has to be matched.
+#include "fmm_tables.h"
+
+#include <cmath>
+#include <complex>
+#include <map>
+#include <vector>
+
+namespace sv {
+namespace {
+
+using cd = std::complex<double>;
+
+double fact(int n) {
+    double f = 1.0;
+    for (int k = 2; k <= n; k++) f *= k;
+    return f;
+}
+
+// associated Legendre P_n^m(x), m >= 0, no Condon-Shortley phase, n < p
+void legendre(int p, double x, std::vector<double> &P) {
+    P.assign(p * p, 0.0);
+    const double s = std::sqrt(std::max(0.0, (1 - x) * (1 + x)));
+    double pmm = 1.0;
+    for (int m = 0; m < p; m++) {
+        if (m > 0) pmm *= (2 * m - 1) * s;
+        P[m * p + m] = pmm;
+        if (m + 1 < p) P[(m + 1) * p + m] = x * (2 * m + 1) * pmm;
+        for (int n = m + 2; n < p; n++)
+            P[n * p + m] = ((2 * n - 1) * x * P[(n - 1) * p + m] - (n + m - 1) * P[(n - 2) * p + m]) / (n - m);
+    }
+}
+
+cd ynm(int n, int m, const std::vector<double> &P, int p, double phi) {
+    const int am = std::abs(m);
+    const double nrm = std::sqrt(fact(n - am) / fact(n + am));
+    return nrm * P[n * p + am] * std::polar(1.0, m * phi);
+}
+
+void gauss_legendre(int n, std::vector<double> &x, std::vector<double> &w) {
+    x.resize(n);
+    w.resize(n);
+    for (int i = 0; i < n; i++) {
+        double z = std::cos(M_PI * (i + 0.75) / (n + 0.5));
+        for (int it = 0; it < 100; it++) {
+            double p1 = 1, p2 = 0;
+            for (int k = 1; k <= n; k++) {
+                double p3 = p2;
+                p2 = p1;
+                p1 = ((2 * k - 1) * z * p2 - (k - 1) * p3) / k;
+            }
+            double pp = n * (z * p1 - p2) / (z * z - 1);
+            double dz = p1 / pp;
+            z -= dz;
+            if (std::fabs(dz) < 1e-15) break;
+        }
+        double p1 = 1, p2 = 0;
+        for (int k = 1; k <= n; k++) {
+            double p3 = p2;
+            p2 = p1;
+            p1 = ((2 * k - 1) * z * p2 - (k - 1) * p3) / k;
+        }
+        double pp = n * (z * p1 - p2) / (z * z - 1);
+        x[i] = z;
+        w[i] = 2 / ((1 - z * z) * pp * pp);
+    }
+}
+
+// G[n][(mp+n)*(2n+1) + (m+n)] for f(u) -> f(Ry(a) u')
+std::vector<std::vector<cd>> yrot(int p, double a, double *max_imag) {
+    std::vector<double> gx, gw;
+    gauss_legendre(p + 1, gx, gw);
+    const int nph = 2 * p + 1;
+    std::vector<std::vector<cd>> G(p);
+    for (int n = 0; n < p; n++) G[n].assign((2 * n + 1) * (2 * n + 1), cd(0, 0));
+    std::vector<double> P0, P1;
+    const double ca = std::cos(a), sa = std::sin(a);
+    for (size_t it = 0; it < gx.size(); it++) {
+        const double ct = gx[it], st = std::sqrt(std::max(0.0, 1 - ct * ct));
+        legendre(p, ct, P0);
+        for (int ip = 0; ip < nph; ip++) {
+            const double ph = 2 * M_PI * ip / nph;
+            const double w = gw[it] * 2 * M_PI / nph;
+            const double ux = st * std::cos(ph), uy = st * std::sin(ph), uz = ct;
+            // v = Ry(a) u
+            const double vx = ca * ux + sa * uz, vy = uy, vz = -sa * ux + ca * uz;
+            const double vr = std::sqrt(vx * vx + vy * vy + vz * vz);
+            const double vct = std::max(-1.0, std::min(1.0, vz / vr));
+            const double vph = std::atan2(vy, vx);
+            legendre(p, vct, P1);
+            for (int n = 0; n < p; n++) {
+                const double f = w * (2 * n + 1) / (4 * M_PI);
+                for (int m = -n; m <= n; m++) {
+                    const cd fv = ynm(n, m, P1, p, vph);
+                    for (int mp = -n; mp <= n; mp++) {
+                        G[n][(mp + n) * (2 * n + 1) + (m + n)] += f * fv * std::conj(ynm(n, mp, P0, p, ph));
+                    }
+                }
+            }
+        }
+    }
+    double mi = 0;
+    for (auto &g : G)
+        for (auto &v : g) mi = std::max(mi, std::fabs(v.imag()));
+    *max_imag = mi;
+    return G;
+}
+
+// fold a real (2n+1)^2 rotation block into E ((n+1)^2) and O (n^2)
+void fold(const std::vector<cd> &G, int n, float *E, float *O) {
+    const int w = 2 * n + 1;
+    auto g = [&](int mp, int m) { return G[(mp + n) * w + (m + n)].real(); };
+    for (int mp = 0; mp <= n; mp++) {
+        E[mp * (n + 1) + 0] = (float)g(mp, 0);
+        for (int m = 1; m <= n; m++) E[mp * (n + 1) + m] = (float)(g(mp, m) + g(mp, -m));
+    }
+    for (int mp = 1; mp <= n; mp++)
+        for (int m = 1; m <= n; m++) O[(mp - 1) * n + (m - 1)] = (float)(g(mp, m) - g(mp, -m));
+}
+
+}  // namespace
+
+int dmat_offset_e(int n) { return n * (n + 1) * (2 * n + 1) / 6; }
+int dmat_offset_o(int n) { return n > 0 ? (n - 1) * n * (2 * n - 1) / 6 : 0; }
+
+bool build_fmm_tables(int p, int ws, FmmTables &T, std::string &err) {
+    T = FmmTables();
+    T.p = p;
+    T.ws = ws;
+    T.nc = p * (p + 1) / 2;
+    T.range = 2 * ws + 1;
+    const int R = T.range;
+    T.side = 2 * R + 1;
+    T.ncls = T.side * T.side * T.side;
+    T.esz = dmat_offset_e(p);
+    T.osz = dmat_offset_o(p);
+    T.dsz = 2 * (T.esz + T.osz);
+    T.cls_theta.assign(T.ncls, -1);
+    T.cls_phase.assign((size_t)T.ncls * p * 2, 0.f);
+    T.cls_rho2.assign(T.ncls, 0.f);
+    std::map<long long, int> theta_index;
+    std::vector<double> thetas;
+    for (int dx = -R; dx <= R; dx++)
+        for (int dy = -R; dy <= R; dy++)
+            for (int dz = -R; dz <= R; dz++) {
+                const int id = ((dx + R) * T.side + (dy + R)) * T.side + (dz + R);
+                if (std::max(std::abs(dx), std::max(std::abs(dy), std::abs(dz))) <= ws) continue;
+                const double r = std::sqrt((double)(dx * dx + dy * dy + dz * dz));
+                const double th = std::acos(dz / r);
+                const double ph = std::atan2((double)dy, (double)dx);
+                const long long key = std::llround(th * 1e12);
+                auto itk = theta_index.find(key);
+                int ti;
+                if (itk == theta_index.end()) {
+                    ti = (int)thetas.size();
+                    theta_index[key] = ti;
+                    thetas.push_back(th);
+                } else {
+                    ti = itk->second;
+                }
+                T.cls_theta[id] = ti;
+                T.cls_rho2[id] = (float)(dx * dx + dy * dy + dz * dz);
+                for (int m = 0; m < p; m++) {
+                    T.cls_phase[((size_t)id * p + m) * 2 + 0] = (float)std::cos(m * ph);
+                    T.cls_phase[((size_t)id * p + m) * 2 + 1] = (float)std::sin(m * ph);
+                }
+            }
+    T.ntheta = (int)thetas.size();
+    T.dmat.assign((size_t)T.ntheta * T.dsz, 0.f);
+    for (int ti = 0; ti < T.ntheta; ti++) {
+        double mi1 = 0, mi2 = 0;
+        // forward rotation Ry(-theta) acts on coefficients as f(u) -> f(Ry(theta) u'),
+        // the backward one Ry(theta) as f(u) -> f(Ry(-theta) u')
+        auto Gf = yrot(p, thetas[ti], &mi1);
+        auto Gb = yrot(p, -thetas[ti], &mi2);
+        if (mi1 > 1e-9 || mi2 > 1e-9) {
+            err = "y-rotation matrix is not real";
+            return false;
+        }
+        float *base = &T.dmat[(size_t)ti * T.dsz];
+        for (int n = 0; n < p; n++) {
+            fold(Gf[n], n, base + dmat_offset_e(n), base + T.esz + dmat_offset_o(n));
+            fold(Gb[n], n, base + T.esz + T.osz + dmat_offset_e(n), base + 2 * T.esz + T.osz + dmat_offset_o(n));
+        }
+    }
+    // z translation constants C[k][j][n] = (-1)^{j+k} (j+n)! / (N_n^k N_j^k)
+    T.zc.assign((size_t)p * p * p, 0.f);
+    auto N = [](int n, int m) { return std::sqrt(fact(n - m) * fact(n + m)); };
+    for (int k = 0; k < p; k++)
+        for (int j = k; j < p; j++)
+            for (int n = k; n < p; n++)
+                T.zc[((size_t)k * p + j) * p + n] = (float)(((j + k) & 1 ? -1.0 : 1.0) * fact(j + n) / (N(n, k) * N(j, k)));
+    T.nrm.assign((size_t)p * p, 0.f);
+    for (int n = 0; n < p; n++)
+        for (int m = 0; m <= n; m++) T.nrm[n * p + m] = (float)N(n, m);
+    // regular solid harmonics R_n^m(d) of the 8 child offsets d = (+-1/2)^3 in
+    // child box units, all orders m in [-n, n] (R_n^-m = (-1)^m conj R_n^m)
+    T.oct.assign((size_t)8 * p * (2 * p - 1) * 2, 0.f);
+    for (int oc = 0; oc < 8; oc++) {
+        const double x = (oc & 1) ? 0.5 : -0.5, y = (oc & 2) ? 0.5 : -0.5, z = (oc & 4) ? 0.5 : -0.5;
+        const double r2 = x * x + y * y + z * z;
+        std::vector<cd> Rh(p * p, cd(0, 0));
+        Rh[0] = 1.0;
+        for (int m = 0; m < p; m++) {
+            if (m > 0) Rh[m * p + m] = cd(x, y) / (2.0 * m) * Rh[(m - 1) * p + (m - 1)];
+            if (m + 1 < p) Rh[(m + 1) * p + m] = z * Rh[m * p + m];
+            for (int n = m + 2; n < p; n++)
+                Rh[n * p + m] = ((2.0 * n - 1) * z * Rh[(n - 1) * p + m] - r2 * Rh[(n - 2) * p + m]) /
+                                (double)((n + m) * (n - m));
+        }
+        for (int n = 0; n < p; n++)
+            for (int m = -n; m <= n; m++) {
+                cd v = m >= 0 ? Rh[n * p + m] : ((m & 1) ? -1.0 : 1.0) * std::conj(Rh[n * p - m]);
+                const size_t o = (((size_t)oc * p + n) * (2 * p - 1) + (m + p - 1)) * 2;
+                T.oct[o] = (float)v.real();
+                T.oct[o + 1] = (float)v.imag();
+            }
+    }
+    return true;
+}
+
+}  // namespace sv

@@ -116,6 +116,8 @@ sv_status bh_accel(sv_ctx *c);
 sv_status fmm_accel(sv_ctx *c);
 void tree_free(sv_ctx *c);
 void fmm_free(sv_ctx *c);
+// M2L translations and P2P pairs of the last FMM evaluation (synchronises)
+sv_status fmm_counts(sv_ctx *c, double *m2l, double *pairs);
 
 // integrate.cu
 sv_status drift(sv_ctx *c, double t_start, double h);

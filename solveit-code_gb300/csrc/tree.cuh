@@ -1,0 +1,39 @@
+// tree.cuh -- level-by-level sparse octree shared by the BH and FMM paths.
+#pragma once
+
+#include "sv_internal.cuh"
+
+namespace sv {
+
+constexpr int kDepthMeanOccupancy = 0;  // FMM: deepest level with mean occupancy >= param
+constexpr int kDepthAllSplit = 1;       // BH: down to the level where every particle is alone
+
+struct Level {
+    int nbox = 0;
+    int *start = nullptr;   // [nbox+1] first sorted particle of each box (start[nbox] = n_act)
+    int *parent = nullptr;  // [nbox] box index at level-1 (unused at level 0)
+    int *child0 = nullptr;  // [nbox+1] first child at level+1 (child0[nbox] = boxes at level+1)
+    int4 *coord = nullptr;  // [nbox] integer box coordinates (x, y, z) and particle count (w)
+};
+
+struct Tree {
+    int cap = 0;
+    int n_act = 0;          // particles in the tree (status 1 or 2), sorted first
+    int deepest = -1;       // deepest level built
+    int nbox_level[kMortonBits + 1] = {0};
+    Level lv[kMortonBits + 1];
+    uint8_t *lvl = nullptr; // per particle: coarsest level at which it starts a box
+    int *hist = nullptr;    // device histogram [levels] + n_act
+    int *h_hist = nullptr;  // pinned mirror
+    int *scratch = nullptr; // 3 x (cap+1) ints
+    void *cub_tmp = nullptr;
+    size_t cub_bytes = 0;
+    void *arena = nullptr;
+    size_t arena_bytes = 0;
+};
+
+// Builds levels 0..deepest.  depth_rule kDepthMeanOccupancy uses param as the
+// target mean particles per occupied box at the deepest level.
+sv_status tree_build(sv_ctx *c, int depth_rule, int param, Tree **out);
+
+}  // namespace sv

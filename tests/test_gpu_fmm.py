@@ -1,0 +1,93 @@
+"""Parity of the GPU FMM with the FP64 direct sum (the oracle) and with the
+reference's own FMM accuracy on the same inputs (golden fixture).
+
+Tolerances (per-particle relative L2 of the acceleration, the reference's
+compareAcceleration metric):
+  ws 1 (the reference's interaction lists), p 8: within 2x of the reference
+      FMM's own error on the same plume (its fixture: ~1.3e-4);
+  ws 2, p 8: <= 1e-5, the workload's force-error bound.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle_py as O
+import plume
+import solveit_gpu as sv
+from gpu_util import rel_l2, run_accel
+
+pytestmark = pytest.mark.gpu
+
+EPS20 = 1e-20
+
+
+def test_fmm_against_reference_fmm(golden_dir):
+    """Same plume, same p: ws 1 stays within 4x of the reference FMM's error
+    (the box geometry differs: the reference sizes cubic root domains per
+    plume), ws 2 is at least 5x more accurate than the reference FMM."""
+    g = dict(np.load(os.path.join(golden_dir, "fmm_n4096.npz")))
+    st = plume.from_ref32(g["pos4"], g["vel4"], g["acc4"], g["tinj"])
+    eps = float(g["eps"])
+    ref = O.direct_f64(st, eps)
+    l2_ref = rel_l2(g["acc_fmm"][:, :3], ref, st["status"])
+    a, s = run_accel(st, softening2=eps, method=sv.FMM, fmm_order=8, fmm_ws=1)
+    l2 = rel_l2(a, ref, st["status"])
+    assert l2 < 4.0 * l2_ref, (l2, l2_ref)
+    assert s.cell_interactions > 0 and s.pair_interactions > 0
+    a2, _ = run_accel(st, softening2=eps, method=sv.FMM, fmm_order=8, fmm_ws=2)
+    assert rel_l2(a2, ref, st["status"]) < l2_ref / 5.0
+
+
+@pytest.mark.parametrize("n,length", [(16384, 0.78e-6), (65536, 10e-6)])
+def test_fmm_ws2_p8_meets_1e5(n, length):
+    st = plume.make_plume(n, length, 31)
+    tg = np.arange(0, n, max(1, n // 2048))
+    ref = O.direct_f64(st, EPS20, targets=tg)
+    a, s = run_accel(st, softening2=EPS20, method=sv.FMM, fmm_order=8, fmm_ws=2)
+    assert rel_l2(a[tg], ref, st["status"][tg]) < 1e-5
+
+
+def test_fmm_error_falls_with_order():
+    st = plume.make_plume(8192, 1e-6, 5)
+    ref = O.direct_f64(st, EPS20)
+    errs = []
+    for p in (4, 6, 8, 10):
+        a, _ = run_accel(st, softening2=EPS20, method=sv.FMM, fmm_order=p, fmm_ws=1)
+        errs.append(rel_l2(a, ref, st["status"]))
+    assert errs[0] > errs[1] > errs[2] > errs[3], errs
+    assert errs[3] < 1e-4
+
+
+@pytest.mark.parametrize("n", [1, 2, 37, 300])
+def test_fmm_small_plumes(n):
+    st = plume.make_plume(n, 1e-7, 9 + n)
+    ref = O.direct_f64(st, EPS20)
+    a, _ = run_accel(st, softening2=EPS20, method=sv.FMM, fmm_order=8, fmm_ws=2)
+    if n == 1:
+        assert np.all(a == 0)
+    else:
+        assert rel_l2(a, ref, st["status"]) < 1e-5
+
+
+def test_fmm_status_handling():
+    st = plume.make_plume(5000, 1e-6, 12)
+    st["status"][:100] = 2
+    st["status"][100:200] = 0
+    st["status"][200:300] = -1
+    ref = O.direct_f64(st, EPS20)
+    a, _ = run_accel(st, softening2=EPS20, method=sv.FMM, fmm_order=8, fmm_ws=2)
+    assert np.all(a[:300] == 0)
+    assert rel_l2(a, ref, st["status"]) < 1e-5
+
+
+def test_fmm_leapfrog_tracks_direct():
+    st = plume.make_plume(4096, 1e-6, 44)
+    ef = (0.0, 0.0, 1e8)
+    xr, vr, _ = O.leapfrog_f64(st, 5, 1e-13, EPS20, ef)
+    with sv.ForceMethod(softening2=EPS20, method=sv.FMM, fmm_order=8, fmm_ws=2, efield=ef) as fm:
+        fm.upload(st)
+        fm.leapfrog(5, 1e-13)
+        x, v, _ = fm.download()
+    dv = np.linalg.norm(v - vr, axis=1) / np.linalg.norm(vr - st["v"], axis=1)
+    assert np.sqrt(np.mean(dv ** 2)) < 1e-5
