@@ -1,0 +1,373 @@
+"""Benchmark: particle-steps/s of the GB300 force-evaluation + leapfrog path.
+
+Default workload (fmm_n1m): one plume of N = 1,048,576 singly charged ions
+(r <= 20 nm, z in [0, 50] um, softening 1e-10 m), leapfrog DKD steps of
+dt = 1e-13 s with E_z = 1e8 V/m, forces by the FMM (p = 8, ws = 2) in mixed
+precision (FP32 pair / expansion arithmetic, FP64 positions, velocities,
+accumulation and integration).  A step = drift dt/2 + force evaluation + kick
++ drift dt/2 over the whole plume.
+
+  value          particle-steps/s with the plume resident in HBM (CUDA events
+                 on the context stream around each step; L2 flushed between
+                 steps by writing 512 MB)
+  e2e            same metric through the C ABI with host buffers: per step,
+                 upload of the state from pinned host memory, one step, and
+                 download of positions / velocities / status
+  fp64_direct    the plain FP64 GPU direct-sum path on the same GPU (measured
+                 at N = 131072, scaled by N^2 to the workload's N)
+  force_err      per-particle relative L2 of the FMM acceleration against the
+                 FP64 GPU direct sum on sampled targets
+  cpu_baseline   the C oracle's FP64 direct sum (the reference's direct sum
+                 restated; the reference's own FMM crashes at this N) on a
+                 bounded sample of targets, all host threads
+
+--impl reference times that CPU path alone (the reference arm).
+Under torchrun with N > 1 GPUs every rank runs an independent plume
+(replicas only: the workload has no exchange step).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "solveit-code_gb300"))
+
+import plume  # noqa: E402
+
+METRIC = "particle-steps/s, mixed-prec vs plain FP64 path, same GB300, force err <=1e-5"
+EPS2 = 1e-20
+DT = 1e-13
+EZ = 1e8
+
+WORKLOADS = {
+    "fmm_n1m": dict(n=1 << 20, length=50e-6, method="fmm", order=8, ws=2, leaf=32, seed=2000,
+                    desc="FMM p=8 ws=2, N=1048576 ions, plume r=20nm z=50um, eps=1e-10m, "
+                         "leapfrog DKD dt=1e-13s, E_z=1e8V/m"),
+    "direct_n4096": dict(n=4096, length=1e-6, method="direct", precision="fp64", seed=0,
+                         desc="FP64 direct sum, N=4096 ions, plume r=20nm z=1um, eps=1e-10m, "
+                              "leapfrog DKD dt=1e-13s, E_z=1e8V/m"),
+}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def sample_clocks_start():
+    try:
+        import tempfile
+
+        path = os.path.join(tempfile.gettempdir(), f"sv_clocks_{os.getpid()}.csv")
+        f = open(path, "w")
+        p = subprocess.Popen(
+            ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+             "--format=csv,noheader,nounits", "-lms", "200"], stdout=f, stderr=subprocess.DEVNULL)
+        return p, f
+    except Exception:
+        return None, None
+
+
+def sample_clocks_stop(p, f, gpu_index):
+    if p is None:
+        return None
+    p.terminate()
+    try:
+        p.wait(timeout=5)
+    except Exception:
+        p.kill()
+    f.close()
+    path = f.name
+    sm, smax, reasons = [], 0.0, set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    try:
+        for line in open(path):
+            cols = [c.strip() for c in line.split(",")]
+            if len(cols) < 9 or cols[0] != str(gpu_index):
+                continue
+            try:
+                sm.append(float(cols[1]))
+                smax = max(smax, float(cols[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if cols[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        os.remove(path)
+    except Exception:
+        pass
+    if not sm:
+        return None
+    loaded = sorted(sm)[len(sm) // 2:]  # upper half: samples under load
+    return {"sm_mhz": float(np.median(loaded)), "sm_max_mhz": smax, "reasons": sorted(reasons),
+            "samples": len(sm)}
+
+
+def cpu_baseline(state, n_sample, threads):
+    """FP64 direct sum of the C oracle on n_sample targets; particle-steps/s."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py as O
+
+    n = state["x"].shape[0]
+    tg = np.linspace(0, n - 1, n_sample).astype(np.int64)
+    O.direct_f64(state, EPS2, targets=tg[:64], threads=threads)  # warm
+    t = time.perf_counter()
+    O.direct_f64(state, EPS2, targets=tg, threads=threads)
+    dt = time.perf_counter() - t
+    return {"value": n_sample / dt, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+            "sample": f"FP64 direct sum (oracle restatement of direct_force_method.cpp:153-190) for "
+                      f"{n_sample} of {n} targets against all {n} sources, one force evaluation "
+                      f"({dt:.2f} s); per-target cost is independent of the target count, so "
+                      f"particle-steps/s = targets / time"}
+
+
+def run_reference(args, wl, rank, world):
+    if rank != 0:
+        return
+    st = plume.make_plume(wl["n"], wl["length"], wl["seed"] * 1000 + 0)
+    threads = os.cpu_count() or 1
+    n_sample = 2048 if wl["n"] > 100000 else min(wl["n"], 4096)
+    vals = []
+    cb = None
+    for k in range(args.warmup + args.steps):
+        cb = cpu_baseline(st, n_sample, threads)
+        if k >= args.warmup:
+            vals.append(cb["value"])
+    v = float(np.mean(vals))
+    cb["value"] = v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "particle-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": wl["n"] / v * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": args.workload, "desc": wl["desc"], "n": wl["n"]},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, wl, rank, world, local):
+    import torch
+
+    import solveit_gpu as sv
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    n = wl["n"]
+    st = plume.make_plume(n, wl["length"], wl["seed"] * 1000 + rank)
+    if wl["method"] == "fmm":
+        kw = dict(method=sv.FMM, precision=sv.MIXED, fmm_order=wl["order"], fmm_ws=wl["ws"],
+                  fmm_leaf_target=wl["leaf"])
+    else:
+        kw = dict(method=sv.DIRECT, precision=sv.FP64 if wl.get("precision") == "fp64" else sv.MIXED)
+    fm = sv.ForceMethod(softening2=EPS2, efield=(0.0, 0.0, EZ), device=local, profile_phases=1, **kw)
+    fm.upload(st)
+    stream = torch.cuda.ExternalStream(fm.stream, device=local)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+
+    # ---- device-resident timing
+    t = 0.0
+    for _ in range(args.warmup):
+        fm.leapfrog(1, DT, t)
+        t += DT
+    fm.sync()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    phase_ms = np.zeros(8)
+    clk_p, clk_f = sample_clocks_start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = fm.launches
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        evs[k][0].record(stream)
+        fm.leapfrog(1, DT, t)
+        evs[k][1].record(stream)
+        t += DT
+        fm.sync()
+        s = fm.stats()
+        phase_ms += np.array(list(s.ms_phase))
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    launches = fm.launches - launches0
+    clocks = sample_clocks_stop(clk_p, clk_f, local)
+    step_ms = float(sum(a.elapsed_time(b) for a, b in evs))
+    if dist:
+        tt = torch.tensor([step_ms], device=f"cuda:{local}")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        step_ms = float(tt.item())
+    ms_per_step = step_ms / args.steps
+    value = world * n * args.steps / (step_ms / 1e3)
+    phase_ms /= args.steps
+    stats = fm.stats()
+
+    if args.timed_only:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "ms_per_step": ms_per_step,
+                              "phases_ms": list(map(float, phase_ms)), "timed_only": True}), flush=True)
+        fm.close()
+        return
+    # ---- end to end through the C ABI with pinned host buffers
+    pin = {k: torch.empty(st[k].shape, dtype=torch.float64 if st[k].dtype == np.float64 else torch.int32,
+                          pin_memory=True) for k in ("x", "v", "q", "m", "status", "t_inj")}
+    for k in pin:
+        pin[k].numpy()[...] = st[k]
+    xo = torch.empty((n, 3), dtype=torch.float64, pin_memory=True)
+    vo = torch.empty((n, 3), dtype=torch.float64, pin_memory=True)
+    so = torch.empty((n,), dtype=torch.int32, pin_memory=True)
+    import ctypes as C
+
+    L = sv.load()
+
+    def ptr(tn):
+        return C.c_void_p(tn.data_ptr())
+
+    def e2e_step(t0):
+        L.sv_upload(fm.h, n, ptr(pin["x"]), ptr(pin["v"]), ptr(pin["q"]), ptr(pin["m"]), ptr(pin["status"]),
+                    ptr(pin["t_inj"]))
+        L.sv_leapfrog(fm.h, 1, DT, t0)
+        rc = L.sv_download(fm.h, ptr(xo), ptr(vo), ptr(so))
+        if rc != 0:
+            raise RuntimeError(L.sv_last_error(fm.h).decode())
+
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step(0.0)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0 = time.perf_counter()
+    for k in range(args.steps):
+        e2e_step(k * DT)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - e0
+    if dist:
+        tt = torch.tensor([e2e_s], device=f"cuda:{local}")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    h2d = n * (3 * 8 + 3 * 8 + 8 + 8 + 4 + 8)
+    d2h = n * (3 * 8 + 3 * 8 + 4)
+    e2e = {"value": world * n * args.steps / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h}
+
+    line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 pair/expansion arithmetic, f64 state and integration",
+            "data": "synthetic (seeded plume generator, seed 1000*workload+rank)",
+            "config": {"workload": args.workload, "desc": wl["desc"], "n_per_gpu": n,
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                       "l2": "512 MB written between timed steps (L2 flush)", "leaf_level": stats.levels,
+                       "leaf_boxes": stats.boxes},
+            "clocks": clocks, "e2e": e2e, "gpu_launches": int(launches // max(1, args.steps)) * args.steps,
+            "wall_s_timed_region": wall}
+
+    if rank == 0:
+        # ---- phase breakdown and roofline of the dominant kernel
+        names = ["sort", "tree", "lists", "upward_p2m_m2m", "downward_m2l_l2l", "l2p", "near_p2p", "scatter"]
+        line["phases_ms"] = {nm: round(float(v), 4) for nm, v in zip(names, phase_ms)}
+        peaks = {}
+        try:
+            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        except Exception:
+            pass
+        sm_max = peaks.get("sm_max_mhz", 2070.0)
+        fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+        if wl["method"] == "fmm":
+            near_flop = 20.0 * stats.pair_interactions
+            dom_ms = phase_ms[6]
+            achieved = near_flop / (dom_ms * 1e-3) / 1e12
+            m2l_flop = stats.flops_algorithmic - near_flop - n * 8.0 * (wl["order"] * (wl["order"] + 1) / 2) * 4
+            line["roofline"] = {"kernel": "p2p_kernel (near field, 20 flop/pair)", "bound": "fp32",
+                                "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                                "frac": achieved / fp32_peak, "traffic": None,
+                                "peak_source": "FP32 FMA rate 152 SMs x 128 lanes x 2 flop x sm_max_mhz of "
+                                               "MEASURED_PEAKS.json (no FP32 peak is measured there; the "
+                                               "kernel runs on the FP32 pipe, not the tensor cores)",
+                                "pairs_per_step": stats.pair_interactions,
+                                "m2l_per_step": stats.cell_interactions,
+                                "m2l_tflops": m2l_flop / (phase_ms[4] * 1e-3) / 1e12 if phase_ms[4] > 0 else None}
+        else:
+            dom_ms = phase_ms[6]
+            achieved = stats.flops_algorithmic / (dom_ms * 1e-3) / 1e12
+            line["roofline"] = {"kernel": "direct kernel", "bound": "fp64", "achieved": achieved,
+                                "peak": None, "unit": "TFLOP/s", "frac": None, "traffic": None}
+        # ---- force error against the FP64 GPU direct sum on sampled targets
+        if wl["method"] == "fmm":
+            x, v, stt = fm.download()
+            cur = dict(st, x=x, v=v, status=stt)
+            a_fmm = fm.accel()
+            rng = np.random.default_rng(7)
+            tg = rng.choice(n, 64, replace=False)
+            cur2 = dict(cur)
+            s2 = np.where(cur["status"] == 1, 2, cur["status"]).astype(np.int32)
+            s2[tg] = cur["status"][tg]
+            cur2["status"] = s2
+            with sv.ForceMethod(softening2=EPS2, method=sv.DIRECT, precision=sv.FP64, device=local) as ref:
+                ref.upload(cur2)
+                a_ref = ref.accel()[tg]
+            d = np.sum((a_fmm[tg] - a_ref) ** 2, axis=1) / np.sum(a_ref ** 2, axis=1)
+            line["force_err_rel_l2"] = float(np.sqrt(np.mean(d)))
+            line["force_err_max"] = float(np.sqrt(np.max(d)))
+            # ---- plain FP64 GPU direct path on the same GPU
+            m = 131072
+            sub = {k: (st[k][:m] if hasattr(st[k], "__len__") else st[k]) for k in st}
+            with sv.ForceMethod(softening2=EPS2, method=sv.DIRECT, precision=sv.FP64, device=local,
+                                efield=(0.0, 0.0, EZ)) as f64:
+                f64.upload(sub)
+                f64.leapfrog(1, DT)
+                f64.sync()
+                t0 = time.perf_counter()
+                f64.leapfrog(1, DT)
+                f64.sync()
+                t_m = time.perf_counter() - t0
+            t_n = t_m * (n / m) ** 2
+            line["fp64_direct"] = {"value": n / t_n, "unit": "particle-steps/s",
+                                   "measured": f"one FP64 direct leapfrog step at N={m}: {t_m * 1e3:.1f} ms, "
+                                               f"scaled by (N/{m})^2 to N={n}",
+                                   "ms_per_step_at_n": t_n * 1e3}
+            line["speedup_vs_fp64_direct"] = value / world / (n / t_n)
+        # ---- CPU baseline (C oracle FP64 direct sum, bounded sample)
+        threads = os.cpu_count() or 1
+        line["cpu_baseline"] = cpu_baseline(st, 2048 if n > 100000 else min(n, 4096), threads)
+        print(json.dumps(line), flush=True)
+    fm.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="fmm_n1m", choices=sorted(WORKLOADS))
+    ap.add_argument("--timed-only", action="store_true",
+                    help="only the device-resident timed steps (for profiler launch lists)")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    rank, world, local = dist_env()
+    wl = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, wl, rank, world)
+    else:
+        run_ours(args, wl, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -84,7 +84,8 @@ typedef struct {
     int32_t sym_levels;      /* numSymmetryLevels: 3^levels cells per periodic axis */
     double domain_size[3];   /* periodic cell size in m (SimulationParameters::domainSize) */
     int32_t device;          /* CUDA device ordinal */
-    int32_t reserved[7];
+    int32_t profile_phases;  /* 1: record device time of each phase into sv_stats.ms_phase */
+    int32_t reserved[6];
 } sv_params;
 
 /* Per-call statistics of the last force evaluation. */
@@ -93,7 +94,8 @@ typedef struct {
     double cell_interactions;     /* BH accepted cells / FMM M2L translations */
     double flops_algorithmic;     /* 20 flop/pair + expansion flops (method's count) */
     double ms_total;              /* device time of the whole evaluation */
-    double ms_phase[8];           /* sort, tree, upward, m2l, downward, near, other, spare */
+    double ms_phase[8];           /* sort, tree, lists, upward (P2M+M2M), downward (M2L+L2L),
+                                     L2P, near field (P2P / direct / BH walk), scatter */
     int32_t levels;               /* FMM leaf level / BH max depth */
     int32_t boxes;                /* occupied leaf boxes / BH nodes */
     int32_t reserved[6];

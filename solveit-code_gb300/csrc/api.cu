@@ -316,6 +316,7 @@ sv_status sv_create(const sv_params *p, sv_ctx **out) {
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_scalar, 64 * sizeof(double));
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev_begin);
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev_end);
+    for (int k = 0; k < 9 && e == cudaSuccess; k++) e = cudaEventCreate(&c->ph_ev[k]);
     if (e != cudaSuccess) {
         sv_destroy(c);
         return e == cudaErrorMemoryAllocation ? SV_ERR_ALLOC : SV_ERR_CUDA;
@@ -341,6 +342,8 @@ void sv_destroy(sv_ctx *c) {
     if (c->h_scalar) cudaFreeHost(c->h_scalar);
     if (c->ev_begin) cudaEventDestroy(c->ev_begin);
     if (c->ev_end) cudaEventDestroy(c->ev_end);
+    for (int k = 0; k < 9; k++)
+        if (c->ph_ev[k]) cudaEventDestroy(c->ph_ev[k]);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -463,16 +466,20 @@ static sv_status compute_accel_device(sv_ctx *c, int64_t first, int64_t last) {
     memset(&c->stats, 0, sizeof(c->stats));
     SV_CK(c, cudaEventRecord(c->ev_begin, c->stream));
     if (n > 0) {
+        phase_mark(c, 0);
         SV_TRY(sort_state(c, first, last));
+        phase_mark(c, 1);
         switch (c->P.method) {
         case SV_METHOD_DIRECT: SV_TRY(direct_accel(c)); break;
         case SV_METHOD_BARNES_HUT: SV_TRY(bh_accel(c)); break;
         case SV_METHOD_FMM: SV_TRY(fmm_accel(c)); break;
         default: return set_error(c, SV_ERR_INVALID, "unknown method");
         }
+        phase_mark(c, 7);
         SV_TRY(unsort_accel(c));
         zero_nontargets<<<grid_of(n), 256, 0, c->stream>>>(c->ax, c->ay, c->az, c->status, first, last, n);
         SV_LAUNCHED(c);
+        phase_mark(c, 8);
     }
     SV_CK(c, cudaEventRecord(c->ev_end, c->stream));
     c->have_accel = true;
@@ -591,6 +598,12 @@ sv_status sv_get_stats(const sv_ctx *cc, sv_stats *out) {
         // rotations and z-translation; P2M + L2P (1 + 3 terms per coefficient)
         c->stats.flops_algorithmic = 20.0 * pairs + m2l * 8.0 * (2.0 * rot + zt) +
                                      (double)c->n * 8.0 * (p * (p + 1) / 2) * 4.0;
+    }
+    if (c->have_accel && c->P.profile_phases && cudaEventQuery(c->ph_ev[8]) == cudaSuccess) {
+        for (int k = 0; k < 8; k++) {
+            float t = 0.f;
+            c->stats.ms_phase[k] = cudaEventElapsedTime(&t, c->ph_ev[k], c->ph_ev[k + 1]) == cudaSuccess ? t : 0.0;
+        }
     }
     *out = c->stats;
     float ms = 0.f;

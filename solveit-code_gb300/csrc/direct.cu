@@ -50,6 +50,17 @@ __device__ __forceinline__ void image_of(const Images &im, int g, double &x, dou
     }
 }
 
+// true when any of the CTA's kTPB*kTPT targets has a nonzero K q/m (a target)
+__device__ __forceinline__ bool block_has_target(const double *__restrict__ qm, int t0, int n) {
+    int any = 0;
+#pragma unroll
+    for (int k = 0; k < kTPT; k++) {
+        const int i = t0 + threadIdx.x + k * kTPB;
+        any |= (i < n && qm[i] != 0.0);
+    }
+    return __syncthreads_or(any) != 0;
+}
+
 __global__ void __launch_bounds__(kTPB)
 direct_mixed_kernel(const double *__restrict__ xs, const double *__restrict__ ys,
                     const double *__restrict__ zs, const float *__restrict__ qs,
@@ -62,6 +73,7 @@ direct_mixed_kernel(const double *__restrict__ xs, const double *__restrict__ ys
     const int j_end = min(n, j_begin + chunk);
     const int o = min(t0, n - 1);
     const double ox = xs[o], oy = ys[o], oz = zs[o];
+    if (!block_has_target(qm, t0, n)) return;  // whole CTA of non-targets (target subsets)
 
     float tx[kTPT], ty[kTPT], tz[kTPT];
     double sx[kTPT], sy[kTPT], sz[kTPT];
@@ -153,6 +165,7 @@ direct_fp64_kernel(const double *__restrict__ xs, const double *__restrict__ ys,
     const int j_begin = blockIdx.y * chunk;
     const int j_end = min(n, j_begin + chunk);
     double tx[kTPT], ty[kTPT], tz[kTPT], sx[kTPT], sy[kTPT], sz[kTPT];
+    if (!block_has_target(qm, t0, n)) return;
 #pragma unroll
     for (int k = 0; k < kTPT; k++) {
         const int ii = min(t0 + (int)threadIdx.x + k * kTPB, n - 1);
@@ -245,6 +258,7 @@ sv_status direct_accel(sv_ctx *c) {
         SV_CK(c, cudaMemsetAsync(S.ay, 0, sizeof(double) * n, c->stream));
         SV_CK(c, cudaMemsetAsync(S.az, 0, sizeof(double) * n, c->stream));
     }
+    for (int k = 2; k <= 6; k++) phase_mark(c, k);
     dim3 grid(tblocks, splits);
     if (c->P.precision == SV_PREC_FP64) {
         direct_fp64_kernel<<<grid, kTPB, 0, c->stream>>>(S.x, S.y, S.z, S.q, S.qm, n, chunk, c->P.softening2,

@@ -543,6 +543,7 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         cnt[l] = (int *)carve(nb * sizeof(int));
         SV_CK(c, cudaMemsetAsync(nbr[l], 0xff, nb * ns * sizeof(int), c->stream));
     }
+    phase_mark(c, 2);
     SV_CK(c, cudaMemsetAsync(F.d_counts, 0, 2 * sizeof(unsigned long long), c->stream));
     root_nbr_kernel<<<1, 32, 0, c->stream>>>(nbr[0], ns);
     SV_LAUNCHED(c);
@@ -557,6 +558,7 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
                 V.nbox, V.parent, V.coord, nbr[l - 1], U.child0, nbr[l], lst[l], cnt[l], cap, F.d_counts);
         SV_LAUNCHED(c);
     }
+    phase_mark(c, 3);
     // upward pass
     {
         const Level &V = T.lv[L];
@@ -570,6 +572,7 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
                                                                               Mv[l + 1], Mv[l], F.nrm, F.oct);
         SV_LAUNCHED(c);
     }
+    phase_mark(c, 4);
     // downward pass: L2L + M2L per level
     for (int l = 2; l <= L; l++) {
         const Level &V = T.lv[l];
@@ -600,6 +603,7 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         down_kernel<P><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(a);
         SV_LAUNCHED(c);
     }
+    phase_mark(c, 5);
     // far field then near field, written in sorted order
     {
         const Level &V = T.lv[L];
@@ -612,6 +616,7 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
             SV_CK(c, cudaMemsetAsync(S.ay, 0, sizeof(double) * c->n, c->stream));
             SV_CK(c, cudaMemsetAsync(S.az, 0, sizeof(double) * c->n, c->stream));
         }
+        phase_mark(c, 6);
         if (ws == 1)
             p2p_kernel<1><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
                 V.nbox, V.start, V.coord, nbr[L], S.x, S.y, S.z, S.q, S.qm, S.root, L, (float)c->P.softening2,

@@ -62,6 +62,9 @@ struct sv_ctx {
     double *d_scalar = nullptr;   // device scratch for small reductions
     double *h_scalar = nullptr;   // pinned mirror
     cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+    // per-phase timing (sv_params.profile_phases): events 0..8 bracket the
+    // phases sort, tree, lists, upward, downward, L2P, near field, scatter
+    cudaEvent_t ph_ev[9] = {};
     unsigned long long launches = 0;
     sv_stats stats{};
     char err[512] = {0};
@@ -96,6 +99,11 @@ struct alignas(32) dbl4_t {
     double x, y, z, w;
 };
 __host__ __device__ inline dbl4_t dbl4(double x, double y, double z, double w) { return dbl4_t{x, y, z, w}; }
+
+// record the boundary event k of the per-phase timing when profiling is on
+inline void phase_mark(sv_ctx *c, int k) {
+    if (c->P.profile_phases && c->ph_ev[k]) cudaEventRecord(c->ph_ev[k], c->stream);
+}
 
 inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 

@@ -39,7 +39,7 @@ class Params(C.Structure):
         ("symmetry", C.c_int32), ("theta", C.c_float), ("leaf_size", C.c_int32),
         ("fmm_order", C.c_int32), ("fmm_ws", C.c_int32), ("fmm_leaf_target", C.c_int32),
         ("sym_axes", C.c_int32 * 3), ("sym_levels", C.c_int32), ("domain_size", C.c_double * 3),
-        ("device", C.c_int32), ("reserved", C.c_int32 * 7),
+        ("device", C.c_int32), ("profile_phases", C.c_int32), ("reserved", C.c_int32 * 6),
     ]
 
 
