@@ -165,6 +165,26 @@ SV_API uint64_t sv_launch_count(const sv_ctx *ctx);
 SV_API const char *sv_last_error(const sv_ctx *ctx);
 SV_API int32_t sv_abi_version(void);
 
+/* Direct sum that allocates no memory.  No counterpart in the reference: it
+ * is for callers that cannot allocate device memory (an allocator owned by a
+ * host framework, real-time loops that forbid cudaMalloc / cudaFree and their
+ * implicit synchronisation).  Computes the same acceleration as
+ * sv_compute_accel with SV_METHOD_DIRECT, SV_PREC_MIXED, SV_SYM_NONE: a3
+ * (3n interleaved, m/s^2) for every particle with status 1, 0 for the others,
+ * sources with status 1 or 2.  All pointers are DEVICE pointers on the current
+ * device; x3 is 3n interleaved (m), q in e, m_amu in amu; stream is a
+ * cudaStream_t (NULL = legacy default stream).  Working storage is one static
+ * device array of SV_NOALLOC_SCRATCH_BYTES that each GPU loading the library
+ * holds until exit; n above SV_NOALLOC_MAX_N returns SV_ERR_CAPACITY.  The
+ * first call on a device looks the array up (cudaGetSymbolAddress) and must
+ * come before any stream capture.  Calls whose work overlaps on the GPU race
+ * on the shared array. */
+#define SV_NOALLOC_MAX_N 262144
+#define SV_NOALLOC_SCRATCH_BYTES (40u << 20)
+SV_API sv_status sv_direct_accel_noalloc(int64_t n, const double *x3, const double *q, const double *m_amu,
+                                         const int32_t *status, double softening2, double k_const,
+                                         double *a3, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

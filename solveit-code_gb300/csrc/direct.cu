@@ -277,4 +277,29 @@ sv_status direct_accel(sv_ctx *c) {
     return SV_OK;
 }
 
+cudaError_t launch_direct_mixed_sorted(const double *xs, const double *ys, const double *zs, const float *qs,
+                                       const double *qm, int n, float eps2, double *ax, double *ay, double *az,
+                                       cudaStream_t stream) {
+    if (n <= 0) return cudaSuccess;
+    const int tblocks = div_up(n, kTPB * kTPT);
+    int splits = div_up(8 * kNumSMs, tblocks);
+    const int max_splits = div_up(n, kTile);
+    if (splits > max_splits) splits = max_splits;
+    if (splits < 1) splits = 1;
+    const int chunk = div_up(div_up(n, splits), kTile) * kTile;
+    splits = div_up(n, chunk);
+    const int atomic_out = splits > 1;
+    cudaError_t e = cudaSuccess;
+    if (atomic_out) {
+        e = cudaMemsetAsync(ax, 0, sizeof(double) * n, stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(ay, 0, sizeof(double) * n, stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(az, 0, sizeof(double) * n, stream);
+        if (e != cudaSuccess) return e;
+    }
+    Images im{0, 1, nullptr};
+    direct_mixed_kernel<<<dim3(tblocks, splits), kTPB, 0, stream>>>(xs, ys, zs, qs, qm, n, chunk, eps2, im, ax, ay,
+                                                                    az, atomic_out);
+    return cudaGetLastError();
+}
+
 }  // namespace sv

@@ -118,6 +118,11 @@ sv_status read_root(sv_ctx *c, double root[8]);
 
 // direct.cu
 sv_status direct_accel(sv_ctx *c);  // sorted -> c->S.a*
+// the mixed-precision all-pairs kernel on caller-provided sorted arrays
+// (no symmetry images); launches only, allocates nothing
+cudaError_t launch_direct_mixed_sorted(const double *xs, const double *ys, const double *zs, const float *qs,
+                                       const double *qm, int n, float eps2, double *ax, double *ay, double *az,
+                                       cudaStream_t stream);
 
 // tree.cu / bh.cu / fmm.cu
 sv_status bh_accel(sv_ctx *c);
