@@ -331,6 +331,7 @@ void sv_destroy(sv_ctx *c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     tree_free(c);
     fmm_free(c);
+    bh_free(c);
     free_state(c);
     Sorted &S = c->S;
     cudaFree(S.x); cudaFree(S.y); cudaFree(S.z); cudaFree(S.q); cudaFree(S.qm);

@@ -37,6 +37,7 @@ struct Sorted {
 
 struct Fmm;   // fmm.cu
 struct Tree;  // tree.cu
+struct Bh;    // bh.cu
 
 }  // namespace sv
 
@@ -56,6 +57,7 @@ struct sv_ctx {
     sv::Sorted S;
     sv::Tree *tree = nullptr;
     sv::Fmm *fmm = nullptr;
+    sv::Bh *bh = nullptr;
     // device staging for interleaved <-> SoA transfers
     void *d_stage = nullptr;
     size_t d_stage_bytes = 0;
@@ -129,6 +131,7 @@ sv_status bh_accel(sv_ctx *c);
 sv_status fmm_accel(sv_ctx *c);
 void tree_free(sv_ctx *c);
 void fmm_free(sv_ctx *c);
+void bh_free(sv_ctx *c);
 // M2L translations and P2P pairs of the last FMM evaluation (synchronises)
 sv_status fmm_counts(sv_ctx *c, double *m2l, double *pairs);
 

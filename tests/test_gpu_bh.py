@@ -1,0 +1,93 @@
+"""Parity of the GPU Barnes-Hut treecode.
+
+theta = 0 opens every cell, so the walk must reproduce the direct sum (FP32
+pair arithmetic on FP32 hi/lo coordinates: <= 2e-6 per-particle relative L2
+against the FP64 oracle), for all three symmetry variants.  theta = 0.5 is an
+approximation; its envelope is the reference's own BH on the same plume (the
+golden fixture: monopole walk, one particle per leaf): ours keeps leaves of
+<= 16 particles, whose rejected leaves are summed directly, so it must not be
+less accurate than the reference (1.5x margin for tree geometry).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle_py as O
+import plume
+import solveit_gpu as sv
+from gpu_util import rel_l2, run_accel
+
+pytestmark = pytest.mark.gpu
+
+EPS20 = 1e-20
+
+
+@pytest.mark.parametrize("sym", [0, 1, 2])
+def test_bh_theta0_is_direct(sym):
+    st = plume.make_plume(3000, 1e-6, 61)
+    st["x"][:, 0] += 3e-8
+    img = O.trans_images(2, (1, 1, 0)) * np.array([2e-6, 2e-6, 0.0]) if sym == 2 else None
+    ref = O.direct_f64(st, EPS20, sym=sym, img_off=img)
+    a, s = run_accel(st, softening2=EPS20, method=sv.BARNES_HUT, theta=0.0, symmetry=sym, sym_axes=(1, 1, 0),
+                     sym_levels=2, domain_size=(2e-6, 2e-6, 0.0))
+    assert rel_l2(a, ref, st["status"]) < 2e-6
+    assert s.cell_interactions == 0 and s.pair_interactions > 0
+
+
+def test_bh_theta05_within_reference_envelope(golden_dir):
+    g = dict(np.load(os.path.join(golden_dir, "bh_n4096.npz")))
+    st = plume.from_ref32(g["pos4"], g["vel4"], g["acc4"], g["tinj"])
+    eps = float(g["eps"])
+    ref = O.direct_f64(st, eps)
+    l2_ref = rel_l2(g["acc_bh"][:, :3], ref, st["status"])
+    a, s = run_accel(st, softening2=eps, method=sv.BARNES_HUT, theta=float(g["theta"]), leaf_size=16)
+    l2 = rel_l2(a, ref, st["status"])
+    assert l2 < 1.5 * l2_ref, (l2, l2_ref)
+    assert s.cell_interactions > 0
+    # one particle per leaf, as the reference builds it
+    a1, _ = run_accel(st, softening2=eps, method=sv.BARNES_HUT, theta=float(g["theta"]), leaf_size=1)
+    assert rel_l2(a1, ref, st["status"]) < 1.5 * l2_ref
+
+
+def test_bh_c1_size_sampled():
+    n = 65536
+    st = plume.make_plume(n, 10e-6, 1001)
+    tg = np.arange(0, n, 61)
+    ref = O.direct_f64(st, EPS20, targets=tg)
+    a, _ = run_accel(st, softening2=EPS20, method=sv.BARNES_HUT, theta=0.5, leaf_size=16)
+    assert rel_l2(a[tg], ref, st["status"][tg]) < 1e-2
+
+
+@pytest.mark.parametrize("sym", [1, 2])
+def test_bh_symmetry_theta05(sym):
+    st = plume.make_plume(4096, 1e-6, 62)
+    st["x"][:, 0] += 3e-8
+    img = O.trans_images(2, (1, 1, 0)) * np.array([2e-6, 2e-6, 0.0]) if sym == 2 else None
+    ref = O.direct_f64(st, EPS20, sym=sym, img_off=img)
+    a, _ = run_accel(st, softening2=EPS20, method=sv.BARNES_HUT, theta=0.5, symmetry=sym, sym_axes=(1, 1, 0),
+                     sym_levels=2, domain_size=(2e-6, 2e-6, 0.0))
+    assert rel_l2(a, ref, st["status"]) < 2e-2
+
+
+def test_bh_status_and_coincident_particles():
+    st = plume.make_plume(2000, 1e-6, 63)
+    st["x"][1] = st["x"][0]        # two particles at the same point
+    st["x"][2] = st["x"][0]
+    st["status"][10:20] = 2
+    st["status"][20:30] = 0
+    st["status"][30:40] = -1
+    ref = O.direct_f64(st, EPS20)
+    a, _ = run_accel(st, softening2=EPS20, method=sv.BARNES_HUT, theta=0.0)
+    assert np.all(a[10:40] == 0.0)
+    assert np.all(np.isfinite(a))
+    assert rel_l2(a, ref, st["status"]) < 2e-6
+
+
+def test_bh_small_and_empty():
+    for n in (0, 1, 2, 33):
+        st = plume.make_plume(n, 1e-7, 64 + n)
+        a, _ = run_accel(st, softening2=EPS20, method=sv.BARNES_HUT, theta=0.5)
+        assert a.shape == (n, 3) and np.all(np.isfinite(a))
+        if n == 1:
+            assert np.all(a == 0.0)
