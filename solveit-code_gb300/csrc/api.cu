@@ -468,7 +468,10 @@ static sv_status compute_accel_device(sv_ctx *c, int64_t first, int64_t last) {
     SV_CK(c, cudaEventRecord(c->ev_begin, c->stream));
     if (n > 0) {
         phase_mark(c, 0);
-        SV_TRY(sort_state(c, first, last));
+        if (c->P.method == SV_METHOD_FMM && c->P.symmetry != SV_SYM_NONE)
+            SV_TRY(fmm_sort_images(c, first, last));
+        else
+            SV_TRY(sort_state(c, first, last));
         phase_mark(c, 1);
         switch (c->P.method) {
         case SV_METHOD_DIRECT: SV_TRY(direct_accel(c)); break;

@@ -298,7 +298,7 @@ sv_status bh_accel(sv_ctx *c) {
         SV_CK(c, cudaMallocHost(&c->bh->h_err, sizeof(int)));
     }
     Bh &B = *c->bh;
-    const int n = (int)c->n;
+    const int n = (int)c->S.n;
     Sorted &S = c->S;
     Tree *Tp = nullptr;
     SV_TRY(tree_build(c, kDepthAllSplit, 0, &Tp));

@@ -227,7 +227,7 @@ direct_fp64_kernel(const double *__restrict__ xs, const double *__restrict__ ys,
 }  // namespace
 
 sv_status direct_accel(sv_ctx *c) {
-    const int n = (int)c->n;
+    const int n = (int)c->S.n;
     Sorted &S = c->S;
     Images im{0, 1, nullptr};
     double *d_off = nullptr;

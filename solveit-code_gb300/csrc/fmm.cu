@@ -31,6 +31,7 @@
 #include <cfloat>
 
 #include <string>
+#include <vector>
 
 #include "fmm_tables.h"
 #include "sv_internal.cuh"
@@ -52,6 +53,13 @@ struct Fmm {
     size_t arena_bytes = 0;
     unsigned long long *d_counts = nullptr;  // [0] M2L translations, [1] P2P pairs
     unsigned long long *h_counts = nullptr;
+    // caller particles followed by their source-only symmetry images
+    double *ex = nullptr, *ey = nullptr, *ez = nullptr, *eq = nullptr, *em = nullptr, *eoff = nullptr;
+    int32_t *est = nullptr;
+    int64_t ecap = 0;
+    int eoff_cap = 0;
+    int *has_tgt = nullptr;  // per box of every level: box holds a target
+    int64_t tgt_cap = 0;
 };
 
 namespace {
@@ -141,6 +149,62 @@ __global__ void build_lists_kernel(int nbox, const int *__restrict__ parent, con
 
 __global__ void root_nbr_kernel(int *nbr, int ns) {
     if (threadIdx.x == 0 && blockIdx.x == 0) nbr[ns / 2] = 0;
+}
+
+// ------------------------------------------------------ symmetry images --
+// Image g of particle i at slot g*n + i: g = 0 is the particle itself; the
+// others are source-only copies (status 2) rotated by g*pi/2 about z
+// (rotational variant) or shifted by offset g (translational variant, zero
+// offset first).  Sources of status 1 or 2 keep being sources in every image;
+// ignored particles (0, -1) stay ignored.
+__global__ void expand_images_kernel(const double *__restrict__ x, const double *__restrict__ y,
+                                     const double *__restrict__ z, const double *__restrict__ q,
+                                     const double *__restrict__ m, const int32_t *__restrict__ st, int64_t n,
+                                     int kind, int nimg, const double *__restrict__ off, double *__restrict__ ex,
+                                     double *__restrict__ ey, double *__restrict__ ez, double *__restrict__ eq,
+                                     double *__restrict__ em, int32_t *__restrict__ est) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= n * nimg) return;
+    const int g = (int)(t / n);
+    const int64_t i = t - (int64_t)g * n;
+    double px = x[i], py = y[i], pz = z[i];
+    if (kind == 1) {
+        const double x0 = px, y0 = py;
+        if (g == 1) { px = -y0; py = x0; }
+        else if (g == 2) { px = -x0; py = -y0; }
+        else if (g == 3) { px = y0; py = -x0; }
+    } else if (kind == 2) {
+        px += off[3 * g];
+        py += off[3 * g + 1];
+        pz += off[3 * g + 2];
+    }
+    ex[t] = px;
+    ey[t] = py;
+    ez[t] = pz;
+    eq[t] = q[i];
+    em[t] = m[i];
+    const int32_t w = st[i];
+    est[t] = g == 0 ? w : ((w == 1 || w == 2) ? 2 : w);
+}
+
+// box holds at least one target (K q/m != 0): leaf level from particles,
+// coarser levels from children
+__global__ void leaf_targets_kernel(int nbox, const int *__restrict__ start, const double *__restrict__ qm,
+                                    int *__restrict__ flag) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbox) return;
+    int f = 0;
+    for (int j = start[b]; j < start[b + 1] && !f; j++) f = qm[j] != 0.0;
+    flag[b] = f;
+}
+
+__global__ void parent_targets_kernel(int nbox, const int *__restrict__ child0, const int *__restrict__ cflag,
+                                      int *__restrict__ flag) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nbox) return;
+    int f = 0;
+    for (int c = child0[b]; c < child0[b + 1] && !f; c++) f = cflag[c];
+    flag[b] = f;
 }
 
 // ------------------------------------------------------------------ P2M --
@@ -267,6 +331,7 @@ struct DownArgs {
     const double *root;
     double eps2;
     float2 *Lout;
+    const int *has_tgt;  // boxes without targets need no local expansion
 };
 
 template <int P>
@@ -275,7 +340,7 @@ __global__ void __launch_bounds__(kWarps * 32) down_kernel(DownArgs a) {
     __shared__ float2 A[kWarps][NC], B[kWarps][NC];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int b = blockIdx.x * kWarps + wid;
-    if (b >= a.nbox) return;
+    if (b >= a.nbox || !a.has_tgt[b]) return;
     // lane slots: coefficient lane and lane + 32, valid while < NC
     int cn[2], cm[2];
     cnm(min(lane, NC - 1), cn[0], cm[0]);
@@ -393,12 +458,12 @@ l2p_kernel(int nbox, const int *__restrict__ start, const int4 *__restrict__ coo
            const double *__restrict__ xs, const double *__restrict__ ys, const double *__restrict__ zs,
            const double *__restrict__ qm, const double *__restrict__ root, int level,
            const float *__restrict__ nrm, const float2 *__restrict__ Lc, double *__restrict__ ax,
-           double *__restrict__ ay, double *__restrict__ az) {
+           double *__restrict__ ay, double *__restrict__ az, const int *__restrict__ has_tgt) {
     constexpr int NC = ncoef(P);
     __shared__ float2 lam[kWarps][NC];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int b = blockIdx.x * kWarps + wid;
-    if (b >= nbox) return;
+    if (b >= nbox || !has_tgt[b]) return;
     for (int c = lane; c < NC; c += 32) {
         int n, m;
         cnm(c, n, m);
@@ -444,12 +509,12 @@ p2p_kernel(int nbox, const int *__restrict__ start, const int4 *__restrict__ coo
            const double *__restrict__ xs, const double *__restrict__ ys, const double *__restrict__ zs,
            const float *__restrict__ qs, const double *__restrict__ qm, const double *__restrict__ root,
            int level, float eps2, double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az,
-           unsigned long long *__restrict__ counts) {
+           unsigned long long *__restrict__ counts, const int *__restrict__ has_tgt) {
     constexpr int NS1 = 2 * WS + 1, NS = NS1 * NS1 * NS1;
     __shared__ float4 src[kWarps][32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int b = blockIdx.x * kWarps + wid;
-    if (b >= nbox) return;
+    if (b >= nbox || !has_tgt[b]) return;
     const double h = root[3] / (double)(1 << level);
     const int4 cb = coord[b];
     const double cx = root[0] + (cb.x + 0.5) * h, cy = root[1] + (cb.y + 0.5) * h, cz = root[2] + (cb.z + 0.5) * h;
@@ -547,6 +612,31 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
     SV_CK(c, cudaMemsetAsync(F.d_counts, 0, 2 * sizeof(unsigned long long), c->stream));
     root_nbr_kernel<<<1, 32, 0, c->stream>>>(nbr[0], ns);
     SV_LAUNCHED(c);
+    // which boxes hold targets (all of them unless symmetry images are present)
+    int *tgt[kMortonBits + 1];
+    {
+        int64_t tot = 0;
+        for (int l = 0; l <= L; l++) tot += T.lv[l].nbox;
+        if (F.tgt_cap < tot) {
+            cudaFree(F.has_tgt);
+            F.has_tgt = nullptr;
+            SV_CK(c, cudaMalloc(&F.has_tgt, sizeof(int) * tot));
+            F.tgt_cap = tot;
+        }
+        int64_t o = 0;
+        for (int l = 0; l <= L; l++) {
+            tgt[l] = F.has_tgt + o;
+            o += T.lv[l].nbox;
+        }
+        leaf_targets_kernel<<<div_up(T.lv[L].nbox, 256), 256, 0, c->stream>>>(T.lv[L].nbox, T.lv[L].start, S.qm,
+                                                                                tgt[L]);
+        SV_LAUNCHED(c);
+        for (int l = L - 1; l >= 0; l--) {
+            parent_targets_kernel<<<div_up(T.lv[l].nbox, 256), 256, 0, c->stream>>>(T.lv[l].nbox, T.lv[l].child0,
+                                                                                      tgt[l + 1], tgt[l]);
+            SV_LAUNCHED(c);
+        }
+    }
     for (int l = 1; l <= L; l++) {
         const Level &V = T.lv[l];
         const Level &U = T.lv[l - 1];
@@ -600,6 +690,7 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         a.root = S.root;
         a.eps2 = c->P.softening2;
         a.Lout = Lv[l];
+        a.has_tgt = tgt[l];
         down_kernel<P><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(a);
         SV_LAUNCHED(c);
     }
@@ -609,22 +700,22 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         const Level &V = T.lv[L];
         if (L >= 2) {
             l2p_kernel<P><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
-                V.nbox, V.start, V.coord, S.x, S.y, S.z, S.qm, S.root, L, F.nrm, Lv[L], S.ax, S.ay, S.az);
+                V.nbox, V.start, V.coord, S.x, S.y, S.z, S.qm, S.root, L, F.nrm, Lv[L], S.ax, S.ay, S.az, tgt[L]);
             SV_LAUNCHED(c);
         } else {
-            SV_CK(c, cudaMemsetAsync(S.ax, 0, sizeof(double) * c->n, c->stream));
-            SV_CK(c, cudaMemsetAsync(S.ay, 0, sizeof(double) * c->n, c->stream));
-            SV_CK(c, cudaMemsetAsync(S.az, 0, sizeof(double) * c->n, c->stream));
+            SV_CK(c, cudaMemsetAsync(S.ax, 0, sizeof(double) * c->S.n, c->stream));
+            SV_CK(c, cudaMemsetAsync(S.ay, 0, sizeof(double) * c->S.n, c->stream));
+            SV_CK(c, cudaMemsetAsync(S.az, 0, sizeof(double) * c->S.n, c->stream));
         }
         phase_mark(c, 6);
         if (ws == 1)
             p2p_kernel<1><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
                 V.nbox, V.start, V.coord, nbr[L], S.x, S.y, S.z, S.q, S.qm, S.root, L, (float)c->P.softening2,
-                S.ax, S.ay, S.az, F.d_counts);
+                S.ax, S.ay, S.az, F.d_counts, tgt[L]);
         else
             p2p_kernel<2><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
                 V.nbox, V.start, V.coord, nbr[L], S.x, S.y, S.z, S.q, S.qm, S.root, L, (float)c->P.softening2,
-                S.ax, S.ay, S.az, F.d_counts);
+                S.ax, S.ay, S.az, F.d_counts, tgt[L]);
         SV_LAUNCHED(c);
     }
     SV_CK(c, cudaMemcpyAsync(F.h_counts, F.d_counts, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
@@ -667,32 +758,93 @@ void fmm_free(sv_ctx *c) {
     Fmm &F = *c->fmm;
     cudaFree(F.cls_theta); cudaFree(F.cls_phase); cudaFree(F.cls_rho2); cudaFree(F.dmat);
     cudaFree(F.zc); cudaFree(F.nrm); cudaFree(F.oct); cudaFree(F.arena); cudaFree(F.d_counts);
+    cudaFree(F.ex); cudaFree(F.ey); cudaFree(F.ez); cudaFree(F.eq); cudaFree(F.em); cudaFree(F.est);
+    cudaFree(F.eoff); cudaFree(F.has_tgt);
     cudaFreeHost(F.h_counts);
     delete c->fmm;
     c->fmm = nullptr;
 }
 
-sv_status fmm_accel(sv_ctx *c) {
-    if (c->P.symmetry != SV_SYM_NONE)
-        return set_error(c, SV_ERR_UNSUPPORTED, "FMM with symmetry images is not built yet");
-    if (c->P.precision != SV_PREC_MIXED)
-        return set_error(c, SV_ERR_UNSUPPORTED, "FMM runs in mixed precision only");
-    const int p = c->P.fmm_order;
-    if (p != 4 && p != 6 && p != 8 && p != 10)
-        return set_error(c, SV_ERR_UNSUPPORTED, "FMM order %d not instantiated (4, 6, 8, 10)", p);
+static sv_status fmm_state(sv_ctx *c) {
     if (!c->fmm) {
         c->fmm = new Fmm();
         SV_CK(c, cudaMalloc(&c->fmm->d_counts, 2 * sizeof(unsigned long long)));
         SV_CK(c, cudaMallocHost(&c->fmm->h_counts, 2 * sizeof(unsigned long long)));
     }
+    return SV_OK;
+}
+
+sv_status fmm_sort_images(sv_ctx *c, int64_t first, int64_t last) {
+    SV_TRY(fmm_state(c));
+    Fmm &F = *c->fmm;
+    const int64_t n = c->n;
+    int kind = 0, nimg = 1;
+    std::vector<double> off;
+    if (c->P.symmetry == SV_SYM_ROTATIONAL) {
+        kind = 1;
+        nimg = 4;
+    } else if (c->P.symmetry == SV_SYM_TRANSLATIONAL) {
+        kind = 2;
+        std::vector<double> h(3 * 4096);
+        nimg = trans_images(c->P, h.data(), 4096);
+        if (nimg <= 0 || nimg > 4096) return set_error(c, SV_ERR_INVALID, "bad translational image set (%d)", nimg);
+        // the zero offset (the particles themselves) goes first
+        off.reserve(3 * nimg);
+        int zero = -1;
+        for (int g = 0; g < nimg; g++)
+            if (h[3 * g] == 0.0 && h[3 * g + 1] == 0.0 && h[3 * g + 2] == 0.0) zero = g;
+        if (zero < 0) return set_error(c, SV_ERR_INVALID, "image set without the zero offset");
+        off.insert(off.end(), {0.0, 0.0, 0.0});
+        for (int g = 0; g < nimg; g++)
+            if (g != zero) off.insert(off.end(), {h[3 * g], h[3 * g + 1], h[3 * g + 2]});
+    }
+    const int64_t ne = n * nimg;
+    if (ne > (int64_t)INT32_MAX) return set_error(c, SV_ERR_CAPACITY, "%lld particles with images", (long long)ne);
+    if (F.ecap < ne) {
+        cudaFree(F.ex); cudaFree(F.ey); cudaFree(F.ez); cudaFree(F.eq); cudaFree(F.em); cudaFree(F.est);
+        F.ex = F.ey = F.ez = F.eq = F.em = nullptr;
+        F.est = nullptr;
+        SV_CK(c, cudaMalloc(&F.ex, sizeof(double) * ne));
+        SV_CK(c, cudaMalloc(&F.ey, sizeof(double) * ne));
+        SV_CK(c, cudaMalloc(&F.ez, sizeof(double) * ne));
+        SV_CK(c, cudaMalloc(&F.eq, sizeof(double) * ne));
+        SV_CK(c, cudaMalloc(&F.em, sizeof(double) * ne));
+        SV_CK(c, cudaMalloc(&F.est, sizeof(int32_t) * ne));
+        F.ecap = ne;
+    }
+    if (kind == 2) {
+        if (F.eoff_cap < nimg) {
+            cudaFree(F.eoff);
+            F.eoff = nullptr;
+            SV_CK(c, cudaMalloc(&F.eoff, sizeof(double) * 3 * nimg));
+            F.eoff_cap = nimg;
+        }
+        SV_CK(c, cudaMemcpyAsync(F.eoff, off.data(), sizeof(double) * 3 * nimg, cudaMemcpyHostToDevice, c->stream));
+        // the host vector must outlive the copy
+        SV_CK(c, cudaStreamSynchronize(c->stream));
+    }
+    expand_images_kernel<<<div_up(ne, 256), 256, 0, c->stream>>>(c->x, c->y, c->z, c->q, c->m, c->status, n, kind,
+                                                                 nimg, F.eoff, F.ex, F.ey, F.ez, F.eq, F.em, F.est);
+    SV_LAUNCHED(c);
+    const ParticleView v{F.ex, F.ey, F.ez, F.eq, F.em, F.est, ne, n};
+    return sort_view(c, v, first, last);
+}
+
+sv_status fmm_accel(sv_ctx *c) {
+    if (c->P.precision != SV_PREC_MIXED)
+        return set_error(c, SV_ERR_UNSUPPORTED, "FMM runs in mixed precision only");
+    const int p = c->P.fmm_order;
+    if (p != 4 && p != 6 && p != 8 && p != 10)
+        return set_error(c, SV_ERR_UNSUPPORTED, "FMM order %d not instantiated (4, 6, 8, 10)", p);
+    SV_TRY(fmm_state(c));
     Fmm &F = *c->fmm;
     SV_TRY(ensure_tables(c, F, p, c->P.fmm_ws));
     Tree *T = nullptr;
     SV_TRY(tree_build(c, kDepthMeanOccupancy, c->P.fmm_leaf_target, &T));
     if (T->n_act == 0) {
-        SV_CK(c, cudaMemsetAsync(c->S.ax, 0, sizeof(double) * c->n, c->stream));
-        SV_CK(c, cudaMemsetAsync(c->S.ay, 0, sizeof(double) * c->n, c->stream));
-        SV_CK(c, cudaMemsetAsync(c->S.az, 0, sizeof(double) * c->n, c->stream));
+        SV_CK(c, cudaMemsetAsync(c->S.ax, 0, sizeof(double) * c->S.n, c->stream));
+        SV_CK(c, cudaMemsetAsync(c->S.ay, 0, sizeof(double) * c->S.n, c->stream));
+        SV_CK(c, cudaMemsetAsync(c->S.az, 0, sizeof(double) * c->S.n, c->stream));
         return SV_OK;
     }
     switch (p) {

@@ -8,6 +8,8 @@
 // reference requires of updateAcceleration.
 #include <cub/device/device_radix_sort.cuh>
 
+#include <algorithm>
+
 #include "sv_internal.cuh"
 
 namespace sv {
@@ -151,13 +153,16 @@ __global__ void gather_sorted(const uint32_t *__restrict__ idx, int64_t n,
     qm[s] = tgt ? kconst * q[i] / m[i] : 0.0;
 }
 
-__global__ void scatter_accel(const uint32_t *__restrict__ idx, int64_t n,
+// sorted slots of image copies (index >= n_orig) are sources only and have
+// no place in the caller's arrays
+__global__ void scatter_accel(const uint32_t *__restrict__ idx, int64_t n, int64_t n_orig,
                               const double *__restrict__ axs, const double *__restrict__ ays,
                               const double *__restrict__ azs, double *__restrict__ ax,
                               double *__restrict__ ay, double *__restrict__ az) {
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (s >= n) return;
     const uint32_t i = idx[s];
+    if ((int64_t)i >= n_orig) return;
     ax[i] = axs[s];
     ay[i] = ays[s];
     az[i] = azs[s];
@@ -199,16 +204,18 @@ sv_status ensure_sorted_capacity(sv_ctx *c, int64_t n) {
     return SV_OK;
 }
 
-sv_status sort_state(sv_ctx *c, int64_t first, int64_t last) {
-    const int64_t n = c->n;
+sv_status sort_view(sv_ctx *c, const ParticleView &v, int64_t first, int64_t last) {
+    const int64_t n = v.n;
     SV_TRY(ensure_sorted_capacity(c, n));
     Sorted &S = c->S;
+    S.n = n;
+    S.n_orig = v.n_orig;
     const int nb = div_up(n, 256);
-    bbox_partial<<<S.red_blocks, kRedThreads, 0, c->stream>>>(c->x, c->y, c->z, c->status, n, S.red);
+    bbox_partial<<<S.red_blocks, kRedThreads, 0, c->stream>>>(v.x, v.y, v.z, v.status, n, S.red);
     SV_LAUNCHED(c);
     bbox_final<<<1, 32, 0, c->stream>>>(S.red, S.red_blocks, S.root);
     SV_LAUNCHED(c);
-    morton_keys<<<nb, 256, 0, c->stream>>>(c->x, c->y, c->z, c->status, n, S.root, S.keys, S.idx);
+    morton_keys<<<nb, 256, 0, c->stream>>>(v.x, v.y, v.z, v.status, n, S.root, S.keys, S.idx);
     SV_LAUNCHED(c);
     cub::DoubleBuffer<uint64_t> kb(S.keys, S.keys_alt);
     cub::DoubleBuffer<uint32_t> vb(S.idx, S.idx_alt);
@@ -222,16 +229,21 @@ sv_status sort_state(sv_ctx *c, int64_t first, int64_t last) {
     if (vb.Current() != S.idx) {
         std::swap(S.idx, S.idx_alt);
     }
-    gather_sorted<<<nb, 256, 0, c->stream>>>(S.idx, n, c->x, c->y, c->z, c->q, c->m, c->status, first,
-                                             last, c->P.k_const, S.x, S.y, S.z, S.q, S.qm);
+    gather_sorted<<<nb, 256, 0, c->stream>>>(S.idx, n, v.x, v.y, v.z, v.q, v.m, v.status, first,
+                                             std::min(last, v.n_orig), c->P.k_const, S.x, S.y, S.z, S.q, S.qm);
     SV_LAUNCHED(c);
     return SV_OK;
 }
 
+sv_status sort_state(sv_ctx *c, int64_t first, int64_t last) {
+    const ParticleView v{c->x, c->y, c->z, c->q, c->m, c->status, c->n, c->n};
+    return sort_view(c, v, first, last);
+}
+
 sv_status unsort_accel(sv_ctx *c) {
-    const int64_t n = c->n;
-    scatter_accel<<<div_up(n, 256), 256, 0, c->stream>>>(c->S.idx, n, c->S.ax, c->S.ay, c->S.az, c->ax,
-                                                         c->ay, c->az);
+    const int64_t n = c->S.n;
+    scatter_accel<<<div_up(n, 256), 256, 0, c->stream>>>(c->S.idx, n, c->S.n_orig, c->S.ax, c->S.ay, c->S.az,
+                                                         c->ax, c->ay, c->az);
     SV_LAUNCHED(c);
     return SV_OK;
 }

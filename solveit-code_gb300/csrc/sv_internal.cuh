@@ -33,6 +33,16 @@ struct Sorted {
     double *red = nullptr;     // device reduction scratch
     int red_blocks = 0;
     int64_t cap = 0;
+    int64_t n = 0;       // sorted entries (caller particles plus any image copies)
+    int64_t n_orig = 0;  // caller particles; sorted idx >= n_orig are image copies
+};
+
+// particle arrays to sort: the caller's state, or the caller's particles
+// followed by source-only image copies (indices >= n_orig)
+struct ParticleView {
+    const double *x, *y, *z, *q, *m;
+    const int32_t *status;
+    int64_t n, n_orig;
 };
 
 struct Fmm;   // fmm.cu
@@ -113,6 +123,7 @@ inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 sv_status ensure_sorted_capacity(sv_ctx *c, int64_t n);
 // Morton-sort the live plume into c->S (targets: inbound with index in [first,last)).
 sv_status sort_state(sv_ctx *c, int64_t first, int64_t last);
+sv_status sort_view(sv_ctx *c, const ParticleView &v, int64_t first, int64_t last);
 // Scatter c->S.a{x,y,z} back to caller order into c->a{x,y,z}.
 sv_status unsort_accel(sv_ctx *c);
 // Read root box (origin, side) to the host (blocking).
@@ -129,6 +140,8 @@ cudaError_t launch_direct_mixed_sorted(const double *xs, const double *ys, const
 // tree.cu / bh.cu / fmm.cu
 sv_status bh_accel(sv_ctx *c);
 sv_status fmm_accel(sv_ctx *c);
+// FMM with symmetry images: sorts the caller's particles plus their images
+sv_status fmm_sort_images(sv_ctx *c, int64_t first, int64_t last);
 void tree_free(sv_ctx *c);
 void fmm_free(sv_ctx *c);
 void bh_free(sv_ctx *c);

@@ -151,7 +151,7 @@ void tree_free(sv_ctx *c) {
 
 // Histogram of split levels and count of active particles (one readback).
 static sv_status tree_levels(sv_ctx *c, Tree &T) {
-    const int n = (int)c->n;
+    const int n = (int)c->S.n;
     if (T.cap < n) {
         cudaFree(T.lvl); cudaFree(T.scratch); cudaFree(T.cub_tmp);
         T.lvl = nullptr; T.scratch = nullptr; T.cub_tmp = nullptr;

@@ -91,3 +91,30 @@ def test_fmm_leapfrog_tracks_direct():
         x, v, _ = fm.download()
     dv = np.linalg.norm(v - vr, axis=1) / np.linalg.norm(vr - st["v"], axis=1)
     assert np.sqrt(np.mean(dv ** 2)) < 1e-5
+
+
+@pytest.mark.parametrize("sym", [1, 2])
+def test_fmm_symmetry_images(sym):
+    """Rotational (4 quadrant images) and translational (x, y periodic, 81
+    images) variants: the images join the tree as source-only particles."""
+    st = plume.make_plume(4096, 1e-6, 71)
+    st["x"][:, 0] += 3e-8
+    img = O.trans_images(2, (1, 1, 0)) * np.array([2e-6, 2e-6, 0.0]) if sym == 2 else None
+    ref = O.direct_f64(st, EPS20, sym=sym, img_off=img)
+    a, s = run_accel(st, softening2=EPS20, method=sv.FMM, fmm_order=8, fmm_ws=2, symmetry=sym,
+                     sym_axes=(1, 1, 0), sym_levels=2, domain_size=(2e-6, 2e-6, 0.0))
+    assert rel_l2(a, ref, st["status"]) < 1e-5
+
+
+def test_fmm_rotational_status_and_range():
+    st = plume.make_plume(3000, 1e-6, 72)
+    st["x"][:, 1] += 2e-8
+    st["status"][:50] = 2
+    st["status"][50:80] = 0
+    ref = O.direct_f64(st, EPS20, sym=1)
+    with sv.ForceMethod(softening2=EPS20, method=sv.FMM, fmm_order=8, fmm_ws=2, symmetry=1) as fm:
+        fm.upload(st)
+        a = fm.accel(first=0, last=2000)
+    assert np.all(a[:80] == 0.0) and np.all(a[2000:] == 0.0)
+    live = np.arange(80, 2000)
+    assert rel_l2(a[live], ref[live], st["status"][live]) < 1e-5
