@@ -56,6 +56,20 @@ WORKLOADS = {
 }
 
 
+def plume_seed(wl, rank):
+    """Replicas: every rank integrates its own realisation of the workload."""
+    return wl["seed"] * 1000 + rank
+
+
+def max_over_ranks(value, dist, device):
+    """Slowest rank's time: the whole job is done when the last replica is."""
+    import torch
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -167,7 +181,7 @@ def run_ours(args, wl, rank, world, local):
 
         dist.init_process_group("nccl")
     n = wl["n"]
-    st = plume.make_plume(n, wl["length"], wl["seed"] * 1000 + rank)
+    st = plume.make_plume(n, wl["length"], plume_seed(wl, rank))
     if wl["method"] == "fmm":
         kw = dict(method=sv.FMM, precision=sv.MIXED, fmm_order=wl["order"], fmm_ws=wl["ws"],
                   fmm_leaf_target=wl["leaf"])
@@ -208,9 +222,7 @@ def run_ours(args, wl, rank, world, local):
     clocks = sample_clocks_stop(clk_p, clk_f, local)
     step_ms = float(sum(a.elapsed_time(b) for a, b in evs))
     if dist:
-        tt = torch.tensor([step_ms], device=f"cuda:{local}")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        step_ms = float(tt.item())
+        step_ms = max_over_ranks(step_ms, dist, f"cuda:{local}")
     ms_per_step = step_ms / args.steps
     value = world * n * args.steps / (step_ms / 1e3)
     phase_ms /= args.steps
@@ -256,9 +268,7 @@ def run_ours(args, wl, rank, world, local):
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - e0
     if dist:
-        tt = torch.tensor([e2e_s], device=f"cuda:{local}")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+        e2e_s = max_over_ranks(e2e_s, dist, f"cuda:{local}")
     h2d = n * (3 * 8 + 3 * 8 + 8 + 8 + 4 + 8)
     d2h = n * (3 * 8 + 3 * 8 + 4)
     e2e = {"value": world * n * args.steps / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
