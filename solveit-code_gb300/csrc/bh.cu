@@ -301,7 +301,7 @@ sv_status bh_accel(sv_ctx *c) {
     const int n = (int)c->S.n;
     Sorted &S = c->S;
     Tree *Tp = nullptr;
-    SV_TRY(tree_build(c, kDepthAllSplit, 0, &Tp));
+    SV_TRY(tree_build(c, kDepthAllSplit, c->P.leaf_size, &Tp));
     Tree &T = *Tp;
     phase_mark(c, 2);
     phase_mark(c, 3);

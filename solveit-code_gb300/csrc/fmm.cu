@@ -19,8 +19,9 @@
 //   L2P   leaf boxes, lanes over particles: gradient of the local expansion.
 //   P2P   leaf boxes, lanes over targets, source chunks staged in shared
 //         memory as FP32 offsets from the target box centre (FP64 subtraction
-//         once per staged source); per-source-box FP32 partial sums are added
-//         into FP64 accumulators.
+//         once per staged source); a box's short tail chunk of targets spreads
+//         each target over a group of lanes that split the sources; per-source-
+//         box FP32 partial sums are accumulated with Kahan compensation.
 //
 // Expansions are kept in box units (coordinates divided by the box side h),
 // so the M2L tables depend on the integer offset only; the softened M2L
@@ -60,6 +61,8 @@ struct Fmm {
     int eoff_cap = 0;
     int *has_tgt = nullptr;  // per box of every level: box holds a target
     int64_t tgt_cap = 0;
+    float4 *rel = nullptr;   // particle offset from its leaf box centre (FP32) + charge
+    int64_t rel_cap = 0;
 };
 
 namespace {
@@ -334,6 +337,61 @@ struct DownArgs {
     const int *has_tgt;  // boxes without targets need no local expansion
 };
 
+// rows of the coefficients held in slot 1 (the EXTRA lowest coefficients)
+template <int P>
+__host__ __device__ constexpr int slot1_rows() {
+    constexpr int NC = ncoef(P);
+    if (NC <= 32) return 1;
+    int n = 0;
+    while ((n + 1) * (n + 2) / 2 < NC - 32) n++;
+    return n + 1;
+}
+
+// One output (n, mp) of a folded y-rotation: real part from the E block (rows
+// of n+1), imaginary part from the O block (rows of n, mp >= 1).  Unrolled to
+// the compile-time bound MAXN with the row length n applied as a predicate.
+template <int MAXN>
+__device__ __forceinline__ float2 rot_row(const float *__restrict__ D, int eoff, int ooff, const float2 *A, int n,
+                                          int mp) {
+    const float *E = D + eoff + (n * (n + 1) * (2 * n + 1)) / 6 + mp * (n + 1);
+    const float2 *An = A + cidx(n, 0);
+    float re = 0.f, im = 0.f;
+#pragma unroll
+    for (int m = 0; m < MAXN; m++)
+        if (m <= n) re = fmaf(E[m], An[m].x, re);
+    if (mp > 0) {
+        const float *O = D + ooff + ((n - 1) * n * (2 * n - 1)) / 6 + (mp - 1) * n;
+#pragma unroll
+        for (int m = 1; m < MAXN; m++)
+            if (m <= n) im = fmaf(O[m - 1], An[m].y, im);
+    }
+    return make_float2(re, im);
+}
+
+// One output (j, k) of the translation along z:
+// L'_j^k = sum_{n >= k} C[k][j][n] rho^-(j+n+1) M'_n^k
+template <int P>
+__device__ __forceinline__ float2 ztrans_row(const float *__restrict__ zc, const float2 *B, int j, int k,
+                                             float inv_rho) {
+    const float *Z = zc + ((size_t)k * P + j) * P;
+    float ip = inv_rho;
+#pragma unroll
+    for (int q = 0; q < 2 * P - 2; q++)
+        if (q < j + k) ip *= inv_rho;  // rho^-(j+k+1)
+    float re = 0.f, im = 0.f;
+#pragma unroll
+    for (int n = 0; n < P; n++) {
+        if (n >= k) {
+            const float2 v = B[cidx(n, k)];
+            const float f = Z[n] * ip;
+            re = fmaf(f, v.x, re);
+            im = fmaf(f, v.y, im);
+            ip *= inv_rho;
+        }
+    }
+    return make_float2(re, im);
+}
+
 template <int P>
 __global__ void __launch_bounds__(kWarps * 32) down_kernel(DownArgs a) {
     constexpr int NC = ncoef(P), W = 2 * P - 1;
@@ -341,11 +399,16 @@ __global__ void __launch_bounds__(kWarps * 32) down_kernel(DownArgs a) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int b = blockIdx.x * kWarps + wid;
     if (b >= a.nbox || !a.has_tgt[b]) return;
-    // lane slots: coefficient lane and lane + 32, valid while < NC
+    // Lane slots.  Slot 0 of every lane holds one of the NC - EXTRA highest
+    // coefficients; slot 1 of the first EXTRA lanes holds one of the EXTRA
+    // lowest (cheapest) coefficients, so the second pass is short.
+    constexpr int EXTRA = NC > 32 ? NC - 32 : 0;
+    const int c0 = lane + EXTRA, c1 = lane;
     int cn[2], cm[2];
-    cnm(min(lane, NC - 1), cn[0], cm[0]);
-    cnm(min(lane + 32, NC - 1), cn[1], cm[1]);
-    const bool has[2] = {lane < NC, lane + 32 < NC};
+    cnm(min(c0, NC - 1), cn[0], cm[0]);
+    cnm(min(c1, NC - 1), cn[1], cm[1]);
+    const int cs[2] = {c0, c1};
+    const bool has[2] = {c0 < NC, lane < EXTRA};
     float2 acc[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
     // ---- L2L from the parent (parent box units -> child box units)
     if (a.has_parent) {
@@ -361,7 +424,7 @@ __global__ void __launch_bounds__(kWarps * 32) down_kernel(DownArgs a) {
         __syncwarp();
 #pragma unroll
         for (int t = 0; t < 2; t++) {
-            if (!has[t]) break;
+            if (!has[t]) continue;
             const int k = cn[t], l = cm[t];
             float2 s = make_float2(0.f, 0.f);
             for (int n = k; n < P; n++) {
@@ -391,64 +454,31 @@ __global__ void __launch_bounds__(kWarps * 32) down_kernel(DownArgs a) {
 #pragma unroll
         for (int t = 0; t < 2; t++) {
             if (!has[t]) break;
-            const int c = lane + 32 * t;
-            A[wid][c] = cmul(a.Ml[(size_t)src * NC + c], ph[cm[t]]);
+            A[wid][cs[t]] = cmul(a.Ml[(size_t)src * NC + cs[t]], ph[cm[t]]);
         }
         __syncwarp();
-        // forward y-rotation (folded real matrices)
-#pragma unroll
-        for (int t = 0; t < 2; t++) {
-            if (!has[t]) break;
-            const int n = cn[t], mp = cm[t];
-            const float *E = D + (n * (n + 1) * (2 * n + 1)) / 6 + mp * (n + 1);
-            float re = 0.f, im = 0.f;
-            const float2 *An = &A[wid][cidx(n, 0)];
-            for (int m = 0; m <= n; m++) re = fmaf(E[m], An[m].x, re);
-            if (mp > 0) {
-                const float *O = D + a.esz + ((n - 1) * n * (2 * n - 1)) / 6 + (mp - 1) * n;
-                for (int m = 1; m <= n; m++) im = fmaf(O[m - 1], An[m].y, im);
-            }
-            B[wid][lane + 32 * t] = make_float2(re, im);
-        }
+        // forward y-rotation (folded real matrices), fully unrolled and predicated
+        if (has[0]) B[wid][cs[0]] = rot_row<P>(D, 0, a.esz, &A[wid][0], cn[0], cm[0]);
+        if (has[1]) B[wid][cs[1]] = rot_row<slot1_rows<P>()>(D, 0, a.esz, &A[wid][0], cn[1], cm[1]);
         __syncwarp();
         // translation along z: L'_j^k = sum_n C[k][j][n] rho^-(j+n+1) M'_n^k
-#pragma unroll
-        for (int t = 0; t < 2; t++) {
-            if (!has[t]) break;
-            const int j = cn[t], k = cm[t];
-            const float *Z = a.zc + ((size_t)k * P + j) * P;
-            float ip = inv_rho;
-            for (int q = 0; q < j + k; q++) ip *= inv_rho;  // rho^-(j+k+1)
-            float re = 0.f, im = 0.f;
-            for (int n = k; n < P; n++) {
-                const float2 v = B[wid][cidx(n, k)];
-                const float f = Z[n] * ip;
-                re = fmaf(f, v.x, re);
-                im = fmaf(f, v.y, im);
-                ip *= inv_rho;
-            }
-            A[wid][lane + 32 * t] = make_float2(re, im);
-        }
+        if (has[0]) A[wid][cs[0]] = ztrans_row<P>(a.zc, &B[wid][0], cn[0], cm[0], inv_rho);
+        if (has[1]) A[wid][cs[1]] = ztrans_row<P>(a.zc, &B[wid][0], cn[1], cm[1], inv_rho);
         __syncwarp();
         // backward y-rotation and phase e^{-i k phi}
-#pragma unroll
-        for (int t = 0; t < 2; t++) {
-            if (!has[t]) break;
-            const int n = cn[t], mp = cm[t];
-            const float *E = D + a.esz + a.osz + (n * (n + 1) * (2 * n + 1)) / 6 + mp * (n + 1);
-            float re = 0.f, im = 0.f;
-            const float2 *An = &A[wid][cidx(n, 0)];
-            for (int m = 0; m <= n; m++) re = fmaf(E[m], An[m].x, re);
-            if (mp > 0) {
-                const float *O = D + 2 * a.esz + a.osz + ((n - 1) * n * (2 * n - 1)) / 6 + (mp - 1) * n;
-                for (int m = 1; m <= n; m++) im = fmaf(O[m - 1], An[m].y, im);
-            }
-            acc[t] = cadd(acc[t], cmul(make_float2(re, im), cconj(ph[mp])));
+        if (has[0]) {
+            const float2 r = rot_row<P>(D, a.esz + a.osz, 2 * a.esz + a.osz, &A[wid][0], cn[0], cm[0]);
+            acc[0] = cadd(acc[0], cmul(r, cconj(ph[cm[0]])));
+        }
+        if (has[1]) {
+            const float2 r =
+                rot_row<slot1_rows<P>()>(D, a.esz + a.osz, 2 * a.esz + a.osz, &A[wid][0], cn[1], cm[1]);
+            acc[1] = cadd(acc[1], cmul(r, cconj(ph[cm[1]])));
         }
         __syncwarp();
     }
-    if (has[0]) a.Lout[(size_t)b * NC + lane] = acc[0];
-    if (has[1]) a.Lout[(size_t)b * NC + lane + 32] = acc[1];
+    if (has[0]) a.Lout[(size_t)b * NC + cs[0]] = acc[0];
+    if (has[1]) a.Lout[(size_t)b * NC + cs[1]] = acc[1];
 }
 
 // ------------------------------------------------------------------ L2P --
@@ -503,64 +533,131 @@ l2p_kernel(int nbox, const int *__restrict__ start, const int4 *__restrict__ coo
 }
 
 // ------------------------------------------------------------------ P2P --
+// Each particle once as an FP32 offset from the centre of its own leaf box
+// (one FP64 subtraction per particle) with its charge: the P2P kernel then
+// forms source offsets from the target box centre as offset + k*h in FP32.
+__global__ void __launch_bounds__(kWarps * 32)
+box_relative_kernel(int nbox, const int *__restrict__ start, const int4 *__restrict__ coord,
+                    const double *__restrict__ xs, const double *__restrict__ ys, const double *__restrict__ zs,
+                    const float *__restrict__ qs, const double *__restrict__ root, int level,
+                    float4 *__restrict__ rel) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int b = blockIdx.x * kWarps + wid;
+    if (b >= nbox) return;
+    const double h = root[3] / (double)(1 << level);
+    const int4 cb = coord[b];
+    const double cx = root[0] + (cb.x + 0.5) * h, cy = root[1] + (cb.y + 0.5) * h, cz = root[2] + (cb.z + 0.5) * h;
+    for (int j = start[b] + lane; j < start[b + 1]; j += 32)
+        rel[j] = make_float4((float)(xs[j] - cx), (float)(ys[j] - cy), (float)(zs[j] - cz), qs[j]);
+}
+
 template <int WS>
 __global__ void __launch_bounds__(kWarps * 32)
 p2p_kernel(int nbox, const int *__restrict__ start, const int4 *__restrict__ coord, const int *__restrict__ nbr,
            const double *__restrict__ xs, const double *__restrict__ ys, const double *__restrict__ zs,
            const float *__restrict__ qs, const double *__restrict__ qm, const double *__restrict__ root,
            int level, float eps2, double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az,
-           unsigned long long *__restrict__ counts, const int *__restrict__ has_tgt) {
+           unsigned long long *__restrict__ counts, const int *__restrict__ has_tgt,
+           const float4 *__restrict__ rel) {
     constexpr int NS1 = 2 * WS + 1, NS = NS1 * NS1 * NS1;
     __shared__ float4 src[kWarps][32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int b = blockIdx.x * kWarps + wid;
     if (b >= nbox || !has_tgt[b]) return;
-    const double h = root[3] / (double)(1 << level);
+    const float hf = (float)(root[3] / (double)(1 << level));  // a power of two: k * hf is exact
     const int4 cb = coord[b];
-    const double cx = root[0] + (cb.x + 0.5) * h, cy = root[1] + (cb.y + 0.5) * h, cz = root[2] + (cb.z + 0.5) * h;
     const int t0 = start[b], t1 = start[b + 1];
     unsigned long long pairs = 0;
     for (int tb = t0; tb < t1; tb += 32) {
-        const int i = tb + lane;
-        const bool valid = i < t1;
-        const int ii = valid ? i : t0;
-        const float tx = (float)(xs[ii] - cx), ty = (float)(ys[ii] - cy), tz = (float)(zs[ii] - cz);
-        double sx = 0.0, sy = 0.0, sz = 0.0;
+        // nt targets in this chunk; each gets a group of g lanes (g a power of
+        // two, nt * g <= 32) that split the sources, so a box's short tail
+        // chunk keeps the warp busy instead of idling 32 - nt lanes
+        const int nt = min(32, t1 - tb);
+        int lg = 0;
+        while ((nt << (lg + 1)) <= 32) lg++;
+        const int g = 1 << lg;
+        const int tloc = lane >> lg, sub = lane & (g - 1);
+        const bool valid = tloc < nt;
+        const int i = tb + (valid ? tloc : 0);
+        const float4 ti = rel[i];
+        const float tx = ti.x, ty = ti.y, tz = ti.z;
+        // per-source-box FP32 partial sums, accumulated across source boxes
+        // with Kahan compensation (FP64-level accuracy without FP64 ops)
+        float sx = 0.f, sy = 0.f, sz = 0.f, ex = 0.f, ey = 0.f, ez = 0.f;
         for (int s = 0; s < NS; s++) {
             const int Q = nbr[b * NS + s];
             if (Q < 0) continue;
             const int j0 = start[Q], j1 = start[Q + 1];
-            if (lane == 0) pairs += (unsigned long long)(j1 - j0) * (unsigned long long)min(32, t1 - tb);
+            if (lane == 0) pairs += (unsigned long long)(j1 - j0) * (unsigned long long)nt;
+            // source box centre relative to the target box centre, exact in FP32
+            const int4 cq = coord[Q];
+            const float ox = (float)(cq.x - cb.x) * hf, oy = (float)(cq.y - cb.y) * hf, oz = (float)(cq.z - cb.z) * hf;
             float fx = 0.f, fy = 0.f, fz = 0.f;
             for (int jb = j0; jb < j1; jb += 32) {
                 const int j = jb + lane;
                 float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (j < j1) v = make_float4((float)(xs[j] - cx), (float)(ys[j] - cy), (float)(zs[j] - cz), qs[j]);
+                if (j < j1) {
+                    const float4 r = rel[j];
+                    v = make_float4(r.x + ox, r.y + oy, r.z + oz, r.w);
+                }
                 src[wid][lane] = v;
                 __syncwarp();
                 const int cnt = min(32, j1 - jb);
-                for (int k = 0; k < cnt; k++) {
-                    const float4 u = src[wid][k];
-                    const float dx = tx - u.x, dy = ty - u.y, dz = tz - u.z;
-                    float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-                    r2 = fmaxf(r2, FLT_MIN);
-                    const float inv = rsqrtf(r2);
-                    const float w = u.w * inv * inv * inv;
-                    fx = fmaf(dx, w, fx);
-                    fy = fmaf(dy, w, fy);
-                    fz = fmaf(dz, w, fz);
+                if (g == 1) {
+                    // full chunk: every lane a target, all staged sources (zero-charge padding)
+#pragma unroll 8
+                    for (int k = 0; k < 32; k++) {
+                        const float4 u = src[wid][k];
+                        const float dx = tx - u.x, dy = ty - u.y, dz = tz - u.z;
+                        const float r2 = fmaxf(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2))), kMinR2);
+                        const float inv = rsqrtf(r2);
+                        const float w = u.w * inv * inv * inv;
+                        fx = fmaf(dx, w, fx);
+                        fy = fmaf(dy, w, fy);
+                        fz = fmaf(dz, w, fz);
+                    }
+                } else {
+                    for (int k = sub; k < cnt; k += g) {
+                        const float4 u = src[wid][k];
+                        const float dx = tx - u.x, dy = ty - u.y, dz = tz - u.z;
+                        const float r2 = fmaxf(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2))), kMinR2);
+                        const float inv = rsqrtf(r2);
+                        const float w = u.w * inv * inv * inv;
+                        fx = fmaf(dx, w, fx);
+                        fy = fmaf(dy, w, fy);
+                        fz = fmaf(dz, w, fz);
+                    }
                 }
                 __syncwarp();
             }
-            sx += fx;
-            sy += fy;
-            sz += fz;
+            {
+                float y = fx - ex, t = sx + y;
+                ex = (t - sx) - y;
+                sx = t;
+                y = fy - ey;
+                t = sy + y;
+                ey = (t - sy) - y;
+                sy = t;
+                y = fz - ez;
+                t = sz + y;
+                ez = (t - sz) - y;
+                sz = t;
+            }
         }
-        if (valid) {
+        sx -= ex;
+        sy -= ey;
+        sz -= ez;
+        // combine the g lanes of each target
+        for (int o = g >> 1; o > 0; o >>= 1) {
+            sx += __shfl_xor_sync(0xffffffffu, sx, o);
+            sy += __shfl_xor_sync(0xffffffffu, sy, o);
+            sz += __shfl_xor_sync(0xffffffffu, sz, o);
+        }
+        if (valid && sub == 0) {
             const double c = qm[i];
-            ax[i] += sx * c;
-            ay[i] += sy * c;
-            az[i] += sz * c;
+            ax[i] += (double)sx * c;
+            ay[i] += (double)sy * c;
+            az[i] += (double)sz * c;
         }
     }
     if (lane == 0 && pairs) atomicAdd(&counts[1], pairs);
@@ -708,14 +805,23 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
             SV_CK(c, cudaMemsetAsync(S.az, 0, sizeof(double) * c->S.n, c->stream));
         }
         phase_mark(c, 6);
+        if (F.rel_cap < c->S.n) {
+            cudaFree(F.rel);
+            F.rel = nullptr;
+            SV_CK(c, cudaMalloc(&F.rel, sizeof(float4) * c->S.n));
+            F.rel_cap = c->S.n;
+        }
+        box_relative_kernel<<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
+            V.nbox, V.start, V.coord, S.x, S.y, S.z, S.q, S.root, L, F.rel);
+        SV_LAUNCHED(c);
         if (ws == 1)
             p2p_kernel<1><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
                 V.nbox, V.start, V.coord, nbr[L], S.x, S.y, S.z, S.q, S.qm, S.root, L, (float)c->P.softening2,
-                S.ax, S.ay, S.az, F.d_counts, tgt[L]);
+                S.ax, S.ay, S.az, F.d_counts, tgt[L], F.rel);
         else
             p2p_kernel<2><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
                 V.nbox, V.start, V.coord, nbr[L], S.x, S.y, S.z, S.q, S.qm, S.root, L, (float)c->P.softening2,
-                S.ax, S.ay, S.az, F.d_counts, tgt[L]);
+                S.ax, S.ay, S.az, F.d_counts, tgt[L], F.rel);
         SV_LAUNCHED(c);
     }
     SV_CK(c, cudaMemcpyAsync(F.h_counts, F.d_counts, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
@@ -759,7 +865,7 @@ void fmm_free(sv_ctx *c) {
     cudaFree(F.cls_theta); cudaFree(F.cls_phase); cudaFree(F.cls_rho2); cudaFree(F.dmat);
     cudaFree(F.zc); cudaFree(F.nrm); cudaFree(F.oct); cudaFree(F.arena); cudaFree(F.d_counts);
     cudaFree(F.ex); cudaFree(F.ey); cudaFree(F.ez); cudaFree(F.eq); cudaFree(F.em); cudaFree(F.est);
-    cudaFree(F.eoff); cudaFree(F.has_tgt);
+    cudaFree(F.eoff); cudaFree(F.has_tgt); cudaFree(F.rel);
     cudaFreeHost(F.h_counts);
     delete c->fmm;
     c->fmm = nullptr;

@@ -14,6 +14,11 @@ namespace sv {
 constexpr int kNumSMs = 152;          // GB300: 2 dies x 76 SMs
 constexpr int kMortonBits = 21;       // bits per axis of the Morton key (63-bit keys)
 constexpr uint64_t kInactiveKey = ~0ull;
+// Floor of r^2 + eps^2 (m^2) in the FP32 pair kernels: 1e-24 keeps 1/r^3 below
+// FP32 overflow, so a zero-distance pair (the self pair, or zero-charge tile
+// padding) contributes 0 * finite = 0 even with eps = 0; it only alters pairs
+// closer than 1 pm.
+constexpr float kMinR2 = 1e-24f;
 
 // Morton-sorted working copy of the plume, rebuilt at every force evaluation.
 // Sorting makes every block of consecutive targets spatially compact, which is

@@ -14,9 +14,6 @@
 // level at which particle i and i-1 fall into different boxes (from the
 // highest differing bit of their Morton keys): particle i starts a box at
 // every level >= lvl[i].
-#include <cub/device/device_scan.cuh>
-#include <cub/device/device_select.cuh>
-
 #include <algorithm>
 #include <vector>
 
@@ -65,45 +62,37 @@ __global__ void split_levels(const uint64_t *__restrict__ keys, int n, uint8_t *
     if (threadIdx.x <= kLevels && sh[threadIdx.x]) atomicAdd(&hist[threadIdx.x], sh[threadIdx.x]);
 }
 
-// flag[i] = particle i (i < n_act) starts a box at level L
-__global__ void flag_particles(const uint8_t *__restrict__ lvl, int n_act, int L, int *__restrict__ flag) {
+constexpr int kBuildThreads = 1024;  // particles per CTA of the level builder
+
+// Deepest level at which some box still holds more than `leaf` particles, as
+// max_i min(lvl[i+1 .. i+leaf]): a window of leaf+1 consecutive particles
+// without a box boundary at level <= l means a box of level l with more than
+// `leaf` particles.  Slots past the active particles count as boundaries.
+__global__ void window_depth(const uint8_t *__restrict__ lvl, int n, int leaf, int *__restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n_act) flag[i] = (i == 0 || lvl[i] <= L) ? 1 : 0;
-}
-
-// flag[b] = level-(l+1) box b starts a box at level l
-__global__ void flag_boxes(const int *__restrict__ start_fine, const uint8_t *__restrict__ lvl, int nfine, int l,
-                           int *__restrict__ flag) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b < nfine) flag[b] = (b == 0 || lvl[start_fine[b]] <= l) ? 1 : 0;
-}
-
-__global__ void iota_kernel(int *__restrict__ a, int n) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) a[i] = i;
-}
-
-// level-l box b: start particle = start of its first child (or itself at the
-// leaf level), close the range arrays, parent of the finer boxes.
-__global__ void finish_level(const int *__restrict__ sel, int nbox, const int *__restrict__ start_fine,
-                             int n_act, int is_leaf_level, int *__restrict__ start, int *__restrict__ child0,
-                             int nfine) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b < nbox) {
-        const int s = sel[b];
-        start[b] = is_leaf_level ? s : start_fine[s];
-        if (!is_leaf_level) child0[b] = s;
+    int m = 0;
+    if (i < n) {
+        m = 255;
+        for (int k = 1; k <= leaf; k++) {
+            const int j = i + k;
+            int v = j < n ? (int)lvl[j] : 0;
+            if (v == 255) v = 0;
+            m = min(m, v);
+        }
+        if (m == 255) m = 0;
     }
-    if (b == 0) {
-        start[nbox] = n_act;
-        if (!is_leaf_level) child0[nbox] = nfine;
-    }
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(out, m);
 }
 
-__global__ void parents_from_scan(const int *__restrict__ incl, int nfine, int *__restrict__ parent) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b < nfine) parent[b] = incl[b] - 1;
-}
+struct LevelPtrs {
+    int *start[kLevels];
+    int *parent[kLevels];
+    int *child0[kLevels];
+    int4 *coord[kLevels];
+    int nbox[kLevels];
+    int first_box[kLevels + 1];  // prefix sums of nbox (flattened box index)
+};
 
 __device__ __forceinline__ uint32_t compact3(uint64_t x) {
     x &= 0x1249249249249249ull;
@@ -115,12 +104,117 @@ __device__ __forceinline__ uint32_t compact3(uint64_t x) {
     return (uint32_t)x;
 }
 
-__global__ void box_coords(const int *__restrict__ start, int nbox, const uint64_t *__restrict__ keys, int l,
-                           int4 *__restrict__ coord) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nbox) return;
-    const uint64_t k = keys[start[b]] >> (3 * (kMortonBits - l));
-    coord[b] = make_int4((int)compact3(k), (int)compact3(k >> 1), (int)compact3(k >> 2), start[b + 1] - start[b]);
+// Per CTA of kBuildThreads particles and per level l <= L: how many of its
+// particles start a box at level l (lvl[i] <= l).
+__global__ void __launch_bounds__(kBuildThreads)
+count_starts(const uint8_t *__restrict__ lvl, int n, int L, int *__restrict__ cnt) {
+    __shared__ int wc[kBuildThreads / 32][kLevels];
+    const int i = blockIdx.x * kBuildThreads + threadIdx.x;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int my = i < n ? (int)lvl[i] : 255;
+    for (int l = 0; l <= L; l++) {
+        const unsigned bal = __ballot_sync(0xffffffffu, my <= l);
+        if (lane == 0) wc[w][l] = __popc(bal);
+    }
+    __syncthreads();
+    if (threadIdx.x <= L) {
+        int s = 0;
+        for (int k = 0; k < kBuildThreads / 32; k++) s += wc[k][threadIdx.x];
+        cnt[blockIdx.x * kLevels + threadIdx.x] = s;
+    }
+}
+
+// Exclusive scan over the CTAs of each level (one block per level).
+__global__ void __launch_bounds__(1024) scan_counts(int *__restrict__ cnt, int nblk) {
+    __shared__ int buf[1024];
+    __shared__ int carry;
+    const int l = blockIdx.x;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < nblk; base += 1024) {
+        const int k = base + threadIdx.x;
+        const int v = k < nblk ? cnt[k * kLevels + l] : 0;
+        buf[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < 1024; o <<= 1) {
+            const int t = threadIdx.x >= o ? buf[threadIdx.x - o] : 0;
+            __syncthreads();
+            buf[threadIdx.x] += t;
+            __syncthreads();
+        }
+        if (k < nblk) cnt[k * kLevels + l] = carry + buf[threadIdx.x] - v;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry += buf[1023];
+        __syncthreads();
+    }
+}
+
+// Every particle that starts a box at level l writes its index as that box's
+// start, and the box's integer coordinates from its Morton key.
+__global__ void __launch_bounds__(kBuildThreads)
+scatter_starts(const uint8_t *__restrict__ lvl, const uint64_t *__restrict__ keys, int n, int L,
+               const int *__restrict__ off, LevelPtrs P) {
+    __shared__ int wc[kBuildThreads / 32];
+    __shared__ int wpre[kBuildThreads / 32];
+    const int i = blockIdx.x * kBuildThreads + threadIdx.x;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int my = i < n ? (int)lvl[i] : 255;
+    const uint64_t key = i < n ? keys[i] : 0ull;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int l = 0; l <= L; l++) {
+        const bool f = my <= l;
+        const unsigned bal = __ballot_sync(0xffffffffu, f);
+        if (lane == 0) wc[w] = __popc(bal);
+        __syncthreads();
+        if (w == 0) {
+            const int v = wc[lane];
+            int inc = v;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += t;
+            }
+            wpre[lane] = inc - v;
+        }
+        __syncthreads();
+        if (f) {
+            const int idx = off[blockIdx.x * kLevels + l] + wpre[w] + __popc(bal & lt);
+            P.start[l][idx] = i;
+            const uint64_t k = key >> (3 * (kMortonBits - l));
+            P.coord[l][idx] = make_int4((int)compact3(k), (int)compact3(k >> 1), (int)compact3(k >> 2), 0);
+        }
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ int upper_bound_i(const int *__restrict__ a, int n, int v) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (a[mid] <= v) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Close every level: particle counts, sentinels, parents and first children
+// (both by binary search on the neighbouring level's sorted starts: the starts
+// of level l-1 are a subset of those of level l).
+__global__ void link_levels(int L, int n_act, int total, LevelPtrs P) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    int l = 0;
+    while (t >= P.first_box[l + 1]) l++;
+    const int b = t - P.first_box[l];
+    const int nb = P.nbox[l];
+    const int s = P.start[l][b];
+    const int e = b + 1 < nb ? P.start[l][b + 1] : n_act;
+    P.coord[l][b].w = e - s;
+    if (b == 0) {
+        P.start[l][nb] = n_act;
+        if (l < L) P.child0[l][nb] = P.nbox[l + 1];
+    }
+    if (l >= 1) P.parent[l][b] = upper_bound_i(P.start[l - 1], P.nbox[l - 1], s) - 1;
+    if (l < L) P.child0[l][b] = upper_bound_i(P.start[l + 1], P.nbox[l + 1], s) - 1;
 }
 
 sv_status arena_reserve(sv_ctx *c, Tree &T, size_t bytes) {
@@ -142,7 +236,6 @@ void tree_free(sv_ctx *c) {
     cudaFree(T.lvl);
     cudaFree(T.hist);
     cudaFree(T.scratch);
-    cudaFree(T.cub_tmp);
     cudaFree(T.arena);
     cudaFreeHost(T.h_hist);
     delete c->tree;
@@ -150,21 +243,16 @@ void tree_free(sv_ctx *c) {
 }
 
 // Histogram of split levels and count of active particles (one readback).
-static sv_status tree_levels(sv_ctx *c, Tree &T) {
+static sv_status tree_levels(sv_ctx *c, Tree &T, int leaf_window) {
     const int n = (int)c->S.n;
     if (T.cap < n) {
-        cudaFree(T.lvl); cudaFree(T.scratch); cudaFree(T.cub_tmp);
-        T.lvl = nullptr; T.scratch = nullptr; T.cub_tmp = nullptr;
+        cudaFree(T.lvl);
+        cudaFree(T.scratch);
+        T.lvl = nullptr;
+        T.scratch = nullptr;
         const int cap = std::max(n, 1024);
         SV_CK(c, cudaMalloc(&T.lvl, cap));
-        SV_CK(c, cudaMalloc(&T.scratch, sizeof(int) * 3 * (size_t)(cap + 1)));
-        size_t b1 = 0, b2 = 0, b3 = 0;
-        SV_CK(c, cub::DeviceScan::InclusiveSum(nullptr, b1, T.scratch, T.scratch, cap, c->stream));
-        SV_CK(c, cub::DeviceSelect::Flagged(nullptr, b2, T.scratch, T.scratch, T.scratch, T.scratch, cap,
-                                            c->stream));
-        b3 = std::max(b1, b2);
-        SV_CK(c, cudaMalloc(&T.cub_tmp, b3));
-        T.cub_bytes = b3;
+        SV_CK(c, cudaMalloc(&T.scratch, sizeof(int) * (size_t)kLevels * (cap / kBuildThreads + 1)));
         T.cap = cap;
     }
     SV_CK(c, cudaMemsetAsync(T.hist, 0, sizeof(int) * (kLevels + 2), c->stream));
@@ -174,6 +262,11 @@ static sv_status tree_levels(sv_ctx *c, Tree &T) {
                              c->stream));
     split_levels<<<div_up(n, 256), 256, 0, c->stream>>>(c->S.keys, n, T.lvl, T.hist, T.hist + kLevels + 1);
     SV_LAUNCHED(c);
+    if (leaf_window > 0) {
+        SV_CK(c, cudaMemsetAsync(T.hist + kLevels, 0, sizeof(int), c->stream));
+        window_depth<<<div_up(n, 256), 256, 0, c->stream>>>(T.lvl, n, leaf_window, T.hist + kLevels);
+        SV_LAUNCHED(c);
+    }
     SV_CK(c, cudaMemcpyAsync(T.h_hist, T.hist, sizeof(int) * (kLevels + 2), cudaMemcpyDeviceToHost, c->stream));
     SV_CK(c, cudaStreamSynchronize(c->stream));
     T.n_act = T.h_hist[kLevels + 1];
@@ -193,7 +286,7 @@ sv_status tree_build(sv_ctx *c, int depth_rule, int param, Tree **out) {
     }
     Tree &T = *c->tree;
     *out = &T;
-    SV_TRY(tree_levels(c, T));
+    SV_TRY(tree_levels(c, T, depth_rule == kDepthAllSplit ? param : 0));
     const int na = T.n_act;
     if (na == 0) {
         T.deepest = -1;
@@ -215,10 +308,10 @@ sv_status tree_build(sv_ctx *c, int depth_rule, int param, Tree **out) {
         // box is bounded by the smallest gap between consecutive starts, which
         // is only known on the device, so use the level of mean occupancy 1/8
         // of param as a safe upper bound and let leaves stop early.
-        L = kLevels - 1;
-        for (int l = 1; l < kLevels; l++) {
-            if (T.nbox_level[l] >= na) { L = l; break; }
-        }
+        // first level at which no box exceeds `param` particles (duplicate
+        // positions stop at the finest level)
+        L = std::min(kLevels - 1, T.h_hist[kLevels]);
+        if (L < 1) L = 1;
     }
     T.deepest = L;
     // carve the arena: per level start[nbox+1], parent[nbox], child0[nbox+1], coord[nbox]
@@ -244,48 +337,27 @@ sv_status tree_build(sv_ctx *c, int depth_rule, int param, Tree **out) {
         V.child0 = (int *)carve(sizeof(int) * (V.nbox + 1));
         V.coord = (int4 *)carve(sizeof(int4) * V.nbox);
     }
-    int *flag = T.scratch;
-    int *incl = T.scratch + (T.cap + 1);
-    int *sel = T.scratch + 2 * (T.cap + 1);
-    int *d_num = T.hist + kLevels;  // reuse a histogram slot as the selection count
-    // leaf level from the particles
-    {
-        Level &V = T.lv[L];
-        flag_particles<<<div_up(na, 256), 256, 0, c->stream>>>(T.lvl, na, L, flag);
-        SV_LAUNCHED(c);
-        iota_kernel<<<div_up(na, 256), 256, 0, c->stream>>>(incl, na);
-        SV_LAUNCHED(c);
-        size_t tb = T.cub_bytes;
-        SV_CK(c, cub::DeviceSelect::Flagged(T.cub_tmp, tb, incl, flag, sel, d_num, na, c->stream));
-        c->launches += 2;
-        finish_level<<<div_up(V.nbox + 1, 256), 256, 0, c->stream>>>(sel, V.nbox, nullptr, na, 1, V.start,
-                                                                      nullptr, 0);
-        SV_LAUNCHED(c);
-    }
-    for (int l = L - 1; l >= 0; l--) {
-        Level &V = T.lv[l];
-        Level &F = T.lv[l + 1];
-        flag_boxes<<<div_up(F.nbox, 256), 256, 0, c->stream>>>(F.start, T.lvl, F.nbox, l, flag);
-        SV_LAUNCHED(c);
-        size_t tb = T.cub_bytes;
-        SV_CK(c, cub::DeviceScan::InclusiveSum(T.cub_tmp, tb, flag, incl, F.nbox, c->stream));
-        c->launches += 2;
-        parents_from_scan<<<div_up(F.nbox, 256), 256, 0, c->stream>>>(incl, F.nbox, F.parent);
-        SV_LAUNCHED(c);
-        iota_kernel<<<div_up(F.nbox, 256), 256, 0, c->stream>>>(incl, F.nbox);
-        SV_LAUNCHED(c);
-        tb = T.cub_bytes;
-        SV_CK(c, cub::DeviceSelect::Flagged(T.cub_tmp, tb, incl, flag, sel, d_num, F.nbox, c->stream));
-        c->launches += 2;
-        finish_level<<<div_up(V.nbox + 1, 256), 256, 0, c->stream>>>(sel, V.nbox, F.start, na, 0, V.start,
-                                                                      V.child0, F.nbox);
-        SV_LAUNCHED(c);
-    }
+    LevelPtrs P{};
+    int total = 0;
     for (int l = 0; l <= L; l++) {
-        Level &V = T.lv[l];
-        box_coords<<<div_up(V.nbox, 256), 256, 0, c->stream>>>(V.start, V.nbox, c->S.keys, l, V.coord);
-        SV_LAUNCHED(c);
+        P.start[l] = T.lv[l].start;
+        P.parent[l] = T.lv[l].parent;
+        P.child0[l] = T.lv[l].child0;
+        P.coord[l] = T.lv[l].coord;
+        P.nbox[l] = T.lv[l].nbox;
+        P.first_box[l] = total;
+        total += T.lv[l].nbox;
     }
+    for (int l = L + 1; l <= kLevels; l++) P.first_box[l] = total;
+    const int nblk = div_up(na, kBuildThreads);
+    count_starts<<<nblk, kBuildThreads, 0, c->stream>>>(T.lvl, na, L, T.scratch);
+    SV_LAUNCHED(c);
+    scan_counts<<<L + 1, 1024, 0, c->stream>>>(T.scratch, nblk);
+    SV_LAUNCHED(c);
+    scatter_starts<<<nblk, kBuildThreads, 0, c->stream>>>(T.lvl, c->S.keys, na, L, T.scratch, P);
+    SV_LAUNCHED(c);
+    link_levels<<<div_up(total, 256), 256, 0, c->stream>>>(L, na, total, P);
+    SV_LAUNCHED(c);
     return SV_OK;
 }
 

@@ -6,7 +6,7 @@
 namespace sv {
 
 constexpr int kDepthMeanOccupancy = 0;  // FMM: deepest level with mean occupancy >= param
-constexpr int kDepthAllSplit = 1;       // BH: down to the level where every particle is alone
+constexpr int kDepthAllSplit = 1;       // BH: down to the level where no box holds more than param
 
 struct Level {
     int nbox = 0;
@@ -25,9 +25,7 @@ struct Tree {
     uint8_t *lvl = nullptr; // per particle: coarsest level at which it starts a box
     int *hist = nullptr;    // device histogram [levels] + n_act
     int *h_hist = nullptr;  // pinned mirror
-    int *scratch = nullptr; // 3 x (cap+1) ints
-    void *cub_tmp = nullptr;
-    size_t cub_bytes = 0;
+    int *scratch = nullptr; // per-CTA, per-level box-start counts of the level builder
     void *arena = nullptr;
     size_t arena_bytes = 0;
 };
