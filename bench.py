@@ -129,21 +129,25 @@ def sample_clocks_stop(p, f, gpu_index):
 
 
 def cpu_baseline(state, n_sample, threads):
-    """FP64 direct sum of the C oracle on n_sample targets; particle-steps/s."""
+    """The reference's direct sum, restated in C (bit-exact with the reference
+    on its FP32 vec4 state), on n_sample targets against all sources, all host
+    threads; particle-steps/s."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_py as O
 
     n = state["x"].shape[0]
-    tg = np.linspace(0, n - 1, n_sample).astype(np.int64)
-    O.direct_f64(state, EPS2, targets=tg[:64], threads=threads)  # warm
+    pos4, vel4, acc4, _ = plume.to_ref32(state)
+    O.direct_ref32(pos4, vel4, acc4, EPS2, i_range=(0, 64), threads=threads)  # warm
     t = time.perf_counter()
-    O.direct_f64(state, EPS2, targets=tg, threads=threads)
+    O.direct_ref32(pos4, vel4, acc4, EPS2, i_range=(0, n_sample), threads=threads)
     dt = time.perf_counter() - t
     return {"value": n_sample / dt, "unit": "particle-steps/s", "cores": threads, "kind": "port",
-            "sample": f"FP64 direct sum (oracle restatement of direct_force_method.cpp:153-190) for "
-                      f"{n_sample} of {n} targets against all {n} sources, one force evaluation "
-                      f"({dt:.2f} s); per-target cost is independent of the target count, so "
-                      f"particle-steps/s = targets / time"}
+            "sample": f"reference direct sum (DirectForceFunction::direct, direct_force_method.cpp:153-190, "
+                      f"restated in C and bit-exact with the reference) for targets 0..{n_sample - 1} of {n} "
+                      f"against all {n} sources, one force evaluation ({dt:.2f} s, {threads} threads); the "
+                      f"per-target cost does not depend on the target count, so particle-steps/s = "
+                      f"targets / time.  The reference's own FMM is not timed: it overflows its heap "
+                      f"buffers at this plume size"}
 
 
 def run_reference(args, wl, rank, world):
