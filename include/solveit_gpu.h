@@ -147,6 +147,19 @@ SV_API sv_status sv_add_accel_ref32(sv_ctx *ctx, float *acc4);
  * of the first step. */
 SV_API sv_status sv_leapfrog(sv_ctx *ctx, int32_t nsteps, double dt, double t0);
 
+/* Adjoint of sv_leapfrog with the direct sum (no reference counterpart: the
+ * reference integrates forward only).  sv_adjoint_forward runs nsteps like
+ * sv_leapfrog and keeps the state every checkpoint_every steps;
+ * sv_adjoint_backward takes dL/dx and dL/dv of the final state (host, 3n
+ * interleaved) and returns dL/dx0, dL/dv0 (3n, nullable) and dL/dE (3,
+ * nullable, per V/m of the uniform field), re-running each checkpointed segment
+ * and applying the transposed Jacobian of the softened Coulomb sum.  The
+ * context's state is the final state again on return. */
+SV_API sv_status sv_adjoint_forward(sv_ctx *ctx, int32_t nsteps, double dt, double t0,
+                                    int32_t checkpoint_every);
+SV_API sv_status sv_adjoint_backward(sv_ctx *ctx, const double *dl_dx3, const double *dl_dv3,
+                                     double *dl_dx0, double *dl_dv0, double *dl_defield);
+
 /* Kinetic and softened potential energy in J, FP64, over all particles
  * (particles.cpp:535-578 with the halving of integration_schemes.cpp:815). */
 SV_API sv_status sv_energy(sv_ctx *ctx, double *ke, double *pe);

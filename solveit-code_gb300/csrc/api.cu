@@ -332,6 +332,7 @@ void sv_destroy(sv_ctx *c) {
     tree_free(c);
     fmm_free(c);
     bh_free(c);
+    adjoint_free(c);
     free_state(c);
     Sorted &S = c->S;
     cudaFree(S.x); cudaFree(S.y); cudaFree(S.z); cudaFree(S.q); cudaFree(S.qm);
@@ -459,7 +460,9 @@ sv_status sv_download_ref32(sv_ctx *c, float *pos4, float *vel4) {
     return SV_OK;
 }
 
-static sv_status compute_accel_device(sv_ctx *c, int64_t first, int64_t last) {
+}  // extern "C"
+
+sv_status sv::compute_accel_device(sv_ctx *c, int64_t first, int64_t last) {
     if (!c->have_state) return set_error(c, SV_ERR_STATE, "no state uploaded");
     if (first < 0) first = 0;
     if (last > c->n || last < 0) last = c->n;
@@ -489,6 +492,8 @@ static sv_status compute_accel_device(sv_ctx *c, int64_t first, int64_t last) {
     c->have_accel = true;
     return SV_OK;
 }
+
+extern "C" {
 
 sv_status sv_compute_accel(sv_ctx *c, int64_t first, int64_t last, double *a3_out) {
     if (!c) return SV_ERR_INVALID;

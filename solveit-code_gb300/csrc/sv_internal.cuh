@@ -53,6 +53,7 @@ struct ParticleView {
 struct Fmm;   // fmm.cu
 struct Tree;  // tree.cu
 struct Bh;    // bh.cu
+struct Adj;   // adjoint.cu
 
 }  // namespace sv
 
@@ -73,6 +74,7 @@ struct sv_ctx {
     sv::Tree *tree = nullptr;
     sv::Fmm *fmm = nullptr;
     sv::Bh *bh = nullptr;
+    sv::Adj *adj = nullptr;
     // device staging for interleaved <-> SoA transfers
     void *d_stage = nullptr;
     size_t d_stage_bytes = 0;
@@ -152,6 +154,12 @@ void fmm_free(sv_ctx *c);
 void bh_free(sv_ctx *c);
 // M2L translations and P2P pairs of the last FMM evaluation (synchronises)
 sv_status fmm_counts(sv_ctx *c, double *m2l, double *pairs);
+
+// api.cu: one force evaluation into c->a{x,y,z} (caller order)
+sv_status compute_accel_device(sv_ctx *c, int64_t first, int64_t last);
+
+// adjoint.cu
+void adjoint_free(sv_ctx *c);
 
 // integrate.cu
 sv_status drift(sv_ctx *c, double t_start, double h);

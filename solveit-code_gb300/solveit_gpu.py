@@ -28,7 +28,8 @@ ABI_SYMBOLS = (
     "sv_default_params", "sv_create", "sv_destroy", "sv_set_params", "sv_get_params", "sv_upload",
     "sv_upload_ref32", "sv_download", "sv_download_ref32", "sv_compute_accel", "sv_add_accel_ref32",
     "sv_leapfrog", "sv_energy", "sv_compare_accel", "sv_get_stats", "sv_sync", "sv_stream",
-    "sv_launch_count", "sv_last_error", "sv_abi_version",
+    "sv_launch_count", "sv_last_error", "sv_abi_version", "sv_adjoint_forward", "sv_adjoint_backward",
+    "sv_direct_accel_noalloc",
 )
 
 
@@ -95,6 +96,9 @@ def load(path: str = LIB_PATH):
     L.sv_last_error.argtypes = [vp]
     L.sv_last_error.restype = C.c_char_p
     L.sv_abi_version.restype = C.c_int32
+    L.sv_adjoint_forward.argtypes = [vp, C.c_int32, C.c_double, C.c_double, C.c_int32]
+    L.sv_adjoint_backward.argtypes = [vp, vp, vp, vp, vp, vp]
+    L.sv_direct_accel_noalloc.argtypes = [C.c_int64, vp, vp, vp, vp, C.c_double, C.c_double, vp, vp]
     for name in ABI_SYMBOLS:
         if name not in ("sv_destroy", "sv_stream", "sv_launch_count", "sv_last_error", "sv_abi_version"):
             getattr(L, name).restype = C.c_int
@@ -200,6 +204,19 @@ class ForceMethod:
 
     def leapfrog(self, nsteps, dt, t0=0.0):
         self._check(self.L.sv_leapfrog(self.h, nsteps, dt, t0))
+
+    def adjoint_forward(self, nsteps, dt, t0=0.0, checkpoint_every=10):
+        self._check(self.L.sv_adjoint_forward(self.h, nsteps, dt, t0, checkpoint_every))
+
+    def adjoint_backward(self, dl_dx, dl_dv):
+        """dL/dx, dL/dv of the final state -> (dL/dx0, dL/dv0, dL/dE)."""
+        gx = np.ascontiguousarray(dl_dx, np.float64)
+        gv = np.ascontiguousarray(dl_dv, np.float64)
+        ox = np.zeros((self.n, 3), np.float64)
+        ov = np.zeros((self.n, 3), np.float64)
+        oe = np.zeros(3, np.float64)
+        self._check(self.L.sv_adjoint_backward(self.h, _p(gx), _p(gv), _p(ox), _p(ov), _p(oe)))
+        return ox, ov, oe
 
     def energy(self):
         ke = C.c_double()
