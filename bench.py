@@ -53,6 +53,11 @@ WORKLOADS = {
     "direct_n4096": dict(n=4096, length=1e-6, method="direct", precision="fp64", seed=0,
                          desc="FP64 direct sum, N=4096 ions, plume r=20nm z=1um, eps=1e-10m, "
                               "leapfrog DKD dt=1e-13s, E_z=1e8V/m"),
+    "batch256": dict(n=None, nplumes=256, length=1e-6, method="batch", order=6, ws=2, seed=3,
+                     desc="256 independent plumes, N_i uniform in [1024, 65536] (seed 3999), r=20nm z=1um, "
+                          "direct sum for N_i < 8192 and FMM p=6 ws=2 above, 4-fold rotational variant on the "
+                          "even plumes, eps=1e-10m, leapfrog DKD dt=1e-13s, E_z=1e8V/m, each step one CUDA "
+                          "graph"),
 }
 
 
@@ -153,6 +158,8 @@ def cpu_baseline(state, n_sample, threads):
 def run_reference(args, wl, rank, world):
     if rank != 0:
         return
+    if wl["method"] == "batch":
+        return run_reference_batch(args, wl, world)
     st = plume.make_plume(wl["n"], wl["length"], wl["seed"] * 1000 + 0)
     threads = os.cpu_count() or 1
     n_sample = 2048 if wl["n"] > 100000 else min(wl["n"], 4096)
@@ -173,10 +180,219 @@ def run_reference(args, wl, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_batch(args, wl, rank, world, local):
+    """The batched-plume workload: every step of all plumes is one graph launch."""
+    import ctypes as C
+
+    import torch
+
+    import solveit_gpu as sv
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    states, methods, syms = plume.make_batch(wl["nplumes"], config=wl["seed"] + 100 * rank, length=wl["length"])
+    counts = np.array([s["x"].shape[0] for s in states])
+    n = int(counts.sum())
+    fm = sv.ForceMethod(softening2=EPS2, efield=(0.0, 0.0, EZ), device=local, fmm_order=wl["order"],
+                        fmm_ws=wl["ws"])
+    fm.upload_batch(states, methods, syms)
+    tuned_ms = fm.tune(None)
+    stream = torch.cuda.ExternalStream(fm.stream, device=local)
+    t = 0.0
+    fm.leapfrog(args.warmup, DT, t)
+    t += args.warmup * DT
+    fm.sync()
+    clk_p, clk_f = sample_clocks_start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    launches0 = fm.launches
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    fm.leapfrog(args.steps, DT, t)  # args.steps graph launches, one capacity check at the end
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = fm.launches - launches0
+    clocks = sample_clocks_stop(clk_p, clk_f, local)
+    step_ms = e0.elapsed_time(e1)
+    if dist:
+        step_ms = max_over_ranks(step_ms, dist, f"cuda:{local}")
+    ms_per_step = step_ms / args.steps
+    value = world * n * args.steps / (step_ms / 1e3)
+    info = fm.batch_info()
+
+    # ---- end to end: upload of the batch state from pinned host memory (same
+    # shape: the plan and graphs are kept), one step, download
+    cat, _ = plume.concat(states)
+    pin = {k: torch.empty(cat[k].shape, dtype=torch.float64 if cat[k].dtype == np.float64 else torch.int32,
+                          pin_memory=True) for k in ("x", "v", "q", "m", "status", "t_inj")}
+    for k in pin:
+        pin[k].numpy()[...] = cat[k]
+    cnt = np.ascontiguousarray(counts, np.int64)
+    meth = np.ascontiguousarray(methods, np.int32)
+    sym = np.ascontiguousarray(syms, np.int32)
+    xo = torch.empty((n, 3), dtype=torch.float64, pin_memory=True)
+    vo = torch.empty((n, 3), dtype=torch.float64, pin_memory=True)
+    so = torch.empty((n,), dtype=torch.int32, pin_memory=True)
+    L = sv.load()
+
+    def ptr(tn):
+        return C.c_void_p(tn.data_ptr())
+
+    def e2e_step(t0):
+        rc = L.sv_upload_batch(fm.h, len(states), cnt.ctypes.data_as(C.c_void_p), meth.ctypes.data_as(C.c_void_p),
+                               sym.ctypes.data_as(C.c_void_p), ptr(pin["x"]), ptr(pin["v"]), ptr(pin["q"]),
+                               ptr(pin["m"]), ptr(pin["status"]), ptr(pin["t_inj"]))
+        rc = rc or L.sv_leapfrog(fm.h, 1, DT, t0)
+        rc = rc or L.sv_download(fm.h, ptr(xo), ptr(vo), ptr(so))
+        if rc != 0:
+            raise RuntimeError(L.sv_last_error(fm.h).decode())
+
+    for _ in range(2):
+        e2e_step(0.0)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    e2e_steps = max(3, args.steps // 4)
+    for k in range(e2e_steps):
+        e2e_step(k * DT)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - w0
+    if dist:
+        e2e_s = max_over_ranks(e2e_s, dist, f"cuda:{local}")
+    e2e = {"value": world * n * e2e_steps / e2e_s, "unit": "particle-steps/s",
+           "h2d_bytes_per_step": n * (3 * 8 + 3 * 8 + 8 + 8 + 4 + 8), "d2h_bytes_per_step": n * (3 * 8 + 3 * 8 + 4),
+           "steps": e2e_steps}
+    line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 pair/expansion arithmetic, f64 state and integration",
+            "data": "synthetic (seeded plume generator)",
+            "config": {"workload": args.workload, "desc": wl["desc"], "particles_per_gpu": n,
+                       "plumes": len(states), "fmm_plumes": info.fmm_plumes, "slots_with_images": info.slots,
+                       "leaf_level": info.leaf_level, "tuned_leaf_target": info.leaf_target,
+                       "tuned_direct_chunk": info.direct_chunk, "kernels_per_step_graph": info.graph_kernels_step,
+                       "capacity_regrows": info.regrows,
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                       "l2": "no flush: the batch state (particles x 48 B plus sorted copies) is far larger than "
+                             "L2"},
+            "clocks": clocks, "e2e": e2e, "gpu_launches": int(launches), "tuned_force_ms": tuned_ms}
+    if rank == 0:
+        peaks = {}
+        try:
+            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        except Exception:
+            pass
+        sm_max = peaks.get("sm_max_mhz", 2070.0)
+        fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+        p = wl["order"]
+        m2l_flop = 8.0 * (2 * sum((k + 1) * (2 * k + 1) for k in range(p)) +
+                          sum(p - k for j in range(p) for k in range(j + 1)))
+        flops = 20.0 * (info.direct_pairs + info.fmm_pairs) + info.fmm_m2l * m2l_flop + \
+            info.fmm_slots * 8.0 * (p * (p + 1) / 2) * 4
+        achieved = flops / (ms_per_step * 1e-3) / 1e12
+        line["roofline"] = {"kernel": "whole step (direct pairs + P2P pairs at 20 flop, M2L at its flop count, "
+                                      "P2M + L2P)", "bound": "fp32", "achieved": achieved, "peak": fp32_peak,
+                            "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
+                            "pairs_per_step": info.direct_pairs + info.fmm_pairs, "m2l_per_step": info.fmm_m2l}
+        # force error on sampled targets of a few plumes against the FP64 oracle
+        import oracle_py as O
+
+        x, v, stt = fm.download()
+        a = fm.accel()
+        offs = np.concatenate([[0], np.cumsum(counts)])
+        rng = np.random.default_rng(11)
+        errs = {}
+        for i in (0, 1, 2, 3, int(np.argmax(counts)), int(np.argmin(counts))):
+            s0, s1 = offs[i], offs[i + 1]
+            cur = dict(states[i], x=x[s0:s1], v=v[s0:s1], status=stt[s0:s1])
+            tg = np.sort(rng.choice(s1 - s0, min(64, s1 - s0), replace=False))
+            ref = O.direct_f64(cur, EPS2, sym=syms[i], targets=tg, threads=os.cpu_count() or 1)
+            d = np.sum((a[s0:s1][tg] - ref) ** 2, axis=1) / np.sum(ref ** 2, axis=1)
+            errs[f"plume{i}_n{s1 - s0}_{'fmm' if methods[i] == 2 else 'direct'}_{'rot4' if syms[i] else 'none'}"] = \
+                float(np.sqrt(np.mean(d)))
+        line["force_err_rel_l2_sampled"] = errs
+        # plain FP64 GPU direct path: measured pair rate at one plume, applied to every plume's pair count
+        big = int(np.argmax(counts))
+        with sv.ForceMethod(softening2=EPS2, method=sv.DIRECT, precision=sv.FP64, device=local) as f64:
+            f64.upload(states[big])
+            f64.accel(out=False)
+            f64.sync()
+            t0 = time.perf_counter()
+            f64.accel(out=False)
+            f64.sync()
+            t_big = time.perf_counter() - t0
+        rate = counts[big] ** 2 / t_big
+        pairs_all = float(sum(int(nn) ** 2 * (4 if sy else 1) for nn, sy in zip(counts, syms)))
+        t_all = pairs_all / rate
+        line["fp64_direct"] = {"value": n / t_all, "unit": "particle-steps/s",
+                               "measured": f"FP64 direct force at N={counts[big]}: {t_big * 1e3:.1f} ms "
+                                           f"({rate:.3g} pairs/s), applied to the batch's {pairs_all:.3g} "
+                                           f"pairs per step (x4 for the rotational plumes)"}
+        line["speedup_vs_fp64_direct"] = value / world / (n / t_all)
+        # CPU baseline: the oracle's bit-exact restatement of the reference direct sum on a target sample,
+        # as a pair rate applied to the whole batch
+        pos4, vel4, acc4, _ = plume.to_ref32(states[big])
+        threads = os.cpu_count() or 1
+        O.direct_ref32(pos4, vel4, acc4, EPS2, i_range=(0, 64), threads=threads)
+        ns = 2048
+        tc = time.perf_counter()
+        O.direct_ref32(pos4, vel4, acc4, EPS2, i_range=(0, ns), threads=threads)
+        tc = time.perf_counter() - tc
+        cpu_rate = ns * counts[big] / tc
+        line["cpu_baseline"] = {"value": n / (pairs_all / cpu_rate), "unit": "particle-steps/s", "cores": threads,
+                                "kind": "port",
+                                "sample": f"reference direct sum restated in C (bit-exact with "
+                                          f"direct_force_method.cpp:153-190), {ns} targets of plume {big} "
+                                          f"(N={counts[big]}) in {tc:.2f} s = {cpu_rate:.3g} pairs/s, applied to "
+                                          f"the batch's direct-sum pair count; the reference's FMM is not timed "
+                                          f"(its rotational FMM is wrong at these sizes)"}
+        print(json.dumps(line), flush=True)
+    fm.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def run_reference_batch(args, wl, world):
+    """Reference arm of the batched workload: the reference's direct sum
+    (restated in C, bit-exact) as a pair rate, applied to every plume."""
+    states, methods, syms = plume.make_batch(wl["nplumes"], config=wl["seed"], length=wl["length"])
+    counts = np.array([s["x"].shape[0] for s in states])
+    n = int(counts.sum())
+    big = int(np.argmax(counts))
+    pairs_all = float(sum(int(nn) ** 2 * (4 if sy else 1) for nn, sy in zip(counts, syms)))
+    threads = os.cpu_count() or 1
+    vals = []
+    cb = None
+    for k in range(args.warmup + args.steps):
+        cb = cpu_baseline(states[big], 2048, threads)
+        if k >= args.warmup:
+            vals.append(cb["value"] * counts[big] / pairs_all * n)
+    v = float(np.mean(vals))
+    cb["value"] = v
+    cb["sample"] += f"; applied to the batch's {pairs_all:.3g} direct-sum pairs per step"
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "particle-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": n / v * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "desc": wl["desc"], "particles": n},
+            "cpu_baseline": cb, "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def run_ours(args, wl, rank, world, local):
     import torch
 
     import solveit_gpu as sv
+
+    if wl["method"] == "batch":
+        return run_batch(args, wl, rank, world, local)
 
     torch.cuda.set_device(local)
     dist = None

@@ -178,6 +178,56 @@ SV_API uint64_t sv_launch_count(const sv_ctx *ctx);
 SV_API const char *sv_last_error(const sv_ctx *ctx);
 SV_API int32_t sv_abi_version(void);
 
+/* Many independent plumes in one context.  The reference runs one
+ * ForceCalculationMethod and one LeapfrogDKD loop per ParticleSystem
+ * (force_calculation_methods.h:28-87, integration_schemes.cpp:856-891); a
+ * batch runs every plume of a study at once.  Plume p owns the caller
+ * particles [counts[0] + ... + counts[p-1], + counts[p]) of the arrays (laid
+ * out as sv_upload's), uses method[p] (SV_METHOD_DIRECT or SV_METHOD_FMM, the
+ * FMM at the context's fmm_order and fmm_ws) and symmetry[p] (SV_SYM_NONE or
+ * SV_SYM_ROTATIONAL), and interacts with no other plume.  Afterwards
+ * sv_compute_accel (whole batch; first/last are ignored), sv_leapfrog,
+ * sv_download, sv_download_ref32 and sv_compare_accel act on all plumes;
+ * sv_energy and the adjoint return SV_ERR_UNSUPPORTED.  Each force evaluation
+ * and each leapfrog step is one CUDA-graph launch.  Uploading a batch of the
+ * same shape (plume counts, methods, symmetries) again keeps the plan and the
+ * graphs; a later sv_upload or sv_upload_ref32 leaves batch mode.  At most
+ * 512 plumes. */
+SV_API sv_status sv_upload_batch(sv_ctx *ctx, int32_t nplumes, const int64_t *counts, const int32_t *method,
+                                 const int32_t *symmetry, const double *x3, const double *v3, const double *q,
+                                 const double *m_amu, const int32_t *status, const double *t_inj);
+/* Autotuner of a batch (no reference counterpart): times the FMM plumes' leaf
+ * occupancy and the direct plumes' work-item size on the uploaded state and
+ * keeps the fastest.  Results are cached per batch shape (plume count, size
+ * buckets, methods, symmetries, order) in the process and, when cache_path is
+ * not null, in that text file (read first, appended to).  best_ms (nullable)
+ * receives the tuned force-evaluation time. */
+SV_API sv_status sv_batch_tune(sv_ctx *ctx, const char *cache_path, double *best_ms);
+/* Sets the two tuned quantities directly (mean FMM leaf occupancy >= 1,
+ * direct sources per work item >= 256) and re-plans the batch. */
+SV_API sv_status sv_batch_set_tuning(sv_ctx *ctx, int32_t leaf_target, int32_t direct_chunk);
+typedef struct {
+    int32_t nplumes, fmm_plumes;
+    int64_t slots, fmm_slots;       /* particles plus FMM rotational image copies */
+    int32_t leaf_level;             /* leaf level of the FMM forest */
+    int32_t leaf_target;            /* tuned mean leaf occupancy */
+    int32_t direct_chunk;           /* tuned sources per direct work item */
+    int32_t direct_items;
+    int32_t graph_kernels_step;     /* kernel nodes of one captured leapfrog step */
+    int32_t graph_kernels_accel;    /* kernel nodes of one captured force evaluation */
+    double tuned_ms;                /* force-evaluation time measured by sv_batch_tune */
+    double direct_pairs;            /* pair interactions of the direct plumes per evaluation */
+    double fmm_m2l;                 /* M2L translations of the last FMM forest evaluation */
+    double fmm_pairs;               /* P2P pair interactions of the last FMM forest evaluation */
+    int32_t regrows;                /* times a box capacity overflowed and the work was redone */
+    int32_t overflow_mask;          /* bit l: forest level l overflowed at the last regrow */
+    int32_t level_boxes[22];        /* forest boxes per level at the last evaluation */
+    int32_t level_cap[22];          /* box capacity per level */
+    int32_t level_max[22];          /* largest box count per level since the last plan */
+    int32_t reserved[6];
+} sv_batch_info;
+SV_API sv_status sv_batch_get_info(const sv_ctx *ctx, sv_batch_info *out);
+
 /* Direct sum that allocates no memory.  No counterpart in the reference: it
  * is for callers that cannot allocate device memory (an allocator owned by a
  * host framework, real-time loops that forbid cudaMalloc / cudaFree and their

@@ -456,6 +456,7 @@ extern "C" sv_status sv_adjoint_forward(sv_ctx *c, int32_t nsteps, double dt, do
     if (!c->have_state) return set_error(c, SV_ERR_STATE, "no state uploaded");
     if (nsteps < 0 || !(dt > 0.0) || checkpoint_every < 1)
         return set_error(c, SV_ERR_INVALID, "nsteps >= 0, dt > 0, checkpoint_every >= 1 required");
+    if (c->batch) return set_error(c, SV_ERR_UNSUPPORTED, "the adjoint runs on single-plume contexts");
     if (c->P.method != SV_METHOD_DIRECT || c->P.symmetry != SV_SYM_NONE)
         return set_error(c, SV_ERR_UNSUPPORTED, "the adjoint covers the direct sum without symmetry images");
     SV_CK(c, cudaSetDevice(c->device));

@@ -268,6 +268,47 @@ using namespace sv;
 
 extern "C" {
 
+static sv_status upload_state(sv_ctx *c, int64_t n, const double *x3, const double *v3, const double *q,
+                              const double *m_amu, const int32_t *status, const double *t_inj);
+
+sv_status sv_upload_batch(sv_ctx *c, int32_t nplumes, const int64_t *counts, const int32_t *method,
+                          const int32_t *symmetry, const double *x3, const double *v3, const double *q,
+                          const double *m_amu, const int32_t *status, const double *t_inj) {
+    if (!c || !counts || !method || !symmetry) return SV_ERR_INVALID;
+    if (nplumes < 1) return set_error(c, SV_ERR_INVALID, "a batch needs at least one plume");
+    int64_t n = 0;
+    for (int p = 0; p < nplumes; p++) n += counts[p];
+    SV_CK(c, cudaSetDevice(c->device));
+    // a batch of the same shape keeps its plan, capacities and graphs
+    const bool same = batch_same_shape(c, nplumes, counts, method, symmetry);
+    if (!same) batch_free(c);
+    SV_TRY(upload_state(c, n, x3, v3, q, m_amu, status, t_inj));
+    if (same) return SV_OK;
+    const sv_status st = batch_plan(c, nplumes, counts, method, symmetry);
+    if (st != SV_OK) batch_free(c);
+    return st;
+}
+
+sv_status sv_batch_tune(sv_ctx *c, const char *cache_path, double *best_ms) {
+    if (!c) return SV_ERR_INVALID;
+    if (!c->batch) return set_error(c, SV_ERR_STATE, "no batch uploaded");
+    SV_CK(c, cudaSetDevice(c->device));
+    return batch_tune(c, cache_path, best_ms);
+}
+
+sv_status sv_batch_set_tuning(sv_ctx *c, int32_t leaf_target, int32_t direct_chunk) {
+    if (!c) return SV_ERR_INVALID;
+    if (!c->batch) return set_error(c, SV_ERR_STATE, "no batch uploaded");
+    SV_CK(c, cudaSetDevice(c->device));
+    return batch_set_tuning(c, leaf_target, direct_chunk);
+}
+
+sv_status sv_batch_get_info(const sv_ctx *c, sv_batch_info *out) {
+    if (!c || !out) return SV_ERR_INVALID;
+    if (!c->batch) return SV_ERR_STATE;
+    return batch_info(c, out);
+}
+
 int32_t sv_abi_version(void) { return SV_ABI_VERSION; }
 
 sv_status sv_default_params(sv_params *p) {
@@ -333,6 +374,7 @@ void sv_destroy(sv_ctx *c) {
     fmm_free(c);
     bh_free(c);
     adjoint_free(c);
+    batch_free(c);
     free_state(c);
     Sorted &S = c->S;
     cudaFree(S.x); cudaFree(S.y); cudaFree(S.z); cudaFree(S.q); cudaFree(S.qm);
@@ -355,6 +397,7 @@ sv_status sv_set_params(sv_ctx *c, const sv_params *p) {
     SV_TRY(check_params(c, p));
     if (p->device != c->device) return set_error(c, SV_ERR_INVALID, "device cannot change on a context");
     c->P = *p;
+    batch_invalidate(c);
     return SV_OK;
 }
 
@@ -364,9 +407,9 @@ sv_status sv_get_params(const sv_ctx *c, sv_params *p) {
     return SV_OK;
 }
 
-sv_status sv_upload(sv_ctx *c, int64_t n, const double *x3, const double *v3, const double *q,
-                    const double *m_amu, const int32_t *status, const double *t_inj) {
-    if (!c) return SV_ERR_INVALID;
+// state upload shared by sv_upload and sv_upload_batch (keeps any batch plan)
+static sv_status upload_state(sv_ctx *c, int64_t n, const double *x3, const double *v3, const double *q,
+                              const double *m_amu, const int32_t *status, const double *t_inj) {
     if (n < 0 || n > (int64_t)INT32_MAX) return set_error(c, SV_ERR_INVALID, "n=%lld out of range", (long long)n);
     if (n > 0 && (!x3 || !q || !m_amu || !status)) return set_error(c, SV_ERR_INVALID, "null state array");
     SV_CK(c, cudaSetDevice(c->device));
@@ -398,12 +441,21 @@ sv_status sv_upload(sv_ctx *c, int64_t n, const double *x3, const double *v3, co
     return SV_OK;
 }
 
+sv_status sv_upload(sv_ctx *c, int64_t n, const double *x3, const double *v3, const double *q,
+                    const double *m_amu, const int32_t *status, const double *t_inj) {
+    if (!c) return SV_ERR_INVALID;
+    SV_CK(c, cudaSetDevice(c->device));
+    batch_free(c);
+    return upload_state(c, n, x3, v3, q, m_amu, status, t_inj);
+}
+
 sv_status sv_upload_ref32(sv_ctx *c, int64_t n, const float *pos4, const float *vel4, const float *acc4,
                           const float *t_inj) {
     if (!c) return SV_ERR_INVALID;
     if (n < 0 || n > (int64_t)INT32_MAX) return set_error(c, SV_ERR_INVALID, "n=%lld out of range", (long long)n);
     if (n > 0 && (!pos4 || !vel4 || !acc4)) return set_error(c, SV_ERR_INVALID, "null state array");
     SV_CK(c, cudaSetDevice(c->device));
+    batch_free(c);
     SV_TRY(ensure_capacity(c, n));
     c->n = n;
     c->have_state = true;
@@ -468,6 +520,13 @@ sv_status sv::compute_accel_device(sv_ctx *c, int64_t first, int64_t last) {
     if (last > c->n || last < 0) last = c->n;
     const int64_t n = c->n;
     memset(&c->stats, 0, sizeof(c->stats));
+    if (c->batch) {
+        SV_CK(c, cudaEventRecord(c->ev_begin, c->stream));
+        SV_TRY(batch_accel(c));
+        SV_CK(c, cudaEventRecord(c->ev_end, c->stream));
+        c->have_accel = true;
+        return SV_OK;
+    }
     SV_CK(c, cudaEventRecord(c->ev_begin, c->stream));
     if (n > 0) {
         phase_mark(c, 0);
@@ -534,6 +593,7 @@ sv_status sv_leapfrog(sv_ctx *c, int32_t nsteps, double dt, double t0) {
     if (!c->have_state) return set_error(c, SV_ERR_STATE, "no state uploaded");
     if (nsteps < 0 || !(dt > 0.0)) return set_error(c, SV_ERR_INVALID, "nsteps >= 0 and dt > 0 required");
     SV_CK(c, cudaSetDevice(c->device));
+    if (c->batch) return batch_leapfrog(c, nsteps, dt, t0);
     const double h = 0.5 * dt;
     for (int it = 0; it < nsteps; it++) {
         const double ts = t0 + dt * it;
@@ -548,6 +608,7 @@ sv_status sv_leapfrog(sv_ctx *c, int32_t nsteps, double dt, double t0) {
 sv_status sv_energy(sv_ctx *c, double *ke, double *pe) {
     if (!c || !ke || !pe) return SV_ERR_INVALID;
     if (!c->have_state) return set_error(c, SV_ERR_STATE, "no state uploaded");
+    if (c->batch) return set_error(c, SV_ERR_UNSUPPORTED, "energy of a batch: evaluate the plumes one by one");
     SV_CK(c, cudaSetDevice(c->device));
     if (c->n == 0) {
         *ke = *pe = 0.0;

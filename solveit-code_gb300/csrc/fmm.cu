@@ -31,10 +31,12 @@
 // field to 5x5x5 boxes, which is what brings p = 8 under 1e-5 force error.
 #include <cfloat>
 
+#include <algorithm>
 #include <string>
 #include <vector>
 
 #include "fmm_tables.h"
+#include "forest.cuh"
 #include "sv_internal.cuh"
 #include "tree.cuh"
 
@@ -63,6 +65,15 @@ struct Fmm {
     int64_t tgt_cap = 0;
     float4 *rel = nullptr;   // particle offset from its leaf box centre (FP32) + charge
     int64_t rel_cap = 0;
+    // forest (batched plumes): tree and per-level arrays carved at reserve time
+    Tree *ftree = nullptr;
+    void *farena = nullptr;
+    size_t farena_bytes = 0;
+    float2 *fM[kMortonBits + 1] = {}, *fL[kMortonBits + 1] = {};
+    int *fnbr[kMortonBits + 1] = {}, *fcnt[kMortonBits + 1] = {}, *ftgt[kMortonBits + 1] = {};
+    int2 *flst[kMortonBits + 1] = {};
+    float4 *frel = nullptr;
+    int64_t frel_cap = 0;
 };
 
 namespace {
@@ -115,16 +126,30 @@ __device__ __forceinline__ float2 half_get(const float2 *C, int n, int m) {
     return (m & 1) ? make_float2(-v.x, v.y) : make_float2(v.x, -v.y);
 }
 
+// Box count of a level: the launch bound nbox, or (forest) the device count.
+__device__ __forceinline__ int level_boxes(int nbox, const int *nbd) { return nbd ? min(nbox, *nbd) : nbox; }
+// Root record (origin xyz, cube side) of the plume that owns box b.
+__device__ __forceinline__ const double *box_root(const double *root, const int *bpid, int b) {
+    return bpid ? root + 8 * bpid[b] : root;
+}
+// First box and stride of the calling warp in a warp-per-box kernel.
+#define SV_WARP_BOXES(W) \
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5; \
+    const int nb_ = level_boxes(nbox, nbd); \
+    for (int b = blockIdx.x * (W) + wid; b < nb_; b += gridDim.x * (W))
+
 // ---------------------------------------------------------------- lists --
 template <int WS>
-__global__ void build_lists_kernel(int nbox, const int *__restrict__ parent, const int4 *__restrict__ coord,
-                                   const int *__restrict__ pnbr, const int *__restrict__ pchild0,
-                                   int *__restrict__ nbr, int2 *__restrict__ m2l, int *__restrict__ m2l_cnt,
-                                   int cap, unsigned long long *__restrict__ counts) {
+__global__ void build_lists_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ parent,
+                                   const int4 *__restrict__ coord, const int *__restrict__ pnbr,
+                                   const int *__restrict__ pchild0, int *__restrict__ nbr, int2 *__restrict__ m2l,
+                                   int *__restrict__ m2l_cnt, int cap, unsigned long long *__restrict__ counts) {
     constexpr int NS1 = 2 * WS + 1, NS = NS1 * NS1 * NS1, R = 2 * WS + 1, SIDE = 2 * R + 1;
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    int cnt = 0;
-    if (b < nbox) {
+    const int nb = level_boxes(nbox, nbd);
+    unsigned long long tot = 0;
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+        int cnt = 0;
+        for (int s = 0; s < NS; s++) nbr[b * NS + s] = -1;
         const int4 cb = coord[b];
         const int par = parent[b];
         for (int s = 0; s < NS; s++) {
@@ -135,6 +160,10 @@ __global__ void build_lists_kernel(int nbox, const int *__restrict__ parent, con
                 const int4 cc = coord[ch];
                 const int ox = cb.x - cc.x, oy = cb.y - cc.y, oz = cb.z - cc.z;
                 const int am = max(abs(ox), max(abs(oy), abs(oz)));
+                // a consistent tree keeps |offset| <= R; a forest level clamped to its
+                // capacity may not, and its result is discarded, but the class index
+                // must stay inside the tables
+                if (am > R) continue;
                 if (am <= WS) {
                     nbr[b * NS + ((ox + WS) * NS1 + (oy + WS)) * NS1 + (oz + WS)] = ch;
                 } else if (cnt < cap) {
@@ -144,14 +173,20 @@ __global__ void build_lists_kernel(int nbox, const int *__restrict__ parent, con
             }
         }
         m2l_cnt[b] = cnt;
+        tot += cnt;
     }
     // warp-aggregated statistics
-    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(&counts[0], (unsigned long long)cnt);
+    for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+    if ((threadIdx.x & 31) == 0 && tot) atomicAdd(&counts[0], tot);
 }
 
-__global__ void root_nbr_kernel(int *nbr, int ns) {
-    if (threadIdx.x == 0 && blockIdx.x == 0) nbr[ns / 2] = 0;
+// Near list of every root: the root itself only (plumes never interact).
+__global__ void root_nbr_kernel(int *nbr, int ns, int nroots, const int *__restrict__ nbd) {
+    const int nr = level_boxes(nroots, nbd);
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nr * ns; t += gridDim.x * blockDim.x) {
+        const int b = t / ns, s = t - b * ns;
+        nbr[t] = s == ns / 2 ? b : -1;
+    }
 }
 
 // ------------------------------------------------------ symmetry images --
@@ -192,22 +227,24 @@ __global__ void expand_images_kernel(const double *__restrict__ x, const double 
 
 // box holds at least one target (K q/m != 0): leaf level from particles,
 // coarser levels from children
-__global__ void leaf_targets_kernel(int nbox, const int *__restrict__ start, const double *__restrict__ qm,
-                                    int *__restrict__ flag) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nbox) return;
-    int f = 0;
-    for (int j = start[b]; j < start[b + 1] && !f; j++) f = qm[j] != 0.0;
-    flag[b] = f;
+__global__ void leaf_targets_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ start,
+                                    const double *__restrict__ qm, int *__restrict__ flag) {
+    const int nb = level_boxes(nbox, nbd);
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+        int f = 0;
+        for (int j = start[b]; j < start[b + 1] && !f; j++) f = qm[j] != 0.0;
+        flag[b] = f;
+    }
 }
 
-__global__ void parent_targets_kernel(int nbox, const int *__restrict__ child0, const int *__restrict__ cflag,
-                                      int *__restrict__ flag) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nbox) return;
-    int f = 0;
-    for (int c = child0[b]; c < child0[b + 1] && !f; c++) f = cflag[c];
-    flag[b] = f;
+__global__ void parent_targets_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ child0,
+                                      const int *__restrict__ cflag, int *__restrict__ flag) {
+    const int nb = level_boxes(nbox, nbd);
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+        int f = 0;
+        for (int c = child0[b]; c < child0[b + 1] && !f; c++) f = cflag[c];
+        flag[b] = f;
+    }
 }
 
 // ------------------------------------------------------------------ P2M --
@@ -216,15 +253,14 @@ constexpr int p2m_warps() { return P >= 9 ? 2 : 4; }
 
 template <int P>
 __global__ void __launch_bounds__(p2m_warps<P>() * 32)
-p2m_kernel(int nbox, const int *__restrict__ start, const int4 *__restrict__ coord,
-           const double *__restrict__ xs, const double *__restrict__ ys, const double *__restrict__ zs,
-           const float *__restrict__ qs, const double *__restrict__ root, int level,
+p2m_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, const int *__restrict__ start,
+           const int4 *__restrict__ coord, const double *__restrict__ xs, const double *__restrict__ ys,
+           const double *__restrict__ zs, const float *__restrict__ qs, const double *__restrict__ roots, int level,
            const float *__restrict__ nrm, float2 *__restrict__ M) {
     constexpr int NC = ncoef(P), WP = p2m_warps<P>();
     __shared__ float2 buf[WP][32][NC + 1];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int b = blockIdx.x * WP + wid;
-    if (b >= nbox) return;
+    SV_WARP_BOXES(WP) {
+    const double *root = box_root(roots, bpid, b);
     const double h = root[3] / (double)(1 << level);
     const int4 cb = coord[b];
     const double cx = root[0] + (cb.x + 0.5) * h, cy = root[1] + (cb.y + 0.5) * h, cz = root[2] + (cb.z + 0.5) * h;
@@ -260,19 +296,19 @@ p2m_kernel(int nbox, const int *__restrict__ start, const int4 *__restrict__ coo
             M[(size_t)b * NC + lane + 32] = cscale(a1, nrm[n * P + m]);
         }
     }
+    __syncwarp();
+    }
 }
 
 // ------------------------------------------------------------------ M2M --
 template <int P>
 __global__ void __launch_bounds__(kWarps * 32)
-m2m_kernel(int nbox, const int *__restrict__ child0, const int4 *__restrict__ ccoord,
+m2m_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ child0, const int4 *__restrict__ ccoord,
            const float2 *__restrict__ Mc, float2 *__restrict__ Mp, const float *__restrict__ nrm,
            const float2 *__restrict__ oct) {
     constexpr int NC = ncoef(P), W = 2 * P - 1;
     __shared__ float2 mu[kWarps][NC];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int b = blockIdx.x * kWarps + wid;
-    if (b >= nbox) return;
+    SV_WARP_BOXES(kWarps) {
     float2 acc[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
     const int ch1 = child0[b + 1];
     for (int ch = child0[b]; ch < ch1; ch++) {
@@ -313,11 +349,14 @@ m2m_kernel(int nbox, const int *__restrict__ child0, const int4 *__restrict__ cc
         // back to G-R normalisation, from child to parent box units (x 2^-n)
         Mp[(size_t)b * NC + c] = cscale(acc[t], nrm[n * P + m] * ldexpf(1.f, -n));
     }
+    }
 }
 
 // ----------------------------------------------------------- downward --
 struct DownArgs {
     int nbox, level, cap, esz, osz, dsz, has_parent;
+    const int *nbd;        // device box count (forest) or null
+    const int *bpid;       // plume of each box (forest) or null
     const int *parent;
     const int4 *coord;
     const float2 *Lp;      // parent locals (level-1) or null
@@ -396,9 +435,10 @@ template <int P>
 __global__ void __launch_bounds__(kWarps * 32) down_kernel(DownArgs a) {
     constexpr int NC = ncoef(P), W = 2 * P - 1;
     __shared__ float2 A[kWarps][NC], B[kWarps][NC];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int b = blockIdx.x * kWarps + wid;
-    if (b >= a.nbox || !a.has_tgt[b]) return;
+    const int nbox = a.nbox;
+    const int *nbd = a.nbd;
+    SV_WARP_BOXES(kWarps) {
+    if (!a.has_tgt[b]) continue;
     // Lane slots.  Slot 0 of every lane holds one of the NC - EXTRA highest
     // coefficients; slot 1 of the first EXTRA lanes holds one of the EXTRA
     // lowest (cheapest) coefficients, so the second pass is short.
@@ -440,7 +480,7 @@ __global__ void __launch_bounds__(kWarps * 32) down_kernel(DownArgs a) {
         __syncwarp();
     }
     // ---- M2L list
-    const double h = a.root[3] / (double)(1 << a.level);
+    const double h = box_root(a.root, a.bpid, b)[3] / (double)(1 << a.level);
     const float eh2 = (float)(a.eps2 / (h * h));
     const int cnt = a.m2l_cnt[b];
     const int2 *lst = a.m2l + (size_t)b * a.cap;
@@ -479,21 +519,27 @@ __global__ void __launch_bounds__(kWarps * 32) down_kernel(DownArgs a) {
     }
     if (has[0]) a.Lout[(size_t)b * NC + cs[0]] = acc[0];
     if (has[1]) a.Lout[(size_t)b * NC + cs[1]] = acc[1];
+    __syncwarp();
+    }
 }
 
 // ------------------------------------------------------------------ L2P --
 template <int P>
 __global__ void __launch_bounds__(kWarps * 32)
-l2p_kernel(int nbox, const int *__restrict__ start, const int4 *__restrict__ coord,
-           const double *__restrict__ xs, const double *__restrict__ ys, const double *__restrict__ zs,
-           const double *__restrict__ qm, const double *__restrict__ root, int level,
+l2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, const int *__restrict__ start,
+           const int4 *__restrict__ coord, const double *__restrict__ xs, const double *__restrict__ ys,
+           const double *__restrict__ zs, const double *__restrict__ qm, const double *__restrict__ roots, int level,
            const float *__restrict__ nrm, const float2 *__restrict__ Lc, double *__restrict__ ax,
            double *__restrict__ ay, double *__restrict__ az, const int *__restrict__ has_tgt) {
     constexpr int NC = ncoef(P);
     __shared__ float2 lam[kWarps][NC];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int b = blockIdx.x * kWarps + wid;
-    if (b >= nbox || !has_tgt[b]) return;
+    SV_WARP_BOXES(kWarps) {
+    const double *root = box_root(roots, bpid, b);
+    if (!has_tgt[b]) {
+        // boxes of image copies only: no targets, zero acceleration
+        for (int i = start[b] + lane; i < start[b + 1]; i += 32) ax[i] = ay[i] = az[i] = 0.0;
+        continue;
+    }
     for (int c = lane; c < NC; c += 32) {
         int n, m;
         cnm(c, n, m);
@@ -530,6 +576,8 @@ l2p_kernel(int nbox, const int *__restrict__ start, const int4 *__restrict__ coo
         ay[i] = f * (double)(-gm.y);
         az[i] = f * (double)gz;
     }
+    __syncwarp();
+    }
 }
 
 // ------------------------------------------------------------------ P2P --
@@ -537,41 +585,79 @@ l2p_kernel(int nbox, const int *__restrict__ start, const int4 *__restrict__ coo
 // (one FP64 subtraction per particle) with its charge: the P2P kernel then
 // forms source offsets from the target box centre as offset + k*h in FP32.
 __global__ void __launch_bounds__(kWarps * 32)
-box_relative_kernel(int nbox, const int *__restrict__ start, const int4 *__restrict__ coord,
-                    const double *__restrict__ xs, const double *__restrict__ ys, const double *__restrict__ zs,
-                    const float *__restrict__ qs, const double *__restrict__ root, int level,
-                    float4 *__restrict__ rel) {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int b = blockIdx.x * kWarps + wid;
-    if (b >= nbox) return;
+box_relative_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid,
+                    const int *__restrict__ start, const int4 *__restrict__ coord, const double *__restrict__ xs,
+                    const double *__restrict__ ys, const double *__restrict__ zs, const float *__restrict__ qs,
+                    const double *__restrict__ roots, int level, float4 *__restrict__ rel) {
+    SV_WARP_BOXES(kWarps) {
+    const double *root = box_root(roots, bpid, b);
     const double h = root[3] / (double)(1 << level);
     const int4 cb = coord[b];
     const double cx = root[0] + (cb.x + 0.5) * h, cy = root[1] + (cb.y + 0.5) * h, cz = root[2] + (cb.z + 0.5) * h;
     for (int j = start[b] + lane; j < start[b + 1]; j += 32)
         rel[j] = make_float4((float)(xs[j] - cx), (float)(ys[j] - cy), (float)(zs[j] - cz), qs[j]);
+    }
 }
 
-template <int WS>
-__global__ void __launch_bounds__(kWarps * 32)
-p2p_kernel(int nbox, const int *__restrict__ start, const int4 *__restrict__ coord, const int *__restrict__ nbr,
-           const double *__restrict__ xs, const double *__restrict__ ys, const double *__restrict__ zs,
-           const float *__restrict__ qs, const double *__restrict__ qm, const double *__restrict__ root,
-           int level, float eps2, double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az,
-           unsigned long long *__restrict__ counts, const int *__restrict__ has_tgt,
+// Near field of one leaf box per warp.  The box's non-empty near boxes are
+// first compacted into shared memory with a running count of their sources;
+// the sources are then streamed 32 at a time across box boundaries (each lane
+// walks forward to the box of its staged source), so the pair loop runs
+// without per-box padding or per-box overhead.  CLAMP: floor r^2 at kMinR2,
+// needed only when eps^2 < kMinR2 (a zero-distance pair without softening).  Targets: one per lane; a
+// chunk of nt < 32 targets gives each target a group of g lanes (a power of
+// two, nt * g <= 32) that split the staged sources.  Each 32-source chunk's
+// FP32 partial sum is added with Kahan compensation.
+template <int WS, bool CLAMP>
+__global__ void __launch_bounds__(kWarps * 32, 8)
+p2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, const int *__restrict__ start,
+           const int4 *__restrict__ coord, const int *__restrict__ nbr, const double *__restrict__ qm,
+           const double *__restrict__ roots, int level, float eps2, double *__restrict__ ax, double *__restrict__ ay,
+           double *__restrict__ az, unsigned long long *__restrict__ counts, const int *__restrict__ has_tgt,
            const float4 *__restrict__ rel) {
     constexpr int NS1 = 2 * WS + 1, NS = NS1 * NS1 * NS1;
+    constexpr int NSP = (NS + 31) / 32 * 32;
     __shared__ float4 src[kWarps][32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int b = blockIdx.x * kWarps + wid;
-    if (b >= nbox || !has_tgt[b]) return;
-    const float hf = (float)(root[3] / (double)(1 << level));  // a power of two: k * hf is exact
-    const int4 cb = coord[b];
-    const int t0 = start[b], t1 = start[b + 1];
+    __shared__ int2 nb_rng[kWarps][NSP];    // (first source, running source count at the box's end)
+    __shared__ float4 nb_off[kWarps][NSP];  // source box centre - target box centre (exact in FP32)
     unsigned long long pairs = 0;
+    const unsigned lt_mask = (1u << (threadIdx.x & 31)) - 1u;
+    SV_WARP_BOXES(kWarps) {
+    if (!has_tgt[b]) continue;
+    // a power of two: k * hf is exact
+    const float hf = (float)(box_root(roots, bpid, b)[3] / (double)(1 << level));
+    const int4 cb = coord[b];
+    int nnz = 0, total = 0;
+    for (int s0 = 0; s0 < NS; s0 += 32) {
+        const int s = s0 + lane;
+        int Q = -1, j0 = 0, cnt = 0;
+        if (s < NS) {
+            Q = nbr[b * NS + s];
+            if (Q >= 0) {
+                j0 = start[Q];
+                cnt = start[Q + 1] - j0;
+            }
+        }
+        const bool f = cnt > 0;
+        const unsigned bal = __ballot_sync(0xffffffffu, f);
+        int inc = cnt;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        if (f) {
+            const int pos = nnz + __popc(bal & lt_mask);
+            const int4 cq = coord[Q];
+            nb_rng[wid][pos] = make_int2(j0, total + inc);
+            nb_off[wid][pos] = make_float4((float)(cq.x - cb.x) * hf, (float)(cq.y - cb.y) * hf,
+                                           (float)(cq.z - cb.z) * hf, 0.f);
+        }
+        nnz += __popc(bal);
+        total += __shfl_sync(0xffffffffu, inc, 31);
+    }
+    __syncwarp();
+    const int t0 = start[b], t1 = start[b + 1];
     for (int tb = t0; tb < t1; tb += 32) {
-        // nt targets in this chunk; each gets a group of g lanes (g a power of
-        // two, nt * g <= 32) that split the sources, so a box's short tail
-        // chunk keeps the warp busy instead of idling 32 - nt lanes
         const int nt = min(32, t1 - tb);
         int lg = 0;
         while ((nt << (lg + 1)) <= 32) lg++;
@@ -581,68 +667,65 @@ p2p_kernel(int nbox, const int *__restrict__ start, const int4 *__restrict__ coo
         const int i = tb + (valid ? tloc : 0);
         const float4 ti = rel[i];
         const float tx = ti.x, ty = ti.y, tz = ti.z;
-        // per-source-box FP32 partial sums, accumulated across source boxes
-        // with Kahan compensation (FP64-level accuracy without FP64 ops)
+        if (lane == 0) pairs += (unsigned long long)total * (unsigned long long)nt;
         float sx = 0.f, sy = 0.f, sz = 0.f, ex = 0.f, ey = 0.f, ez = 0.f;
-        for (int s = 0; s < NS; s++) {
-            const int Q = nbr[b * NS + s];
-            if (Q < 0) continue;
-            const int j0 = start[Q], j1 = start[Q + 1];
-            if (lane == 0) pairs += (unsigned long long)(j1 - j0) * (unsigned long long)nt;
-            // source box centre relative to the target box centre, exact in FP32
-            const int4 cq = coord[Q];
-            const float ox = (float)(cq.x - cb.x) * hf, oy = (float)(cq.y - cb.y) * hf, oz = (float)(cq.z - cb.z) * hf;
+        int kb = 0, kbeg = 0;  // this lane's current source box and its first running index
+        for (int c0 = 0; c0 < total; c0 += 32) {
+            const int j = c0 + lane;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (j < total) {
+                int2 rg = nb_rng[wid][kb];
+                while (rg.y <= j) {
+                    kbeg = rg.y;
+                    rg = nb_rng[wid][++kb];
+                }
+                const float4 r = rel[rg.x + (j - kbeg)];
+                const float4 o = nb_off[wid][kb];
+                v = make_float4(r.x + o.x, r.y + o.y, r.z + o.z, r.w);
+            }
+            src[wid][lane] = v;
+            __syncwarp();
             float fx = 0.f, fy = 0.f, fz = 0.f;
-            for (int jb = j0; jb < j1; jb += 32) {
-                const int j = jb + lane;
-                float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-                if (j < j1) {
-                    const float4 r = rel[j];
-                    v = make_float4(r.x + ox, r.y + oy, r.z + oz, r.w);
-                }
-                src[wid][lane] = v;
-                __syncwarp();
-                const int cnt = min(32, j1 - jb);
-                if (g == 1) {
-                    // full chunk: every lane a target, all staged sources (zero-charge padding)
+            if (g == 1) {
+                // every lane a target, all 32 staged sources (zero-charge padding)
 #pragma unroll 8
-                    for (int k = 0; k < 32; k++) {
-                        const float4 u = src[wid][k];
-                        const float dx = tx - u.x, dy = ty - u.y, dz = tz - u.z;
-                        const float r2 = fmaxf(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2))), kMinR2);
-                        const float inv = rsqrtf(r2);
-                        const float w = u.w * inv * inv * inv;
-                        fx = fmaf(dx, w, fx);
-                        fy = fmaf(dy, w, fy);
-                        fz = fmaf(dz, w, fz);
-                    }
-                } else {
-                    for (int k = sub; k < cnt; k += g) {
-                        const float4 u = src[wid][k];
-                        const float dx = tx - u.x, dy = ty - u.y, dz = tz - u.z;
-                        const float r2 = fmaxf(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2))), kMinR2);
-                        const float inv = rsqrtf(r2);
-                        const float w = u.w * inv * inv * inv;
-                        fx = fmaf(dx, w, fx);
-                        fy = fmaf(dy, w, fy);
-                        fz = fmaf(dz, w, fz);
-                    }
+                for (int k = 0; k < 32; k++) {
+                    const float4 u = src[wid][k];
+                    const float dx = tx - u.x, dy = ty - u.y, dz = tz - u.z;
+                    float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+                    if (CLAMP) r2 = fmaxf(r2, kMinR2);
+                    const float inv = rsqrtf(r2);
+                    const float w = u.w * inv * inv * inv;
+                    fx = fmaf(dx, w, fx);
+                    fy = fmaf(dy, w, fy);
+                    fz = fmaf(dz, w, fz);
                 }
-                __syncwarp();
+            } else {
+#pragma unroll 4
+                for (int k = sub; k < 32; k += g) {
+                    const float4 u = src[wid][k];
+                    const float dx = tx - u.x, dy = ty - u.y, dz = tz - u.z;
+                    float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+                    if (CLAMP) r2 = fmaxf(r2, kMinR2);
+                    const float inv = rsqrtf(r2);
+                    const float w = u.w * inv * inv * inv;
+                    fx = fmaf(dx, w, fx);
+                    fy = fmaf(dy, w, fy);
+                    fz = fmaf(dz, w, fz);
+                }
             }
-            {
-                float y = fx - ex, t = sx + y;
-                ex = (t - sx) - y;
-                sx = t;
-                y = fy - ey;
-                t = sy + y;
-                ey = (t - sy) - y;
-                sy = t;
-                y = fz - ez;
-                t = sz + y;
-                ez = (t - sz) - y;
-                sz = t;
-            }
+            __syncwarp();
+            float y = fx - ex, t = sx + y;
+            ex = (t - sx) - y;
+            sx = t;
+            y = fy - ey;
+            t = sy + y;
+            ey = (t - sy) - y;
+            sy = t;
+            y = fz - ez;
+            t = sz + y;
+            ez = (t - sz) - y;
+            sz = t;
         }
         sx -= ex;
         sy -= ey;
@@ -660,7 +743,27 @@ p2p_kernel(int nbox, const int *__restrict__ start, const int4 *__restrict__ coo
             az[i] += (double)sz * c;
         }
     }
-    if (lane == 0 && pairs) atomicAdd(&counts[1], pairs);
+    __syncwarp();
+    }
+    if ((threadIdx.x & 31) == 0 && pairs) atomicAdd(&counts[1], pairs);
+}
+
+// P2P launch: well-separation and whether r^2 needs the kMinR2 floor
+inline void launch_p2p(int ws, float eps2, int grid, cudaStream_t st, int nbox, const int *nbd, const int *bpid,
+                       const int *start, const int4 *coord, const int *nbr, const double *qm, const double *roots,
+                       int level, double *ax, double *ay, double *az, unsigned long long *counts,
+                       const int *has_tgt, const float4 *rel) {
+    const bool clamp = !(eps2 >= kMinR2);
+#define SV_P2P(W, C) p2p_kernel<W, C><<<grid, kWarps * 32, 0, st>>>(nbox, nbd, bpid, start, coord, nbr, qm, roots, \
+                                                                   level, eps2, ax, ay, az, counts, has_tgt, rel)
+    if (ws == 1) {
+        if (clamp) SV_P2P(1, true);
+        else SV_P2P(1, false);
+    } else {
+        if (clamp) SV_P2P(2, true);
+        else SV_P2P(2, false);
+    }
+#undef SV_P2P
 }
 
 template <int P>
@@ -703,11 +806,10 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         nbr[l] = (int *)carve(nb * ns * sizeof(int));
         lst[l] = (int2 *)carve(nb * cap * sizeof(int2));
         cnt[l] = (int *)carve(nb * sizeof(int));
-        SV_CK(c, cudaMemsetAsync(nbr[l], 0xff, nb * ns * sizeof(int), c->stream));
     }
     phase_mark(c, 2);
     SV_CK(c, cudaMemsetAsync(F.d_counts, 0, 2 * sizeof(unsigned long long), c->stream));
-    root_nbr_kernel<<<1, 32, 0, c->stream>>>(nbr[0], ns);
+    root_nbr_kernel<<<1, 128, 0, c->stream>>>(nbr[0], ns, 1, nullptr);
     SV_LAUNCHED(c);
     // which boxes hold targets (all of them unless symmetry images are present)
     int *tgt[kMortonBits + 1];
@@ -725,12 +827,12 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
             tgt[l] = F.has_tgt + o;
             o += T.lv[l].nbox;
         }
-        leaf_targets_kernel<<<div_up(T.lv[L].nbox, 256), 256, 0, c->stream>>>(T.lv[L].nbox, T.lv[L].start, S.qm,
-                                                                                tgt[L]);
+        leaf_targets_kernel<<<div_up(T.lv[L].nbox, 256), 256, 0, c->stream>>>(T.lv[L].nbox, nullptr,
+                                                                                T.lv[L].start, S.qm, tgt[L]);
         SV_LAUNCHED(c);
         for (int l = L - 1; l >= 0; l--) {
-            parent_targets_kernel<<<div_up(T.lv[l].nbox, 256), 256, 0, c->stream>>>(T.lv[l].nbox, T.lv[l].child0,
-                                                                                      tgt[l + 1], tgt[l]);
+            parent_targets_kernel<<<div_up(T.lv[l].nbox, 256), 256, 0, c->stream>>>(
+                T.lv[l].nbox, nullptr, T.lv[l].child0, tgt[l + 1], tgt[l]);
             SV_LAUNCHED(c);
         }
     }
@@ -739,10 +841,10 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         const Level &U = T.lv[l - 1];
         if (ws == 1)
             build_lists_kernel<1><<<div_up(V.nbox, 128), 128, 0, c->stream>>>(
-                V.nbox, V.parent, V.coord, nbr[l - 1], U.child0, nbr[l], lst[l], cnt[l], cap, F.d_counts);
+                V.nbox, nullptr, V.parent, V.coord, nbr[l - 1], U.child0, nbr[l], lst[l], cnt[l], cap, F.d_counts);
         else
             build_lists_kernel<2><<<div_up(V.nbox, 128), 128, 0, c->stream>>>(
-                V.nbox, V.parent, V.coord, nbr[l - 1], U.child0, nbr[l], lst[l], cnt[l], cap, F.d_counts);
+                V.nbox, nullptr, V.parent, V.coord, nbr[l - 1], U.child0, nbr[l], lst[l], cnt[l], cap, F.d_counts);
         SV_LAUNCHED(c);
     }
     phase_mark(c, 3);
@@ -750,13 +852,13 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
     {
         const Level &V = T.lv[L];
         p2m_kernel<P><<<div_up(V.nbox, p2m_warps<P>()), p2m_warps<P>() * 32, 0, c->stream>>>(
-            V.nbox, V.start, V.coord, S.x, S.y, S.z, S.q, S.root, L, F.nrm, Mv[L]);
+            V.nbox, nullptr, nullptr, V.start, V.coord, S.x, S.y, S.z, S.q, S.root, L, F.nrm, Mv[L]);
         SV_LAUNCHED(c);
     }
     for (int l = L - 1; l >= 2; l--) {
         const Level &V = T.lv[l];
-        m2m_kernel<P><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(V.nbox, V.child0, T.lv[l + 1].coord,
-                                                                              Mv[l + 1], Mv[l], F.nrm, F.oct);
+        m2m_kernel<P><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
+            V.nbox, nullptr, V.child0, T.lv[l + 1].coord, Mv[l + 1], Mv[l], F.nrm, F.oct);
         SV_LAUNCHED(c);
     }
     phase_mark(c, 4);
@@ -765,6 +867,8 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         const Level &V = T.lv[l];
         DownArgs a;
         a.nbox = V.nbox;
+        a.nbd = nullptr;
+        a.bpid = nullptr;
         a.level = l;
         a.cap = cap;
         a.esz = F.H.esz;
@@ -797,7 +901,8 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         const Level &V = T.lv[L];
         if (L >= 2) {
             l2p_kernel<P><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
-                V.nbox, V.start, V.coord, S.x, S.y, S.z, S.qm, S.root, L, F.nrm, Lv[L], S.ax, S.ay, S.az, tgt[L]);
+                V.nbox, nullptr, nullptr, V.start, V.coord, S.x, S.y, S.z, S.qm, S.root, L, F.nrm, Lv[L], S.ax, S.ay,
+                S.az, tgt[L]);
             SV_LAUNCHED(c);
         } else {
             SV_CK(c, cudaMemsetAsync(S.ax, 0, sizeof(double) * c->S.n, c->stream));
@@ -812,22 +917,123 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
             F.rel_cap = c->S.n;
         }
         box_relative_kernel<<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
-            V.nbox, V.start, V.coord, S.x, S.y, S.z, S.q, S.root, L, F.rel);
+            V.nbox, nullptr, nullptr, V.start, V.coord, S.x, S.y, S.z, S.q, S.root, L, F.rel);
         SV_LAUNCHED(c);
-        if (ws == 1)
-            p2p_kernel<1><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
-                V.nbox, V.start, V.coord, nbr[L], S.x, S.y, S.z, S.q, S.qm, S.root, L, (float)c->P.softening2,
-                S.ax, S.ay, S.az, F.d_counts, tgt[L], F.rel);
-        else
-            p2p_kernel<2><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
-                V.nbox, V.start, V.coord, nbr[L], S.x, S.y, S.z, S.q, S.qm, S.root, L, (float)c->P.softening2,
-                S.ax, S.ay, S.az, F.d_counts, tgt[L], F.rel);
+        launch_p2p(ws, (float)c->P.softening2, div_up(V.nbox, kWarps), c->stream, V.nbox, nullptr, nullptr, V.start,
+                   V.coord, nbr[L], S.qm, S.root, L, S.ax, S.ay, S.az, F.d_counts, tgt[L], F.rel);
         SV_LAUNCHED(c);
     }
     SV_CK(c, cudaMemcpyAsync(F.h_counts, F.d_counts, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                              c->stream));
     c->stats.levels = L;
     c->stats.boxes = T.lv[L].nbox;
+    return SV_OK;
+}
+
+
+// ------------------------------------------------------------------ forest --
+constexpr int kMaxGrid = 16 * kNumSMs;  // grid-stride launches: at most 16 CTAs per SM
+
+inline int forest_grid(int cap, int per_cta) {
+    const int g = div_up(cap > 0 ? cap : 1, per_cta);
+    return g < kMaxGrid ? g : kMaxGrid;
+}
+
+template <int P>
+sv_status run_fmm_forest(sv_ctx *c, Fmm &F, const ForestArgs &fa) {
+    const ForestSpec &f = fa.spec;
+    const int L = f.L;
+    const int ws = F.ws;
+    const int ns1 = 2 * ws + 1, ns = ns1 * ns1 * ns1;
+    const int cap = ns * 8 - ns;
+    Sorted &S = c->S;
+    Tree &T = *F.ftree;
+    int *nbd = fa.d_nbox;
+    SV_TRY(tree_build_forest(c, T, f, nbd, fa.d_err));
+    SV_CK(c, cudaMemsetAsync(F.d_counts, 0, 2 * sizeof(unsigned long long), c->stream));
+    root_nbr_kernel<<<forest_grid(f.cap[0] * ns, 256), 256, 0, c->stream>>>(F.fnbr[0], ns, f.cap[0], nbd);
+    SV_LAUNCHED(c);
+    leaf_targets_kernel<<<forest_grid(f.cap[L], 256), 256, 0, c->stream>>>(f.cap[L], nbd + L, T.lv[L].start, S.qm,
+                                                                         F.ftgt[L]);
+    SV_LAUNCHED(c);
+    for (int l = L - 1; l >= 0; l--) {
+        parent_targets_kernel<<<forest_grid(f.cap[l], 256), 256, 0, c->stream>>>(f.cap[l], nbd + l, T.lv[l].child0,
+                                                                               F.ftgt[l + 1], F.ftgt[l]);
+        SV_LAUNCHED(c);
+    }
+    for (int l = 1; l <= L; l++) {
+        const Level &V = T.lv[l];
+        const Level &U = T.lv[l - 1];
+        if (ws == 1)
+            build_lists_kernel<1><<<forest_grid(f.cap[l], 128), 128, 0, c->stream>>>(
+                f.cap[l], nbd + l, V.parent, V.coord, F.fnbr[l - 1], U.child0, F.fnbr[l], F.flst[l], F.fcnt[l], cap,
+                F.d_counts);
+        else
+            build_lists_kernel<2><<<forest_grid(f.cap[l], 128), 128, 0, c->stream>>>(
+                f.cap[l], nbd + l, V.parent, V.coord, F.fnbr[l - 1], U.child0, F.fnbr[l], F.flst[l], F.fcnt[l], cap,
+                F.d_counts);
+        SV_LAUNCHED(c);
+    }
+    {
+        const Level &V = T.lv[L];
+        p2m_kernel<P><<<forest_grid(f.cap[L], p2m_warps<P>()), p2m_warps<P>() * 32, 0, c->stream>>>(
+            f.cap[L], nbd + L, V.pid, V.start, V.coord, S.x, S.y, S.z, S.q, fa.roots, L, F.nrm, F.fM[L]);
+        SV_LAUNCHED(c);
+    }
+    for (int l = L - 1; l >= 2; l--) {
+        const Level &V = T.lv[l];
+        m2m_kernel<P><<<forest_grid(f.cap[l], kWarps), kWarps * 32, 0, c->stream>>>(
+            f.cap[l], nbd + l, V.child0, T.lv[l + 1].coord, F.fM[l + 1], F.fM[l], F.nrm, F.oct);
+        SV_LAUNCHED(c);
+    }
+    for (int l = 2; l <= L; l++) {
+        const Level &V = T.lv[l];
+        DownArgs a;
+        a.nbox = f.cap[l];
+        a.nbd = nbd + l;
+        a.bpid = V.pid;
+        a.level = l;
+        a.cap = cap;
+        a.esz = F.H.esz;
+        a.osz = F.H.osz;
+        a.dsz = F.H.dsz;
+        a.has_parent = l > 2;
+        a.parent = V.parent;
+        a.coord = V.coord;
+        a.Lp = l > 2 ? F.fL[l - 1] : nullptr;
+        a.Ml = F.fM[l];
+        a.m2l = F.flst[l];
+        a.m2l_cnt = F.fcnt[l];
+        a.cls_theta = F.cls_theta;
+        a.cls_phase = F.cls_phase;
+        a.cls_rho2 = F.cls_rho2;
+        a.dmat = F.dmat;
+        a.zc = F.zc;
+        a.nrm = F.nrm;
+        a.oct = F.oct;
+        a.root = fa.roots;
+        a.eps2 = c->P.softening2;
+        a.Lout = F.fL[l];
+        a.has_tgt = F.ftgt[l];
+        down_kernel<P><<<forest_grid(f.cap[l], kWarps), kWarps * 32, 0, c->stream>>>(a);
+        SV_LAUNCHED(c);
+    }
+    {
+        const Level &V = T.lv[L];
+        const int g = forest_grid(f.cap[L], kWarps);
+        l2p_kernel<P><<<g, kWarps * 32, 0, c->stream>>>(f.cap[L], nbd + L, V.pid, V.start, V.coord, S.x, S.y, S.z,
+                                                        S.qm, fa.roots, L, F.nrm, F.fL[L], S.ax, S.ay, S.az,
+                                                        F.ftgt[L]);
+        SV_LAUNCHED(c);
+        box_relative_kernel<<<g, kWarps * 32, 0, c->stream>>>(f.cap[L], nbd + L, V.pid, V.start, V.coord, S.x, S.y,
+                                                              S.z, S.q, fa.roots, L, F.frel);
+        SV_LAUNCHED(c);
+        launch_p2p(ws, (float)c->P.softening2, g, c->stream, f.cap[L], nbd + L, V.pid, V.start, V.coord, F.fnbr[L],
+                   S.qm, fa.roots, L, S.ax, S.ay, S.az, F.d_counts, F.ftgt[L], F.frel);
+        SV_LAUNCHED(c);
+    }
+    SV_CK(c, cudaMemcpyAsync(F.h_counts, F.d_counts, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                             c->stream));
     return SV_OK;
 }
 
@@ -866,6 +1072,11 @@ void fmm_free(sv_ctx *c) {
     cudaFree(F.zc); cudaFree(F.nrm); cudaFree(F.oct); cudaFree(F.arena); cudaFree(F.d_counts);
     cudaFree(F.ex); cudaFree(F.ey); cudaFree(F.ez); cudaFree(F.eq); cudaFree(F.em); cudaFree(F.est);
     cudaFree(F.eoff); cudaFree(F.has_tgt); cudaFree(F.rel);
+    cudaFree(F.farena); cudaFree(F.frel);
+    if (F.ftree) {
+        tree_release(*F.ftree);
+        delete F.ftree;
+    }
     cudaFreeHost(F.h_counts);
     delete c->fmm;
     c->fmm = nullptr;
@@ -960,6 +1171,74 @@ sv_status fmm_accel(sv_ctx *c) {
     default: SV_TRY(run_fmm<10>(c, F, *T)); break;
     }
     return SV_OK;
+}
+
+sv_status fmm_forest_reserve(sv_ctx *c, const ForestArgs &fa) {
+    const int p = fa.p;
+    if (p != 4 && p != 6 && p != 8 && p != 10)
+        return set_error(c, SV_ERR_UNSUPPORTED, "FMM order %d not instantiated (4, 6, 8, 10)", p);
+    if (fa.ws != 1 && fa.ws != 2) return set_error(c, SV_ERR_INVALID, "well-separation must be 1 or 2");
+    const ForestSpec &f = fa.spec;
+    if (f.L < 2 || f.L > kMortonBits) return set_error(c, SV_ERR_INVALID, "forest leaf level %d", f.L);
+    SV_TRY(fmm_state(c));
+    Fmm &F = *c->fmm;
+    SV_TRY(ensure_tables(c, F, p, fa.ws));
+    if (!F.ftree) F.ftree = new Tree();
+    SV_TRY(tree_forest_reserve(c, *F.ftree, f));
+    const int NC = p * (p + 1) / 2;
+    const int ns1 = 2 * fa.ws + 1, ns = ns1 * ns1 * ns1, cap = 7 * ns;
+    auto rounded = [](size_t sz) { return (sz + 255) & ~(size_t)255; };
+    size_t bytes = 0;
+    for (int l = 0; l <= f.L; l++) {
+        const size_t nb = (size_t)f.cap[l];
+        bytes += 2 * rounded(nb * NC * sizeof(float2)) + rounded(nb * ns * sizeof(int)) +
+                 rounded(nb * cap * sizeof(int2)) + 2 * rounded(nb * sizeof(int));
+    }
+    if (F.farena_bytes < bytes) {
+        cudaFree(F.farena);
+        F.farena = nullptr;
+        F.farena_bytes = 0;
+        SV_CK(c, cudaMalloc(&F.farena, bytes));
+        F.farena_bytes = bytes;
+    }
+    char *q = (char *)F.farena;
+    auto carve = [&](size_t sz) {
+        char *r = q;
+        q += (sz + 255) & ~(size_t)255;
+        return (void *)r;
+    };
+    for (int l = 0; l <= kMortonBits; l++) {
+        F.fM[l] = F.fL[l] = nullptr;
+        F.fnbr[l] = F.fcnt[l] = F.ftgt[l] = nullptr;
+        F.flst[l] = nullptr;
+    }
+    for (int l = 0; l <= f.L; l++) {
+        const size_t nb = (size_t)f.cap[l];
+        F.fM[l] = (float2 *)carve(nb * NC * sizeof(float2));
+        F.fL[l] = (float2 *)carve(nb * NC * sizeof(float2));
+        F.fnbr[l] = (int *)carve(nb * ns * sizeof(int));
+        F.flst[l] = (int2 *)carve(nb * cap * sizeof(int2));
+        F.fcnt[l] = (int *)carve(nb * sizeof(int));
+        F.ftgt[l] = (int *)carve(nb * sizeof(int));
+    }
+    if (F.frel_cap < f.n) {
+        cudaFree(F.frel);
+        F.frel = nullptr;
+        SV_CK(c, cudaMalloc(&F.frel, sizeof(float4) * (size_t)std::max(f.n, 1)));
+        F.frel_cap = f.n;
+    }
+    return SV_OK;
+}
+
+sv_status fmm_forest_run(sv_ctx *c, const ForestArgs &fa) {
+    if (fa.spec.n <= 0) return SV_OK;
+    Fmm &F = *c->fmm;
+    switch (fa.p) {
+    case 4: return run_fmm_forest<4>(c, F, fa);
+    case 6: return run_fmm_forest<6>(c, F, fa);
+    case 8: return run_fmm_forest<8>(c, F, fa);
+    default: return run_fmm_forest<10>(c, F, fa);
+    }
 }
 
 sv_status fmm_counts(sv_ctx *c, double *m2l, double *pairs) {

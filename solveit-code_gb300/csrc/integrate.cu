@@ -17,7 +17,9 @@ namespace {
 __global__ void drift_kernel(double *__restrict__ x, double *__restrict__ y, double *__restrict__ z,
                              const double *__restrict__ vx, const double *__restrict__ vy,
                              const double *__restrict__ vz, const int32_t *__restrict__ st,
-                             const double *__restrict__ t_inj, int64_t n, double t_start, double h) {
+                             const double *__restrict__ t_inj, int64_t n, double t_start, double h,
+                             const double *__restrict__ tb) {
+    if (tb) t_start += tb[0] + tb[1] * tb[2];
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         const int32_t w = st[i];
@@ -34,7 +36,8 @@ __global__ void kick_kernel(double *__restrict__ vx, double *__restrict__ vy, do
                             const double *__restrict__ az, const double *__restrict__ q,
                             const double *__restrict__ m, const int32_t *__restrict__ st,
                             const double *__restrict__ t_inj, int64_t n, double t_start, double dt,
-                            double eoa, double ex, double ey, double ez) {
+                            double eoa, double ex, double ey, double ez, const double *__restrict__ tb) {
+    if (tb) t_start += tb[0] + tb[1] * tb[2];
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         if (st[i] != 1) continue;
@@ -113,17 +116,17 @@ int stream_grid(int64_t n) {
 
 }  // namespace
 
-sv_status drift(sv_ctx *c, double t_start, double h) {
+sv_status drift(sv_ctx *c, double t_start, double h, const double *tb) {
     drift_kernel<<<stream_grid(c->n), 256, 0, c->stream>>>(c->x, c->y, c->z, c->vx, c->vy, c->vz, c->status,
-                                                           c->t_inj, c->n, t_start, h);
+                                                           c->t_inj, c->n, t_start, h, tb);
     SV_LAUNCHED(c);
     return SV_OK;
 }
 
-sv_status kick(sv_ctx *c, double t_start, double dt) {
+sv_status kick(sv_ctx *c, double t_start, double dt, const double *tb) {
     kick_kernel<<<stream_grid(c->n), 256, 0, c->stream>>>(
         c->vx, c->vy, c->vz, c->ax, c->ay, c->az, c->q, c->m, c->status, c->t_inj, c->n, t_start, dt,
-        c->P.e_over_amu, c->P.efield[0], c->P.efield[1], c->P.efield[2]);
+        c->P.e_over_amu, c->P.efield[0], c->P.efield[1], c->P.efield[2], tb);
     SV_LAUNCHED(c);
     return SV_OK;
 }

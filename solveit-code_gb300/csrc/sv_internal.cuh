@@ -54,6 +54,7 @@ struct Fmm;   // fmm.cu
 struct Tree;  // tree.cu
 struct Bh;    // bh.cu
 struct Adj;   // adjoint.cu
+struct Batch; // batch.cu
 
 }  // namespace sv
 
@@ -75,6 +76,7 @@ struct sv_ctx {
     sv::Fmm *fmm = nullptr;
     sv::Bh *bh = nullptr;
     sv::Adj *adj = nullptr;
+    sv::Batch *batch = nullptr;   // set by sv_upload_batch
     // device staging for interleaved <-> SoA transfers
     void *d_stage = nullptr;
     size_t d_stage_bytes = 0;
@@ -161,9 +163,22 @@ sv_status compute_accel_device(sv_ctx *c, int64_t first, int64_t last);
 // adjoint.cu
 void adjoint_free(sv_ctx *c);
 
-// integrate.cu
-sv_status drift(sv_ctx *c, double t_start, double h);
-sv_status kick(sv_ctx *c, double t_start, double dt);
+// batch.cu: many plumes in one context (sv_upload_batch)
+sv_status batch_plan(sv_ctx *c, int32_t np, const int64_t *counts, const int32_t *method, const int32_t *sym);
+sv_status batch_accel(sv_ctx *c);
+sv_status batch_leapfrog(sv_ctx *c, int32_t nsteps, double dt, double t0);
+sv_status batch_tune(sv_ctx *c, const char *cache_path, double *best_ms);
+sv_status batch_set_tuning(sv_ctx *c, int leaf_target, int direct_chunk);
+sv_status batch_info(const sv_ctx *c, sv_batch_info *out);
+void batch_invalidate(sv_ctx *c);
+bool batch_same_shape(const sv_ctx *c, int32_t np, const int64_t *counts, const int32_t *method,
+                      const int32_t *sym);
+void batch_free(sv_ctx *c);
+
+// integrate.cu.  With tb (device {t0, dt, k}), the step's start time
+// t0 + dt * k is added to t_start on the device (CUDA-graph replays).
+sv_status drift(sv_ctx *c, double t_start, double h, const double *tb = nullptr);
+sv_status kick(sv_ctx *c, double t_start, double dt, const double *tb = nullptr);
 sv_status energy(sv_ctx *c, double *ke, double *pe);
 
 // image offsets (metres) of the translational lattice, in summation order

@@ -85,12 +85,33 @@ __global__ void window_depth(const uint8_t *__restrict__ lvl, int n, int leaf, i
     if ((threadIdx.x & 31) == 0 && m > 0) atomicMax(out, m);
 }
 
+// Forest variant: keys hold the plume id above 3*mbits Morton bits; a change
+// of plume opens a new root (level 0).  Every slot takes part (slots that are
+// no source carry zero charge), so there is no inactive tail.
+__global__ void split_levels_forest(const uint64_t *__restrict__ keys, int n, int mbits, uint8_t *__restrict__ lvl) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint8_t l = 0;
+    if (i > 0) {
+        const uint64_t x = keys[i] ^ keys[i - 1];
+        if (x == 0) {
+            l = kLevels;
+        } else {
+            const int b = 63 - __clzll((long long)x);
+            l = b >= 3 * mbits ? 0 : (uint8_t)(mbits - b / 3);
+        }
+    }
+    lvl[i] = l;
+}
+
 struct LevelPtrs {
     int *start[kLevels];
     int *parent[kLevels];
     int *child0[kLevels];
     int4 *coord[kLevels];
+    int *pid[kLevels];           // plume of each box (forest) or null
     int nbox[kLevels];
+    int cap[kLevels];            // box capacity per level (forest) or 0
     int first_box[kLevels + 1];  // prefix sums of nbox (flattened box index)
 };
 
@@ -124,8 +145,10 @@ count_starts(const uint8_t *__restrict__ lvl, int n, int L, int *__restrict__ cn
     }
 }
 
-// Exclusive scan over the CTAs of each level (one block per level).
-__global__ void __launch_bounds__(1024) scan_counts(int *__restrict__ cnt, int nblk) {
+// Exclusive scan over the CTAs of each level (one block per level).  With
+// nbox_out: the level's box count, clamped to cap[l] (err set when clamped).
+__global__ void __launch_bounds__(1024) scan_counts(int *__restrict__ cnt, int nblk, int *__restrict__ nbox_out,
+                                                    const int *__restrict__ cap, int *__restrict__ err) {
     __shared__ int buf[1024];
     __shared__ int carry;
     const int l = blockIdx.x;
@@ -147,13 +170,23 @@ __global__ void __launch_bounds__(1024) scan_counts(int *__restrict__ cnt, int n
         if (threadIdx.x == 1023) carry += buf[1023];
         __syncthreads();
     }
+    if (nbox_out && threadIdx.x == 0) {
+        int t = carry;
+        atomicMax(&nbox_out[2 * kLevels + l], t);  // largest count seen, for capacity planning
+        if (t > cap[l]) {
+            atomicOr(err, 1 << l);
+            t = cap[l];
+        }
+        nbox_out[l] = t;
+    }
 }
 
 // Every particle that starts a box at level l writes its index as that box's
 // start, and the box's integer coordinates from its Morton key.
 __global__ void __launch_bounds__(kBuildThreads)
-scatter_starts(const uint8_t *__restrict__ lvl, const uint64_t *__restrict__ keys, int n, int L,
+scatter_starts(const uint8_t *__restrict__ lvl, const uint64_t *__restrict__ keys, int n, int L, int mbits,
                const int *__restrict__ off, LevelPtrs P) {
+    const uint64_t mmask = mbits >= 21 ? ~0ull : ((1ull << (3 * mbits)) - 1ull);
     __shared__ int wc[kBuildThreads / 32];
     __shared__ int wpre[kBuildThreads / 32];
     const int i = blockIdx.x * kBuildThreads + threadIdx.x;
@@ -178,9 +211,12 @@ scatter_starts(const uint8_t *__restrict__ lvl, const uint64_t *__restrict__ key
         __syncthreads();
         if (f) {
             const int idx = off[blockIdx.x * kLevels + l] + wpre[w] + __popc(bal & lt);
-            P.start[l][idx] = i;
-            const uint64_t k = key >> (3 * (kMortonBits - l));
-            P.coord[l][idx] = make_int4((int)compact3(k), (int)compact3(k >> 1), (int)compact3(k >> 2), 0);
+            if (P.cap[l] == 0 || idx < P.cap[l]) {
+                P.start[l][idx] = i;
+                const uint64_t k = (key & mmask) >> (3 * (mbits - l));
+                P.coord[l][idx] = make_int4((int)compact3(k), (int)compact3(k >> 1), (int)compact3(k >> 2), 0);
+                if (P.pid[l]) P.pid[l][idx] = (int)(key >> (3 * mbits));
+            }
         }
         __syncthreads();
     }
@@ -215,6 +251,25 @@ __global__ void link_levels(int L, int n_act, int total, LevelPtrs P) {
     }
     if (l >= 1) P.parent[l][b] = upper_bound_i(P.start[l - 1], P.nbox[l - 1], s) - 1;
     if (l < L) P.child0[l][b] = upper_bound_i(P.start[l + 1], P.nbox[l + 1], s) - 1;
+}
+
+// Forest variant of link_levels: box counts live on the device; blockIdx.y
+// is the level, boxes are visited grid-stride.
+__global__ void link_levels_forest(int L, int n, const int *__restrict__ nbox, LevelPtrs P) {
+    const int l = blockIdx.y;
+    const int nb = nbox[l];
+    const int nb_up = l >= 1 ? nbox[l - 1] : 0, nb_dn = l < L ? nbox[l + 1] : 0;
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
+        const int s = P.start[l][b];
+        const int e = b + 1 < nb ? P.start[l][b + 1] : n;
+        P.coord[l][b].w = e - s;
+        if (b == 0) {
+            P.start[l][nb] = n;
+            if (l < L) P.child0[l][nb] = nb_dn;
+        }
+        if (l >= 1) P.parent[l][b] = upper_bound_i(P.start[l - 1], nb_up, s) - 1;
+        if (l < L) P.child0[l][b] = upper_bound_i(P.start[l + 1], nb_dn, s) - 1;
+    }
 }
 
 sv_status arena_reserve(sv_ctx *c, Tree &T, size_t bytes) {
@@ -352,11 +407,88 @@ sv_status tree_build(sv_ctx *c, int depth_rule, int param, Tree **out) {
     const int nblk = div_up(na, kBuildThreads);
     count_starts<<<nblk, kBuildThreads, 0, c->stream>>>(T.lvl, na, L, T.scratch);
     SV_LAUNCHED(c);
-    scan_counts<<<L + 1, 1024, 0, c->stream>>>(T.scratch, nblk);
+    scan_counts<<<L + 1, 1024, 0, c->stream>>>(T.scratch, nblk, nullptr, nullptr, nullptr);
     SV_LAUNCHED(c);
-    scatter_starts<<<nblk, kBuildThreads, 0, c->stream>>>(T.lvl, c->S.keys, na, L, T.scratch, P);
+    scatter_starts<<<nblk, kBuildThreads, 0, c->stream>>>(T.lvl, c->S.keys, na, L, kMortonBits, T.scratch, P);
     SV_LAUNCHED(c);
     link_levels<<<div_up(total, 256), 256, 0, c->stream>>>(L, na, total, P);
+    SV_LAUNCHED(c);
+    return SV_OK;
+}
+
+void tree_release(Tree &T) {
+    cudaFree(T.lvl);
+    cudaFree(T.hist);
+    cudaFree(T.scratch);
+    cudaFree(T.arena);
+    cudaFreeHost(T.h_hist);
+    T = Tree();
+}
+
+sv_status tree_forest_reserve(sv_ctx *c, Tree &T, const ForestSpec &f) {
+    const int n = std::max(f.n, 1);
+    if (T.cap < n) {
+        cudaFree(T.lvl);
+        cudaFree(T.scratch);
+        T.lvl = nullptr;
+        T.scratch = nullptr;
+        const int cap = std::max(n, 1024);
+        SV_CK(c, cudaMalloc(&T.lvl, cap));
+        SV_CK(c, cudaMalloc(&T.scratch, sizeof(int) * (size_t)kLevels * (cap / kBuildThreads + 1)));
+        T.cap = cap;
+    }
+    auto rounded = [](size_t sz) { return (sz + 255) & ~(size_t)255; };
+    size_t bytes = 0;
+    for (int l = 0; l <= f.L; l++) {
+        const size_t nb = (size_t)f.cap[l];
+        bytes += 2 * rounded(sizeof(int) * (nb + 1)) + 2 * rounded(sizeof(int) * nb) + rounded(sizeof(int4) * nb);
+    }
+    SV_TRY(arena_reserve(c, T, bytes));
+    char *p = (char *)T.arena;
+    auto carve = [&](size_t sz) {
+        char *r = p;
+        p += (sz + 255) & ~(size_t)255;
+        return (void *)r;
+    };
+    for (int l = 0; l <= f.L; l++) {
+        Level &V = T.lv[l];
+        V.cap = f.cap[l];
+        V.nbox = f.cap[l];
+        V.start = (int *)carve(sizeof(int) * (V.cap + 1));
+        V.parent = (int *)carve(sizeof(int) * V.cap);
+        V.child0 = (int *)carve(sizeof(int) * (V.cap + 1));
+        V.coord = (int4 *)carve(sizeof(int4) * V.cap);
+        V.pid = (int *)carve(sizeof(int) * V.cap);
+    }
+    T.deepest = f.L;
+    T.n_act = f.n;
+    return SV_OK;
+}
+
+sv_status tree_build_forest(sv_ctx *c, Tree &T, const ForestSpec &f, int *d_nbox, int *d_err) {
+    const int n = f.n, L = f.L;
+    if (n <= 0) return SV_OK;
+    split_levels_forest<<<div_up(n, 256), 256, 0, c->stream>>>(c->S.keys, n, f.mbits, T.lvl);
+    SV_LAUNCHED(c);
+    LevelPtrs P{};
+    for (int l = 0; l <= L; l++) {
+        P.start[l] = T.lv[l].start;
+        P.parent[l] = T.lv[l].parent;
+        P.child0[l] = T.lv[l].child0;
+        P.coord[l] = T.lv[l].coord;
+        P.pid[l] = T.lv[l].pid;
+        P.cap[l] = T.lv[l].cap;
+    }
+    const int nblk = div_up(n, kBuildThreads);
+    count_starts<<<nblk, kBuildThreads, 0, c->stream>>>(T.lvl, n, L, T.scratch);
+    SV_LAUNCHED(c);
+    scan_counts<<<L + 1, 1024, 0, c->stream>>>(T.scratch, nblk, d_nbox, d_nbox + kLevels, d_err);
+    SV_LAUNCHED(c);
+    scatter_starts<<<nblk, kBuildThreads, 0, c->stream>>>(T.lvl, c->S.keys, n, L, f.mbits, T.scratch, P);
+    SV_LAUNCHED(c);
+    int maxcap = 1;
+    for (int l = 0; l <= L; l++) maxcap = std::max(maxcap, f.cap[l]);
+    link_levels_forest<<<dim3(std::min(div_up(maxcap, 256), 4 * kNumSMs), L + 1), 256, 0, c->stream>>>(L, n, d_nbox, P);
     SV_LAUNCHED(c);
     return SV_OK;
 }

@@ -14,6 +14,8 @@ struct Level {
     int *parent = nullptr;  // [nbox] box index at level-1 (unused at level 0)
     int *child0 = nullptr;  // [nbox+1] first child at level+1 (child0[nbox] = boxes at level+1)
     int4 *coord = nullptr;  // [nbox] integer box coordinates (x, y, z) and particle count (w)
+    int *pid = nullptr;     // [nbox] plume of the box (forest only)
+    int cap = 0;            // box capacity (forest only)
 };
 
 struct Tree {
@@ -33,5 +35,25 @@ struct Tree {
 // Builds levels 0..deepest.  depth_rule kDepthMeanOccupancy uses param as the
 // target mean particles per occupied box at the deepest level.
 sv_status tree_build(sv_ctx *c, int depth_rule, int param, Tree **out);
+
+// A forest of octrees over many plumes sorted by (plume id, Morton key): the
+// first n slots of c->S, keys with the plume id above 3*mbits Morton bits.
+// Level 0 holds one root per plume.  The depth L and the per-level box
+// capacities are fixed, and box counts stay on the device, so a build issues
+// no host synchronisation and can be captured in a CUDA graph.
+struct ForestSpec {
+    int n = 0;
+    int L = 0;
+    int mbits = 18;
+    int cap[kMortonBits + 1] = {0};
+};
+// Allocates the forest's arrays for spec (host call, outside any capture).
+sv_status tree_forest_reserve(sv_ctx *c, Tree &T, const ForestSpec &f);
+// Launches only.  d_nbox is a device array of 3 (kMortonBits + 1) ints: the
+// first third receives each level's box count, clamped to the capacity that
+// the caller stored in the second third; the last third keeps the largest
+// unclamped count seen.  Bit l of *d_err is set when level l overflowed.
+sv_status tree_build_forest(sv_ctx *c, Tree &T, const ForestSpec &f, int *d_nbox, int *d_err);
+void tree_release(Tree &T);
 
 }  // namespace sv

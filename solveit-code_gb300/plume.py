@@ -55,6 +55,32 @@ def make_plume(n: int, length: float, seed: int, radius: float = 20e-9,
     }
 
 
+def make_batch(nplumes: int = 256, config: int = 3, nmin: int = 1024, nmax: int = 65536,
+               length: float = 1e-6, direct_below: int = 8192):
+    """The batched-plume workload: nplumes independent realisations.
+
+    Plume sizes are uniform integers in [nmin, nmax] drawn with seed
+    1000*config + 999; plume i is make_plume(N_i, length, 1000*config + i).
+    Plumes with N < direct_below use the direct sum, the others the FMM; the
+    even-numbered plumes use the 4-fold rotational variant.
+    Returns (states, methods, symmetries) with method 0 = direct, 2 = FMM and
+    symmetry 0 = none, 1 = rotational (the C ABI's codes).
+    """
+    rng = np.random.Generator(np.random.PCG64(1000 * config + 999))
+    sizes = rng.integers(nmin, nmax + 1, size=nplumes)
+    states = [make_plume(int(n), length, 1000 * config + i) for i, n in enumerate(sizes)]
+    methods = [0 if int(n) < direct_below else 2 for n in sizes]
+    syms = [1 if i % 2 == 0 else 0 for i in range(nplumes)]
+    return states, methods, syms
+
+
+def concat(states):
+    """One state dict holding every plume back to back, and the plume sizes."""
+    keys = ("x", "v", "q", "m", "species", "status", "t_inj")
+    out = {k: np.ascontiguousarray(np.concatenate([s[k] for s in states])) for k in keys}
+    return out, np.array([s["x"].shape[0] for s in states], np.int64)
+
+
 def to_ref32(state):
     """Pack a plume into the reference's FP32 vec4 arrays.
 

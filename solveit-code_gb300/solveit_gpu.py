@@ -29,7 +29,7 @@ ABI_SYMBOLS = (
     "sv_upload_ref32", "sv_download", "sv_download_ref32", "sv_compute_accel", "sv_add_accel_ref32",
     "sv_leapfrog", "sv_energy", "sv_compare_accel", "sv_get_stats", "sv_sync", "sv_stream",
     "sv_launch_count", "sv_last_error", "sv_abi_version", "sv_adjoint_forward", "sv_adjoint_backward",
-    "sv_direct_accel_noalloc",
+    "sv_direct_accel_noalloc", "sv_upload_batch", "sv_batch_tune", "sv_batch_get_info", "sv_batch_set_tuning",
 )
 
 
@@ -49,6 +49,18 @@ class Stats(C.Structure):
         ("pair_interactions", C.c_double), ("cell_interactions", C.c_double),
         ("flops_algorithmic", C.c_double), ("ms_total", C.c_double), ("ms_phase", C.c_double * 8),
         ("levels", C.c_int32), ("boxes", C.c_int32), ("reserved", C.c_int32 * 6),
+    ]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [
+        ("nplumes", C.c_int32), ("fmm_plumes", C.c_int32), ("slots", C.c_int64), ("fmm_slots", C.c_int64),
+        ("leaf_level", C.c_int32), ("leaf_target", C.c_int32), ("direct_chunk", C.c_int32),
+        ("direct_items", C.c_int32), ("graph_kernels_step", C.c_int32), ("graph_kernels_accel", C.c_int32),
+        ("tuned_ms", C.c_double), ("direct_pairs", C.c_double), ("fmm_m2l", C.c_double),
+        ("fmm_pairs", C.c_double), ("regrows", C.c_int32), ("overflow_mask", C.c_int32),
+        ("level_boxes", C.c_int32 * 22), ("level_cap", C.c_int32 * 22), ("level_max", C.c_int32 * 22),
+        ("reserved", C.c_int32 * 6),
     ]
 
 
@@ -99,6 +111,10 @@ def load(path: str = LIB_PATH):
     L.sv_adjoint_forward.argtypes = [vp, C.c_int32, C.c_double, C.c_double, C.c_int32]
     L.sv_adjoint_backward.argtypes = [vp, vp, vp, vp, vp, vp]
     L.sv_direct_accel_noalloc.argtypes = [C.c_int64, vp, vp, vp, vp, C.c_double, C.c_double, vp, vp]
+    L.sv_upload_batch.argtypes = [vp, C.c_int32, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+    L.sv_batch_tune.argtypes = [vp, C.c_char_p, C.POINTER(C.c_double)]
+    L.sv_batch_get_info.argtypes = [vp, C.POINTER(BatchInfo)]
+    L.sv_batch_set_tuning.argtypes = [vp, C.c_int32, C.c_int32]
     for name in ABI_SYMBOLS:
         if name not in ("sv_destroy", "sv_stream", "sv_launch_count", "sv_last_error", "sv_abi_version"):
             getattr(L, name).restype = C.c_int
@@ -184,6 +200,40 @@ class ForceMethod:
         t = None if t_inj is None else np.ascontiguousarray(t_inj, np.float32)
         self.n = p.shape[0]
         self._check(self.L.sv_upload_ref32(self.h, self.n, _p(p), _p(v), _p(a), _p(t)))
+
+    def upload_batch(self, states, methods, symmetries):
+        """Load many plumes (a list of state dicts) into this context.
+
+        methods[i]: DIRECT or FMM; symmetries[i]: SYM_NONE or SYM_ROTATIONAL.
+        """
+        x = np.ascontiguousarray(np.concatenate([s["x"] for s in states]), np.float64)
+        v = np.ascontiguousarray(np.concatenate([s["v"] for s in states]), np.float64)
+        q = np.ascontiguousarray(np.concatenate([s["q"] for s in states]), np.float64)
+        m = np.ascontiguousarray(np.concatenate([s["m"] for s in states]), np.float64)
+        st = np.ascontiguousarray(np.concatenate([s["status"] for s in states]), np.int32)
+        t = np.ascontiguousarray(np.concatenate([s["t_inj"] for s in states]), np.float64)
+        counts = np.array([s["x"].shape[0] for s in states], np.int64)
+        meth = np.ascontiguousarray(methods, np.int32)
+        sym = np.ascontiguousarray(symmetries, np.int32)
+        self.n = int(counts.sum())
+        self.counts = counts
+        self._check(self.L.sv_upload_batch(self.h, len(states), _p(counts), _p(meth), _p(sym), _p(x), _p(v),
+                                           _p(q), _p(m), _p(st), _p(t)))
+
+    def tune(self, cache_path=None):
+        """Autotune the uploaded batch; returns the tuned force-evaluation time in ms."""
+        ms = C.c_double()
+        path = None if cache_path is None else str(cache_path).encode()
+        self._check(self.L.sv_batch_tune(self.h, path, C.byref(ms)))
+        return ms.value
+
+    def set_tuning(self, leaf_target, direct_chunk):
+        self._check(self.L.sv_batch_set_tuning(self.h, leaf_target, direct_chunk))
+
+    def batch_info(self) -> BatchInfo:
+        b = BatchInfo()
+        self._check(self.L.sv_batch_get_info(self.h, C.byref(b)))
+        return b
 
     def download(self):
         x = np.zeros((self.n, 3), np.float64)
