@@ -140,43 +140,65 @@ __device__ __forceinline__ const double *box_root(const double *root, const int 
 
 // ---------------------------------------------------------------- lists --
 template <int WS>
-__global__ void build_lists_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ parent,
-                                   const int4 *__restrict__ coord, const int *__restrict__ pnbr,
-                                   const int *__restrict__ pchild0, int *__restrict__ nbr, int2 *__restrict__ m2l,
-                                   int *__restrict__ m2l_cnt, int cap, unsigned long long *__restrict__ counts) {
+__global__ void __launch_bounds__(kWarps * 32)
+build_lists_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ parent,
+                   const int4 *__restrict__ coord, const int *__restrict__ pnbr, const int *__restrict__ pchild0,
+                   int *__restrict__ nbr, int2 *__restrict__ m2l, int *__restrict__ m2l_cnt, int cap,
+                   unsigned long long *__restrict__ counts) {
+    // one warp per box: lanes take the parent's near slots; the children of
+    // each are classified round by round, M2L entries compacted by ballot
     constexpr int NS1 = 2 * WS + 1, NS = NS1 * NS1 * NS1, R = 2 * WS + 1, SIDE = 2 * R + 1;
-    const int nb = level_boxes(nbox, nbd);
     unsigned long long tot = 0;
-    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) {
-        int cnt = 0;
-        for (int s = 0; s < NS; s++) nbr[b * NS + s] = -1;
-        const int4 cb = coord[b];
-        const int par = parent[b];
-        for (int s = 0; s < NS; s++) {
+    const unsigned lt_mask = (1u << (threadIdx.x & 31)) - 1u;
+    SV_WARP_BOXES(kWarps) {
+    for (int s = lane; s < NS; s += 32) nbr[b * NS + s] = -1;
+    __syncwarp();
+    const int4 cb = coord[b];
+    const int par = parent[b];
+    int cnt = 0;
+    for (int s0 = 0; s0 < NS; s0 += 32) {
+        const int s = s0 + lane;
+        int c0 = 0, c1 = 0;
+        if (s < NS) {
             const int Q = pnbr[par * NS + s];
-            if (Q < 0) continue;
-            const int c1 = pchild0[Q + 1];
-            for (int ch = pchild0[Q]; ch < c1; ch++) {
+            if (Q >= 0) {
+                c0 = pchild0[Q];
+                c1 = pchild0[Q + 1];
+            }
+        }
+        for (int r = 0; r < 8; r++) {
+            const int ch = c0 + r;
+            bool far = false;
+            int cls = 0;
+            if (ch < c1) {
                 const int4 cc = coord[ch];
                 const int ox = cb.x - cc.x, oy = cb.y - cc.y, oz = cb.z - cc.z;
                 const int am = max(abs(ox), max(abs(oy), abs(oz)));
-                // a consistent tree keeps |offset| <= R; a forest level clamped to its
-                // capacity may not, and its result is discarded, but the class index
-                // must stay inside the tables
-                if (am > R) continue;
+                // a consistent tree keeps |offset| <= R; a forest level clamped to
+                // its capacity may not, and its result is discarded, but the class
+                // index must stay inside the tables
                 if (am <= WS) {
                     nbr[b * NS + ((ox + WS) * NS1 + (oy + WS)) * NS1 + (oz + WS)] = ch;
-                } else if (cnt < cap) {
-                    m2l[(size_t)b * cap + cnt] = make_int2(ch, ((ox + R) * SIDE + (oy + R)) * SIDE + (oz + R));
-                    cnt++;
+                } else if (am <= R) {
+                    far = true;
+                    cls = ((ox + R) * SIDE + (oy + R)) * SIDE + (oz + R);
                 }
             }
+            const unsigned bal = __ballot_sync(0xffffffffu, far);
+            if (far) {
+                const int pos = cnt + __popc(bal & lt_mask);
+                if (pos < cap) m2l[(size_t)b * cap + pos] = make_int2(ch, cls);
+            }
+            cnt += __popc(bal);
+            if (!__any_sync(0xffffffffu, ch + 1 < c1)) break;
         }
+    }
+    if (cnt > cap) cnt = cap;
+    if (lane == 0) {
         m2l_cnt[b] = cnt;
         tot += cnt;
     }
-    // warp-aggregated statistics
-    for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+    }
     if ((threadIdx.x & 31) == 0 && tot) atomicAdd(&counts[0], tot);
 }
 
@@ -840,10 +862,10 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         const Level &V = T.lv[l];
         const Level &U = T.lv[l - 1];
         if (ws == 1)
-            build_lists_kernel<1><<<div_up(V.nbox, 128), 128, 0, c->stream>>>(
+            build_lists_kernel<1><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
                 V.nbox, nullptr, V.parent, V.coord, nbr[l - 1], U.child0, nbr[l], lst[l], cnt[l], cap, F.d_counts);
         else
-            build_lists_kernel<2><<<div_up(V.nbox, 128), 128, 0, c->stream>>>(
+            build_lists_kernel<2><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
                 V.nbox, nullptr, V.parent, V.coord, nbr[l - 1], U.child0, nbr[l], lst[l], cnt[l], cap, F.d_counts);
         SV_LAUNCHED(c);
     }
@@ -965,11 +987,11 @@ sv_status run_fmm_forest(sv_ctx *c, Fmm &F, const ForestArgs &fa) {
         const Level &V = T.lv[l];
         const Level &U = T.lv[l - 1];
         if (ws == 1)
-            build_lists_kernel<1><<<forest_grid(f.cap[l], 128), 128, 0, c->stream>>>(
+            build_lists_kernel<1><<<forest_grid(f.cap[l], kWarps), kWarps * 32, 0, c->stream>>>(
                 f.cap[l], nbd + l, V.parent, V.coord, F.fnbr[l - 1], U.child0, F.fnbr[l], F.flst[l], F.fcnt[l], cap,
                 F.d_counts);
         else
-            build_lists_kernel<2><<<forest_grid(f.cap[l], 128), 128, 0, c->stream>>>(
+            build_lists_kernel<2><<<forest_grid(f.cap[l], kWarps), kWarps * 32, 0, c->stream>>>(
                 f.cap[l], nbd + l, V.parent, V.coord, F.fnbr[l - 1], U.child0, F.fnbr[l], F.flst[l], F.fcnt[l], cap,
                 F.d_counts);
         SV_LAUNCHED(c);
