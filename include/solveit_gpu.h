@@ -67,6 +67,19 @@ typedef enum {
     SV_PREC_FP64 = 1
 } sv_precision;
 
+/* FMM variant (FmmType, structures.h:283-288).  The treecode evaluates the
+ * far-field multipoles directly at the particles (M2P) instead of M2L/L2L/L2P;
+ * the outlier variants take particles whose position deviates from the median
+ * by 3 or more scaled median absolute deviations on any axis
+ * (DomainBoundsFunction::isOutlier, domain_bounds_functions.cpp:16-99) out of
+ * the tree and sum every interaction that involves one of them directly. */
+typedef enum {
+    SV_FMM_FMM = 0,               /* FmmType::fmm */
+    SV_FMM_FMM_OUTLIERS = 1,      /* FmmType::fmmOutliers */
+    SV_FMM_TREECODE = 2,          /* FmmType::treecode */
+    SV_FMM_TREECODE_OUTLIERS = 3  /* FmmType::treecodeOutliers */
+} sv_fmm_type;
+
 typedef struct {
     double softening2;       /* eps^2 in m^2 (constants.h:31 SOFTENING) */
     double k_const;          /* e^2/(4 pi eps0 amu) (constants.h:46 K_CONST) */
@@ -85,7 +98,8 @@ typedef struct {
     double domain_size[3];   /* periodic cell size in m (SimulationParameters::domainSize) */
     int32_t device;          /* CUDA device ordinal */
     int32_t profile_phases;  /* 1: record device time of each phase into sv_stats.ms_phase */
-    int32_t reserved[6];
+    int32_t fmm_type;        /* sv_fmm_type */
+    int32_t reserved[5];
 } sv_params;
 
 /* Per-call statistics of the last force evaluation. */
@@ -159,6 +173,12 @@ SV_API sv_status sv_adjoint_forward(sv_ctx *ctx, int32_t nsteps, double dt, doub
                                     int32_t checkpoint_every);
 SV_API sv_status sv_adjoint_backward(sv_ctx *ctx, const double *dl_dx3, const double *dl_dv3,
                                      double *dl_dx0, double *dl_dv0, double *dl_defield);
+
+/* Outlier flags of the last evaluation with an outlier variant of the FMM, in
+ * the caller's order, as the reference's outlierCheck
+ * (domain_bounds_functions.cpp:78-89): 1 outlier, 0 source within bounds,
+ * -1 no source; count receives the number of outliers.  Either may be null. */
+SV_API sv_status sv_get_outliers(sv_ctx *ctx, int32_t *flags, int64_t *count);
 
 /* Kinetic and softened potential energy in J, FP64, over all particles
  * (particles.cpp:535-578 with the halving of integration_schemes.cpp:815). */

@@ -57,6 +57,8 @@ def lib():
                                      C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int]
         L.orc_rel_l2.argtypes = [C.c_int64, _f64p, _f64p, C.c_void_p, C.POINTER(C.c_double),
                                  C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_double)]
+        L.orc_outliers.restype = C.c_int64
+        L.orc_outliers.argtypes = [C.c_int64, _f64p, _i32p, _i32p]
         _lib = L
     return _lib
 
@@ -165,6 +167,15 @@ def energy_f64(state, eps2, threads=0):
                          np.ascontiguousarray(state["m"], np.float64), eps2, C.byref(ke), C.byref(pe),
                          threads)
     return ke.value, pe.value
+
+
+def outliers(state):
+    """isOutlier restated: (flags, count), flags 1 / 0 / -1 as outlierCheck."""
+    x = np.ascontiguousarray(state["x"], np.float64).reshape(-1)
+    st = np.ascontiguousarray(state["status"], np.int32)
+    f = np.zeros(st.size, np.int32)
+    cnt = lib().orc_outliers(st.size, x, st, f)
+    return f, int(cnt)
 
 
 def rel_l2(a, ref, status=None):

@@ -8,7 +8,9 @@
 // reference's own updateAcceleration() / propagate*New() methods.
 //
 // usage: ref_harness <mode> <in.bin> <out.bin> [key=value ...]
-//   modes: direct | bh | fmm | dkd | grid
+//   modes: direct | bh | fmm | dkd | grid | outliers
+//          (outliers mode: int32 count, int32 outlierCheck[n] of
+//           DomainBoundsFunction::isOutlier)
 //   keys : threads, sym (0 none, 1 rotational, 2 translational), levels,
 //          axes (e.g. 110), dom (domain size x,y,z in metres), theta, p,
 //          maxlevel, steps, dt, ez
@@ -87,6 +89,23 @@ int main(int argc, char **argv) {
     }
     cp.firstParticle = 0;
     cp.lastParticle = n;
+
+    if (mode == "outliers") {
+        std::vector<int> check(n, 0);
+        int count = 0;
+        DomainBoundsFunction::isOutlier(cp, check.data(), count);
+        FILE *fo = std::fopen(argv[3], "wb");
+        if (!fo) return 3;
+        const int32_t cnt = count;
+        std::fwrite(&cnt, 4, 1, fo);
+        for (int i = 0; i < n; i++) {
+            const int32_t v = check[i];
+            std::fwrite(&v, 4, 1, fo);
+        }
+        std::fclose(fo);
+        std::fflush(nullptr);
+        std::_Exit(0);
+    }
 
     ps.params.numThreads = threads;
     ps.params.symType = sym == 1 ? SymmetryType::rotational

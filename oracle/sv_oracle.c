@@ -585,3 +585,59 @@ void orc_rel_l2(int64_t n, const double *a, const double *r,
     *argmax = arg;
     *global_l2 = den > 0 ? sqrt(num / den) : 0.0;
 }
+
+/* ------------------------------------------------------------- outliers -- */
+static int cmp_float(const void *a, const void *b) {
+    const float x = *(const float *)a, y = *(const float *)b;
+    return (x > y) - (x < y);
+}
+
+/* findTrueMedian (outlier_detection.h:117-133) by sorting a copy */
+static float true_median(float *v, int64_t n) {
+    if (n <= 0) return 0.0f;
+    qsort(v, (size_t)n, sizeof(float), cmp_float);
+    if (n & 1) return v[n / 2];
+    return (v[(n - 1) / 2] + v[n / 2]) / 2;
+}
+
+int64_t orc_outliers(int64_t n, const double *x3, const int32_t *status, int32_t *flags) {
+    const float factor = 1.482602218505602f; /* domain_bounds_functions.h:37 */
+    const float max_dev = 3.0f;              /* domain_bounds_functions.h:38 */
+    float *pos[3], *dev[3], *tmp = (float *)malloc(sizeof(float) * (size_t)(n > 0 ? n : 1));
+    float med[3], mad[3];
+    int64_t nv = 0, nout = 0;
+    for (int d = 0; d < 3; d++) {
+        pos[d] = (float *)malloc(sizeof(float) * (size_t)(n > 0 ? n : 1));
+        dev[d] = (float *)malloc(sizeof(float) * (size_t)(n > 0 ? n : 1));
+    }
+    for (int64_t i = 0; i < n; i++)
+        if (status[i] == 1 || status[i] == 2) {
+            for (int d = 0; d < 3; d++) pos[d][nv] = (float)x3[3 * i + d];
+            nv++;
+        }
+    for (int d = 0; d < 3; d++) {
+        memcpy(tmp, pos[d], sizeof(float) * (size_t)nv);
+        med[d] = true_median(tmp, nv);
+        for (int64_t k = 0; k < nv; k++) dev[d][k] = fabsf(pos[d][k] - med[d]);
+        memcpy(tmp, dev[d], sizeof(float) * (size_t)nv);
+        mad[d] = factor * true_median(tmp, nv);
+    }
+    int64_t k = 0;
+    for (int64_t i = 0; i < n; i++) {
+        if (!(status[i] == 1 || status[i] == 2)) {
+            flags[i] = -1;
+            continue;
+        }
+        int out = 0;
+        for (int d = 0; d < 3; d++) out |= (dev[d][k] / mad[d]) >= max_dev;
+        flags[i] = out;
+        nout += out;
+        k++;
+    }
+    for (int d = 0; d < 3; d++) {
+        free(pos[d]);
+        free(dev[d]);
+    }
+    free(tmp);
+    return nout;
+}

@@ -116,6 +116,19 @@ void orc_rel_l2(int64_t n, const double *a, const double *r,
                 const int32_t *status, double *l2, double *maxl2,
                 int64_t *argmax, double *global_l2);
 
+/* Outlier classification of DomainBoundsFunction::isOutlier
+ * (domain_bounds_functions.cpp:16-99) on FP32 positions: per axis the true
+ * median of the sources' positions (findTrueMedian, outlier_detection.h:117:
+ * middle element, or the mean of the two middle ones), the median of the
+ * absolute deviations times 1.482602218505602, and a source is an outlier
+ * when any axis deviates by >= 3 of those.  x3: 3n FP64 positions (rounded
+ * to FP32 as the reference's state is); flags[i] = 1 outlier, 0 inlier
+ * source, -1 not a source (status not 1 or 2).  Returns the outlier count.
+ * The deviations' median is taken over the sources (the reference takes it
+ * over its whole particle range; the two agree when every particle is a
+ * source). */
+int64_t orc_outliers(int64_t n, const double *x3, const int32_t *status, int32_t *flags);
+
 #ifdef __cplusplus
 }
 #endif

@@ -250,6 +250,8 @@ sv_status check_params(sv_ctx *c, const sv_params *p) {
     if (!(p->theta >= 0.0f) || p->theta > 1.0f) return set_error(c, SV_ERR_INVALID, "theta outside [0, 1]");
     if (p->fmm_leaf_target < 1 || p->fmm_leaf_target > 4096)
         return set_error(c, SV_ERR_INVALID, "fmm_leaf_target outside 1..4096");
+    if (p->fmm_type < SV_FMM_FMM || p->fmm_type > SV_FMM_TREECODE_OUTLIERS)
+        return set_error(c, SV_ERR_INVALID, "unknown fmm_type %d", p->fmm_type);
     if (p->symmetry == SV_SYM_TRANSLATIONAL) {
         if (p->sym_levels < 0 || p->sym_levels > 4) return set_error(c, SV_ERR_INVALID, "sym_levels outside 0..4");
         for (int d = 0; d < 3; d++)
@@ -294,6 +296,12 @@ sv_status sv_batch_tune(sv_ctx *c, const char *cache_path, double *best_ms) {
     if (!c->batch) return set_error(c, SV_ERR_STATE, "no batch uploaded");
     SV_CK(c, cudaSetDevice(c->device));
     return batch_tune(c, cache_path, best_ms);
+}
+
+sv_status sv_get_outliers(sv_ctx *c, int32_t *flags, int64_t *count) {
+    if (!c) return SV_ERR_INVALID;
+    SV_CK(c, cudaSetDevice(c->device));
+    return outliers_get(c, flags, count);
 }
 
 sv_status sv_batch_set_tuning(sv_ctx *c, int32_t leaf_target, int32_t direct_chunk) {
@@ -375,6 +383,7 @@ void sv_destroy(sv_ctx *c) {
     bh_free(c);
     adjoint_free(c);
     batch_free(c);
+    outliers_free(c);
     free_state(c);
     Sorted &S = c->S;
     cudaFree(S.x); cudaFree(S.y); cudaFree(S.z); cudaFree(S.q); cudaFree(S.qm);
@@ -528,12 +537,23 @@ sv_status sv::compute_accel_device(sv_ctx *c, int64_t first, int64_t last) {
         return SV_OK;
     }
     SV_CK(c, cudaEventRecord(c->ev_begin, c->stream));
+    const bool outliers = c->P.method == SV_METHOD_FMM &&
+                          (c->P.fmm_type == SV_FMM_FMM_OUTLIERS || c->P.fmm_type == SV_FMM_TREECODE_OUTLIERS);
+    if (outliers && c->P.symmetry != SV_SYM_NONE)
+        return set_error(c, SV_ERR_UNSUPPORTED, "the outlier variants run without symmetry images");
     if (n > 0) {
         phase_mark(c, 0);
-        if (c->P.method == SV_METHOD_FMM && c->P.symmetry != SV_SYM_NONE)
+        if (outliers) {
+            // outliers leave the tree; their interactions are summed directly below
+            const int32_t *st2 = nullptr;
+            SV_TRY(outliers_detect(c, &st2));
+            const ParticleView v{c->x, c->y, c->z, c->q, c->m, st2, c->n, c->n};
+            SV_TRY(sort_view(c, v, first, last));
+        } else if (c->P.method == SV_METHOD_FMM && c->P.symmetry != SV_SYM_NONE) {
             SV_TRY(fmm_sort_images(c, first, last));
-        else
+        } else {
             SV_TRY(sort_state(c, first, last));
+        }
         phase_mark(c, 1);
         switch (c->P.method) {
         case SV_METHOD_DIRECT: SV_TRY(direct_accel(c)); break;
@@ -545,6 +565,7 @@ sv_status sv::compute_accel_device(sv_ctx *c, int64_t first, int64_t last) {
         SV_TRY(unsort_accel(c));
         zero_nontargets<<<grid_of(n), 256, 0, c->stream>>>(c->ax, c->ay, c->az, c->status, first, last, n);
         SV_LAUNCHED(c);
+        if (outliers) SV_TRY(outliers_add(c, first, last));
         phase_mark(c, 8);
     }
     SV_CK(c, cudaEventRecord(c->ev_end, c->stream));

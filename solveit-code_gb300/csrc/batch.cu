@@ -702,6 +702,8 @@ sv_status batch_plan(sv_ctx *c, int32_t np, const int64_t *counts, const int32_t
                                             (long long)B.off[np], (long long)c->n);
     if (c->P.fmm_order != 4 && c->P.fmm_order != 6 && c->P.fmm_order != 8 && c->P.fmm_order != 10)
         return set_error(c, SV_ERR_UNSUPPORTED, "FMM order %d not instantiated (4, 6, 8, 10)", c->P.fmm_order);
+    if (c->P.fmm_type != SV_FMM_FMM)
+        return set_error(c, SV_ERR_UNSUPPORTED, "batches run the plain FMM (no treecode or outlier variant)");
     // plume ids: FMM plumes first, in plume order, then the direct plumes
     B.pid_of.assign(np, -1);
     for (int p = 0; p < np; p++)

@@ -602,6 +602,138 @@ l2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, 
     }
 }
 
+
+// ----------------------------------------------------------- treecode M2P --
+// The treecode mode (FmmType::treecode, m2p_kernel fmm_cpukernel.cpp:1399-1533)
+// evaluates every far-field multipole directly at the target particles
+// instead of translating it into local expansions.  A leaf box's particles
+// receive the multipoles of the interaction lists of all its ancestors
+// (levels L..2).  With M in the regular-harmonic normalisation of P2M
+// (M = sum q conj(R_n^m(d)), R_n^m = r^n P_n^m e^{im phi} / (n+m)!), the
+// potential is phi(x) = sum_{n,m} M_n^m S_n^m(x - c) with the irregular
+// harmonics S_n^m = (n-m)! r^{-n-1} P_n^m e^{im phi}, and
+//   d/dz S_n^m = -S_{n+1}^m,   (d/dx + i d/dy) S_n^m = -S_{n+1}^{m+1}.
+// The softened distance r^2 + eps^2/h^2 enters the recurrences, as the
+// reference softens r in its M2P and M2L.
+
+// Irregular solid harmonics S_n^m, m >= 0, degrees 0..Q-1:
+// S_0^0 = 1/r; S_m^m = (2m-1)(x+iy)/r^2 S_{m-1}^{m-1}; S_{m+1}^m = (2m+1) z/r^2 S_m^m;
+// S_n^m = ((2n-1) z S_{n-1}^m - ((n-1)^2 - m^2) S_{n-2}^m) / r^2.
+template <int Q>
+__device__ __forceinline__ void irregular_harmonics(float x, float y, float z, float r2, float2 *S) {
+    const float ir2 = 1.f / r2;
+    S[0] = make_float2(rsqrtf(r2), 0.f);
+#pragma unroll
+    for (int m = 0; m < Q; m++) {
+        if (m > 0) {
+            const float2 prev = S[cidx(m - 1, m - 1)];
+            const float s = (2.f * m - 1.f) * ir2;
+            S[cidx(m, m)] = make_float2((x * prev.x - y * prev.y) * s, (x * prev.y + y * prev.x) * s);
+        }
+        if (m + 1 < Q) S[cidx(m + 1, m)] = cscale(S[cidx(m, m)], (2.f * m + 1.f) * z * ir2);
+#pragma unroll
+        for (int n = m + 2; n < Q; n++) {
+            const float a = (2.f * n - 1.f) * z, d = (float)((n - 1) * (n - 1) - m * m);
+            const float2 s1 = S[cidx(n - 1, m)], s0 = S[cidx(n - 2, m)];
+            S[cidx(n, m)] = make_float2((a * s1.x - d * s0.x) * ir2, (a * s1.y - d * s0.y) * ir2);
+        }
+    }
+}
+
+struct TreecodeArgs {
+    int L, cap, ws, nleaf;
+    const int *parent[kMortonBits + 1];
+    const int4 *coord[kMortonBits + 1];
+    const int2 *m2l[kMortonBits + 1];
+    const int *m2l_cnt[kMortonBits + 1];
+    const float2 *M[kMortonBits + 1];
+    const int *leaf_start;
+    const int *has_tgt;
+    const double *x, *y, *z, *qm;
+    const double *root;
+    const float *nrm;
+    double eps2;
+    double *ax, *ay, *az;
+};
+
+template <int P>
+__global__ void __launch_bounds__(kWarps * 32) m2p_kernel(TreecodeArgs a) {
+    constexpr int NC = ncoef(P), NS = ncoef(P + 1);
+    __shared__ float2 Mw[kWarps][NC];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int b = blockIdx.x * kWarps + wid;
+    if (b >= a.nleaf) return;
+    const int s0 = a.leaf_start[b], s1 = a.leaf_start[b + 1];
+    if (!a.has_tgt[b]) {
+        for (int i = s0 + lane; i < s1; i += 32) a.ax[i] = a.ay[i] = a.az[i] = 0.0;
+        return;
+    }
+    const int R = 2 * a.ws + 1, SIDE = 2 * R + 1;
+    for (int tb = s0; tb < s1; tb += 32) {
+        const int i = tb + lane;
+        const bool valid = i < s1;
+        const int ii = valid ? i : s0;
+        double gx = 0.0, gy = 0.0, gz = 0.0;
+        int box = b;
+        for (int l = a.L; l >= 2; l--) {
+            const double h = a.root[3] / (double)(1 << l);
+            const int4 cb = a.coord[l][box];
+            const double ih = 1.0 / h;
+            const float dx0 = (float)((a.x[ii] - (a.root[0] + (cb.x + 0.5) * h)) * ih);
+            const float dy0 = (float)((a.y[ii] - (a.root[1] + (cb.y + 0.5) * h)) * ih);
+            const float dz0 = (float)((a.z[ii] - (a.root[2] + (cb.z + 0.5) * h)) * ih);
+            const float e2 = (float)(a.eps2 * ih * ih);
+            const int cnt = a.m2l_cnt[l][box];
+            const int2 *lst = a.m2l[l] + (size_t)box * a.cap;
+            float fx = 0.f, fy = 0.f, fz = 0.f;
+            for (int e = 0; e < cnt; e++) {
+                const int2 ent = lst[e];
+                __syncwarp();
+                for (int c = lane; c < NC; c += 32) {
+                    int n, m;
+                    cnm(c, n, m);
+                    Mw[wid][c] = cscale(a.M[l][(size_t)ent.x * NC + c], 1.f / a.nrm[n * P + m]);
+                }
+                __syncwarp();
+                // target ancestor minus source box, in boxes (exact)
+                const int oz = ent.y % SIDE - R, oy = (ent.y / SIDE) % SIDE - R, ox = ent.y / (SIDE * SIDE) - R;
+                const float dx = dx0 + (float)ox, dy = dy0 + (float)oy, dz = dz0 + (float)oz;
+                float2 S[NS];
+                irregular_harmonics<P + 1>(dx, dy, dz, fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, e2))), S);
+                float2 gp = make_float2(0.f, 0.f);
+                float gzz = 0.f;
+#pragma unroll
+                for (int n = 0; n < P; n++) {
+                    const float2 *Mn = &Mw[wid][cidx(n, 0)];
+                    const float2 *Sn = &S[cidx(n + 1, 0)];
+                    gzz += cmul(Mn[0], Sn[0]).x;
+#pragma unroll
+                    for (int m = 1; m <= n; m++) gzz += 2.f * cmul(Mn[m], Sn[m]).x;
+#pragma unroll
+                    for (int m = 0; m <= n; m++) gp = cadd(gp, cmul(Mn[m], Sn[m + 1]));
+#pragma unroll
+                    for (int k = 1; k <= n; k++) gp = cadd(gp, cscale(cconj(cmul(Mn[k], Sn[k - 1])), -1.f));
+                }
+                fx -= gp.x;
+                fy -= gp.y;
+                fz -= gzz;
+            }
+            const double s = ih * ih;
+            gx += (double)fx * s;
+            gy += (double)fy * s;
+            gz += (double)fz * s;
+            box = a.parent[l][box];
+        }
+        if (valid) {
+            // a = -K q/m grad(phi)
+            const double c = a.qm[i];
+            a.ax[i] = -c * gx;
+            a.ay[i] = -c * gy;
+            a.az[i] = -c * gz;
+        }
+    }
+}
+
 // ------------------------------------------------------------------ P2P --
 // Each particle once as an FP32 offset from the centre of its own leaf box
 // (one FP64 subtraction per particle) with its charge: the P2P kernel then
@@ -884,8 +1016,9 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         SV_LAUNCHED(c);
     }
     phase_mark(c, 4);
-    // downward pass: L2L + M2L per level
-    for (int l = 2; l <= L; l++) {
+    const bool treecode = c->P.fmm_type == SV_FMM_TREECODE || c->P.fmm_type == SV_FMM_TREECODE_OUTLIERS;
+    // downward pass: L2L + M2L per level (the treecode evaluates multipoles at the particles instead)
+    for (int l = 2; l <= L && !treecode; l++) {
         const Level &V = T.lv[l];
         DownArgs a;
         a.nbox = V.nbox;
@@ -921,7 +1054,34 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
     // far field then near field, written in sorted order
     {
         const Level &V = T.lv[L];
-        if (L >= 2) {
+        if (L >= 2 && treecode) {
+            TreecodeArgs ta{};
+            ta.L = L;
+            ta.cap = cap;
+            ta.ws = ws;
+            ta.nleaf = V.nbox;
+            for (int l = 0; l <= L; l++) {
+                ta.parent[l] = T.lv[l].parent;
+                ta.coord[l] = T.lv[l].coord;
+                ta.m2l[l] = lst[l];
+                ta.m2l_cnt[l] = cnt[l];
+                ta.M[l] = Mv[l];
+            }
+            ta.leaf_start = V.start;
+            ta.has_tgt = tgt[L];
+            ta.x = S.x;
+            ta.y = S.y;
+            ta.z = S.z;
+            ta.qm = S.qm;
+            ta.root = S.root;
+            ta.nrm = F.nrm;
+            ta.eps2 = c->P.softening2;
+            ta.ax = S.ax;
+            ta.ay = S.ay;
+            ta.az = S.az;
+            m2p_kernel<P><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(ta);
+            SV_LAUNCHED(c);
+        } else if (L >= 2) {
             l2p_kernel<P><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
                 V.nbox, nullptr, nullptr, V.start, V.coord, S.x, S.y, S.z, S.qm, S.root, L, F.nrm, Lv[L], S.ax, S.ay,
                 S.az, tgt[L]);

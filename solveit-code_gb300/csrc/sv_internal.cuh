@@ -55,6 +55,7 @@ struct Tree;  // tree.cu
 struct Bh;    // bh.cu
 struct Adj;   // adjoint.cu
 struct Batch; // batch.cu
+struct Outliers; // outliers.cu
 
 }  // namespace sv
 
@@ -77,6 +78,7 @@ struct sv_ctx {
     sv::Bh *bh = nullptr;
     sv::Adj *adj = nullptr;
     sv::Batch *batch = nullptr;   // set by sv_upload_batch
+    sv::Outliers *outliers = nullptr;  // outlier variants of the FMM
     // device staging for interleaved <-> SoA transfers
     void *d_stage = nullptr;
     size_t d_stage_bytes = 0;
@@ -162,6 +164,13 @@ sv_status compute_accel_device(sv_ctx *c, int64_t first, int64_t last);
 
 // adjoint.cu
 void adjoint_free(sv_ctx *c);
+
+// outliers.cu: detection (status with outliers masked for the tree), the
+// direct sums of every interaction with an outlier, the flags of the last run
+sv_status outliers_detect(sv_ctx *c, const int32_t **status_for_tree);
+sv_status outliers_add(sv_ctx *c, int64_t first, int64_t last);
+sv_status outliers_get(sv_ctx *c, int32_t *flags, int64_t *count);
+void outliers_free(sv_ctx *c);
 
 // batch.cu: many plumes in one context (sv_upload_batch)
 sv_status batch_plan(sv_ctx *c, int32_t np, const int64_t *counts, const int32_t *method, const int32_t *sym);

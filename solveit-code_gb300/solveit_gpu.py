@@ -19,6 +19,7 @@ LIB_PATH = os.path.join(PKG, "_build", "libsolveit_gpu.so")
 DIRECT, BARNES_HUT, FMM = 0, 1, 2
 SYM_NONE, SYM_ROTATIONAL, SYM_TRANSLATIONAL = 0, 1, 2
 MIXED, FP64 = 0, 1
+FMM_FMM, FMM_OUTLIERS, TREECODE, TREECODE_OUTLIERS = 0, 1, 2, 3
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "allocation failed", 4: "bad state",
           5: "capacity exceeded", 6: "device wait timed out", 7: "unsupported"}
@@ -30,6 +31,7 @@ ABI_SYMBOLS = (
     "sv_leapfrog", "sv_energy", "sv_compare_accel", "sv_get_stats", "sv_sync", "sv_stream",
     "sv_launch_count", "sv_last_error", "sv_abi_version", "sv_adjoint_forward", "sv_adjoint_backward",
     "sv_direct_accel_noalloc", "sv_upload_batch", "sv_batch_tune", "sv_batch_get_info", "sv_batch_set_tuning",
+    "sv_get_outliers",
 )
 
 
@@ -40,7 +42,7 @@ class Params(C.Structure):
         ("symmetry", C.c_int32), ("theta", C.c_float), ("leaf_size", C.c_int32),
         ("fmm_order", C.c_int32), ("fmm_ws", C.c_int32), ("fmm_leaf_target", C.c_int32),
         ("sym_axes", C.c_int32 * 3), ("sym_levels", C.c_int32), ("domain_size", C.c_double * 3),
-        ("device", C.c_int32), ("profile_phases", C.c_int32), ("reserved", C.c_int32 * 6),
+        ("device", C.c_int32), ("profile_phases", C.c_int32), ("fmm_type", C.c_int32), ("reserved", C.c_int32 * 5),
     ]
 
 
@@ -115,6 +117,7 @@ def load(path: str = LIB_PATH):
     L.sv_batch_tune.argtypes = [vp, C.c_char_p, C.POINTER(C.c_double)]
     L.sv_batch_get_info.argtypes = [vp, C.POINTER(BatchInfo)]
     L.sv_batch_set_tuning.argtypes = [vp, C.c_int32, C.c_int32]
+    L.sv_get_outliers.argtypes = [vp, vp, C.POINTER(C.c_int64)]
     for name in ABI_SYMBOLS:
         if name not in ("sv_destroy", "sv_stream", "sv_launch_count", "sv_last_error", "sv_abi_version"):
             getattr(L, name).restype = C.c_int
@@ -267,6 +270,13 @@ class ForceMethod:
         oe = np.zeros(3, np.float64)
         self._check(self.L.sv_adjoint_backward(self.h, _p(gx), _p(gv), _p(ox), _p(ov), _p(oe)))
         return ox, ov, oe
+
+    def outliers(self):
+        """(flags, count) of the last outlier-variant FMM evaluation."""
+        f = np.zeros(self.n, np.int32)
+        cnt = C.c_int64()
+        self._check(self.L.sv_get_outliers(self.h, _p(f), C.byref(cnt)))
+        return f, cnt.value
 
     def energy(self):
         ke = C.c_double()

@@ -52,6 +52,9 @@ def run_ref(variant, mode, pos4, vel4, acc4, tinj, **kw):
         if mode == "grid":
             raw = np.fromfile(fout, np.int32)
             return raw[1:].reshape(raw[0], 3)
+        if mode == "outliers":
+            raw = np.fromfile(fout, np.int32)
+            return raw[1:].copy(), int(raw[0])
         out = np.fromfile(fout, np.float32).reshape(3, n, 4)
     return out[0].copy(), out[1].copy(), out[2].copy()
 
@@ -90,8 +93,27 @@ def main():
     _, _, af = run_ref("stock", "fmm", pos4, vel4, acc4, tinj, threads=4, p=8)
     np.savez_compressed(os.path.join(HERE, "fmm_n4096.npz"), pos4=pos4, vel4=vel4, acc4=acc4,
                         tinj=tinj, acc_fmm=af, p=np.int32(8), eps=np.float64(6.4e-19))
+    outliers()
     print("fixtures written to", HERE)
 
 
+def outliers():
+    """isOutlier on plumes with ions far off the plume (odd and even counts)."""
+    cases = {}
+    for n, seed in ((2001, 9005), (2000, 9006)):
+        st = plume.make_plume(n, 1e-6, seed)
+        rng = np.random.default_rng(seed)
+        st["x"][:6] += rng.normal(size=(6, 3)) * 5e-6
+        pos4, vel4, acc4, tinj = plume.to_ref32(st)
+        flags, count = run_ref("stock", "outliers", pos4, vel4, acc4, tinj)
+        cases[f"n{n}"] = (pos4, vel4, acc4, tinj, flags, count)
+    np.savez_compressed(os.path.join(HERE, "outliers.npz"),
+                        **{f"{k}_{name}": v for k, c in cases.items()
+                           for name, v in zip(("pos4", "vel4", "acc4", "tinj", "flags", "count"), c)})
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["outliers"]:
+        outliers()
+    else:
+        main()
