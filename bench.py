@@ -201,7 +201,7 @@ def run_batch(args, wl, rank, world, local):
     fm = sv.ForceMethod(softening2=EPS2, efield=(0.0, 0.0, EZ), device=local, fmm_order=wl["order"],
                         fmm_ws=wl["ws"])
     fm.upload_batch(states, methods, syms)
-    tuned_ms = fm.tune(None)
+    tuned_ms = None if args.no_tune else fm.tune(None)
     stream = torch.cuda.ExternalStream(fm.stream, device=local)
     t = 0.0
     fm.leapfrog(args.warmup, DT, t)
@@ -225,6 +225,13 @@ def run_batch(args, wl, rank, world, local):
     ms_per_step = step_ms / args.steps
     value = world * n * args.steps / (step_ms / 1e3)
     info = fm.batch_info()
+    if args.timed_only:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "ms_per_step": ms_per_step, "timed_only": True,
+                              "m2l_weight": info.m2l_weight, "leaf_level": info.leaf_level,
+                              "regrows": info.regrows}), flush=True)
+        fm.close()
+        return
 
     # ---- end to end: upload of the batch state from pinned host memory (same
     # shape: the plan and graphs are kept), one step, download
@@ -275,7 +282,7 @@ def run_batch(args, wl, rank, world, local):
             "data": "synthetic (seeded plume generator)",
             "config": {"workload": args.workload, "desc": wl["desc"], "particles_per_gpu": n,
                        "plumes": len(states), "fmm_plumes": info.fmm_plumes, "slots_with_images": info.slots,
-                       "leaf_level": info.leaf_level, "tuned_leaf_target": info.leaf_target,
+                       "leaf_level": info.leaf_level, "tuned_m2l_weight": info.m2l_weight,
                        "tuned_direct_chunk": info.direct_chunk, "kernels_per_step_graph": info.graph_kernels_step,
                        "capacity_regrows": info.regrows,
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
@@ -589,6 +596,8 @@ def main():
     ap.add_argument("--workload", default="fmm_n1m", choices=sorted(WORKLOADS))
     ap.add_argument("--timed-only", action="store_true",
                     help="only the device-resident timed steps (for profiler launch lists)")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="batch workload: skip the autotuner (default depth-model weight)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world, local = dist_env()

@@ -216,21 +216,23 @@ SV_API int32_t sv_abi_version(void);
 SV_API sv_status sv_upload_batch(sv_ctx *ctx, int32_t nplumes, const int64_t *counts, const int32_t *method,
                                  const int32_t *symmetry, const double *x3, const double *v3, const double *q,
                                  const double *m_amu, const int32_t *status, const double *t_inj);
-/* Autotuner of a batch (no reference counterpart): times the FMM plumes' leaf
- * occupancy and the direct plumes' work-item size on the uploaded state and
- * keeps the fastest.  Results are cached per batch shape (plume count, size
+/* Autotuner of a batch (no reference counterpart): times the weight of the
+ * FMM plumes' depth model (the cost of one M2L translation in pair
+ * interactions; each plume's depth is chosen on the device at every
+ * evaluation to minimise P2P pairs + weight * M2L translations) and the direct
+ * plumes' work-item size on the uploaded state and keeps the fastest.  Results are cached per batch shape (plume count, size
  * buckets, methods, symmetries, order) in the process and, when cache_path is
  * not null, in that text file (read first, appended to).  best_ms (nullable)
  * receives the tuned force-evaluation time. */
 SV_API sv_status sv_batch_tune(sv_ctx *ctx, const char *cache_path, double *best_ms);
-/* Sets the two tuned quantities directly (mean FMM leaf occupancy >= 1,
- * direct sources per work item >= 256) and re-plans the batch. */
-SV_API sv_status sv_batch_set_tuning(sv_ctx *ctx, int32_t leaf_target, int32_t direct_chunk);
+/* Sets the two tuned quantities directly (M2L weight >= 1, direct sources
+ * per work item >= 256) and re-plans the batch. */
+SV_API sv_status sv_batch_set_tuning(sv_ctx *ctx, int32_t m2l_weight, int32_t direct_chunk);
 typedef struct {
     int32_t nplumes, fmm_plumes;
     int64_t slots, fmm_slots;       /* particles plus FMM rotational image copies */
     int32_t leaf_level;             /* leaf level of the FMM forest */
-    int32_t leaf_target;            /* tuned mean leaf occupancy */
+    int32_t m2l_weight;             /* tuned M2L cost in pair units of the depth model */
     int32_t direct_chunk;           /* tuned sources per direct work item */
     int32_t direct_items;
     int32_t graph_kernels_step;     /* kernel nodes of one captured leapfrog step */
@@ -244,7 +246,8 @@ typedef struct {
     int32_t level_boxes[22];        /* forest boxes per level at the last evaluation */
     int32_t level_cap[22];          /* box capacity per level */
     int32_t level_max[22];          /* largest box count per level since the last plan */
-    int32_t reserved[6];
+    int32_t max_leaf;               /* most slots in one leaf box at the last evaluation */
+    int32_t reserved[5];
 } sv_batch_info;
 SV_API sv_status sv_batch_get_info(const sv_ctx *ctx, sv_batch_info *out);
 

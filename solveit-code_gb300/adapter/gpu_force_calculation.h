@@ -44,6 +44,9 @@ public:
     void setLeafSize(int n) { params_.leaf_size = n; }
     void setSoftening(double eps2) { params_.softening2 = eps2; }
     void setDevice(int device) { params_.device = device; }
+    // the FmmType the reference passes to MultipoleMethodForceCalculation's
+    // constructor (multipole_method_force_calculation.cpp:9-104)
+    void setFmmType(sv_fmm_type t) { params_.fmm_type = t; }
 
     void updateAcceleration() override {
         if (particleSystem == nullptr) {

@@ -13,11 +13,12 @@
 //    Morton code relative to the plume's own root cube, so each plume's slots
 //    stay contiguous and spatially ordered.
 //  * FMM plumes: one forest of octrees (forest.cuh).  Each plume's cube is
-//    enlarged by 2^delta so that a single leaf level L gives every plume the
-//    leaf occupancy the autotuner chose.  delta is chosen on the device at
-//    every evaluation from the plume's split-level histogram (dense plumes
-//    expand by tens of percent within a few steps), and applied by shifting
-//    the plume's sorted Morton keys right by 3*delta, which keeps their order.
+//    enlarged by 2^delta so that a single leaf level L is, for every plume,
+//    the level its cost model picks.  delta is chosen on the device at every
+//    evaluation from the plume's split-level histogram (dense plumes expand
+//    radially by tens of percent within a few steps, which changes the best
+//    depth), and applied by shifting the plume's sorted Morton keys right by
+//    3*delta, which keeps their order.
 //  * direct plumes: a persistent kernel pulls work items (256 targets x a
 //    source chunk x images) from an atomic queue, largest first, on a second
 //    stream that runs beside the FMM.
@@ -90,7 +91,7 @@ struct Batch {
     double *backup = nullptr;         // 6 n: state at the start of a leapfrog call
     double step_dt = 0;               // dt baked into g_step
     // tuning
-    int leaf_target = 48, direct_chunk = 2048;
+    int m2l_weight = 400, direct_chunk = 2048;  // tuned: M2L cost in pair units, direct work-item size
     double tuned_ms = 0;
     int regrows = 0;
 };
@@ -305,20 +306,47 @@ __global__ void __launch_bounds__(256) plume_levels_kernel(const uint64_t *__res
         if (sh[t]) atomicAdd(&hist[(pid0 + t / kBLevels) * kBLevels + t % kBLevels], sh[t]);
 }
 
-// Per FMM plume: its own leaf level Lp (deepest level whose mean occupancy is
-// still >= target, at least 2), delta = L - Lp, and the root side scaled by
-// 2^delta.
+// The leaf level of one plume from a cost model on its box counts per level:
+//   cost(l) = P2P pairs(l) + W * (M2L translations of levels 2..l)
+// with the occupied boxes' growth ratio g_k = boxes(k) / boxes(k-1) giving the
+// dimension d_k = log2(g_k) in which the plume is resolved at level k (1 for a
+// thin filament, 3 for a bulk), near boxes (2ws+1)^d and M2L boxes
+// (4ws+2)^d - (2ws+1)^d per box, pairs = n * occupancy * near.  W is the cost
+// of one M2L in pair units (tuned).  Levels below an occupancy of 2 are not
+// considered.
+__host__ __device__ inline int pick_level(double np_slots, const long long *boxes, double w, int ws) {
+    const double a = 2.0 * ws + 1.0, b = 4.0 * ws + 2.0;
+    int best = 2;
+    double bestc = 1e300, m2l = 0.0;
+    for (int l = 2; l <= kBatchBits; l++) {
+        const double nb = (double)boxes[l];
+        double g = nb / (double)boxes[l - 1];
+        g = g < 1.0 ? 1.0 : (g > 8.0 ? 8.0 : g);
+        const double d = log2(g);
+        const double near = pow(a, d), far = pow(b, d) - near;
+        m2l += nb * far;
+        const double occ = np_slots / nb;
+        if (occ < 2.0 && l > 2) break;
+        const double cost = np_slots * occ * near + w * m2l;
+        if (cost < bestc) {
+            bestc = cost;
+            best = l;
+        }
+    }
+    return best;
+}
+
+// Per FMM plume: its own leaf level Lp, delta = L - Lp, and the root side
+// scaled by 2^delta.
 __global__ void choose_delta_kernel(int nfp, const int *__restrict__ hist, const int *__restrict__ vbeg, int L,
-                                    int target, int *__restrict__ delta, double *__restrict__ roots) {
+                                    double w, int ws, int *__restrict__ delta, double *__restrict__ roots) {
     const int pid = blockIdx.x * blockDim.x + threadIdx.x;
     if (pid >= nfp) return;
     const double np_slots = (double)(vbeg[pid + 1] - vbeg[pid]);
-    long long boxes = 1;
-    int lp = 2;
-    for (int l = 1; l <= kBatchBits; l++) {
-        boxes += hist[pid * kBLevels + l];
-        if (l >= 2 && np_slots >= (double)target * (double)boxes) lp = l;
-    }
+    long long boxes[kBatchBits + 1];
+    boxes[0] = 1;
+    for (int l = 1; l <= kBatchBits; l++) boxes[l] = boxes[l - 1] + hist[pid * kBLevels + l];
+    const int lp = pick_level(np_slots, boxes, w, ws);
     const int d = L > lp ? L - lp : 0;
     delta[pid] = d;
     roots[8 * pid + 3] = ldexp(roots[8 * pid + 3], d);
@@ -485,7 +513,8 @@ sv_status sort_batch(sv_ctx *c, Batch &B, bool adapt) {
         plume_levels_kernel<<<div_up(B.nf, 256), 256, 0, c->stream>>>(S.keys, B.nf, B.d_hist);
         SV_LAUNCHED(c);
         choose_delta_kernel<<<div_up(B.nfp, 128), 128, 0, c->stream>>>(B.nfp, B.d_hist, B.d_vbeg, B.fa.spec.L,
-                                                                       B.leaf_target, B.delta, B.roots);
+                                                                       (double)B.m2l_weight, c->P.fmm_ws, B.delta,
+                                                                       B.roots);
         SV_LAUNCHED(c);
         shift_keys_kernel<<<div_up(B.nf, 256), 256, 0, c->stream>>>(S.keys, B.nf, B.delta);
         SV_LAUNCHED(c);
@@ -541,19 +570,16 @@ sv_status plan_forest(sv_ctx *c, Batch &B, int cap_scale) {
     SV_CK(c, cudaMemcpyAsync(hist.data(), B.d_hist, sizeof(int) * hist.size(), cudaMemcpyDeviceToHost, c->stream));
     SV_CK(c, cudaStreamSynchronize(c->stream));
     // boxes of plume pid at its own level l: 1 + splits at levels 1..l
-    std::vector<std::vector<int64_t>> boxes(B.nfp, std::vector<int64_t>(kBatchBits + 1, 1));
+    std::vector<std::vector<long long>> boxes(B.nfp, std::vector<long long>(kBatchBits + 1, 1));
     std::vector<int> Lp(B.nfp, 2);
     for (int pid = 0; pid < B.nfp; pid++) {
-        int64_t acc = 1;
+        long long acc = 1;
         for (int l = 0; l <= kBatchBits; l++) {
             if (l > 0) acc += hist[(size_t)pid * kBLevels + l];
             boxes[pid][l] = acc;
         }
-        const double np_slots = (double)(B.vbeg[pid + 1] - B.vbeg[pid]);
-        int best = 2;
-        for (int l = 2; l <= kBatchBits; l++)
-            if (np_slots / (double)boxes[pid][l] >= (double)B.leaf_target) best = l;
-        Lp[pid] = best;
+        Lp[pid] = pick_level((double)(B.vbeg[pid + 1] - B.vbeg[pid]), boxes[pid].data(), (double)B.m2l_weight,
+                             c->P.fmm_ws);
     }
     // one level of headroom: a plume that contracts can still deepen
     int L = 2;
@@ -571,7 +597,7 @@ sv_status plan_forest(sv_ctx *c, Batch &B, int cap_scale) {
             const int lo = l - B.h_delta[pid];
             tot += lo < 0 ? 1 : boxes[pid][lo];
         }
-        int64_t cap = (tot + tot / 2 + 1024) * cap_scale;
+        int64_t cap = (2 * tot + 4096) * cap_scale;
         cap = std::min<int64_t>(cap, B.nf + 1);
         f.cap[l] = (int)cap;
         caps[kBLevels + l] = (int)cap;
@@ -920,7 +946,7 @@ sv_status batch_tune(sv_ctx *c, const char *cache_path, double *best_ms) {
     const std::string key = shape_key(c, B);
     auto it = g_tune_cache.find(key);
     if (it != g_tune_cache.end()) {
-        B.leaf_target = it->second.first;
+        B.m2l_weight = it->second.first;
         B.direct_chunk = it->second.second;
         SV_TRY(build_items(c, B));
         SV_TRY(plan_forest(c, B, 1));
@@ -931,11 +957,11 @@ sv_status batch_tune(sv_ctx *c, const char *cache_path, double *best_ms) {
         return SV_OK;
     }
     // leaf occupancy first (FMM plumes), then the direct work-item size
-    int best_lt = B.leaf_target, best_dc = B.direct_chunk;
+    int best_lt = B.m2l_weight, best_dc = B.direct_chunk;
     double best = 1e30;
     if (B.nfp > 0) {
-        for (int lt : {16, 24, 32, 48, 64, 96}) {
-            B.leaf_target = lt;
+        for (int lt : {100, 200, 400, 800, 1600, 3200}) {
+            B.m2l_weight = lt;
             SV_TRY(plan_forest(c, B, 1));
             double ms = 0;
             SV_TRY(time_accel(c, B, 5, &ms));
@@ -945,7 +971,7 @@ sv_status batch_tune(sv_ctx *c, const char *cache_path, double *best_ms) {
             }
         }
     }
-    B.leaf_target = best_lt;
+    B.m2l_weight = best_lt;
     SV_TRY(plan_forest(c, B, 1));
     if (B.nfp < B.np) {
         best = 1e30;
@@ -973,11 +999,11 @@ sv_status batch_tune(sv_ctx *c, const char *cache_path, double *best_ms) {
     return SV_OK;
 }
 
-sv_status batch_set_tuning(sv_ctx *c, int leaf_target, int direct_chunk) {
+sv_status batch_set_tuning(sv_ctx *c, int m2l_weight, int direct_chunk) {
     Batch &B = *c->batch;
-    if (leaf_target < 1 || direct_chunk < kDTile)
-        return set_error(c, SV_ERR_INVALID, "leaf target >= 1 and direct chunk >= %d required", kDTile);
-    B.leaf_target = leaf_target;
+    if (m2l_weight < 1 || direct_chunk < kDTile)
+        return set_error(c, SV_ERR_INVALID, "M2L weight >= 1 and direct chunk >= %d required", kDTile);
+    B.m2l_weight = m2l_weight;
     B.direct_chunk = direct_chunk;
     SV_TRY(build_items(c, B));
     drop_graphs(B);
@@ -999,7 +1025,7 @@ sv_status batch_info(const sv_ctx *c, sv_batch_info *out) {
     out->slots = B.nv;
     out->fmm_slots = B.nf;
     out->leaf_level = B.fa.spec.L;
-    out->leaf_target = B.leaf_target;
+    out->m2l_weight = B.m2l_weight;
     out->direct_chunk = B.direct_chunk;
     out->direct_items = B.nitems;
     out->graph_kernels_step = (int32_t)B.step_kernels;
@@ -1007,6 +1033,11 @@ sv_status batch_info(const sv_ctx *c, sv_batch_info *out) {
     out->tuned_ms = B.tuned_ms;
     out->direct_pairs = B.direct_pairs;
     out->regrows = B.regrows;
+    if (B.planned && B.nfp > 0) {
+        int ml = 0;
+        SV_TRY(fmm_forest_max_leaf(const_cast<sv_ctx *>(c), B.fa, &ml));
+        out->max_leaf = ml;
+    }
     out->overflow_mask = B.overflow_mask;
     if (B.planned && B.nfp > 0) {
         int h[3 * kBLevels];

@@ -753,6 +753,13 @@ box_relative_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict
     }
 }
 
+// s += v with Kahan compensation e (the running sum is s - e)
+__device__ __forceinline__ void kahan_add(float &s, float &e, float v) {
+    const float y = v - e, t = s + y;
+    e = (t - s) - y;
+    s = t;
+}
+
 // Near field of one leaf box per warp.  The box's non-empty near boxes are
 // first compacted into shared memory with a running count of their sources;
 // the sources are then streamed 32 at a time across box boundaries (each lane
@@ -811,7 +818,79 @@ p2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, 
     }
     __syncwarp();
     const int t0 = start[b], t1 = start[b + 1];
-    for (int tb = t0; tb < t1; tb += 32) {
+    int tb = t0;
+    // two targets per lane while more than 32 remain: each staged source
+    // (one shared-memory load) then feeds two pairs
+    for (; t1 - tb > 32; tb += 64) {
+        const int ia = tb + lane, ib = tb + 32 + lane;
+        const bool vb = ib < t1;
+        const float4 ta = rel[ia], tbv = rel[vb ? ib : ia];
+        if (lane == 0) pairs += (unsigned long long)total * (unsigned long long)min(64, t1 - tb);
+        float sax = 0.f, say = 0.f, saz = 0.f, eax = 0.f, eay = 0.f, eaz = 0.f;
+        float sbx = 0.f, sby = 0.f, sbz = 0.f, ebx = 0.f, eby = 0.f, ebz = 0.f;
+        int kb = 0, kbeg = 0;
+        for (int c0 = 0; c0 < total; c0 += 32) {
+            const int j = c0 + lane;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (j < total) {
+                int2 rg = nb_rng[wid][kb];
+                while (rg.y <= j) {
+                    kbeg = rg.y;
+                    rg = nb_rng[wid][++kb];
+                }
+                const float4 r = rel[rg.x + (j - kbeg)];
+                const float4 o = nb_off[wid][kb];
+                v = make_float4(r.x + o.x, r.y + o.y, r.z + o.z, r.w);
+            }
+            src[wid][lane] = v;
+            __syncwarp();
+            float fax = 0.f, fay = 0.f, faz = 0.f, fbx = 0.f, fby = 0.f, fbz = 0.f;
+#pragma unroll 8
+            for (int k = 0; k < 32; k++) {
+                const float4 u = src[wid][k];
+                {
+                    const float dx = ta.x - u.x, dy = ta.y - u.y, dz = ta.z - u.z;
+                    float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+                    if (CLAMP) r2 = fmaxf(r2, kMinR2);
+                    const float inv = rsqrtf(r2);
+                    const float w = u.w * inv * inv * inv;
+                    fax = fmaf(dx, w, fax);
+                    fay = fmaf(dy, w, fay);
+                    faz = fmaf(dz, w, faz);
+                }
+                {
+                    const float dx = tbv.x - u.x, dy = tbv.y - u.y, dz = tbv.z - u.z;
+                    float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+                    if (CLAMP) r2 = fmaxf(r2, kMinR2);
+                    const float inv = rsqrtf(r2);
+                    const float w = u.w * inv * inv * inv;
+                    fbx = fmaf(dx, w, fbx);
+                    fby = fmaf(dy, w, fby);
+                    fbz = fmaf(dz, w, fbz);
+                }
+            }
+            __syncwarp();
+            kahan_add(sax, eax, fax);
+            kahan_add(say, eay, fay);
+            kahan_add(saz, eaz, faz);
+            kahan_add(sbx, ebx, fbx);
+            kahan_add(sby, eby, fby);
+            kahan_add(sbz, ebz, fbz);
+        }
+        {
+            const double c = qm[ia];
+            ax[ia] += (double)(sax - eax) * c;
+            ay[ia] += (double)(say - eay) * c;
+            az[ia] += (double)(saz - eaz) * c;
+        }
+        if (vb) {
+            const double c = qm[ib];
+            ax[ib] += (double)(sbx - ebx) * c;
+            ay[ib] += (double)(sby - eby) * c;
+            az[ib] += (double)(sbz - ebz) * c;
+        }
+    }
+    for (; tb < t1; tb += 32) {
         const int nt = min(32, t1 - tb);
         int lg = 0;
         while ((nt << (lg + 1)) <= 32) lg++;
@@ -1409,6 +1488,33 @@ sv_status fmm_forest_reserve(sv_ctx *c, const ForestArgs &fa) {
         SV_CK(c, cudaMalloc(&F.frel, sizeof(float4) * (size_t)std::max(f.n, 1)));
         F.frel_cap = f.n;
     }
+    return SV_OK;
+}
+
+__global__ void max_count_kernel(const int4 *__restrict__ coord, const int *__restrict__ nbd, int cap,
+                                 int *__restrict__ out) {
+    const int nb = level_boxes(cap, nbd);
+    int m = 0;
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < nb; b += gridDim.x * blockDim.x) m = max(m, coord[b].w);
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(out, m);
+}
+
+sv_status fmm_forest_max_leaf(sv_ctx *c, const ForestArgs &fa, int *out) {
+    if (!c->fmm || !c->fmm->ftree) {
+        *out = 0;
+        return SV_OK;
+    }
+    const int L = fa.spec.L;
+    int *d = nullptr;
+    SV_CK(c, cudaMallocAsync(&d, sizeof(int), c->stream));
+    SV_CK(c, cudaMemsetAsync(d, 0, sizeof(int), c->stream));
+    max_count_kernel<<<forest_grid(fa.spec.cap[L], 256), 256, 0, c->stream>>>(c->fmm->ftree->lv[L].coord,
+                                                                             fa.d_nbox + L, fa.spec.cap[L], d);
+    SV_CK(c, cudaMemcpyAsync(c->h_scalar, d, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    SV_CK(c, cudaFreeAsync(d, c->stream));
+    SV_CK(c, cudaStreamSynchronize(c->stream));
+    memcpy(out, c->h_scalar, sizeof(int));
     return SV_OK;
 }
 

@@ -26,5 +26,7 @@ sv_status fmm_forest_reserve(sv_ctx *c, const ForestArgs &a);
 // Launches the tree build, lists, P2M/M2M, M2L/L2L, L2P and P2P; writes the
 // acceleration of slots [0, spec.n) into c->S.a{x,y,z}.
 sv_status fmm_forest_run(sv_ctx *c, const ForestArgs &a);
+// Largest leaf-box occupancy of the last run (blocking; diagnostics).
+sv_status fmm_forest_max_leaf(sv_ctx *c, const ForestArgs &a, int *out);
 
 }  // namespace sv

@@ -177,7 +177,7 @@ sv_status batch_plan(sv_ctx *c, int32_t np, const int64_t *counts, const int32_t
 sv_status batch_accel(sv_ctx *c);
 sv_status batch_leapfrog(sv_ctx *c, int32_t nsteps, double dt, double t0);
 sv_status batch_tune(sv_ctx *c, const char *cache_path, double *best_ms);
-sv_status batch_set_tuning(sv_ctx *c, int leaf_target, int direct_chunk);
+sv_status batch_set_tuning(sv_ctx *c, int m2l_weight, int direct_chunk);
 sv_status batch_info(const sv_ctx *c, sv_batch_info *out);
 void batch_invalidate(sv_ctx *c);
 bool batch_same_shape(const sv_ctx *c, int32_t np, const int64_t *counts, const int32_t *method,

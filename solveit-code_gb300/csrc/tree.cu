@@ -253,6 +253,13 @@ __global__ void link_levels(int L, int n_act, int total, LevelPtrs P) {
     if (l < L) P.child0[l][b] = upper_bound_i(P.start[l + 1], P.nbox[l + 1], s) - 1;
 }
 
+// After a capacity overflow the run is redone by the host with larger
+// capacities: empty every level so that the rest of the run (and any further
+// captured step) does no work.
+__global__ void drop_if_overflow(int L, int *__restrict__ nbox, const int *__restrict__ err) {
+    if (*err && threadIdx.x <= L) nbox[threadIdx.x] = 0;
+}
+
 // Forest variant of link_levels: box counts live on the device; blockIdx.y
 // is the level, boxes are visited grid-stride.
 __global__ void link_levels_forest(int L, int n, const int *__restrict__ nbox, LevelPtrs P) {
@@ -485,6 +492,8 @@ sv_status tree_build_forest(sv_ctx *c, Tree &T, const ForestSpec &f, int *d_nbox
     scan_counts<<<L + 1, 1024, 0, c->stream>>>(T.scratch, nblk, d_nbox, d_nbox + kLevels, d_err);
     SV_LAUNCHED(c);
     scatter_starts<<<nblk, kBuildThreads, 0, c->stream>>>(T.lvl, c->S.keys, n, L, f.mbits, T.scratch, P);
+    SV_LAUNCHED(c);
+    drop_if_overflow<<<1, 32, 0, c->stream>>>(L, d_nbox, d_err);
     SV_LAUNCHED(c);
     int maxcap = 1;
     for (int l = 0; l <= L; l++) maxcap = std::max(maxcap, f.cap[l]);

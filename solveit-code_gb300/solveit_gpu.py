@@ -57,12 +57,12 @@ class Stats(C.Structure):
 class BatchInfo(C.Structure):
     _fields_ = [
         ("nplumes", C.c_int32), ("fmm_plumes", C.c_int32), ("slots", C.c_int64), ("fmm_slots", C.c_int64),
-        ("leaf_level", C.c_int32), ("leaf_target", C.c_int32), ("direct_chunk", C.c_int32),
+        ("leaf_level", C.c_int32), ("m2l_weight", C.c_int32), ("direct_chunk", C.c_int32),
         ("direct_items", C.c_int32), ("graph_kernels_step", C.c_int32), ("graph_kernels_accel", C.c_int32),
         ("tuned_ms", C.c_double), ("direct_pairs", C.c_double), ("fmm_m2l", C.c_double),
         ("fmm_pairs", C.c_double), ("regrows", C.c_int32), ("overflow_mask", C.c_int32),
         ("level_boxes", C.c_int32 * 22), ("level_cap", C.c_int32 * 22), ("level_max", C.c_int32 * 22),
-        ("reserved", C.c_int32 * 6),
+        ("max_leaf", C.c_int32), ("reserved", C.c_int32 * 5),
     ]
 
 
@@ -230,8 +230,8 @@ class ForceMethod:
         self._check(self.L.sv_batch_tune(self.h, path, C.byref(ms)))
         return ms.value
 
-    def set_tuning(self, leaf_target, direct_chunk):
-        self._check(self.L.sv_batch_set_tuning(self.h, leaf_target, direct_chunk))
+    def set_tuning(self, m2l_weight, direct_chunk):
+        self._check(self.L.sv_batch_set_tuning(self.h, m2l_weight, direct_chunk))
 
     def batch_info(self) -> BatchInfo:
         b = BatchInfo()

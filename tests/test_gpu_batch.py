@@ -115,16 +115,16 @@ def test_batch_tune_and_cache(tmp_path):
         info = fm.batch_info()
         a = split(fm.accel(), states)
     assert ms > 0 and info.tuned_ms == pytest.approx(ms)
-    assert info.leaf_target in (16, 24, 32, 48, 64, 96)
+    assert info.m2l_weight in (100, 200, 400, 800, 1600, 3200)
     assert info.direct_chunk in (1024, 2048, 4096, 8192)
     lines = cache.read_text().split()
-    assert len(lines) == 4 and int(lines[1]) == info.leaf_target
+    assert len(lines) == 4 and int(lines[1]) == info.m2l_weight
     # a new context with the same shape reads the cached choice
     with batch_ctx() as fm2:
         fm2.upload_batch(states, methods, syms)
         fm2.tune(cache)
         i2 = fm2.batch_info()
-    assert (i2.leaf_target, i2.direct_chunk) == (info.leaf_target, info.direct_chunk)
+    assert (i2.m2l_weight, i2.direct_chunk) == (info.m2l_weight, info.direct_chunk)
     assert len(cache.read_text().split()) == 4
     for s, ap, meth, sym in zip(states, a, methods, syms):
         ref = O.direct_f64(s, EPS20, sym=sym)
