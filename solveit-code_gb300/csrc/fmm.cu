@@ -69,7 +69,8 @@ struct Fmm {
     Tree *ftree = nullptr;
     void *farena = nullptr;
     size_t farena_bytes = 0;
-    float2 *fM[kMortonBits + 1] = {}, *fL[kMortonBits + 1] = {};
+    float2 *fM[kMortonBits + 1] = {}, *fL[kMortonBits + 1] = {}, *fpart[kMortonBits + 1] = {};
+    int fchunks[kMortonBits + 1] = {};
     int *fnbr[kMortonBits + 1] = {}, *fcnt[kMortonBits + 1] = {}, *ftgt[kMortonBits + 1] = {};
     int2 *flst[kMortonBits + 1] = {};
     float4 *frel = nullptr;
@@ -375,27 +376,47 @@ m2m_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ child0
 }
 
 // ----------------------------------------------------------- downward --
-struct DownArgs {
-    int nbox, level, cap, esz, osz, dsz, has_parent;
-    const int *nbd;        // device box count (forest) or null
-    const int *bpid;       // plume of each box (forest) or null
-    const int *parent;
-    const int4 *coord;
-    const float2 *Lp;      // parent locals (level-1) or null
-    const float2 *Ml;      // multipoles of this level
+// M2L of every level in one launch, then L2L level by level.  A level with few
+// boxes (the coarse ones, whose lists are long) splits each box's list over
+// `chunks` warps; the chunks' partial sums are kept apart and added in order by
+// the L2L pass, so the result does not depend on scheduling.
+struct M2LLevel {
+    int nbox;             // launch bound: boxes, or the forest capacity
+    int chunks;           // warps per box
+    int warp0;            // first global warp of the level
+    int level;
+    const int *nbd;       // device box count (forest) or null
+    const int *bpid;      // plume of each box (forest) or null
     const int2 *m2l;
-    const int *m2l_cnt;
+    const int *cnt;
+    const int *has_tgt;   // boxes without targets need no local expansion
+    const float2 *M;      // multipoles of the level
+    float2 *out;          // [box][chunk][coefficient]; with one chunk the level's local expansions
+};
+
+struct M2LArgs {
+    int nlev, cap, esz, osz, dsz;
+    double eps2;
+    const double *root;
     const int *cls_theta;
     const float2 *cls_phase;
     const float *cls_rho2;
     const float *dmat;
     const float *zc;
+    M2LLevel lv[kMortonBits + 1];
+};
+
+struct L2LArgs {
+    int nbox, chunks, has_parent;
+    const int *nbd;
+    const int *parent;
+    const int4 *coord;
+    const int *has_tgt;
+    const float2 *Lp;     // final locals of the parent level
+    const float2 *part;   // this level's M2L partials [box][chunk]
+    float2 *L;            // this level's locals (may alias part when chunks == 1)
     const float *nrm;
     const float2 *oct;
-    const double *root;
-    double eps2;
-    float2 *Lout;
-    const int *has_tgt;  // boxes without targets need no local expansion
 };
 
 // rows of the coefficients held in slot 1 (the EXTRA lowest coefficients)
@@ -408,59 +429,104 @@ __host__ __device__ constexpr int slot1_rows() {
     return n + 1;
 }
 
-// One output (n, mp) of a folded y-rotation: real part from the E block (rows
-// of n+1), imaginary part from the O block (rows of n, mp >= 1).  Unrolled to
-// the compile-time bound MAXN with the row length n applied as a predicate.
-template <int MAXN>
+// Rotation / translation rows are RS = p rounded up to 4 floats (16-byte
+// rows, zero padded).  In shared memory the coefficients sit in rows of RS
+// complex values: A[n][m] by degree (n-major) for the rotations, B[k][n] by
+// order (k-major) for the z-translation; entries outside a row's range stay
+// zero, so whole float4 groups can be read without masks.
+template <int P>
+__host__ __device__ constexpr int rot_rs() { return (P + 3) / 4 * 4; }
+
+// One output (n, mp) of a folded y-rotation: real part = E row . Re(A_n),
+// imaginary part = O row . Im(A_n) (the O row starts with a zero for m = 0).
+// G is the number of 4-coefficient groups to visit (a compile-time bound; a
+// lane stops at the groups its degree n covers).
+template <int P, int G>
 __device__ __forceinline__ float2 rot_row(const float *__restrict__ D, int eoff, int ooff, const float2 *A, int n,
                                           int mp) {
-    const float *E = D + eoff + (n * (n + 1) * (2 * n + 1)) / 6 + mp * (n + 1);
-    const float2 *An = A + cidx(n, 0);
+    constexpr int RS = rot_rs<P>();
+    const float4 *E = reinterpret_cast<const float4 *>(D + eoff + RS * (n * (n + 1) / 2 + mp));
+    const float4 *O = reinterpret_cast<const float4 *>(D + ooff + RS * (n * (n - 1) / 2 + (mp > 0 ? mp - 1 : 0)));
+    const float4 *A4 = reinterpret_cast<const float4 *>(A + n * RS);
     float re = 0.f, im = 0.f;
 #pragma unroll
-    for (int m = 0; m < MAXN; m++)
-        if (m <= n) re = fmaf(E[m], An[m].x, re);
-    if (mp > 0) {
-        const float *O = D + ooff + ((n - 1) * n * (2 * n - 1)) / 6 + (mp - 1) * n;
-#pragma unroll
-        for (int m = 1; m < MAXN; m++)
-            if (m <= n) im = fmaf(O[m - 1], An[m].y, im);
-    }
-    return make_float2(re, im);
-}
-
-// One output (j, k) of the translation along z:
-// L'_j^k = sum_{n >= k} C[k][j][n] rho^-(j+n+1) M'_n^k
-template <int P>
-__device__ __forceinline__ float2 ztrans_row(const float *__restrict__ zc, const float2 *B, int j, int k,
-                                             float inv_rho) {
-    const float *Z = zc + ((size_t)k * P + j) * P;
-    float ip = inv_rho;
-#pragma unroll
-    for (int q = 0; q < 2 * P - 2; q++)
-        if (q < j + k) ip *= inv_rho;  // rho^-(j+k+1)
-    float re = 0.f, im = 0.f;
-#pragma unroll
-    for (int n = 0; n < P; n++) {
-        if (n >= k) {
-            const float2 v = B[cidx(n, k)];
-            const float f = Z[n] * ip;
-            re = fmaf(f, v.x, re);
-            im = fmaf(f, v.y, im);
-            ip *= inv_rho;
+    for (int q = 0; q < G; q++) {
+        if (4 * q <= n) {
+            const float4 e = E[q];
+            const float4 a0 = A4[2 * q], a1 = A4[2 * q + 1];
+            re = fmaf(e.x, a0.x, re);
+            re = fmaf(e.y, a0.z, re);
+            re = fmaf(e.z, a1.x, re);
+            re = fmaf(e.w, a1.z, re);
+            if (mp > 0) {
+                const float4 o = O[q];
+                im = fmaf(o.x, a0.y, im);
+                im = fmaf(o.y, a0.w, im);
+                im = fmaf(o.z, a1.y, im);
+                im = fmaf(o.w, a1.w, im);
+            }
         }
     }
     return make_float2(re, im);
 }
 
+// One output (j, k) of the translation along z:
+// L'_j^k = sum_{n >= k} C[k][j][n] rho^-(j+n+1) M'_n^k  (C is zero for n < k)
 template <int P>
-__global__ void __launch_bounds__(kWarps * 32) down_kernel(DownArgs a) {
-    constexpr int NC = ncoef(P), W = 2 * P - 1;
-    __shared__ float2 A[kWarps][NC], B[kWarps][NC];
-    const int nbox = a.nbox;
-    const int *nbd = a.nbd;
-    SV_WARP_BOXES(kWarps) {
-    if (!a.has_tgt[b]) continue;
+__device__ __forceinline__ float2 ztrans_row(const float *__restrict__ zc, const float2 *Bk, int j, int k,
+                                             float inv_rho) {
+    constexpr int RS = rot_rs<P>();
+    const float4 *Z = reinterpret_cast<const float4 *>(zc + ((size_t)k * P + j) * RS);
+    const float4 *B4 = reinterpret_cast<const float4 *>(Bk + k * RS);
+    float ip = inv_rho;
+#pragma unroll
+    for (int q = 0; q < 2 * P - 2; q++)
+        if (q < j) ip *= inv_rho;  // rho^-(j+1)
+    float re = 0.f, im = 0.f;
+#pragma unroll
+    for (int q = 0; q < RS / 4; q++) {
+        const float4 z = Z[q];
+        const float4 b0 = B4[2 * q], b1 = B4[2 * q + 1];
+        const float f0 = z.x * ip;
+        ip *= inv_rho;
+        const float f1 = z.y * ip;
+        ip *= inv_rho;
+        const float f2 = z.z * ip;
+        ip *= inv_rho;
+        const float f3 = z.w * ip;
+        ip *= inv_rho;
+        re = fmaf(f0, b0.x, fmaf(f1, b0.z, fmaf(f2, b1.x, fmaf(f3, b1.z, re))));
+        im = fmaf(f0, b0.y, fmaf(f1, b0.w, fmaf(f2, b1.y, fmaf(f3, b1.w, im))));
+    }
+    return make_float2(re, im);
+}
+
+template <int P>
+constexpr int m2l_warps() { return P >= 10 ? 2 : 4; }
+
+// The z-translation table (the same for every entry) is staged once per CTA
+// in shared memory; the rotation rows of each entry's polar angle are read
+// from global memory (L1/L2), one 16-byte row segment per lane and group.
+template <int P>
+__global__ void __launch_bounds__(m2l_warps<P>() * 32) m2l_kernel(M2LArgs a) {
+    constexpr int NC = ncoef(P), RS = rot_rs<P>(), WP = m2l_warps<P>();
+    __shared__ __align__(16) float2 A[WP][2][P * RS], B[WP][2][P * RS];
+    __shared__ __align__(16) float Zsh[P * P * RS];
+    for (int t = threadIdx.x; t < P * P * RS / 4; t += blockDim.x)
+        reinterpret_cast<float4 *>(Zsh)[t] = __ldg(reinterpret_cast<const float4 *>(a.zc) + t);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int t = lane; t < 2 * P * RS; t += 32) {
+        A[wid][t / (P * RS)][t % (P * RS)] = make_float2(0.f, 0.f);
+        B[wid][t / (P * RS)][t % (P * RS)] = make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    const int gw = blockIdx.x * WP + wid;
+    int li = 0;
+    while (li + 1 < a.nlev && gw >= a.lv[li + 1].warp0) li++;
+    const int chunks = a.lv[li].chunks;
+    const int local = gw - a.lv[li].warp0;
+    const int b = local / chunks, ch = local - b * chunks;
+    if (b >= level_boxes(a.lv[li].nbox, a.lv[li].nbd) || !a.lv[li].has_tgt[b]) return;
     // Lane slots.  Slot 0 of every lane holds one of the NC - EXTRA highest
     // coefficients; slot 1 of the first EXTRA lanes holds one of the EXTRA
     // lowest (cheapest) coefficients, so the second pass is short.
@@ -472,8 +538,84 @@ __global__ void __launch_bounds__(kWarps * 32) down_kernel(DownArgs a) {
     const int cs[2] = {c0, c1};
     const bool has[2] = {c0 < NC, lane < EXTRA};
     float2 acc[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-    // ---- L2L from the parent (parent box units -> child box units)
+    const double h = box_root(a.root, a.lv[li].bpid, b)[3] / (double)(1 << a.lv[li].level);
+    const float eh2 = (float)(a.eps2 / (h * h));
+    const int cnt = a.lv[li].cnt[b];
+    const int per = (cnt + chunks - 1) / chunks;
+    const int e0 = ch * per, e1 = min(cnt, e0 + per);
+    const int2 *lst = a.lv[li].m2l + (size_t)b * a.cap;
+    const float2 *Ml = a.lv[li].M;
+    // two entries in flight per iteration: their loads and the warp
+    // synchronisations overlap (the second is skipped past the range's end)
+    constexpr int G0 = RS / 4, G1 = slot1_rows<P>() / 4 + 1;
+    for (int e = e0; e < e1; e += 2) {
+        const bool v1 = e + 1 < e1;
+        const int2 en0 = lst[e], en1 = v1 ? lst[e + 1] : en0;
+        const int src[2] = {en0.x, en1.x};
+        const float2 *ph[2] = {a.cls_phase + (size_t)en0.y * P, a.cls_phase + (size_t)en1.y * P};
+        const float *D[2] = {a.dmat + (size_t)a.cls_theta[en0.y] * a.dsz, a.dmat + (size_t)a.cls_theta[en1.y] * a.dsz};
+        const float inv_rho[2] = {rsqrtf(a.cls_rho2[en0.y] + eh2), rsqrtf(a.cls_rho2[en1.y] + eh2)};
+        // phase e^{i m phi}, into the degree-major rows
+#pragma unroll
+        for (int u = 0; u < 2; u++)
+#pragma unroll
+            for (int t = 0; t < 2; t++)
+                if (has[t]) A[wid][u][cn[t] * RS + cm[t]] = cmul(Ml[(size_t)src[u] * NC + cs[t]], ph[u][cm[t]]);
+        __syncwarp();
+        // forward y-rotation (folded real matrices), into the order-major rows
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            if (has[0]) B[wid][u][cm[0] * RS + cn[0]] = rot_row<P, G0>(D[u], 0, a.esz, &A[wid][u][0], cn[0], cm[0]);
+            if (has[1]) B[wid][u][cm[1] * RS + cn[1]] = rot_row<P, G1>(D[u], 0, a.esz, &A[wid][u][0], cn[1], cm[1]);
+        }
+        __syncwarp();
+        // translation along z: L'_j^k = sum_n C[k][j][n] rho^-(j+n+1) M'_n^k
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            if (has[0]) A[wid][u][cn[0] * RS + cm[0]] = ztrans_row<P>(Zsh, &B[wid][u][0], cn[0], cm[0], inv_rho[u]);
+            if (has[1]) A[wid][u][cn[1] * RS + cm[1]] = ztrans_row<P>(Zsh, &B[wid][u][0], cn[1], cm[1], inv_rho[u]);
+        }
+        __syncwarp();
+        // backward y-rotation and phase e^{-i k phi}
+#pragma unroll
+        for (int u = 0; u < 2; u++) {
+            if (u == 1 && !v1) break;
+            if (has[0]) {
+                const float2 r =
+                    rot_row<P, G0>(D[u], a.esz + a.osz, 2 * a.esz + a.osz, &A[wid][u][0], cn[0], cm[0]);
+                acc[0] = cadd(acc[0], cmul(r, cconj(ph[u][cm[0]])));
+            }
+            if (has[1]) {
+                const float2 r =
+                    rot_row<P, G1>(D[u], a.esz + a.osz, 2 * a.esz + a.osz, &A[wid][u][0], cn[1], cm[1]);
+                acc[1] = cadd(acc[1], cmul(r, cconj(ph[u][cm[1]])));
+            }
+        }
+        __syncwarp();
+    }
+    float2 *dst = a.lv[li].out + ((size_t)b * chunks + ch) * NC;
+    if (has[0]) dst[cs[0]] = acc[0];
+    if (has[1]) dst[cs[1]] = acc[1];
+}
+
+// L = (sum of the level's M2L partials, in chunk order) + L2L(parent's L)
+template <int P>
+__global__ void __launch_bounds__(kWarps * 32) l2l_kernel(L2LArgs a) {
+    constexpr int NC = ncoef(P), W = 2 * P - 1;
+    __shared__ float2 A[kWarps][NC];
+    const int nbox = a.nbox;
+    const int *nbd = a.nbd;
+    SV_WARP_BOXES(kWarps) {
+    if (!a.has_tgt[b]) continue;
+    float2 acc[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+    for (int t = 0; t < 2; t++) {
+        const int c = lane + 32 * t;
+        if (c >= NC) break;
+        for (int ch = 0; ch < a.chunks; ch++) acc[t] = cadd(acc[t], a.part[((size_t)b * a.chunks + ch) * NC + c]);
+    }
     if (a.has_parent) {
+        // L2L from the parent (parent box units -> child box units)
         const int par = a.parent[b];
         const int4 cb = a.coord[b];
         const int oc = (cb.x & 1) | ((cb.y & 1) << 1) | ((cb.z & 1) << 2);
@@ -486,8 +628,10 @@ __global__ void __launch_bounds__(kWarps * 32) down_kernel(DownArgs a) {
         __syncwarp();
 #pragma unroll
         for (int t = 0; t < 2; t++) {
-            if (!has[t]) continue;
-            const int k = cn[t], l = cm[t];
+            const int c = lane + 32 * t;
+            if (c >= NC) break;
+            int k, l;
+            cnm(c, k, l);
             float2 s = make_float2(0.f, 0.f);
             for (int n = k; n < P; n++) {
                 const int nk = n - k;
@@ -497,52 +641,24 @@ __global__ void __launch_bounds__(kWarps * 32) down_kernel(DownArgs a) {
                     s = cadd(s, cmul(half_get(A[wid], n, m), Rd[nk * W + ml + P - 1]));
                 }
             }
-            acc[t] = cscale(s, 1.f / a.nrm[k * P + l]);
+            acc[t] = cadd(acc[t], cscale(s, 1.f / a.nrm[k * P + l]));
         }
         __syncwarp();
     }
-    // ---- M2L list
-    const double h = box_root(a.root, a.bpid, b)[3] / (double)(1 << a.level);
-    const float eh2 = (float)(a.eps2 / (h * h));
-    const int cnt = a.m2l_cnt[b];
-    const int2 *lst = a.m2l + (size_t)b * a.cap;
-    for (int e = 0; e < cnt; e++) {
-        const int2 ent = lst[e];
-        const int src = ent.x, cls = ent.y;
-        const float2 *ph = a.cls_phase + (size_t)cls * P;
-        const float *D = a.dmat + (size_t)a.cls_theta[cls] * a.dsz;
-        const float inv_rho = rsqrtf(a.cls_rho2[cls] + eh2);
-        // phase e^{i m phi}
 #pragma unroll
-        for (int t = 0; t < 2; t++) {
-            if (!has[t]) break;
-            A[wid][cs[t]] = cmul(a.Ml[(size_t)src * NC + cs[t]], ph[cm[t]]);
-        }
-        __syncwarp();
-        // forward y-rotation (folded real matrices), fully unrolled and predicated
-        if (has[0]) B[wid][cs[0]] = rot_row<P>(D, 0, a.esz, &A[wid][0], cn[0], cm[0]);
-        if (has[1]) B[wid][cs[1]] = rot_row<slot1_rows<P>()>(D, 0, a.esz, &A[wid][0], cn[1], cm[1]);
-        __syncwarp();
-        // translation along z: L'_j^k = sum_n C[k][j][n] rho^-(j+n+1) M'_n^k
-        if (has[0]) A[wid][cs[0]] = ztrans_row<P>(a.zc, &B[wid][0], cn[0], cm[0], inv_rho);
-        if (has[1]) A[wid][cs[1]] = ztrans_row<P>(a.zc, &B[wid][0], cn[1], cm[1], inv_rho);
-        __syncwarp();
-        // backward y-rotation and phase e^{-i k phi}
-        if (has[0]) {
-            const float2 r = rot_row<P>(D, a.esz + a.osz, 2 * a.esz + a.osz, &A[wid][0], cn[0], cm[0]);
-            acc[0] = cadd(acc[0], cmul(r, cconj(ph[cm[0]])));
-        }
-        if (has[1]) {
-            const float2 r =
-                rot_row<slot1_rows<P>()>(D, a.esz + a.osz, 2 * a.esz + a.osz, &A[wid][0], cn[1], cm[1]);
-            acc[1] = cadd(acc[1], cmul(r, cconj(ph[cm[1]])));
-        }
-        __syncwarp();
+    for (int t = 0; t < 2; t++) {
+        const int c = lane + 32 * t;
+        if (c < NC) a.L[(size_t)b * NC + c] = acc[t];
     }
-    if (has[0]) a.Lout[(size_t)b * NC + cs[0]] = acc[0];
-    if (has[1]) a.Lout[(size_t)b * NC + cs[1]] = acc[1];
-    __syncwarp();
     }
+}
+
+// warps per box for a level of nbox boxes: enough to give every SM a few
+// warps even at the coarse levels, at most 16
+inline int m2l_chunks(int nbox) {
+    const int want = 16 * kNumSMs;
+    int c = nbox > 0 ? (want + nbox - 1) / nbox : 1;
+    return c < 1 ? 1 : (c > 16 ? 16 : c);
 }
 
 // ------------------------------------------------------------------ L2P --
@@ -1007,13 +1123,16 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
     const int ns1 = 2 * ws + 1, ns = ns1 * ns1 * ns1;
     const int cap = ns * 8 - ns;
     Sorted &S = c->S;
-    // arena: per level M, Loc, nbr, m2l, cnt
+    // arena: per level M, Loc, nbr, m2l, cnt, and M2L partials where a box's list is split
     auto rounded = [](size_t sz) { return (sz + 255) & ~(size_t)255; };
+    int chunks[kMortonBits + 1];
     size_t bytes = 0;
     for (int l = 0; l <= L; l++) {
         const size_t nb = T.lv[l].nbox;
+        chunks[l] = m2l_chunks((int)nb);
         bytes += 2 * rounded(nb * NC * sizeof(float2)) + rounded(nb * ns * sizeof(int)) +
                  rounded(nb * cap * sizeof(int2)) + rounded(nb * sizeof(int));
+        if (chunks[l] > 1) bytes += rounded(nb * chunks[l] * NC * sizeof(float2));
     }
     if (F.arena_bytes < bytes) {
         cudaFree(F.arena);
@@ -1029,7 +1148,7 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         p += (sz + 255) & ~(size_t)255;
         return (void *)r;
     };
-    float2 *Mv[kMortonBits + 1], *Lv[kMortonBits + 1];
+    float2 *Mv[kMortonBits + 1], *Lv[kMortonBits + 1], *part[kMortonBits + 1];
     int *nbr[kMortonBits + 1], *cnt[kMortonBits + 1];
     int2 *lst[kMortonBits + 1];
     for (int l = 0; l <= L; l++) {
@@ -1039,6 +1158,7 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         nbr[l] = (int *)carve(nb * ns * sizeof(int));
         lst[l] = (int2 *)carve(nb * cap * sizeof(int2));
         cnt[l] = (int *)carve(nb * sizeof(int));
+        part[l] = chunks[l] > 1 ? (float2 *)carve(nb * chunks[l] * NC * sizeof(float2)) : Lv[l];
     }
     phase_mark(c, 2);
     SV_CK(c, cudaMemsetAsync(F.d_counts, 0, 2 * sizeof(unsigned long long), c->stream));
@@ -1096,38 +1216,57 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
     }
     phase_mark(c, 4);
     const bool treecode = c->P.fmm_type == SV_FMM_TREECODE || c->P.fmm_type == SV_FMM_TREECODE_OUTLIERS;
-    // downward pass: L2L + M2L per level (the treecode evaluates multipoles at the particles instead)
-    for (int l = 2; l <= L && !treecode; l++) {
-        const Level &V = T.lv[l];
-        DownArgs a;
-        a.nbox = V.nbox;
-        a.nbd = nullptr;
-        a.bpid = nullptr;
-        a.level = l;
+    // downward pass: M2L of all levels in one launch, then L2L level by level
+    // (the treecode evaluates multipoles at the particles instead)
+    if (!treecode && L >= 2) {
+        M2LArgs a{};
         a.cap = cap;
         a.esz = F.H.esz;
         a.osz = F.H.osz;
         a.dsz = F.H.dsz;
-        a.has_parent = l > 2;
-        a.parent = V.parent;
-        a.coord = V.coord;
-        a.Lp = l > 2 ? Lv[l - 1] : nullptr;
-        a.Ml = Mv[l];
-        a.m2l = lst[l];
-        a.m2l_cnt = cnt[l];
+        a.eps2 = c->P.softening2;
+        a.root = S.root;
         a.cls_theta = F.cls_theta;
         a.cls_phase = F.cls_phase;
         a.cls_rho2 = F.cls_rho2;
         a.dmat = F.dmat;
         a.zc = F.zc;
-        a.nrm = F.nrm;
-        a.oct = F.oct;
-        a.root = S.root;
-        a.eps2 = c->P.softening2;
-        a.Lout = Lv[l];
-        a.has_tgt = tgt[l];
-        down_kernel<P><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(a);
+        int warps = 0;
+        for (int l = 2; l <= L; l++) {
+            M2LLevel &V = a.lv[a.nlev++];
+            V.nbox = T.lv[l].nbox;
+            V.chunks = chunks[l];
+            V.warp0 = warps;
+            V.level = l;
+            V.nbd = nullptr;
+            V.bpid = nullptr;
+            V.m2l = lst[l];
+            V.cnt = cnt[l];
+            V.has_tgt = tgt[l];
+            V.M = Mv[l];
+            V.out = part[l];
+            warps += V.nbox * V.chunks;
+        }
+        m2l_kernel<P><<<div_up(warps, m2l_warps<P>()), m2l_warps<P>() * 32, 0, c->stream>>>(a);
         SV_LAUNCHED(c);
+        for (int l = 2; l <= L; l++) {
+            const Level &V = T.lv[l];
+            L2LArgs b{};
+            b.nbox = V.nbox;
+            b.chunks = chunks[l];
+            b.has_parent = l > 2;
+            b.nbd = nullptr;
+            b.parent = V.parent;
+            b.coord = V.coord;
+            b.has_tgt = tgt[l];
+            b.Lp = l > 2 ? Lv[l - 1] : nullptr;
+            b.part = part[l];
+            b.L = Lv[l];
+            b.nrm = F.nrm;
+            b.oct = F.oct;
+            l2l_kernel<P><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(b);
+            SV_LAUNCHED(c);
+        }
     }
     phase_mark(c, 5);
     // far field then near field, written in sorted order
@@ -1247,37 +1386,56 @@ sv_status run_fmm_forest(sv_ctx *c, Fmm &F, const ForestArgs &fa) {
             f.cap[l], nbd + l, V.child0, T.lv[l + 1].coord, F.fM[l + 1], F.fM[l], F.nrm, F.oct);
         SV_LAUNCHED(c);
     }
-    for (int l = 2; l <= L; l++) {
-        const Level &V = T.lv[l];
-        DownArgs a;
-        a.nbox = f.cap[l];
-        a.nbd = nbd + l;
-        a.bpid = V.pid;
-        a.level = l;
+    {
+        M2LArgs a{};
         a.cap = cap;
         a.esz = F.H.esz;
         a.osz = F.H.osz;
         a.dsz = F.H.dsz;
-        a.has_parent = l > 2;
-        a.parent = V.parent;
-        a.coord = V.coord;
-        a.Lp = l > 2 ? F.fL[l - 1] : nullptr;
-        a.Ml = F.fM[l];
-        a.m2l = F.flst[l];
-        a.m2l_cnt = F.fcnt[l];
+        a.eps2 = c->P.softening2;
+        a.root = fa.roots;
         a.cls_theta = F.cls_theta;
         a.cls_phase = F.cls_phase;
         a.cls_rho2 = F.cls_rho2;
         a.dmat = F.dmat;
         a.zc = F.zc;
-        a.nrm = F.nrm;
-        a.oct = F.oct;
-        a.root = fa.roots;
-        a.eps2 = c->P.softening2;
-        a.Lout = F.fL[l];
-        a.has_tgt = F.ftgt[l];
-        down_kernel<P><<<forest_grid(f.cap[l], kWarps), kWarps * 32, 0, c->stream>>>(a);
+        long long warps = 0;
+        for (int l = 2; l <= L; l++) {
+            M2LLevel &V = a.lv[a.nlev++];
+            V.nbox = f.cap[l];
+            V.chunks = F.fchunks[l];
+            V.warp0 = (int)warps;
+            V.level = l;
+            V.nbd = nbd + l;
+            V.bpid = T.lv[l].pid;
+            V.m2l = F.flst[l];
+            V.cnt = F.fcnt[l];
+            V.has_tgt = F.ftgt[l];
+            V.M = F.fM[l];
+            V.out = F.fpart[l];
+            warps += (long long)V.nbox * V.chunks;
+        }
+        m2l_kernel<P><<<(int)((warps + m2l_warps<P>() - 1) / m2l_warps<P>()), m2l_warps<P>() * 32, 0,
+                          c->stream>>>(a);
         SV_LAUNCHED(c);
+        for (int l = 2; l <= L; l++) {
+            const Level &V = T.lv[l];
+            L2LArgs b{};
+            b.nbox = f.cap[l];
+            b.chunks = F.fchunks[l];
+            b.has_parent = l > 2;
+            b.nbd = nbd + l;
+            b.parent = V.parent;
+            b.coord = V.coord;
+            b.has_tgt = F.ftgt[l];
+            b.Lp = l > 2 ? F.fL[l - 1] : nullptr;
+            b.part = F.fpart[l];
+            b.L = F.fL[l];
+            b.nrm = F.nrm;
+            b.oct = F.oct;
+            l2l_kernel<P><<<forest_grid(f.cap[l], kWarps), kWarps * 32, 0, c->stream>>>(b);
+            SV_LAUNCHED(c);
+        }
     }
     {
         const Level &V = T.lv[L];
@@ -1452,8 +1610,10 @@ sv_status fmm_forest_reserve(sv_ctx *c, const ForestArgs &fa) {
     size_t bytes = 0;
     for (int l = 0; l <= f.L; l++) {
         const size_t nb = (size_t)f.cap[l];
+        F.fchunks[l] = m2l_chunks((int)nb);
         bytes += 2 * rounded(nb * NC * sizeof(float2)) + rounded(nb * ns * sizeof(int)) +
                  rounded(nb * cap * sizeof(int2)) + 2 * rounded(nb * sizeof(int));
+        if (F.fchunks[l] > 1) bytes += rounded(nb * F.fchunks[l] * NC * sizeof(float2));
     }
     if (F.farena_bytes < bytes) {
         cudaFree(F.farena);
@@ -1469,7 +1629,7 @@ sv_status fmm_forest_reserve(sv_ctx *c, const ForestArgs &fa) {
         return (void *)r;
     };
     for (int l = 0; l <= kMortonBits; l++) {
-        F.fM[l] = F.fL[l] = nullptr;
+        F.fM[l] = F.fL[l] = F.fpart[l] = nullptr;
         F.fnbr[l] = F.fcnt[l] = F.ftgt[l] = nullptr;
         F.flst[l] = nullptr;
     }
@@ -1481,6 +1641,7 @@ sv_status fmm_forest_reserve(sv_ctx *c, const ForestArgs &fa) {
         F.flst[l] = (int2 *)carve(nb * cap * sizeof(int2));
         F.fcnt[l] = (int *)carve(nb * sizeof(int));
         F.ftgt[l] = (int *)carve(nb * sizeof(int));
+        F.fpart[l] = F.fchunks[l] > 1 ? (float2 *)carve(nb * F.fchunks[l] * NC * sizeof(float2)) : F.fL[l];
     }
     if (F.frel_cap < f.n) {
         cudaFree(F.frel);

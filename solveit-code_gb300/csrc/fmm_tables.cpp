@@ -119,22 +119,25 @@ std::vector<std::vector<cd>> yrot(int p, double a, double *max_imag) {
     return G;
 }
 
-// fold a real (2n+1)^2 rotation block into E ((n+1)^2) and O (n^2)
-void fold(const std::vector<cd> &G, int n, float *E, float *O) {
+// fold a real (2n+1)^2 rotation block into E ((n+1) rows) and O (n rows),
+// every row `stride` floats long and zero-padded; O rows carry a leading zero
+// so that both blocks pair with the coefficients m = 0..n
+void fold(const std::vector<cd> &G, int n, int stride, float *E, float *O) {
     const int w = 2 * n + 1;
     auto g = [&](int mp, int m) { return G[(mp + n) * w + (m + n)].real(); };
     for (int mp = 0; mp <= n; mp++) {
-        E[mp * (n + 1) + 0] = (float)g(mp, 0);
-        for (int m = 1; m <= n; m++) E[mp * (n + 1) + m] = (float)(g(mp, m) + g(mp, -m));
+        E[mp * stride + 0] = (float)g(mp, 0);
+        for (int m = 1; m <= n; m++) E[mp * stride + m] = (float)(g(mp, m) + g(mp, -m));
     }
     for (int mp = 1; mp <= n; mp++)
-        for (int m = 1; m <= n; m++) O[(mp - 1) * n + (m - 1)] = (float)(g(mp, m) - g(mp, -m));
+        for (int m = 1; m <= n; m++) O[(mp - 1) * stride + m] = (float)(g(mp, m) - g(mp, -m));
 }
 
 }  // namespace
 
-int dmat_offset_e(int n) { return n * (n + 1) * (2 * n + 1) / 6; }
-int dmat_offset_o(int n) { return n > 0 ? (n - 1) * n * (2 * n - 1) / 6 : 0; }
+int rot_stride(int p) { return (p + 3) / 4 * 4; }
+int dmat_offset_e(int n, int p) { return rot_stride(p) * n * (n + 1) / 2; }
+int dmat_offset_o(int n, int p) { return rot_stride(p) * n * (n - 1) / 2; }
 
 bool build_fmm_tables(int p, int ws, FmmTables &T, std::string &err) {
     T = FmmTables();
@@ -145,8 +148,9 @@ bool build_fmm_tables(int p, int ws, FmmTables &T, std::string &err) {
     const int R = T.range;
     T.side = 2 * R + 1;
     T.ncls = T.side * T.side * T.side;
-    T.esz = dmat_offset_e(p);
-    T.osz = dmat_offset_o(p);
+    T.stride = rot_stride(p);
+    T.esz = dmat_offset_e(p, p);
+    T.osz = dmat_offset_o(p, p);
     T.dsz = 2 * (T.esz + T.osz);
     T.cls_theta.assign(T.ncls, -1);
     T.cls_phase.assign((size_t)T.ncls * p * 2, 0.f);
@@ -192,17 +196,20 @@ bool build_fmm_tables(int p, int ws, FmmTables &T, std::string &err) {
         }
         float *base = &T.dmat[(size_t)ti * T.dsz];
         for (int n = 0; n < p; n++) {
-            fold(Gf[n], n, base + dmat_offset_e(n), base + T.esz + dmat_offset_o(n));
-            fold(Gb[n], n, base + T.esz + T.osz + dmat_offset_e(n), base + 2 * T.esz + T.osz + dmat_offset_o(n));
+            fold(Gf[n], n, T.stride, base + dmat_offset_e(n, p), base + T.esz + dmat_offset_o(n, p));
+            fold(Gb[n], n, T.stride, base + T.esz + T.osz + dmat_offset_e(n, p),
+                 base + 2 * T.esz + T.osz + dmat_offset_o(n, p));
         }
     }
     // z translation constants C[k][j][n] = (-1)^{j+k} (j+n)! / (N_n^k N_j^k)
-    T.zc.assign((size_t)p * p * p, 0.f);
+    // rows of n padded to the rotation stride, zero for n < k
+    T.zc.assign((size_t)p * p * T.stride, 0.f);
     auto N = [](int n, int m) { return std::sqrt(fact(n - m) * fact(n + m)); };
     for (int k = 0; k < p; k++)
         for (int j = k; j < p; j++)
             for (int n = k; n < p; n++)
-                T.zc[((size_t)k * p + j) * p + n] = (float)(((j + k) & 1 ? -1.0 : 1.0) * fact(j + n) / (N(n, k) * N(j, k)));
+                T.zc[((size_t)k * p + j) * T.stride + n] =
+                    (float)(((j + k) & 1 ? -1.0 : 1.0) * fact(j + n) / (N(n, k) * N(j, k)));
     T.nrm.assign((size_t)p * p, 0.f);
     for (int n = 0; n < p; n++)
         for (int m = 0; m <= n; m++) T.nrm[n * p + m] = (float)N(n, m);

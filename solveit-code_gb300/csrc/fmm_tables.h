@@ -12,18 +12,20 @@ struct FmmTables {
     int side = 0;    // 2*range+1: offsets per axis in the class index
     int ncls = 0;    // side^3 offset classes (target - source, box units)
     int ntheta = 0;  // distinct polar angles among the M2L offsets
+    int stride = 0;  // floats per rotation / translation row: p rounded up to 4 (16-byte rows)
     int esz = 0, osz = 0, dsz = 0;
     std::vector<int> cls_theta;    // [ncls] polar-angle index, -1 for near offsets
     std::vector<float> cls_phase;  // [ncls][p][2] cos(m phi), sin(m phi)
     std::vector<float> cls_rho2;   // [ncls] |offset|^2
-    std::vector<float> dmat;       // [ntheta][Ef | Of | Eb | Ob] folded y-rotations
-    std::vector<float> zc;         // [p][p][p] z-translation constants C[k][j][n]
+    std::vector<float> dmat;       // [ntheta][Ef | Of | Eb | Ob] folded y-rotations, rows of `stride`
+    std::vector<float> zc;         // [p][p][stride] z-translation constants C[k][j][n]
     std::vector<float> nrm;        // [p][p] sqrt((n-m)!(n+m)!)
     std::vector<float> oct;        // [8][p][2p-1][2] R_n^m of the child offsets
 };
 
-int dmat_offset_e(int n);  // sum_{k<n} (k+1)^2
-int dmat_offset_o(int n);  // sum_{k<n} k^2
+int rot_stride(int p);              // p rounded up to a multiple of 4
+int dmat_offset_e(int n, int p);    // stride * sum_{k<n} (k+1): E block of degree n
+int dmat_offset_o(int n, int p);    // stride * sum_{k<n} k: O block of degree n (rows mp = 1..n)
 bool build_fmm_tables(int p, int ws, FmmTables &T, std::string &err);
 
 }  // namespace sv
