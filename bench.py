@@ -53,6 +53,10 @@ WORKLOADS = {
     "direct_n4096": dict(n=4096, length=1e-6, method="direct", precision="fp64", seed=0,
                          desc="FP64 direct sum, N=4096 ions, plume r=20nm z=1um, eps=1e-10m, "
                               "leapfrog DKD dt=1e-13s, E_z=1e8V/m"),
+    "adjoint_n16384": dict(n=16384, length=1e-6, method="adjoint", nsteps=50, every=10, seed=4,
+                           desc="adjoint of 50 leapfrog DKD steps (direct sum, mixed precision), N=16384 ions, "
+                                "plume r=20nm z=1um, eps=1e-10m, dt=1e-13s, E_z=1e8V/m, checkpoint every 10 steps; "
+                                "loss = mean z-momentum + 1e3 x mean transverse radius"),
     "batch256": dict(n=None, nplumes=256, length=1e-6, method="batch", order=6, ws=2, seed=3,
                      desc="256 independent plumes, N_i uniform in [1024, 65536] (seed 3999), r=20nm z=1um, "
                           "direct sum for N_i < 8192 and FMM p=6 ws=2 above, 4-fold rotational variant on the "
@@ -160,6 +164,10 @@ def run_reference(args, wl, rank, world):
         return
     if wl["method"] == "batch":
         return run_reference_batch(args, wl, world)
+    if wl["method"] == "adjoint":
+        print(json.dumps({"impl": "reference", "unavailable": "the reference has no adjoint: its integrator "
+                          "runs forward only"}), flush=True)
+        return
     st = plume.make_plume(wl["n"], wl["length"], wl["seed"] * 1000 + 0)
     threads = os.cpu_count() or 1
     n_sample = 2048 if wl["n"] > 100000 else min(wl["n"], 4096)
@@ -393,6 +401,67 @@ def run_reference_batch(args, wl, world):
     print(json.dumps(line), flush=True)
 
 
+def run_adjoint(args, wl, rank, world, local):
+    """Gradient throughput: one forward rollout with checkpoints plus the
+    backward sweep per step of the metric (particle-steps of the rollout per
+    second of forward + backward time)."""
+    import torch
+
+    import solveit_gpu as sv
+
+    torch.cuda.set_device(local)
+    n, nsteps, every = wl["n"], wl["nsteps"], wl["every"]
+    st = plume.make_plume(n, wl["length"], plume_seed(wl, rank))
+
+    def grads(x, v, m):
+        gx = np.zeros_like(x)
+        gv = np.zeros_like(v)
+        gv[:, 2] = m / n
+        r = np.sqrt(x[:, 0] ** 2 + x[:, 1] ** 2)
+        gx[:, 0] = 1e3 / n * x[:, 0] / r
+        gx[:, 1] = 1e3 / n * x[:, 1] / r
+        return gx, gv
+
+    def one(prec):
+        with sv.ForceMethod(softening2=EPS2, precision=prec, efield=(0.0, 0.0, EZ), device=local) as fm:
+            fm.upload(st)
+            fm.adjoint_forward(nsteps, DT, 0.0, every)
+            x, v, _ = fm.download()
+            gx, gv = grads(x, v, st["m"])
+            fm.adjoint_backward(gx, gv)  # warm-up sweep
+            times, out = [], None
+            for _ in range(max(1, args.steps)):
+                fm.upload(st)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                fm.adjoint_forward(nsteps, DT, 0.0, every)
+                x, v, _ = fm.download()
+                out = fm.adjoint_backward(*grads(x, v, st["m"]))
+                times.append(time.perf_counter() - t0)
+            return float(np.median(times)), out
+
+    t_mixed, g_mixed = one(sv.MIXED)
+    t_fp64, g_fp64 = one(sv.FP64)
+    err = {k: float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+           for k, a, b in (("dL_dx0", g_mixed[0], g_fp64[0]), ("dL_dv0", g_mixed[1], g_fp64[1]),
+                           ("dL_dEz", g_mixed[2][2:], g_fp64[2][2:]))}
+    value = world * n * nsteps / t_mixed
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": value, "unit": "particle-steps/s (forward + backward)", "n_gpus": world,
+            "steps": args.steps, "warmup": 1, "ms_per_step": t_mixed / nsteps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 pairs (hi/lo splits in the Jacobian), f64 state",
+            "data": "synthetic (seeded plume generator)",
+            "config": {"workload": args.workload, "desc": wl["desc"], "n": n, "rollout_steps": nsteps,
+                       "checkpoint_every": every},
+            "e2e": {"value": value, "unit": "particle-steps/s", "note": "the timed region is the C ABI calls with "
+                    "host buffers (forward, download of the final state, backward with host gradients)",
+                    "h2d_bytes_per_step": 48 * n / nsteps, "d2h_bytes_per_step": 100 * n / nsteps},
+            "fp64_adjoint": {"value": world * n * nsteps / t_fp64, "unit": "particle-steps/s",
+                             "ms_rollout": t_fp64 * 1e3},
+            "speedup_vs_fp64_adjoint": t_fp64 / t_mixed, "grad_rel_diff_mixed_vs_fp64": err}), flush=True)
+
+
 def run_ours(args, wl, rank, world, local):
     import torch
 
@@ -400,6 +469,8 @@ def run_ours(args, wl, rank, world, local):
 
     if wl["method"] == "batch":
         return run_batch(args, wl, rank, world, local)
+    if wl["method"] == "adjoint":
+        return run_adjoint(args, wl, rank, world, local)
 
     torch.cuda.set_device(local)
     dist = None

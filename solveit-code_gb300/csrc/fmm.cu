@@ -445,21 +445,22 @@ template <int P, int G>
 __device__ __forceinline__ float2 rot_row(const float *__restrict__ D, int eoff, int ooff, const float2 *A, int n,
                                           int mp) {
     constexpr int RS = rot_rs<P>();
-    const float4 *E = reinterpret_cast<const float4 *>(D + eoff + RS * (n * (n + 1) / 2 + mp));
-    const float4 *O = reinterpret_cast<const float4 *>(D + ooff + RS * (n * (n - 1) / 2 + (mp > 0 ? mp - 1 : 0)));
+    // group-major blocks: group q of row r at (q * rows + r) float4s from the block start
+    const float4 *E = reinterpret_cast<const float4 *>(D + eoff + RS * (n * (n + 1) / 2)) + mp;
+    const float4 *O = reinterpret_cast<const float4 *>(D + ooff + RS * (n * (n - 1) / 2)) + (mp > 0 ? mp - 1 : 0);
     const float4 *A4 = reinterpret_cast<const float4 *>(A + n * RS);
     float re = 0.f, im = 0.f;
 #pragma unroll
     for (int q = 0; q < G; q++) {
         if (4 * q <= n) {
-            const float4 e = E[q];
+            const float4 e = E[q * (n + 1)];
             const float4 a0 = A4[2 * q], a1 = A4[2 * q + 1];
             re = fmaf(e.x, a0.x, re);
             re = fmaf(e.y, a0.z, re);
             re = fmaf(e.z, a1.x, re);
             re = fmaf(e.w, a1.z, re);
             if (mp > 0) {
-                const float4 o = O[q];
+                const float4 o = O[q * n];
                 im = fmaf(o.x, a0.y, im);
                 im = fmaf(o.y, a0.w, im);
                 im = fmaf(o.z, a1.y, im);

@@ -119,18 +119,22 @@ std::vector<std::vector<cd>> yrot(int p, double a, double *max_imag) {
     return G;
 }
 
-// fold a real (2n+1)^2 rotation block into E ((n+1) rows) and O (n rows),
-// every row `stride` floats long and zero-padded; O rows carry a leading zero
-// so that both blocks pair with the coefficients m = 0..n
+// fold a real (2n+1)^2 rotation block into E ((n+1) rows) and O (n rows) of
+// `stride` zero-padded floats; O rows carry a leading zero so that both
+// blocks pair with the coefficients m = 0..n.  Storage is group-major: the
+// 4-float group g of row r sits at (g * rows + r) * 4, so lanes that read
+// the same group of consecutive rows read consecutive 16-byte pieces.
 void fold(const std::vector<cd> &G, int n, int stride, float *E, float *O) {
+    (void)stride;
     const int w = 2 * n + 1;
     auto g = [&](int mp, int m) { return G[(mp + n) * w + (m + n)].real(); };
+    auto at = [](int rows, int r, int m) { return ((m / 4) * rows + r) * 4 + (m % 4); };
     for (int mp = 0; mp <= n; mp++) {
-        E[mp * stride + 0] = (float)g(mp, 0);
-        for (int m = 1; m <= n; m++) E[mp * stride + m] = (float)(g(mp, m) + g(mp, -m));
+        E[at(n + 1, mp, 0)] = (float)g(mp, 0);
+        for (int m = 1; m <= n; m++) E[at(n + 1, mp, m)] = (float)(g(mp, m) + g(mp, -m));
     }
     for (int mp = 1; mp <= n; mp++)
-        for (int m = 1; m <= n; m++) O[(mp - 1) * stride + m] = (float)(g(mp, m) - g(mp, -m));
+        for (int m = 1; m <= n; m++) O[at(n, mp - 1, m)] = (float)(g(mp, m) - g(mp, -m));
 }
 
 }  // namespace

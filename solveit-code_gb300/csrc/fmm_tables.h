@@ -17,7 +17,7 @@ struct FmmTables {
     std::vector<int> cls_theta;    // [ncls] polar-angle index, -1 for near offsets
     std::vector<float> cls_phase;  // [ncls][p][2] cos(m phi), sin(m phi)
     std::vector<float> cls_rho2;   // [ncls] |offset|^2
-    std::vector<float> dmat;       // [ntheta][Ef | Of | Eb | Ob] folded y-rotations, rows of `stride`
+    std::vector<float> dmat;       // [ntheta][Ef | Of | Eb | Ob] folded y-rotations, group-major rows of `stride`
     std::vector<float> zc;         // [p][p][stride] z-translation constants C[k][j][n]
     std::vector<float> nrm;        // [p][p] sqrt((n-m)!(n+m)!)
     std::vector<float> oct;        // [8][p][2p-1][2] R_n^m of the child offsets
