@@ -51,7 +51,7 @@ struct Fmm {
     float *dmat = nullptr;
     float *zc = nullptr;
     float *nrm = nullptr;
-    float2 *oct = nullptr;
+    float *otab = nullptr;   // rotation-based M2M / L2L tables (oct_layout)
     void *arena = nullptr;
     size_t arena_bytes = 0;
     unsigned long long *d_counts = nullptr;  // [0] M2L translations, [1] P2P pairs
@@ -118,13 +118,6 @@ __device__ __forceinline__ void solid_harmonics(float x, float y, float z, float
             R[cidx(n, m)] = make_float2((a * r1.x - r2 * r0.x) * d, (a * r1.y - r2 * r0.y) * d);
         }
     }
-}
-
-// R_n^m for any order from the m >= 0 half: R_n^-m = (-1)^m conj(R_n^m)
-__device__ __forceinline__ float2 half_get(const float2 *C, int n, int m) {
-    if (m >= 0) return C[cidx(n, m)];
-    const float2 v = C[cidx(n, -m)];
-    return (m & 1) ? make_float2(-v.x, v.y) : make_float2(v.x, -v.y);
 }
 
 // Box count of a level: the launch bound nbox, or (forest) the device count.
@@ -324,57 +317,7 @@ p2m_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, 
 }
 
 // ------------------------------------------------------------------ M2M --
-template <int P>
-__global__ void __launch_bounds__(kWarps * 32)
-m2m_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ child0, const int4 *__restrict__ ccoord,
-           const float2 *__restrict__ Mc, float2 *__restrict__ Mp, const float *__restrict__ nrm,
-           const float2 *__restrict__ oct) {
-    constexpr int NC = ncoef(P), W = 2 * P - 1;
-    __shared__ float2 mu[kWarps][NC];
-    SV_WARP_BOXES(kWarps) {
-    float2 acc[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
-    const int ch1 = child0[b + 1];
-    for (int ch = child0[b]; ch < ch1; ch++) {
-        const int4 cc = ccoord[ch];
-        const int oc = (cc.x & 1) | ((cc.y & 1) << 1) | ((cc.z & 1) << 2);
-        const float2 *Rd = oct + (size_t)oc * P * W;
-        for (int c = lane; c < NC; c += 32) {
-            int n, m;
-            cnm(c, n, m);
-            mu[wid][c] = cscale(Mc[(size_t)ch * NC + c], 1.f / nrm[n * P + m]);
-        }
-        __syncwarp();
-#pragma unroll
-        for (int t = 0; t < 2; t++) {
-            const int c = lane + 32 * t;
-            if (c >= NC) break;
-            int n, m;
-            cnm(c, n, m);
-            float2 s = make_float2(0.f, 0.f);
-            for (int k = 0; k <= n; k++) {
-                const int nk = n - k;
-                for (int l = -k; l <= k; l++) {
-                    const int ml = m - l;
-                    if (ml > nk || ml < -nk) continue;
-                    s = cadd(s, cmul(half_get(mu[wid], k, l), cconj(Rd[nk * W + ml + P - 1])));
-                }
-            }
-            acc[t] = cadd(acc[t], s);
-        }
-        __syncwarp();
-    }
-#pragma unroll
-    for (int t = 0; t < 2; t++) {
-        const int c = lane + 32 * t;
-        if (c >= NC) break;
-        int n, m;
-        cnm(c, n, m);
-        // back to G-R normalisation, from child to parent box units (x 2^-n)
-        Mp[(size_t)b * NC + c] = cscale(acc[t], nrm[n * P + m] * ldexpf(1.f, -n));
-    }
-    }
-}
-
+// (defined after the rotation helpers below)
 // ----------------------------------------------------------- downward --
 // M2L of every level in one launch, then L2L level by level.  A level with few
 // boxes (the coarse ones, whose lists are long) splits each box's list over
@@ -415,8 +358,7 @@ struct L2LArgs {
     const float2 *Lp;     // final locals of the parent level
     const float2 *part;   // this level's M2L partials [box][chunk]
     float2 *L;            // this level's locals (may alias part when chunks == 1)
-    const float *nrm;
-    const float2 *oct;
+    const float *otab;    // rotation-based translation tables
 };
 
 // rows of the coefficients held in slot 1 (the EXTRA lowest coefficients)
@@ -500,6 +442,104 @@ __device__ __forceinline__ float2 ztrans_row(const float *__restrict__ zc, const
         im = fmaf(f0, b0.y, fmaf(f1, b0.w, fmaf(f2, b1.y, fmaf(f3, b1.w, im))));
     }
     return make_float2(re, im);
+}
+
+// Offsets in the octant table (same as oct_layout on the host).
+template <int P>
+struct OctOff {
+    static constexpr int RS = rot_rs<P>(), DSZ = 2 * RS * P * P, ZSZ = P * P * RS;
+    static constexpr int rot = 0, zm2m = 2 * DSZ, zl2l = zm2m + ZSZ, ph_m2m = zl2l + ZSZ, ph_l2l = ph_m2m + 16 * P,
+                         th_m2m = ph_l2l + 16 * P, th_l2l = th_m2m + 8;
+};
+
+// One output (j, k) of a z-shift by a fixed distance: sum_n Z[k][j][n] B[k][n]
+template <int P>
+__device__ __forceinline__ float2 zshift_row(const float *__restrict__ zt, const float2 *Bk, int j, int k) {
+    constexpr int RS = rot_rs<P>();
+    const float4 *Z = reinterpret_cast<const float4 *>(zt + ((size_t)k * P + j) * RS);
+    const float4 *B4 = reinterpret_cast<const float4 *>(Bk + k * RS);
+    float re = 0.f, im = 0.f;
+#pragma unroll
+    for (int q = 0; q < RS / 4; q++) {
+        const float4 z = __ldg(Z + q);
+        const float4 b0 = B4[2 * q], b1 = B4[2 * q + 1];
+        re = fmaf(z.x, b0.x, fmaf(z.y, b0.z, fmaf(z.z, b1.x, fmaf(z.w, b1.z, re))));
+        im = fmaf(z.x, b0.y, fmaf(z.y, b0.w, fmaf(z.z, b1.y, fmaf(z.w, b1.w, im))));
+    }
+    return make_float2(re, im);
+}
+
+// Rotation-based translation of one coefficient vector (GR normalisation,
+// compact layout) along an octant direction: phase e^{i m phi}, y-rotation
+// that takes the direction to +z, fixed z-shift Z, back-rotation, phase
+// e^{-i m phi}; the result is added into the lane's accumulators.  A and B are
+// the warp's degree-major / order-major rows, zero outside (n, m <= n).
+template <int P>
+__device__ __forceinline__ void oct_translate(const float2 *__restrict__ in, const float2 *__restrict__ ph,
+                                              const float *__restrict__ D, const float *__restrict__ Z, float2 *A,
+                                              float2 *B, const int *cn, const int *cm, const int *cs,
+                                              const bool *has, float2 *acc) {
+    constexpr int RS = rot_rs<P>(), G0 = RS / 4, G1 = slot1_rows<P>() / 4 + 1;
+    constexpr int ESZ = RS * P * (P + 1) / 2, OSZ = RS * P * (P - 1) / 2;
+#pragma unroll
+    for (int t = 0; t < 2; t++)
+        if (has[t]) A[cn[t] * RS + cm[t]] = cmul(in[cs[t]], ph[cm[t]]);
+    __syncwarp();
+    if (has[0]) B[cm[0] * RS + cn[0]] = rot_row<P, G0>(D, 0, ESZ, A, cn[0], cm[0]);
+    if (has[1]) B[cm[1] * RS + cn[1]] = rot_row<P, G1>(D, 0, ESZ, A, cn[1], cm[1]);
+    __syncwarp();
+    if (has[0]) A[cn[0] * RS + cm[0]] = zshift_row<P>(Z, B, cn[0], cm[0]);
+    if (has[1]) A[cn[1] * RS + cm[1]] = zshift_row<P>(Z, B, cn[1], cm[1]);
+    __syncwarp();
+    if (has[0]) acc[0] = cadd(acc[0], cmul(rot_row<P, G0>(D, ESZ + OSZ, 2 * ESZ + OSZ, A, cn[0], cm[0]), cconj(ph[cm[0]])));
+    if (has[1]) acc[1] = cadd(acc[1], cmul(rot_row<P, G1>(D, ESZ + OSZ, 2 * ESZ + OSZ, A, cn[1], cm[1]), cconj(ph[cm[1]])));
+    __syncwarp();
+}
+
+// lane slots of the translation kernels: slot 0 of every lane holds one of
+// the NC - EXTRA highest coefficients, slot 1 of the first EXTRA lanes one of
+// the EXTRA lowest (NC > 32 at p >= 8)
+template <int P>
+__device__ __forceinline__ void coef_slots(int lane, int *cn, int *cm, int *cs, bool *has) {
+    constexpr int NC = ncoef(P), EXTRA = NC > 32 ? NC - 32 : 0;
+    cs[0] = lane + EXTRA;
+    cs[1] = lane;
+    cnm(min(cs[0], NC - 1), cn[0], cm[0]);
+    cnm(min(cs[1], NC - 1), cn[1], cm[1]);
+    has[0] = cs[0] < NC;
+    has[1] = lane < EXTRA;
+}
+
+// M2M: one warp per parent box; each child's multipole translated to the
+// parent centre by rotation (O(p^3) per child instead of the O(p^4) direct
+// R-convolution), child -> parent box units folded into the z-shift table.
+template <int P>
+__global__ void __launch_bounds__(kWarps * 32)
+m2m_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ child0, const int4 *__restrict__ ccoord,
+           const float2 *__restrict__ Mc, float2 *__restrict__ Mp, const float *__restrict__ otab) {
+    constexpr int NC = ncoef(P), RS = rot_rs<P>();
+    using O = OctOff<P>;
+    __shared__ __align__(16) float2 A[kWarps][P * RS], B[kWarps][P * RS];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int t = lane; t < P * RS; t += 32) A[wid][t] = B[wid][t] = make_float2(0.f, 0.f);
+    __syncwarp();
+    int cn[2], cm[2], cs[2];
+    bool has[2];
+    coef_slots<P>(lane, cn, cm, cs, has);
+    const int nb = level_boxes(nbox, nbd);
+    for (int b = blockIdx.x * kWarps + wid; b < nb; b += gridDim.x * kWarps) {
+        float2 acc[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+        const int ch1 = child0[b + 1];
+        for (int ch = child0[b]; ch < ch1; ch++) {
+            const int4 cc = ccoord[ch];
+            const int oc = (cc.x & 1) | ((cc.y & 1) << 1) | ((cc.z & 1) << 2);
+            const int th = (int)otab[O::th_m2m + oc];
+            oct_translate<P>(Mc + (size_t)ch * NC, reinterpret_cast<const float2 *>(otab + O::ph_m2m) + oc * P,
+                             otab + O::rot + th * O::DSZ, otab + O::zm2m, A[wid], B[wid], cn, cm, cs, has, acc);
+        }
+        if (has[0]) Mp[(size_t)b * NC + cs[0]] = acc[0];
+        if (has[1]) Mp[(size_t)b * NC + cs[1]] = acc[1];
+    }
 }
 
 template <int P>
@@ -599,58 +639,39 @@ __global__ void __launch_bounds__(m2l_warps<P>() * 32) m2l_kernel(M2LArgs a) {
     if (has[1]) dst[cs[1]] = acc[1];
 }
 
-// L = (sum of the level's M2L partials, in chunk order) + L2L(parent's L)
+// L = (sum of the level's M2L partials, in chunk order) + L2L(parent's L),
+// the L2L by rotation (O(p^3)), parent -> child box units folded into the
+// z-shift table
 template <int P>
 __global__ void __launch_bounds__(kWarps * 32) l2l_kernel(L2LArgs a) {
-    constexpr int NC = ncoef(P), W = 2 * P - 1;
-    __shared__ float2 A[kWarps][NC];
-    const int nbox = a.nbox;
-    const int *nbd = a.nbd;
-    SV_WARP_BOXES(kWarps) {
-    if (!a.has_tgt[b]) continue;
-    float2 acc[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+    constexpr int NC = ncoef(P), RS = rot_rs<P>();
+    using O = OctOff<P>;
+    __shared__ __align__(16) float2 A[kWarps][P * RS], B[kWarps][P * RS];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int t = lane; t < P * RS; t += 32) A[wid][t] = B[wid][t] = make_float2(0.f, 0.f);
+    __syncwarp();
+    int cn[2], cm[2], cs[2];
+    bool has[2];
+    coef_slots<P>(lane, cn, cm, cs, has);
+    const int nb = level_boxes(a.nbox, a.nbd);
+    for (int b = blockIdx.x * kWarps + wid; b < nb; b += gridDim.x * kWarps) {
+        if (!a.has_tgt[b]) continue;
+        float2 acc[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
 #pragma unroll
-    for (int t = 0; t < 2; t++) {
-        const int c = lane + 32 * t;
-        if (c >= NC) break;
-        for (int ch = 0; ch < a.chunks; ch++) acc[t] = cadd(acc[t], a.part[((size_t)b * a.chunks + ch) * NC + c]);
-    }
-    if (a.has_parent) {
-        // L2L from the parent (parent box units -> child box units)
-        const int par = a.parent[b];
-        const int4 cb = a.coord[b];
-        const int oc = (cb.x & 1) | ((cb.y & 1) << 1) | ((cb.z & 1) << 2);
-        const float2 *Rd = a.oct + (size_t)oc * P * W;
-        for (int c = lane; c < NC; c += 32) {
-            int n, m;
-            cnm(c, n, m);
-            A[wid][c] = cscale(a.Lp[(size_t)par * NC + c], a.nrm[n * P + m] * ldexpf(1.f, -(n + 1)));
+        for (int t = 0; t < 2; t++)
+            if (has[t])
+                for (int ch = 0; ch < a.chunks; ch++)
+                    acc[t] = cadd(acc[t], a.part[((size_t)b * a.chunks + ch) * NC + cs[t]]);
+        if (a.has_parent) {
+            const int4 cb = a.coord[b];
+            const int oc = (cb.x & 1) | ((cb.y & 1) << 1) | ((cb.z & 1) << 2);
+            const int th = (int)a.otab[O::th_l2l + oc];
+            oct_translate<P>(a.Lp + (size_t)a.parent[b] * NC,
+                             reinterpret_cast<const float2 *>(a.otab + O::ph_l2l) + oc * P,
+                             a.otab + O::rot + th * O::DSZ, a.otab + O::zl2l, A[wid], B[wid], cn, cm, cs, has, acc);
         }
-        __syncwarp();
-#pragma unroll
-        for (int t = 0; t < 2; t++) {
-            const int c = lane + 32 * t;
-            if (c >= NC) break;
-            int k, l;
-            cnm(c, k, l);
-            float2 s = make_float2(0.f, 0.f);
-            for (int n = k; n < P; n++) {
-                const int nk = n - k;
-                for (int m = -n; m <= n; m++) {
-                    const int ml = m - l;
-                    if (ml > nk || ml < -nk) continue;
-                    s = cadd(s, cmul(half_get(A[wid], n, m), Rd[nk * W + ml + P - 1]));
-                }
-            }
-            acc[t] = cadd(acc[t], cscale(s, 1.f / a.nrm[k * P + l]));
-        }
-        __syncwarp();
-    }
-#pragma unroll
-    for (int t = 0; t < 2; t++) {
-        const int c = lane + 32 * t;
-        if (c < NC) a.L[(size_t)b * NC + c] = acc[t];
-    }
+        if (has[0]) a.L[(size_t)b * NC + cs[0]] = acc[0];
+        if (has[1]) a.L[(size_t)b * NC + cs[1]] = acc[1];
     }
 }
 
@@ -1212,7 +1233,7 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
     for (int l = L - 1; l >= 2; l--) {
         const Level &V = T.lv[l];
         m2m_kernel<P><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
-            V.nbox, nullptr, V.child0, T.lv[l + 1].coord, Mv[l + 1], Mv[l], F.nrm, F.oct);
+            V.nbox, nullptr, V.child0, T.lv[l + 1].coord, Mv[l + 1], Mv[l], F.otab);
         SV_LAUNCHED(c);
     }
     phase_mark(c, 4);
@@ -1263,8 +1284,7 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
             b.Lp = l > 2 ? Lv[l - 1] : nullptr;
             b.part = part[l];
             b.L = Lv[l];
-            b.nrm = F.nrm;
-            b.oct = F.oct;
+            b.otab = F.otab;
             l2l_kernel<P><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(b);
             SV_LAUNCHED(c);
         }
@@ -1384,7 +1404,7 @@ sv_status run_fmm_forest(sv_ctx *c, Fmm &F, const ForestArgs &fa) {
     for (int l = L - 1; l >= 2; l--) {
         const Level &V = T.lv[l];
         m2m_kernel<P><<<forest_grid(f.cap[l], kWarps), kWarps * 32, 0, c->stream>>>(
-            f.cap[l], nbd + l, V.child0, T.lv[l + 1].coord, F.fM[l + 1], F.fM[l], F.nrm, F.oct);
+            f.cap[l], nbd + l, V.child0, T.lv[l + 1].coord, F.fM[l + 1], F.fM[l], F.otab);
         SV_LAUNCHED(c);
     }
     {
@@ -1432,8 +1452,7 @@ sv_status run_fmm_forest(sv_ctx *c, Fmm &F, const ForestArgs &fa) {
             b.Lp = l > 2 ? F.fL[l - 1] : nullptr;
             b.part = F.fpart[l];
             b.L = F.fL[l];
-            b.nrm = F.nrm;
-            b.oct = F.oct;
+            b.otab = F.otab;
             l2l_kernel<P><<<forest_grid(f.cap[l], kWarps), kWarps * 32, 0, c->stream>>>(b);
             SV_LAUNCHED(c);
         }
@@ -1462,7 +1481,7 @@ sv_status ensure_tables(sv_ctx *c, Fmm &F, int p, int ws) {
     std::string err;
     if (!build_fmm_tables(p, ws, F.H, err)) return set_error(c, SV_ERR_INVALID, "FMM tables: %s", err.c_str());
     cudaFree(F.cls_theta); cudaFree(F.cls_phase); cudaFree(F.cls_rho2); cudaFree(F.dmat);
-    cudaFree(F.zc); cudaFree(F.nrm); cudaFree(F.oct);
+    cudaFree(F.zc); cudaFree(F.nrm); cudaFree(F.otab);
     const FmmTables &H = F.H;
     SV_CK(c, cudaMalloc(&F.cls_theta, sizeof(int) * H.cls_theta.size()));
     SV_CK(c, cudaMalloc(&F.cls_phase, sizeof(float) * H.cls_phase.size()));
@@ -1470,14 +1489,14 @@ sv_status ensure_tables(sv_ctx *c, Fmm &F, int p, int ws) {
     SV_CK(c, cudaMalloc(&F.dmat, sizeof(float) * H.dmat.size()));
     SV_CK(c, cudaMalloc(&F.zc, sizeof(float) * H.zc.size()));
     SV_CK(c, cudaMalloc(&F.nrm, sizeof(float) * H.nrm.size()));
-    SV_CK(c, cudaMalloc(&F.oct, sizeof(float) * H.oct.size()));
+    SV_CK(c, cudaMalloc(&F.otab, sizeof(float) * H.otab.size()));
     SV_CK(c, cudaMemcpy(F.cls_theta, H.cls_theta.data(), sizeof(int) * H.cls_theta.size(), cudaMemcpyHostToDevice));
     SV_CK(c, cudaMemcpy(F.cls_phase, H.cls_phase.data(), sizeof(float) * H.cls_phase.size(), cudaMemcpyHostToDevice));
     SV_CK(c, cudaMemcpy(F.cls_rho2, H.cls_rho2.data(), sizeof(float) * H.cls_rho2.size(), cudaMemcpyHostToDevice));
     SV_CK(c, cudaMemcpy(F.dmat, H.dmat.data(), sizeof(float) * H.dmat.size(), cudaMemcpyHostToDevice));
     SV_CK(c, cudaMemcpy(F.zc, H.zc.data(), sizeof(float) * H.zc.size(), cudaMemcpyHostToDevice));
     SV_CK(c, cudaMemcpy(F.nrm, H.nrm.data(), sizeof(float) * H.nrm.size(), cudaMemcpyHostToDevice));
-    SV_CK(c, cudaMemcpy(F.oct, H.oct.data(), sizeof(float) * H.oct.size(), cudaMemcpyHostToDevice));
+    SV_CK(c, cudaMemcpy(F.otab, H.otab.data(), sizeof(float) * H.otab.size(), cudaMemcpyHostToDevice));
     F.p = p;
     F.ws = ws;
     return SV_OK;
@@ -1489,7 +1508,7 @@ void fmm_free(sv_ctx *c) {
     if (!c->fmm) return;
     Fmm &F = *c->fmm;
     cudaFree(F.cls_theta); cudaFree(F.cls_phase); cudaFree(F.cls_rho2); cudaFree(F.dmat);
-    cudaFree(F.zc); cudaFree(F.nrm); cudaFree(F.oct); cudaFree(F.arena); cudaFree(F.d_counts);
+    cudaFree(F.zc); cudaFree(F.nrm); cudaFree(F.otab); cudaFree(F.arena); cudaFree(F.d_counts);
     cudaFree(F.ex); cudaFree(F.ey); cudaFree(F.ez); cudaFree(F.eq); cudaFree(F.em); cudaFree(F.est);
     cudaFree(F.eoff); cudaFree(F.has_tgt); cudaFree(F.rel);
     cudaFree(F.farena); cudaFree(F.frel);

@@ -140,6 +140,20 @@ void fold(const std::vector<cd> &G, int n, int stride, float *E, float *O) {
 }  // namespace
 
 int rot_stride(int p) { return (p + 3) / 4 * 4; }
+
+OctLayout oct_layout(int p) {
+    const int rs = rot_stride(p), dsz = 2 * rs * p * p, zsz = p * p * rs;
+    OctLayout o;
+    o.rot = 0;
+    o.zm2m = 2 * dsz;
+    o.zl2l = o.zm2m + zsz;
+    o.ph_m2m = o.zl2l + zsz;
+    o.ph_l2l = o.ph_m2m + 16 * p;
+    o.th_m2m = o.ph_l2l + 16 * p;
+    o.th_l2l = o.th_m2m + 8;
+    o.size = o.th_l2l + 8;
+    return o;
+}
 int dmat_offset_e(int n, int p) { return rot_stride(p) * n * (n + 1) / 2; }
 int dmat_offset_o(int n, int p) { return rot_stride(p) * n * (n - 1) / 2; }
 
@@ -217,28 +231,55 @@ bool build_fmm_tables(int p, int ws, FmmTables &T, std::string &err) {
     T.nrm.assign((size_t)p * p, 0.f);
     for (int n = 0; n < p; n++)
         for (int m = 0; m <= n; m++) T.nrm[n * p + m] = (float)N(n, m);
-    // regular solid harmonics R_n^m(d) of the 8 child offsets d = (+-1/2)^3 in
-    // child box units, all orders m in [-n, n] (R_n^-m = (-1)^m conj R_n^m)
-    T.oct.assign((size_t)8 * p * (2 * p - 1) * 2, 0.f);
-    for (int oc = 0; oc < 8; oc++) {
-        const double x = (oc & 1) ? 0.5 : -0.5, y = (oc & 2) ? 0.5 : -0.5, z = (oc & 4) ? 0.5 : -0.5;
-        const double r2 = x * x + y * y + z * z;
-        std::vector<cd> Rh(p * p, cd(0, 0));
-        Rh[0] = 1.0;
-        for (int m = 0; m < p; m++) {
-            if (m > 0) Rh[m * p + m] = cd(x, y) / (2.0 * m) * Rh[(m - 1) * p + (m - 1)];
-            if (m + 1 < p) Rh[(m + 1) * p + m] = z * Rh[m * p + m];
-            for (int n = m + 2; n < p; n++)
-                Rh[n * p + m] = ((2.0 * n - 1) * z * Rh[(n - 1) * p + m] - r2 * Rh[(n - 2) * p + m]) /
-                                (double)((n + m) * (n - m));
-        }
-        for (int n = 0; n < p; n++)
-            for (int m = -n; m <= n; m++) {
-                cd v = m >= 0 ? Rh[n * p + m] : ((m & 1) ? -1.0 : 1.0) * std::conj(Rh[n * p - m]);
-                const size_t o = (((size_t)oc * p + n) * (2 * p - 1) + (m + p - 1)) * 2;
-                T.oct[o] = (float)v.real();
-                T.oct[o + 1] = (float)v.imag();
+    // rotation-based M2M / L2L tables (see oct_layout)
+    {
+        const OctLayout L = oct_layout(p);
+        T.otab.assign(L.size, 0.f);
+        const double th0 = std::acos(1.0 / std::sqrt(3.0)), rho = std::sqrt(3.0) / 2.0;
+        const double ths[2] = {th0, M_PI - th0};
+        for (int ti = 0; ti < 2; ti++) {
+            double mi1 = 0, mi2 = 0;
+            auto Gf = yrot(p, ths[ti], &mi1);
+            auto Gb = yrot(p, -ths[ti], &mi2);
+            if (mi1 > 1e-9 || mi2 > 1e-9) {
+                err = "octant y-rotation matrix is not real";
+                return false;
             }
+            float *base = &T.otab[(size_t)L.rot + (size_t)ti * T.dsz];
+            for (int n = 0; n < p; n++) {
+                fold(Gf[n], n, T.stride, base + dmat_offset_e(n, p), base + T.esz + dmat_offset_o(n, p));
+                fold(Gb[n], n, T.stride, base + T.esz + T.osz + dmat_offset_e(n, p),
+                     base + 2 * T.esz + T.osz + dmat_offset_o(n, p));
+            }
+        }
+        auto Nn = [](int n, int m) { return std::sqrt(fact(n - m) * fact(n + m)); };
+        for (int k = 0; k < p; k++)
+            for (int j = k; j < p; j++)
+                for (int n = k; n < p; n++) {
+                    // multipole: new centre = old + rho z (child -> parent centre), child -> parent units
+                    if (n <= j)
+                        T.otab[L.zm2m + ((size_t)k * p + j) * T.stride + n] =
+                            (float)(Nn(j, k) / Nn(n, k) * std::pow(-rho, j - n) / fact(j - n) * std::ldexp(1.0, -j));
+                    // local: new centre = old + rho z (parent -> child centre), parent -> child units
+                    if (n >= j)
+                        T.otab[L.zl2l + ((size_t)k * p + j) * T.stride + n] =
+                            (float)(Nn(n, k) / Nn(j, k) * std::pow(rho, n - j) / fact(n - j) * std::ldexp(1.0, -(n + 1)));
+                }
+        for (int oc = 0; oc < 8; oc++) {
+            // child centre - parent centre, child box units
+            const double d[3] = {(oc & 1) ? 0.5 : -0.5, (oc & 2) ? 0.5 : -0.5, (oc & 4) ? 0.5 : -0.5};
+            for (int kind = 0; kind < 2; kind++) {
+                const double sgn = kind == 0 ? -1.0 : 1.0;  // M2M moves parent-ward, L2L child-ward
+                const double tx = sgn * d[0], ty = sgn * d[1], tz = sgn * d[2];
+                const double ph = std::atan2(ty, tx);
+                const int ph0 = kind == 0 ? L.ph_m2m : L.ph_l2l, th = kind == 0 ? L.th_m2m : L.th_l2l;
+                T.otab[th + oc] = tz > 0 ? 0.f : 1.f;
+                for (int m = 0; m < p; m++) {
+                    T.otab[ph0 + ((size_t)oc * p + m) * 2 + 0] = (float)std::cos(m * ph);
+                    T.otab[ph0 + ((size_t)oc * p + m) * 2 + 1] = (float)std::sin(m * ph);
+                }
+            }
+        }
     }
     return true;
 }

@@ -20,8 +20,22 @@ struct FmmTables {
     std::vector<float> dmat;       // [ntheta][Ef | Of | Eb | Ob] folded y-rotations, group-major rows of `stride`
     std::vector<float> zc;         // [p][p][stride] z-translation constants C[k][j][n]
     std::vector<float> nrm;        // [p][p] sqrt((n-m)!(n+m)!)
-    std::vector<float> oct;        // [8][p][2p-1][2] R_n^m of the child offsets
+    // rotation-based M2M / L2L along the 8 child directions (layout: oct_layout)
+    std::vector<float> otab;
 };
+
+// Offsets (floats) inside FmmTables::otab for order p.  The child offsets
+// (+-1/2)^3 (child box units) have two polar angles, theta0 = acos(1/sqrt 3)
+// and pi - theta0:
+//   rot    [2][dsz]        folded y-rotation blocks of both angles (dmat layout)
+//   zm2m   [p][p][stride]  z-shift of a multipole by -sqrt(3)/2, child -> parent units
+//   zl2l   [p][p][stride]  z-shift of a local expansion by +sqrt(3)/2, parent -> child units
+//   ph_m2m, ph_l2l [8][p][2]  e^{i m phi} of each octant's translation direction
+//   th_m2m, th_l2l [8]        polar-angle index (0 or 1) of each octant's direction
+struct OctLayout {
+    int rot, zm2m, zl2l, ph_m2m, ph_l2l, th_m2m, th_l2l, size;
+};
+OctLayout oct_layout(int p);
 
 int rot_stride(int p);              // p rounded up to a multiple of 4
 int dmat_offset_e(int n, int p);    // stride * sum_{k<n} (k+1): E block of degree n
