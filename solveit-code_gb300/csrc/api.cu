@@ -127,9 +127,9 @@ sv_status dev_alloc(sv_ctx *c, T **p, int64_t count) {
 void free_state(sv_ctx *c) {
     cudaFree(c->x); cudaFree(c->y); cudaFree(c->z);
     cudaFree(c->vx); cudaFree(c->vy); cudaFree(c->vz);
-    cudaFree(c->q); cudaFree(c->m); cudaFree(c->t_inj); cudaFree(c->status);
+    cudaFree(c->q); cudaFree(c->m); cudaFree(c->t_inj); cudaFree(c->status); cudaFree(c->qom);
     cudaFree(c->ax); cudaFree(c->ay); cudaFree(c->az);
-    c->x = c->y = c->z = c->vx = c->vy = c->vz = c->q = c->m = c->t_inj = nullptr;
+    c->x = c->y = c->z = c->vx = c->vy = c->vz = c->q = c->m = c->t_inj = c->qom = nullptr;
     c->ax = c->ay = c->az = nullptr;
     c->status = nullptr;
     c->cap = 0;
@@ -142,10 +142,17 @@ sv_status ensure_capacity(sv_ctx *c, int64_t n) {
     SV_TRY(dev_alloc(c, &c->x, cap)); SV_TRY(dev_alloc(c, &c->y, cap)); SV_TRY(dev_alloc(c, &c->z, cap));
     SV_TRY(dev_alloc(c, &c->vx, cap)); SV_TRY(dev_alloc(c, &c->vy, cap)); SV_TRY(dev_alloc(c, &c->vz, cap));
     SV_TRY(dev_alloc(c, &c->q, cap)); SV_TRY(dev_alloc(c, &c->m, cap)); SV_TRY(dev_alloc(c, &c->t_inj, cap));
+    SV_TRY(dev_alloc(c, &c->qom, cap));
     SV_TRY(dev_alloc(c, &c->status, cap));
     SV_TRY(dev_alloc(c, &c->ax, cap)); SV_TRY(dev_alloc(c, &c->ay, cap)); SV_TRY(dev_alloc(c, &c->az, cap));
     c->cap = cap;
     return SV_OK;
+}
+
+__global__ void charge_over_mass(const double *__restrict__ q, const double *__restrict__ m, int64_t n,
+                                 double *__restrict__ qom) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) qom[i] = m[i] > 0.0 ? q[i] / m[i] : 0.0;
 }
 
 __global__ void unpack_fp64(const double *__restrict__ x3, const double *__restrict__ v3,
@@ -447,6 +454,8 @@ static sv_status upload_state(sv_ctx *c, int64_t n, const double *x3, const doub
                                                    c->x, c->y, c->z, c->vx, c->vy, c->vz, c->q, c->m,
                                                    c->status, c->t_inj);
     SV_LAUNCHED(c);
+    charge_over_mass<<<grid_of(n), 256, 0, c->stream>>>(c->q, c->m, n, c->qom);
+    SV_LAUNCHED(c);
     return SV_OK;
 }
 
@@ -484,6 +493,8 @@ sv_status sv_upload_ref32(sv_ctx *c, int64_t n, const float *pos4, const float *
     if (t_inj) SV_CK(c, cudaMemcpyAsync(dt, t_inj, 4 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
     unpack_ref32<<<grid_of(n), 256, 0, c->stream>>>(dp, dv, da, dt, n, t_inj != nullptr, c->x, c->y, c->z,
                                                     c->vx, c->vy, c->vz, c->q, c->m, c->status, c->t_inj);
+    SV_LAUNCHED(c);
+    charge_over_mass<<<grid_of(n), 256, 0, c->stream>>>(c->q, c->m, n, c->qom);
     SV_LAUNCHED(c);
     return SV_OK;
 }
@@ -547,7 +558,7 @@ sv_status sv::compute_accel_device(sv_ctx *c, int64_t first, int64_t last) {
             // outliers leave the tree; their interactions are summed directly below
             const int32_t *st2 = nullptr;
             SV_TRY(outliers_detect(c, &st2));
-            const ParticleView v{c->x, c->y, c->z, c->q, c->m, st2, c->n, c->n};
+            const ParticleView v{c->x, c->y, c->z, c->q, c->m, st2, c->n, c->n, c->qom};
             SV_TRY(sort_view(c, v, first, last));
         } else if (c->P.method == SV_METHOD_FMM && c->P.symmetry != SV_SYM_NONE) {
             SV_TRY(fmm_sort_images(c, first, last));

@@ -245,7 +245,8 @@ __global__ void batch_gather_kernel(int64_t nv, const uint32_t *__restrict__ idx
                                     const uint32_t *__restrict__ vtag, const double *__restrict__ x,
                                     const double *__restrict__ y, const double *__restrict__ z,
                                     const double *__restrict__ q, const double *__restrict__ m,
-                                    const int32_t *__restrict__ st, const double *__restrict__ roots, double kconst,
+                                    const double *__restrict__ qom, const int32_t *__restrict__ st,
+                                    const double *__restrict__ roots, double kconst,
                                     double *__restrict__ xs, double *__restrict__ ys, double *__restrict__ zs,
                                     float *__restrict__ qs, double *__restrict__ qm) {
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -260,7 +261,7 @@ __global__ void batch_gather_kernel(int64_t nv, const uint32_t *__restrict__ idx
     zs[s] = pz;
     qs[s] = src ? (float)q[i] : 0.0f;
     const bool tgt = (tag & 3u) == 0 && st[i] == 1 && m[i] > 0.0;
-    qm[s] = tgt ? kconst * q[i] / m[i] : 0.0;
+    qm[s] = tgt ? kconst * qom[i] : 0.0;
 }
 
 __global__ void batch_scatter_kernel(int64_t nv, const uint32_t *__restrict__ idx, const uint32_t *__restrict__ vsrc,
@@ -520,8 +521,8 @@ sv_status sort_batch(sv_ctx *c, Batch &B, bool adapt) {
         SV_LAUNCHED(c);
     }
     batch_gather_kernel<<<div_up(nv, 256), 256, 0, c->stream>>>(nv, S.idx, B.vsrc, B.vtag, c->x, c->y, c->z, c->q,
-                                                                c->m, c->status, B.roots, c->P.k_const, S.x, S.y,
-                                                                S.z, S.q, S.qm);
+                                                                c->m, c->qom, c->status, B.roots, c->P.k_const,
+                                                                S.x, S.y, S.z, S.q, S.qm);
     SV_LAUNCHED(c);
     return SV_OK;
 }

@@ -33,15 +33,15 @@ __global__ void drift_kernel(double *__restrict__ x, double *__restrict__ y, dou
 
 __global__ void kick_kernel(double *__restrict__ vx, double *__restrict__ vy, double *__restrict__ vz,
                             const double *__restrict__ ax, const double *__restrict__ ay,
-                            const double *__restrict__ az, const double *__restrict__ q,
-                            const double *__restrict__ m, const int32_t *__restrict__ st,
+                            const double *__restrict__ az, const double *__restrict__ qom,
+                            const int32_t *__restrict__ st,
                             const double *__restrict__ t_inj, int64_t n, double t_start, double dt,
                             double eoa, double ex, double ey, double ez, const double *__restrict__ tb) {
     if (tb) t_start += tb[0] + tb[1] * tb[2];
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         if (st[i] != 1) continue;
-        const double f = m[i] > 0.0 ? eoa * q[i] / m[i] : 0.0;
+        const double f = eoa * qom[i];
         const double s = fmin(fmax(t_start + dt - t_inj[i], 0.0), dt);
         vx[i] += (ax[i] + ex * f) * s;
         vy[i] += (ay[i] + ey * f) * s;
@@ -125,7 +125,7 @@ sv_status drift(sv_ctx *c, double t_start, double h, const double *tb) {
 
 sv_status kick(sv_ctx *c, double t_start, double dt, const double *tb) {
     kick_kernel<<<stream_grid(c->n), 256, 0, c->stream>>>(
-        c->vx, c->vy, c->vz, c->ax, c->ay, c->az, c->q, c->m, c->status, c->t_inj, c->n, t_start, dt,
+        c->vx, c->vy, c->vz, c->ax, c->ay, c->az, c->qom, c->status, c->t_inj, c->n, t_start, dt,
         c->P.e_over_amu, c->P.efield[0], c->P.efield[1], c->P.efield[2], tb);
     SV_LAUNCHED(c);
     return SV_OK;

@@ -58,16 +58,30 @@ __global__ void bbox_partial(const double *__restrict__ x, const double *__restr
     }
 }
 
-// Final reduction; root = origin (bbox min), cube side S = smallest power of
-// two >= the largest extent (so every box side and every box-centre offset
-// S/2^l * k is exact in binary floating point), then the bbox max.
-__global__ void bbox_final(const double *__restrict__ part, int nblocks, double *__restrict__ root) {
+// Final reduction (kRedThreads threads over the block partials); root =
+// origin (bbox min), cube side S = smallest power of two >= the largest
+// extent (so every box side and every box-centre offset S/2^l * k is exact in
+// binary floating point), bbox max, empty flag, and 2^21 / S for the keys.
+__global__ void __launch_bounds__(kRedThreads) bbox_final(const double *__restrict__ part, int nblocks,
+                                                          double *__restrict__ root) {
     __shared__ double sh[6];
+    __shared__ double wsh[6][kRedThreads / 32];
+    double v[6] = {1e300, 1e300, 1e300, -1e300, -1e300, -1e300};
+    for (int k = threadIdx.x; k < nblocks; k += blockDim.x)
+        for (int d = 0; d < 6; d++) v[d] = d < 3 ? fmin(v[d], part[k * 6 + d]) : fmax(v[d], part[k * 6 + d]);
+    for (int d = 0; d < 6; d++)
+        for (int o = 16; o > 0; o >>= 1) {
+            const double u = __shfl_xor_sync(0xffffffffu, v[d], o);
+            v[d] = d < 3 ? fmin(v[d], u) : fmax(v[d], u);
+        }
+    if ((threadIdx.x & 31) == 0)
+        for (int d = 0; d < 6; d++) wsh[d][threadIdx.x >> 5] = v[d];
+    __syncthreads();
     if (threadIdx.x < 6) {
         const int d = threadIdx.x;
-        double v = d < 3 ? 1e300 : -1e300;
-        for (int k = 0; k < nblocks; k++) v = d < 3 ? fmin(v, part[k * 6 + d]) : fmax(v, part[k * 6 + d]);
-        sh[d] = v;
+        double r = d < 3 ? 1e300 : -1e300;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) r = d < 3 ? fmin(r, wsh[d][k]) : fmax(r, wsh[d][k]);
+        sh[d] = r;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -96,6 +110,7 @@ __global__ void bbox_final(const double *__restrict__ part, int nblocks, double 
         root[5] = sh[4];
         root[6] = sh[5];
         root[7] = empty ? 1.0 : 0.0;
+        root[8] = (double)(1u << kMortonBits) / S;
     }
 }
 
@@ -120,7 +135,7 @@ __global__ void morton_keys(const double *__restrict__ x, const double *__restri
         keys[i] = kInactiveKey;
         return;
     }
-    const double inv = (double)(1u << kMortonBits) / root[3];
+    const double inv = root[8];  // 2^21 / S, exact (S is a power of two)
     const double p[3] = {x[i] - root[0], y[i] - root[1], z[i] - root[2]};
     uint32_t c[3];
 #pragma unroll
@@ -136,8 +151,8 @@ __global__ void morton_keys(const double *__restrict__ x, const double *__restri
 __global__ void gather_sorted(const uint32_t *__restrict__ idx, int64_t n,
                               const double *__restrict__ x, const double *__restrict__ y,
                               const double *__restrict__ z, const double *__restrict__ q,
-                              const double *__restrict__ m, const int32_t *__restrict__ st,
-                              int64_t first, int64_t last, double kconst,
+                              const double *__restrict__ m, const double *__restrict__ qom,
+                              const int32_t *__restrict__ st, int64_t first, int64_t last, double kconst,
                               double *__restrict__ xs, double *__restrict__ ys,
                               double *__restrict__ zs, float *__restrict__ qs,
                               double *__restrict__ qm) {
@@ -150,7 +165,7 @@ __global__ void gather_sorted(const uint32_t *__restrict__ idx, int64_t n,
     const int32_t w = st[i];
     qs[s] = is_source(w) ? (float)q[i] : 0.0f;
     const bool tgt = (w == 1) && (int64_t)i >= first && (int64_t)i < last && m[i] > 0.0;
-    qm[s] = tgt ? kconst * q[i] / m[i] : 0.0;
+    qm[s] = tgt ? kconst * (qom ? qom[i] : q[i] / m[i]) : 0.0;
 }
 
 // sorted slots of image copies (index >= n_orig) are sources only and have
@@ -199,7 +214,7 @@ sv_status ensure_sorted_capacity(sv_ctx *c, int64_t n) {
     SV_CK(c, cudaMalloc(&S.cub_tmp, bytes));
     S.red_blocks = 2 * kNumSMs;
     SV_CK(c, cudaMalloc(&S.red, (size_t)S.red_blocks * 6 * sizeof(double)));
-    SV_CK(c, cudaMalloc(&S.root, 8 * sizeof(double)));
+    SV_CK(c, cudaMalloc(&S.root, 16 * sizeof(double)));
     S.cap = cap;
     return SV_OK;
 }
@@ -213,7 +228,7 @@ sv_status sort_view(sv_ctx *c, const ParticleView &v, int64_t first, int64_t las
     const int nb = div_up(n, 256);
     bbox_partial<<<S.red_blocks, kRedThreads, 0, c->stream>>>(v.x, v.y, v.z, v.status, n, S.red);
     SV_LAUNCHED(c);
-    bbox_final<<<1, 32, 0, c->stream>>>(S.red, S.red_blocks, S.root);
+    bbox_final<<<1, kRedThreads, 0, c->stream>>>(S.red, S.red_blocks, S.root);
     SV_LAUNCHED(c);
     morton_keys<<<nb, 256, 0, c->stream>>>(v.x, v.y, v.z, v.status, n, S.root, S.keys, S.idx);
     SV_LAUNCHED(c);
@@ -229,14 +244,14 @@ sv_status sort_view(sv_ctx *c, const ParticleView &v, int64_t first, int64_t las
     if (vb.Current() != S.idx) {
         std::swap(S.idx, S.idx_alt);
     }
-    gather_sorted<<<nb, 256, 0, c->stream>>>(S.idx, n, v.x, v.y, v.z, v.q, v.m, v.status, first,
+    gather_sorted<<<nb, 256, 0, c->stream>>>(S.idx, n, v.x, v.y, v.z, v.q, v.m, v.qom, v.status, first,
                                              std::min(last, v.n_orig), c->P.k_const, S.x, S.y, S.z, S.q, S.qm);
     SV_LAUNCHED(c);
     return SV_OK;
 }
 
 sv_status sort_state(sv_ctx *c, int64_t first, int64_t last) {
-    const ParticleView v{c->x, c->y, c->z, c->q, c->m, c->status, c->n, c->n};
+    const ParticleView v{c->x, c->y, c->z, c->q, c->m, c->status, c->n, c->n, c->qom};
     return sort_view(c, v, first, last);
 }
 

@@ -34,7 +34,7 @@ struct Sorted {
     double *ax = nullptr, *ay = nullptr, *az = nullptr;  // acceleration, sorted order
     void *cub_tmp = nullptr;
     size_t cub_bytes = 0;
-    double *root = nullptr;    // device [8]: origin xyz, cube side S, bbox max xyz, spare
+    double *root = nullptr;    // device [16]: origin xyz, cube side S, bbox max xyz, empty flag, 2^21/S
     double *red = nullptr;     // device reduction scratch
     int red_blocks = 0;
     int64_t cap = 0;
@@ -48,6 +48,7 @@ struct ParticleView {
     const double *x, *y, *z, *q, *m;
     const int32_t *status;
     int64_t n, n_orig;
+    const double *qom = nullptr;  // q/m per particle (0 for m <= 0), or null: divide on the fly
 };
 
 struct Fmm;   // fmm.cu
@@ -68,6 +69,7 @@ struct sv_ctx {
     double *x = nullptr, *y = nullptr, *z = nullptr;
     double *vx = nullptr, *vy = nullptr, *vz = nullptr;
     double *q = nullptr, *m = nullptr, *t_inj = nullptr;
+    double *qom = nullptr;  // q/m (0 where m <= 0), set at upload: no FP64 division per step
     int32_t *status = nullptr;
     // last acceleration (force only), caller order, FP64
     double *ax = nullptr, *ay = nullptr, *az = nullptr;
