@@ -158,8 +158,85 @@ SV_API sv_status sv_add_accel_ref32(sv_ctx *ctx, float *acc4);
 /* nsteps of LeapfrogDKD (integration_schemes.cpp:856-891): drift dt/2,
  * kick dt (force + uniform field), drift dt/2, with the reference's
  * injection-time clamps (particles.cpp:693-786).  t0 is the time at the start
- * of the first step. */
+ * of the first step.  Injection window (LeapfrogDKD::driftNew,
+ * integration_schemes.cpp:705-723, and ChargedParticles::findMostRecentInjected,
+ * particles.cpp:1328-1366): a half-step drift over [t, t + dt/2] acts on the
+ * particles with t_inj <= t + dt/2, and the force and kick of a step act on the
+ * particles with t_inj <= its mid time, as sources and as targets; particles
+ * injected later keep their state.  With t_inj ascending in index order (the
+ * reference's precondition) this is the reference's [firstParticle,
+ * lastParticle) window.  The boundary set by sv_set_boundary is applied after
+ * every drift. */
 SV_API sv_status sv_leapfrog(sv_ctx *ctx, int32_t nsteps, double dt, double t0);
+
+/* Crash and boundary conditions of the drift, as ParticleSystem::
+ * propagatePositionNew (particles.cpp:33-40) applies them for every particle
+ * in the injection window:
+ * 1. crash (CrashParameters::checkExtractorGridCrash, structures.h:467-517,
+ *    called from ChargedParticles::propagatePositionNew, particles.cpp:
+ *    693-739): the segment of a status 1 or 2 particle's drift, in the (r, z)
+ *    plane, against the extractor grid (the ring r >= crash_r between z =
+ *    crash_z and crash_z + crash_width): on a hit the status becomes -1
+ *    (crashed), z the hit's z, and x, y follow the straight path to that z;
+ * 2. folding when fold != 0 (enforceSymmetryConditions, particles.cpp:
+ *    199-333), of every particle in the window whatever its status: with the
+ *    rotational symmetry into the first quadrant (positions and velocities),
+ *    with the translational one into [-L/2, L/2) on each periodic axis;
+ * 3. boundary conditions (enforceBoundaryConditions, particles.cpp:73-177) on
+ *    inbound particles: spatial, |x| > bc_space[0], |y| > bc_space[1],
+ *    |z| > bc_space[2] or sqrt(x^2 + y^2) > bc_space[3] (a zero limit is off),
+ *    then temporal, t - t_inj > bc_time; either sets the status to 0 (out of
+ *    bounds).
+ * Every crash and boundary hit records an sv_event. */
+typedef enum {
+    SV_CRASH_NONE = 0,            /* CrashConditionOptions::none */
+    SV_CRASH_EXTRACTOR_GRID = 1   /* CrashConditionOptions::extractorGrid */
+} sv_crash_kind;
+
+typedef enum {
+    SV_BC_NONE = 0,               /* BoundaryConditionOptions::none */
+    SV_BC_SPACE = 1,              /* ::space */
+    SV_BC_TIME = 2,               /* ::time */
+    SV_BC_SPACE_AND_TIME = 3      /* ::space_and_time */
+} sv_bc_kind;
+
+typedef struct {
+    int32_t crash;          /* sv_crash_kind */
+    int32_t bc;             /* sv_bc_kind */
+    double crash_z;         /* z_distance: bottom of the grid (m) */
+    double crash_width;     /* z_width: thickness of the grid (m) */
+    double crash_r;         /* r_distance: inner radius of the grid (m) */
+    double bc_space[4];     /* spatialBoundaryConditions x, y, z, w (m; 0 = off) */
+    double bc_time;         /* temporalBoundaryCondition (s) */
+    int32_t fold;           /* 1: fold into the symmetry domain of the context's symmetry */
+    int32_t reserved[7];
+} sv_boundary;
+
+/* Default: no crash, no boundary conditions, no folding. */
+SV_API sv_status sv_set_boundary(sv_ctx *ctx, const sv_boundary *b);
+SV_API sv_status sv_get_boundary(const sv_ctx *ctx, sv_boundary *b);
+
+/* One crash or boundary event: the 40-byte record that
+ * ChargedParticles::writeToEventsFile (particles.cpp:666-684) appends to the
+ * events file, field for field (time of the event; position and velocity
+ * after the event; particle index; species code; status after the event,
+ * -1 crashed or 0 out of bounds, written as its 32-bit pattern). */
+typedef struct {
+    float time;
+    float x, y, z;
+    float vx, vy, vz;
+    int32_t index;
+    uint32_t species;       /* velocity.w of the reference (0xffffffff: mass not in the species table) */
+    int32_t status;
+} sv_event;
+
+/* Events recorded since the last call, in the reference's file order (by
+ * drift, then crashes before spatial before temporal hits, then particle
+ * index).  out may be null to query the count; otherwise up to cap records are
+ * copied and all recorded events are released.  A context keeps up to
+ * max(65536, n) events between calls; events past that are dropped, and the
+ * next call returns SV_ERR_CAPACITY with count = events recorded + dropped. */
+SV_API sv_status sv_get_events(sv_ctx *ctx, sv_event *out, int64_t cap, int64_t *count);
 
 /* Adjoint of sv_leapfrog with the direct sum (no reference counterpart: the
  * reference integrates forward only).  sv_adjoint_forward runs nsteps like

@@ -53,6 +53,10 @@ def lib():
         L.orc_leapfrog_f64.argtypes = [C.c_int64, _f64p, _f64p, _f64p, _f64p, _i32p, _f64p, C.c_int,
                                        C.c_double, C.c_double, C.c_double, C.c_double, _f64p, C.c_int,
                                        C.c_int, C.c_void_p, C.c_void_p, C.c_int]
+        L.orc_leapfrog_ref32_bc.argtypes = L.orc_leapfrog_ref32.argtypes[:-1] + [
+            C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_int]
+        L.orc_leapfrog_f64_bc.argtypes = L.orc_leapfrog_f64.argtypes[:-2] + [
+            C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_int]
         L.orc_energy_f64.argtypes = [C.c_int64, _f64p, _f64p, _f64p, _f64p, C.c_double,
                                      C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int]
         L.orc_rel_l2.argtypes = [C.c_int64, _f64p, _f64p, C.c_void_p, C.POINTER(C.c_double),
@@ -156,6 +160,71 @@ def leapfrog_f64(state, nsteps, dt, eps2, efield=(0.0, 0.0, 0.0), t0=0.0, sym=0,
                            k_const(), np.asarray(efield, np.float64), sym, nimg, _ptr(io), _ptr(a),
                            threads)
     return x.reshape(n, 3), v.reshape(n, 3), a.reshape(n, 3)
+
+
+class Boundary(C.Structure):
+    """orc_boundary: crash test, folding and boundary conditions of the drift."""
+    _fields_ = [("crash", C.c_int), ("bc", C.c_int), ("fold", C.c_int), ("axes", C.c_int * 3),
+                ("crash_z", C.c_double), ("crash_width", C.c_double), ("crash_r", C.c_double),
+                ("bc_space", C.c_double * 4), ("bc_time", C.c_double), ("domain", C.c_double * 3)]
+
+
+# the events-file record (ChargedParticles::writeToEventsFile, particles.cpp:666-684)
+EVENT_DTYPE = np.dtype([("time", "<f4"), ("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("vx", "<f4"), ("vy", "<f4"),
+                        ("vz", "<f4"), ("index", "<i4"), ("species", "<u4"), ("status", "<i4")])
+
+
+def boundary(crash=0, crash_z=0.0, crash_width=0.0, crash_r=0.0, bc=0, bc_space=(0, 0, 0, 0), bc_time=0.0,
+             fold=0, axes=(0, 0, 0), domain=(0.0, 0.0, 0.0)):
+    b = Boundary()
+    b.crash, b.bc, b.fold = crash, bc, fold
+    b.crash_z, b.crash_width, b.crash_r, b.bc_time = crash_z, crash_width, crash_r, bc_time
+    for k in range(3):
+        b.axes[k] = axes[k]
+        b.domain[k] = domain[k]
+    for k in range(4):
+        b.bc_space[k] = bc_space[k]
+    return b
+
+
+def leapfrog_ref32_bc(pos4, vel4, acc4, t_inj, nsteps, dt, eps, efield=(0.0, 0.0, 0.0), sym=0, bd=None,
+                      images=None, domain_size=(2e-6, 2e-6, 0.0), threads=0, ev_cap=1 << 16):
+    """The reference's loop with its injection window, crash test, folding and
+    boundary conditions: (pos4, vel4, acc4, events)."""
+    p = np.ascontiguousarray(pos4, np.float32).copy()
+    v = np.ascontiguousarray(vel4, np.float32).copy()
+    a = np.ascontiguousarray(acc4, np.float32).copy()
+    t = np.ascontiguousarray(t_inj, np.float32)
+    e = np.asarray(efield, np.float32)
+    img = None if images is None else np.ascontiguousarray(images, np.int32).reshape(-1)
+    nimg = 0 if img is None else img.size // 3
+    ev = np.zeros(ev_cap, EVENT_DTYPE)
+    cnt = C.c_int()
+    lib().orc_leapfrog_ref32_bc(p.shape[0], p, v, a, t, nsteps, dt, eps, e, sym, nimg, _ptr(img),
+                                np.asarray(domain_size, np.float32), None if bd is None else C.byref(bd),
+                                ev.ctypes.data, ev_cap, C.byref(cnt), threads)
+    return p, v, a, ev[:min(cnt.value, ev_cap)].copy()
+
+
+def leapfrog_f64_bc(state, nsteps, dt, eps2, efield=(0.0, 0.0, 0.0), t0=0.0, sym=0, img_off=None, bd=None,
+                    threads=0, ev_cap=1 << 16):
+    """FP64 DKD with the window, crash, folding and boundary conditions:
+    (x, v, status, events)."""
+    x = np.ascontiguousarray(state["x"], np.float64).reshape(-1).copy()
+    v = np.ascontiguousarray(state["v"], np.float64).reshape(-1).copy()
+    n = x.size // 3
+    st = np.ascontiguousarray(state["status"], np.int32).copy()
+    io = None if img_off is None else np.ascontiguousarray(img_off, np.float64).reshape(-1)
+    nimg = 0 if io is None else io.size // 3
+    ev = np.zeros(ev_cap, EVENT_DTYPE)
+    cnt = C.c_int()
+    lib().orc_leapfrog_f64_bc(n, x, v, np.ascontiguousarray(state["q"], np.float64),
+                              np.ascontiguousarray(state["m"], np.float64), st,
+                              np.ascontiguousarray(state["t_inj"], np.float64), nsteps, dt, t0, eps2,
+                              k_const(), np.asarray(efield, np.float64), sym, nimg, _ptr(io),
+                              None if bd is None else C.byref(bd), ev.ctypes.data, ev_cap, C.byref(cnt),
+                              threads)
+    return x.reshape(n, 3), v.reshape(n, 3), st, ev[:min(cnt.value, ev_cap)].copy()
 
 
 def energy_f64(state, eps2, threads=0):

@@ -13,9 +13,15 @@
 //           DomainBoundsFunction::isOutlier)
 //   keys : threads, sym (0 none, 1 rotational, 2 translational), levels,
 //          axes (e.g. 110), dom (domain size x,y,z in metres), theta, p,
-//          maxlevel, steps, dt, ez
+//          maxlevel, steps, dt, ez;
+//          dkd only: crash (1 extractor grid), cz, cw, cr (z_distance,
+//          z_width, r_distance), bc (BoundaryConditionOptions 0..3), bx, by,
+//          bz, br (spatial limits), bt (temporal limit), events (1: append the
+//          events file)
 // in.bin : int32 n, float pos4[4n], float vel4[4n], float acc4[4n], float tinj[n]
 // out.bin: float pos4[4n], float vel4[4n], float acc4[4n]
+//          (dkd with events=1: then int32 count, count 40-byte event records
+//          as ChargedParticles::writeToEventsFile wrote them)
 //          (grid mode: int32 count, int32 points[3*count] in the Grid's order)
 #include "force_calculation_methods.h"
 
@@ -147,24 +153,56 @@ int main(int argc, char **argv) {
     fm->setLastParticle(n);
     fm->setGrid(&grid);
 
+    FILE *events = nullptr;
     if (mode == "dkd") {
         // LeapfrogDKD::runSimulation step structure (integration_schemes.cpp:
-        // 867-888) on the reference's own propagate*New methods; the uniform
-        // background field is added as computeBackgroundAcceleration adds the
-        // interpolated one (particles.cpp:496-520).
+        // 867-888) with driftNew's injection window (:705-723) on the
+        // reference's own methods: findMostRecentInjected, ParticleSystem::
+        // propagatePositionNew (drift with the crash test, symmetry folding,
+        // boundary conditions), resetFirstChargedParticle and
+        // propagateVelocityNew.  The uniform background field is added as
+        // computeBackgroundAcceleration adds the interpolated one
+        // (particles.cpp:496-520), over the same window.
         const int steps = (int)getd(kv, "steps", 1);
         const float dt = (float)getd(kv, "dt", 1e-13);
         const float ez = (float)getd(kv, "ez", 0.0);
+        CrashParameters &cr = ps.params.crashParameters;
+        cr.crashOptions = getd(kv, "crash", 0) != 0 ? CrashConditionOptions::extractorGrid
+                                                     : CrashConditionOptions::none;
+        cr.z_distance = (float)getd(kv, "cz", 0.0);
+        cr.z_width = (float)getd(kv, "cw", 0.0);
+        cr.r_distance = (float)getd(kv, "cr", 0.0);
+        BoundaryConditionParameters &bc = ps.params.boundaryConditions;
+        const int bck = (int)getd(kv, "bc", 0);
+        bc.boundaryConditionType = bck == 1 ? BoundaryConditionOptions::space
+                                 : bck == 2 ? BoundaryConditionOptions::time
+                                 : bck == 3 ? BoundaryConditionOptions::space_and_time
+                                            : BoundaryConditionOptions::none;
+        bc.spatialBoundaryConditions = vec4<float>((float)getd(kv, "bx", 0.0), (float)getd(kv, "by", 0.0),
+                                                   (float)getd(kv, "bz", 0.0), (float)getd(kv, "br", 0.0));
+        bc.temporalBoundaryCondition = (float)getd(kv, "bt", 0.0);
+        events = std::tmpfile();
+        if (!events) return 3;
+        ps.params.eventsFile = events;
         const float inbound = 1.0f;
         const double factor = PhysicalConstant::ELEM_CHARGE / PhysicalConstant::AMU;
+        auto drift_new = [&](float tstart, float h) {
+            const int last = cp.findMostRecentInjected(tstart + h) + 1;
+            cp.lastParticle = last;
+            fm->setLastParticle(last);
+            ps.propagatePositionNew(tstart, h);
+            ps.resetFirstChargedParticle();
+            fm->setFirstParticle(cp.firstParticle);
+        };
+        cp.lastParticle = 0;
         for (int it = 1; it <= steps; it++) {
             float tpos = dt * (it - 1);
             float tvel = dt * (it - 1);
-            cp.propagatePositionNew(tpos, dt / 2, ps.params.crashParameters, nullptr);
+            drift_new(tpos, dt / 2);
             tpos += dt / 2;
             cp.zeroAcceleration();
             fm->updateAcceleration();
-            for (int i = 0; i < n; i++) {
+            for (int i = cp.firstParticle; i < cp.lastParticle; i++) {
                 if (cp.acceleration[i].w != inbound) continue;
                 float efactor = factor * cp.position[i].w / cp.getMass(i);
                 vec3<float> e(0.0f, 0.0f, ez);
@@ -173,8 +211,8 @@ int main(int argc, char **argv) {
                 cp.acceleration[i].y += e.y;
                 cp.acceleration[i].z += e.z;
             }
-            cp.propagateVelocityNew(tvel, dt);
-            cp.propagatePositionNew(tpos, dt / 2, ps.params.crashParameters, nullptr);
+            ps.propagateVelocityNew(tvel, dt);
+            drift_new(tpos, dt / 2);
         }
     } else {
         fm->updateAcceleration();
@@ -185,6 +223,16 @@ int main(int argc, char **argv) {
     std::fwrite(cp.position, 16, n, fo);
     std::fwrite(cp.velocity, 16, n, fo);
     std::fwrite(cp.acceleration, 16, n, fo);
+    if (events && getd(kv, "events", 0) != 0) {
+        std::fflush(events);
+        const long bytes = std::ftell(events);
+        const int32_t cnt = (int32_t)(bytes / 40);
+        std::fwrite(&cnt, 4, 1, fo);
+        std::rewind(events);
+        std::vector<char> buf((size_t)bytes);
+        if (bytes > 0 && std::fread(buf.data(), 1, (size_t)bytes, events) != (size_t)bytes) return 5;
+        if (bytes > 0) std::fwrite(buf.data(), 1, (size_t)bytes, fo);
+    }
     std::fclose(fo);
     // SimulationParameters' destructor releases members the headless set-up
     // never initialised (file handles, storage arrays); leave without running

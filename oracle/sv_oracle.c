@@ -426,47 +426,242 @@ static float clampf_dt(float v, float dt) {
     return dt < a ? dt : a;
 }
 
-static void drift_ref32(int n, float *pos4, const float *vel4, const float *acc4,
-                        const float *t_inj, float tstart, float dt) {
-    /* ChargedParticles::propagatePositionNew (particles.cpp:693-739), crash
-     * checks disabled (CrashConditionOptions::none). */
+/* std::max / std::min as the reference calls them */
+static float ref_maxf(float a, float b) { return a < b ? b : a; }
+static float ref_minf(float a, float b) { return b < a ? b : a; }
+static double ref_max(double a, double b) { return a < b ? b : a; }
+static double ref_min(double a, double b) { return b < a ? b : a; }
+
+/* CrashParameters::checkExtractorGridCrash (structures.h:467-517), FP32:
+ * returns 1 on a crash with *fz the crossing's z. */
+static int crash_ref32(const orc_boundary *bd, float ix, float iy, float iz, float fx, float fy, float fz0,
+                       float *fz) {
+    const float zd = (float)bd->crash_z, zw = (float)bd->crash_width, rd = (float)bd->crash_r;
+    float initial_r = sqrtf(ix * ix + iy * iy);
+    float final_r = sqrtf(fx * fx + fy * fy);
+    float m = (fz0 - iz) / (final_r - initial_r);
+    float b = iz - m * initial_r;
+    float min_r = ref_minf(initial_r, final_r), max_r = ref_maxf(initial_r, final_r);
+    float min_z = ref_minf(iz, fz0), max_z = ref_maxf(iz, fz0);
+    float temp_r, temp_z;
+    if (zd >= min_z && zd <= max_z) {
+        temp_r = (zd - b) / m;
+        if (temp_r >= ref_maxf(min_r, rd) && temp_r <= max_r) {
+            *fz = zd;
+            return 1;
+        }
+    }
+    if (zd + zw >= min_z && zd + zw <= max_z) {
+        temp_r = (zd + zw - b) / m;
+        if (temp_r >= ref_maxf(min_r, rd) && temp_r <= max_r) {
+            *fz = zd + zw;
+            return 1;
+        }
+    }
+    if (rd >= min_r && rd <= max_r) {
+        temp_z = m * rd + b;
+        if (temp_z >= ref_maxf(min_z, zd) && temp_z <= ref_minf(max_z, zd + zw)) {
+            *fz = temp_z;
+            return 1;
+        }
+    }
+    return 0;
+}
+
+static int crash_f64(const orc_boundary *bd, double ix, double iy, double iz, double fx, double fy, double fz0,
+                     double *fz) {
+    const double zd = bd->crash_z, zw = bd->crash_width, rd = bd->crash_r;
+    const double ri = sqrt(ix * ix + iy * iy), rf = sqrt(fx * fx + fy * fy);
+    const double m = (fz0 - iz) / (rf - ri), b = iz - m * ri;
+    const double rmin = ref_min(ri, rf), rmax = ref_max(ri, rf);
+    const double zmin = ref_min(iz, fz0), zmax = ref_max(iz, fz0);
+    if (zd >= zmin && zd <= zmax) {
+        const double tr = (zd - b) / m;
+        if (tr >= ref_max(rmin, rd) && tr <= rmax) {
+            *fz = zd;
+            return 1;
+        }
+    }
+    if (zd + zw >= zmin && zd + zw <= zmax) {
+        const double tr = (zd + zw - b) / m;
+        if (tr >= ref_max(rmin, rd) && tr <= rmax) {
+            *fz = zd + zw;
+            return 1;
+        }
+    }
+    if (rd >= rmin && rd <= rmax) {
+        const double tz = m * rd + b;
+        if (tz >= ref_max(zmin, zd) && tz <= ref_min(zmax, zd + zw)) {
+            *fz = tz;
+            return 1;
+        }
+    }
+    return 0;
+}
+
+static void push_event(orc_event *ev, int ev_cap, int *ev_count, float t, float x, float y, float z, float vx,
+                       float vy, float vz, int index, uint32_t species, int32_t status) {
+    if (ev && *ev_count < ev_cap) {
+        orc_event *e = &ev[*ev_count];
+        e->time = t;
+        e->x = x; e->y = y; e->z = z;
+        e->vx = vx; e->vy = vy; e->vz = vz;
+        e->index = index;
+        e->species = species;
+        e->status = status;
+    }
+    (*ev_count)++;
+}
+
+/* ChargedParticles::findMostRecentInjected (particles.cpp:1328-1359) */
+static int most_recent_injected(int n, const float *t_inj, float time) {
+    int max_i = n - 1, min_i = 0, t;
+    do {
+        t = (max_i + min_i) / 2;
+        if (t_inj[t] <= time)
+            min_i = t + 1;
+        else if (t_inj[t] > time)
+            max_i = t - 1;
+    } while (max_i > min_i);
+    t = max_i;
+    if (t_inj[t] > time) t--;
+    return t;
+}
+
+/* ParticleSystem::translateToSymmetryDomain, one axis (particles.cpp:278-333), FP32 */
+static float wrap_ref32(float p, float L) {
+    float temp = p + L / 2;
+    if (temp >= 0) return fmodf(temp, L) - L / 2;
+    temp = fmodf(temp, L);
+    return temp < 0 ? temp + L / 2 : temp - L / 2;
+}
+
+static double wrap_f64(double p, double L) {
+    double temp = p + L / 2;
+    if (temp >= 0) return fmod(temp, L) - L / 2;
+    temp = fmod(temp, L);
+    return temp < 0 ? temp + L / 2 : temp - L / 2;
+}
+
+/* ParticleSystem::propagatePositionNew (particles.cpp:33-40) for the charged
+ * particles of [first, last), FP32: drift with the crash test
+ * (particles.cpp:693-739), symmetry folding (particles.cpp:199-333; sym 1
+ * rotational, 2 translational), boundary conditions (particles.cpp:73-177). */
+static void drift_ref32(int first, int last, float *pos4, float *vel4, float *acc4, const float *t_inj,
+                        float tstart, float dt, int sym, const float domain[3], const orc_boundary *bd,
+                        orc_event *ev, int ev_cap, int *ev_count) {
     const float tend = tstart + dt;
-    for (int i = 0; i < n; i++) {
+    for (int i = first; i < last; i++) {
         float w = acc4[4 * i + 3];
         if (!(w == 1.0f || w == 2.0f)) continue;
+        float *p = &pos4[4 * i];
+        const float *v = &vel4[4 * i];
+        const float ix = p[0], iy = p[1], iz = p[2];
         float s = clampf_dt(tend - t_inj[i], dt);
-        pos4[4 * i + 0] += vel4[4 * i + 0] * s;
-        pos4[4 * i + 1] += vel4[4 * i + 1] * s;
-        pos4[4 * i + 2] += vel4[4 * i + 2] * s;
+        p[0] += v[0] * s;
+        p[1] += v[1] * s;
+        p[2] += v[2] * s;
+        float fz;
+        if (bd && bd->crash && crash_ref32(bd, ix, iy, iz, p[0], p[1], p[2], &fz)) {
+            acc4[4 * i + 3] = -1.0f;
+            p[2] = fz;
+            float temp_dt = (fz - iz) / v[2];
+            p[0] = ix + temp_dt * v[0];
+            p[1] = iy + temp_dt * v[1];
+            push_event(ev, ev_cap, ev_count, tstart + temp_dt, p[0], p[1], p[2], v[0], v[1], v[2], i,
+                       (uint32_t)(int)vel4[4 * i + 3], -1);
+        }
+    }
+    if (sym == 1) {
+        for (int i = first; i < last; i++) {
+            float *p = &pos4[4 * i], *v = &vel4[4 * i];
+            float tx, ty;
+            if (p[0] < 0 && p[1] < 0) {
+                p[0] = -p[0]; p[1] = -p[1]; v[0] = -v[0]; v[1] = -v[1];
+            } else if (p[0] < 0) {
+                tx = p[1]; ty = -p[0]; p[0] = tx; p[1] = ty;
+                tx = v[1]; ty = -v[0]; v[0] = tx; v[1] = ty;
+            } else if (p[1] < 0) {
+                tx = -p[1]; ty = p[0]; p[0] = tx; p[1] = ty;
+                tx = -v[1]; ty = v[0]; v[0] = tx; v[1] = ty;
+            }
+        }
+    } else if (sym == 2 && bd) {
+        for (int i = first; i < last; i++)
+            for (int d = 0; d < 3; d++)
+                if (bd->axes[d]) pos4[4 * i + d] = wrap_ref32(pos4[4 * i + d], domain[d]);
+    }
+    if (!bd) return;
+    const float now = tstart + dt;
+    if (bd->bc == 1 || bd->bc == 3) {
+        const float X = (float)bd->bc_space[0], Y = (float)bd->bc_space[1], Z = (float)bd->bc_space[2],
+                    W = (float)bd->bc_space[3];
+        for (int i = first; i < last; i++) {
+            if (acc4[4 * i + 3] != 1.0f) continue;
+            const float x = pos4[4 * i], y = pos4[4 * i + 1], z = pos4[4 * i + 2];
+            int out = (X != 0 && fabsf(x) > X) || (Y != 0 && fabsf(y) > Y) || (Z != 0 && fabsf(z) > Z) ||
+                      (W != 0 && sqrtf(x * x + y * y) > W);
+            if (out) {
+                acc4[4 * i + 3] = 0.0f;
+                push_event(ev, ev_cap, ev_count, now, x, y, z, vel4[4 * i], vel4[4 * i + 1], vel4[4 * i + 2], i,
+                           (uint32_t)(int)vel4[4 * i + 3], 0);
+            }
+        }
+    }
+    if (bd->bc == 2 || bd->bc == 3) {
+        const float T = (float)bd->bc_time;
+        for (int i = first; i < last; i++) {
+            if (acc4[4 * i + 3] != 1.0f) continue;
+            if (now - t_inj[i] > T) {
+                acc4[4 * i + 3] = 0.0f;
+                push_event(ev, ev_cap, ev_count, now, pos4[4 * i], pos4[4 * i + 1], pos4[4 * i + 2], vel4[4 * i],
+                           vel4[4 * i + 1], vel4[4 * i + 2], i, (uint32_t)(int)vel4[4 * i + 3], 0);
+            }
+        }
     }
 }
 
-void orc_leapfrog_ref32(int n, float *pos4, float *vel4, float *acc4,
-                        const float *t_inj, int nsteps, float dt, double eps,
-                        const float efield[3], int sym, int nimg,
-                        const int *images, const float domain_size[3],
-                        int nthreads) {
+/* ParticleSystem::resetFirstChargedParticle (particles.cpp:179-193) */
+static int reset_first(int first, int last, const float *acc4) {
+    for (int i = first; i < last; i++) {
+        const float w = acc4[4 * i + 3];
+        if (w == 2.0f || w == 1.0f) return i;
+    }
+    return first;
+}
+
+void orc_leapfrog_ref32_bc(int n, float *pos4, float *vel4, float *acc4,
+                           const float *t_inj, int nsteps, float dt, double eps,
+                           const float efield[3], int sym, int nimg,
+                           const int *images, const float domain_size[3],
+                           const orc_boundary *bd, orc_event *ev, int ev_cap,
+                           int *ev_count, int nthreads) {
     /* LeapfrogDKD::runSimulation (integration_schemes.cpp:856-891):
-     * driftNew(dt/2), kick(dt), driftNew(dt/2) per step. */
+     * driftNew(dt/2), kick(dt), driftNew(dt/2) per step; driftNew
+     * (integration_schemes.cpp:705-723) sets lastParticle from the injection
+     * times, drifts, then moves firstParticle past inactive particles. */
     const float factor = REF_ELEM_CHARGE / REF_AMU;
+    int first = 0, last = 0, cnt = 0;
     for (int it = 1; it <= nsteps; it++) {
         float tpos = dt * (float)(it - 1);
         float tvel = dt * (float)(it - 1);
-        drift_ref32(n, pos4, vel4, acc4, t_inj, tpos, dt / 2);
+        last = most_recent_injected(n, t_inj, tpos + dt / 2) + 1;
+        drift_ref32(first, last, pos4, vel4, acc4, t_inj, tpos, dt / 2, sym, domain_size, bd, ev, ev_cap, &cnt);
+        first = reset_first(first, last, acc4);
         tpos += dt / 2;
         /* kick: zeroAcceleration (particles.cpp:1031-1044) + force */
-        for (int i = 0; i < n; i++)
+        for (int i = first; i < last; i++)
             if (acc4[4 * i + 3] == 1.0f) acc4[4 * i] = acc4[4 * i + 1] = acc4[4 * i + 2] = 0.0f;
         if (sym == 0)
-            orc_direct_ref32(pos4, vel4, acc4, 0, n, 0, n, eps, nthreads);
+            orc_direct_ref32(pos4, vel4, acc4, first, last, first, last, eps, nthreads);
         else if (sym == 1)
-            orc_direct_rot4_ref32(pos4, vel4, acc4, 0, n, 0, n, eps, nthreads);
+            orc_direct_rot4_ref32(pos4, vel4, acc4, first, last, first, last, eps, nthreads);
         else
-            orc_direct_trans_ref32(pos4, vel4, acc4, 0, n, 0, n, eps, nimg, images,
+            orc_direct_trans_ref32(pos4, vel4, acc4, first, last, first, last, eps, nimg, images,
                                    domain_size, nthreads);
         /* computeBackgroundAcceleration with a uniform field
          * (particles.cpp:496-520): Efactor in float, E*Efactor per axis. */
-        for (int i = 0; i < n; i++) {
+        for (int i = first; i < last; i++) {
             if (acc4[4 * i + 3] != 1.0f) continue;
             long double m = species_mass_ld((int)vel4[4 * i + 3]);
             float ef = (float)((double)factor * (double)pos4[4 * i + 3] / m);
@@ -478,7 +673,7 @@ void orc_leapfrog_ref32(int n, float *pos4, float *vel4, float *acc4,
         /* propagateVelocityNew (particles.cpp:763-786) */
         {
             const float tend = tvel + dt;
-            for (int i = 0; i < n; i++) {
+            for (int i = first; i < last; i++) {
                 if (acc4[4 * i + 3] != 1.0f) continue;
                 float s = clampf_dt(tend - t_inj[i], dt);
                 vel4[4 * i + 0] += acc4[4 * i + 0] * s;
@@ -486,8 +681,138 @@ void orc_leapfrog_ref32(int n, float *pos4, float *vel4, float *acc4,
                 vel4[4 * i + 2] += acc4[4 * i + 2] * s;
             }
         }
-        drift_ref32(n, pos4, vel4, acc4, t_inj, tpos, dt / 2);
+        last = most_recent_injected(n, t_inj, tpos + dt / 2) + 1;
+        drift_ref32(first, last, pos4, vel4, acc4, t_inj, tpos, dt / 2, sym, domain_size, bd, ev, ev_cap, &cnt);
+        first = reset_first(first, last, acc4);
     }
+    if (ev_count) *ev_count = cnt;
+}
+
+void orc_leapfrog_ref32(int n, float *pos4, float *vel4, float *acc4,
+                        const float *t_inj, int nsteps, float dt, double eps,
+                        const float efield[3], int sym, int nimg,
+                        const int *images, const float domain_size[3],
+                        int nthreads) {
+    orc_leapfrog_ref32_bc(n, pos4, vel4, acc4, t_inj, nsteps, dt, eps, efield, sym, nimg, images, domain_size,
+                          NULL, NULL, 0, NULL, nthreads);
+}
+
+static uint32_t species_of_mass(double m) {
+    for (int k = 0; k < 8; k++)
+        if (k != 3 && m == (double)species_mass_ld(k)) return (uint32_t)k;
+    return 0xffffffffu;
+}
+
+/* Events of one drift in the reference's file order: crashes (drift loop),
+ * then spatial, then temporal boundary hits, each in index order. */
+static void drift_f64(int64_t n, double *x, double *v, const double *m, int32_t *status, const double *t_inj,
+                      double t_start, double h, const orc_boundary *bd, orc_event *ev, int ev_cap, int *cnt) {
+    const double T = t_start + h;
+    int fold = bd ? bd->fold : 0;
+    for (int64_t i = 0; i < n; i++) {
+        if (!(t_inj[i] <= T)) continue;
+        if (!(status[i] == 1 || status[i] == 2)) continue;
+        double *p = &x[3 * i];
+        const double *u = &v[3 * i];
+        const double ix = p[0], iy = p[1], iz = p[2];
+        double s = T - t_inj[i];
+        s = s < 0 ? 0 : (s > h ? h : s);
+        for (int d = 0; d < 3; d++) p[d] += u[d] * s;
+        double zc;
+        if (bd && bd->crash && crash_f64(bd, ix, iy, iz, p[0], p[1], p[2], &zc)) {
+            status[i] = -1;
+            p[2] = zc;
+            const double td = (zc - iz) / u[2];
+            p[0] = ix + td * u[0];
+            p[1] = iy + td * u[1];
+            push_event(ev, ev_cap, cnt, (float)(t_start + td), (float)p[0], (float)p[1], (float)p[2], (float)u[0],
+                       (float)u[1], (float)u[2], (int)i, species_of_mass(m[i]), -1);
+        }
+    }
+    for (int64_t i = 0; i < n && fold; i++) {
+        if (!(t_inj[i] <= T)) continue;
+        double *p = &x[3 * i], *u = &v[3 * i];
+        if (fold == 1) {
+            double tx, ty;
+            if (p[0] < 0 && p[1] < 0) {
+                p[0] = -p[0]; p[1] = -p[1]; u[0] = -u[0]; u[1] = -u[1];
+            } else if (p[0] < 0) {
+                tx = p[1]; ty = -p[0]; p[0] = tx; p[1] = ty;
+                tx = u[1]; ty = -u[0]; u[0] = tx; u[1] = ty;
+            } else if (p[1] < 0) {
+                tx = -p[1]; ty = p[0]; p[0] = tx; p[1] = ty;
+                tx = -u[1]; ty = u[0]; u[0] = tx; u[1] = ty;
+            }
+        } else {
+            for (int d = 0; d < 3; d++)
+                if (bd->axes[d]) p[d] = wrap_f64(p[d], bd->domain[d]);
+        }
+    }
+    if (!bd) return;
+    for (int pass = 0; pass < 2; pass++) {
+        if (pass == 0 && !(bd->bc == 1 || bd->bc == 3)) continue;
+        if (pass == 1 && !(bd->bc == 2 || bd->bc == 3)) continue;
+        for (int64_t i = 0; i < n; i++) {
+            if (!(t_inj[i] <= T) || status[i] != 1) continue;
+            const double *p = &x[3 * i];
+            int out;
+            if (pass == 0)
+                out = (bd->bc_space[0] != 0 && fabs(p[0]) > bd->bc_space[0]) ||
+                      (bd->bc_space[1] != 0 && fabs(p[1]) > bd->bc_space[1]) ||
+                      (bd->bc_space[2] != 0 && fabs(p[2]) > bd->bc_space[2]) ||
+                      (bd->bc_space[3] != 0 && sqrt(p[0] * p[0] + p[1] * p[1]) > bd->bc_space[3]);
+            else
+                out = T - t_inj[i] > bd->bc_time;
+            if (out) {
+                status[i] = 0;
+                push_event(ev, ev_cap, cnt, (float)T, (float)p[0], (float)p[1], (float)p[2], (float)v[3 * i],
+                           (float)v[3 * i + 1], (float)v[3 * i + 2], (int)i, species_of_mass(m[i]), 0);
+            }
+        }
+    }
+}
+
+static void leapfrog_f64(int64_t n, double *x, double *v, const double *q, const double *m, int32_t *status,
+                         const double *t_inj, int nsteps, double dt, double t0, double eps2, double kconst,
+                         const double efield[3], int sym, int nimg, const double *img_off, const orc_boundary *bd,
+                         orc_event *ev, int ev_cap, int *ev_count, double *a_out, int nthreads) {
+    double *a = (double *)malloc(sizeof(double) * 3 * (size_t)(n > 0 ? n : 1));
+    int32_t *win = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n > 0 ? n : 1));
+    const double eoa = orc_e_over_amu();
+    const double h = 0.5 * dt;
+    int cnt = 0;
+    for (int it = 0; it < nsteps; it++) {
+        const double ts = t0 + dt * it;
+        drift_f64(n, x, v, m, status, t_inj, ts, h, bd, ev, ev_cap, &cnt);
+        /* force and kick over the particles injected by the mid time */
+        for (int64_t i = 0; i < n; i++) win[i] = t_inj[i] <= ts + h ? status[i] : 0;
+        orc_direct_f64(n, x, q, m, win, NULL, 0, eps2, kconst, sym, nimg, img_off, a, nthreads);
+        for (int64_t i = 0; i < n; i++) {
+            if (win[i] != 1) continue;
+            const double ef = eoa * q[i] / m[i];
+            double s = ts + dt - t_inj[i];
+            s = s < 0 ? 0 : (s > dt ? dt : s);
+            for (int d = 0; d < 3; d++) {
+                a[3 * i + d] += efield[d] * ef;
+                v[3 * i + d] += a[3 * i + d] * s;
+            }
+        }
+        drift_f64(n, x, v, m, status, t_inj, ts + h, h, bd, ev, ev_cap, &cnt);
+    }
+    if (a_out) memcpy(a_out, a, sizeof(double) * 3 * (size_t)n);
+    free(a);
+    free(win);
+    if (ev_count) *ev_count = cnt;
+}
+
+void orc_leapfrog_f64_bc(int64_t n, double *x, double *v, const double *q,
+                         const double *m, int32_t *status, const double *t_inj,
+                         int nsteps, double dt, double t0, double eps2,
+                         double kconst, const double efield[3], int sym, int nimg,
+                         const double *img_off, const orc_boundary *bd,
+                         orc_event *ev, int ev_cap, int *ev_count, int nthreads) {
+    leapfrog_f64(n, x, v, q, m, status, t_inj, nsteps, dt, t0, eps2, kconst, efield, sym, nimg, img_off, bd, ev,
+                 ev_cap, ev_count, NULL, nthreads);
 }
 
 void orc_leapfrog_f64(int64_t n, double *x, double *v, const double *q,
@@ -495,39 +820,8 @@ void orc_leapfrog_f64(int64_t n, double *x, double *v, const double *q,
                       int nsteps, double dt, double t0, double eps2,
                       double kconst, const double efield[3], int sym, int nimg,
                       const double *img_off, double *a_out, int nthreads) {
-    double *a = (double *)malloc(sizeof(double) * 3 * (size_t)(n > 0 ? n : 1));
-    const double eoa = orc_e_over_amu();
-    const double h = 0.5 * dt;
-    for (int it = 0; it < nsteps; it++) {
-        const double ts = t0 + dt * it;
-        for (int half = 0; half < 2; half++) {
-            const double t_start = ts + (half ? h : 0.0);
-            if (half == 1) {
-                /* kick over [ts, ts+dt] */
-                orc_direct_f64(n, x, q, m, status, NULL, 0, eps2, kconst, sym, nimg,
-                               img_off, a, nthreads);
-                for (int64_t i = 0; i < n; i++) {
-                    if (status[i] != 1) continue;
-                    const double ef = eoa * q[i] / m[i];
-                    double s = ts + dt - t_inj[i];
-                    s = s < 0 ? 0 : (s > dt ? dt : s);
-                    for (int d = 0; d < 3; d++) {
-                        a[3 * i + d] += efield[d] * ef;
-                        v[3 * i + d] += a[3 * i + d] * s;
-                    }
-                }
-            }
-            /* drift over [t_start, t_start + dt/2] */
-            for (int64_t i = 0; i < n; i++) {
-                if (!(status[i] == 1 || status[i] == 2)) continue;
-                double s = t_start + h - t_inj[i];
-                s = s < 0 ? 0 : (s > h ? h : s);
-                for (int d = 0; d < 3; d++) x[3 * i + d] += v[3 * i + d] * s;
-            }
-        }
-    }
-    if (a_out) memcpy(a_out, a, sizeof(double) * 3 * (size_t)n);
-    free(a);
+    leapfrog_f64(n, x, v, q, m, status, t_inj, nsteps, dt, t0, eps2, kconst, efield, sym, nimg, img_off, NULL,
+                 NULL, 0, NULL, a_out, nthreads);
 }
 
 /* ---- energy ------------------------------------------------------------ */

@@ -101,6 +101,50 @@ void orc_leapfrog_f64(int64_t n, double *x, double *v, const double *q,
                       double kconst, const double efield[3], int sym, int nimg,
                       const double *img_off, double *a_out, int nthreads);
 
+/* Crash test, symmetry folding and boundary conditions of the drift
+ * (ParticleSystem::propagatePositionNew, particles.cpp:33-40). */
+typedef struct {
+    int crash;              /* 1: CrashConditionOptions::extractorGrid */
+    int bc;                 /* BoundaryConditionOptions: 0 none, 1 space, 2 time, 3 both */
+    int fold;               /* f64 only: 0 none, 1 rotational, 2 translational */
+    int axes[3];            /* symmetryAxes (translational folding) */
+    double crash_z, crash_width, crash_r;   /* z_distance, z_width, r_distance */
+    double bc_space[4];     /* spatialBoundaryConditions x, y, z, w */
+    double bc_time;         /* temporalBoundaryCondition */
+    double domain[3];       /* domainSize (translational folding) */
+} orc_boundary;
+
+/* One record of the events file (ChargedParticles::writeToEventsFile,
+ * particles.cpp:666-684), 40 bytes. */
+typedef struct {
+    float time, x, y, z, vx, vy, vz;
+    int32_t index;
+    uint32_t species;
+    int32_t status;
+} orc_event;
+
+/* orc_leapfrog_ref32 with the crash test, folding and boundary conditions of
+ * bd (nullable; the folding follows sym as the reference's does), on the
+ * reference's [firstParticle, lastParticle) window (LeapfrogDKD::driftNew,
+ * findMostRecentInjected, resetFirstChargedParticle).  Events go to ev (up to
+ * ev_cap; *ev_count receives the total). */
+void orc_leapfrog_ref32_bc(int n, float *pos4, float *vel4, float *acc4,
+                           const float *t_inj, int nsteps, float dt, double eps,
+                           const float efield[3], int sym, int nimg,
+                           const int *images, const float domain_size[3],
+                           const orc_boundary *bd, orc_event *ev, int ev_cap,
+                           int *ev_count, int nthreads);
+
+/* orc_leapfrog_f64 with bd (nullable; folding per bd->fold) and the
+ * injection window as a per-particle test (t_inj <= end of the half step;
+ * force and kick: t_inj <= mid step), with species codes for the events. */
+void orc_leapfrog_f64_bc(int64_t n, double *x, double *v, const double *q,
+                         const double *m, int32_t *status, const double *t_inj,
+                         int nsteps, double dt, double t0, double eps2,
+                         double kconst, const double efield[3], int sym, int nimg,
+                         const double *img_off, const orc_boundary *bd,
+                         orc_event *ev, int ev_cap, int *ev_count, int nthreads);
+
 /* Energy diagnostic in FP64 (particles.cpp:535-578): kinetic
  * 0.5*amu*m*|v|^2 and potential 0.5*sum_{i!=j} q_i q_j e^2 ke/sqrt(r^2+eps2),
  * over all particles in [0,n) as the reference does (no status test). */

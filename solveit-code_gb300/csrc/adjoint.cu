@@ -7,6 +7,9 @@
 //     a       = F(x_h) + c E                    c = (e/amu) q/m, F = direct sum
 //     v_{s+1} = v_s + k a                       k  = clamp(t_s + dt - t_inj, 0, dt), status 1
 //     x_{s+1} = x_h + h2 v_{s+1}                h2 = clamp(t_s + dt - t_inj, 0, dt/2)
+// F and k act on the injection window t_inj <= t_s + dt/2 only (targets and
+// sources); crash, boundary and folding steps are not differentiated (the
+// adjoint refuses a context that has them on).
 // Reverse step with adjoints (lx, lv) of (x_{s+1}, v_{s+1}):
 //     lv += h2 lx;   lh = lx;   la = k lv;   lE += sum_i c_i la_i
 //     lh += J(x_h)^T la;        lx = lh;     lv += h1 lh
@@ -49,14 +52,15 @@ __global__ void adj_prep(double *__restrict__ lx, double *__restrict__ ly, doubl
                          double *__restrict__ lvx, double *__restrict__ lvy, double *__restrict__ lvz,
                          double *__restrict__ lax, double *__restrict__ lay, double *__restrict__ laz,
                          const double *__restrict__ q, const double *__restrict__ m, const int32_t *__restrict__ st,
-                         const double *__restrict__ t_inj, int64_t n, double ts, double dt, double eoa,
-                         double *__restrict__ lE) {
+                         const int32_t *__restrict__ wst, const double *__restrict__ t_inj, int64_t n, double ts,
+                         double dt, double eoa, double *__restrict__ lE) {
     double e0 = 0, e1 = 0, e2 = 0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const int32_t w = st[i];
         const double h = 0.5 * dt;
         const double h2 = (w == 1 || w == 2) ? clampd(ts + dt - t_inj[i], h) : 0.0;
-        const double k = (w == 1) ? clampd(ts + dt - t_inj[i], dt) : 0.0;
+        // kicked: inbound and injected by the step's mid time (the window of the force)
+        const double k = (wst[i] == 1) ? clampd(ts + dt - t_inj[i], dt) : 0.0;
         double vx = lvx[i] + h2 * lx[i], vy = lvy[i] + h2 * ly[i], vz = lvz[i] + h2 * lz[i];
         lvx[i] = vx;
         lvy[i] = vy;
@@ -380,25 +384,14 @@ sv_status load_state(sv_ctx *c, const double *src) {
     return SV_OK;
 }
 
-sv_status dkd_step(sv_ctx *c, double ts, double dt, double *save_xh) {
-    const double h = 0.5 * dt;
-    SV_TRY(drift(c, ts, h));
-    if (save_xh) {
-        const size_t b = sizeof(double) * c->n;
-        SV_CK(c, cudaMemcpyAsync(save_xh, c->x, b, cudaMemcpyDeviceToDevice, c->stream));
-        SV_CK(c, cudaMemcpyAsync(save_xh + c->n, c->y, b, cudaMemcpyDeviceToDevice, c->stream));
-        SV_CK(c, cudaMemcpyAsync(save_xh + 2 * c->n, c->z, b, cudaMemcpyDeviceToDevice, c->stream));
-    }
-    SV_TRY(compute_accel_device(c, 0, c->n));
-    SV_TRY(kick(c, ts, dt));
-    SV_TRY(drift(c, ts + h, h));
-    return SV_OK;
-}
-
-// J(x)^T la for the positions currently in c->x: result added into (lx, ly, lz)
+// J(x)^T la for the positions currently in c->x, over the particles of
+// c->wstatus (the step's window): result added into (lx, ly, lz)
 sv_status jtv_add(sv_ctx *c, const double *lax, const double *lay, const double *laz, double *lx, double *ly,
                   double *lz) {
-    SV_TRY(sort_state(c, 0, c->n));
+    c->fstatus = c->wstatus;
+    const sv_status st = sort_state(c, 0, c->n);
+    c->fstatus = nullptr;
+    SV_TRY(st);
     Sorted &S = c->S;
     const int n = (int)S.n;
     Adj &A = *c->adj;
@@ -459,6 +452,8 @@ extern "C" sv_status sv_adjoint_forward(sv_ctx *c, int32_t nsteps, double dt, do
     if (c->batch) return set_error(c, SV_ERR_UNSUPPORTED, "the adjoint runs on single-plume contexts");
     if (c->P.method != SV_METHOD_DIRECT || c->P.symmetry != SV_SYM_NONE)
         return set_error(c, SV_ERR_UNSUPPORTED, "the adjoint covers the direct sum without symmetry images");
+    if (c->B.crash != SV_CRASH_NONE || c->B.bc != SV_BC_NONE || c->B.fold)
+        return set_error(c, SV_ERR_UNSUPPORTED, "the adjoint covers drifts without crash, boundary or folding steps");
     SV_CK(c, cudaSetDevice(c->device));
     if (!c->adj) c->adj = new Adj();
     Adj &A = *c->adj;
@@ -485,7 +480,7 @@ extern "C" sv_status sv_adjoint_forward(sv_ctx *c, int32_t nsteps, double dt, do
     A.t0 = t0;
     for (int s = 0; s < nsteps; s++) {
         if (s % checkpoint_every == 0) SV_TRY(copy_state(c, A.ck + (size_t)(s / checkpoint_every) * 6 * n));
-        SV_TRY(dkd_step(c, t0 + dt * s, dt, nullptr));
+        SV_TRY(leapfrog_step(c, t0 + dt * s, dt, nullptr));
     }
     A.forward_done = true;
     return SV_OK;
@@ -517,15 +512,18 @@ extern "C" sv_status sv_adjoint_backward(sv_ctx *c, const double *dl_dx3, const 
         const int s1 = s0 + A.every < A.nsteps ? s0 + A.every : A.nsteps;
         // recompute the segment from its checkpoint, keeping every x_h
         SV_TRY(load_state(c, A.ck + (size_t)k * 6 * n));
-        for (int s = s0; s < s1; s++) SV_TRY(dkd_step(c, A.t0 + dt * s, dt, A.xh + (size_t)(s - s0) * 3 * n));
+        for (int s = s0; s < s1; s++)
+            SV_TRY(leapfrog_step(c, A.t0 + dt * s, dt, A.xh + (size_t)(s - s0) * 3 * n));
         for (int s = s1 - 1; s >= s0; s--) {
             const double ts = A.t0 + dt * s;
             const double *xh = A.xh + (size_t)(s - s0) * 3 * n;
             SV_CK(c, cudaMemcpyAsync(c->x, xh, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
             SV_CK(c, cudaMemcpyAsync(c->y, xh + n, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
             SV_CK(c, cudaMemcpyAsync(c->z, xh + 2 * n, sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
+            SV_TRY(window_status(c, ts + 0.5 * dt));
             adj_prep<<<stream_grid(n), 256, 0, c->stream>>>(lx, ly, lz, lvx, lvy, lvz, lax, lay, laz, c->q, c->m,
-                                                            c->status, c->t_inj, n, ts, dt, c->P.e_over_amu, A.lE);
+                                                            c->status, c->wstatus, c->t_inj, n, ts, dt,
+                                                            c->P.e_over_amu, A.lE);
             SV_LAUNCHED(c);
             SV_TRY(jtv_add(c, lax, lay, laz, lx, ly, lz));
             adj_drift_back<<<stream_grid(n), 256, 0, c->stream>>>(lx, ly, lz, lvx, lvy, lvz, c->status, c->t_inj, n,

@@ -128,10 +128,11 @@ void free_state(sv_ctx *c) {
     cudaFree(c->x); cudaFree(c->y); cudaFree(c->z);
     cudaFree(c->vx); cudaFree(c->vy); cudaFree(c->vz);
     cudaFree(c->q); cudaFree(c->m); cudaFree(c->t_inj); cudaFree(c->status); cudaFree(c->qom);
+    cudaFree(c->species); cudaFree(c->wstatus);
     cudaFree(c->ax); cudaFree(c->ay); cudaFree(c->az);
     c->x = c->y = c->z = c->vx = c->vy = c->vz = c->q = c->m = c->t_inj = c->qom = nullptr;
     c->ax = c->ay = c->az = nullptr;
-    c->status = nullptr;
+    c->status = c->species = c->wstatus = nullptr;
     c->cap = 0;
 }
 
@@ -144,15 +145,26 @@ sv_status ensure_capacity(sv_ctx *c, int64_t n) {
     SV_TRY(dev_alloc(c, &c->q, cap)); SV_TRY(dev_alloc(c, &c->m, cap)); SV_TRY(dev_alloc(c, &c->t_inj, cap));
     SV_TRY(dev_alloc(c, &c->qom, cap));
     SV_TRY(dev_alloc(c, &c->status, cap));
+    SV_TRY(dev_alloc(c, &c->species, cap)); SV_TRY(dev_alloc(c, &c->wstatus, cap));
     SV_TRY(dev_alloc(c, &c->ax, cap)); SV_TRY(dev_alloc(c, &c->ay, cap)); SV_TRY(dev_alloc(c, &c->az, cap));
     c->cap = cap;
     return SV_OK;
 }
 
+__device__ double species_mass(int s);
+
+// q/m, and the species code of the mass (ParticleSpeciesFunction::getMass,
+// particles.h:65-87, inverted; the codes' masses are distinct) for the event records
 __global__ void charge_over_mass(const double *__restrict__ q, const double *__restrict__ m, int64_t n,
-                                 double *__restrict__ qom) {
+                                 double *__restrict__ qom, int32_t *__restrict__ species) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i < n) qom[i] = m[i] > 0.0 ? q[i] / m[i] : 0.0;
+    if (i >= n) return;
+    const double mi = m[i];
+    qom[i] = mi > 0.0 ? q[i] / mi : 0.0;
+    int32_t code = -1;
+    for (int k = 0; k < 8; k++)
+        if (k != 3 && mi == species_mass(k)) code = k;
+    species[i] = code;
 }
 
 __global__ void unpack_fp64(const double *__restrict__ x3, const double *__restrict__ v3,
@@ -391,6 +403,7 @@ void sv_destroy(sv_ctx *c) {
     adjoint_free(c);
     batch_free(c);
     outliers_free(c);
+    events_free(c);
     free_state(c);
     Sorted &S = c->S;
     cudaFree(S.x); cudaFree(S.y); cudaFree(S.z); cudaFree(S.q); cudaFree(S.qm);
@@ -433,6 +446,8 @@ static sv_status upload_state(sv_ctx *c, int64_t n, const double *x3, const doub
     c->n = n;
     c->have_state = true;
     c->have_accel = false;
+    c->ev_seq = 0;
+    if (c->d_ev_count) SV_CK(c, cudaMemsetAsync(c->d_ev_count, 0, sizeof(unsigned long long), c->stream));
     if (n == 0) return SV_OK;
     const size_t b3 = sizeof(double) * 3 * (size_t)n, b1 = sizeof(double) * (size_t)n;
     void *stg = nullptr;
@@ -454,7 +469,7 @@ static sv_status upload_state(sv_ctx *c, int64_t n, const double *x3, const doub
                                                    c->x, c->y, c->z, c->vx, c->vy, c->vz, c->q, c->m,
                                                    c->status, c->t_inj);
     SV_LAUNCHED(c);
-    charge_over_mass<<<grid_of(n), 256, 0, c->stream>>>(c->q, c->m, n, c->qom);
+    charge_over_mass<<<grid_of(n), 256, 0, c->stream>>>(c->q, c->m, n, c->qom, c->species);
     SV_LAUNCHED(c);
     return SV_OK;
 }
@@ -478,6 +493,8 @@ sv_status sv_upload_ref32(sv_ctx *c, int64_t n, const float *pos4, const float *
     c->n = n;
     c->have_state = true;
     c->have_accel = false;
+    c->ev_seq = 0;
+    if (c->d_ev_count) SV_CK(c, cudaMemsetAsync(c->d_ev_count, 0, sizeof(unsigned long long), c->stream));
     if (n == 0) return SV_OK;
     const size_t b4 = 16 * (size_t)n;
     void *stg = nullptr;
@@ -494,7 +511,7 @@ sv_status sv_upload_ref32(sv_ctx *c, int64_t n, const float *pos4, const float *
     unpack_ref32<<<grid_of(n), 256, 0, c->stream>>>(dp, dv, da, dt, n, t_inj != nullptr, c->x, c->y, c->z,
                                                     c->vx, c->vy, c->vz, c->q, c->m, c->status, c->t_inj);
     SV_LAUNCHED(c);
-    charge_over_mass<<<grid_of(n), 256, 0, c->stream>>>(c->q, c->m, n, c->qom);
+    charge_over_mass<<<grid_of(n), 256, 0, c->stream>>>(c->q, c->m, n, c->qom, c->species);
     SV_LAUNCHED(c);
     return SV_OK;
 }
@@ -574,7 +591,7 @@ sv_status sv::compute_accel_device(sv_ctx *c, int64_t first, int64_t last) {
         }
         phase_mark(c, 7);
         SV_TRY(unsort_accel(c));
-        zero_nontargets<<<grid_of(n), 256, 0, c->stream>>>(c->ax, c->ay, c->az, c->status, first, last, n);
+        zero_nontargets<<<grid_of(n), 256, 0, c->stream>>>(c->ax, c->ay, c->az, force_status(c), first, last, n);
         SV_LAUNCHED(c);
         if (outliers) SV_TRY(outliers_add(c, first, last));
         phase_mark(c, 8);
@@ -626,14 +643,65 @@ sv_status sv_leapfrog(sv_ctx *c, int32_t nsteps, double dt, double t0) {
     if (nsteps < 0 || !(dt > 0.0)) return set_error(c, SV_ERR_INVALID, "nsteps >= 0 and dt > 0 required");
     SV_CK(c, cudaSetDevice(c->device));
     if (c->batch) return batch_leapfrog(c, nsteps, dt, t0);
-    const double h = 0.5 * dt;
-    for (int it = 0; it < nsteps; it++) {
-        const double ts = t0 + dt * it;
-        SV_TRY(drift(c, ts, h));
-        SV_TRY(compute_accel_device(c, 0, c->n));
-        SV_TRY(kick(c, ts, dt));
-        SV_TRY(drift(c, ts + h, h));
+    for (int it = 0; it < nsteps; it++) SV_TRY(leapfrog_step(c, t0 + dt * it, dt));
+    return SV_OK;
+}
+
+sv_status sv_set_boundary(sv_ctx *c, const sv_boundary *b) {
+    if (!c || !b) return SV_ERR_INVALID;
+    if (b->crash != SV_CRASH_NONE && b->crash != SV_CRASH_EXTRACTOR_GRID)
+        return set_error(c, SV_ERR_INVALID, "unknown crash condition %d", b->crash);
+    if (b->bc < SV_BC_NONE || b->bc > SV_BC_SPACE_AND_TIME)
+        return set_error(c, SV_ERR_INVALID, "unknown boundary condition %d", b->bc);
+    for (int k = 0; k < 4; k++)
+        if (!(b->bc_space[k] >= 0.0)) return set_error(c, SV_ERR_INVALID, "spatial limits must be >= 0");
+    if (b->fold && c->P.symmetry == SV_SYM_TRANSLATIONAL)
+        for (int k = 0; k < 3; k++)
+            if (c->P.sym_axes[k] && !(c->P.domain_size[k] > 0.0))
+                return set_error(c, SV_ERR_INVALID, "folding a periodic axis needs domain_size > 0");
+    c->B = *b;
+    if (c->batch) batch_invalidate(c);
+    return SV_OK;
+}
+
+sv_status sv_get_boundary(const sv_ctx *c, sv_boundary *b) {
+    if (!c || !b) return SV_ERR_INVALID;
+    *b = c->B;
+    return SV_OK;
+}
+
+sv_status sv_get_events(sv_ctx *c, sv_event *out, int64_t cap, int64_t *count) {
+    if (!c || !count || cap < 0) return SV_ERR_INVALID;
+    *count = 0;
+    if (!c->d_ev_count) return SV_OK;
+    SV_CK(c, cudaSetDevice(c->device));
+    unsigned long long recorded = 0;
+    SV_CK(c, cudaMemcpyAsync(&recorded, c->d_ev_count, sizeof(recorded), cudaMemcpyDeviceToHost, c->stream));
+    SV_CK(c, cudaStreamSynchronize(c->stream));
+    *count = (int64_t)recorded;
+    if (!out) return recorded > (unsigned long long)c->ev_cap
+                         ? set_error(c, SV_ERR_CAPACITY, "%llu events recorded, %lld kept", recorded,
+                                     (long long)c->ev_cap)
+                         : SV_OK;
+    const int64_t kept = std::min<int64_t>((int64_t)recorded, c->ev_cap);
+    std::vector<sv_event> ev(kept);
+    std::vector<unsigned long long> key(kept);
+    if (kept > 0) {
+        SV_CK(c, cudaMemcpyAsync(ev.data(), c->d_events, sizeof(sv_event) * kept, cudaMemcpyDeviceToHost, c->stream));
+        SV_CK(c, cudaMemcpyAsync(key.data(), c->d_ev_key, sizeof(unsigned long long) * kept, cudaMemcpyDeviceToHost,
+                                 c->stream));
     }
+    SV_CK(c, cudaMemsetAsync(c->d_ev_count, 0, sizeof(unsigned long long), c->stream));
+    SV_CK(c, cudaStreamSynchronize(c->stream));
+    // the device appends in arrival order; the reference's file order is by
+    // drift, kind of event, particle index
+    std::vector<int64_t> ord(kept);
+    for (int64_t k = 0; k < kept; k++) ord[k] = k;
+    std::sort(ord.begin(), ord.end(), [&](int64_t a, int64_t b) { return key[a] < key[b]; });
+    const int64_t ncopy = std::min<int64_t>(kept, cap);
+    for (int64_t k = 0; k < ncopy; k++) out[k] = ev[ord[k]];
+    if (recorded > (unsigned long long)c->ev_cap)
+        return set_error(c, SV_ERR_CAPACITY, "%llu events recorded, %lld kept", recorded, (long long)c->ev_cap);
     return SV_OK;
 }
 

@@ -82,13 +82,16 @@ struct Batch {
     int *d_nbox = nullptr, *d_err = nullptr, *h_err = nullptr;
     int overflow_mask = 0;            // levels that overflowed at the last regrow
     // graphs
-    double *d_time = nullptr;         // {t0, dt, k}
+    double *d_time = nullptr;         // {t0, dt, k, first event sequence number}
     double *h_time = nullptr;         // pinned
     cudaGraphExec_t g_accel = nullptr, g_step = nullptr;
     unsigned long long accel_kernels = 0, step_kernels = 0;
     cudaStream_t side = nullptr;
     cudaEvent_t fork = nullptr, join = nullptr;
     double *backup = nullptr;         // 6 n: state at the start of a leapfrog call
+    int32_t *backup_st = nullptr;     // n: status at the start of a leapfrog call
+    unsigned long long *ev_count0 = nullptr;  // event count at the start of a leapfrog call
+    int8_t *pfold = nullptr;          // n: 1 for the particles of rotational plumes (folding)
     double step_dt = 0;               // dt baked into g_step
     // tuning
     int m2l_weight = 400, direct_chunk = 2048;  // tuned: M2L cost in pair units, direct work-item size
@@ -497,12 +500,12 @@ sv_status build_items(sv_ctx *c, Batch &B) {
 sv_status sort_batch(sv_ctx *c, Batch &B, bool adapt) {
     Sorted &S = c->S;
     const int64_t nv = B.nv;
-    bbox_chunks_kernel<<<B.nchunks, 256, 0, c->stream>>>(B.chunk_beg, B.vsrc, B.vtag, c->x, c->y, c->z, c->status,
+    bbox_chunks_kernel<<<B.nchunks, 256, 0, c->stream>>>(B.chunk_beg, B.vsrc, B.vtag, c->x, c->y, c->z, force_status(c),
                                                          B.chunk_red);
     SV_LAUNCHED(c);
     plume_roots_kernel<<<div_up(B.np, 128), 128, 0, c->stream>>>(B.np, B.pid_chunk, B.chunk_red, B.roots);
     SV_LAUNCHED(c);
-    batch_keys_kernel<<<div_up(nv, 256), 256, 0, c->stream>>>(nv, B.vsrc, B.vtag, c->x, c->y, c->z, c->status,
+    batch_keys_kernel<<<div_up(nv, 256), 256, 0, c->stream>>>(nv, B.vsrc, B.vtag, c->x, c->y, c->z, force_status(c),
                                                               B.roots, S.keys_alt, S.idx_alt);
     SV_LAUNCHED(c);
     size_t bytes = B.cub_bytes;
@@ -521,7 +524,7 @@ sv_status sort_batch(sv_ctx *c, Batch &B, bool adapt) {
         SV_LAUNCHED(c);
     }
     batch_gather_kernel<<<div_up(nv, 256), 256, 0, c->stream>>>(nv, S.idx, B.vsrc, B.vtag, c->x, c->y, c->z, c->q,
-                                                                c->m, c->qom, c->status, B.roots, c->P.k_const,
+                                                                c->m, c->qom, force_status(c), B.roots, c->P.k_const,
                                                                 S.x, S.y, S.z, S.q, S.qm);
     SV_LAUNCHED(c);
     return SV_OK;
@@ -645,10 +648,13 @@ sv_status ensure_step_graph(sv_ctx *c, Batch &B) {
     if (B.g_step) return SV_OK;
     return capture(c, &B.g_step, &B.step_kernels, [&]() -> sv_status {
         const double dt = B.step_dt, h = 0.5 * dt;
-        SV_TRY(drift(c, 0.0, h, B.d_time));
-        SV_TRY(batch_force(c, B));
-        SV_TRY(kick(c, 0.0, dt, B.d_time));
-        SV_TRY(drift(c, h, h, B.d_time));
+        SV_TRY(drift(c, 0.0, h, c->wstatus, B.d_time, 0));
+        c->fstatus = c->wstatus;
+        const sv_status s = batch_force(c, B);
+        c->fstatus = nullptr;
+        SV_TRY(s);
+        SV_TRY(kick(c, 0.0, dt, c->wstatus, B.d_time));
+        SV_TRY(drift(c, h, h, nullptr, B.d_time, 1));
         advance_step_kernel<<<1, 1, 0, c->stream>>>(B.d_time);
         SV_LAUNCHED(c);
         return SV_OK;
@@ -680,6 +686,10 @@ void batch_free(sv_ctx *c) {
     cudaFree(B.chunk_beg); cudaFree(B.pid_chunk); cudaFree(B.chunk_red); cudaFree(B.items);
     cudaFree(B.queue); cudaFree(B.cub_tmp); cudaFree(B.d_nbox); cudaFree(B.d_err); cudaFree(B.d_time);
     cudaFree(B.backup);
+    cudaFree(B.backup_st);
+    cudaFree(B.ev_count0);
+    cudaFree(B.pfold);
+    c->pfold = nullptr;
     cudaFreeHost(B.h_err);
     cudaFreeHost(B.h_time);
     if (B.side) cudaStreamDestroy(B.side);
@@ -792,9 +802,18 @@ sv_status batch_plan(sv_ctx *c, int32_t np, const int64_t *counts, const int32_t
     SV_CK(c, cudaMalloc(&B.queue, sizeof(int)));
     SV_CK(c, cudaMalloc(&B.d_nbox, sizeof(int) * 3 * kBLevels));
     SV_CK(c, cudaMalloc(&B.d_err, sizeof(int)));
-    SV_CK(c, cudaMalloc(&B.d_time, sizeof(double) * 3));
+    SV_CK(c, cudaMalloc(&B.d_time, sizeof(double) * 4));
     SV_CK(c, cudaMallocHost(&B.h_err, sizeof(int)));
-    SV_CK(c, cudaMallocHost(&B.h_time, sizeof(double) * 3));
+    SV_CK(c, cudaMallocHost(&B.h_time, sizeof(double) * 4));
+    {
+        std::vector<int8_t> pf((size_t)std::max<int64_t>(c->n, 1), 0);
+        for (int p = 0; p < np; p++)
+            if (sym[p] == SV_SYM_ROTATIONAL)
+                std::fill(pf.begin() + B.off[p], pf.begin() + B.off[p] + counts[p], (int8_t)1);
+        SV_CK(c, cudaMalloc(&B.pfold, pf.size()));
+        SV_CK(c, cudaMemcpy(B.pfold, pf.data(), pf.size(), cudaMemcpyHostToDevice));
+        c->pfold = B.pfold;
+    }
     SV_CK(c, cudaMemset(B.d_err, 0, sizeof(int)));
     SV_CK(c, cudaMemset(B.d_nbox, 0, sizeof(int) * 3 * kBLevels));
     if (B.nv > 0) {
@@ -843,9 +862,17 @@ sv_status batch_leapfrog(sv_ctx *c, int32_t nsteps, double dt, double t0) {
     if (!B.planned) SV_TRY(plan_forest(c, B, 1));
     const int64_t n = c->n;
     if (!B.backup) SV_CK(c, cudaMalloc(&B.backup, sizeof(double) * 6 * std::max<int64_t>(n, 1)));
+    if (!B.backup_st) SV_CK(c, cudaMalloc(&B.backup_st, sizeof(int32_t) * std::max<int64_t>(n, 1)));
+    if (!B.ev_count0) SV_CK(c, cudaMalloc(&B.ev_count0, sizeof(unsigned long long)));
+    // the drift may change status and record events: both are part of the state a retry restores
+    if (c->B.crash != SV_CRASH_NONE || c->B.bc != SV_BC_NONE) SV_TRY(events_reserve(c));
     double *st[6] = {c->x, c->y, c->z, c->vx, c->vy, c->vz};
     for (int k = 0; k < 6; k++)
         SV_CK(c, cudaMemcpyAsync(B.backup + k * n, st[k], sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
+    SV_CK(c, cudaMemcpyAsync(B.backup_st, c->status, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, c->stream));
+    if (c->d_ev_count)
+        SV_CK(c, cudaMemcpyAsync(B.ev_count0, c->d_ev_count, sizeof(unsigned long long), cudaMemcpyDeviceToDevice,
+                                 c->stream));
     for (int attempt = 0; attempt < 4; attempt++) {
         // dt is baked into the step graph
         if (B.g_step && B.step_dt != dt) {
@@ -857,17 +884,25 @@ sv_status batch_leapfrog(sv_ctx *c, int32_t nsteps, double dt, double t0) {
         B.h_time[0] = t0;
         B.h_time[1] = dt;
         B.h_time[2] = 0.0;
-        SV_CK(c, cudaMemcpyAsync(B.d_time, B.h_time, sizeof(double) * 3, cudaMemcpyHostToDevice, c->stream));
+        B.h_time[3] = (double)c->ev_seq;
+        SV_CK(c, cudaMemcpyAsync(B.d_time, B.h_time, sizeof(double) * 4, cudaMemcpyHostToDevice, c->stream));
         for (int s = 0; s < nsteps; s++) {
             SV_CK(c, cudaGraphLaunch(B.g_step, c->stream));
             c->launches += B.step_kernels;
         }
         int err = 0;
         SV_TRY(read_err(c, B, &err));
-        if (!err) return SV_OK;
+        if (!err) {
+            c->ev_seq += 2LL * nsteps;
+            return SV_OK;
+        }
         for (int k = 0; k < 6; k++)
             SV_CK(c, cudaMemcpyAsync(st[k], B.backup + k * n, sizeof(double) * n, cudaMemcpyDeviceToDevice,
                                      c->stream));
+        SV_CK(c, cudaMemcpyAsync(c->status, B.backup_st, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, c->stream));
+        if (c->d_ev_count)
+            SV_CK(c, cudaMemcpyAsync(c->d_ev_count, B.ev_count0, sizeof(unsigned long long),
+                                     cudaMemcpyDeviceToDevice, c->stream));
         SV_TRY(grow(c, B, 2 << attempt));
     }
     return set_error(c, SV_ERR_CAPACITY, "forest box capacity still exceeded after growing it");

@@ -1579,7 +1579,7 @@ sv_status fmm_sort_images(sv_ctx *c, int64_t first, int64_t last) {
         // the host vector must outlive the copy
         SV_CK(c, cudaStreamSynchronize(c->stream));
     }
-    expand_images_kernel<<<div_up(ne, 256), 256, 0, c->stream>>>(c->x, c->y, c->z, c->q, c->m, c->status, n, kind,
+    expand_images_kernel<<<div_up(ne, 256), 256, 0, c->stream>>>(c->x, c->y, c->z, c->q, c->m, force_status(c), n, kind,
                                                                  nimg, F.eoff, F.ex, F.ey, F.ez, F.eq, F.em, F.est);
     SV_LAUNCHED(c);
     const ParticleView v{F.ex, F.ey, F.ez, F.eq, F.em, F.est, ne, n};

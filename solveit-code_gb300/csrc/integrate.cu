@@ -1,33 +1,200 @@
 // integrate.cu -- FP64 leapfrog pieces and the energy diagnostic.
 //
-// drift: ChargedParticles::propagatePositionNew (particles.cpp:693-739)
-//        x += v * clamp(t_start + h - t_inj, 0, h) for status 1 or 2.
+// drift: ParticleSystem::propagatePositionNew (particles.cpp:33-40):
+//        ChargedParticles::propagatePositionNew (particles.cpp:693-739),
+//        x += v * clamp(t_start + h - t_inj, 0, h) for status 1 or 2, with the
+//        extractor-grid crash test (structures.h:467-517); then
+//        enforceSymmetryConditions (particles.cpp:199-333) and
+//        enforceBoundaryConditions (particles.cpp:73-177).  Only particles
+//        inside the injection window (t_inj <= t_start + h: LeapfrogDKD::
+//        driftNew and findMostRecentInjected, integration_schemes.cpp:705-723,
+//        particles.cpp:1328-1366) are touched.
 // kick:  computeBackgroundAcceleration (particles.cpp:496-520) with a uniform
 //        field + propagateVelocityNew (particles.cpp:763-786)
 //        v += (a + (e/amu)(q/m) E) * clamp(t_start + dt - t_inj, 0, dt) for
-//        status 1.
-// Both are HBM-bound streams (drift 56 B, kick 88 B per particle).
+//        windowed status 1.
+// Both are HBM-bound streams (drift 60 B, kick 92 B per particle).
 // energy: computeChargedKineticEnergy / computeChargedElectricPotentialEnergy
 //        (particles.cpp:535-578), FP64, all particles, potential halved.
 #include "sv_internal.cuh"
 
+#include <algorithm>
+#include <numeric>
+#include <vector>
+
 namespace sv {
 namespace {
 
-__global__ void drift_kernel(double *__restrict__ x, double *__restrict__ y, double *__restrict__ z,
-                             const double *__restrict__ vx, const double *__restrict__ vy,
-                             const double *__restrict__ vz, const int32_t *__restrict__ st,
-                             const double *__restrict__ t_inj, int64_t n, double t_start, double h,
-                             const double *__restrict__ tb) {
-    if (tb) t_start += tb[0] + tb[1] * tb[2];
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+struct DriftArgs {
+    double *x, *y, *z, *vx, *vy, *vz;
+    int32_t *st;
+    const double *t_inj;
+    const int32_t *species;
+    int32_t *window;  // status for the force and kick of the step, or null
+    int64_t n;
+    double t_start, h;
+    const double *tb;
+    long long seq_base;
+    // crash (extractor grid), boundary conditions, folding
+    int crash, bc, fold;    // fold: 0 none, 1 rotational, 2 translational, 3 per particle from pfold
+    const int8_t *pfold;
+    double cz, cw, cr;
+    double bsx, bsy, bsz, bsr, bt;
+    double Lx, Ly, Lz;
+    int ax, ay, az;
+    // event log
+    sv_event *ev;
+    unsigned long long *ev_key, *ev_count;
+    long long ev_cap;
+};
+
+// std::max / std::min as the reference calls them (a NaN operand falls through the same way)
+__device__ __forceinline__ double ref_max(double a, double b) { return a < b ? b : a; }
+__device__ __forceinline__ double ref_min(double a, double b) { return b < a ? b : a; }
+
+// CrashParameters::checkExtractorGridCrash (structures.h:467-517): does the
+// drift segment (r0, z0) -> (r1, z1) of the (r, z) plane cross the bottom,
+// top or inner side of the grid?  *zc receives the z of the crossing.
+__device__ bool extractor_crash(double x0, double y0, double z0, double x1, double y1, double z1, double zd,
+                                double zw, double rd, double *zc) {
+    const double ri = sqrt(x0 * x0 + y0 * y0), rf = sqrt(x1 * x1 + y1 * y1);
+    const double m = (z1 - z0) / (rf - ri);
+    const double b = z0 - m * ri;
+    const double rmin = ref_min(ri, rf), rmax = ref_max(ri, rf);
+    const double zmin = ref_min(z0, z1), zmax = ref_max(z0, z1);
+    if (zd >= zmin && zd <= zmax) {
+        const double tr = (zd - b) / m;
+        if (tr >= ref_max(rmin, rd) && tr <= rmax) {
+            *zc = zd;
+            return true;
+        }
+    }
+    const double zt = zd + zw;
+    if (zt >= zmin && zt <= zmax) {
+        const double tr = (zt - b) / m;
+        if (tr >= ref_max(rmin, rd) && tr <= rmax) {
+            *zc = zt;
+            return true;
+        }
+    }
+    if (rd >= rmin && rd <= rmax) {
+        const double tz = m * rd + b;
+        if (tz >= ref_max(zmin, zd) && tz <= ref_min(zmax, zt)) {
+            *zc = tz;
+            return true;
+        }
+    }
+    return false;
+}
+
+// ParticleSystem::translateToSymmetryDomain, one axis (particles.cpp:278-333)
+__device__ __forceinline__ double wrap_axis(double p, double L) {
+    double t = p + L / 2;
+    if (t >= 0) return fmod(t, L) - L / 2;
+    t = fmod(t, L);
+    return t < 0 ? t + L / 2 : t - L / 2;
+}
+
+// phase 0 crash, 1 spatial, 2 temporal: the reference writes each kind of
+// event in its own pass over the particles
+__device__ void record_event(const DriftArgs &a, long long seq, int phase, int64_t i, double t, double x, double y,
+                             double z, double vx, double vy, double vz, int32_t status) {
+    const unsigned long long slot = atomicAdd(a.ev_count, 1ull);
+    if ((long long)slot >= a.ev_cap) return;
+    sv_event e;
+    e.time = (float)t;
+    e.x = (float)x;
+    e.y = (float)y;
+    e.z = (float)z;
+    e.vx = (float)vx;
+    e.vy = (float)vy;
+    e.vz = (float)vz;
+    e.index = (int32_t)i;
+    e.species = a.species ? (uint32_t)a.species[i] : 0xffffffffu;
+    e.status = status;
+    a.ev[slot] = e;
+    a.ev_key[slot] = ((unsigned long long)seq << 34) | ((unsigned long long)phase << 32) | (unsigned long long)(uint32_t)i;
+}
+
+__global__ void drift_kernel(DriftArgs a) {
+    double t_start = a.t_start;
+    long long seq = a.seq_base;
+    if (a.tb) {
+        t_start += a.tb[0] + a.tb[1] * a.tb[2];
+        seq += (long long)a.tb[3] + 2 * (long long)a.tb[2];
+    }
+    const double h = a.h, T = t_start + h;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n;
          i += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t w = st[i];
-        if (!(w == 1 || w == 2)) continue;
-        const double s = fmin(fmax(t_start + h - t_inj[i], 0.0), h);
-        x[i] += vx[i] * s;
-        y[i] += vy[i] * s;
-        z[i] += vz[i] * s;
+        const double ti = a.t_inj[i];
+        if (!(ti <= T)) {  // not injected by the end of this half step: outside the window
+            if (a.window) a.window[i] = 0;
+            continue;
+        }
+        int32_t w = a.st[i];
+        const int32_t w0 = w;
+        double x = a.x[i], y = a.y[i], z = a.z[i];
+        double vx = a.vx[i], vy = a.vy[i], vz = a.vz[i];
+        const double x0 = x, y0 = y, z0 = z, vx0 = vx, vy0 = vy;
+        if (w == 1 || w == 2) {
+            const double s = fmin(fmax(T - ti, 0.0), h);
+            x += vx * s;
+            y += vy * s;
+            z += vz * s;
+            double zc;
+            if (a.crash == SV_CRASH_EXTRACTOR_GRID && extractor_crash(x0, y0, z0, x, y, z, a.cz, a.cw, a.cr, &zc)) {
+                w = -1;
+                z = zc;
+                const double td = (zc - z0) / vz;
+                x = x0 + td * vx;
+                y = y0 + td * vy;
+                record_event(a, seq, 0, i, t_start + td, x, y, z, vx, vy, vz, w);
+            }
+        }
+        const int fold = a.fold == 3 ? a.pfold[i] : a.fold;
+        if (fold == 1) {
+            // ParticleSystem::rotateToFirstQuadrant (particles.cpp:225-264)
+            if (x < 0 && y < 0) {
+                x = -x; y = -y; vx = -vx; vy = -vy;
+            } else if (x < 0) {
+                const double tx = y, ty = -x, tvx = vy, tvy = -vx;
+                x = tx; y = ty; vx = tvx; vy = tvy;
+            } else if (y < 0) {
+                const double tx = -y, ty = x, tvx = -vy, tvy = vx;
+                x = tx; y = ty; vx = tvx; vy = tvy;
+            }
+        } else if (fold == 2) {
+            if (a.ax) x = wrap_axis(x, a.Lx);
+            if (a.ay) y = wrap_axis(y, a.Ly);
+            if (a.az) z = wrap_axis(z, a.Lz);
+        }
+        if (w == 1 && (a.bc == SV_BC_SPACE || a.bc == SV_BC_SPACE_AND_TIME)) {
+            // checkOutOfSpatialBounds (particles.cpp:117-139)
+            const bool out = (a.bsx != 0 && fabs(x) > a.bsx) || (a.bsy != 0 && fabs(y) > a.bsy) ||
+                             (a.bsz != 0 && fabs(z) > a.bsz) || (a.bsr != 0 && sqrt(x * x + y * y) > a.bsr);
+            if (out) {
+                w = 0;
+                record_event(a, seq, 1, i, T, x, y, z, vx, vy, vz, w);
+            }
+        }
+        if (w == 1 && (a.bc == SV_BC_TIME || a.bc == SV_BC_SPACE_AND_TIME)) {
+            // checkOutOfTemporalBounds (particles.cpp:163-168)
+            if (T - ti > a.bt) {
+                w = 0;
+                record_event(a, seq, 2, i, T, x, y, z, vx, vy, vz, w);
+            }
+        }
+        if (x != x0 || y != y0 || z != z0) {
+            a.x[i] = x;
+            a.y[i] = y;
+            a.z[i] = z;
+        }
+        if (vx != vx0 || vy != vy0) {
+            a.vx[i] = vx;
+            a.vy[i] = vy;
+        }
+        if (w != w0) a.st[i] = w;
+        if (a.window) a.window[i] = w;
     }
 }
 
@@ -47,6 +214,13 @@ __global__ void kick_kernel(double *__restrict__ vx, double *__restrict__ vy, do
         vy[i] += (ay[i] + ey * f) * s;
         vz[i] += (az[i] + ez * f) * s;
     }
+}
+
+__global__ void window_kernel(const int32_t *__restrict__ st, const double *__restrict__ t_inj, int64_t n, double T,
+                              int32_t *__restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = t_inj[i] <= T ? st[i] : 0;
 }
 
 constexpr int kETile = 256;
@@ -116,18 +290,92 @@ int stream_grid(int64_t n) {
 
 }  // namespace
 
-sv_status drift(sv_ctx *c, double t_start, double h, const double *tb) {
-    drift_kernel<<<stream_grid(c->n), 256, 0, c->stream>>>(c->x, c->y, c->z, c->vx, c->vy, c->vz, c->status,
-                                                           c->t_inj, c->n, t_start, h, tb);
+sv_status events_reserve(sv_ctx *c) {
+    const int64_t want = std::max<int64_t>(65536, c->n);
+    if (c->d_events && c->ev_cap >= want) return SV_OK;
+    events_free(c);
+    SV_CK(c, cudaMalloc(&c->d_events, sizeof(sv_event) * want));
+    SV_CK(c, cudaMalloc(&c->d_ev_key, sizeof(unsigned long long) * want));
+    SV_CK(c, cudaMalloc(&c->d_ev_count, sizeof(unsigned long long)));
+    SV_CK(c, cudaMemsetAsync(c->d_ev_count, 0, sizeof(unsigned long long), c->stream));
+    c->ev_cap = want;
+    return SV_OK;
+}
+
+void events_free(sv_ctx *c) {
+    cudaFree(c->d_events);
+    cudaFree(c->d_ev_key);
+    cudaFree(c->d_ev_count);
+    c->d_events = nullptr;
+    c->d_ev_key = nullptr;
+    c->d_ev_count = nullptr;
+    c->ev_cap = 0;
+}
+
+sv_status drift(sv_ctx *c, double t_start, double h, int32_t *window, const double *tb, long long seq_base) {
+    const sv_boundary &B = c->B;
+    DriftArgs a{};
+    a.x = c->x; a.y = c->y; a.z = c->z;
+    a.vx = c->vx; a.vy = c->vy; a.vz = c->vz;
+    a.st = c->status;
+    a.t_inj = c->t_inj;
+    a.species = c->species;
+    a.window = window;
+    a.n = c->n;
+    a.t_start = t_start;
+    a.h = h;
+    a.tb = tb;
+    a.seq_base = tb ? seq_base : c->ev_seq;
+    a.crash = B.crash;
+    a.bc = B.bc;
+    a.fold = !B.fold ? 0 : c->pfold ? 3 : c->P.symmetry == SV_SYM_ROTATIONAL ? 1
+                              : c->P.symmetry == SV_SYM_TRANSLATIONAL ? 2 : 0;
+    a.pfold = c->pfold;
+    a.cz = B.crash_z; a.cw = B.crash_width; a.cr = B.crash_r;
+    a.bsx = B.bc_space[0]; a.bsy = B.bc_space[1]; a.bsz = B.bc_space[2]; a.bsr = B.bc_space[3];
+    a.bt = B.bc_time;
+    a.Lx = c->P.domain_size[0]; a.Ly = c->P.domain_size[1]; a.Lz = c->P.domain_size[2];
+    a.ax = c->P.sym_axes[0]; a.ay = c->P.sym_axes[1]; a.az = c->P.sym_axes[2];
+    a.ev = c->d_events;
+    a.ev_key = c->d_ev_key;
+    a.ev_count = c->d_ev_count;
+    a.ev_cap = c->ev_cap;
+    drift_kernel<<<stream_grid(c->n), 256, 0, c->stream>>>(a);
+    SV_LAUNCHED(c);
+    if (!tb) c->ev_seq++;
+    return SV_OK;
+}
+
+sv_status kick(sv_ctx *c, double t_start, double dt, const int32_t *st, const double *tb) {
+    kick_kernel<<<stream_grid(c->n), 256, 0, c->stream>>>(
+        c->vx, c->vy, c->vz, c->ax, c->ay, c->az, c->qom, st, c->t_inj, c->n, t_start, dt,
+        c->P.e_over_amu, c->P.efield[0], c->P.efield[1], c->P.efield[2], tb);
     SV_LAUNCHED(c);
     return SV_OK;
 }
 
-sv_status kick(sv_ctx *c, double t_start, double dt, const double *tb) {
-    kick_kernel<<<stream_grid(c->n), 256, 0, c->stream>>>(
-        c->vx, c->vy, c->vz, c->ax, c->ay, c->az, c->qom, c->status, c->t_inj, c->n, t_start, dt,
-        c->P.e_over_amu, c->P.efield[0], c->P.efield[1], c->P.efield[2], tb);
+sv_status window_status(sv_ctx *c, double t_window) {
+    window_kernel<<<stream_grid(c->n), 256, 0, c->stream>>>(c->status, c->t_inj, c->n, t_window, c->wstatus);
     SV_LAUNCHED(c);
+    return SV_OK;
+}
+
+sv_status leapfrog_step(sv_ctx *c, double ts, double dt, double *save_xh) {
+    const double h = 0.5 * dt;
+    if (c->B.crash != SV_CRASH_NONE || c->B.bc != SV_BC_NONE) SV_TRY(events_reserve(c));
+    SV_TRY(drift(c, ts, h, c->wstatus));
+    if (save_xh) {
+        const size_t b = sizeof(double) * c->n;
+        SV_CK(c, cudaMemcpyAsync(save_xh, c->x, b, cudaMemcpyDeviceToDevice, c->stream));
+        SV_CK(c, cudaMemcpyAsync(save_xh + c->n, c->y, b, cudaMemcpyDeviceToDevice, c->stream));
+        SV_CK(c, cudaMemcpyAsync(save_xh + 2 * c->n, c->z, b, cudaMemcpyDeviceToDevice, c->stream));
+    }
+    c->fstatus = c->wstatus;
+    const sv_status s = compute_accel_device(c, 0, c->n);
+    c->fstatus = nullptr;
+    SV_TRY(s);
+    SV_TRY(kick(c, ts, dt, c->wstatus));
+    SV_TRY(drift(c, ts + h, h, nullptr));
     return SV_OK;
 }
 

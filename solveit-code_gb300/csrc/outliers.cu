@@ -230,12 +230,12 @@ sv_status outliers_detect(sv_ctx *c, const int32_t **status_for_tree) {
     SV_TRY(reserve(c, O, n));
     const int g = div_up(n, 256);
     SV_CK(c, cudaMemsetAsync(O.count, 0, sizeof(int) * 2, c->stream));
-    count_sources_kernel<<<std::min(g, 16 * kNumSMs), 256, 0, c->stream>>>(c->status, n, O.count);
+    count_sources_kernel<<<std::min(g, 16 * kNumSMs), 256, 0, c->stream>>>(force_status(c), n, O.count);
     SV_LAUNCHED(c);
     const double *axis[3] = {c->x, c->y, c->z};
     for (int pass = 0; pass < 2; pass++) {
         for (int d = 0; d < 3; d++) {
-            axis_values_kernel<<<g, 256, 0, c->stream>>>(axis[d], c->status, n, pass ? O.stats + d : nullptr, O.keys);
+            axis_values_kernel<<<g, 256, 0, c->stream>>>(axis[d], force_status(c), n, pass ? O.stats + d : nullptr, O.keys);
             SV_LAUNCHED(c);
             size_t bytes = O.cub_bytes;
             SV_CK(c, cub::DeviceRadixSort::SortKeys(O.cub_tmp, bytes, O.keys, O.keys_alt, (int)n, 0, 32, c->stream));
@@ -245,7 +245,7 @@ sv_status outliers_detect(sv_ctx *c, const int32_t **status_for_tree) {
             SV_LAUNCHED(c);
         }
     }
-    flag_kernel<<<g, 256, 0, c->stream>>>(c->x, c->y, c->z, c->status, n, O.stats, O.flag, O.status2, O.list,
+    flag_kernel<<<g, 256, 0, c->stream>>>(c->x, c->y, c->z, force_status(c), n, O.stats, O.flag, O.status2, O.list,
                                           O.count);
     SV_LAUNCHED(c);
     SV_CK(c, cudaMemcpyAsync(O.h_count, O.count, sizeof(int) * 2, cudaMemcpyDeviceToHost, c->stream));
@@ -267,10 +267,10 @@ sv_status outliers_add(sv_ctx *c, int64_t first, int64_t last) {
     if (O.n_out == 0) return SV_OK;
     const int64_t n = c->n;
     outlier_sources_kernel<<<div_up(n, 256), 256, 0, c->stream>>>(
-        c->x, c->y, c->z, c->q, c->m, c->status, O.flag, O.list, O.n_out, n, first, last, c->P.softening2,
+        c->x, c->y, c->z, c->q, c->m, force_status(c), O.flag, O.list, O.n_out, n, first, last, c->P.softening2,
         c->P.k_const, c->ax, c->ay, c->az);
     SV_LAUNCHED(c);
-    outlier_targets_kernel<<<O.n_out, 256, 0, c->stream>>>(c->x, c->y, c->z, c->q, c->m, c->status, O.list, n,
+    outlier_targets_kernel<<<O.n_out, 256, 0, c->stream>>>(c->x, c->y, c->z, c->q, c->m, force_status(c), O.list, n,
                                                            first, last, c->P.softening2, c->P.k_const, c->ax,
                                                            c->ay, c->az);
     SV_LAUNCHED(c);

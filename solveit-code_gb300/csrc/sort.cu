@@ -251,7 +251,7 @@ sv_status sort_view(sv_ctx *c, const ParticleView &v, int64_t first, int64_t las
 }
 
 sv_status sort_state(sv_ctx *c, int64_t first, int64_t last) {
-    const ParticleView v{c->x, c->y, c->z, c->q, c->m, c->status, c->n, c->n, c->qom};
+    const ParticleView v{c->x, c->y, c->z, c->q, c->m, force_status(c), c->n, c->n, c->qom};
     return sort_view(c, v, first, last);
 }
 

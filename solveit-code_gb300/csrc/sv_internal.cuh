@@ -71,6 +71,19 @@ struct sv_ctx {
     double *q = nullptr, *m = nullptr, *t_inj = nullptr;
     double *qom = nullptr;  // q/m (0 where m <= 0), set at upload: no FP64 division per step
     int32_t *status = nullptr;
+    int32_t *species = nullptr;  // species code per particle (event records), 0xffffffff unknown
+    // status the force and the kick see: the injection-windowed copy during a
+    // leapfrog step (written by the first drift), else null (use status)
+    int32_t *wstatus = nullptr;
+    const int32_t *fstatus = nullptr;
+    // crash / boundary / folding applied after every drift, and the event log
+    sv_boundary B{};
+    sv_event *d_events = nullptr;
+    unsigned long long *d_ev_key = nullptr;  // file-order sort key per recorded event
+    unsigned long long *d_ev_count = nullptr;
+    int64_t ev_cap = 0;
+    long long ev_seq = 0;       // drifts issued so far (event order across calls)
+    const int8_t *pfold = nullptr;  // batch: per-particle folding (1 rotational plume), else null
     // last acceleration (force only), caller order, FP64
     double *ax = nullptr, *ay = nullptr, *az = nullptr;
     bool have_state = false, have_accel = false;
@@ -188,8 +201,24 @@ void batch_free(sv_ctx *c);
 
 // integrate.cu.  With tb (device {t0, dt, k}), the step's start time
 // t0 + dt * k is added to t_start on the device (CUDA-graph replays).
-sv_status drift(sv_ctx *c, double t_start, double h, const double *tb = nullptr);
-sv_status kick(sv_ctx *c, double t_start, double dt, const double *tb = nullptr);
+// Half-step drift over [t_start, t_start + h] with the injection window, the
+// crash test, folding and boundary conditions of c->B.  window != null
+// receives the status the following force and kick see (0 outside the
+// window).  With tb (device {t0, dt, k}) t_start is taken relative to
+// tb[0] + tb[1] * tb[2] and the event order from seq_base + 2 * tb[2].
+sv_status drift(sv_ctx *c, double t_start, double h, int32_t *window, const double *tb = nullptr,
+                long long seq_base = 0);
+// Kick over [t_start, t_start + dt] of the particles with st == 1 (st: the
+// windowed status of the step).
+sv_status kick(sv_ctx *c, double t_start, double dt, const int32_t *st, const double *tb = nullptr);
+// One DKD step of sv_leapfrog on a single-plume context (save_xh: mid-step positions, 3n, or null).
+sv_status leapfrog_step(sv_ctx *c, double ts, double dt, double *save_xh = nullptr);
+// status as the force sees it (windowed during a leapfrog step)
+inline const int32_t *force_status(const sv_ctx *c) { return c->fstatus ? c->fstatus : c->status; }
+// wstatus[i] = status[i] if t_inj[i] <= t_window else 0 (adjoint re-runs)
+sv_status window_status(sv_ctx *c, double t_window);
+sv_status events_reserve(sv_ctx *c);
+void events_free(sv_ctx *c);
 sv_status energy(sv_ctx *c, double *ke, double *pe);
 
 // image offsets (metres) of the translational lattice, in summation order

@@ -20,6 +20,8 @@ DIRECT, BARNES_HUT, FMM = 0, 1, 2
 SYM_NONE, SYM_ROTATIONAL, SYM_TRANSLATIONAL = 0, 1, 2
 MIXED, FP64 = 0, 1
 FMM_FMM, FMM_OUTLIERS, TREECODE, TREECODE_OUTLIERS = 0, 1, 2, 3
+CRASH_NONE, CRASH_EXTRACTOR_GRID = 0, 1
+BC_NONE, BC_SPACE, BC_TIME, BC_SPACE_AND_TIME = 0, 1, 2, 3
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "allocation failed", 4: "bad state",
           5: "capacity exceeded", 6: "device wait timed out", 7: "unsupported"}
@@ -31,7 +33,7 @@ ABI_SYMBOLS = (
     "sv_leapfrog", "sv_energy", "sv_compare_accel", "sv_get_stats", "sv_sync", "sv_stream",
     "sv_launch_count", "sv_last_error", "sv_abi_version", "sv_adjoint_forward", "sv_adjoint_backward",
     "sv_direct_accel_noalloc", "sv_upload_batch", "sv_batch_tune", "sv_batch_get_info", "sv_batch_set_tuning",
-    "sv_get_outliers",
+    "sv_get_outliers", "sv_set_boundary", "sv_get_boundary", "sv_get_events",
 )
 
 
@@ -64,6 +66,19 @@ class BatchInfo(C.Structure):
         ("level_boxes", C.c_int32 * 22), ("level_cap", C.c_int32 * 22), ("level_max", C.c_int32 * 22),
         ("max_leaf", C.c_int32), ("reserved", C.c_int32 * 5),
     ]
+
+
+class Boundary(C.Structure):
+    _fields_ = [
+        ("crash", C.c_int32), ("bc", C.c_int32), ("crash_z", C.c_double), ("crash_width", C.c_double),
+        ("crash_r", C.c_double), ("bc_space", C.c_double * 4), ("bc_time", C.c_double), ("fold", C.c_int32),
+        ("reserved", C.c_int32 * 7),
+    ]
+
+
+# the 40-byte events-file record (ChargedParticles::writeToEventsFile, particles.cpp:666-684)
+EVENT_DTYPE = np.dtype([("time", "<f4"), ("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("vx", "<f4"), ("vy", "<f4"),
+                        ("vz", "<f4"), ("index", "<i4"), ("species", "<u4"), ("status", "<i4")])
 
 
 class SolveitError(RuntimeError):
@@ -118,6 +133,9 @@ def load(path: str = LIB_PATH):
     L.sv_batch_get_info.argtypes = [vp, C.POINTER(BatchInfo)]
     L.sv_batch_set_tuning.argtypes = [vp, C.c_int32, C.c_int32]
     L.sv_get_outliers.argtypes = [vp, vp, C.POINTER(C.c_int64)]
+    L.sv_set_boundary.argtypes = [vp, C.POINTER(Boundary)]
+    L.sv_get_boundary.argtypes = [vp, C.POINTER(Boundary)]
+    L.sv_get_events.argtypes = [vp, vp, C.c_int64, C.POINTER(C.c_int64)]
     for name in ABI_SYMBOLS:
         if name not in ("sv_destroy", "sv_stream", "sv_launch_count", "sv_last_error", "sv_abi_version"):
             getattr(L, name).restype = C.c_int
@@ -257,6 +275,25 @@ class ForceMethod:
 
     def leapfrog(self, nsteps, dt, t0=0.0):
         self._check(self.L.sv_leapfrog(self.h, nsteps, dt, t0))
+
+    def set_boundary(self, crash=CRASH_NONE, crash_z=0.0, crash_width=0.0, crash_r=0.0, bc=BC_NONE,
+                     bc_space=(0.0, 0.0, 0.0, 0.0), bc_time=0.0, fold=0):
+        b = Boundary()
+        b.crash, b.crash_z, b.crash_width, b.crash_r = crash, crash_z, crash_width, crash_r
+        b.bc, b.bc_time, b.fold = bc, bc_time, fold
+        for k in range(4):
+            b.bc_space[k] = bc_space[k]
+        self._check(self.L.sv_set_boundary(self.h, C.byref(b)))
+
+    def events(self):
+        """Events recorded since the last call (structured array of EVENT_DTYPE, file order)."""
+        cnt = C.c_int64()
+        rc = self.L.sv_get_events(self.h, None, 0, C.byref(cnt))
+        if rc not in (0, 5):
+            self._check(rc)
+        out = np.zeros(cnt.value, EVENT_DTYPE)
+        self._check(self.L.sv_get_events(self.h, out.ctypes.data if len(out) else None, len(out), C.byref(cnt)))
+        return out
 
     def adjoint_forward(self, nsteps, dt, t0=0.0, checkpoint_every=10):
         self._check(self.L.sv_adjoint_forward(self.h, nsteps, dt, t0, checkpoint_every))

@@ -20,6 +20,11 @@ Fixtures (all FP32 vec4 arrays in the reference layout):
                     1e-20 m^2, direct force).
   bh_n4096.npz      Barnes-Hut theta 0.5 (reference tree: 1 particle/leaf).
   fmm_n4096.npz     FMM p = 8 (reference uniform-depth rotation FMM).
+  drift_bc.npz      10 LeapfrogDKD steps with staggered injection (the
+                    driftNew window), the extractor-grid crash test, spatial
+                    and temporal boundary conditions, rotational and
+                    translational folding, and the events file
+                    (``python tests/golden/make_golden.py drift_bc``).
 """
 from __future__ import annotations
 
@@ -55,7 +60,12 @@ def run_ref(variant, mode, pos4, vel4, acc4, tinj, **kw):
         if mode == "outliers":
             raw = np.fromfile(fout, np.int32)
             return raw[1:].copy(), int(raw[0])
-        out = np.fromfile(fout, np.float32).reshape(3, n, 4)
+        raw = np.fromfile(fout, np.uint8)
+        out = raw[:48 * n].view(np.float32).reshape(3, n, 4)
+        if kw.get("events"):
+            cnt = int(raw[48 * n:48 * n + 4].view(np.int32)[0])
+            ev = raw[48 * n + 4:48 * n + 4 + 40 * cnt].copy()
+            return out[0].copy(), out[1].copy(), out[2].copy(), ev
     return out[0].copy(), out[1].copy(), out[2].copy()
 
 
@@ -112,8 +122,48 @@ def outliers():
                            for name, v in zip(("pos4", "vel4", "acc4", "tinj", "flags", "count"), c)})
 
 
+# staggered injection: groups of 32 injected 1 ps apart (sorted, the first at 0)
+DRIFT_BC_CASES = {
+    # name: (sym, plume x offset, reference keys)
+    "plain": (0, 0.0, dict(crash=1, cz=5e-7, cw=1e-7, cr=1e-8, bc=3, bz=9e-7, br=2.5e-8, bt=5.25e-12)),
+    "rot": (1, 0.0, dict(crash=1, cz=5e-7, cw=1e-7, cr=1e-8, bc=1, bz=9e-7, br=2.5e-8)),
+    "trans": (2, 9.95e-7, dict()),
+}
+
+
+def drift_bc_state(sym, xoff, seed=9010, n=256):
+    st = plume.make_plume(n, 1e-6, seed)
+    st["x"][:, 0] += xoff
+    st["t_inj"][:] = np.floor(np.arange(n) / 32) * 1e-12
+    st["status"][[17, 90, 201]] = 2  # source-only particles
+    return st
+
+
+def drift_bc():
+    """The reference's own drift, crash, folding and boundary code on a plume
+    that crosses the grid, leaves the bounds and is injected in groups."""
+    out = {}
+    for name, (sym, xoff, keys) in DRIFT_BC_CASES.items():
+        st = drift_bc_state(sym, xoff)
+        pos4, vel4, acc4, tinj = plume.to_ref32(st)
+        extra = dict(levels=2, axes="110", dom="2e-6,2e-6,0") if sym == 2 else {}
+        p, v, a, ev = run_ref("eps20", "dkd", pos4, vel4, acc4, tinj, threads=4, steps=10, dt=1e-12, ez=1e8,
+                              sym=sym, events=1, **keys, **extra)
+        out.update({f"{name}_pos4": pos4, f"{name}_vel4": vel4, f"{name}_acc4": acc4, f"{name}_tinj": tinj,
+                    f"{name}_pos4_out": p, f"{name}_vel4_out": v, f"{name}_acc4_out": a, f"{name}_events": ev})
+        print(name, "events", len(ev) // 40, "crashed", int((a[:, 3] == -1).sum()), "out",
+              int((a[:, 3] == 0).sum()))
+    st = drift_bc_state(0, 0.0)
+    lattice = run_ref("eps20", "grid", *plume.to_ref32(st), levels=2, axes="110")
+    np.savez_compressed(os.path.join(HERE, "drift_bc.npz"), steps=np.int32(10), dt=np.float32(1e-12),
+                        ez=np.float32(1e8), eps=np.float64(1e-20), lattice=lattice.astype(np.int32),
+                        domain=np.array([2e-6, 2e-6, 0.0], np.float32), **out)
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["outliers"]:
         outliers()
+    elif sys.argv[1:] == ["drift_bc"]:
+        drift_bc()
     else:
         main()
