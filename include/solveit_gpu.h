@@ -238,6 +238,36 @@ typedef struct {
  * next call returns SV_ERR_CAPACITY with count = events recorded + dropped. */
 SV_API sv_status sv_get_events(sv_ctx *ctx, sv_event *out, int64_t cap, int64_t *count);
 
+/* Background field of a single emitter (BackgroundEfield::singleEmitter), as
+ * InterpolationScheme::computeEfieldSingleEmitter (interpolation_scheme.cpp:
+ * 206-262) evaluates it from the field map the reference reads from its
+ * Fields and Triangles files (fillInterpolationScheme / fillTriangleScheme,
+ * interpolation_scheme.cpp:66-150):
+ *   node_rz    2 n_nodes: (r, z) of the nodes in units of r0
+ *   e_r, e_z   n_nodes: the field's radial and axial components in units of e0
+ *   triangles  3 n_triangles node indices
+ *   neighbors  3 n_triangles: the triangle across the edge opposite each
+ *              vertex, -1 on the hull
+ * At a particle (x, y, z), (r, z) = (sqrt(x^2 + y^2), z) / r0; for z outside
+ * [0, z_max] there is no field (the reference uses z_max = 140).  Otherwise the
+ * triangle holding (r, z) is found by the walk of triangulation_search_delaunay
+ * (pwl_interp_2d_scattered.c:1762-1992; outside the hull the field is
+ * extrapolated from the triangle where the walk stops), E_r and E_z are
+ * interpolated linearly in it (pwl_interp_2d_scattered_value, :887-957), and
+ * E = e0 (E_r x/r, E_r y/r, E_z).  sv_leapfrog's kick adds (e/amu)(q/m) E for
+ * inbound particles (computeBackgroundAcceleration, particles.cpp:496-520),
+ * with sv_params.efield on top.  Each particle's walk starts from its triangle
+ * of the previous kick.  n_nodes = 0 removes the map.  A walk that does not end
+ * (a triangulation with a cycle) or a degenerate triangle makes sv_leapfrog
+ * return SV_ERR_INVALID. */
+SV_API sv_status sv_set_emitter_field(sv_ctx *ctx, int32_t n_nodes, const double *node_rz, const double *e_r,
+                                      const double *e_z, int32_t n_triangles, const int32_t *triangles,
+                                      const int32_t *neighbors, double r0, double e0, double z_max);
+/* The emitter field in V/m at n points (x3, e3: 3n interleaved, host); each
+ * walk starts from the middle triangle, (n_triangles + 1)/2 - 1, as the
+ * reference's first search does. */
+SV_API sv_status sv_emitter_field_at(sv_ctx *ctx, int64_t n, const double *x3, double *e3);
+
 /* Adjoint of sv_leapfrog with the direct sum (no reference counterpart: the
  * reference integrates forward only).  sv_adjoint_forward runs nsteps like
  * sv_leapfrog and keeps the state every checkpoint_every steps;

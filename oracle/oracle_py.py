@@ -54,9 +54,11 @@ def lib():
                                        C.c_double, C.c_double, C.c_double, C.c_double, _f64p, C.c_int,
                                        C.c_int, C.c_void_p, C.c_void_p, C.c_int]
         L.orc_leapfrog_ref32_bc.argtypes = L.orc_leapfrog_ref32.argtypes[:-1] + [
-            C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_int]
+            C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_int]
         L.orc_leapfrog_f64_bc.argtypes = L.orc_leapfrog_f64.argtypes[:-2] + [
-            C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_int]
+            C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_int]
+        L.orc_emitter_field_ref32.argtypes = [C.c_void_p, C.c_int, _f32p, _f32p, C.POINTER(C.c_int)]
+        L.orc_emitter_field_f64.argtypes = [C.c_void_p, C.c_int64, _f64p, _f64p]
         L.orc_energy_f64.argtypes = [C.c_int64, _f64p, _f64p, _f64p, _f64p, C.c_double,
                                      C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int]
         L.orc_rel_l2.argtypes = [C.c_int64, _f64p, _f64p, C.c_void_p, C.POINTER(C.c_double),
@@ -187,8 +189,42 @@ def boundary(crash=0, crash_z=0.0, crash_width=0.0, crash_r=0.0, bc=0, bc_space=
     return b
 
 
+class Field(C.Structure):
+    """orc_field: a single emitter's field map (keeps its arrays alive)."""
+    _fields_ = [("n_nodes", C.c_int), ("n_tri", C.c_int), ("node_rz", C.c_void_p), ("er", C.c_void_p),
+                ("ez", C.c_void_p), ("tri", C.c_void_p), ("nbr", C.c_void_p), ("r0", C.c_double),
+                ("e0", C.c_double), ("zmax", C.c_double)]
+
+
+def field(node_rz, e_r, e_z, triangles, neighbors, r0, e0, zmax=140.0):
+    f = Field()
+    f._keep = [np.ascontiguousarray(node_rz, np.float64), np.ascontiguousarray(e_r, np.float64),
+               np.ascontiguousarray(e_z, np.float64), np.ascontiguousarray(triangles, np.int32),
+               np.ascontiguousarray(neighbors, np.int32)]
+    f.n_nodes, f.n_tri = f._keep[1].size, f._keep[3].size // 3
+    f.node_rz, f.er, f.ez, f.tri, f.nbr = (a.ctypes.data for a in f._keep)
+    f.r0, f.e0, f.zmax = r0, e0, zmax
+    return f
+
+
+def emitter_field_ref32(fld, pos4):
+    """InterpolationScheme::Efield at each particle in index order (FP32)."""
+    p = np.ascontiguousarray(pos4, np.float32)
+    out = np.zeros(3 * p.shape[0], np.float32)
+    save = C.c_int(-1)
+    lib().orc_emitter_field_ref32(C.byref(fld), p.shape[0], p.reshape(-1), out, C.byref(save))
+    return out.reshape(-1, 3)
+
+
+def emitter_field_f64(fld, x3):
+    x = np.ascontiguousarray(x3, np.float64)
+    out = np.zeros(x.size, np.float64)
+    lib().orc_emitter_field_f64(C.byref(fld), x.shape[0], x.reshape(-1), out)
+    return out.reshape(-1, 3)
+
+
 def leapfrog_ref32_bc(pos4, vel4, acc4, t_inj, nsteps, dt, eps, efield=(0.0, 0.0, 0.0), sym=0, bd=None,
-                      images=None, domain_size=(2e-6, 2e-6, 0.0), threads=0, ev_cap=1 << 16):
+                      images=None, domain_size=(2e-6, 2e-6, 0.0), threads=0, ev_cap=1 << 16, fld=None):
     """The reference's loop with its injection window, crash test, folding and
     boundary conditions: (pos4, vel4, acc4, events)."""
     p = np.ascontiguousarray(pos4, np.float32).copy()
@@ -202,12 +238,13 @@ def leapfrog_ref32_bc(pos4, vel4, acc4, t_inj, nsteps, dt, eps, efield=(0.0, 0.0
     cnt = C.c_int()
     lib().orc_leapfrog_ref32_bc(p.shape[0], p, v, a, t, nsteps, dt, eps, e, sym, nimg, _ptr(img),
                                 np.asarray(domain_size, np.float32), None if bd is None else C.byref(bd),
-                                ev.ctypes.data, ev_cap, C.byref(cnt), threads)
+                                None if fld is None else C.byref(fld), ev.ctypes.data, ev_cap, C.byref(cnt),
+                                threads)
     return p, v, a, ev[:min(cnt.value, ev_cap)].copy()
 
 
 def leapfrog_f64_bc(state, nsteps, dt, eps2, efield=(0.0, 0.0, 0.0), t0=0.0, sym=0, img_off=None, bd=None,
-                    threads=0, ev_cap=1 << 16):
+                    threads=0, ev_cap=1 << 16, fld=None):
     """FP64 DKD with the window, crash, folding and boundary conditions:
     (x, v, status, events)."""
     x = np.ascontiguousarray(state["x"], np.float64).reshape(-1).copy()
@@ -222,8 +259,8 @@ def leapfrog_f64_bc(state, nsteps, dt, eps2, efield=(0.0, 0.0, 0.0), t0=0.0, sym
                               np.ascontiguousarray(state["m"], np.float64), st,
                               np.ascontiguousarray(state["t_inj"], np.float64), nsteps, dt, t0, eps2,
                               k_const(), np.asarray(efield, np.float64), sym, nimg, _ptr(io),
-                              None if bd is None else C.byref(bd), ev.ctypes.data, ev_cap, C.byref(cnt),
-                              threads)
+                              None if bd is None else C.byref(bd), None if fld is None else C.byref(fld),
+                              ev.ctypes.data, ev_cap, C.byref(cnt), threads)
     return x.reshape(n, 3), v.reshape(n, 3), st, ev[:min(cnt.value, ev_cap)].copy()
 
 

@@ -17,7 +17,11 @@
 //          dkd only: crash (1 extractor grid), cz, cw, cr (z_distance,
 //          z_width, r_distance), bc (BoundaryConditionOptions 0..3), bx, by,
 //          bz, br (spatial limits), bt (temporal limit), events (1: append the
-//          events file)
+//          events file);
+//          efield and dkd: fdir (folder, with its trailing /), fnodes, ftris
+//          (the Fields / Triangles files in the reference's CSV format), r0, e0:
+//          a singleEmitter background field (dkd: replaces ez)
+//   mode efield: InterpolationScheme::Efield at each particle, float e[3n]
 // in.bin : int32 n, float pos4[4n], float vel4[4n], float acc4[4n], float tinj[n]
 // out.bin: float pos4[4n], float vel4[4n], float acc4[4n]
 //          (dkd with events=1: then int32 count, count 40-byte event records
@@ -54,6 +58,7 @@ int main(int argc, char **argv) {
     }
     std::string mode = argv[1];
     auto kv = parse_kv(argc, argv, 4);
+    const bool field = kv.count("fdir") > 0;
     const int threads = (int)getd(kv, "threads", 1);
     const int sym = (int)getd(kv, "sym", 0);
     const int levels = (int)getd(kv, "levels", 2);
@@ -95,6 +100,26 @@ int main(int argc, char **argv) {
     }
     cp.firstParticle = 0;
     cp.lastParticle = n;
+    if (field) {
+        // ParticleSystem::initializeBackgroundEField (particles.cpp:452-463)
+        ps.params.r0 = (float)getd(kv, "r0", 1.0);
+        ps.params.E0 = (float)getd(kv, "e0", 1.0);
+        ps.initializeBackgroundEField(BackgroundEfield::singleEmitter, kv["fdir"].c_str(), kv["fnodes"].c_str(),
+                                      kv["ftris"].c_str());
+    }
+
+    if (mode == "efield") {
+        FILE *fo = std::fopen(argv[3], "wb");
+        if (!fo) return 3;
+        for (int i = 0; i < n; i++) {
+            vec3<float> e = ps.interpScheme.Efield(cp.position[i].x, cp.position[i].y, cp.position[i].z);
+            const float v[3] = {e.x, e.y, e.z};
+            std::fwrite(v, 4, 3, fo);
+        }
+        std::fclose(fo);
+        std::fflush(nullptr);
+        std::_Exit(0);
+    }
 
     if (mode == "outliers") {
         std::vector<int> check(n, 0);
@@ -202,14 +227,18 @@ int main(int argc, char **argv) {
             tpos += dt / 2;
             cp.zeroAcceleration();
             fm->updateAcceleration();
-            for (int i = cp.firstParticle; i < cp.lastParticle; i++) {
-                if (cp.acceleration[i].w != inbound) continue;
-                float efactor = factor * cp.position[i].w / cp.getMass(i);
-                vec3<float> e(0.0f, 0.0f, ez);
-                e *= efactor;
-                cp.acceleration[i].x += e.x;
-                cp.acceleration[i].y += e.y;
-                cp.acceleration[i].z += e.z;
+            if (field) {
+                ps.computeBackgroundAcceleration();
+            } else {
+                for (int i = cp.firstParticle; i < cp.lastParticle; i++) {
+                    if (cp.acceleration[i].w != inbound) continue;
+                    float efactor = factor * cp.position[i].w / cp.getMass(i);
+                    vec3<float> e(0.0f, 0.0f, ez);
+                    e *= efactor;
+                    cp.acceleration[i].x += e.x;
+                    cp.acceleration[i].y += e.y;
+                    cp.acceleration[i].z += e.z;
+                }
             }
             ps.propagateVelocityNew(tvel, dt);
             drift_new(tpos, dt / 2);

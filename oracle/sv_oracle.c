@@ -543,6 +543,111 @@ static double wrap_f64(double p, double L) {
     return temp < 0 ? temp + L / 2 : temp - L / 2;
 }
 
+/* triangulation_search_delaunay (pwl_interp_2d_scattered.c:1762-1992): walk
+ * from *t to the triangle holding p; returns it (or -1 at a dead end) and the
+ * barycentric coordinates; *t keeps the start for the next search when the
+ * walk ended normally (the reference's triangle_index_save). */
+static int field_walk(const orc_field *f, const double p[2], int *t, double *al, double *be, double *ga) {
+    int ti = (*t < 0 || f->n_tri <= *t) ? (f->n_tri + 1) / 2 - 1 : *t;
+    for (int step = 0;; step++) {
+        if (f->n_tri < step) return -1;
+        const int a = f->tri[3 * ti], b = f->tri[3 * ti + 1], c = f->tri[3 * ti + 2];
+        const double dxa = f->node_rz[2 * a] - f->node_rz[2 * c];
+        const double dya = f->node_rz[2 * a + 1] - f->node_rz[2 * c + 1];
+        const double dxb = f->node_rz[2 * b] - f->node_rz[2 * c];
+        const double dyb = f->node_rz[2 * b + 1] - f->node_rz[2 * c + 1];
+        const double dxp = p[0] - f->node_rz[2 * c];
+        const double dyp = p[1] - f->node_rz[2 * c + 1];
+        const double det = dxa * dyb - dya * dxb;
+        *al = (dxp * dyb - dyp * dxb) / det;
+        *be = (dxa * dyp - dya * dxp) / det;
+        *ga = 1.0 - *al - *be;
+        if (0.0 <= *al && 0.0 <= *be && 0.0 <= *ga) break;
+        if (*al < 0.0 && 0 <= f->nbr[3 * ti]) {
+            ti = f->nbr[3 * ti];
+            continue;
+        } else if (*be < 0.0 && 0 <= f->nbr[3 * ti + 1]) {
+            ti = f->nbr[3 * ti + 1];
+            continue;
+        } else if (*ga < 0.0 && 0 <= f->nbr[3 * ti + 2]) {
+            ti = f->nbr[3 * ti + 2];
+            continue;
+        }
+        if (*al < 0.0 || *be < 0.0 || *ga < 0.0) break; /* outside the hull */
+        return -1;
+    }
+    *t = ti;
+    return ti;
+}
+
+/* pwl_interp_2d_scattered_value (pwl_interp_2d_scattered.c:887-957), one point */
+static double field_value(const orc_field *f, const double *zd, int t, double al, double be, double ga) {
+    return al * zd[f->tri[3 * t]] + be * zd[f->tri[3 * t + 1]] + ga * zd[f->tri[3 * t + 2]];
+}
+
+/* InterpolationScheme::computeEfieldSingleEmitter (interpolation_scheme.cpp:206-262) */
+static void efield_ref32(const orc_field *f, float x, float y, float z, int *save, float out[3]) {
+    const long double PI = 3.14159265358979323846264338328L;
+    const float r0 = (float)f->r0, e0 = (float)f->e0;
+    float phi = atanf(y / x);
+    if (x < 0) phi = (float)((long double)phi + PI);
+    if (x == 0 && y != 0)
+        phi = (float)(PI / 2);
+    else if (x == 0 && y == 0)
+        phi = 0;
+    x /= r0;
+    y /= r0;
+    z /= r0;
+    float e[3] = {0, 0, 0};
+    double coords[2];
+    coords[0] = (double)sqrt((double)(x * x + y * y));
+    coords[1] = (double)z;
+    if (!(z < 0 || z > (float)f->zmax)) {
+        double al, be, ga;
+        int t = field_walk(f, coords, save, &al, &be, &ga);
+        const double ri = t < 0 ? -1.0 : field_value(f, f->er, t, al, be, ga);
+        t = field_walk(f, coords, save, &al, &be, &ga);
+        const double zi = t < 0 ? -1.0 : field_value(f, f->ez, t, al, be, ga);
+        e[0] = (float)ri;
+        e[0] *= cosf(phi);
+        e[1] = (float)ri;
+        e[1] *= sinf(phi);
+        e[2] = (float)zi;
+    }
+    for (int d = 0; d < 3; d++) out[d] = (float)((double)e[d] * (double)e0);
+}
+
+void orc_emitter_field_ref32(const orc_field *f, int n, const float *pos4, float *e3, int *save) {
+    for (int i = 0; i < n; i++) efield_ref32(f, pos4[4 * i], pos4[4 * i + 1], pos4[4 * i + 2], save, &e3[3 * i]);
+}
+
+static void efield_f64(const orc_field *f, const double *x, double out[3]) {
+    out[0] = out[1] = out[2] = 0.0;
+    const double pz = x[2] / f->r0;
+    if (pz < 0.0 || pz > f->zmax) return;
+    const double rr = sqrt(x[0] * x[0] + x[1] * x[1]);
+    const double p[2] = {rr / f->r0, pz};
+    int t = -1;
+    double al, be, ga;
+    if (field_walk(f, p, &t, &al, &be, &ga) < 0) return;
+    const double fr = field_value(f, f->er, t, al, be, ga), fz = field_value(f, f->ez, t, al, be, ga);
+    double c = 1.0, sn = 0.0;
+    if (x[0] == 0.0) {
+        c = x[1] != 0.0 ? 0.0 : 1.0;
+        sn = x[1] != 0.0 ? 1.0 : 0.0;
+    } else {
+        c = x[0] / rr;
+        sn = x[1] / rr;
+    }
+    out[0] = f->e0 * fr * c;
+    out[1] = f->e0 * fr * sn;
+    out[2] = f->e0 * fz;
+}
+
+void orc_emitter_field_f64(const orc_field *f, int64_t n, const double *x3, double *e3) {
+    for (int64_t i = 0; i < n; i++) efield_f64(f, &x3[3 * i], &e3[3 * i]);
+}
+
 /* ParticleSystem::propagatePositionNew (particles.cpp:33-40) for the charged
  * particles of [first, last), FP32: drift with the crash test
  * (particles.cpp:693-739), symmetry folding (particles.cpp:199-333; sym 1
@@ -634,14 +739,14 @@ void orc_leapfrog_ref32_bc(int n, float *pos4, float *vel4, float *acc4,
                            const float *t_inj, int nsteps, float dt, double eps,
                            const float efield[3], int sym, int nimg,
                            const int *images, const float domain_size[3],
-                           const orc_boundary *bd, orc_event *ev, int ev_cap,
-                           int *ev_count, int nthreads) {
+                           const orc_boundary *bd, const orc_field *field,
+                           orc_event *ev, int ev_cap, int *ev_count, int nthreads) {
     /* LeapfrogDKD::runSimulation (integration_schemes.cpp:856-891):
      * driftNew(dt/2), kick(dt), driftNew(dt/2) per step; driftNew
      * (integration_schemes.cpp:705-723) sets lastParticle from the injection
      * times, drifts, then moves firstParticle past inactive particles. */
     const float factor = REF_ELEM_CHARGE / REF_AMU;
-    int first = 0, last = 0, cnt = 0;
+    int first = 0, last = 0, cnt = 0, save = -1;
     for (int it = 1; it <= nsteps; it++) {
         float tpos = dt * (float)(it - 1);
         float tvel = dt * (float)(it - 1);
@@ -665,8 +770,10 @@ void orc_leapfrog_ref32_bc(int n, float *pos4, float *vel4, float *acc4,
             if (acc4[4 * i + 3] != 1.0f) continue;
             long double m = species_mass_ld((int)vel4[4 * i + 3]);
             float ef = (float)((double)factor * (double)pos4[4 * i + 3] / m);
+            float ev3[3] = {efield[0], efield[1], efield[2]};
+            if (field) efield_ref32(field, pos4[4 * i], pos4[4 * i + 1], pos4[4 * i + 2], &save, ev3);
             for (int d = 0; d < 3; d++) {
-                float e = (float)((double)efield[d] * (double)ef);
+                float e = (float)((double)ev3[d] * (double)ef);
                 acc4[4 * i + d] += e;
             }
         }
@@ -694,7 +801,7 @@ void orc_leapfrog_ref32(int n, float *pos4, float *vel4, float *acc4,
                         const int *images, const float domain_size[3],
                         int nthreads) {
     orc_leapfrog_ref32_bc(n, pos4, vel4, acc4, t_inj, nsteps, dt, eps, efield, sym, nimg, images, domain_size,
-                          NULL, NULL, 0, NULL, nthreads);
+                          NULL, NULL, NULL, 0, NULL, nthreads);
 }
 
 static uint32_t species_of_mass(double m) {
@@ -775,7 +882,8 @@ static void drift_f64(int64_t n, double *x, double *v, const double *m, int32_t 
 static void leapfrog_f64(int64_t n, double *x, double *v, const double *q, const double *m, int32_t *status,
                          const double *t_inj, int nsteps, double dt, double t0, double eps2, double kconst,
                          const double efield[3], int sym, int nimg, const double *img_off, const orc_boundary *bd,
-                         orc_event *ev, int ev_cap, int *ev_count, double *a_out, int nthreads) {
+                         const orc_field *field, orc_event *ev, int ev_cap, int *ev_count, double *a_out,
+                         int nthreads) {
     double *a = (double *)malloc(sizeof(double) * 3 * (size_t)(n > 0 ? n : 1));
     int32_t *win = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n > 0 ? n : 1));
     const double eoa = orc_e_over_amu();
@@ -792,8 +900,10 @@ static void leapfrog_f64(int64_t n, double *x, double *v, const double *q, const
             const double ef = eoa * q[i] / m[i];
             double s = ts + dt - t_inj[i];
             s = s < 0 ? 0 : (s > dt ? dt : s);
+            double e3[3] = {0.0, 0.0, 0.0};
+            if (field) efield_f64(field, &x[3 * i], e3);
             for (int d = 0; d < 3; d++) {
-                a[3 * i + d] += efield[d] * ef;
+                a[3 * i + d] += (efield[d] + e3[d]) * ef;
                 v[3 * i + d] += a[3 * i + d] * s;
             }
         }
@@ -810,9 +920,10 @@ void orc_leapfrog_f64_bc(int64_t n, double *x, double *v, const double *q,
                          int nsteps, double dt, double t0, double eps2,
                          double kconst, const double efield[3], int sym, int nimg,
                          const double *img_off, const orc_boundary *bd,
-                         orc_event *ev, int ev_cap, int *ev_count, int nthreads) {
-    leapfrog_f64(n, x, v, q, m, status, t_inj, nsteps, dt, t0, eps2, kconst, efield, sym, nimg, img_off, bd, ev,
-                 ev_cap, ev_count, NULL, nthreads);
+                         const orc_field *field, orc_event *ev, int ev_cap,
+                         int *ev_count, int nthreads) {
+    leapfrog_f64(n, x, v, q, m, status, t_inj, nsteps, dt, t0, eps2, kconst, efield, sym, nimg, img_off, bd,
+                 field, ev, ev_cap, ev_count, NULL, nthreads);
 }
 
 void orc_leapfrog_f64(int64_t n, double *x, double *v, const double *q,
@@ -821,7 +932,7 @@ void orc_leapfrog_f64(int64_t n, double *x, double *v, const double *q,
                       double kconst, const double efield[3], int sym, int nimg,
                       const double *img_off, double *a_out, int nthreads) {
     leapfrog_f64(n, x, v, q, m, status, t_inj, nsteps, dt, t0, eps2, kconst, efield, sym, nimg, img_off, NULL,
-                 NULL, 0, NULL, a_out, nthreads);
+                 NULL, NULL, 0, NULL, a_out, nthreads);
 }
 
 /* ---- energy ------------------------------------------------------------ */

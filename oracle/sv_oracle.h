@@ -123,6 +123,28 @@ typedef struct {
     int32_t status;
 } orc_event;
 
+/* Field map of a single emitter (InterpolationScheme, interpolation_scheme.cpp:
+ * 66-262): node (r, z) in units of r0, field components in units of e0, a
+ * triangulation and its neighbour table (the triangle across the edge
+ * opposite each vertex, -1 on the hull). */
+typedef struct {
+    int n_nodes, n_tri;
+    const double *node_rz;   /* 2 n_nodes */
+    const double *er, *ez;   /* n_nodes */
+    const int *tri, *nbr;    /* 3 n_tri each */
+    double r0, e0, zmax;     /* the reference: zmax = 140 */
+} orc_field;
+
+/* InterpolationScheme::Efield for a singleEmitter map at the FP32 positions of
+ * pos4, in index order, FP32 out (3n), as the reference evaluates it:
+ * triangulation_search_delaunay's walk starts where the previous search
+ * ended (its static triangle_index_save; *save = -1 before the first call). */
+void orc_emitter_field_ref32(const orc_field *f, int n, const float *pos4, float *e3, int *save);
+
+/* The same field in FP64 at FP64 points (3n), each walk starting from the
+ * middle triangle, E = e0 (E_r x/r, E_r y/r, E_z). */
+void orc_emitter_field_f64(const orc_field *f, int64_t n, const double *x3, double *e3);
+
 /* orc_leapfrog_ref32 with the crash test, folding and boundary conditions of
  * bd (nullable; the folding follows sym as the reference's does), on the
  * reference's [firstParticle, lastParticle) window (LeapfrogDKD::driftNew,
@@ -132,18 +154,22 @@ void orc_leapfrog_ref32_bc(int n, float *pos4, float *vel4, float *acc4,
                            const float *t_inj, int nsteps, float dt, double eps,
                            const float efield[3], int sym, int nimg,
                            const int *images, const float domain_size[3],
-                           const orc_boundary *bd, orc_event *ev, int ev_cap,
-                           int *ev_count, int nthreads);
+                           const orc_boundary *bd, const orc_field *field,
+                           orc_event *ev, int ev_cap, int *ev_count, int nthreads);
 
 /* orc_leapfrog_f64 with bd (nullable; folding per bd->fold) and the
  * injection window as a per-particle test (t_inj <= end of the half step;
- * force and kick: t_inj <= mid step), with species codes for the events. */
+ * force and kick: t_inj <= mid step), with species codes for the events.
+ * field (nullable): the emitter's field added to efield in the kick; with
+ * field, the ref32 loop replaces the uniform field by it, as the reference's
+ * computeBackgroundAcceleration does. */
 void orc_leapfrog_f64_bc(int64_t n, double *x, double *v, const double *q,
                          const double *m, int32_t *status, const double *t_inj,
                          int nsteps, double dt, double t0, double eps2,
                          double kconst, const double efield[3], int sym, int nimg,
                          const double *img_off, const orc_boundary *bd,
-                         orc_event *ev, int ev_cap, int *ev_count, int nthreads);
+                         const orc_field *field, orc_event *ev, int ev_cap,
+                         int *ev_count, int nthreads);
 
 /* Energy diagnostic in FP64 (particles.cpp:535-578): kinetic
  * 0.5*amu*m*|v|^2 and potential 0.5*sum_{i!=j} q_i q_j e^2 ke/sqrt(r^2+eps2),

@@ -404,6 +404,7 @@ void sv_destroy(sv_ctx *c) {
     batch_free(c);
     outliers_free(c);
     events_free(c);
+    field_free(c);
     free_state(c);
     Sorted &S = c->S;
     cudaFree(S.x); cudaFree(S.y); cudaFree(S.z); cudaFree(S.q); cudaFree(S.qm);
@@ -448,6 +449,8 @@ static sv_status upload_state(sv_ctx *c, int64_t n, const double *x3, const doub
     c->have_accel = false;
     c->ev_seq = 0;
     if (c->d_ev_count) SV_CK(c, cudaMemsetAsync(c->d_ev_count, 0, sizeof(unsigned long long), c->stream));
+    SV_TRY(field_prepare(c));
+    SV_TRY(field_reset(c));
     if (n == 0) return SV_OK;
     const size_t b3 = sizeof(double) * 3 * (size_t)n, b1 = sizeof(double) * (size_t)n;
     void *stg = nullptr;
@@ -495,6 +498,8 @@ sv_status sv_upload_ref32(sv_ctx *c, int64_t n, const float *pos4, const float *
     c->have_accel = false;
     c->ev_seq = 0;
     if (c->d_ev_count) SV_CK(c, cudaMemsetAsync(c->d_ev_count, 0, sizeof(unsigned long long), c->stream));
+    SV_TRY(field_prepare(c));
+    SV_TRY(field_reset(c));
     if (n == 0) return SV_OK;
     const size_t b4 = 16 * (size_t)n;
     void *stg = nullptr;
@@ -642,9 +647,12 @@ sv_status sv_leapfrog(sv_ctx *c, int32_t nsteps, double dt, double t0) {
     if (!c->have_state) return set_error(c, SV_ERR_STATE, "no state uploaded");
     if (nsteps < 0 || !(dt > 0.0)) return set_error(c, SV_ERR_INVALID, "nsteps >= 0 and dt > 0 required");
     SV_CK(c, cudaSetDevice(c->device));
-    if (c->batch) return batch_leapfrog(c, nsteps, dt, t0);
-    for (int it = 0; it < nsteps; it++) SV_TRY(leapfrog_step(c, t0 + dt * it, dt));
-    return SV_OK;
+    if (c->batch) {
+        SV_TRY(batch_leapfrog(c, nsteps, dt, t0));
+    } else {
+        for (int it = 0; it < nsteps; it++) SV_TRY(leapfrog_step(c, t0 + dt * it, dt));
+    }
+    return field_check(c);
 }
 
 sv_status sv_set_boundary(sv_ctx *c, const sv_boundary *b) {

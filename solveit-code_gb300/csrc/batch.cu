@@ -866,6 +866,7 @@ sv_status batch_leapfrog(sv_ctx *c, int32_t nsteps, double dt, double t0) {
     if (!B.ev_count0) SV_CK(c, cudaMalloc(&B.ev_count0, sizeof(unsigned long long)));
     // the drift may change status and record events: both are part of the state a retry restores
     if (c->B.crash != SV_CRASH_NONE || c->B.bc != SV_BC_NONE) SV_TRY(events_reserve(c));
+    SV_TRY(field_prepare(c));  // before capture: the graph keeps the walk caches' address
     double *st[6] = {c->x, c->y, c->z, c->vx, c->vy, c->vz};
     for (int k = 0; k < 6; k++)
         SV_CK(c, cudaMemcpyAsync(B.backup + k * n, st[k], sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));

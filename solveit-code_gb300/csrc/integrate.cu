@@ -198,21 +198,35 @@ __global__ void drift_kernel(DriftArgs a) {
     }
 }
 
+// With an emitter field map (M.nt > 0) the field at the particle is added to
+// the uniform one: computeBackgroundAcceleration (particles.cpp:496-520).
 __global__ void kick_kernel(double *__restrict__ vx, double *__restrict__ vy, double *__restrict__ vz,
                             const double *__restrict__ ax, const double *__restrict__ ay,
                             const double *__restrict__ az, const double *__restrict__ qom,
                             const int32_t *__restrict__ st,
                             const double *__restrict__ t_inj, int64_t n, double t_start, double dt,
-                            double eoa, double ex, double ey, double ez, const double *__restrict__ tb) {
+                            double eoa, double ex, double ey, double ez, const double *__restrict__ tb,
+                            const double *__restrict__ x, const double *__restrict__ y,
+                            const double *__restrict__ z, FieldMesh M) {
     if (tb) t_start += tb[0] + tb[1] * tb[2];
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         if (st[i] != 1) continue;
         const double f = eoa * qom[i];
         const double s = fmin(fmax(t_start + dt - t_inj[i], 0.0), dt);
-        vx[i] += (ax[i] + ex * f) * s;
-        vy[i] += (ay[i] + ey * f) * s;
-        vz[i] += (az[i] + ez * f) * s;
+        double fx = ex, fy = ey, fz = ez;
+        if (M.nt > 0) {
+            int t = M.cache[i];
+            double gx, gy, gz;
+            field_at(M, x[i], y[i], z[i], &t, &gx, &gy, &gz);
+            M.cache[i] = t;
+            fx += gx;
+            fy += gy;
+            fz += gz;
+        }
+        vx[i] += (ax[i] + fx * f) * s;
+        vy[i] += (ay[i] + fy * f) * s;
+        vz[i] += (az[i] + fz * f) * s;
     }
 }
 
@@ -349,7 +363,7 @@ sv_status drift(sv_ctx *c, double t_start, double h, int32_t *window, const doub
 sv_status kick(sv_ctx *c, double t_start, double dt, const int32_t *st, const double *tb) {
     kick_kernel<<<stream_grid(c->n), 256, 0, c->stream>>>(
         c->vx, c->vy, c->vz, c->ax, c->ay, c->az, c->qom, st, c->t_inj, c->n, t_start, dt,
-        c->P.e_over_amu, c->P.efield[0], c->P.efield[1], c->P.efield[2], tb);
+        c->P.e_over_amu, c->P.efield[0], c->P.efield[1], c->P.efield[2], tb, c->x, c->y, c->z, c->field);
     SV_LAUNCHED(c);
     return SV_OK;
 }
@@ -363,6 +377,7 @@ sv_status window_status(sv_ctx *c, double t_window) {
 sv_status leapfrog_step(sv_ctx *c, double ts, double dt, double *save_xh) {
     const double h = 0.5 * dt;
     if (c->B.crash != SV_CRASH_NONE || c->B.bc != SV_BC_NONE) SV_TRY(events_reserve(c));
+    SV_TRY(field_prepare(c));
     SV_TRY(drift(c, ts, h, c->wstatus));
     if (save_xh) {
         const size_t b = sizeof(double) * c->n;

@@ -8,6 +8,7 @@
 #include <cstring>
 
 #include "solveit_gpu.h"
+#include "field.cuh"
 
 namespace sv {
 
@@ -84,6 +85,10 @@ struct sv_ctx {
     int64_t ev_cap = 0;
     long long ev_seq = 0;       // drifts issued so far (event order across calls)
     const int8_t *pfold = nullptr;  // batch: per-particle folding (1 rotational plume), else null
+    // emitter field map (sv_set_emitter_field): device copies; field.cache has
+    // one start triangle per particle (field_cap entries)
+    sv::FieldMesh field{};
+    int64_t field_cap = 0;
     // last acceleration (force only), caller order, FP64
     double *ax = nullptr, *ay = nullptr, *az = nullptr;
     bool have_state = false, have_accel = false;
@@ -219,6 +224,11 @@ inline const int32_t *force_status(const sv_ctx *c) { return c->fstatus ? c->fst
 sv_status window_status(sv_ctx *c, double t_window);
 sv_status events_reserve(sv_ctx *c);
 void events_free(sv_ctx *c);
+// field.cu: the per-particle walk caches of the emitter field (grown to n, reset to -1)
+sv_status field_prepare(sv_ctx *c);
+sv_status field_reset(sv_ctx *c);
+sv_status field_check(sv_ctx *c);
+void field_free(sv_ctx *c);
 sv_status energy(sv_ctx *c, double *ke, double *pe);
 
 // image offsets (metres) of the translational lattice, in summation order

@@ -33,7 +33,8 @@ ABI_SYMBOLS = (
     "sv_leapfrog", "sv_energy", "sv_compare_accel", "sv_get_stats", "sv_sync", "sv_stream",
     "sv_launch_count", "sv_last_error", "sv_abi_version", "sv_adjoint_forward", "sv_adjoint_backward",
     "sv_direct_accel_noalloc", "sv_upload_batch", "sv_batch_tune", "sv_batch_get_info", "sv_batch_set_tuning",
-    "sv_get_outliers", "sv_set_boundary", "sv_get_boundary", "sv_get_events",
+    "sv_get_outliers", "sv_set_boundary", "sv_get_boundary", "sv_get_events", "sv_set_emitter_field",
+    "sv_emitter_field_at",
 )
 
 
@@ -136,6 +137,9 @@ def load(path: str = LIB_PATH):
     L.sv_set_boundary.argtypes = [vp, C.POINTER(Boundary)]
     L.sv_get_boundary.argtypes = [vp, C.POINTER(Boundary)]
     L.sv_get_events.argtypes = [vp, vp, C.c_int64, C.POINTER(C.c_int64)]
+    L.sv_set_emitter_field.argtypes = [vp, C.c_int32, vp, vp, vp, C.c_int32, vp, vp, C.c_double, C.c_double,
+                                       C.c_double]
+    L.sv_emitter_field_at.argtypes = [vp, C.c_int64, vp, vp]
     for name in ABI_SYMBOLS:
         if name not in ("sv_destroy", "sv_stream", "sv_launch_count", "sv_last_error", "sv_abi_version"):
             getattr(L, name).restype = C.c_int
@@ -284,6 +288,25 @@ class ForceMethod:
         for k in range(4):
             b.bc_space[k] = bc_space[k]
         self._check(self.L.sv_set_boundary(self.h, C.byref(b)))
+
+    def set_emitter_field(self, node_rz, e_r, e_z, triangles, neighbors, r0, e0, z_max=140.0):
+        """Field map of a single emitter (None removes it)."""
+        if node_rz is None:
+            self._check(self.L.sv_set_emitter_field(self.h, 0, None, None, None, 0, None, None, 1.0, 0.0, 0.0))
+            return
+        nd = np.ascontiguousarray(node_rz, np.float64)
+        er = np.ascontiguousarray(e_r, np.float64)
+        ez = np.ascontiguousarray(e_z, np.float64)
+        tr = np.ascontiguousarray(triangles, np.int32)
+        nb = np.ascontiguousarray(neighbors, np.int32)
+        self._check(self.L.sv_set_emitter_field(self.h, er.size, _p(nd), _p(er), _p(ez), tr.size // 3, _p(tr),
+                                                _p(nb), r0, e0, z_max))
+
+    def emitter_field_at(self, x3):
+        x = np.ascontiguousarray(x3, np.float64)
+        out = np.zeros_like(x)
+        self._check(self.L.sv_emitter_field_at(self.h, x.shape[0], _p(x), _p(out)))
+        return out
 
     def events(self):
         """Events recorded since the last call (structured array of EVENT_DTYPE, file order)."""

@@ -25,6 +25,12 @@ Fixtures (all FP32 vec4 arrays in the reference layout):
                     and temporal boundary conditions, rotational and
                     translational folding, and the events file
                     (``python tests/golden/make_golden.py drift_bc``).
+  emitter_field.npz a seeded single-emitter field map (Delaunay triangulation
+                    of jittered nodes, scipy) in the reference's Fields /
+                    Triangles CSV format, InterpolationScheme::Efield at plume
+                    particles (inside and outside the map) and 10 DKD steps
+                    with computeBackgroundAcceleration
+                    (``python tests/golden/make_golden.py emitter_field``).
 """
 from __future__ import annotations
 
@@ -54,6 +60,8 @@ def run_ref(variant, mode, pos4, vel4, acc4, tinj, **kw):
                 np.ascontiguousarray(a).tofile(f)
         args = [HARNESS.format(variant), mode, fin, fout] + [f"{k}={v}" for k, v in kw.items()]
         subprocess.check_call(args)
+        if mode == "efield":
+            return np.fromfile(fout, np.float32).reshape(n, 3)
         if mode == "grid":
             raw = np.fromfile(fout, np.int32)
             return raw[1:].reshape(raw[0], 3)
@@ -160,10 +168,66 @@ def drift_bc():
                         domain=np.array([2e-6, 2e-6, 0.0], np.float32), **out)
 
 
+def emitter_mesh(seed=9020, r_max=8.0, z_max=140.0):
+    """Jittered (r, z) nodes in units of r0, their Delaunay triangulation
+    (neighbour k across the edge opposite vertex k, -1 on the hull) and a
+    smooth synthetic field in units of E0."""
+    from scipy.spatial import Delaunay
+
+    rng = np.random.default_rng(seed)
+    r = np.linspace(0.0, r_max, 17)
+    z = np.linspace(0.0, z_max, 141)
+    rr, zz = np.meshgrid(r, z, indexing="ij")
+    pts = np.stack([rr.ravel(), zz.ravel()], axis=1)
+    inner = (pts[:, 0] > 0) & (pts[:, 0] < r_max) & (pts[:, 1] > 0) & (pts[:, 1] < z_max)
+    pts[inner] += rng.uniform(-0.2, 0.2, (inner.sum(), 2)) * [r[1], z[1]]
+    d = Delaunay(pts)
+    er = 0.3 * pts[:, 0] * np.exp(-pts[:, 1] / 60.0) / (1.0 + 0.05 * pts[:, 0] ** 2)
+    ez = np.exp(-pts[:, 1] / 40.0) * (1.0 - 0.02 * pts[:, 0]) + 0.1
+    return pts, er, ez, d.simplices.astype(np.int32), d.neighbors.astype(np.int32)
+
+
+def emitter_field():
+    """The reference's InterpolationScheme reading a seeded field map through
+    its own CSV readers; Efield at plume particles and a leapfrog with it."""
+    nodes, er, ez, tri, nbr = emitter_mesh()
+    r0, e0 = 1e-8, 1e9
+    st = plume.make_plume(256, 1.2e-6, 9021)
+    st["x"][:8, 2] = [-5e-8, -1e-9, 1.39e-6, 1.41e-6, 1.5e-6, 0.3e-6, 0.7e-6, 1.0e-6]  # z outside [0, 140 r0]
+    st["x"][5:8, 0] = [9e-8, 1.2e-7, -1.0e-7]  # r outside the map: extrapolated
+    st["x"][8, :2] = 0.0      # on the axis
+    st["x"][9, 0] = 0.0       # on the y axis (phi = pi/2 whatever the sign of y)
+    st["x"][9, 1] = -1e-8
+    pos4, vel4, acc4, tinj = plume.to_ref32(st)
+    with tempfile.TemporaryDirectory() as td:
+        with open(os.path.join(td, "fields.csv"), "w") as f:
+            for k in range(len(er)):
+                f.write(f"{nodes[k, 0]:.17g},{nodes[k, 1]:.17g},{er[k]:.17g},{ez[k]:.17g}\n")
+        with open(os.path.join(td, "triangles.csv"), "w") as f:
+            for t, nb in zip(tri, nbr):
+                f.write(",".join(str(int(v)) for v in (*t, *nb)) + "\n")
+        keys = dict(fdir=td + "/", fnodes="fields.csv", ftris="triangles.csv", r0=r0, e0=e0)
+        e_at = run_ref("eps20", "efield", pos4, vel4, acc4, tinj, **keys)
+        # leapfrog inside the map only (the walk outside the hull depends on the search order)
+        st2 = plume.make_plume(256, 1.2e-6, 9022)
+        st2["t_inj"][:] = np.floor(np.arange(256) / 64) * 1e-12
+        p4, v4, a4, t4 = plume.to_ref32(st2)
+        p, v, a = run_ref("eps20", "dkd", p4, v4, a4, t4, threads=4, steps=10, dt=1e-12, **keys)
+    np.savez_compressed(os.path.join(HERE, "emitter_field.npz"), node_rz=nodes, e_r=er, e_z=ez, triangles=tri,
+                        neighbors=nbr, r0=np.float64(r0), e0=np.float64(e0), pos4=pos4, vel4=vel4, acc4=acc4,
+                        tinj=tinj, e_out=e_at, dkd_pos4=p4, dkd_vel4=v4, dkd_acc4=a4, dkd_tinj=t4, dkd_pos4_out=p,
+                        dkd_vel4_out=v, dkd_acc4_out=a, steps=np.int32(10), dt=np.float32(1e-12),
+                        eps=np.float64(1e-20))
+    print("emitter field:", len(er), "nodes", len(tri), "triangles;", int((e_at == 0).all(1).sum()),
+          "points without field")
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["outliers"]:
         outliers()
     elif sys.argv[1:] == ["drift_bc"]:
         drift_bc()
+    elif sys.argv[1:] == ["emitter_field"]:
+        emitter_field()
     else:
         main()
