@@ -143,3 +143,42 @@ def test_mixed_accumulation_large_n_property():
     a, s = run_accel(st, softening2=EPS20, precision=sv.MIXED)
     assert rel_l2(a[tg], ref, st["status"][tg]) < 1e-5
     assert s.pair_interactions > 0
+
+
+def test_page_locked_upload_and_download_match_pageable():
+    """Page-locked host arrays (the end-to-end bench's buffers, copied
+    asynchronously): an upload / download round trip returns the input
+    exactly, and a leapfrog from either kind of buffer agrees to round-off
+    (the direct sum's split accumulation is not bit-reproducible)."""
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+
+    st = plume.make_plume(5000, 1e-6, 61)
+    st["t_inj"][:] = np.linspace(0.0, 2e-13, 5000)
+    st["status"][::7] = 2
+    pin = {k: torch.from_numpy(np.ascontiguousarray(st[k])).pin_memory() for k in ("x", "v", "q", "m", "status",
+                                                                                  "t_inj")}
+    ptr = {k: C.c_void_p(t.data_ptr()) for k, t in pin.items()}
+    L = sv.load()
+
+    def download_pinned(fm):
+        xo = torch.zeros((5000, 3), dtype=torch.float64).pin_memory()
+        vo = torch.zeros((5000, 3), dtype=torch.float64).pin_memory()
+        so = torch.zeros(5000, dtype=torch.int32).pin_memory()
+        assert L.sv_download(fm.h, C.c_void_p(xo.data_ptr()), C.c_void_p(vo.data_ptr()),
+                             C.c_void_p(so.data_ptr())) == 0
+        return xo.numpy().copy(), vo.numpy().copy(), so.numpy().copy()
+
+    with sv.ForceMethod(softening2=EPS20, efield=(0.0, 0.0, 1e8)) as fm:
+        assert L.sv_upload(fm.h, 5000, ptr["x"], ptr["v"], ptr["q"], ptr["m"], ptr["status"], ptr["t_inj"]) == 0
+        x, v, s = download_pinned(fm)
+        assert np.array_equal(x, st["x"]) and np.array_equal(v, st["v"]) and np.array_equal(s, st["status"])
+        fm.leapfrog(3, 1e-13)
+        xp, vp, sp = download_pinned(fm)
+    with sv.ForceMethod(softening2=EPS20, efield=(0.0, 0.0, 1e8)) as fm:
+        fm.upload(st)
+        fm.leapfrog(3, 1e-13)
+        xr, vr, sr = fm.download()
+    assert np.array_equal(sp, sr)
+    assert np.max(np.abs(xp - xr)) <= 1e-13 * np.max(np.abs(xr))
+    assert np.max(np.abs(vp - vr)) <= 1e-10 * np.max(np.abs(vr))
