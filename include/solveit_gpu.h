@@ -238,6 +238,34 @@ typedef struct {
  * next call returns SV_ERR_CAPACITY with count = events recorded + dropped. */
 SV_API sv_status sv_get_events(sv_ctx *ctx, sv_event *out, int64_t cap, int64_t *count);
 
+/* Multi-rate leapfrog (LeapfrogDKDSubsteps, integration_schemes.cpp:899-1528).
+ * Each entry asks for steps of at most dt inside a region: spatial limits
+ * bc_space (|x|, |y|, |z|, r; 0 = unbounded) and/or a limit bc_time on the
+ * time since injection, of kind bc (sv_bc_kind).  The entries are resolved
+ * into levels l = 0 .. L with steps time_step / 3^l exactly as
+ * setSubstepTimes (:1361-1427) resolves them.  sv_leapfrog then runs
+ * LeapfrogDKDSubsteps::runSimulation's recursion (:1494-1526): a level's drift
+ * half is drift, kick, drift of the next finer level; only the finest level
+ * drifts (every particle) and kicks; a kick makes the particles at levels >=
+ * its top level targets (status 1) and the coarser ones sources only (status
+ * 2, setParticleStatus :1216-1236), evaluates the force with the context's
+ * method plus the background field, and kicks each target by its own level's
+ * step (variableTimestepKick :1241-1262); particles are moved between levels
+ * after each coarser drift half (crossoverParticles / checkConditions
+ * :932-1111).  Every particle starts at the finest level (set and upload).
+ * sv_leapfrog must then be called with dt = time_step.  n = 0 returns to the
+ * single-rate leapfrog.  Single-plume contexts only; at most 16 levels. */
+typedef struct {
+    double dt;              /* largest step inside the region (s) */
+    int32_t bc;             /* sv_bc_kind of the region */
+    double bc_space[4];     /* |x|, |y|, |z|, r limits (m); 0 = unbounded */
+    double bc_time;         /* limit on the time since injection (s); 0 = unbounded */
+} sv_substep;
+
+SV_API sv_status sv_set_substeps(sv_ctx *ctx, double time_step, int32_t n, const sv_substep *substeps);
+/* The substep level of every particle (n bytes). */
+SV_API sv_status sv_get_substep_levels(sv_ctx *ctx, int8_t *levels);
+
 /* Background field of a single emitter (BackgroundEfield::singleEmitter), as
  * InterpolationScheme::computeEfieldSingleEmitter (interpolation_scheme.cpp:
  * 206-262) evaluates it from the field map the reference reads from its

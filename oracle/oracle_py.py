@@ -57,6 +57,9 @@ def lib():
             C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_int]
         L.orc_leapfrog_f64_bc.argtypes = L.orc_leapfrog_f64.argtypes[:-2] + [
             C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.POINTER(C.c_int), C.c_int]
+        L.orc_leapfrog_substeps_ref32.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_int, C.c_float,
+                                                  C.c_double, _f32p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                                  C.c_void_p, C.c_int]
         L.orc_emitter_field_ref32.argtypes = [C.c_void_p, C.c_int, _f32p, _f32p, C.POINTER(C.c_int)]
         L.orc_emitter_field_f64.argtypes = [C.c_void_p, C.c_int64, _f64p, _f64p]
         L.orc_energy_f64.argtypes = [C.c_int64, _f64p, _f64p, _f64p, _f64p, C.c_double,
@@ -262,6 +265,31 @@ def leapfrog_f64_bc(state, nsteps, dt, eps2, efield=(0.0, 0.0, 0.0), t0=0.0, sym
                               None if bd is None else C.byref(bd), None if fld is None else C.byref(fld),
                               ev.ctypes.data, ev_cap, C.byref(cnt), threads)
     return x.reshape(n, 3), v.reshape(n, 3), st, ev[:min(cnt.value, ev_cap)].copy()
+
+
+class Substep(C.Structure):
+    """orc_substep: one setSubstepTimes request."""
+    _fields_ = [("dt", C.c_float), ("bc", C.c_int), ("s", C.c_float * 4), ("t", C.c_float)]
+
+
+def leapfrog_substeps_ref32(pos4, vel4, acc4, t_inj, nsteps, dt, eps, subs, efield=(0.0, 0.0, 0.0), sym=0,
+                            bd=None, threads=0):
+    """LeapfrogDKDSubsteps restated (FP32): subs = [(dt, bc, (bx, by, bz, br), bt), ...];
+    returns (pos4, vel4, acc4, levels)."""
+    p = np.ascontiguousarray(pos4, np.float32).copy()
+    v = np.ascontiguousarray(vel4, np.float32).copy()
+    a = np.ascontiguousarray(acc4, np.float32).copy()
+    t = np.ascontiguousarray(t_inj, np.float32)
+    arr = (Substep * len(subs))()
+    for k, (sdt, bc, space, bt) in enumerate(subs):
+        arr[k].dt, arr[k].bc, arr[k].t = sdt, bc, bt
+        for j in range(4):
+            arr[k].s[j] = space[j]
+    lev = np.zeros(p.shape[0], np.int8)
+    lib().orc_leapfrog_substeps_ref32(p.shape[0], p, v, a, t, nsteps, dt, eps, np.asarray(efield, np.float32), sym,
+                                      len(subs), C.cast(arr, C.c_void_p), None if bd is None else C.byref(bd),
+                                      lev.ctypes.data, threads)
+    return p, v, a, lev
 
 
 def energy_f64(state, eps2, threads=0):

@@ -22,12 +22,18 @@
 //          (the Fields / Triangles files in the reference's CSV format), r0, e0:
 //          a singleEmitter background field (dkd: replaces ez)
 //   mode efield: InterpolationScheme::Efield at each particle, float e[3n]
+//   mode run: the reference's own integrator, LeapfrogDKD::runSimulation, or
+//          with subs=dt,bc,bx,by,bz,br,bt;... LeapfrogDKDSubsteps with
+//          setSubstepTimes (direct force); keys steps, dt, crash / bc keys as
+//          dkd; out.bin as dkd, then int32 bytes and the snapshot file
+//          (SaveDataOptions::newOriginal) written at the start and the end
 // in.bin : int32 n, float pos4[4n], float vel4[4n], float acc4[4n], float tinj[n]
 // out.bin: float pos4[4n], float vel4[4n], float acc4[4n]
 //          (dkd with events=1: then int32 count, count 40-byte event records
 //          as ChargedParticles::writeToEventsFile wrote them)
 //          (grid mode: int32 count, int32 points[3*count] in the Grid's order)
 #include "force_calculation_methods.h"
+#include "integration_schemes.h"
 
 #include <cstdio>
 #include <cstdlib>
@@ -158,7 +164,7 @@ int main(int argc, char **argv) {
     DirectForceCalculation *df = nullptr;
     BarnesHutForceCalculation *bh = nullptr;
     MultipoleMethodForceCalculation *fmm = nullptr;
-    if (mode == "direct" || mode == "dkd") {
+    if (mode == "direct" || mode == "dkd" || mode == "run") {
         df = new DirectForceCalculation(&ps);
         fm = df;
     } else if (mode == "bh") {
@@ -179,7 +185,69 @@ int main(int argc, char **argv) {
     fm->setGrid(&grid);
 
     FILE *events = nullptr;
-    if (mode == "dkd") {
+    FILE *snap = nullptr;
+    if (mode == "run") {
+        const int steps = (int)getd(kv, "steps", 1);
+        ps.params.timeStep = (float)getd(kv, "dt", 1e-13);
+        ps.params.numIters = steps;
+        ps.params.interval = steps;  // one saveData at the end (constantRate)
+        ps.params.timerInfo = TimerOptions::off;
+        ps.params.saveDataToggle = SaveDataOptions::newOriginal;
+        snap = std::tmpfile();
+        events = std::tmpfile();
+        if (!snap || !events) return 3;
+        static FILE *files[1];
+        files[0] = snap;
+        ps.params.saveDataFiles = files;
+        ps.params.numSaveDataFiles = 1;
+        ps.params.eventsFile = events;
+        CrashParameters &cr = ps.params.crashParameters;
+        cr.crashOptions = getd(kv, "crash", 0) != 0 ? CrashConditionOptions::extractorGrid
+                                                     : CrashConditionOptions::none;
+        cr.z_distance = (float)getd(kv, "cz", 0.0);
+        cr.z_width = (float)getd(kv, "cw", 0.0);
+        cr.r_distance = (float)getd(kv, "cr", 0.0);
+        BoundaryConditionParameters &bc = ps.params.boundaryConditions;
+        const int bck = (int)getd(kv, "bc", 0);
+        bc.boundaryConditionType = bck == 1 ? BoundaryConditionOptions::space
+                                 : bck == 2 ? BoundaryConditionOptions::time
+                                 : bck == 3 ? BoundaryConditionOptions::space_and_time
+                                            : BoundaryConditionOptions::none;
+        bc.spatialBoundaryConditions = vec4<float>((float)getd(kv, "bx", 0.0), (float)getd(kv, "by", 0.0),
+                                                   (float)getd(kv, "bz", 0.0), (float)getd(kv, "br", 0.0));
+        bc.temporalBoundaryCondition = (float)getd(kv, "bt", 0.0);
+        if (kv.count("subs")) {
+            // "dt,bc,bx,by,bz,br,bt;..." -> setSubstepTimes(times, bcs, size)
+            std::vector<float> times;
+            std::vector<BoundaryConditionParameters> bcs;
+            std::string list = kv["subs"];
+            size_t pos = 0;
+            while (pos < list.size()) {
+                size_t end = list.find(';', pos);
+                if (end == std::string::npos) end = list.size();
+                float v[7] = {0, 0, 0, 0, 0, 0, 0};
+                std::sscanf(list.substr(pos, end - pos).c_str(), "%f,%f,%f,%f,%f,%f,%f", &v[0], &v[1], &v[2], &v[3],
+                            &v[4], &v[5], &v[6]);
+                BoundaryConditionParameters b;
+                const int k = (int)v[1];
+                b.boundaryConditionType = k == 1 ? BoundaryConditionOptions::space
+                                        : k == 2 ? BoundaryConditionOptions::time
+                                        : k == 3 ? BoundaryConditionOptions::space_and_time
+                                                 : BoundaryConditionOptions::none;
+                b.spatialBoundaryConditions = vec4<float>(v[2], v[3], v[4], v[5]);
+                b.temporalBoundaryCondition = v[6];
+                times.push_back(v[0]);
+                bcs.push_back(b);
+                pos = end + 1;
+            }
+            LeapfrogDKDSubsteps leap(ps, *fm);
+            leap.setSubstepTimes(times.data(), bcs.data(), (int)times.size());
+            leap.runSimulation();
+        } else {
+            LeapfrogDKD leap(ps, *fm);
+            leap.runSimulation();
+        }
+    } else if (mode == "dkd") {
         // LeapfrogDKD::runSimulation step structure (integration_schemes.cpp:
         // 867-888) with driftNew's injection window (:705-723) on the
         // reference's own methods: findMostRecentInjected, ParticleSystem::
@@ -252,6 +320,16 @@ int main(int argc, char **argv) {
     std::fwrite(cp.position, 16, n, fo);
     std::fwrite(cp.velocity, 16, n, fo);
     std::fwrite(cp.acceleration, 16, n, fo);
+    if (snap) {
+        std::fflush(snap);
+        const long bytes = std::ftell(snap);
+        const int32_t cnt = (int32_t)bytes;
+        std::fwrite(&cnt, 4, 1, fo);
+        std::rewind(snap);
+        std::vector<char> buf((size_t)bytes);
+        if (bytes > 0 && std::fread(buf.data(), 1, (size_t)bytes, snap) != (size_t)bytes) return 5;
+        if (bytes > 0) std::fwrite(buf.data(), 1, (size_t)bytes, fo);
+    }
     if (events && getd(kv, "events", 0) != 0) {
         std::fflush(events);
         const long bytes = std::ftell(events);

@@ -804,6 +804,271 @@ void orc_leapfrog_ref32(int n, float *pos4, float *vel4, float *acc4,
                           NULL, NULL, NULL, 0, NULL, nthreads);
 }
 
+/* ---- multi-rate leapfrog (LeapfrogDKDSubsteps) -------------------------- */
+
+typedef struct {
+    int type;
+    float t, s[4];
+} ref_bc;
+
+static void bc_most_stringent(ref_bc *b) {
+    /* BoundaryConditionParameters::setMostStringentBoundaryConditionType (structures.h:309-326) */
+    if (b->type == 0) {
+        b->t = 0.0f;
+        for (int k = 0; k < 4; k++) b->s[k] = 0.0f;
+    } else if (b->type == 1) {
+        b->t = 0.0f;
+    } else if (b->type == 2) {
+        for (int k = 0; k < 4; k++) b->s[k] = 0.0f;
+    }
+    b->type = 3;
+}
+
+static void bc_choose_min(ref_bc *a, const ref_bc *b) {
+    /* chooseMinimumBoundaryConditionParameters (structures.h:328-363) */
+    a->t = (a->t == 0 && b->t == 0) ? 0.0f : ref_minf(a->t, b->t);
+    for (int k = 0; k < 4; k++) a->s[k] = (a->s[k] == 0 && b->s[k] == 0) ? 0.0f : ref_minf(a->s[k], b->s[k]);
+}
+
+static void bc_choose_max(ref_bc *a, const ref_bc *b) {
+    /* chooseMaximumBoundaryConditionParameters (structures.h:365-400) */
+    a->t = (a->t == 0 || b->t == 0) ? 0.0f : ref_maxf(a->t, b->t);
+    for (int k = 0; k < 4; k++) a->s[k] = (a->s[k] == 0 || b->s[k] == 0) ? 0.0f : ref_maxf(a->s[k], b->s[k]);
+}
+
+#define ORC_MAX_LEVELS 16
+
+typedef struct {
+    int L;
+    float dt[ORC_MAX_LEVELS];
+    ref_bc bc[ORC_MAX_LEVELS];
+} sub_table;
+
+static int cmp_substep(const void *a, const void *b) {
+    const float x = ((const orc_substep *)a)->dt, y = ((const orc_substep *)b)->dt;
+    return (x > y) - (x < y);
+}
+
+/* LeapfrogDKDSubsteps::setSubstepTimes (integration_schemes.cpp:1361-1412) */
+static int resolve_substeps(float step, int nsub, const orc_substep *subs_in, sub_table *T) {
+    orc_substep *in = (orc_substep *)malloc(sizeof(orc_substep) * (size_t)nsub);
+    memcpy(in, subs_in, sizeof(orc_substep) * (size_t)nsub);
+    qsort(in, (size_t)nsub, sizeof(orc_substep), cmp_substep);
+    float temp_dt = step;
+    int L = 0;
+    while (temp_dt > in[0].dt) {
+        temp_dt /= 3.0;
+        L++;
+    }
+    if (L >= ORC_MAX_LEVELS) {
+        free(in);
+        return -1;
+    }
+    memset(T, 0, sizeof(*T));
+    T->L = L;
+    if (L != 0) {
+        T->dt[L] = in[0].dt;
+        T->bc[L].type = in[0].bc;
+        T->bc[L].t = in[0].t;
+        for (int k = 0; k < 4; k++) T->bc[L].s[k] = in[0].s[k];
+    }
+    for (int i = 0; i <= L; i++) bc_most_stringent(&T->bc[i]);
+    for (int i = 1; i < nsub; i++) {
+        int ind = 0;
+        temp_dt = step;
+        while (temp_dt > in[i].dt) {
+            temp_dt /= 3.0;
+            ind++;
+        }
+        ref_bc b;
+        b.type = in[i].bc;
+        b.t = in[i].t;
+        for (int k = 0; k < 4; k++) b.s[k] = in[i].s[k];
+        if (T->dt[ind] == 0) {
+            T->dt[ind] = temp_dt;
+            if (ind != 0) T->bc[ind] = b;
+        } else {
+            bc_choose_min(&T->bc[ind], &b);
+        }
+    }
+    T->dt[0] = step;
+    for (int i = 1; i <= L; i++) T->dt[i] = (float)(T->dt[i - 1] / 3.0);
+    for (int i = L - 1; i >= 0; i--) bc_choose_max(&T->bc[i], &T->bc[i + 1]);
+    free(in);
+    return 0;
+}
+
+/* the scan of checkSpatialConditions / checkTemporalConditions
+ * (integration_schemes.cpp:956-1094) for one coordinate (comp 0..3: |x|, |y|,
+ * |z|, r; comp 4: time since injection) */
+static int scan_levels_ref32(const sub_table *T, int level, float value, int comp) {
+    int possible = -1;
+    float boundary = 0.0f;
+    for (int i = T->L; i >= level; i--) {
+        const float lim = comp < 4 ? T->bc[i].s[comp] : T->bc[i].t;
+        if (possible == -1) {
+            const int in = comp < 4 ? (fabsf(value) < lim || lim == 0) : (value < lim || lim == 0);
+            if (in) {
+                possible = i;
+                boundary = lim;
+            }
+        } else {
+            if (boundary == lim)
+                possible--;
+            else
+                break;
+        }
+    }
+    return possible;
+}
+
+typedef struct {
+    int n, first, last, nthreads, sym;
+    float *pos4, *vel4, *acc4;
+    const float *t_inj;
+    const float *efield;
+    const float *domain;
+    const orc_boundary *bd;
+    double eps;
+    float t_pos, t_vel;
+    const sub_table *T;
+    int *lev;
+    int ev_count;
+} sub_run;
+
+static void sub_crossover(sub_run *r, int level) {
+    /* crossoverParticles / checkConditions (integration_schemes.cpp:932-1111) */
+    const sub_table *T = r->T;
+    for (int i = r->first; i < r->last; i++) {
+        if (r->lev[i] != level && r->lev[i] != level + 1) continue;
+        const int type = T->bc[level + 1].type;
+        const float *p = &r->pos4[4 * i];
+        const float w = sqrtf(p[0] * p[0] + p[1] * p[1]);
+        const float ts = r->t_pos - r->t_inj[i];
+        int out = r->lev[i], sp = 0;
+        if (type == 1 || type == 3) {
+            sp = scan_levels_ref32(T, level, p[0], 0);
+            int q = scan_levels_ref32(T, level, p[1], 1);
+            sp = sp > q ? sp : q;
+            q = scan_levels_ref32(T, level, p[2], 2);
+            sp = sp > q ? sp : q;
+            q = scan_levels_ref32(T, level, w, 3);
+            sp = sp > q ? sp : q;
+            out = sp;
+        }
+        if (type == 2) out = scan_levels_ref32(T, level, ts, 4);
+        if (type == 3) {
+            const int q = scan_levels_ref32(T, level, ts, 4);
+            out = q > sp ? q : sp;
+        }
+        r->lev[i] = out < 0 ? level : out;
+    }
+}
+
+static void sub_drift(sub_run *r, int level, int toggle);
+
+static void sub_kick(sub_run *r, int level, int top) {
+    const sub_table *T = r->T;
+    if (level != T->L) {
+        sub_drift(r, level + 1, 0);
+        sub_kick(r, level + 1, top);
+        sub_drift(r, level + 1, 1);
+        return;
+    }
+    /* setParticleStatus (integration_schemes.cpp:1216-1236) */
+    for (int i = r->first; i < r->last; i++) {
+        float *w = &r->acc4[4 * i + 3];
+        if (*w != 0.0f && *w != -1.0f) {
+            if (r->lev[i] <= level && r->lev[i] >= top)
+                *w = 1.0f;
+            else if (r->lev[i] < top)
+                *w = 2.0f;
+        }
+    }
+    /* updateAcceleration / updateAccelerationSubsteps: zeroAcceleration + force */
+    for (int i = r->first; i < r->last; i++)
+        if (r->acc4[4 * i + 3] == 1.0f) r->acc4[4 * i] = r->acc4[4 * i + 1] = r->acc4[4 * i + 2] = 0.0f;
+    orc_direct_ref32(r->pos4, r->vel4, r->acc4, r->first, r->last, r->first, r->last, r->eps, r->nthreads);
+    /* computeBackgroundAcceleration with a uniform field */
+    const float factor = REF_ELEM_CHARGE / REF_AMU;
+    for (int i = r->first; i < r->last; i++) {
+        if (r->acc4[4 * i + 3] != 1.0f) continue;
+        long double m = species_mass_ld((int)r->vel4[4 * i + 3]);
+        float ef = (float)((double)factor * (double)r->pos4[4 * i + 3] / m);
+        for (int d = 0; d < 3; d++) r->acc4[4 * i + d] += (float)((double)r->efield[d] * (double)ef);
+    }
+    /* variableTimestepKick (integration_schemes.cpp:1241-1262) */
+    float tend[ORC_MAX_LEVELS];
+    for (int l = 0; l <= T->L; l++) tend[l] = r->t_vel + T->dt[l];
+    for (int i = r->first; i < r->last; i++) {
+        if (r->acc4[4 * i + 3] != 1.0f) continue;
+        const int l = r->lev[i];
+        const float temp_dt = T->dt[l];
+        const float s = clampf_dt(tend[l] - r->t_inj[i], temp_dt);
+        for (int d = 0; d < 3; d++) r->vel4[4 * i + d] += r->acc4[4 * i + d] * s;
+    }
+    r->t_vel += T->dt[T->L];
+}
+
+static void sub_drift(sub_run *r, int level, int toggle) {
+    const sub_table *T = r->T;
+    if (level != T->L) {
+        sub_drift(r, level + 1, 0);
+        sub_kick(r, level + 1, level + 1);
+        sub_drift(r, level + 1, 1);
+        if (toggle) sub_crossover(r, level);
+        return;
+    }
+    /* LeapfrogDKDSubsteps::driftNew at the finest level (integration_schemes.cpp:1162-1201) */
+    const float h = T->dt[T->L] / 2;
+    r->last = most_recent_injected(r->n, r->t_inj, r->t_pos + h) + 1;
+    drift_ref32(r->first, r->last, r->pos4, r->vel4, r->acc4, r->t_inj, r->t_pos, h, r->sym, r->domain, r->bd,
+                NULL, 0, &r->ev_count);
+    r->first = reset_first(r->first, r->last, r->acc4);
+    r->t_pos += h;
+}
+
+void orc_leapfrog_substeps_ref32(int n, float *pos4, float *vel4, float *acc4,
+                                 const float *t_inj, int nsteps, float dt, double eps,
+                                 const float efield[3], int sym, int nsub,
+                                 const orc_substep *subs, const orc_boundary *bd,
+                                 int8_t *levels_out, int nthreads) {
+    sub_table T;
+    if (resolve_substeps(dt, nsub, subs, &T) != 0) return;
+    int *lev = (int *)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    for (int i = 0; i < n; i++) lev[i] = T.L;  /* initializeParticleLevels */
+    const float dom0[3] = {0, 0, 0};
+    sub_run r;
+    memset(&r, 0, sizeof(r));
+    r.n = n;
+    r.nthreads = nthreads;
+    r.sym = sym;
+    r.pos4 = pos4;
+    r.vel4 = vel4;
+    r.acc4 = acc4;
+    r.t_inj = t_inj;
+    r.efield = efield;
+    r.domain = bd ? NULL : dom0;
+    r.bd = bd;
+    r.eps = eps;
+    r.T = &T;
+    r.lev = lev;
+    float dom[3] = {0, 0, 0};
+    if (bd)
+        for (int d = 0; d < 3; d++) dom[d] = (float)bd->domain[d];
+    r.domain = dom;
+    for (int it = 1; it <= nsteps; it++) {
+        r.t_pos = dt * (float)(it - 1);
+        r.t_vel = dt * (float)(it - 1);
+        sub_drift(&r, 0, 0);
+        sub_kick(&r, 0, 0);
+        sub_drift(&r, 0, 1);
+    }
+    if (levels_out)
+        for (int i = 0; i < n; i++) levels_out[i] = (int8_t)lev[i];
+    free(lev);
+}
+
 static uint32_t species_of_mass(double m) {
     for (int k = 0; k < 8; k++)
         if (k != 3 && m == (double)species_mass_ld(k)) return (uint32_t)k;

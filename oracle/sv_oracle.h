@@ -157,6 +157,28 @@ void orc_leapfrog_ref32_bc(int n, float *pos4, float *vel4, float *acc4,
                            const orc_boundary *bd, const orc_field *field,
                            orc_event *ev, int ev_cap, int *ev_count, int nthreads);
 
+/* One substep request of LeapfrogDKDSubsteps::setSubstepTimes: the largest
+ * step dt inside a region (bc: BoundaryConditionOptions; spatial limits s =
+ * |x|, |y|, |z|, r; t: time since injection; 0 = unbounded). */
+typedef struct {
+    float dt;
+    int bc;
+    float s[4];
+    float t;
+} orc_substep;
+
+/* LeapfrogDKDSubsteps::runSimulation (integration_schemes.cpp:899-1528) with
+ * setSubstepTimes(subs, nsub) and the direct force, FP32 as the reference;
+ * bd: crash / boundary conditions of the drift (nullable; folding follows sym
+ * as the reference's does); efield: uniform field in the kick (the
+ * reference's runSimulation has none: pass zeros to compare with it).
+ * levels_out (n, nullable): each particle's substep level at the end. */
+void orc_leapfrog_substeps_ref32(int n, float *pos4, float *vel4, float *acc4,
+                                 const float *t_inj, int nsteps, float dt, double eps,
+                                 const float efield[3], int sym, int nsub,
+                                 const orc_substep *subs, const orc_boundary *bd,
+                                 int8_t *levels_out, int nthreads);
+
 /* orc_leapfrog_f64 with bd (nullable; folding per bd->fold) and the
  * injection window as a per-particle test (t_inj <= end of the half step;
  * force and kick: t_inj <= mid step), with species codes for the events.

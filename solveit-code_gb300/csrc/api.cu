@@ -405,6 +405,7 @@ void sv_destroy(sv_ctx *c) {
     outliers_free(c);
     events_free(c);
     field_free(c);
+    substeps_free(c);
     free_state(c);
     Sorted &S = c->S;
     cudaFree(S.x); cudaFree(S.y); cudaFree(S.z); cudaFree(S.q); cudaFree(S.qm);
@@ -451,6 +452,7 @@ static sv_status upload_state(sv_ctx *c, int64_t n, const double *x3, const doub
     if (c->d_ev_count) SV_CK(c, cudaMemsetAsync(c->d_ev_count, 0, sizeof(unsigned long long), c->stream));
     SV_TRY(field_prepare(c));
     SV_TRY(field_reset(c));
+    SV_TRY(substeps_reset_levels(c));
     if (n == 0) return SV_OK;
     const size_t b3 = sizeof(double) * 3 * (size_t)n, b1 = sizeof(double) * (size_t)n;
     void *stg = nullptr;
@@ -500,6 +502,7 @@ sv_status sv_upload_ref32(sv_ctx *c, int64_t n, const float *pos4, const float *
     if (c->d_ev_count) SV_CK(c, cudaMemsetAsync(c->d_ev_count, 0, sizeof(unsigned long long), c->stream));
     SV_TRY(field_prepare(c));
     SV_TRY(field_reset(c));
+    SV_TRY(substeps_reset_levels(c));
     if (n == 0) return SV_OK;
     const size_t b4 = 16 * (size_t)n;
     void *stg = nullptr;
@@ -649,6 +652,8 @@ sv_status sv_leapfrog(sv_ctx *c, int32_t nsteps, double dt, double t0) {
     SV_CK(c, cudaSetDevice(c->device));
     if (c->batch) {
         SV_TRY(batch_leapfrog(c, nsteps, dt, t0));
+    } else if (c->sub.on) {
+        SV_TRY(substeps_run(c, nsteps, dt, t0));
     } else {
         for (int it = 0; it < nsteps; it++) SV_TRY(leapfrog_step(c, t0 + dt * it, dt));
     }

@@ -720,6 +720,7 @@ bool batch_same_shape(const sv_ctx *c, int32_t np, const int64_t *counts, const 
 sv_status batch_plan(sv_ctx *c, int32_t np, const int64_t *counts, const int32_t *method, const int32_t *sym) {
     batch_free(c);
     if (np < 1 || np > kMaxPlumes) return set_error(c, SV_ERR_INVALID, "1..%d plumes per batch", kMaxPlumes);
+    if (c->sub.on) return set_error(c, SV_ERR_UNSUPPORTED, "substeps run on single-plume contexts");
     c->batch = new Batch();
     Batch &B = *c->batch;
     B.np = np;

@@ -61,6 +61,20 @@ struct Outliers; // outliers.cu
 
 }  // namespace sv
 
+namespace sv {
+// substep levels of the multi-rate leapfrog (substeps.cu): level l has the
+// step dt[l] and the region limits (bs: |x|, |y|, |z|, r; bt: time since
+// injection; 0 = unbounded) of kind type[l] (sv_bc_kind)
+constexpr int kMaxSubLevels = 16;
+struct SubTable {
+    int on = 0, L = 0;  // L: finest level
+    double dt[kMaxSubLevels] = {};
+    int type[kMaxSubLevels] = {};
+    double bs[kMaxSubLevels][4] = {};
+    double bt[kMaxSubLevels] = {};
+};
+}  // namespace sv
+
 struct sv_ctx {
     sv_params P{};
     int device = 0;
@@ -89,6 +103,10 @@ struct sv_ctx {
     // one start triangle per particle (field_cap entries)
     sv::FieldMesh field{};
     int64_t field_cap = 0;
+    // multi-rate leapfrog (sv_set_substeps): level table and per-particle level
+    sv::SubTable sub{};
+    int8_t *sub_level = nullptr;
+    int64_t sub_cap = 0;
     // last acceleration (force only), caller order, FP64
     double *ax = nullptr, *ay = nullptr, *az = nullptr;
     bool have_state = false, have_accel = false;
@@ -229,6 +247,10 @@ sv_status field_prepare(sv_ctx *c);
 sv_status field_reset(sv_ctx *c);
 sv_status field_check(sv_ctx *c);
 void field_free(sv_ctx *c);
+// substeps.cu: the multi-rate leapfrog
+sv_status substeps_run(sv_ctx *c, int32_t nsteps, double dt, double t0);
+sv_status substeps_reset_levels(sv_ctx *c);
+void substeps_free(sv_ctx *c);
 sv_status energy(sv_ctx *c, double *ke, double *pe);
 
 // image offsets (metres) of the translational lattice, in summation order

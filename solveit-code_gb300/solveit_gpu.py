@@ -34,7 +34,7 @@ ABI_SYMBOLS = (
     "sv_launch_count", "sv_last_error", "sv_abi_version", "sv_adjoint_forward", "sv_adjoint_backward",
     "sv_direct_accel_noalloc", "sv_upload_batch", "sv_batch_tune", "sv_batch_get_info", "sv_batch_set_tuning",
     "sv_get_outliers", "sv_set_boundary", "sv_get_boundary", "sv_get_events", "sv_set_emitter_field",
-    "sv_emitter_field_at",
+    "sv_emitter_field_at", "sv_set_substeps", "sv_get_substep_levels",
 )
 
 
@@ -80,6 +80,10 @@ class Boundary(C.Structure):
 # the 40-byte events-file record (ChargedParticles::writeToEventsFile, particles.cpp:666-684)
 EVENT_DTYPE = np.dtype([("time", "<f4"), ("x", "<f4"), ("y", "<f4"), ("z", "<f4"), ("vx", "<f4"), ("vy", "<f4"),
                         ("vz", "<f4"), ("index", "<i4"), ("species", "<u4"), ("status", "<i4")])
+
+
+class Substep(C.Structure):
+    _fields_ = [("dt", C.c_double), ("bc", C.c_int32), ("bc_space", C.c_double * 4), ("bc_time", C.c_double)]
 
 
 class SolveitError(RuntimeError):
@@ -140,6 +144,8 @@ def load(path: str = LIB_PATH):
     L.sv_set_emitter_field.argtypes = [vp, C.c_int32, vp, vp, vp, C.c_int32, vp, vp, C.c_double, C.c_double,
                                        C.c_double]
     L.sv_emitter_field_at.argtypes = [vp, C.c_int64, vp, vp]
+    L.sv_set_substeps.argtypes = [vp, C.c_double, C.c_int32, vp]
+    L.sv_get_substep_levels.argtypes = [vp, vp]
     for name in ABI_SYMBOLS:
         if name not in ("sv_destroy", "sv_stream", "sv_launch_count", "sv_last_error", "sv_abi_version"):
             getattr(L, name).restype = C.c_int
@@ -306,6 +312,20 @@ class ForceMethod:
         x = np.ascontiguousarray(x3, np.float64)
         out = np.zeros_like(x)
         self._check(self.L.sv_emitter_field_at(self.h, x.shape[0], _p(x), _p(out)))
+        return out
+
+    def set_substeps(self, time_step, substeps):
+        """substeps: list of (dt, bc, (bx, by, bz, br), bt); [] returns to the single-rate leapfrog."""
+        arr = (Substep * max(len(substeps), 1))()
+        for k, (dt, bc, space, bt) in enumerate(substeps):
+            arr[k].dt, arr[k].bc, arr[k].bc_time = dt, bc, bt
+            for j in range(4):
+                arr[k].bc_space[j] = space[j]
+        self._check(self.L.sv_set_substeps(self.h, time_step, len(substeps), C.cast(arr, C.c_void_p)))
+
+    def substep_levels(self):
+        out = np.zeros(self.n, np.int8)
+        self._check(self.L.sv_get_substep_levels(self.h, _p(out)))
         return out
 
     def events(self):

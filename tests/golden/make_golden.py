@@ -31,6 +31,10 @@ Fixtures (all FP32 vec4 arrays in the reference layout):
                     particles (inside and outside the map) and 10 DKD steps
                     with computeBackgroundAcceleration
                     (``python tests/golden/make_golden.py emitter_field``).
+  substeps.npz      the reference's own LeapfrogDKD::runSimulation and
+                    LeapfrogDKDSubsteps::runSimulation (two substep tables)
+                    over 6 steps with staggered injection, with the snapshot
+                    files they write (``... make_golden.py substeps``).
 """
 from __future__ import annotations
 
@@ -60,6 +64,11 @@ def run_ref(variant, mode, pos4, vel4, acc4, tinj, **kw):
                 np.ascontiguousarray(a).tofile(f)
         args = [HARNESS.format(variant), mode, fin, fout] + [f"{k}={v}" for k, v in kw.items()]
         subprocess.check_call(args)
+        if mode == "run":
+            raw = np.fromfile(fout, np.uint8)
+            out = raw[:48 * n].view(np.float32).reshape(3, n, 4)
+            nb = int(raw[48 * n:48 * n + 4].view(np.int32)[0])
+            return out[0].copy(), out[1].copy(), out[2].copy(), raw[48 * n + 4:48 * n + 4 + nb].copy()
         if mode == "efield":
             return np.fromfile(fout, np.float32).reshape(n, 3)
         if mode == "grid":
@@ -222,6 +231,43 @@ def emitter_field():
           "points without field")
 
 
+# substep requests: (dt, BoundaryConditionOptions, (|x|, |y|, |z|, r) limits, time limit)
+SUBSTEP_CASES = {
+    # the plume core (r < 10 nm) at dt/27, the rest at dt
+    "core": [(1e-13, 1, (0.0, 0.0, 0.0, 1e-8), 0.0)],
+    # two nested regions: r < 14 nm at dt/3, r < 8 nm and the first 2.9 ps after injection at dt/9
+    # (the time limit off the grid of half-step times, where FP32 and FP64 clocks could order a tie apart)
+    "nested": [(3.4e-13, 1, (0.0, 0.0, 0.0, 1.4e-8), 0.0), (1.2e-13, 3, (0.0, 0.0, 0.0, 8e-9), 2.9e-12)],
+}
+
+
+def substeps_arg(subs):
+    return ";".join(f"{dt:.9g},{bc},{s[0]:.9g},{s[1]:.9g},{s[2]:.9g},{s[3]:.9g},{bt:.9g}" for dt, bc, s, bt in subs)
+
+
+def substeps():
+    """The reference's own LeapfrogDKDSubsteps::runSimulation (and
+    LeapfrogDKD::runSimulation) on plumes injected in groups, with its
+    snapshot file."""
+    out = {}
+    st = plume.make_plume(256, 1e-6, 9040)
+    # injection times off the grid of half-step times (a tie there is broken
+    # differently by FP32 and FP64 clocks)
+    st["t_inj"][:] = np.floor(np.arange(256) / 64) * 2.03e-12
+    st["status"][[11, 77]] = 2
+    pos4, vel4, acc4, tinj = plume.to_ref32(st)
+    out.update(pos4=pos4, vel4=vel4, acc4=acc4, tinj=tinj)
+    p, v, a, snap = run_ref("eps20", "run", pos4, vel4, acc4, tinj, threads=4, steps=6, dt=1e-12)
+    out.update(single_pos4_out=p, single_vel4_out=v, single_acc4_out=a, single_snapshot=snap)
+    for name, subs in SUBSTEP_CASES.items():
+        p, v, a, snap = run_ref("eps20", "run", pos4, vel4, acc4, tinj, threads=4, steps=6, dt=1e-12,
+                                subs=substeps_arg(subs))
+        out.update({f"{name}_pos4_out": p, f"{name}_vel4_out": v, f"{name}_acc4_out": a, f"{name}_snapshot": snap})
+        print(name, "statuses", dict(zip(*np.unique(a[:, 3], return_counts=True))))
+    np.savez_compressed(os.path.join(HERE, "substeps.npz"), steps=np.int32(6), dt=np.float32(1e-12),
+                        eps=np.float64(1e-20), **out)
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["outliers"]:
         outliers()
@@ -229,5 +275,7 @@ if __name__ == "__main__":
         drift_bc()
     elif sys.argv[1:] == ["emitter_field"]:
         emitter_field()
+    elif sys.argv[1:] == ["substeps"]:
+        substeps()
     else:
         main()
