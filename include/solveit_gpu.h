@@ -238,6 +238,29 @@ typedef struct {
  * next call returns SV_ERR_CAPACITY with count = events recorded + dropped. */
 SV_API sv_status sv_get_events(sv_ctx *ctx, sv_event *out, int64_t cap, int64_t *count);
 
+/* Snapshot records (Integrator::saveData, integration_schemes.cpp:266-331,
+ * SaveDataOptions, structures.h:244-247): one record per particle with status
+ * 1 or 2 and index in [first, last), in index order; last < 0 means n.
+ *   SV_SNAPSHOT_ORIGINAL: x, y, z, vx, vy, vz, E1[3], E2[3] (float32), species
+ *     (uint32), index (int32), lastParticle (int32): 60 bytes per record;
+ *   SV_SNAPSHOT_NEW_ORIGINAL: a 12-byte header (0xffffffff, lastParticle,
+ *     currentTime as float32), then index (int32), species (uint32), x, y, z,
+ *     vx, vy, vz, E1[3], E2[3] (float32): 56 bytes per record.
+ * lastParticle is `last`, currentTime is current_time.  E1 and E2 are the
+ * particle-particle field, (amu/e)(m/q) a (Integrator::updateAcceleration,
+ * :336-367), and the background field (particles.cpp:512) at the particle's
+ * last kick of sv_leapfrog as a target (zero before its first one), as the
+ * reference's Efield1 / Efield2 arrays hold them.
+ * *bytes receives the size; out (cap_bytes) may be null to query it.  The
+ * records go to the file as they are (fwrite). */
+typedef enum {
+    SV_SNAPSHOT_ORIGINAL = 0,     /* SaveDataOptions::original */
+    SV_SNAPSHOT_NEW_ORIGINAL = 1  /* SaveDataOptions::newOriginal */
+} sv_snapshot_format;
+
+SV_API sv_status sv_snapshot(sv_ctx *ctx, int32_t format, int64_t first, int64_t last, float current_time,
+                             void *out, int64_t cap_bytes, int64_t *bytes);
+
 /* Multi-rate leapfrog (LeapfrogDKDSubsteps, integration_schemes.cpp:899-1528).
  * Each entry asks for steps of at most dt inside a region: spatial limits
  * bc_space (|x|, |y|, |z|, r; 0 = unbounded) and/or a limit bc_time on the

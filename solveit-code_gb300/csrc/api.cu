@@ -128,11 +128,12 @@ void free_state(sv_ctx *c) {
     cudaFree(c->x); cudaFree(c->y); cudaFree(c->z);
     cudaFree(c->vx); cudaFree(c->vy); cudaFree(c->vz);
     cudaFree(c->q); cudaFree(c->m); cudaFree(c->t_inj); cudaFree(c->status); cudaFree(c->qom);
-    cudaFree(c->species); cudaFree(c->wstatus);
+    cudaFree(c->species); cudaFree(c->wstatus); cudaFree(c->e2); cudaFree(c->e1);
     cudaFree(c->ax); cudaFree(c->ay); cudaFree(c->az);
     c->x = c->y = c->z = c->vx = c->vy = c->vz = c->q = c->m = c->t_inj = c->qom = nullptr;
     c->ax = c->ay = c->az = nullptr;
     c->status = c->species = c->wstatus = nullptr;
+    c->e2 = c->e1 = nullptr;
     c->cap = 0;
 }
 
@@ -146,6 +147,7 @@ sv_status ensure_capacity(sv_ctx *c, int64_t n) {
     SV_TRY(dev_alloc(c, &c->qom, cap));
     SV_TRY(dev_alloc(c, &c->status, cap));
     SV_TRY(dev_alloc(c, &c->species, cap)); SV_TRY(dev_alloc(c, &c->wstatus, cap));
+    SV_TRY(dev_alloc(c, &c->e2, 3 * cap)); SV_TRY(dev_alloc(c, &c->e1, 3 * cap));
     SV_TRY(dev_alloc(c, &c->ax, cap)); SV_TRY(dev_alloc(c, &c->ay, cap)); SV_TRY(dev_alloc(c, &c->az, cap));
     c->cap = cap;
     return SV_OK;
@@ -454,6 +456,8 @@ static sv_status upload_state(sv_ctx *c, int64_t n, const double *x3, const doub
     SV_TRY(field_reset(c));
     SV_TRY(substeps_reset_levels(c));
     if (n == 0) return SV_OK;
+    SV_CK(c, cudaMemsetAsync(c->e2, 0, sizeof(float) * 3 * (size_t)n, c->stream));
+    SV_CK(c, cudaMemsetAsync(c->e1, 0, sizeof(float) * 3 * (size_t)n, c->stream));
     const size_t b3 = sizeof(double) * 3 * (size_t)n, b1 = sizeof(double) * (size_t)n;
     void *stg = nullptr;
     SV_TRY(stage_bytes(c, 2 * b3 + 3 * b1 + sizeof(int32_t) * (size_t)n, &stg));
@@ -504,6 +508,8 @@ sv_status sv_upload_ref32(sv_ctx *c, int64_t n, const float *pos4, const float *
     SV_TRY(field_reset(c));
     SV_TRY(substeps_reset_levels(c));
     if (n == 0) return SV_OK;
+    SV_CK(c, cudaMemsetAsync(c->e2, 0, sizeof(float) * 3 * (size_t)n, c->stream));
+    SV_CK(c, cudaMemsetAsync(c->e1, 0, sizeof(float) * 3 * (size_t)n, c->stream));
     const size_t b4 = 16 * (size_t)n;
     void *stg = nullptr;
     SV_TRY(stage_bytes(c, 3 * b4 + 4 * (size_t)n, &stg));

@@ -207,7 +207,8 @@ __global__ void kick_kernel(double *__restrict__ vx, double *__restrict__ vy, do
                             const double *__restrict__ t_inj, int64_t n, double t_start, double dt,
                             double eoa, double ex, double ey, double ez, const double *__restrict__ tb,
                             const double *__restrict__ x, const double *__restrict__ y,
-                            const double *__restrict__ z, FieldMesh M) {
+                            const double *__restrict__ z, FieldMesh M, float *__restrict__ e2,
+                            float *__restrict__ e1) {
     if (tb) t_start += tb[0] + tb[1] * tb[2];
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
@@ -224,6 +225,15 @@ __global__ void kick_kernel(double *__restrict__ vx, double *__restrict__ vy, do
             fy += gy;
             fz += gz;
         }
+        // the fields of the snapshot records: E1 = a / ((e/amu) q/m)
+        // (Integrator::updateAcceleration, integration_schemes.cpp:350-356), E2
+        const double inv = f != 0.0 ? 1.0 / f : 0.0;
+        e1[3 * i] = (float)(ax[i] * inv);
+        e1[3 * i + 1] = (float)(ay[i] * inv);
+        e1[3 * i + 2] = (float)(az[i] * inv);
+        e2[3 * i] = (float)fx;  // Efield2 of the snapshot records (particles.cpp:512)
+        e2[3 * i + 1] = (float)fy;
+        e2[3 * i + 2] = (float)fz;
         vx[i] += (ax[i] + fx * f) * s;
         vy[i] += (ay[i] + fy * f) * s;
         vz[i] += (az[i] + fz * f) * s;
@@ -363,7 +373,7 @@ sv_status drift(sv_ctx *c, double t_start, double h, int32_t *window, const doub
 sv_status kick(sv_ctx *c, double t_start, double dt, const int32_t *st, const double *tb) {
     kick_kernel<<<stream_grid(c->n), 256, 0, c->stream>>>(
         c->vx, c->vy, c->vz, c->ax, c->ay, c->az, c->qom, st, c->t_inj, c->n, t_start, dt,
-        c->P.e_over_amu, c->P.efield[0], c->P.efield[1], c->P.efield[2], tb, c->x, c->y, c->z, c->field);
+        c->P.e_over_amu, c->P.efield[0], c->P.efield[1], c->P.efield[2], tb, c->x, c->y, c->z, c->field, c->e2, c->e1);
     SV_LAUNCHED(c);
     return SV_OK;
 }

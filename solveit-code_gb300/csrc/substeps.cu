@@ -115,7 +115,8 @@ __global__ void substep_kick_kernel(double *__restrict__ vx, double *__restrict_
                                     const int32_t *__restrict__ win, const int8_t *__restrict__ lev,
                                     const double *__restrict__ t_inj, int64_t n, double t_vel, SubTable T,
                                     double eoa, double ex, double ey, double ez, const double *__restrict__ x,
-                                    const double *__restrict__ y, const double *__restrict__ z, FieldMesh M) {
+                                    const double *__restrict__ y, const double *__restrict__ z, FieldMesh M,
+                                    float *__restrict__ e2, float *__restrict__ e1) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         if (win[i] != 1) continue;
         const int l = lev[i];
@@ -132,6 +133,15 @@ __global__ void substep_kick_kernel(double *__restrict__ vx, double *__restrict_
             fy += gy;
             fz += gz;
         }
+        // the fields of the snapshot records: E1 = a / ((e/amu) q/m)
+        // (Integrator::updateAcceleration, integration_schemes.cpp:350-356), E2
+        const double inv = f != 0.0 ? 1.0 / f : 0.0;
+        e1[3 * i] = (float)(ax[i] * inv);
+        e1[3 * i + 1] = (float)(ay[i] * inv);
+        e1[3 * i + 2] = (float)(az[i] * inv);
+        e2[3 * i] = (float)fx;
+        e2[3 * i + 1] = (float)fy;
+        e2[3 * i + 2] = (float)fz;
         vx[i] += (ax[i] + fx * f) * s;
         vy[i] += (ay[i] + fy * f) * s;
         vz[i] += (az[i] + fz * f) * s;
@@ -214,7 +224,7 @@ struct Runner {
         SV_TRY(s);
         substep_kick_kernel<<<grid_n(c->n), 256, 0, c->stream>>>(
             c->vx, c->vy, c->vz, c->ax, c->ay, c->az, c->qom, c->wstatus, c->sub_level, c->t_inj, c->n, t_vel, T,
-            c->P.e_over_amu, c->P.efield[0], c->P.efield[1], c->P.efield[2], c->x, c->y, c->z, c->field);
+            c->P.e_over_amu, c->P.efield[0], c->P.efield[1], c->P.efield[2], c->x, c->y, c->z, c->field, c->e2, c->e1);
         SV_LAUNCHED(c);
         t_vel += T.dt[T.L];
         return SV_OK;

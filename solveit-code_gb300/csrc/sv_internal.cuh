@@ -87,6 +87,8 @@ struct sv_ctx {
     double *qom = nullptr;  // q/m (0 where m <= 0), set at upload: no FP64 division per step
     int32_t *status = nullptr;
     int32_t *species = nullptr;  // species code per particle (event records), 0xffffffff unknown
+    float *e2 = nullptr;         // 3n: background field (V/m) at each inbound particle's last kick (Efield2)
+    float *e1 = nullptr;         // 3n: particle-particle field (V/m) of each inbound particle's last kick (Efield1)
     // status the force and the kick see: the injection-windowed copy during a
     // leapfrog step (written by the first drift), else null (use status)
     int32_t *wstatus = nullptr;

@@ -21,6 +21,7 @@ SYM_NONE, SYM_ROTATIONAL, SYM_TRANSLATIONAL = 0, 1, 2
 MIXED, FP64 = 0, 1
 FMM_FMM, FMM_OUTLIERS, TREECODE, TREECODE_OUTLIERS = 0, 1, 2, 3
 CRASH_NONE, CRASH_EXTRACTOR_GRID = 0, 1
+SNAPSHOT_ORIGINAL, SNAPSHOT_NEW_ORIGINAL = 0, 1
 BC_NONE, BC_SPACE, BC_TIME, BC_SPACE_AND_TIME = 0, 1, 2, 3
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "allocation failed", 4: "bad state",
@@ -34,7 +35,7 @@ ABI_SYMBOLS = (
     "sv_launch_count", "sv_last_error", "sv_abi_version", "sv_adjoint_forward", "sv_adjoint_backward",
     "sv_direct_accel_noalloc", "sv_upload_batch", "sv_batch_tune", "sv_batch_get_info", "sv_batch_set_tuning",
     "sv_get_outliers", "sv_set_boundary", "sv_get_boundary", "sv_get_events", "sv_set_emitter_field",
-    "sv_emitter_field_at", "sv_set_substeps", "sv_get_substep_levels",
+    "sv_emitter_field_at", "sv_set_substeps", "sv_get_substep_levels", "sv_snapshot",
 )
 
 
@@ -145,6 +146,7 @@ def load(path: str = LIB_PATH):
                                        C.c_double]
     L.sv_emitter_field_at.argtypes = [vp, C.c_int64, vp, vp]
     L.sv_set_substeps.argtypes = [vp, C.c_double, C.c_int32, vp]
+    L.sv_snapshot.argtypes = [vp, C.c_int32, C.c_int64, C.c_int64, C.c_float, vp, C.c_int64, C.POINTER(C.c_int64)]
     L.sv_get_substep_levels.argtypes = [vp, vp]
     for name in ABI_SYMBOLS:
         if name not in ("sv_destroy", "sv_stream", "sv_launch_count", "sv_last_error", "sv_abi_version"):
@@ -326,6 +328,15 @@ class ForceMethod:
     def substep_levels(self):
         out = np.zeros(self.n, np.int8)
         self._check(self.L.sv_get_substep_levels(self.h, _p(out)))
+        return out
+
+    def snapshot(self, fmt=1, first=0, last=-1, current_time=0.0):
+        """The snapshot-file bytes of the current state (fmt: SNAPSHOT_ORIGINAL / SNAPSHOT_NEW_ORIGINAL)."""
+        nb = C.c_int64()
+        self._check(self.L.sv_snapshot(self.h, fmt, first, last, current_time, None, 0, C.byref(nb)))
+        out = np.zeros(nb.value, np.uint8)
+        self._check(self.L.sv_snapshot(self.h, fmt, first, last, current_time, out.ctypes.data, nb.value,
+                                       C.byref(nb)))
         return out
 
     def events(self):
