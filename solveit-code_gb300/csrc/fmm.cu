@@ -372,12 +372,20 @@ __host__ __device__ constexpr int slot1_rows() {
 }
 
 // Rotation / translation rows are RS = p rounded up to 4 floats (16-byte
-// rows, zero padded).  In shared memory the coefficients sit in rows of RS
-// complex values: A[n][m] by degree (n-major) for the rotations, B[k][n] by
-// order (k-major) for the z-translation; entries outside a row's range stay
-// zero, so whole float4 groups can be read without masks.
+// rows, zero padded).  In shared memory the coefficients sit in rows of SR =
+// RS + 2 complex values: A[n][m] by degree (n-major) for the rotations, B[k][n]
+// by order (k-major) for the z-translation; entries outside a row's range stay
+// zero, so whole float4 groups can be read without masks.  The 16-byte pad
+// puts the rows of up to 8 consecutive degrees in 8 different 16-byte bank
+// groups, so the lanes of a quarter warp (which read rows of different
+// degrees) do not conflict; the shared z-translation rows get a 16-byte pad
+// (ZR floats) for the same reason.
 template <int P>
 __host__ __device__ constexpr int rot_rs() { return (P + 3) / 4 * 4; }
+template <int P>
+__host__ __device__ constexpr int sh_rs() { return rot_rs<P>() + 2; }
+template <int P>
+__host__ __device__ constexpr int z_rs() { return rot_rs<P>() + 4; }
 
 // One output (n, mp) of a folded y-rotation: real part = E row . Re(A_n),
 // imaginary part = O row . Im(A_n) (the O row starts with a zero for m = 0).
@@ -390,7 +398,7 @@ __device__ __forceinline__ float2 rot_row(const float *__restrict__ D, int eoff,
     // group-major blocks: group q of row r at (q * rows + r) float4s from the block start
     const float4 *E = reinterpret_cast<const float4 *>(D + eoff + RS * (n * (n + 1) / 2)) + mp;
     const float4 *O = reinterpret_cast<const float4 *>(D + ooff + RS * (n * (n - 1) / 2)) + (mp > 0 ? mp - 1 : 0);
-    const float4 *A4 = reinterpret_cast<const float4 *>(A + n * RS);
+    const float4 *A4 = reinterpret_cast<const float4 *>(A + n * sh_rs<P>());
     float re = 0.f, im = 0.f;
 #pragma unroll
     for (int q = 0; q < G; q++) {
@@ -419,8 +427,8 @@ template <int P>
 __device__ __forceinline__ float2 ztrans_row(const float *__restrict__ zc, const float2 *Bk, int j, int k,
                                              float inv_rho) {
     constexpr int RS = rot_rs<P>();
-    const float4 *Z = reinterpret_cast<const float4 *>(zc + ((size_t)k * P + j) * RS);
-    const float4 *B4 = reinterpret_cast<const float4 *>(Bk + k * RS);
+    const float4 *Z = reinterpret_cast<const float4 *>(zc + ((size_t)k * P + j) * z_rs<P>());
+    const float4 *B4 = reinterpret_cast<const float4 *>(Bk + k * sh_rs<P>());
     float ip = inv_rho;
 #pragma unroll
     for (int q = 0; q < 2 * P - 2; q++)
@@ -457,7 +465,7 @@ template <int P>
 __device__ __forceinline__ float2 zshift_row(const float *__restrict__ zt, const float2 *Bk, int j, int k) {
     constexpr int RS = rot_rs<P>();
     const float4 *Z = reinterpret_cast<const float4 *>(zt + ((size_t)k * P + j) * RS);
-    const float4 *B4 = reinterpret_cast<const float4 *>(Bk + k * RS);
+    const float4 *B4 = reinterpret_cast<const float4 *>(Bk + k * sh_rs<P>());
     float re = 0.f, im = 0.f;
 #pragma unroll
     for (int q = 0; q < RS / 4; q++) {
@@ -479,17 +487,17 @@ __device__ __forceinline__ void oct_translate(const float2 *__restrict__ in, con
                                               const float *__restrict__ D, const float *__restrict__ Z, float2 *A,
                                               float2 *B, const int *cn, const int *cm, const int *cs,
                                               const bool *has, float2 *acc) {
-    constexpr int RS = rot_rs<P>(), G0 = RS / 4, G1 = slot1_rows<P>() / 4 + 1;
+    constexpr int RS = rot_rs<P>(), SR = sh_rs<P>(), G0 = RS / 4, G1 = slot1_rows<P>() / 4 + 1;
     constexpr int ESZ = RS * P * (P + 1) / 2, OSZ = RS * P * (P - 1) / 2;
 #pragma unroll
     for (int t = 0; t < 2; t++)
-        if (has[t]) A[cn[t] * RS + cm[t]] = cmul(in[cs[t]], ph[cm[t]]);
+        if (has[t]) A[cn[t] * SR + cm[t]] = cmul(in[cs[t]], ph[cm[t]]);
     __syncwarp();
-    if (has[0]) B[cm[0] * RS + cn[0]] = rot_row<P, G0>(D, 0, ESZ, A, cn[0], cm[0]);
-    if (has[1]) B[cm[1] * RS + cn[1]] = rot_row<P, G1>(D, 0, ESZ, A, cn[1], cm[1]);
+    if (has[0]) B[cm[0] * SR + cn[0]] = rot_row<P, G0>(D, 0, ESZ, A, cn[0], cm[0]);
+    if (has[1]) B[cm[1] * SR + cn[1]] = rot_row<P, G1>(D, 0, ESZ, A, cn[1], cm[1]);
     __syncwarp();
-    if (has[0]) A[cn[0] * RS + cm[0]] = zshift_row<P>(Z, B, cn[0], cm[0]);
-    if (has[1]) A[cn[1] * RS + cm[1]] = zshift_row<P>(Z, B, cn[1], cm[1]);
+    if (has[0]) A[cn[0] * SR + cm[0]] = zshift_row<P>(Z, B, cn[0], cm[0]);
+    if (has[1]) A[cn[1] * SR + cm[1]] = zshift_row<P>(Z, B, cn[1], cm[1]);
     __syncwarp();
     if (has[0]) acc[0] = cadd(acc[0], cmul(rot_row<P, G0>(D, ESZ + OSZ, 2 * ESZ + OSZ, A, cn[0], cm[0]), cconj(ph[cm[0]])));
     if (has[1]) acc[1] = cadd(acc[1], cmul(rot_row<P, G1>(D, ESZ + OSZ, 2 * ESZ + OSZ, A, cn[1], cm[1]), cconj(ph[cm[1]])));
@@ -517,11 +525,11 @@ template <int P>
 __global__ void __launch_bounds__(kWarps * 32)
 m2m_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ child0, const int4 *__restrict__ ccoord,
            const float2 *__restrict__ Mc, float2 *__restrict__ Mp, const float *__restrict__ otab) {
-    constexpr int NC = ncoef(P), RS = rot_rs<P>();
+    constexpr int NC = ncoef(P), SR = sh_rs<P>();
     using O = OctOff<P>;
-    __shared__ __align__(16) float2 A[kWarps][P * RS], B[kWarps][P * RS];
+    __shared__ __align__(16) float2 A[kWarps][P * SR], B[kWarps][P * SR];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int t = lane; t < P * RS; t += 32) A[wid][t] = B[wid][t] = make_float2(0.f, 0.f);
+    for (int t = lane; t < P * SR; t += 32) A[wid][t] = B[wid][t] = make_float2(0.f, 0.f);
     __syncwarp();
     int cn[2], cm[2], cs[2];
     bool has[2];
@@ -550,15 +558,19 @@ constexpr int m2l_warps() { return P >= 10 ? 2 : 4; }
 // from global memory (L1/L2), one 16-byte row segment per lane and group.
 template <int P>
 __global__ void __launch_bounds__(m2l_warps<P>() * 32) m2l_kernel(M2LArgs a) {
-    constexpr int NC = ncoef(P), RS = rot_rs<P>(), WP = m2l_warps<P>();
-    __shared__ __align__(16) float2 A[WP][2][P * RS], B[WP][2][P * RS];
-    __shared__ __align__(16) float Zsh[P * P * RS];
-    for (int t = threadIdx.x; t < P * P * RS / 4; t += blockDim.x)
-        reinterpret_cast<float4 *>(Zsh)[t] = __ldg(reinterpret_cast<const float4 *>(a.zc) + t);
+    constexpr int NC = ncoef(P), RS = rot_rs<P>(), SR = sh_rs<P>(), ZR = z_rs<P>(), WP = m2l_warps<P>();
+    __shared__ __align__(16) float2 A[WP][2][P * SR], B[WP][2][P * SR];
+    __shared__ __align__(16) float Zsh[P * P * ZR];
+    // the table's rows (RS floats) into padded rows of ZR floats
+    for (int t = threadIdx.x; t < P * P * (ZR / 4); t += blockDim.x) {
+        const int row = t / (ZR / 4), g = t % (ZR / 4);
+        reinterpret_cast<float4 *>(Zsh)[t] =
+            g < RS / 4 ? __ldg(reinterpret_cast<const float4 *>(a.zc) + row * (RS / 4) + g) : make_float4(0, 0, 0, 0);
+    }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int t = lane; t < 2 * P * RS; t += 32) {
-        A[wid][t / (P * RS)][t % (P * RS)] = make_float2(0.f, 0.f);
-        B[wid][t / (P * RS)][t % (P * RS)] = make_float2(0.f, 0.f);
+    for (int t = lane; t < 2 * P * SR; t += 32) {
+        A[wid][t / (P * SR)][t % (P * SR)] = make_float2(0.f, 0.f);
+        B[wid][t / (P * SR)][t % (P * SR)] = make_float2(0.f, 0.f);
     }
     __syncthreads();
     const int gw = blockIdx.x * WP + wid;
@@ -601,20 +613,20 @@ __global__ void __launch_bounds__(m2l_warps<P>() * 32) m2l_kernel(M2LArgs a) {
         for (int u = 0; u < 2; u++)
 #pragma unroll
             for (int t = 0; t < 2; t++)
-                if (has[t]) A[wid][u][cn[t] * RS + cm[t]] = cmul(Ml[(size_t)src[u] * NC + cs[t]], ph[u][cm[t]]);
+                if (has[t]) A[wid][u][cn[t] * SR + cm[t]] = cmul(Ml[(size_t)src[u] * NC + cs[t]], ph[u][cm[t]]);
         __syncwarp();
         // forward y-rotation (folded real matrices), into the order-major rows
 #pragma unroll
         for (int u = 0; u < 2; u++) {
-            if (has[0]) B[wid][u][cm[0] * RS + cn[0]] = rot_row<P, G0>(D[u], 0, a.esz, &A[wid][u][0], cn[0], cm[0]);
-            if (has[1]) B[wid][u][cm[1] * RS + cn[1]] = rot_row<P, G1>(D[u], 0, a.esz, &A[wid][u][0], cn[1], cm[1]);
+            if (has[0]) B[wid][u][cm[0] * SR + cn[0]] = rot_row<P, G0>(D[u], 0, a.esz, &A[wid][u][0], cn[0], cm[0]);
+            if (has[1]) B[wid][u][cm[1] * SR + cn[1]] = rot_row<P, G1>(D[u], 0, a.esz, &A[wid][u][0], cn[1], cm[1]);
         }
         __syncwarp();
         // translation along z: L'_j^k = sum_n C[k][j][n] rho^-(j+n+1) M'_n^k
 #pragma unroll
         for (int u = 0; u < 2; u++) {
-            if (has[0]) A[wid][u][cn[0] * RS + cm[0]] = ztrans_row<P>(Zsh, &B[wid][u][0], cn[0], cm[0], inv_rho[u]);
-            if (has[1]) A[wid][u][cn[1] * RS + cm[1]] = ztrans_row<P>(Zsh, &B[wid][u][0], cn[1], cm[1], inv_rho[u]);
+            if (has[0]) A[wid][u][cn[0] * SR + cm[0]] = ztrans_row<P>(Zsh, &B[wid][u][0], cn[0], cm[0], inv_rho[u]);
+            if (has[1]) A[wid][u][cn[1] * SR + cm[1]] = ztrans_row<P>(Zsh, &B[wid][u][0], cn[1], cm[1], inv_rho[u]);
         }
         __syncwarp();
         // backward y-rotation and phase e^{-i k phi}
@@ -644,11 +656,11 @@ __global__ void __launch_bounds__(m2l_warps<P>() * 32) m2l_kernel(M2LArgs a) {
 // z-shift table
 template <int P>
 __global__ void __launch_bounds__(kWarps * 32) l2l_kernel(L2LArgs a) {
-    constexpr int NC = ncoef(P), RS = rot_rs<P>();
+    constexpr int NC = ncoef(P), SR = sh_rs<P>();
     using O = OctOff<P>;
-    __shared__ __align__(16) float2 A[kWarps][P * RS], B[kWarps][P * RS];
+    __shared__ __align__(16) float2 A[kWarps][P * SR], B[kWarps][P * SR];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int t = lane; t < P * RS; t += 32) A[wid][t] = B[wid][t] = make_float2(0.f, 0.f);
+    for (int t = lane; t < P * SR; t += 32) A[wid][t] = B[wid][t] = make_float2(0.f, 0.f);
     __syncwarp();
     int cn[2], cm[2], cs[2];
     bool has[2];
