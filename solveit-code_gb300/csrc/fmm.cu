@@ -378,14 +378,16 @@ __host__ __device__ constexpr int slot1_rows() {
 // zero, so whole float4 groups can be read without masks.  The 16-byte pad
 // puts the rows of up to 8 consecutive degrees in 8 different 16-byte bank
 // groups, so the lanes of a quarter warp (which read rows of different
-// degrees) do not conflict; the shared z-translation rows get a 16-byte pad
-// (ZR floats) for the same reason.
+// degrees) do not conflict.  The shared z-translation table keeps rows (k, j)
+// of RS floats at k * ZK + j * RS, with the order stride ZK padded by a few
+// 16-byte groups (chosen by counting, per order p, the bank groups the lanes
+// of each quarter warp hit).
 template <int P>
 __host__ __device__ constexpr int rot_rs() { return (P + 3) / 4 * 4; }
 template <int P>
 __host__ __device__ constexpr int sh_rs() { return rot_rs<P>() + 2; }
 template <int P>
-__host__ __device__ constexpr int z_rs() { return rot_rs<P>() + 4; }
+__host__ __device__ constexpr int z_ks() { return P * rot_rs<P>() + 4 * (P >= 10 ? 7 : (P <= 4 ? 0 : 3)); }
 
 // One output (n, mp) of a folded y-rotation: real part = E row . Re(A_n),
 // imaginary part = O row . Im(A_n) (the O row starts with a zero for m = 0).
@@ -427,7 +429,7 @@ template <int P>
 __device__ __forceinline__ float2 ztrans_row(const float *__restrict__ zc, const float2 *Bk, int j, int k,
                                              float inv_rho) {
     constexpr int RS = rot_rs<P>();
-    const float4 *Z = reinterpret_cast<const float4 *>(zc + ((size_t)k * P + j) * z_rs<P>());
+    const float4 *Z = reinterpret_cast<const float4 *>(zc + k * z_ks<P>() + j * RS);
     const float4 *B4 = reinterpret_cast<const float4 *>(Bk + k * sh_rs<P>());
     float ip = inv_rho;
 #pragma unroll
@@ -552,23 +554,26 @@ m2m_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ child0
 
 template <int P>
 constexpr int m2l_warps() { return P >= 10 ? 2 : 4; }
+// list entries a warp carries through one pass of the M2L loop
+template <int P>
+constexpr int m2l_inflight() { return 2; }
 
 // The z-translation table (the same for every entry) is staged once per CTA
 // in shared memory; the rotation rows of each entry's polar angle are read
 // from global memory (L1/L2), one 16-byte row segment per lane and group.
 template <int P>
 __global__ void __launch_bounds__(m2l_warps<P>() * 32) m2l_kernel(M2LArgs a) {
-    constexpr int NC = ncoef(P), RS = rot_rs<P>(), SR = sh_rs<P>(), ZR = z_rs<P>(), WP = m2l_warps<P>();
-    __shared__ __align__(16) float2 A[WP][2][P * SR], B[WP][2][P * SR];
-    __shared__ __align__(16) float Zsh[P * P * ZR];
-    // the table's rows (RS floats) into padded rows of ZR floats
-    for (int t = threadIdx.x; t < P * P * (ZR / 4); t += blockDim.x) {
-        const int row = t / (ZR / 4), g = t % (ZR / 4);
-        reinterpret_cast<float4 *>(Zsh)[t] =
-            g < RS / 4 ? __ldg(reinterpret_cast<const float4 *>(a.zc) + row * (RS / 4) + g) : make_float4(0, 0, 0, 0);
+    constexpr int NC = ncoef(P), RS = rot_rs<P>(), SR = sh_rs<P>(), ZK = z_ks<P>(), WP = m2l_warps<P>();
+    constexpr int NU = m2l_inflight<P>();
+    __shared__ __align__(16) float2 A[WP][NU][P * SR], B[WP][NU][P * SR];
+    __shared__ __align__(16) float Zsh[P * ZK];
+    // the table's rows (k, j), RS floats each, to k * ZK + j * RS
+    for (int t = threadIdx.x; t < P * P * (RS / 4); t += blockDim.x) {
+        const int row = t / (RS / 4), g = t % (RS / 4), k = row / P, j = row % P;
+        reinterpret_cast<float4 *>(Zsh + k * ZK + j * RS)[g] = __ldg(reinterpret_cast<const float4 *>(a.zc) + t);
     }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int t = lane; t < 2 * P * SR; t += 32) {
+    for (int t = lane; t < NU * P * SR; t += 32) {
         A[wid][t / (P * SR)][t % (P * SR)] = make_float2(0.f, 0.f);
         B[wid][t / (P * SR)][t % (P * SR)] = make_float2(0.f, 0.f);
     }
@@ -598,41 +603,48 @@ __global__ void __launch_bounds__(m2l_warps<P>() * 32) m2l_kernel(M2LArgs a) {
     const int e0 = ch * per, e1 = min(cnt, e0 + per);
     const int2 *lst = a.lv[li].m2l + (size_t)b * a.cap;
     const float2 *Ml = a.lv[li].M;
-    // two entries in flight per iteration: their loads and the warp
-    // synchronisations overlap (the second is skipped past the range's end)
+    // NU entries in flight per iteration: their loads and the warp
+    // synchronisations overlap (entries past the range's end repeat the last
+    // one and are not accumulated)
     constexpr int G0 = RS / 4, G1 = slot1_rows<P>() / 4 + 1;
-    for (int e = e0; e < e1; e += 2) {
-        const bool v1 = e + 1 < e1;
-        const int2 en0 = lst[e], en1 = v1 ? lst[e + 1] : en0;
-        const int src[2] = {en0.x, en1.x};
-        const float2 *ph[2] = {a.cls_phase + (size_t)en0.y * P, a.cls_phase + (size_t)en1.y * P};
-        const float *D[2] = {a.dmat + (size_t)a.cls_theta[en0.y] * a.dsz, a.dmat + (size_t)a.cls_theta[en1.y] * a.dsz};
-        const float inv_rho[2] = {rsqrtf(a.cls_rho2[en0.y] + eh2), rsqrtf(a.cls_rho2[en1.y] + eh2)};
+    for (int e = e0; e < e1; e += NU) {
+        int src[NU];
+        const float2 *ph[NU];
+        const float *D[NU];
+        float inv_rho[NU];
+#pragma unroll
+        for (int u = 0; u < NU; u++) {
+            const int2 en = lst[min(e + u, e1 - 1)];
+            src[u] = en.x;
+            ph[u] = a.cls_phase + (size_t)en.y * P;
+            D[u] = a.dmat + (size_t)a.cls_theta[en.y] * a.dsz;
+            inv_rho[u] = rsqrtf(a.cls_rho2[en.y] + eh2);
+        }
         // phase e^{i m phi}, into the degree-major rows
 #pragma unroll
-        for (int u = 0; u < 2; u++)
+        for (int u = 0; u < NU; u++)
 #pragma unroll
             for (int t = 0; t < 2; t++)
                 if (has[t]) A[wid][u][cn[t] * SR + cm[t]] = cmul(Ml[(size_t)src[u] * NC + cs[t]], ph[u][cm[t]]);
         __syncwarp();
         // forward y-rotation (folded real matrices), into the order-major rows
 #pragma unroll
-        for (int u = 0; u < 2; u++) {
+        for (int u = 0; u < NU; u++) {
             if (has[0]) B[wid][u][cm[0] * SR + cn[0]] = rot_row<P, G0>(D[u], 0, a.esz, &A[wid][u][0], cn[0], cm[0]);
             if (has[1]) B[wid][u][cm[1] * SR + cn[1]] = rot_row<P, G1>(D[u], 0, a.esz, &A[wid][u][0], cn[1], cm[1]);
         }
         __syncwarp();
         // translation along z: L'_j^k = sum_n C[k][j][n] rho^-(j+n+1) M'_n^k
 #pragma unroll
-        for (int u = 0; u < 2; u++) {
+        for (int u = 0; u < NU; u++) {
             if (has[0]) A[wid][u][cn[0] * SR + cm[0]] = ztrans_row<P>(Zsh, &B[wid][u][0], cn[0], cm[0], inv_rho[u]);
             if (has[1]) A[wid][u][cn[1] * SR + cm[1]] = ztrans_row<P>(Zsh, &B[wid][u][0], cn[1], cm[1], inv_rho[u]);
         }
         __syncwarp();
         // backward y-rotation and phase e^{-i k phi}
 #pragma unroll
-        for (int u = 0; u < 2; u++) {
-            if (u == 1 && !v1) break;
+        for (int u = 0; u < NU; u++) {
+            if (e + u >= e1) break;
             if (has[0]) {
                 const float2 r =
                     rot_row<P, G0>(D[u], a.esz + a.osz, 2 * a.esz + a.osz, &A[wid][u][0], cn[0], cm[0]);
