@@ -109,7 +109,10 @@ typedef struct {
     double flops_algorithmic;     /* 20 flop/pair + expansion flops (method's count) */
     double ms_total;              /* device time of the whole evaluation */
     double ms_phase[8];           /* sort, tree, lists, upward (P2M+M2M), downward (M2L+L2L),
-                                     L2P, near field (P2P / direct / BH walk), scatter */
+                                     L2P, near field (P2P / direct / BH walk), scatter; the FMM
+                                     runs its near field on a second stream beside the upward
+                                     and downward passes, so its entry is the P2P's own device
+                                     time and overlaps them */
     int32_t levels;               /* FMM leaf level / BH max depth */
     int32_t boxes;                /* occupied leaf boxes / BH nodes */
     int32_t reserved[6];

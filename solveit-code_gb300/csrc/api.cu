@@ -571,6 +571,7 @@ sv_status sv::compute_accel_device(sv_ctx *c, int64_t first, int64_t last) {
     if (last > c->n || last < 0) last = c->n;
     const int64_t n = c->n;
     memset(&c->stats, 0, sizeof(c->stats));
+    c->near_ev[0] = c->near_ev[1] = nullptr;  // set by an FMM evaluation that times its near field
     if (c->batch) {
         SV_CK(c, cudaEventRecord(c->ev_begin, c->stream));
         SV_TRY(batch_accel(c));
@@ -793,6 +794,9 @@ sv_status sv_get_stats(const sv_ctx *cc, sv_stats *out) {
             float t = 0.f;
             c->stats.ms_phase[k] = cudaEventElapsedTime(&t, c->ph_ev[k], c->ph_ev[k + 1]) == cudaSuccess ? t : 0.0;
         }
+        float t = 0.f;
+        if (c->near_ev[0] && cudaEventElapsedTime(&t, c->near_ev[0], c->near_ev[1]) == cudaSuccess)
+            c->stats.ms_phase[6] = t;
     }
     *out = c->stats;
     float ms = 0.f;

@@ -75,6 +75,9 @@ struct Fmm {
     int2 *flst[kMortonBits + 1] = {};
     float4 *frel = nullptr;
     int64_t frel_cap = 0;
+    // the near field runs on its own stream beside the upward and downward passes
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_near[2] = {};
 };
 
 namespace {
@@ -714,14 +717,15 @@ l2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, 
            const int4 *__restrict__ coord, const double *__restrict__ xs, const double *__restrict__ ys,
            const double *__restrict__ zs, const double *__restrict__ qm, const double *__restrict__ roots, int level,
            const float *__restrict__ nrm, const float2 *__restrict__ Lc, double *__restrict__ ax,
-           double *__restrict__ ay, double *__restrict__ az, const int *__restrict__ has_tgt) {
+           double *__restrict__ ay, double *__restrict__ az, const int *__restrict__ has_tgt, int accumulate) {
     constexpr int NC = ncoef(P);
     __shared__ float2 lam[kWarps][NC];
     SV_WARP_BOXES(kWarps) {
     const double *root = box_root(roots, bpid, b);
     if (!has_tgt[b]) {
         // boxes of image copies only: no targets, zero acceleration
-        for (int i = start[b] + lane; i < start[b + 1]; i += 32) ax[i] = ay[i] = az[i] = 0.0;
+        if (!accumulate)
+            for (int i = start[b] + lane; i < start[b + 1]; i += 32) ax[i] = ay[i] = az[i] = 0.0;
         continue;
     }
     for (int c = lane; c < NC; c += 32) {
@@ -754,11 +758,18 @@ l2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, 
 #pragma unroll
             for (int t = 0; t + 1 < n; t++) gm = cadd(gm, cscale(cconj(cmul(ln[t], R[cidx(n - 1, t + 1)])), -1.f));
         }
-        // a = -grad(phi) * K q / m, grad in box units / h^2
+        // a = -grad(phi) * K q / m, grad in box units / h^2 (added to the
+        // near field when that ran first)
         const double f = -qm[i] * ih * ih;
-        ax[i] = f * (double)gm.x;
-        ay[i] = f * (double)(-gm.y);
-        az[i] = f * (double)gz;
+        if (accumulate) {
+            ax[i] += f * (double)gm.x;
+            ay[i] += f * (double)(-gm.y);
+            az[i] += f * (double)gz;
+        } else {
+            ax[i] = f * (double)gm.x;
+            ay[i] = f * (double)(-gm.y);
+            az[i] = f * (double)gz;
+        }
     }
     __syncwarp();
     }
@@ -816,6 +827,7 @@ struct TreecodeArgs {
     const float *nrm;
     double eps2;
     double *ax, *ay, *az;
+    int accumulate;  // 1: add to ax (the near field ran first), 0: overwrite
 };
 
 template <int P>
@@ -827,7 +839,8 @@ __global__ void __launch_bounds__(kWarps * 32) m2p_kernel(TreecodeArgs a) {
     if (b >= a.nleaf) return;
     const int s0 = a.leaf_start[b], s1 = a.leaf_start[b + 1];
     if (!a.has_tgt[b]) {
-        for (int i = s0 + lane; i < s1; i += 32) a.ax[i] = a.ay[i] = a.az[i] = 0.0;
+        if (!a.accumulate)
+            for (int i = s0 + lane; i < s1; i += 32) a.ax[i] = a.ay[i] = a.az[i] = 0.0;
         return;
     }
     const int R = 2 * a.ws + 1, SIDE = 2 * R + 1;
@@ -889,9 +902,15 @@ __global__ void __launch_bounds__(kWarps * 32) m2p_kernel(TreecodeArgs a) {
         if (valid) {
             // a = -K q/m grad(phi)
             const double c = a.qm[i];
-            a.ax[i] = -c * gx;
-            a.ay[i] = -c * gy;
-            a.az[i] = -c * gz;
+            if (a.accumulate) {
+                a.ax[i] += -c * gx;
+                a.ay[i] += -c * gy;
+                a.az[i] += -c * gz;
+            } else {
+                a.ax[i] = -c * gx;
+                a.ay[i] = -c * gy;
+                a.az[i] = -c * gz;
+            }
         }
     }
 }
@@ -1247,6 +1266,36 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         SV_LAUNCHED(c);
     }
     phase_mark(c, 3);
+    // near field on its own stream, beside the upward and downward passes: it
+    // needs only the sorted particles, the leaf boxes and their near lists.
+    // It sums into the zeroed accelerations; L2P adds the far field after the join.
+    {
+        const Level &V = T.lv[L];
+        if (F.rel_cap < c->S.n) {
+            cudaFree(F.rel);
+            F.rel = nullptr;
+            SV_CK(c, cudaMalloc(&F.rel, sizeof(float4) * c->S.n));
+            F.rel_cap = c->S.n;
+        }
+        SV_CK(c, cudaEventRecord(F.ev_fork, c->stream));
+        SV_CK(c, cudaStreamWaitEvent(F.side, F.ev_fork, 0));
+        SV_CK(c, cudaMemsetAsync(S.ax, 0, sizeof(double) * c->S.n, F.side));
+        SV_CK(c, cudaMemsetAsync(S.ay, 0, sizeof(double) * c->S.n, F.side));
+        SV_CK(c, cudaMemsetAsync(S.az, 0, sizeof(double) * c->S.n, F.side));
+        box_relative_kernel<<<div_up(V.nbox, kWarps), kWarps * 32, 0, F.side>>>(
+            V.nbox, nullptr, nullptr, V.start, V.coord, S.x, S.y, S.z, S.q, S.root, L, F.rel);
+        SV_LAUNCHED(c);
+        if (c->P.profile_phases) SV_CK(c, cudaEventRecord(F.ev_near[0], F.side));
+        launch_p2p(ws, (float)c->P.softening2, div_up(V.nbox, kWarps), F.side, V.nbox, nullptr, nullptr, V.start,
+                   V.coord, nbr[L], S.qm, S.root, L, S.ax, S.ay, S.az, F.d_counts, tgt[L], F.rel);
+        SV_LAUNCHED(c);
+        if (c->P.profile_phases) {
+            SV_CK(c, cudaEventRecord(F.ev_near[1], F.side));
+            c->near_ev[0] = F.ev_near[0];
+            c->near_ev[1] = F.ev_near[1];
+        }
+        SV_CK(c, cudaEventRecord(F.ev_join, F.side));
+    }
     // upward pass
     {
         const Level &V = T.lv[L];
@@ -1314,7 +1363,8 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         }
     }
     phase_mark(c, 5);
-    // far field then near field, written in sorted order
+    // far field, added to the near field once that has finished
+    SV_CK(c, cudaStreamWaitEvent(c->stream, F.ev_join, 0));
     {
         const Level &V = T.lv[L];
         if (L >= 2 && treecode) {
@@ -1342,31 +1392,16 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
             ta.ax = S.ax;
             ta.ay = S.ay;
             ta.az = S.az;
+            ta.accumulate = 1;
             m2p_kernel<P><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(ta);
             SV_LAUNCHED(c);
         } else if (L >= 2) {
             l2p_kernel<P><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
                 V.nbox, nullptr, nullptr, V.start, V.coord, S.x, S.y, S.z, S.qm, S.root, L, F.nrm, Lv[L], S.ax, S.ay,
-                S.az, tgt[L]);
+                S.az, tgt[L], 1);
             SV_LAUNCHED(c);
-        } else {
-            SV_CK(c, cudaMemsetAsync(S.ax, 0, sizeof(double) * c->S.n, c->stream));
-            SV_CK(c, cudaMemsetAsync(S.ay, 0, sizeof(double) * c->S.n, c->stream));
-            SV_CK(c, cudaMemsetAsync(S.az, 0, sizeof(double) * c->S.n, c->stream));
         }
         phase_mark(c, 6);
-        if (F.rel_cap < c->S.n) {
-            cudaFree(F.rel);
-            F.rel = nullptr;
-            SV_CK(c, cudaMalloc(&F.rel, sizeof(float4) * c->S.n));
-            F.rel_cap = c->S.n;
-        }
-        box_relative_kernel<<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
-            V.nbox, nullptr, nullptr, V.start, V.coord, S.x, S.y, S.z, S.q, S.root, L, F.rel);
-        SV_LAUNCHED(c);
-        launch_p2p(ws, (float)c->P.softening2, div_up(V.nbox, kWarps), c->stream, V.nbox, nullptr, nullptr, V.start,
-                   V.coord, nbr[L], S.qm, S.root, L, S.ax, S.ay, S.az, F.d_counts, tgt[L], F.rel);
-        SV_LAUNCHED(c);
     }
     SV_CK(c, cudaMemcpyAsync(F.h_counts, F.d_counts, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                              c->stream));
@@ -1486,7 +1521,7 @@ sv_status run_fmm_forest(sv_ctx *c, Fmm &F, const ForestArgs &fa) {
         const int g = forest_grid(f.cap[L], kWarps);
         l2p_kernel<P><<<g, kWarps * 32, 0, c->stream>>>(f.cap[L], nbd + L, V.pid, V.start, V.coord, S.x, S.y, S.z,
                                                         S.qm, fa.roots, L, F.nrm, F.fL[L], S.ax, S.ay, S.az,
-                                                        F.ftgt[L]);
+                                                        F.ftgt[L], 0);
         SV_LAUNCHED(c);
         box_relative_kernel<<<g, kWarps * 32, 0, c->stream>>>(f.cap[L], nbd + L, V.pid, V.start, V.coord, S.x, S.y,
                                                               S.z, S.q, fa.roots, L, F.frel);
@@ -1541,6 +1576,12 @@ void fmm_free(sv_ctx *c) {
         delete F.ftree;
     }
     cudaFreeHost(F.h_counts);
+    if (F.side) cudaStreamDestroy(F.side);
+    if (F.ev_fork) cudaEventDestroy(F.ev_fork);
+    if (F.ev_join) cudaEventDestroy(F.ev_join);
+    for (cudaEvent_t e : F.ev_near)
+        if (e) cudaEventDestroy(e);
+    c->near_ev[0] = c->near_ev[1] = nullptr;
     delete c->fmm;
     c->fmm = nullptr;
 }
@@ -1548,8 +1589,14 @@ void fmm_free(sv_ctx *c) {
 static sv_status fmm_state(sv_ctx *c) {
     if (!c->fmm) {
         c->fmm = new Fmm();
-        SV_CK(c, cudaMalloc(&c->fmm->d_counts, 2 * sizeof(unsigned long long)));
-        SV_CK(c, cudaMallocHost(&c->fmm->h_counts, 2 * sizeof(unsigned long long)));
+        Fmm &F = *c->fmm;
+        SV_CK(c, cudaMalloc(&F.d_counts, 2 * sizeof(unsigned long long)));
+        SV_CK(c, cudaMallocHost(&F.h_counts, 2 * sizeof(unsigned long long)));
+        SV_CK(c, cudaStreamCreateWithFlags(&F.side, cudaStreamNonBlocking));
+        SV_CK(c, cudaEventCreateWithFlags(&F.ev_fork, cudaEventDisableTiming));
+        SV_CK(c, cudaEventCreateWithFlags(&F.ev_join, cudaEventDisableTiming));
+        SV_CK(c, cudaEventCreate(&F.ev_near[0]));
+        SV_CK(c, cudaEventCreate(&F.ev_near[1]));
     }
     return SV_OK;
 }

@@ -128,6 +128,9 @@ struct sv_ctx {
     // per-phase timing (sv_params.profile_phases): events 0..8 bracket the
     // phases sort, tree, lists, upward, downward, L2P, near field, scatter
     cudaEvent_t ph_ev[9] = {};
+    // the FMM's near field on its own stream: its start / end events (phase 6
+    // of the statistics is then its own duration, overlapping phases 3-5)
+    cudaEvent_t near_ev[2] = {};
     unsigned long long launches = 0;
     sv_stats stats{};
     char err[512] = {0};
