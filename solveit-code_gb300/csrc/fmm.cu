@@ -77,7 +77,7 @@ struct Fmm {
     int64_t frel_cap = 0;
     // the near field runs on its own stream beside the upward and downward passes
     cudaStream_t side = nullptr;
-    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_near[2] = {};
+    cudaEvent_t ev_fork = nullptr, ev_lists = nullptr, ev_join = nullptr, ev_near[2] = {};
 };
 
 namespace {
@@ -1227,8 +1227,6 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
     }
     phase_mark(c, 2);
     SV_CK(c, cudaMemsetAsync(F.d_counts, 0, 2 * sizeof(unsigned long long), c->stream));
-    root_nbr_kernel<<<1, 128, 0, c->stream>>>(nbr[0], ns, 1, nullptr);
-    SV_LAUNCHED(c);
     // which boxes hold targets (all of them unless symmetry images are present)
     int *tgt[kMortonBits + 1];
     {
@@ -1245,40 +1243,45 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
             tgt[l] = F.has_tgt + o;
             o += T.lv[l].nbox;
         }
-        leaf_targets_kernel<<<div_up(T.lv[L].nbox, 256), 256, 0, c->stream>>>(T.lv[L].nbox, nullptr,
-                                                                                T.lv[L].start, S.qm, tgt[L]);
+    }
+    if (F.rel_cap < c->S.n) {
+        cudaFree(F.rel);
+        F.rel = nullptr;
+        SV_CK(c, cudaMalloc(&F.rel, sizeof(float4) * c->S.n));
+        F.rel_cap = c->S.n;
+    }
+    // Two streams from here on.  The second builds the target flags and the
+    // interaction lists, then runs the near field (P2P), which needs only the
+    // sorted particles, the leaf boxes and their near lists, summing into the
+    // zeroed accelerations.  The main stream runs the upward pass beside the
+    // lists, waits for them, runs M2L / L2L beside the near field, waits for
+    // it and adds the far field (L2P or the treecode's M2P).
+    SV_CK(c, cudaEventRecord(F.ev_fork, c->stream));
+    SV_CK(c, cudaStreamWaitEvent(F.side, F.ev_fork, 0));
+    root_nbr_kernel<<<1, 128, 0, F.side>>>(nbr[0], ns, 1, nullptr);
+    SV_LAUNCHED(c);
+    leaf_targets_kernel<<<div_up(T.lv[L].nbox, 256), 256, 0, F.side>>>(T.lv[L].nbox, nullptr, T.lv[L].start, S.qm,
+                                                                         tgt[L]);
+    SV_LAUNCHED(c);
+    for (int l = L - 1; l >= 0; l--) {
+        parent_targets_kernel<<<div_up(T.lv[l].nbox, 256), 256, 0, F.side>>>(T.lv[l].nbox, nullptr, T.lv[l].child0,
+                                                                              tgt[l + 1], tgt[l]);
         SV_LAUNCHED(c);
-        for (int l = L - 1; l >= 0; l--) {
-            parent_targets_kernel<<<div_up(T.lv[l].nbox, 256), 256, 0, c->stream>>>(
-                T.lv[l].nbox, nullptr, T.lv[l].child0, tgt[l + 1], tgt[l]);
-            SV_LAUNCHED(c);
-        }
     }
     for (int l = 1; l <= L; l++) {
         const Level &V = T.lv[l];
         const Level &U = T.lv[l - 1];
         if (ws == 1)
-            build_lists_kernel<1><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
+            build_lists_kernel<1><<<div_up(V.nbox, kWarps), kWarps * 32, 0, F.side>>>(
                 V.nbox, nullptr, V.parent, V.coord, nbr[l - 1], U.child0, nbr[l], lst[l], cnt[l], cap, F.d_counts);
         else
-            build_lists_kernel<2><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
+            build_lists_kernel<2><<<div_up(V.nbox, kWarps), kWarps * 32, 0, F.side>>>(
                 V.nbox, nullptr, V.parent, V.coord, nbr[l - 1], U.child0, nbr[l], lst[l], cnt[l], cap, F.d_counts);
         SV_LAUNCHED(c);
     }
-    phase_mark(c, 3);
-    // near field on its own stream, beside the upward and downward passes: it
-    // needs only the sorted particles, the leaf boxes and their near lists.
-    // It sums into the zeroed accelerations; L2P adds the far field after the join.
+    SV_CK(c, cudaEventRecord(F.ev_lists, F.side));
     {
         const Level &V = T.lv[L];
-        if (F.rel_cap < c->S.n) {
-            cudaFree(F.rel);
-            F.rel = nullptr;
-            SV_CK(c, cudaMalloc(&F.rel, sizeof(float4) * c->S.n));
-            F.rel_cap = c->S.n;
-        }
-        SV_CK(c, cudaEventRecord(F.ev_fork, c->stream));
-        SV_CK(c, cudaStreamWaitEvent(F.side, F.ev_fork, 0));
         SV_CK(c, cudaMemsetAsync(S.ax, 0, sizeof(double) * c->S.n, F.side));
         SV_CK(c, cudaMemsetAsync(S.ay, 0, sizeof(double) * c->S.n, F.side));
         SV_CK(c, cudaMemsetAsync(S.az, 0, sizeof(double) * c->S.n, F.side));
@@ -1296,6 +1299,7 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         }
         SV_CK(c, cudaEventRecord(F.ev_join, F.side));
     }
+    phase_mark(c, 3);
     // upward pass
     {
         const Level &V = T.lv[L];
@@ -1310,6 +1314,7 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         SV_LAUNCHED(c);
     }
     phase_mark(c, 4);
+    SV_CK(c, cudaStreamWaitEvent(c->stream, F.ev_lists, 0));
     const bool treecode = c->P.fmm_type == SV_FMM_TREECODE || c->P.fmm_type == SV_FMM_TREECODE_OUTLIERS;
     // downward pass: M2L of all levels in one launch, then L2L level by level
     // (the treecode evaluates multipoles at the particles instead)
@@ -1579,6 +1584,7 @@ void fmm_free(sv_ctx *c) {
     if (F.side) cudaStreamDestroy(F.side);
     if (F.ev_fork) cudaEventDestroy(F.ev_fork);
     if (F.ev_join) cudaEventDestroy(F.ev_join);
+    if (F.ev_lists) cudaEventDestroy(F.ev_lists);
     for (cudaEvent_t e : F.ev_near)
         if (e) cudaEventDestroy(e);
     c->near_ev[0] = c->near_ev[1] = nullptr;
@@ -1595,6 +1601,7 @@ static sv_status fmm_state(sv_ctx *c) {
         SV_CK(c, cudaStreamCreateWithFlags(&F.side, cudaStreamNonBlocking));
         SV_CK(c, cudaEventCreateWithFlags(&F.ev_fork, cudaEventDisableTiming));
         SV_CK(c, cudaEventCreateWithFlags(&F.ev_join, cudaEventDisableTiming));
+        SV_CK(c, cudaEventCreateWithFlags(&F.ev_lists, cudaEventDisableTiming));
         SV_CK(c, cudaEventCreate(&F.ev_near[0]));
         SV_CK(c, cudaEventCreate(&F.ev_near[1]));
     }
