@@ -1436,28 +1436,49 @@ sv_status run_fmm_forest(sv_ctx *c, Fmm &F, const ForestArgs &fa) {
     int *nbd = fa.d_nbox;
     SV_TRY(tree_build_forest(c, T, f, nbd, fa.d_err));
     SV_CK(c, cudaMemsetAsync(F.d_counts, 0, 2 * sizeof(unsigned long long), c->stream));
-    root_nbr_kernel<<<forest_grid(f.cap[0] * ns, 256), 256, 0, c->stream>>>(F.fnbr[0], ns, f.cap[0], nbd);
+    // Two streams, as in run_fmm: target flags, lists and the near field on the
+    // second (the forest's slots only: the direct plumes' slots belong to
+    // another stream), the upward and downward passes on the main one.
+    cudaStream_t sd = F.side;
+    SV_CK(c, cudaEventRecord(F.ev_fork, c->stream));
+    SV_CK(c, cudaStreamWaitEvent(sd, F.ev_fork, 0));
+    root_nbr_kernel<<<forest_grid(f.cap[0] * ns, 256), 256, 0, sd>>>(F.fnbr[0], ns, f.cap[0], nbd);
     SV_LAUNCHED(c);
-    leaf_targets_kernel<<<forest_grid(f.cap[L], 256), 256, 0, c->stream>>>(f.cap[L], nbd + L, T.lv[L].start, S.qm,
-                                                                         F.ftgt[L]);
+    leaf_targets_kernel<<<forest_grid(f.cap[L], 256), 256, 0, sd>>>(f.cap[L], nbd + L, T.lv[L].start, S.qm,
+                                                                  F.ftgt[L]);
     SV_LAUNCHED(c);
     for (int l = L - 1; l >= 0; l--) {
-        parent_targets_kernel<<<forest_grid(f.cap[l], 256), 256, 0, c->stream>>>(f.cap[l], nbd + l, T.lv[l].child0,
-                                                                               F.ftgt[l + 1], F.ftgt[l]);
+        parent_targets_kernel<<<forest_grid(f.cap[l], 256), 256, 0, sd>>>(f.cap[l], nbd + l, T.lv[l].child0,
+                                                                        F.ftgt[l + 1], F.ftgt[l]);
         SV_LAUNCHED(c);
     }
     for (int l = 1; l <= L; l++) {
         const Level &V = T.lv[l];
         const Level &U = T.lv[l - 1];
         if (ws == 1)
-            build_lists_kernel<1><<<forest_grid(f.cap[l], kWarps), kWarps * 32, 0, c->stream>>>(
+            build_lists_kernel<1><<<forest_grid(f.cap[l], kWarps), kWarps * 32, 0, sd>>>(
                 f.cap[l], nbd + l, V.parent, V.coord, F.fnbr[l - 1], U.child0, F.fnbr[l], F.flst[l], F.fcnt[l], cap,
                 F.d_counts);
         else
-            build_lists_kernel<2><<<forest_grid(f.cap[l], kWarps), kWarps * 32, 0, c->stream>>>(
+            build_lists_kernel<2><<<forest_grid(f.cap[l], kWarps), kWarps * 32, 0, sd>>>(
                 f.cap[l], nbd + l, V.parent, V.coord, F.fnbr[l - 1], U.child0, F.fnbr[l], F.flst[l], F.fcnt[l], cap,
                 F.d_counts);
         SV_LAUNCHED(c);
+    }
+    SV_CK(c, cudaEventRecord(F.ev_lists, sd));
+    {
+        const Level &V = T.lv[L];
+        const int g = forest_grid(f.cap[L], kWarps);
+        SV_CK(c, cudaMemsetAsync(S.ax, 0, sizeof(double) * f.n, sd));
+        SV_CK(c, cudaMemsetAsync(S.ay, 0, sizeof(double) * f.n, sd));
+        SV_CK(c, cudaMemsetAsync(S.az, 0, sizeof(double) * f.n, sd));
+        box_relative_kernel<<<g, kWarps * 32, 0, sd>>>(f.cap[L], nbd + L, V.pid, V.start, V.coord, S.x, S.y, S.z,
+                                                       S.q, fa.roots, L, F.frel);
+        SV_LAUNCHED(c);
+        launch_p2p(ws, (float)c->P.softening2, g, sd, f.cap[L], nbd + L, V.pid, V.start, V.coord, F.fnbr[L], S.qm,
+                   fa.roots, L, S.ax, S.ay, S.az, F.d_counts, F.ftgt[L], F.frel);
+        SV_LAUNCHED(c);
+        SV_CK(c, cudaEventRecord(F.ev_join, sd));
     }
     {
         const Level &V = T.lv[L];
@@ -1471,6 +1492,7 @@ sv_status run_fmm_forest(sv_ctx *c, Fmm &F, const ForestArgs &fa) {
             f.cap[l], nbd + l, V.child0, T.lv[l + 1].coord, F.fM[l + 1], F.fM[l], F.otab);
         SV_LAUNCHED(c);
     }
+    SV_CK(c, cudaStreamWaitEvent(c->stream, F.ev_lists, 0));
     {
         M2LArgs a{};
         a.cap = cap;
@@ -1521,18 +1543,13 @@ sv_status run_fmm_forest(sv_ctx *c, Fmm &F, const ForestArgs &fa) {
             SV_LAUNCHED(c);
         }
     }
+    SV_CK(c, cudaStreamWaitEvent(c->stream, F.ev_join, 0));
     {
         const Level &V = T.lv[L];
         const int g = forest_grid(f.cap[L], kWarps);
         l2p_kernel<P><<<g, kWarps * 32, 0, c->stream>>>(f.cap[L], nbd + L, V.pid, V.start, V.coord, S.x, S.y, S.z,
                                                         S.qm, fa.roots, L, F.nrm, F.fL[L], S.ax, S.ay, S.az,
-                                                        F.ftgt[L], 0);
-        SV_LAUNCHED(c);
-        box_relative_kernel<<<g, kWarps * 32, 0, c->stream>>>(f.cap[L], nbd + L, V.pid, V.start, V.coord, S.x, S.y,
-                                                              S.z, S.q, fa.roots, L, F.frel);
-        SV_LAUNCHED(c);
-        launch_p2p(ws, (float)c->P.softening2, g, c->stream, f.cap[L], nbd + L, V.pid, V.start, V.coord, F.fnbr[L],
-                   S.qm, fa.roots, L, S.ax, S.ay, S.az, F.d_counts, F.ftgt[L], F.frel);
+                                                        F.ftgt[L], 1);
         SV_LAUNCHED(c);
     }
     SV_CK(c, cudaMemcpyAsync(F.h_counts, F.d_counts, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
