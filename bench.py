@@ -42,6 +42,9 @@ sys.path.insert(0, os.path.join(ROOT, "solveit-code_gb300"))
 import plume  # noqa: E402
 
 METRIC = "particle-steps/s, mixed-prec vs plain FP64 path, same GB300, force err <=1e-5"
+# DRAM bytes (read + write) of one near-field launch of the fmm_n1m workload at
+# leaf level 11, from one ncu capture (profiles/p2p_kernel_fmm_n1m.md)
+P2P_TRAFFIC_BYTES = 53962240 + 430336
 EPS2 = 1e-20
 DT = 1e-13
 EZ = 1e8
@@ -601,13 +604,18 @@ def run_ours(args, wl, rank, world, local):
             m2l_flop = stats.flops_algorithmic - near_flop - n * 8.0 * (wl["order"] * (wl["order"] + 1) / 2) * 4
             line["roofline"] = {"kernel": "p2p_kernel (near field, 20 flop/pair)", "bound": "fp32",
                                 "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                                "frac": achieved / fp32_peak, "traffic": None,
+                                "frac": achieved / fp32_peak, "traffic": P2P_TRAFFIC_BYTES,
+                                "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one p2p_kernel "
+                                                  "launch at leaf level 11 (the 15th force evaluation of this "
+                                                  "workload), one ncu capture, profiles/p2p_kernel_fmm_n1m.md",
                                 "peak_source": "FP32 FMA rate 152 SMs x 128 lanes x 2 flop x sm_max_mhz of "
                                                "MEASURED_PEAKS.json (no FP32 peak is measured there; the "
                                                "kernel runs on the FP32 pipe, not the tensor cores)",
+                                "timing": "CUDA events on the near field's own stream; the kernel shares the "
+                                          "GPU with the concurrent upward / downward passes",
                                 "pairs_per_step": stats.pair_interactions,
                                 "m2l_per_step": stats.cell_interactions,
-                                "m2l_tflops": m2l_flop / (phase_ms[4] * 1e-3) / 1e12 if phase_ms[4] > 0 else None}
+                                "m2l_flop_per_step": m2l_flop}
         else:
             dom_ms = phase_ms[6]
             achieved = stats.flops_algorithmic / (dom_ms * 1e-3) / 1e12

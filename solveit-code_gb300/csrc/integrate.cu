@@ -116,6 +116,9 @@ __device__ void record_event(const DriftArgs &a, long long seq, int phase, int64
     a.ev_key[slot] = ((unsigned long long)seq << 34) | ((unsigned long long)phase << 32) | (unsigned long long)(uint32_t)i;
 }
 
+// FULL = false: no crash test, folding or boundary conditions (the common
+// case), compiled without their code so the streaming loop keeps few registers
+template <bool FULL>
 __global__ void drift_kernel(DriftArgs a) {
     double t_start = a.t_start;
     long long seq = a.seq_base;
@@ -124,17 +127,33 @@ __global__ void drift_kernel(DriftArgs a) {
         seq += (long long)a.tb[3] + 2 * (long long)a.tb[2];
     }
     const double h = a.h, T = t_start + h;
+    // the arrays are distinct: restrict-qualified copies let the loads and
+    // stores of one particle be scheduled freely
+    double *__restrict__ px = a.x, *__restrict__ py = a.y, *__restrict__ pz = a.z;
+    double *__restrict__ pvx = a.vx, *__restrict__ pvy = a.vy;
+    const double *__restrict__ pvz = a.vz, *__restrict__ tinj = a.t_inj;
+    int32_t *__restrict__ pst = a.st, *__restrict__ win = a.window;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < a.n;
          i += (int64_t)gridDim.x * blockDim.x) {
-        const double ti = a.t_inj[i];
+        const double ti = tinj[i];
         if (!(ti <= T)) {  // not injected by the end of this half step: outside the window
-            if (a.window) a.window[i] = 0;
+            if (win) win[i] = 0;
             continue;
         }
-        int32_t w = a.st[i];
+        int32_t w = pst[i];
+        if (!FULL) {
+            if (w == 1 || w == 2) {
+                const double s = fmin(fmax(T - ti, 0.0), h);
+                px[i] += pvx[i] * s;
+                py[i] += pvy[i] * s;
+                pz[i] += pvz[i] * s;
+            }
+            if (win) win[i] = w;
+            continue;
+        }
         const int32_t w0 = w;
-        double x = a.x[i], y = a.y[i], z = a.z[i];
-        double vx = a.vx[i], vy = a.vy[i], vz = a.vz[i];
+        double x = px[i], y = py[i], z = pz[i];
+        double vx = pvx[i], vy = pvy[i], vz = pvz[i];
         const double x0 = x, y0 = y, z0 = z, vx0 = vx, vy0 = vy;
         if (w == 1 || w == 2) {
             const double s = fmin(fmax(T - ti, 0.0), h);
@@ -142,7 +161,8 @@ __global__ void drift_kernel(DriftArgs a) {
             y += vy * s;
             z += vz * s;
             double zc;
-            if (a.crash == SV_CRASH_EXTRACTOR_GRID && extractor_crash(x0, y0, z0, x, y, z, a.cz, a.cw, a.cr, &zc)) {
+            if (FULL && a.crash == SV_CRASH_EXTRACTOR_GRID &&
+                extractor_crash(x0, y0, z0, x, y, z, a.cz, a.cw, a.cr, &zc)) {
                 w = -1;
                 z = zc;
                 const double td = (zc - z0) / vz;
@@ -151,7 +171,7 @@ __global__ void drift_kernel(DriftArgs a) {
                 record_event(a, seq, 0, i, t_start + td, x, y, z, vx, vy, vz, w);
             }
         }
-        const int fold = a.fold == 3 ? a.pfold[i] : a.fold;
+        const int fold = !FULL ? 0 : a.fold == 3 ? a.pfold[i] : a.fold;
         if (fold == 1) {
             // ParticleSystem::rotateToFirstQuadrant (particles.cpp:225-264)
             if (x < 0 && y < 0) {
@@ -168,7 +188,7 @@ __global__ void drift_kernel(DriftArgs a) {
             if (a.ay) y = wrap_axis(y, a.Ly);
             if (a.az) z = wrap_axis(z, a.Lz);
         }
-        if (w == 1 && (a.bc == SV_BC_SPACE || a.bc == SV_BC_SPACE_AND_TIME)) {
+        if (FULL && w == 1 && (a.bc == SV_BC_SPACE || a.bc == SV_BC_SPACE_AND_TIME)) {
             // checkOutOfSpatialBounds (particles.cpp:117-139)
             const bool out = (a.bsx != 0 && fabs(x) > a.bsx) || (a.bsy != 0 && fabs(y) > a.bsy) ||
                              (a.bsz != 0 && fabs(z) > a.bsz) || (a.bsr != 0 && sqrt(x * x + y * y) > a.bsr);
@@ -177,7 +197,7 @@ __global__ void drift_kernel(DriftArgs a) {
                 record_event(a, seq, 1, i, T, x, y, z, vx, vy, vz, w);
             }
         }
-        if (w == 1 && (a.bc == SV_BC_TIME || a.bc == SV_BC_SPACE_AND_TIME)) {
+        if (FULL && w == 1 && (a.bc == SV_BC_TIME || a.bc == SV_BC_SPACE_AND_TIME)) {
             // checkOutOfTemporalBounds (particles.cpp:163-168)
             if (T - ti > a.bt) {
                 w = 0;
@@ -185,21 +205,22 @@ __global__ void drift_kernel(DriftArgs a) {
             }
         }
         if (x != x0 || y != y0 || z != z0) {
-            a.x[i] = x;
-            a.y[i] = y;
-            a.z[i] = z;
+            px[i] = x;
+            py[i] = y;
+            pz[i] = z;
         }
         if (vx != vx0 || vy != vy0) {
-            a.vx[i] = vx;
-            a.vy[i] = vy;
+            pvx[i] = vx;
+            pvy[i] = vy;
         }
-        if (w != w0) a.st[i] = w;
-        if (a.window) a.window[i] = w;
+        if (w != w0) pst[i] = w;
+        if (win) win[i] = w;
     }
 }
 
-// With an emitter field map (M.nt > 0) the field at the particle is added to
-// the uniform one: computeBackgroundAcceleration (particles.cpp:496-520).
+// With an emitter field map (FIELD: M.nt > 0) the field at the particle is
+// added to the uniform one: computeBackgroundAcceleration (particles.cpp:496-520).
+template <bool FIELD>
 __global__ void kick_kernel(double *__restrict__ vx, double *__restrict__ vy, double *__restrict__ vz,
                             const double *__restrict__ ax, const double *__restrict__ ay,
                             const double *__restrict__ az, const double *__restrict__ qom,
@@ -216,7 +237,7 @@ __global__ void kick_kernel(double *__restrict__ vx, double *__restrict__ vy, do
         const double f = eoa * qom[i];
         const double s = fmin(fmax(t_start + dt - t_inj[i], 0.0), dt);
         double fx = ex, fy = ey, fz = ez;
-        if (M.nt > 0) {
+        if (FIELD) {
             int t = M.cache[i];
             double gx, gy, gz;
             field_at(M, x[i], y[i], z[i], &t, &gx, &gy, &gz);
@@ -225,12 +246,11 @@ __global__ void kick_kernel(double *__restrict__ vx, double *__restrict__ vy, do
             fy += gy;
             fz += gz;
         }
-        // the fields of the snapshot records: E1 = a / ((e/amu) q/m)
-        // (Integrator::updateAcceleration, integration_schemes.cpp:350-356), E2
-        const double inv = f != 0.0 ? 1.0 / f : 0.0;
-        e1[3 * i] = (float)(ax[i] * inv);
-        e1[3 * i + 1] = (float)(ay[i] * inv);
-        e1[3 * i + 2] = (float)(az[i] * inv);
+        // the snapshot records' fields: the force's acceleration (turned into
+        // E1 = (amu/e)(m/q) a when a snapshot is packed) and E2
+        e1[3 * i] = (float)ax[i];
+        e1[3 * i + 1] = (float)ay[i];
+        e1[3 * i + 2] = (float)az[i];
         e2[3 * i] = (float)fx;  // Efield2 of the snapshot records (particles.cpp:512)
         e2[3 * i + 1] = (float)fy;
         e2[3 * i + 2] = (float)fz;
@@ -364,16 +384,20 @@ sv_status drift(sv_ctx *c, double t_start, double h, int32_t *window, const doub
     a.ev_key = c->d_ev_key;
     a.ev_count = c->d_ev_count;
     a.ev_cap = c->ev_cap;
-    drift_kernel<<<stream_grid(c->n), 256, 0, c->stream>>>(a);
+    if (a.crash != SV_CRASH_NONE || a.bc != SV_BC_NONE || a.fold != 0)
+        drift_kernel<true><<<stream_grid(c->n), 256, 0, c->stream>>>(a);
+    else
+        drift_kernel<false><<<stream_grid(c->n), 256, 0, c->stream>>>(a);
     SV_LAUNCHED(c);
     if (!tb) c->ev_seq++;
     return SV_OK;
 }
 
 sv_status kick(sv_ctx *c, double t_start, double dt, const int32_t *st, const double *tb) {
-    kick_kernel<<<stream_grid(c->n), 256, 0, c->stream>>>(
-        c->vx, c->vy, c->vz, c->ax, c->ay, c->az, c->qom, st, c->t_inj, c->n, t_start, dt,
-        c->P.e_over_amu, c->P.efield[0], c->P.efield[1], c->P.efield[2], tb, c->x, c->y, c->z, c->field, c->e2, c->e1);
+    auto k = c->field.nt > 0 ? kick_kernel<true> : kick_kernel<false>;
+    k<<<stream_grid(c->n), 256, 0, c->stream>>>(c->vx, c->vy, c->vz, c->ax, c->ay, c->az, c->qom, st, c->t_inj,
+                                                c->n, t_start, dt, c->P.e_over_amu, c->P.efield[0], c->P.efield[1],
+                                                c->P.efield[2], tb, c->x, c->y, c->z, c->field, c->e2, c->e1);
     SV_LAUNCHED(c);
     return SV_OK;
 }

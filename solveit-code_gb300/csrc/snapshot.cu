@@ -30,14 +30,17 @@ __global__ void active_flags(const int32_t *__restrict__ st, int64_t n, int64_t 
 __global__ void pack_records(const int *__restrict__ flag, const int *__restrict__ pos, int64_t n,
                              const double *__restrict__ x, const double *__restrict__ y, const double *__restrict__ z,
                              const double *__restrict__ vx, const double *__restrict__ vy,
-                             const double *__restrict__ vz, const int32_t *__restrict__ species,
-                             const float *__restrict__ e1, const float *__restrict__ e2, int fmt,
+                             const double *__restrict__ vz, const double *__restrict__ q,
+                             const double *__restrict__ m, double amu_over_e, const int32_t *__restrict__ species,
+                             const float *__restrict__ a1, const float *__restrict__ e2, int fmt,
                              int32_t last_particle, unsigned char *__restrict__ out) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n || !flag[i]) return;
+    // E1 = (amu/e) (m/q) a (Integrator::updateAcceleration, integration_schemes.cpp:350-356)
+    const double k = q[i] != 0.0 ? amu_over_e * m[i] / q[i] : 0.0;
     const float f[12] = {(float)x[i],    (float)y[i],    (float)z[i],    (float)vx[i],
-                         (float)vy[i],   (float)vz[i],   e1[3 * i],      e1[3 * i + 1],
-                         e1[3 * i + 2],  e2[3 * i],      e2[3 * i + 1],  e2[3 * i + 2]};
+                         (float)vy[i],   (float)vz[i],   (float)(k * a1[3 * i]),      (float)(k * a1[3 * i + 1]),
+                         (float)(k * a1[3 * i + 2]),  e2[3 * i],      e2[3 * i + 1],  e2[3 * i + 2]};
     const uint32_t sp = species[i] < 0 ? 0xffffffffu : (uint32_t)species[i];
     const int32_t idx = (int32_t)i;
     if (fmt == SV_SNAPSHOT_ORIGINAL) {
@@ -100,8 +103,8 @@ extern "C" sv_status sv_snapshot(sv_ctx *c, int32_t format, int64_t first, int64
             e = cudaMalloc(&d_out, total);
             if (e == cudaSuccess) {
                 pack_records<<<div_up(n, 256), 256, 0, c->stream>>>(
-                    flag, pos, n, c->x, c->y, c->z, c->vx, c->vy, c->vz, c->species, c->e1, c->e2, format,
-                    last_particle, d_out);
+                    flag, pos, n, c->x, c->y, c->z, c->vx, c->vy, c->vz, c->q, c->m, 1.0 / c->P.e_over_amu,
+                    c->species, c->e1, c->e2, format, last_particle, d_out);
                 c->launches++;
                 e = cudaGetLastError();
             }

@@ -133,12 +133,10 @@ __global__ void substep_kick_kernel(double *__restrict__ vx, double *__restrict_
             fy += gy;
             fz += gz;
         }
-        // the fields of the snapshot records: E1 = a / ((e/amu) q/m)
-        // (Integrator::updateAcceleration, integration_schemes.cpp:350-356), E2
-        const double inv = f != 0.0 ? 1.0 / f : 0.0;
-        e1[3 * i] = (float)(ax[i] * inv);
-        e1[3 * i + 1] = (float)(ay[i] * inv);
-        e1[3 * i + 2] = (float)(az[i] * inv);
+        // the snapshot records' fields (E1 formed from the acceleration when packed)
+        e1[3 * i] = (float)ax[i];
+        e1[3 * i + 1] = (float)ay[i];
+        e1[3 * i + 2] = (float)az[i];
         e2[3 * i] = (float)fx;
         e2[3 * i + 1] = (float)fy;
         e2[3 * i + 2] = (float)fz;

@@ -88,7 +88,7 @@ struct sv_ctx {
     int32_t *status = nullptr;
     int32_t *species = nullptr;  // species code per particle (event records), 0xffffffff unknown
     float *e2 = nullptr;         // 3n: background field (V/m) at each inbound particle's last kick (Efield2)
-    float *e1 = nullptr;         // 3n: particle-particle field (V/m) of each inbound particle's last kick (Efield1)
+    float *e1 = nullptr;         // 3n: force acceleration (m/s^2) of each inbound particle's last kick (Efield1 / ((e/amu) q/m))
     // status the force and the kick see: the injection-windowed copy during a
     // leapfrog step (written by the first drift), else null (use status)
     int32_t *wstatus = nullptr;
