@@ -149,10 +149,11 @@ SV_API sv_status sv_download_ref32(sv_ctx *ctx, float *pos4, float *vel4);
 /* One force evaluation with the context's method: the body of
  * updateAcceleration() (direct_force_method.cpp:347-428,
  * barnes_hut_force_calculation.cpp:574-715,
- * multipole_method_force_calculation.cpp:148-522).  Targets are inbound
- * particles with index in [first, last); sources are all particles with
- * status 1 or 2.  The result (m/s^2, FP64) stays on the device; a3_out, if
- * not null, receives a copy (3n interleaved, zero for non-targets). */
+ * multipole_method_force_calculation.cpp:148-522).  As there, only particles
+ * with index in [first, last) take part: targets are the inbound ones, sources
+ * those with status 1 or 2 (direct_force_method.cpp:374-377).  The result
+ * (m/s^2, FP64) stays on the device; a3_out, if not null, receives a copy (3n
+ * interleaved, zero for non-targets). */
 SV_API sv_status sv_compute_accel(sv_ctx *ctx, int64_t first, int64_t last, double *a3_out);
 /* acceleration[i].xyz += a_i for inbound i, i.e. the += contract of
  * ForceCalculationMethod::updateAcceleration on the reference's vec4 array. */

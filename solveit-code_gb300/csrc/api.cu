@@ -128,11 +128,11 @@ void free_state(sv_ctx *c) {
     cudaFree(c->x); cudaFree(c->y); cudaFree(c->z);
     cudaFree(c->vx); cudaFree(c->vy); cudaFree(c->vz);
     cudaFree(c->q); cudaFree(c->m); cudaFree(c->t_inj); cudaFree(c->status); cudaFree(c->qom);
-    cudaFree(c->species); cudaFree(c->wstatus); cudaFree(c->e2); cudaFree(c->e1);
+    cudaFree(c->species); cudaFree(c->wstatus); cudaFree(c->e2); cudaFree(c->e1); cudaFree(c->rstatus);
     cudaFree(c->ax); cudaFree(c->ay); cudaFree(c->az);
     c->x = c->y = c->z = c->vx = c->vy = c->vz = c->q = c->m = c->t_inj = c->qom = nullptr;
     c->ax = c->ay = c->az = nullptr;
-    c->status = c->species = c->wstatus = nullptr;
+    c->status = c->species = c->wstatus = c->rstatus = nullptr;
     c->e2 = c->e1 = nullptr;
     c->cap = 0;
 }
@@ -147,6 +147,7 @@ sv_status ensure_capacity(sv_ctx *c, int64_t n) {
     SV_TRY(dev_alloc(c, &c->qom, cap));
     SV_TRY(dev_alloc(c, &c->status, cap));
     SV_TRY(dev_alloc(c, &c->species, cap)); SV_TRY(dev_alloc(c, &c->wstatus, cap));
+    SV_TRY(dev_alloc(c, &c->rstatus, cap));
     SV_TRY(dev_alloc(c, &c->e2, 3 * cap)); SV_TRY(dev_alloc(c, &c->e1, 3 * cap));
     SV_TRY(dev_alloc(c, &c->ax, cap)); SV_TRY(dev_alloc(c, &c->ay, cap)); SV_TRY(dev_alloc(c, &c->az, cap));
     c->cap = cap;
@@ -233,6 +234,14 @@ __global__ void pack_accel(const double *__restrict__ ax, const double *__restri
     a3[3 * i] = t ? ax[i] : 0.0;
     a3[3 * i + 1] = t ? ay[i] : 0.0;
     a3[3 * i + 2] = t ? az[i] : 0.0;
+}
+
+// the status of an evaluation over [first, last): particles outside the range
+// take no part, as sources or as targets
+__global__ void range_status(const int32_t *__restrict__ st, int64_t first, int64_t last, int64_t n,
+                             int32_t *__restrict__ out) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (i >= first && i < last) ? st[i] : 0;
 }
 
 __global__ void zero_nontargets(double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az,
@@ -584,6 +593,15 @@ sv_status sv::compute_accel_device(sv_ctx *c, int64_t first, int64_t last) {
                           (c->P.fmm_type == SV_FMM_FMM_OUTLIERS || c->P.fmm_type == SV_FMM_TREECODE_OUTLIERS);
     if (outliers && c->P.symmetry != SV_SYM_NONE)
         return set_error(c, SV_ERR_UNSUPPORTED, "the outlier variants run without symmetry images");
+    // a partial range: the reference's methods take their sources from
+    // [firstParticle, lastParticle) as well as their targets
+    const int32_t *saved_fstatus = c->fstatus;
+    if (n > 0 && (first > 0 || last < n)) {
+        range_status<<<grid_of(n), 256, 0, c->stream>>>(force_status(c), first, last, n, c->rstatus);
+        SV_LAUNCHED(c);
+        c->fstatus = c->rstatus;
+    }
+    const sv_status st_run = [&]() -> sv_status {
     if (n > 0) {
         phase_mark(c, 0);
         if (outliers) {
@@ -611,6 +629,10 @@ sv_status sv::compute_accel_device(sv_ctx *c, int64_t first, int64_t last) {
         if (outliers) SV_TRY(outliers_add(c, first, last));
         phase_mark(c, 8);
     }
+    return SV_OK;
+    }();
+    c->fstatus = saved_fstatus;
+    SV_TRY(st_run);
     SV_CK(c, cudaEventRecord(c->ev_end, c->stream));
     c->have_accel = true;
     return SV_OK;

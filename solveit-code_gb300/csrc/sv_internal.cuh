@@ -93,6 +93,7 @@ struct sv_ctx {
     // leapfrog step (written by the first drift), else null (use status)
     int32_t *wstatus = nullptr;
     const int32_t *fstatus = nullptr;
+    int32_t *rstatus = nullptr;  // status of an evaluation over a partial [first, last) range
     // crash / boundary / folding applied after every drift, and the event log
     sv_boundary B{};
     sv_event *d_events = nullptr;

@@ -86,8 +86,13 @@ def test_status_and_target_range():
         assert np.all(a[10:40] == 0.0)
         assert rel_l2(a, ref, st["status"]) < 1e-12
         a2 = fm.accel(first=100, last=200)
+    # the reference's [firstParticle, lastParticle) bounds the sources too
+    # (direct_force_method.cpp:374-377)
+    win = dict(st, status=np.where((np.arange(600) >= 100) & (np.arange(600) < 200), st["status"], 0).astype(np.int32))
+    ref_w = O.direct_f64(win, EPS20)
     assert np.all(a2[:100] == 0.0) and np.all(a2[200:] == 0.0)
-    np.testing.assert_allclose(a2[100:200], ref[100:200], rtol=1e-11, atol=0)
+    np.testing.assert_allclose(a2[100:200], ref_w[100:200], rtol=1e-11, atol=0)
+    assert np.max(np.abs(ref_w[100:200] - ref[100:200])) > 1e-3 * np.max(np.abs(ref[100:200]))
 
 
 def test_empty_plume():
