@@ -54,7 +54,7 @@ struct Fmm {
     float *otab = nullptr;   // rotation-based M2M / L2L tables (oct_layout)
     void *arena = nullptr;
     size_t arena_bytes = 0;
-    unsigned long long *d_counts = nullptr;  // [0] M2L translations, [1] P2P pairs
+    unsigned long long *d_counts = nullptr;  // [0] M2L translations, [1] P2P pairs, [2] charges differ
     unsigned long long *h_counts = nullptr;
     // caller particles followed by their source-only symmetry images
     double *ex = nullptr, *ey = nullptr, *ez = nullptr, *eq = nullptr, *em = nullptr, *eoff = nullptr;
@@ -919,19 +919,28 @@ __global__ void __launch_bounds__(kWarps * 32) m2p_kernel(TreecodeArgs a) {
 // Each particle once as an FP32 offset from the centre of its own leaf box
 // (one FP64 subtraction per particle) with its charge: the P2P kernel then
 // forms source offsets from the target box centre as offset + k*h in FP32.
+// A charge other than qs[0] sets *mixed (zeroed beforehand), which keeps the
+// P2P kernel on its per-source charge path.
 __global__ void __launch_bounds__(kWarps * 32)
 box_relative_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid,
                     const int *__restrict__ start, const int4 *__restrict__ coord, const double *__restrict__ xs,
                     const double *__restrict__ ys, const double *__restrict__ zs, const float *__restrict__ qs,
-                    const double *__restrict__ roots, int level, float4 *__restrict__ rel) {
+                    const double *__restrict__ roots, int level, float4 *__restrict__ rel,
+                    unsigned long long *__restrict__ mixed) {
+    const float q0 = qs[0];
+    bool diff = false;
     SV_WARP_BOXES(kWarps) {
     const double *root = box_root(roots, bpid, b);
     const double h = root[3] / (double)(1 << level);
     const int4 cb = coord[b];
     const double cx = root[0] + (cb.x + 0.5) * h, cy = root[1] + (cb.y + 0.5) * h, cz = root[2] + (cb.z + 0.5) * h;
-    for (int j = start[b] + lane; j < start[b + 1]; j += 32)
-        rel[j] = make_float4((float)(xs[j] - cx), (float)(ys[j] - cy), (float)(zs[j] - cz), qs[j]);
+    for (int j = start[b] + lane; j < start[b + 1]; j += 32) {
+        const float q = qs[j];
+        diff |= q != q0;
+        rel[j] = make_float4((float)(xs[j] - cx), (float)(ys[j] - cy), (float)(zs[j] - cz), q);
     }
+    }
+    if (__any_sync(0xffffffffu, diff) && (threadIdx.x & 31) == 0) *mixed = 1ull;
 }
 
 // s += v with Kahan compensation e (the running sum is s - e)
@@ -949,19 +958,24 @@ __device__ __forceinline__ void kahan_add(float &s, float &e, float v) {
 // needed only when eps^2 < kMinR2 (a zero-distance pair without softening).  Targets: one per lane; a
 // chunk of nt < 32 targets gives each target a group of g lanes (a power of
 // two, nt * g <= 32) that split the staged sources.  Each 32-source chunk's
-// FP32 partial sum is added with Kahan compensation.
-template <int WS, bool CLAMP>
-__global__ void __launch_bounds__(kWarps * 32, 8)
-p2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, const int *__restrict__ start,
-           const int4 *__restrict__ coord, const int *__restrict__ nbr, const double *__restrict__ qm,
-           const double *__restrict__ roots, int level, float eps2, double *__restrict__ ax, double *__restrict__ ay,
-           double *__restrict__ az, unsigned long long *__restrict__ counts, const int *__restrict__ has_tgt,
-           const float4 *__restrict__ rel) {
+// FP32 partial sum is added with Kahan compensation.  UQ: every particle of
+// the tree carries the same charge Q (box_relative_kernel found no other), so
+// the pair weight is r^-3 alone, the sums are scaled by the target's own
+// charge (= Q) at the end, and padding sources sit far away (r^-3 underflows
+// to zero) instead of carrying zero charge.
+template <int WS>
+constexpr int p2p_nsp() { return ((2 * WS + 1) * (2 * WS + 1) * (2 * WS + 1) + 31) / 32 * 32; }
+
+template <int WS, bool CLAMP, bool UQ>
+__device__ __forceinline__ void
+p2p_body(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, const int *__restrict__ start,
+         const int4 *__restrict__ coord, const int *__restrict__ nbr, const double *__restrict__ qm,
+         const double *__restrict__ roots, int level, float eps2, double *__restrict__ ax, double *__restrict__ ay,
+         double *__restrict__ az, unsigned long long *__restrict__ counts, const int *__restrict__ has_tgt,
+         const float4 *__restrict__ rel, float4 (*src)[32], int2 (*nb_rng)[p2p_nsp<WS>()],
+         float4 (*nb_off)[p2p_nsp<WS>()]) {
     constexpr int NS1 = 2 * WS + 1, NS = NS1 * NS1 * NS1;
-    constexpr int NSP = (NS + 31) / 32 * 32;
-    __shared__ float4 src[kWarps][32];
-    __shared__ int2 nb_rng[kWarps][NSP];    // (first source, running source count at the box's end)
-    __shared__ float4 nb_off[kWarps][NSP];  // source box centre - target box centre (exact in FP32)
+    const float4 pad = UQ ? make_float4(1e18f, 0.f, 0.f, 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
     unsigned long long pairs = 0;
     const unsigned lt_mask = (1u << (threadIdx.x & 31)) - 1u;
     SV_WARP_BOXES(kWarps) {
@@ -1012,7 +1026,7 @@ p2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, 
         int kb = 0, kbeg = 0;
         for (int c0 = 0; c0 < total; c0 += 32) {
             const int j = c0 + lane;
-            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            float4 v = pad;
             if (j < total) {
                 int2 rg = nb_rng[wid][kb];
                 while (rg.y <= j) {
@@ -1034,7 +1048,7 @@ p2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, 
                     float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
                     if (CLAMP) r2 = fmaxf(r2, kMinR2);
                     const float inv = rsqrtf(r2);
-                    const float w = u.w * inv * inv * inv;
+                    const float w = UQ ? inv * inv * inv : u.w * inv * inv * inv;
                     fax = fmaf(dx, w, fax);
                     fay = fmaf(dy, w, fay);
                     faz = fmaf(dz, w, faz);
@@ -1044,7 +1058,7 @@ p2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, 
                     float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
                     if (CLAMP) r2 = fmaxf(r2, kMinR2);
                     const float inv = rsqrtf(r2);
-                    const float w = u.w * inv * inv * inv;
+                    const float w = UQ ? inv * inv * inv : u.w * inv * inv * inv;
                     fbx = fmaf(dx, w, fbx);
                     fby = fmaf(dy, w, fby);
                     fbz = fmaf(dz, w, fbz);
@@ -1059,13 +1073,13 @@ p2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, 
             kahan_add(sbz, ebz, fbz);
         }
         {
-            const double c = qm[ia];
+            const double c = UQ ? qm[ia] * (double)ta.w : qm[ia];
             ax[ia] += (double)(sax - eax) * c;
             ay[ia] += (double)(say - eay) * c;
             az[ia] += (double)(saz - eaz) * c;
         }
         if (vb) {
-            const double c = qm[ib];
+            const double c = UQ ? qm[ib] * (double)tbv.w : qm[ib];
             ax[ib] += (double)(sbx - ebx) * c;
             ay[ib] += (double)(sby - eby) * c;
             az[ib] += (double)(sbz - ebz) * c;
@@ -1086,7 +1100,7 @@ p2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, 
         int kb = 0, kbeg = 0;  // this lane's current source box and its first running index
         for (int c0 = 0; c0 < total; c0 += 32) {
             const int j = c0 + lane;
-            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            float4 v = pad;
             if (j < total) {
                 int2 rg = nb_rng[wid][kb];
                 while (rg.y <= j) {
@@ -1101,7 +1115,7 @@ p2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, 
             __syncwarp();
             float fx = 0.f, fy = 0.f, fz = 0.f;
             if (g == 1) {
-                // every lane a target, all 32 staged sources (zero-charge padding)
+                // every lane a target, all 32 staged sources (padding adds nothing)
 #pragma unroll 8
                 for (int k = 0; k < 32; k++) {
                     const float4 u = src[wid][k];
@@ -1109,7 +1123,7 @@ p2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, 
                     float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
                     if (CLAMP) r2 = fmaxf(r2, kMinR2);
                     const float inv = rsqrtf(r2);
-                    const float w = u.w * inv * inv * inv;
+                    const float w = UQ ? inv * inv * inv : u.w * inv * inv * inv;
                     fx = fmaf(dx, w, fx);
                     fy = fmaf(dy, w, fy);
                     fz = fmaf(dz, w, fz);
@@ -1122,7 +1136,7 @@ p2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, 
                     float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
                     if (CLAMP) r2 = fmaxf(r2, kMinR2);
                     const float inv = rsqrtf(r2);
-                    const float w = u.w * inv * inv * inv;
+                    const float w = UQ ? inv * inv * inv : u.w * inv * inv * inv;
                     fx = fmaf(dx, w, fx);
                     fy = fmaf(dy, w, fy);
                     fz = fmaf(dz, w, fz);
@@ -1151,7 +1165,7 @@ p2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, 
             sz += __shfl_xor_sync(0xffffffffu, sz, o);
         }
         if (valid && sub == 0) {
-            const double c = qm[i];
+            const double c = UQ ? qm[i] * (double)ti.w : qm[i];
             ax[i] += (double)sx * c;
             ay[i] += (double)sy * c;
             az[i] += (double)sz * c;
@@ -1160,6 +1174,25 @@ p2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, 
     __syncwarp();
     }
     if ((threadIdx.x & 31) == 0 && pairs) atomicAdd(&counts[1], pairs);
+}
+
+// counts[2] != 0: box_relative_kernel met two different charges
+template <int WS, bool CLAMP>
+__global__ void __launch_bounds__(kWarps * 32, 8)
+p2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, const int *__restrict__ start,
+           const int4 *__restrict__ coord, const int *__restrict__ nbr, const double *__restrict__ qm,
+           const double *__restrict__ roots, int level, float eps2, double *__restrict__ ax, double *__restrict__ ay,
+           double *__restrict__ az, unsigned long long *__restrict__ counts, const int *__restrict__ has_tgt,
+           const float4 *__restrict__ rel) {
+    __shared__ float4 src[kWarps][32];
+    __shared__ int2 nb_rng[kWarps][p2p_nsp<WS>()];    // (first source, running source count at the box's end)
+    __shared__ float4 nb_off[kWarps][p2p_nsp<WS>()];  // source box centre - target box centre (exact in FP32)
+    if (counts[2] == 0)
+        p2p_body<WS, CLAMP, true>(nbox, nbd, bpid, start, coord, nbr, qm, roots, level, eps2, ax, ay, az, counts,
+                                  has_tgt, rel, src, nb_rng, nb_off);
+    else
+        p2p_body<WS, CLAMP, false>(nbox, nbd, bpid, start, coord, nbr, qm, roots, level, eps2, ax, ay, az, counts,
+                                   has_tgt, rel, src, nb_rng, nb_off);
 }
 
 // P2P launch: well-separation and whether r^2 needs the kMinR2 floor
@@ -1226,7 +1259,7 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         part[l] = chunks[l] > 1 ? (float2 *)carve(nb * chunks[l] * NC * sizeof(float2)) : Lv[l];
     }
     phase_mark(c, 2);
-    SV_CK(c, cudaMemsetAsync(F.d_counts, 0, 2 * sizeof(unsigned long long), c->stream));
+    SV_CK(c, cudaMemsetAsync(F.d_counts, 0, 3 * sizeof(unsigned long long), c->stream));
     // which boxes hold targets (all of them unless symmetry images are present)
     int *tgt[kMortonBits + 1];
     {
@@ -1286,7 +1319,7 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         SV_CK(c, cudaMemsetAsync(S.ay, 0, sizeof(double) * c->S.n, F.side));
         SV_CK(c, cudaMemsetAsync(S.az, 0, sizeof(double) * c->S.n, F.side));
         box_relative_kernel<<<div_up(V.nbox, kWarps), kWarps * 32, 0, F.side>>>(
-            V.nbox, nullptr, nullptr, V.start, V.coord, S.x, S.y, S.z, S.q, S.root, L, F.rel);
+            V.nbox, nullptr, nullptr, V.start, V.coord, S.x, S.y, S.z, S.q, S.root, L, F.rel, F.d_counts + 2);
         SV_LAUNCHED(c);
         if (c->P.profile_phases) SV_CK(c, cudaEventRecord(F.ev_near[0], F.side));
         launch_p2p(ws, (float)c->P.softening2, div_up(V.nbox, kWarps), F.side, V.nbox, nullptr, nullptr, V.start,
@@ -1435,7 +1468,7 @@ sv_status run_fmm_forest(sv_ctx *c, Fmm &F, const ForestArgs &fa) {
     Tree &T = *F.ftree;
     int *nbd = fa.d_nbox;
     SV_TRY(tree_build_forest(c, T, f, nbd, fa.d_err));
-    SV_CK(c, cudaMemsetAsync(F.d_counts, 0, 2 * sizeof(unsigned long long), c->stream));
+    SV_CK(c, cudaMemsetAsync(F.d_counts, 0, 3 * sizeof(unsigned long long), c->stream));
     // Two streams, as in run_fmm: target flags, lists and the near field on the
     // second (the forest's slots only: the direct plumes' slots belong to
     // another stream), the upward and downward passes on the main one.
@@ -1473,7 +1506,7 @@ sv_status run_fmm_forest(sv_ctx *c, Fmm &F, const ForestArgs &fa) {
         SV_CK(c, cudaMemsetAsync(S.ay, 0, sizeof(double) * f.n, sd));
         SV_CK(c, cudaMemsetAsync(S.az, 0, sizeof(double) * f.n, sd));
         box_relative_kernel<<<g, kWarps * 32, 0, sd>>>(f.cap[L], nbd + L, V.pid, V.start, V.coord, S.x, S.y, S.z,
-                                                       S.q, fa.roots, L, F.frel);
+                                                       S.q, fa.roots, L, F.frel, F.d_counts + 2);
         SV_LAUNCHED(c);
         launch_p2p(ws, (float)c->P.softening2, g, sd, f.cap[L], nbd + L, V.pid, V.start, V.coord, F.fnbr[L], S.qm,
                    fa.roots, L, S.ax, S.ay, S.az, F.d_counts, F.ftgt[L], F.frel);
@@ -1613,7 +1646,7 @@ static sv_status fmm_state(sv_ctx *c) {
     if (!c->fmm) {
         c->fmm = new Fmm();
         Fmm &F = *c->fmm;
-        SV_CK(c, cudaMalloc(&F.d_counts, 2 * sizeof(unsigned long long)));
+        SV_CK(c, cudaMalloc(&F.d_counts, 3 * sizeof(unsigned long long)));
         SV_CK(c, cudaMallocHost(&F.h_counts, 2 * sizeof(unsigned long long)));
         SV_CK(c, cudaStreamCreateWithFlags(&F.side, cudaStreamNonBlocking));
         SV_CK(c, cudaEventCreateWithFlags(&F.ev_fork, cudaEventDisableTiming));

@@ -120,3 +120,45 @@ def test_fmm_rotational_status_and_range():
     assert np.all(a[:80] == 0.0) and np.all(a[2000:] == 0.0)
     live = np.arange(80, 2000)
     assert rel_l2(a[live], ref[live], st["status"][live]) < 1e-5
+
+
+@pytest.mark.parametrize("charges", ["uniform2", "negative", "mixed", "one_differs"])
+def test_fmm_charge_patterns(charges):
+    """The near field has a uniform-charge path (every source of the tree
+    carries one charge) and a per-source-charge path; each against the FP64
+    direct sum, including the particles around a single odd charge."""
+    n = 20000
+    st = plume.make_plume(n, 1e-6, 81)
+    if charges == "uniform2":
+        st["q"][:] = 2.0
+    elif charges == "negative":
+        st["q"][:] = -1.0
+    elif charges == "mixed":
+        st["q"][:] = np.random.default_rng(5).choice([1.0, 2.0, 3.0], n)
+    else:
+        st["q"][n // 2] = 1.5
+    ref = O.direct_f64(st, EPS20)
+    a, _ = run_accel(st, softening2=EPS20, method=sv.FMM, fmm_order=8, fmm_ws=2)
+    mean, mx, _, _ = O.rel_l2(a, ref, st["status"])
+    assert mean < 1e-5 and mx < 1e-3, (mean, mx)
+    # the odd particle's nearest neighbours feel its charge most
+    d = np.linalg.norm(st["x"] - st["x"][n // 2], axis=1)
+    near = np.argsort(d)[:16]
+    assert O.rel_l2(a[near], ref[near], st["status"][near])[1] < 1e-4
+
+
+def test_fmm_forest_mixed_charges():
+    """One FMM plume of a batch with charge 2: the forest's near field takes
+    the per-source-charge path for every plume."""
+    states = [plume.make_plume(n, 1e-6, 8200 + i) for i, n in enumerate((6000, 9000, 12000))]
+    states[1]["q"][:] = 2.0
+    methods, syms = [sv.FMM] * 3, [sv.SYM_NONE] * 3
+    with sv.ForceMethod(softening2=EPS20, fmm_order=8, fmm_ws=2) as fm:
+        fm.upload_batch(states, methods, syms)
+        a = fm.accel()
+    o = 0
+    for s in states:
+        k = s["x"].shape[0]
+        ref = O.direct_f64(s, EPS20)
+        assert rel_l2(a[o:o + k], ref, s["status"]) < 1e-5
+        o += k
