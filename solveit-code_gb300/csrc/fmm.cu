@@ -1014,9 +1014,11 @@ p2p_body(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, co
     __syncwarp();
     const int t0 = start[b], t1 = start[b + 1];
     int tb = t0;
-    // two targets per lane while more than 32 remain: each staged source
-    // (one shared-memory load) then feeds two pairs
-    for (; t1 - tb > 32; tb += 64) {
+    // two targets per lane while more than 48 remain: each staged source
+    // (one shared-memory load) then feeds two pairs.  33-48 targets cost less
+    // as one full pass of 32 and a pass that splits the sources of the
+    // remaining 1-16 targets over 2-32 lanes each.
+    for (; t1 - tb > 48; tb += 64) {
         const int ia = tb + lane, ib = tb + 32 + lane;
         const bool vb = ib < t1;
         const float4 ta = rel[ia], tbv = rel[vb ? ib : ia];
