@@ -255,15 +255,52 @@ SV_API sv_status sv_get_events(sv_ctx *ctx, sv_event *out, int64_t cap, int64_t 
  * :336-367), and the background field (particles.cpp:512) at the particle's
  * last kick of sv_leapfrog as a target (zero before its first one), as the
  * reference's Efield1 / Efield2 arrays hold them.
+ * With SV_SNAPSHOT_FULL or-ed into the format, the records are those of
+ * Integrator::saveFullCurrentConditions (integration_schemes.cpp:197-258):
+ * every particle of [0, n) whatever its status and injection time (first is
+ * ignored; last is still written as lastParticle).
  * *bytes receives the size; out (cap_bytes) may be null to query it.  The
  * records go to the file as they are (fwrite). */
 typedef enum {
     SV_SNAPSHOT_ORIGINAL = 0,     /* SaveDataOptions::original */
-    SV_SNAPSHOT_NEW_ORIGINAL = 1  /* SaveDataOptions::newOriginal */
+    SV_SNAPSHOT_NEW_ORIGINAL = 1, /* SaveDataOptions::newOriginal */
+    SV_SNAPSHOT_FULL = 16         /* flag: saveFullCurrentConditions */
 } sv_snapshot_format;
 
 SV_API sv_status sv_snapshot(sv_ctx *ctx, int32_t format, int64_t first, int64_t last, float current_time,
                              void *out, int64_t cap_bytes, int64_t *bytes);
+
+/* Energy bookkeeping of the reference's integrator (Integrator::toggleEnergy,
+ * integration_schemes.cpp:85-97; initializeEnergyData :757-775;
+ * updateEnergyInjectionData :783-793; updateEnergyIntervalData :799-835).
+ * enable = 1 arms it; the next step of sv_leapfrog first takes, for every
+ * particle, its kinetic energy and the work of the emitter field along z from
+ * (0, 0, z_max r0) and then along (x, y) (init_steps samples per leg; zero
+ * without an emitter field).  Before each drift, the particles injected since
+ * the previous drift add their kinetic energy and field energy of the set-up
+ * and their potential energy at that moment to KE_inj, FE_inj, PE_inj.  After
+ * every `interval`-th step (counted as the reference does: the step that
+ * starts at t is number round(t / dt) + 1), each particle of the window
+ * updates its field energy along the path it moved since the previous update
+ * (max(min(dt interval, t - t_inj) steps / dt, 2) samples per leg), and one
+ * record is kept: KE_inj, PE_inj, FE_inj and the window's KE, PE (halved) and
+ * FE.  The window is the reference's [firstParticle, lastParticle): the
+ * injected particles from the first one with status 1 or 2 on, whatever their
+ * status; potential energies are q_i q_j e^2 / (4 pi eps0 sqrt(r^2 + eps^2))
+ * over it.  Sums are FP64 (the reference's are FP32), the potential's pairs
+ * FP32 on FP32 hi + lo offsets.  The potential energy costs a direct sum over
+ * the window per record (O(n^2)), as in the reference.  sv_upload re-arms the
+ * set-up and clears the records; enable = 0 releases everything.  Single-rate
+ * leapfrog of a single-plume context only (batch, substeps and the adjoint
+ * return SV_ERR_UNSUPPORTED). */
+typedef struct {
+    float ke_inj, pe_inj, fe_inj, ke, pe, fe;  /* J: the energy file's 24-byte record */
+} sv_energy_record;
+
+SV_API sv_status sv_set_energy(sv_ctx *ctx, int32_t enable, int32_t init_steps, int32_t steps, int32_t interval);
+/* Copies up to cap records (oldest first) to out and releases them; *count
+ * receives how many were kept.  out may be null to query the count. */
+SV_API sv_status sv_get_energy_records(sv_ctx *ctx, sv_energy_record *out, int64_t cap, int64_t *count);
 
 /* Multi-rate leapfrog (LeapfrogDKDSubsteps, integration_schemes.cpp:899-1528).
  * Each entry asks for steps of at most dt inside a region: spatial limits

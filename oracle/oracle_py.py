@@ -60,6 +60,8 @@ def lib():
         L.orc_leapfrog_substeps_ref32.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_int, C.c_float,
                                                   C.c_double, _f32p, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
                                                   C.c_void_p, C.c_int]
+        L.orc_leapfrog_ref32_energy.argtypes = [C.c_int, _f32p, _f32p, _f32p, _f32p, C.c_int, C.c_float,
+                                                C.c_double, _f32p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         L.orc_emitter_field_ref32.argtypes = [C.c_void_p, C.c_int, _f32p, _f32p, C.POINTER(C.c_int)]
         L.orc_emitter_field_f64.argtypes = [C.c_void_p, C.c_int64, _f64p, _f64p]
         L.orc_energy_f64.argtypes = [C.c_int64, _f64p, _f64p, _f64p, _f64p, C.c_double,
@@ -265,6 +267,30 @@ def leapfrog_f64_bc(state, nsteps, dt, eps2, efield=(0.0, 0.0, 0.0), t0=0.0, sym
                               None if bd is None else C.byref(bd), None if fld is None else C.byref(fld),
                               ev.ctypes.data, ev_cap, C.byref(cnt), threads)
     return x.reshape(n, 3), v.reshape(n, 3), st, ev[:min(cnt.value, ev_cap)].copy()
+
+
+class Energy(C.Structure):
+    """orc_energy: the energy bookkeeping's settings and its records."""
+    _fields_ = [("init_steps", C.c_int), ("steps", C.c_int), ("interval", C.c_int), ("rec", C.c_void_p),
+                ("rec_cap", C.c_int), ("rec_count", C.c_int)]
+
+
+def leapfrog_ref32_energy(pos4, vel4, acc4, t_inj, nsteps, dt, eps, init_steps, steps, interval,
+                          efield=(0.0, 0.0, 0.0), bd=None, fld=None, threads=0):
+    """The reference's loop with toggleEnergy(1, init_steps, steps): (pos4,
+    vel4, acc4, records), records (k, 6) float32 = KE_inj, PE_inj, FE_inj, KE,
+    PE, FE per interval, as the energy file holds them."""
+    p = np.ascontiguousarray(pos4, np.float32).copy()
+    v = np.ascontiguousarray(vel4, np.float32).copy()
+    a = np.ascontiguousarray(acc4, np.float32).copy()
+    t = np.ascontiguousarray(t_inj, np.float32)
+    cap = nsteps // max(interval, 1) + 1
+    rec = np.zeros((cap, 6), np.float32)
+    en = Energy(init_steps, steps, interval, rec.ctypes.data, cap, 0)
+    lib().orc_leapfrog_ref32_energy(p.shape[0], p, v, a, t, nsteps, dt, eps, np.asarray(efield, np.float32),
+                                    None if bd is None else C.byref(bd), None if fld is None else C.byref(fld),
+                                    C.byref(en), threads)
+    return p, v, a, rec[:min(en.rec_count, cap)].copy()
 
 
 class Substep(C.Structure):

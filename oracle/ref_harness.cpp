@@ -26,7 +26,11 @@
 //          with subs=dt,bc,bx,by,bz,br,bt;... LeapfrogDKDSubsteps with
 //          setSubstepTimes (direct force); keys steps, dt, crash / bc keys as
 //          dkd; out.bin as dkd, then int32 bytes and the snapshot file
-//          (SaveDataOptions::newOriginal) written at the start and the end
+//          (SaveDataOptions::newOriginal) written at the start and the end;
+//          interval=k: saveData and the energy records every k steps;
+//          energy=init,steps with edir=<folder/>: Integrator::toggleEnergy
+//          (its file goes to edir), out.bin then ends with int32 records and
+//          the energy file (six floats per record)
 // in.bin : int32 n, float pos4[4n], float vel4[4n], float acc4[4n], float tinj[n]
 // out.bin: float pos4[4n], float vel4[4n], float acc4[4n]
 //          (dkd with events=1: then int32 count, count 40-byte event records
@@ -34,6 +38,8 @@
 //          (grid mode: int32 count, int32 points[3*count] in the Grid's order)
 #include "force_calculation_methods.h"
 #include "integration_schemes.h"
+
+#include <dirent.h>
 
 #include <cstdio>
 #include <cstdlib>
@@ -190,7 +196,7 @@ int main(int argc, char **argv) {
         const int steps = (int)getd(kv, "steps", 1);
         ps.params.timeStep = (float)getd(kv, "dt", 1e-13);
         ps.params.numIters = steps;
-        ps.params.interval = steps;  // one saveData at the end (constantRate)
+        ps.params.interval = (int)getd(kv, "interval", steps);  // saveData every interval (constantRate)
         ps.params.timerInfo = TimerOptions::off;
         ps.params.saveDataToggle = SaveDataOptions::newOriginal;
         snap = std::tmpfile();
@@ -245,6 +251,11 @@ int main(int argc, char **argv) {
             leap.runSimulation();
         } else {
             LeapfrogDKD leap(ps, *fm);
+            if (kv.count("energy")) {
+                int init = 0, each = 0;
+                std::sscanf(kv["energy"].c_str(), "%d,%d", &init, &each);
+                leap.toggleEnergy(1, init, each, kv["edir"].c_str());
+            }
             leap.runSimulation();
         }
     } else if (mode == "dkd") {
@@ -339,6 +350,25 @@ int main(int argc, char **argv) {
         std::vector<char> buf((size_t)bytes);
         if (bytes > 0 && std::fread(buf.data(), 1, (size_t)bytes, events) != (size_t)bytes) return 5;
         if (bytes > 0) std::fwrite(buf.data(), 1, (size_t)bytes, fo);
+    }
+    if (mode == "run" && kv.count("energy")) {
+        // the one file toggleEnergy created in edir (closed with the integrator)
+        std::string path;
+        if (DIR *d = opendir(kv["edir"].c_str())) {
+            while (dirent *e = readdir(d))
+                if (std::strncmp(e->d_name, "energy_", 7) == 0) path = kv["edir"] + e->d_name;
+            closedir(d);
+        }
+        std::vector<char> buf;
+        if (FILE *fe = path.empty() ? nullptr : std::fopen(path.c_str(), "rb")) {
+            char tmp[4096];
+            size_t got;
+            while ((got = std::fread(tmp, 1, sizeof tmp, fe)) > 0) buf.insert(buf.end(), tmp, tmp + got);
+            std::fclose(fe);
+        }
+        const int32_t cnt = (int32_t)(buf.size() / 24);
+        std::fwrite(&cnt, 4, 1, fo);
+        if (!buf.empty()) std::fwrite(buf.data(), 1, (size_t)cnt * 24, fo);
     }
     std::fclose(fo);
     // SimulationParameters' destructor releases members the headless set-up

@@ -735,22 +735,143 @@ static int reset_first(int first, int last, const float *acc4) {
     return first;
 }
 
-void orc_leapfrog_ref32_bc(int n, float *pos4, float *vel4, float *acc4,
-                           const float *t_inj, int nsteps, float dt, double eps,
-                           const float efield[3], int sym, int nimg,
-                           const int *images, const float domain_size[3],
-                           const orc_boundary *bd, const orc_field *field,
-                           orc_event *ev, int ev_cap, int *ev_count, int nthreads) {
+/* ---- energy bookkeeping, FP32 as the reference ------------------------ */
+
+/* ParticleSystem::computeChargedKineticEnergy (particles.cpp:535-542):
+ * ((0.5 * AMU) * getMass) * |v|^2, the mass a long double */
+static float ke_ref32(const float *vel4, int i) {
+    const float *v = vel4 + 4 * i;
+    const float s = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    return (float)((long double)(0.5 * (double)REF_AMU) * species_mass_ld((int)v[3]) * (long double)s);
+}
+
+/* ParticleSystem::computeChargedElectricPotentialEnergy (particles.cpp:
+ * 551-571): r^2 in float plus the softening in double, sqrt, q_i q_j / r
+ * summed in float over [first, last) in index order */
+static float pe_ref32(const float *pos4, int i, int first, int last, double eps) {
+    const float ke = (float)(1 / (4.0 * REF_PI * REF_EPS0));
+    const float q2 = REF_ELEM_CHARGE * REF_ELEM_CHARGE;
+    const float *p = pos4 + 4 * i;
+    float epe = 0;
+    for (int j = first; j < last; j++) {
+        if (j == i) continue;
+        const float *o = pos4 + 4 * j;
+        const float dx = p[0] - o[0], dy = p[1] - o[1], dz = p[2] - o[2];
+        float r = (float)((double)(dx * dx + dy * dy + dz * dz) + eps);
+        r = sqrtf(r);
+        epe += p[3] * o[3] / r;
+    }
+    return epe * q2 * ke;
+}
+
+/* ParticleSystem::updateChargedFieldEnergy (particles.cpp:594-638): the work
+ * of the field from init to the particle, first along z at init's (x, y),
+ * then along (x, y) at the particle's z, steps left-point samples each */
+static void fe_update_ref32(const orc_field *f, int *save, const float *pos4, int i, int steps, const float init[3],
+                            float *fe) {
+    if (!f) return;
+    const float *p = pos4 + 4 * i;
+    const double dx = (double)(p[0] - init[0]), dy = (double)(p[1] - init[1]), dz = (double)(p[2] - init[2]);
+    const double px = init[0], py = init[1];
+    double pz = init[2];
+    double tz = 0, tr = 0;
+    float e[3];
+    for (int k = 0; k < steps; k++) {
+        efield_ref32(f, (float)px, (float)py, (float)(pz + k * dz / steps), save, e);
+        tz += e[2] * dz / steps;
+    }
+    pz += dz;
+    for (int k = 0; k < steps; k++) {
+        efield_ref32(f, (float)(px + k * dx / steps), (float)(py + k * dy / steps), (float)pz, save, e);
+        tr += e[0] * dx / steps + e[1] * dy / steps;
+    }
+    double t = tz + tr;
+    t *= (double)(-REF_ELEM_CHARGE * p[3]);
+    fe[i] = (float)((double)fe[i] + t);
+}
+
+typedef struct {
+    float *fe, *ke_inj, *init;   /* per particle; init: 3 per particle */
+    float KE_inj, PE_inj, FE_inj;
+    int prev;                    /* the integrator's tempLastParticlePrev */
+} energy_state;
+
+/* Integrator::initializeEnergyData (integration_schemes.cpp:757-775) at the
+ * state before the first step; the reference position is (0, 0, 140 r0)
+ * (InterpolationScheme::setReferencePosition, interpolation_scheme.cpp:38-47) */
+static void energy_init_ref32(energy_state *E, int n, const float *pos4, const float *vel4, const orc_field *f,
+                              int *save, int steps) {
+    const float ref[3] = {0.0f, 0.0f, f ? 140 * (float)f->r0 : 0.0f};
+    for (int i = 0; i < n; i++) {
+        E->fe[i] = 0;
+        fe_update_ref32(f, save, pos4, i, steps, ref, E->fe);
+        E->ke_inj[i] = ke_ref32(vel4, i);
+        for (int d = 0; d < 3; d++) E->init[3 * i + d] = pos4[4 * i + d];
+    }
+    E->KE_inj = E->PE_inj = E->FE_inj = 0;
+    E->prev = 0;
+}
+
+/* Integrator::updateEnergyInjectionData (integration_schemes.cpp:783-793),
+ * called by driftNew after it set lastParticle, before the drift */
+static void energy_inject_ref32(energy_state *E, const float *pos4, int first, int last, double eps) {
+    for (int i = E->prev; i < last; i++) {
+        E->KE_inj += E->ke_inj[i];
+        E->PE_inj += pe_ref32(pos4, i, first, last, eps);
+        E->FE_inj += E->fe[i];
+    }
+    E->prev = last;
+}
+
+/* Integrator::updateEnergyIntervalData (integration_schemes.cpp:799-835) */
+static void energy_interval_ref32(energy_state *E, orc_energy *en, const float *pos4, const float *vel4,
+                                  const float *t_inj, int first, int last, float tpos, float dt,
+                                  const orc_field *f, int *save, double eps) {
+    float KE = 0, PE = 0, FE = 0;
+    for (int i = first; i < last; i++) {
+        const float tt = fminf(dt * en->interval, tpos - t_inj[i]);
+        const int fe_steps = (int)fmaxf(tt * en->steps / dt, 2.0f);
+        fe_update_ref32(f, save, pos4, i, fe_steps, &E->init[3 * i], E->fe);
+        for (int d = 0; d < 3; d++) E->init[3 * i + d] = pos4[4 * i + d];
+        KE += ke_ref32(vel4, i);
+        PE += pe_ref32(pos4, i, first, last, eps);
+        FE += E->fe[i];
+    }
+    PE /= 2;
+    if (en->rec && en->rec_count < en->rec_cap) {
+        float *r = en->rec + 6 * en->rec_count;
+        r[0] = E->KE_inj; r[1] = E->PE_inj; r[2] = E->FE_inj;
+        r[3] = KE; r[4] = PE; r[5] = FE;
+    }
+    en->rec_count++;
+}
+
+static void leapfrog_ref32_impl(int n, float *pos4, float *vel4, float *acc4,
+                                const float *t_inj, int nsteps, float dt, double eps,
+                                const float efield[3], int sym, int nimg,
+                                const int *images, const float domain_size[3],
+                                const orc_boundary *bd, const orc_field *field,
+                                orc_event *ev, int ev_cap, int *ev_count, orc_energy *en,
+                                int nthreads) {
     /* LeapfrogDKD::runSimulation (integration_schemes.cpp:856-891):
      * driftNew(dt/2), kick(dt), driftNew(dt/2) per step; driftNew
      * (integration_schemes.cpp:705-723) sets lastParticle from the injection
      * times, drifts, then moves firstParticle past inactive particles. */
     const float factor = REF_ELEM_CHARGE / REF_AMU;
     int first = 0, last = 0, cnt = 0, save = -1;
+    energy_state E = {0};
+    if (en) {
+        E.fe = (float *)malloc(sizeof(float) * (size_t)n);
+        E.ke_inj = (float *)malloc(sizeof(float) * (size_t)n);
+        E.init = (float *)malloc(sizeof(float) * 3 * (size_t)n);
+        energy_init_ref32(&E, n, pos4, vel4, field, &save, en->init_steps);
+        en->rec_count = 0;
+    }
     for (int it = 1; it <= nsteps; it++) {
         float tpos = dt * (float)(it - 1);
         float tvel = dt * (float)(it - 1);
         last = most_recent_injected(n, t_inj, tpos + dt / 2) + 1;
+        if (en) energy_inject_ref32(&E, pos4, first, last, eps);
         drift_ref32(first, last, pos4, vel4, acc4, t_inj, tpos, dt / 2, sym, domain_size, bd, ev, ev_cap, &cnt);
         first = reset_first(first, last, acc4);
         tpos += dt / 2;
@@ -789,11 +910,39 @@ void orc_leapfrog_ref32_bc(int n, float *pos4, float *vel4, float *acc4,
             }
         }
         last = most_recent_injected(n, t_inj, tpos + dt / 2) + 1;
+        if (en) energy_inject_ref32(&E, pos4, first, last, eps);
         drift_ref32(first, last, pos4, vel4, acc4, t_inj, tpos, dt / 2, sym, domain_size, bd, ev, ev_cap, &cnt);
         first = reset_first(first, last, acc4);
+        /* Integrator::finishIter (integration_schemes.cpp:584-601) */
+        if (en && it % en->interval == 0)
+            energy_interval_ref32(&E, en, pos4, vel4, t_inj, first, last, tpos + dt / 2, dt, field, &save, eps);
     }
     if (ev_count) *ev_count = cnt;
+    free(E.fe);
+    free(E.ke_inj);
+    free(E.init);
 }
+
+void orc_leapfrog_ref32_bc(int n, float *pos4, float *vel4, float *acc4,
+                           const float *t_inj, int nsteps, float dt, double eps,
+                           const float efield[3], int sym, int nimg,
+                           const int *images, const float domain_size[3],
+                           const orc_boundary *bd, const orc_field *field,
+                           orc_event *ev, int ev_cap, int *ev_count, int nthreads) {
+    leapfrog_ref32_impl(n, pos4, vel4, acc4, t_inj, nsteps, dt, eps, efield, sym, nimg, images, domain_size, bd,
+                        field, ev, ev_cap, ev_count, NULL, nthreads);
+}
+
+void orc_leapfrog_ref32_energy(int n, float *pos4, float *vel4, float *acc4,
+                               const float *t_inj, int nsteps, float dt, double eps,
+                               const float efield[3], const orc_boundary *bd,
+                               const orc_field *field, orc_energy *en, int nthreads) {
+    const float dom[3] = {0, 0, 0};
+    if (!en || en->interval < 1) return;
+    leapfrog_ref32_impl(n, pos4, vel4, acc4, t_inj, nsteps, dt, eps, efield, 0, 0, NULL, dom, bd, field, NULL, 0,
+                        NULL, en, nthreads);
+}
+
 
 void orc_leapfrog_ref32(int n, float *pos4, float *vel4, float *acc4,
                         const float *t_inj, int nsteps, float dt, double eps,

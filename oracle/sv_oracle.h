@@ -157,6 +157,28 @@ void orc_leapfrog_ref32_bc(int n, float *pos4, float *vel4, float *acc4,
                            const orc_boundary *bd, const orc_field *field,
                            orc_event *ev, int ev_cap, int *ev_count, int nthreads);
 
+/* Energy bookkeeping of Integrator (toggleEnergy, integration_schemes.cpp:
+ * 85-97; initializeEnergyData :757-775; updateEnergyInjectionData :783-793;
+ * updateEnergyIntervalData :799-835): init_steps / steps are the numbers of
+ * integration steps of the field energy at initialisation and per interval;
+ * every `interval` steps a record of six floats (KE_inj, PE_inj, FE_inj, KE,
+ * PE, FE in J, the energy file's layout) goes to rec (up to rec_cap records;
+ * rec_count receives the total). */
+typedef struct {
+    int init_steps, steps, interval;
+    float *rec;
+    int rec_cap, rec_count;
+} orc_energy;
+
+/* orc_leapfrog_ref32_bc with the energy bookkeeping of en, FP32 as the
+ * reference keeps it: the potential of a particle sums over the window
+ * [firstParticle, lastParticle) whatever the status, the field energy
+ * integrates the emitter's field (field; none: zero) along z, then r. */
+void orc_leapfrog_ref32_energy(int n, float *pos4, float *vel4, float *acc4,
+                               const float *t_inj, int nsteps, float dt, double eps,
+                               const float efield[3], const orc_boundary *bd,
+                               const orc_field *field, orc_energy *en, int nthreads);
+
 /* One substep request of LeapfrogDKDSubsteps::setSubstepTimes: the largest
  * step dt inside a region (bc: BoundaryConditionOptions; spatial limits s =
  * |x|, |y|, |z|, r; t: time since injection; 0 = unbounded). */

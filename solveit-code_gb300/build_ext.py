@@ -19,7 +19,10 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libsolveit_gpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code: no contraction into fused multiply-adds (gcc contracts by default
+# on aarch64), so FP32 clocks and level tables match the reference's x86 build
 NVFLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+           "-Xcompiler", "-ffp-contract=off",
            "--expt-relaxed-constexpr", "-diag-suppress", "1444"]
 
 

@@ -455,6 +455,7 @@ extern "C" sv_status sv_adjoint_forward(sv_ctx *c, int32_t nsteps, double dt, do
     if (c->B.crash != SV_CRASH_NONE || c->B.bc != SV_BC_NONE || c->B.fold)
         return set_error(c, SV_ERR_UNSUPPORTED, "the adjoint covers drifts without crash, boundary or folding steps");
     if (c->sub.on) return set_error(c, SV_ERR_UNSUPPORTED, "the adjoint covers the single-rate leapfrog");
+    if (c->en.on) return set_error(c, SV_ERR_UNSUPPORTED, "the adjoint runs without the energy bookkeeping");
     if (c->field.nt > 0)
         return set_error(c, SV_ERR_UNSUPPORTED, "the adjoint covers the uniform field only (no emitter field map)");
     SV_CK(c, cudaSetDevice(c->device));

@@ -417,6 +417,7 @@ void sv_destroy(sv_ctx *c) {
     events_free(c);
     field_free(c);
     substeps_free(c);
+    energy_free(c);
     free_state(c);
     Sorted &S = c->S;
     cudaFree(S.x); cudaFree(S.y); cudaFree(S.z); cudaFree(S.q); cudaFree(S.qm);
@@ -464,6 +465,7 @@ static sv_status upload_state(sv_ctx *c, int64_t n, const double *x3, const doub
     SV_TRY(field_prepare(c));
     SV_TRY(field_reset(c));
     SV_TRY(substeps_reset_levels(c));
+    energy_rearm(c);
     if (n == 0) return SV_OK;
     SV_CK(c, cudaMemsetAsync(c->e2, 0, sizeof(float) * 3 * (size_t)n, c->stream));
     SV_CK(c, cudaMemsetAsync(c->e1, 0, sizeof(float) * 3 * (size_t)n, c->stream));
@@ -516,6 +518,7 @@ sv_status sv_upload_ref32(sv_ctx *c, int64_t n, const float *pos4, const float *
     SV_TRY(field_prepare(c));
     SV_TRY(field_reset(c));
     SV_TRY(substeps_reset_levels(c));
+    energy_rearm(c);
     if (n == 0) return SV_OK;
     SV_CK(c, cudaMemsetAsync(c->e2, 0, sizeof(float) * 3 * (size_t)n, c->stream));
     SV_CK(c, cudaMemsetAsync(c->e1, 0, sizeof(float) * 3 * (size_t)n, c->stream));
@@ -679,6 +682,8 @@ sv_status sv_leapfrog(sv_ctx *c, int32_t nsteps, double dt, double t0) {
     if (!c->have_state) return set_error(c, SV_ERR_STATE, "no state uploaded");
     if (nsteps < 0 || !(dt > 0.0)) return set_error(c, SV_ERR_INVALID, "nsteps >= 0 and dt > 0 required");
     SV_CK(c, cudaSetDevice(c->device));
+    if (c->en.on && (c->batch || c->sub.on))
+        return set_error(c, SV_ERR_UNSUPPORTED, "energy bookkeeping runs with the single-rate leapfrog of one plume");
     if (c->batch) {
         SV_TRY(batch_leapfrog(c, nsteps, dt, t0));
     } else if (c->sub.on) {

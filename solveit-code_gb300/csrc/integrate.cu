@@ -412,7 +412,9 @@ sv_status leapfrog_step(sv_ctx *c, double ts, double dt, double *save_xh) {
     const double h = 0.5 * dt;
     if (c->B.crash != SV_CRASH_NONE || c->B.bc != SV_BC_NONE) SV_TRY(events_reserve(c));
     SV_TRY(field_prepare(c));
+    SV_TRY(energy_inject(c, ts + h));
     SV_TRY(drift(c, ts, h, c->wstatus));
+    SV_TRY(energy_first(c, ts + h));
     if (save_xh) {
         const size_t b = sizeof(double) * c->n;
         SV_CK(c, cudaMemcpyAsync(save_xh, c->x, b, cudaMemcpyDeviceToDevice, c->stream));
@@ -424,8 +426,10 @@ sv_status leapfrog_step(sv_ctx *c, double ts, double dt, double *save_xh) {
     c->fstatus = nullptr;
     SV_TRY(s);
     SV_TRY(kick(c, ts, dt, c->wstatus));
+    SV_TRY(energy_inject(c, ts + dt));
     SV_TRY(drift(c, ts + h, h, nullptr));
-    return SV_OK;
+    SV_TRY(energy_first(c, ts + dt));
+    return energy_interval(c, ts, dt);
 }
 
 sv_status energy(sv_ctx *c, double *ke, double *pe) {

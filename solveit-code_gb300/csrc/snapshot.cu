@@ -1,7 +1,8 @@
 // snapshot.cu -- the state records of the reference's snapshot files
 // (Integrator::saveData, integration_schemes.cpp:266-331), packed on the
 // device: one record per active particle (status 1 or 2) with index in
-// [first, last), in index order (a flag scan gives each record its place).
+// [first, last), or per particle (saveFullCurrentConditions, :197-258), in
+// index order (a flag scan gives each record its place).
 //   original:    x, y, z, vx, vy, vz, E1[3], E2[3] (float), species (u32),
 //                index (i32), lastParticle (i32)                    60 bytes
 //   newOriginal: header 0xffffffff (u32), lastParticle (i32), currentTime
@@ -19,12 +20,14 @@
 namespace sv {
 namespace {
 
-__global__ void active_flags(const int32_t *__restrict__ st, int64_t n, int64_t first, int64_t last,
+// saveData keeps status 1 and 2 in [first, last); saveFullCurrentConditions
+// (integration_schemes.cpp:197-258) every particle
+__global__ void active_flags(const int32_t *__restrict__ st, int64_t n, int64_t first, int64_t last, int full,
                              int *__restrict__ flag) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int32_t w = st[i];
-    flag[i] = (i >= first && i < last && (w == 1 || w == 2)) ? 1 : 0;
+    flag[i] = (full || (i >= first && i < last && (w == 1 || w == 2))) ? 1 : 0;
 }
 
 __global__ void pack_records(const int *__restrict__ flag, const int *__restrict__ pos, int64_t n,
@@ -65,6 +68,8 @@ using namespace sv;
 extern "C" sv_status sv_snapshot(sv_ctx *c, int32_t format, int64_t first, int64_t last, float current_time,
                                  void *out, int64_t cap_bytes, int64_t *bytes) {
     if (!c || !bytes || cap_bytes < 0) return SV_ERR_INVALID;
+    const int full = (format & SV_SNAPSHOT_FULL) ? 1 : 0;
+    format &= ~SV_SNAPSHOT_FULL;
     if (format != SV_SNAPSHOT_ORIGINAL && format != SV_SNAPSHOT_NEW_ORIGINAL)
         return set_error(c, SV_ERR_INVALID, "unknown snapshot format %d", format);
     if (!c->have_state) return set_error(c, SV_ERR_STATE, "no state uploaded");
@@ -89,7 +94,7 @@ extern "C" sv_status sv_snapshot(sv_ctx *c, int32_t format, int64_t first, int64
         flag = (int *)((char *)stg + tmp_al);
         int *pos = flag + n;
         cudaError_t e = cudaSuccess;
-        active_flags<<<div_up(n, 256), 256, 0, c->stream>>>(c->status, n, first, last, flag);
+        active_flags<<<div_up(n, 256), 256, 0, c->stream>>>(c->status, n, first, last, full, flag);
         c->launches++;
         if ((e = cudaGetLastError()) == cudaSuccess)
             e = cub::DeviceScan::ExclusiveSum(cub_tmp, tmp, flag, pos, (int)n, c->stream);

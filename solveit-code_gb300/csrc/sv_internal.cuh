@@ -73,6 +73,28 @@ struct SubTable {
     double bs[kMaxSubLevels][4] = {};
     double bt[kMaxSubLevels] = {};
 };
+
+// energy bookkeeping of the reference's integrator (sv_set_energy, energy.cu)
+struct EnergyBook {
+    int on = 0, init_steps = 0, steps = 0, interval = 1;
+    bool need_init = true;        // initialise at the next leapfrog step
+    bool have_prev = false;       // an injection pass has run (t_prev is set)
+    double t_prev = 0.0;          // particles with t_inj <= t_prev are counted as injected
+    int64_t cap = 0;
+    double *fe = nullptr, *ke_inj = nullptr;     // per particle: field energy, kinetic energy at set-up (J)
+    double *ix = nullptr, *iy = nullptr, *iz = nullptr;  // end of the last field-energy path
+    float4 *ph = nullptr, *pl = nullptr;         // positions as FP32 hi + lo, charge / index
+    int *list = nullptr;                         // compacted particles of one pass
+    double *pot = nullptr;                       // their sum of q_j / r over the window
+    int *walk = nullptr;                         // per particle: start triangle of the field walk
+    void *scan_tmp = nullptr;
+    size_t scan_bytes = 0;
+    unsigned long long *d_first = nullptr;       // [0] the window's first particle, [1] candidate
+    int *d_cnt = nullptr;                        // compacted count
+    double *d_acc = nullptr;                     // KE_inj, PE_inj, FE_inj, KE, PE, FE (J)
+    sv_energy_record *recs = nullptr;            // host records not yet drained
+    int64_t nrec = 0, rec_cap = 0;
+};
 }  // namespace sv
 
 struct sv_ctx {
@@ -110,6 +132,8 @@ struct sv_ctx {
     sv::SubTable sub{};
     int8_t *sub_level = nullptr;
     int64_t sub_cap = 0;
+    // energy bookkeeping (sv_set_energy)
+    sv::EnergyBook en{};
     // last acceleration (force only), caller order, FP64
     double *ax = nullptr, *ay = nullptr, *az = nullptr;
     bool have_state = false, have_accel = false;
@@ -258,6 +282,16 @@ sv_status substeps_run(sv_ctx *c, int32_t nsteps, double dt, double t0);
 sv_status substeps_reset_levels(sv_ctx *c);
 void substeps_free(sv_ctx *c);
 sv_status energy(sv_ctx *c, double *ke, double *pe);
+// energy.cu: the bookkeeping hooks of a leapfrog step (no-ops when off).
+// Before a drift that ends at t_end: count the particles injected since the
+// previous one; after it: move the window's first particle; after the step
+// that starts at ts: the interval record.
+sv_status energy_inject(sv_ctx *c, double t_end);
+sv_status energy_first(sv_ctx *c, double t_end);
+sv_status energy_interval(sv_ctx *c, double ts, double dt);
+void energy_free(sv_ctx *c);
+// a new state: set-up again at the next step, records cleared
+void energy_rearm(sv_ctx *c);
 
 // image offsets (metres) of the translational lattice, in summation order
 int trans_images(const sv_params &P, double *out, int max_out);

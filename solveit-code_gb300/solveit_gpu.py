@@ -21,7 +21,7 @@ SYM_NONE, SYM_ROTATIONAL, SYM_TRANSLATIONAL = 0, 1, 2
 MIXED, FP64 = 0, 1
 FMM_FMM, FMM_OUTLIERS, TREECODE, TREECODE_OUTLIERS = 0, 1, 2, 3
 CRASH_NONE, CRASH_EXTRACTOR_GRID = 0, 1
-SNAPSHOT_ORIGINAL, SNAPSHOT_NEW_ORIGINAL = 0, 1
+SNAPSHOT_ORIGINAL, SNAPSHOT_NEW_ORIGINAL, SNAPSHOT_FULL = 0, 1, 16
 BC_NONE, BC_SPACE, BC_TIME, BC_SPACE_AND_TIME = 0, 1, 2, 3
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "allocation failed", 4: "bad state",
@@ -35,8 +35,13 @@ ABI_SYMBOLS = (
     "sv_launch_count", "sv_last_error", "sv_abi_version", "sv_adjoint_forward", "sv_adjoint_backward",
     "sv_direct_accel_noalloc", "sv_upload_batch", "sv_batch_tune", "sv_batch_get_info", "sv_batch_set_tuning",
     "sv_get_outliers", "sv_set_boundary", "sv_get_boundary", "sv_get_events", "sv_set_emitter_field",
-    "sv_emitter_field_at", "sv_set_substeps", "sv_get_substep_levels", "sv_snapshot",
+    "sv_emitter_field_at", "sv_set_substeps", "sv_get_substep_levels", "sv_snapshot", "sv_set_energy",
+    "sv_get_energy_records",
 )
+
+# sv_energy_record: the energy file's record (J)
+ENERGY_DTYPE = np.dtype([("ke_inj", "<f4"), ("pe_inj", "<f4"), ("fe_inj", "<f4"), ("ke", "<f4"), ("pe", "<f4"),
+                         ("fe", "<f4")])
 
 
 class Params(C.Structure):
@@ -148,6 +153,8 @@ def load(path: str = LIB_PATH):
     L.sv_set_substeps.argtypes = [vp, C.c_double, C.c_int32, vp]
     L.sv_snapshot.argtypes = [vp, C.c_int32, C.c_int64, C.c_int64, C.c_float, vp, C.c_int64, C.POINTER(C.c_int64)]
     L.sv_get_substep_levels.argtypes = [vp, vp]
+    L.sv_set_energy.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
+    L.sv_get_energy_records.argtypes = [vp, vp, C.c_int64, C.POINTER(C.c_int64)]
     for name in ABI_SYMBOLS:
         if name not in ("sv_destroy", "sv_stream", "sv_launch_count", "sv_last_error", "sv_abi_version"):
             getattr(L, name).restype = C.c_int
@@ -330,8 +337,21 @@ class ForceMethod:
         self._check(self.L.sv_get_substep_levels(self.h, _p(out)))
         return out
 
+    def set_energy(self, init_steps, steps, interval, enable=True):
+        """Integrator::toggleEnergy: records every `interval` steps of leapfrog()."""
+        self._check(self.L.sv_set_energy(self.h, 1 if enable else 0, init_steps, steps, interval))
+
+    def energy_records(self):
+        """The energy records kept since the last call (structured array of ENERGY_DTYPE)."""
+        cnt = C.c_int64()
+        self._check(self.L.sv_get_energy_records(self.h, None, 0, C.byref(cnt)))
+        out = np.zeros(cnt.value, ENERGY_DTYPE)
+        self._check(self.L.sv_get_energy_records(self.h, out.ctypes.data, cnt.value, C.byref(cnt)))
+        return out[:cnt.value]
+
     def snapshot(self, fmt=1, first=0, last=-1, current_time=0.0):
-        """The snapshot-file bytes of the current state (fmt: SNAPSHOT_ORIGINAL / SNAPSHOT_NEW_ORIGINAL)."""
+        """The snapshot-file bytes of the current state (fmt: SNAPSHOT_ORIGINAL / SNAPSHOT_NEW_ORIGINAL,
+        with SNAPSHOT_FULL or-ed in for saveFullCurrentConditions)."""
         nb = C.c_int64()
         self._check(self.L.sv_snapshot(self.h, fmt, first, last, current_time, None, 0, C.byref(nb)))
         out = np.zeros(nb.value, np.uint8)

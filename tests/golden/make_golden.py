@@ -35,6 +35,10 @@ Fixtures (all FP32 vec4 arrays in the reference layout):
                     LeapfrogDKDSubsteps::runSimulation (two substep tables)
                     over 6 steps with staggered injection, with the snapshot
                     files they write (``... make_golden.py substeps``).
+  energy.npz        the reference's LeapfrogDKD::runSimulation with
+                    toggleEnergy over 6 steps: the energy file's records,
+                    without and with the emitter field and with inactive
+                    particles at the front (``... make_golden.py energy``).
 """
 from __future__ import annotations
 
@@ -62,13 +66,22 @@ def run_ref(variant, mode, pos4, vel4, acc4, tinj, **kw):
             np.array([n], np.int32).tofile(f)
             for a in (pos4, vel4, acc4, tinj):
                 np.ascontiguousarray(a).tofile(f)
+        if "energy" in kw:
+            kw = dict(kw, edir=os.path.join(td, "energy") + "/")
+            os.mkdir(kw["edir"])
         args = [HARNESS.format(variant), mode, fin, fout] + [f"{k}={v}" for k, v in kw.items()]
-        subprocess.check_call(args)
+        subprocess.check_call(args, stdout=subprocess.DEVNULL)
         if mode == "run":
             raw = np.fromfile(fout, np.uint8)
             out = raw[:48 * n].view(np.float32).reshape(3, n, 4)
             nb = int(raw[48 * n:48 * n + 4].view(np.int32)[0])
-            return out[0].copy(), out[1].copy(), out[2].copy(), raw[48 * n + 4:48 * n + 4 + nb].copy()
+            snap = raw[48 * n + 4:48 * n + 4 + nb].copy()
+            if "energy" in kw:
+                o = 48 * n + 4 + nb
+                cnt = int(raw[o:o + 4].view(np.int32)[0])
+                rec = raw[o + 4:o + 4 + 24 * cnt].view(np.float32).reshape(cnt, 6).copy()
+                return out[0].copy(), out[1].copy(), out[2].copy(), snap, rec
+            return out[0].copy(), out[1].copy(), out[2].copy(), snap
         if mode == "efield":
             return np.fromfile(fout, np.float32).reshape(n, 3)
         if mode == "grid":
@@ -268,6 +281,50 @@ def substeps():
                         eps=np.float64(1e-20), **out)
 
 
+# energy bookkeeping runs: (init steps, steps per interval, interval, with the emitter field, leading inactive)
+ENERGY_CASES = {
+    "plain": (10, 10, 2, False, False),
+    "field": (40, 20, 2, True, False),
+    "window": (40, 20, 3, True, True),
+}
+
+
+def energy():
+    """The reference's own LeapfrogDKD::runSimulation with toggleEnergy: the
+    energy file's records (KE_inj, PE_inj, FE_inj, KE, PE, FE per interval)
+    on a plume injected in groups, without and with the emitter field, and
+    with inactive particles at the front of the array (the window's first
+    particle moves past them; inactive ones behind it still count)."""
+    nodes, er, ez, tri, nbr = emitter_mesh()
+    r0, e0 = 1e-8, 1e9
+    out = dict(node_rz=nodes, e_r=er, e_z=ez, triangles=tri, neighbors=nbr, r0=np.float64(r0), e0=np.float64(e0))
+    st = plume.make_plume(256, 1.2e-6, 9050)
+    st["t_inj"][:] = np.floor(np.arange(256) / 64) * 2.03e-12
+    st["status"][[11, 77]] = 2
+    with tempfile.TemporaryDirectory() as td:
+        with open(os.path.join(td, "fields.csv"), "w") as f:
+            for k in range(len(er)):
+                f.write(f"{nodes[k, 0]:.17g},{nodes[k, 1]:.17g},{er[k]:.17g},{ez[k]:.17g}\n")
+        with open(os.path.join(td, "triangles.csv"), "w") as f:
+            for t, nb in zip(tri, nbr):
+                f.write(",".join(str(int(v)) for v in (*t, *nb)) + "\n")
+        keys = dict(fdir=td + "/", fnodes="fields.csv", ftris="triangles.csv", r0=r0, e0=e0)
+        for name, (init, each, interval, fld, lead) in ENERGY_CASES.items():
+            s = {k: v.copy() for k, v in st.items()}
+            if lead:
+                s["status"][:5] = 0
+                s["status"][100] = -1
+            pos4, vel4, acc4, tinj = plume.to_ref32(s)
+            p, v, a, _, rec = run_ref("eps20", "run", pos4, vel4, acc4, tinj, threads=4, steps=6, dt=1e-12,
+                                      interval=interval, energy=f"{init},{each}", **(keys if fld else {}))
+            out.update({f"{name}_pos4": pos4, f"{name}_vel4": vel4, f"{name}_acc4": acc4, f"{name}_tinj": tinj,
+                        f"{name}_pos4_out": p, f"{name}_vel4_out": v, f"{name}_acc4_out": a,
+                        f"{name}_records": rec, f"{name}_setup": np.array([init, each, interval, fld], np.int32)})
+            print(name, "records", rec.shape[0])
+    np.savez_compressed(os.path.join(HERE, "energy.npz"), steps=np.int32(6), dt=np.float32(1e-12),
+                        eps=np.float64(1e-20), **out)
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["outliers"]:
         outliers()
@@ -277,5 +334,7 @@ if __name__ == "__main__":
         emitter_field()
     elif sys.argv[1:] == ["substeps"]:
         substeps()
+    elif sys.argv[1:] == ["energy"]:
+        energy()
     else:
         main()
