@@ -251,6 +251,37 @@ __global__ void zero_nontargets(double *__restrict__ ax, double *__restrict__ ay
     if (!(st[i] == 1 && i >= first && i < last)) ax[i] = ay[i] = az[i] = 0.0;
 }
 
+// Host <-> device copies split in pieces over the copy streams, so that
+// several copy engines share a large transfer: ordered after the work already
+// on c->stream and joined back into it.
+struct HostCopy {
+    void *dst;
+    const void *src;
+    size_t bytes;
+};
+constexpr int kCopyWays = 4;
+
+static sv_status copy_split(sv_ctx *c, const HostCopy *cp, int ncp, cudaMemcpyKind kind) {
+    if (!c->cps[0]) {
+        for (int k = 0; k < kCopyWays; k++) SV_CK(c, cudaStreamCreateWithFlags(&c->cps[k], cudaStreamNonBlocking));
+        for (int k = 0; k <= kCopyWays; k++) SV_CK(c, cudaEventCreateWithFlags(&c->cpe[k], cudaEventDisableTiming));
+    }
+    SV_CK(c, cudaEventRecord(c->cpe[kCopyWays], c->stream));
+    for (int k = 0; k < kCopyWays; k++) SV_CK(c, cudaStreamWaitEvent(c->cps[k], c->cpe[kCopyWays], 0));
+    for (int i = 0; i < ncp; i++) {
+        const size_t piece = (cp[i].bytes / kCopyWays + 4095) & ~(size_t)4095;
+        for (int k = 0; k < kCopyWays && piece * k < cp[i].bytes; k++) {
+            const size_t o = piece * k, b = std::min(piece, cp[i].bytes - o);
+            SV_CK(c, cudaMemcpyAsync((char *)cp[i].dst + o, (const char *)cp[i].src + o, b, kind, c->cps[k]));
+        }
+    }
+    for (int k = 0; k < kCopyWays; k++) {
+        SV_CK(c, cudaEventRecord(c->cpe[k], c->cps[k]));
+        SV_CK(c, cudaStreamWaitEvent(c->stream, c->cpe[k], 0));
+    }
+    return SV_OK;
+}
+
 sv_status stage_bytes(sv_ctx *c, size_t bytes, void **p) {
     if (c->d_stage_bytes < bytes) {
         cudaFree(c->d_stage);
@@ -431,6 +462,10 @@ void sv_destroy(sv_ctx *c) {
     if (c->ev_end) cudaEventDestroy(c->ev_end);
     for (int k = 0; k < 9; k++)
         if (c->ph_ev[k]) cudaEventDestroy(c->ph_ev[k]);
+    for (int k = 0; k < 4; k++)
+        if (c->cps[k]) cudaStreamDestroy(c->cps[k]);
+    for (int k = 0; k < 5; k++)
+        if (c->cpe[k]) cudaEventDestroy(c->cpe[k]);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -479,12 +514,13 @@ static sv_status upload_state(sv_ctx *c, int64_t n, const double *x3, const doub
     double *dm = (double *)p; p += b1;
     double *dt = (double *)p; p += b1;
     int32_t *ds = (int32_t *)p;
-    SV_CK(c, cudaMemcpyAsync(dx3, x3, b3, cudaMemcpyHostToDevice, c->stream));
-    if (v3) SV_CK(c, cudaMemcpyAsync(dv3, v3, b3, cudaMemcpyHostToDevice, c->stream));
-    SV_CK(c, cudaMemcpyAsync(dq, q, b1, cudaMemcpyHostToDevice, c->stream));
-    SV_CK(c, cudaMemcpyAsync(dm, m_amu, b1, cudaMemcpyHostToDevice, c->stream));
-    if (t_inj) SV_CK(c, cudaMemcpyAsync(dt, t_inj, b1, cudaMemcpyHostToDevice, c->stream));
-    SV_CK(c, cudaMemcpyAsync(ds, status, sizeof(int32_t) * n, cudaMemcpyHostToDevice, c->stream));
+    const HostCopy cp[6] = {{dx3, x3, b3},
+                            {dv3, v3, v3 ? b3 : 0},
+                            {dq, q, b1},
+                            {dm, m_amu, b1},
+                            {dt, t_inj, t_inj ? b1 : 0},
+                            {ds, status, sizeof(int32_t) * (size_t)n}};
+    SV_TRY(copy_split(c, cp, 6, cudaMemcpyHostToDevice));
     unpack_fp64<<<grid_of(n), 256, 0, c->stream>>>(dx3, dv3, dq, dm, ds, dt, n, v3 != nullptr, t_inj != nullptr,
                                                    c->x, c->y, c->z, c->vx, c->vy, c->vz, c->q, c->m,
                                                    c->status, c->t_inj);
@@ -554,9 +590,10 @@ sv_status sv_download(sv_ctx *c, double *x3, double *v3, int32_t *status) {
     double *dx3 = (double *)stg, *dv3 = dx3 + 3 * n;
     pack_fp64<<<grid_of(n), 256, 0, c->stream>>>(c->x, c->y, c->z, c->vx, c->vy, c->vz, n, dx3, dv3);
     SV_LAUNCHED(c);
-    if (x3) SV_CK(c, cudaMemcpyAsync(x3, dx3, b3, cudaMemcpyDeviceToHost, c->stream));
-    if (v3) SV_CK(c, cudaMemcpyAsync(v3, dv3, b3, cudaMemcpyDeviceToHost, c->stream));
-    if (status) SV_CK(c, cudaMemcpyAsync(status, c->status, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, c->stream));
+    const HostCopy cp[3] = {{x3, dx3, x3 ? b3 : 0},
+                            {v3, dv3, v3 ? b3 : 0},
+                            {status, c->status, status ? sizeof(int32_t) * (size_t)n : 0}};
+    SV_TRY(copy_split(c, cp, 3, cudaMemcpyDeviceToHost));
     SV_CK(c, cudaStreamSynchronize(c->stream));
     return SV_OK;
 }
@@ -607,6 +644,7 @@ sv_status sv::compute_accel_device(sv_ctx *c, int64_t first, int64_t last) {
     const sv_status st_run = [&]() -> sv_status {
     if (n > 0) {
         phase_mark(c, 0);
+        c->S.far = nullptr;
         if (outliers) {
             // outliers leave the tree; their interactions are summed directly below
             const int32_t *st2 = nullptr;

@@ -65,6 +65,7 @@ struct Fmm {
     int64_t tgt_cap = 0;
     float4 *rel = nullptr;   // particle offset from its leaf box centre (FP32) + charge
     int64_t rel_cap = 0;
+    double *far = nullptr;   // far-field acceleration (L2P / M2P), 3 x rel_cap, added in the scatter
     // forest (batched plumes): tree and per-level arrays carved at reserve time
     Tree *ftree = nullptr;
     void *farena = nullptr;
@@ -958,7 +959,9 @@ __device__ __forceinline__ void kahan_add(float &s, float &e, float v) {
 // needed only when eps^2 < kMinR2 (a zero-distance pair without softening).  Targets: one per lane; a
 // chunk of nt < 32 targets gives each target a group of g lanes (a power of
 // two, nt * g <= 32) that split the staged sources.  Each 32-source chunk's
-// FP32 partial sum is added with Kahan compensation.  UQ: every particle of
+// FP32 partial sum is added with Kahan compensation.  The result is stored
+// (each particle of a box with targets once; boxes without targets are left
+// as they are).  UQ: every particle of
 // the tree carries the same charge Q (box_relative_kernel found no other), so
 // the pair weight is r^-3 alone, the sums are scaled by the target's own
 // charge (= Q) at the end, and padding sources sit far away (r^-3 underflows
@@ -1076,15 +1079,15 @@ p2p_body(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, co
         }
         {
             const double c = UQ ? qm[ia] * (double)ta.w : qm[ia];
-            ax[ia] += (double)(sax - eax) * c;
-            ay[ia] += (double)(say - eay) * c;
-            az[ia] += (double)(saz - eaz) * c;
+            ax[ia] = (double)(sax - eax) * c;
+            ay[ia] = (double)(say - eay) * c;
+            az[ia] = (double)(saz - eaz) * c;
         }
         if (vb) {
             const double c = UQ ? qm[ib] * (double)tbv.w : qm[ib];
-            ax[ib] += (double)(sbx - ebx) * c;
-            ay[ib] += (double)(sby - eby) * c;
-            az[ib] += (double)(sbz - ebz) * c;
+            ax[ib] = (double)(sbx - ebx) * c;
+            ay[ib] = (double)(sby - eby) * c;
+            az[ib] = (double)(sbz - ebz) * c;
         }
     }
     for (; tb < t1; tb += 32) {
@@ -1168,9 +1171,9 @@ p2p_body(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, co
         }
         if (valid && sub == 0) {
             const double c = UQ ? qm[i] * (double)ti.w : qm[i];
-            ax[i] += (double)sx * c;
-            ay[i] += (double)sy * c;
-            az[i] += (double)sz * c;
+            ax[i] = (double)sx * c;
+            ay[i] = (double)sy * c;
+            az[i] = (double)sz * c;
         }
     }
     __syncwarp();
@@ -1281,16 +1284,21 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
     }
     if (F.rel_cap < c->S.n) {
         cudaFree(F.rel);
+        cudaFree(F.far);
         F.rel = nullptr;
+        F.far = nullptr;
         SV_CK(c, cudaMalloc(&F.rel, sizeof(float4) * c->S.n));
+        SV_CK(c, cudaMalloc(&F.far, 3 * sizeof(double) * c->S.n));
         F.rel_cap = c->S.n;
     }
+    double *fx = F.far, *fy = F.far + F.rel_cap, *fz = F.far + 2 * F.rel_cap;
     // Two streams from here on.  The second builds the target flags and the
     // interaction lists, then runs the near field (P2P), which needs only the
-    // sorted particles, the leaf boxes and their near lists, summing into the
-    // zeroed accelerations.  The main stream runs the upward pass beside the
-    // lists, waits for them, runs M2L / L2L beside the near field, waits for
-    // it and adds the far field (L2P or the treecode's M2P).
+    // sorted particles, the leaf boxes and their near lists, and writes the
+    // accelerations.  The main stream runs the upward pass beside the lists,
+    // waits for them, runs M2L / L2L and the far field (L2P or the treecode's
+    // M2P, into their own arrays) beside the near field, then waits for it;
+    // the scatter to the caller's order adds the two.
     SV_CK(c, cudaEventRecord(F.ev_fork, c->stream));
     SV_CK(c, cudaStreamWaitEvent(F.side, F.ev_fork, 0));
     root_nbr_kernel<<<1, 128, 0, F.side>>>(nbr[0], ns, 1, nullptr);
@@ -1317,9 +1325,6 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
     SV_CK(c, cudaEventRecord(F.ev_lists, F.side));
     {
         const Level &V = T.lv[L];
-        SV_CK(c, cudaMemsetAsync(S.ax, 0, sizeof(double) * c->S.n, F.side));
-        SV_CK(c, cudaMemsetAsync(S.ay, 0, sizeof(double) * c->S.n, F.side));
-        SV_CK(c, cudaMemsetAsync(S.az, 0, sizeof(double) * c->S.n, F.side));
         box_relative_kernel<<<div_up(V.nbox, kWarps), kWarps * 32, 0, F.side>>>(
             V.nbox, nullptr, nullptr, V.start, V.coord, S.x, S.y, S.z, S.q, S.root, L, F.rel, F.d_counts + 2);
         SV_LAUNCHED(c);
@@ -1403,8 +1408,8 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         }
     }
     phase_mark(c, 5);
-    // far field, added to the near field once that has finished
-    SV_CK(c, cudaStreamWaitEvent(c->stream, F.ev_join, 0));
+    // far field into its own arrays, beside the near field
+    S.far = nullptr;
     {
         const Level &V = T.lv[L];
         if (L >= 2 && treecode) {
@@ -1429,20 +1434,24 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
             ta.root = S.root;
             ta.nrm = F.nrm;
             ta.eps2 = c->P.softening2;
-            ta.ax = S.ax;
-            ta.ay = S.ay;
-            ta.az = S.az;
-            ta.accumulate = 1;
+            ta.ax = fx;
+            ta.ay = fy;
+            ta.az = fz;
+            ta.accumulate = 0;
             m2p_kernel<P><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(ta);
             SV_LAUNCHED(c);
+            S.far = F.far;
         } else if (L >= 2) {
             l2p_kernel<P><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
-                V.nbox, nullptr, nullptr, V.start, V.coord, S.x, S.y, S.z, S.qm, S.root, L, F.nrm, Lv[L], S.ax, S.ay,
-                S.az, tgt[L], 1);
+                V.nbox, nullptr, nullptr, V.start, V.coord, S.x, S.y, S.z, S.qm, S.root, L, F.nrm, Lv[L], fx, fy, fz,
+                tgt[L], 0);
             SV_LAUNCHED(c);
+            S.far = F.far;
         }
+        S.far_stride = F.rel_cap;
         phase_mark(c, 6);
     }
+    SV_CK(c, cudaStreamWaitEvent(c->stream, F.ev_join, 0));
     SV_CK(c, cudaMemcpyAsync(F.h_counts, F.d_counts, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                              c->stream));
     c->stats.levels = L;
@@ -1626,7 +1635,7 @@ void fmm_free(sv_ctx *c) {
     cudaFree(F.cls_theta); cudaFree(F.cls_phase); cudaFree(F.cls_rho2); cudaFree(F.dmat);
     cudaFree(F.zc); cudaFree(F.nrm); cudaFree(F.otab); cudaFree(F.arena); cudaFree(F.d_counts);
     cudaFree(F.ex); cudaFree(F.ey); cudaFree(F.ez); cudaFree(F.eq); cudaFree(F.em); cudaFree(F.est);
-    cudaFree(F.eoff); cudaFree(F.has_tgt); cudaFree(F.rel);
+    cudaFree(F.eoff); cudaFree(F.has_tgt); cudaFree(F.rel); cudaFree(F.far);
     cudaFree(F.farena); cudaFree(F.frel);
     if (F.ftree) {
         tree_release(*F.ftree);

@@ -33,6 +33,10 @@ struct Sorted {
     uint64_t *keys = nullptr, *keys_alt = nullptr;
     uint32_t *idx_alt = nullptr;
     double *ax = nullptr, *ay = nullptr, *az = nullptr;  // acceleration, sorted order
+    // a second field to add in the scatter (the FMM's far field: x, y, z at
+    // far, far + far_stride, far + 2 far_stride), or null; cleared by it
+    const double *far = nullptr;
+    int64_t far_stride = 0;
     void *cub_tmp = nullptr;
     size_t cub_bytes = 0;
     double *root = nullptr;    // device [16]: origin xyz, cube side S, bbox max xyz, empty flag, 2^21/S
@@ -147,6 +151,10 @@ struct sv_ctx {
     // device staging for interleaved <-> SoA transfers
     void *d_stage = nullptr;
     size_t d_stage_bytes = 0;
+    // copy streams of the host <-> device transfers (upload, download) and
+    // their join events, the last one the fork from the context's stream
+    cudaStream_t cps[4] = {};
+    cudaEvent_t cpe[5] = {};
     double *d_scalar = nullptr;   // device scratch for small reductions
     double *h_scalar = nullptr;   // pinned mirror
     cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
