@@ -490,6 +490,10 @@ def run_ours(args, wl, rank, world, local):
         kw = dict(method=sv.DIRECT, precision=sv.FP64 if wl.get("precision") == "fp64" else sv.MIXED)
     fm = sv.ForceMethod(softening2=EPS2, efield=(0.0, 0.0, EZ), device=local, profile_phases=1, **kw)
     fm.upload(st)
+    root_scale, tune_ms = None, None
+    if wl["method"] == "fmm" and not args.no_tune:
+        # untimed set-up: the root cube's scale (leaf box size) for this plume
+        root_scale, tune_ms = fm.fmm_tune()
     stream = torch.cuda.ExternalStream(fm.stream, device=local)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
 
@@ -582,7 +586,10 @@ def run_ours(args, wl, rank, world, local):
             "config": {"workload": args.workload, "desc": wl["desc"], "n_per_gpu": n,
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                        "l2": "512 MB written between timed steps (L2 flush)", "leaf_level": stats.levels,
-                       "leaf_boxes": stats.boxes},
+                       "leaf_boxes": stats.boxes, "fmm_root_scale": root_scale,
+                       "tuning": None if root_scale is None else
+                       f"sv_fmm_tune before the warm-up (untimed): root scales 1..1.875, kept {root_scale} "
+                       f"({tune_ms:.3f} ms per force evaluation)"},
             "clocks": clocks, "e2e": e2e, "gpu_launches": int(launches // max(1, args.steps)) * args.steps,
             "wall_s_timed_region": wall}
 
@@ -676,7 +683,7 @@ def main():
     ap.add_argument("--timed-only", action="store_true",
                     help="only the device-resident timed steps (for profiler launch lists)")
     ap.add_argument("--no-tune", action="store_true",
-                    help="batch workload: skip the autotuner (default depth-model weight)")
+                    help="skip the autotuner (batch: default depth-model weight; FMM: power-of-two root cube)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     rank, world, local = dist_env()

@@ -99,7 +99,11 @@ typedef struct {
     int32_t device;          /* CUDA device ordinal */
     int32_t profile_phases;  /* 1: record device time of each phase into sv_stats.ms_phase */
     int32_t fmm_type;        /* sv_fmm_type */
-    int32_t reserved[5];
+    float fmm_root_scale;    /* FMM root cube side = this x the smallest power of two >= the
+                                plume's extent, rounded down to a multiple of 1/8 in [1, 2)
+                                (0: 1): leaf boxes between two octree levels' sizes, so the
+                                box side can follow the plume (sv_fmm_tune picks it) */
+    int32_t reserved[4];
 } sv_params;
 
 /* Per-call statistics of the last force evaluation. */
@@ -424,6 +428,14 @@ SV_API sv_status sv_upload_batch(sv_ctx *ctx, int32_t nplumes, const int64_t *co
  * not null, in that text file (read first, appended to).  best_ms (nullable)
  * receives the tuned force-evaluation time. */
 SV_API sv_status sv_batch_tune(sv_ctx *ctx, const char *cache_path, double *best_ms);
+/* Autotuner of a single-plume FMM context, after the reference's timing-driven
+ * choice of the FMM's level (MultipoleMethodForceCalculation::setOptimumLevel,
+ * multipole_method_force_calculation.cpp:835-881; Integrator::compareAcceleration
+ * raising maxLevel from measured times, integration_schemes.cpp:470-570): times
+ * force evaluations of the uploaded state at fmm_root_scale = 1, 1.125, ...,
+ * 1.875 and keeps the fastest in the context's parameters (sv_get_params
+ * shows it).  best_ms (nullable) receives its force-evaluation time. */
+SV_API sv_status sv_fmm_tune(sv_ctx *ctx, double *best_ms);
 /* Sets the two tuned quantities directly (M2L weight >= 1, direct sources
  * per work item >= 256) and re-plans the batch. */
 SV_API sv_status sv_batch_set_tuning(sv_ctx *ctx, int32_t m2l_weight, int32_t direct_chunk);

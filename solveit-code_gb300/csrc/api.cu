@@ -313,6 +313,8 @@ sv_status check_params(sv_ctx *c, const sv_params *p) {
         return set_error(c, SV_ERR_INVALID, "fmm_leaf_target outside 1..4096");
     if (p->fmm_type < SV_FMM_FMM || p->fmm_type > SV_FMM_TREECODE_OUTLIERS)
         return set_error(c, SV_ERR_INVALID, "unknown fmm_type %d", p->fmm_type);
+    if (!(p->fmm_root_scale == 0.0f || (p->fmm_root_scale >= 1.0f && p->fmm_root_scale < 2.0f)))
+        return set_error(c, SV_ERR_INVALID, "fmm_root_scale must be 0 or in [1, 2)");
     if (p->symmetry == SV_SYM_TRANSLATIONAL) {
         if (p->sym_levels < 0 || p->sym_levels > 4) return set_error(c, SV_ERR_INVALID, "sym_levels outside 0..4");
         for (int d = 0; d < 3; d++)
@@ -800,6 +802,35 @@ sv_status sv_energy(sv_ctx *c, double *ke, double *pe) {
         return SV_OK;
     }
     return energy(c, ke, pe);
+}
+
+sv_status sv_fmm_tune(sv_ctx *c, double *best_ms) {
+    if (!c) return SV_ERR_INVALID;
+    if (!c->have_state) return set_error(c, SV_ERR_STATE, "no state uploaded");
+    if (c->batch) return set_error(c, SV_ERR_UNSUPPORTED, "batches tune with sv_batch_tune");
+    if (c->P.method != SV_METHOD_FMM) return set_error(c, SV_ERR_UNSUPPORTED, "sv_fmm_tune tunes the FMM");
+    SV_CK(c, cudaSetDevice(c->device));
+    float best_scale = 1.0f;
+    double best = 1e300;
+    for (int k = 0; k < 8; k++) {
+        c->P.fmm_root_scale = 1.0f + 0.125f * (float)k;
+        double t = 1e300;
+        for (int r = 0; r < 3; r++) {  // the first evaluation warms the scale's buffers
+            SV_TRY(compute_accel_device(c, 0, c->n));
+            SV_CK(c, cudaEventSynchronize(c->ev_end));
+            float ms = 0.f;
+            SV_CK(c, cudaEventElapsedTime(&ms, c->ev_begin, c->ev_end));
+            if (r > 0) t = std::min(t, (double)ms);
+        }
+        if (t < best) {
+            best = t;
+            best_scale = c->P.fmm_root_scale;
+        }
+    }
+    c->P.fmm_root_scale = best_scale;
+    SV_TRY(compute_accel_device(c, 0, c->n));  // the last acceleration and statistics at the kept scale
+    if (best_ms) *best_ms = best;
+    return SV_OK;
 }
 
 sv_status sv_compare_accel(sv_ctx *c, const double *ref3, double *l2, double *maxl2, int64_t *argmax) {

@@ -9,6 +9,7 @@
 #include <cub/device/device_radix_sort.cuh>
 
 #include <algorithm>
+#include <cmath>
 
 #include "sv_internal.cuh"
 
@@ -59,11 +60,12 @@ __global__ void bbox_partial(const double *__restrict__ x, const double *__restr
 }
 
 // Final reduction (kRedThreads threads over the block partials); root =
-// origin (bbox min), cube side S = smallest power of two >= the largest
-// extent (so every box side and every box-centre offset S/2^l * k is exact in
-// binary floating point), bbox max, empty flag, and 2^21 / S for the keys.
+// origin (bbox min), cube side S = scale x the smallest power of two > the
+// largest extent, with scale a multiple of 1/8 in [1, 2) (so every box side
+// and every box-centre offset S/2^l * k, |k| < 8, is exact in binary floating
+// point, FP32 included), bbox max, empty flag, and 2^21 / S for the keys.
 __global__ void __launch_bounds__(kRedThreads) bbox_final(const double *__restrict__ part, int nblocks,
-                                                          double *__restrict__ root) {
+                                                          double *__restrict__ root, double scale) {
     __shared__ double sh[6];
     __shared__ double wsh[6][kRedThreads / 32];
     double v[6] = {1e300, 1e300, 1e300, -1e300, -1e300, -1e300};
@@ -98,7 +100,7 @@ __global__ void __launch_bounds__(kRedThreads) bbox_final(const double *__restri
         if (ext > 0.0) {
             int e;
             frexp(ext, &e);            // ext = f * 2^e, f in [0.5, 1)
-            S = ldexp(1.0, e);         // 2^e > ext
+            S = ldexp(1.0, e) * scale; // >= 2^e > ext
         } else {
             S = 1e-12;
         }
@@ -225,6 +227,13 @@ sv_status ensure_sorted_capacity(sv_ctx *c, int64_t n) {
     return SV_OK;
 }
 
+// the FMM's root scale rounded down to a multiple of 1/8 (1 for the other methods)
+static double root_scale(const sv_ctx *c) {
+    const double s = c->P.fmm_root_scale;
+    if (c->P.method != SV_METHOD_FMM || !(s >= 1.0)) return 1.0;
+    return std::floor(std::min(s, 1.875) * 8.0) / 8.0;
+}
+
 sv_status sort_view(sv_ctx *c, const ParticleView &v, int64_t first, int64_t last) {
     const int64_t n = v.n;
     SV_TRY(ensure_sorted_capacity(c, n));
@@ -234,7 +243,7 @@ sv_status sort_view(sv_ctx *c, const ParticleView &v, int64_t first, int64_t las
     const int nb = div_up(n, 256);
     bbox_partial<<<S.red_blocks, kRedThreads, 0, c->stream>>>(v.x, v.y, v.z, v.status, n, S.red);
     SV_LAUNCHED(c);
-    bbox_final<<<1, kRedThreads, 0, c->stream>>>(S.red, S.red_blocks, S.root);
+    bbox_final<<<1, kRedThreads, 0, c->stream>>>(S.red, S.red_blocks, S.root, root_scale(c));
     SV_LAUNCHED(c);
     morton_keys<<<nb, 256, 0, c->stream>>>(v.x, v.y, v.z, v.status, n, S.root, S.keys, S.idx);
     SV_LAUNCHED(c);

@@ -36,7 +36,7 @@ ABI_SYMBOLS = (
     "sv_direct_accel_noalloc", "sv_upload_batch", "sv_batch_tune", "sv_batch_get_info", "sv_batch_set_tuning",
     "sv_get_outliers", "sv_set_boundary", "sv_get_boundary", "sv_get_events", "sv_set_emitter_field",
     "sv_emitter_field_at", "sv_set_substeps", "sv_get_substep_levels", "sv_snapshot", "sv_set_energy",
-    "sv_get_energy_records",
+    "sv_get_energy_records", "sv_fmm_tune",
 )
 
 # sv_energy_record: the energy file's record (J)
@@ -51,7 +51,8 @@ class Params(C.Structure):
         ("symmetry", C.c_int32), ("theta", C.c_float), ("leaf_size", C.c_int32),
         ("fmm_order", C.c_int32), ("fmm_ws", C.c_int32), ("fmm_leaf_target", C.c_int32),
         ("sym_axes", C.c_int32 * 3), ("sym_levels", C.c_int32), ("domain_size", C.c_double * 3),
-        ("device", C.c_int32), ("profile_phases", C.c_int32), ("fmm_type", C.c_int32), ("reserved", C.c_int32 * 5),
+        ("device", C.c_int32), ("profile_phases", C.c_int32), ("fmm_type", C.c_int32),
+        ("fmm_root_scale", C.c_float), ("reserved", C.c_int32 * 4),
     ]
 
 
@@ -154,6 +155,7 @@ def load(path: str = LIB_PATH):
     L.sv_snapshot.argtypes = [vp, C.c_int32, C.c_int64, C.c_int64, C.c_float, vp, C.c_int64, C.POINTER(C.c_int64)]
     L.sv_get_substep_levels.argtypes = [vp, vp]
     L.sv_set_energy.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
+    L.sv_fmm_tune.argtypes = [vp, C.POINTER(C.c_double)]
     L.sv_get_energy_records.argtypes = [vp, vp, C.c_int64, C.POINTER(C.c_int64)]
     for name in ABI_SYMBOLS:
         if name not in ("sv_destroy", "sv_stream", "sv_launch_count", "sv_last_error", "sv_abi_version"):
@@ -336,6 +338,14 @@ class ForceMethod:
         out = np.zeros(self.n, np.int8)
         self._check(self.L.sv_get_substep_levels(self.h, _p(out)))
         return out
+
+    def fmm_tune(self):
+        """sv_fmm_tune: returns (root scale kept, its force-evaluation ms)."""
+        ms = C.c_double()
+        self._check(self.L.sv_fmm_tune(self.h, C.byref(ms)))
+        p = Params()
+        self._check(self.L.sv_get_params(self.h, C.byref(p)))
+        return p.fmm_root_scale, ms.value
 
     def set_energy(self, init_steps, steps, interval, enable=True):
         """Integrator::toggleEnergy: records every `interval` steps of leapfrog()."""

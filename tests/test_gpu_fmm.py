@@ -162,3 +162,32 @@ def test_fmm_forest_mixed_charges():
         ref = O.direct_f64(s, EPS20)
         assert rel_l2(a[o:o + k], ref, s["status"]) < 1e-5
         o += k
+
+
+@pytest.mark.parametrize("scale", [1.125, 1.5, 1.875])
+def test_fmm_root_scale_keeps_accuracy(scale):
+    """Root cubes scaled between two powers of two (leaf boxes between two
+    octree levels' sizes) keep the ws 2, p 8 accuracy."""
+    st = plume.make_plume(65536, 10e-6, 33)
+    tg = np.arange(0, 65536, 32)
+    ref = O.direct_f64(st, EPS20, targets=tg)
+    a, s = run_accel(st, softening2=EPS20, method=sv.FMM, fmm_order=8, fmm_ws=2, fmm_root_scale=scale)
+    assert rel_l2(a[tg], ref, st["status"][tg]) < 1e-5
+
+
+def test_fmm_tune_keeps_a_scale():
+    st = plume.make_plume(65536, 10e-6, 34)
+    with sv.ForceMethod(softening2=EPS20, method=sv.FMM, fmm_order=8, fmm_ws=2) as fm:
+        fm.upload(st)
+        scale, ms = fm.fmm_tune()
+        assert scale in [1 + k / 8 for k in range(8)] and ms > 0
+        a = fm.accel()
+    tg = np.arange(0, 65536, 64)
+    ref = O.direct_f64(st, EPS20, targets=tg)
+    assert rel_l2(a[tg], ref, st["status"][tg]) < 1e-5
+    with sv.ForceMethod(softening2=EPS20, method=sv.DIRECT) as fm:
+        fm.upload(st)
+        with pytest.raises(sv.SolveitError):
+            fm.fmm_tune()
+    with pytest.raises(sv.SolveitError):
+        sv.ForceMethod(softening2=EPS20, method=sv.FMM, fmm_root_scale=2.5)
