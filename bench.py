@@ -491,7 +491,10 @@ def run_ours(args, wl, rank, world, local):
     fm = sv.ForceMethod(softening2=EPS2, efield=(0.0, 0.0, EZ), device=local, profile_phases=1, **kw)
     fm.upload(st)
     root_scale, tune_ms = None, None
-    if wl["method"] == "fmm" and not args.no_tune:
+    if wl["method"] == "fmm" and args.root_scale is not None:
+        fm.set_params(fmm_root_scale=args.root_scale)
+        root_scale = args.root_scale
+    elif wl["method"] == "fmm" and not args.no_tune:
         # untimed set-up: the root cube's scale (leaf box size) for this plume
         root_scale, tune_ms = fm.fmm_tune()
     stream = torch.cuda.ExternalStream(fm.stream, device=local)
@@ -587,7 +590,7 @@ def run_ours(args, wl, rank, world, local):
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                        "l2": "512 MB written between timed steps (L2 flush)", "leaf_level": stats.levels,
                        "leaf_boxes": stats.boxes, "fmm_root_scale": root_scale,
-                       "tuning": None if root_scale is None else
+                       "tuning": None if tune_ms is None else
                        f"sv_fmm_tune before the warm-up (untimed): root scales 1..1.875, kept {root_scale} "
                        f"({tune_ms:.3f} ms per force evaluation)"},
             "clocks": clocks, "e2e": e2e, "gpu_launches": int(launches // max(1, args.steps)) * args.steps,
@@ -680,6 +683,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="fmm_n1m", choices=sorted(WORKLOADS))
+    ap.add_argument("--root-scale", type=float, default=None,
+                    help="FMM: this root-cube scale instead of sv_fmm_tune's (profiling a fixed configuration)")
     ap.add_argument("--timed-only", action="store_true",
                     help="only the device-resident timed steps (for profiler launch lists)")
     ap.add_argument("--no-tune", action="store_true",

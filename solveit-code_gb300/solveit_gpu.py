@@ -343,9 +343,8 @@ class ForceMethod:
         """sv_fmm_tune: returns (root scale kept, its force-evaluation ms)."""
         ms = C.c_double()
         self._check(self.L.sv_fmm_tune(self.h, C.byref(ms)))
-        p = Params()
-        self._check(self.L.sv_get_params(self.h, C.byref(p)))
-        return p.fmm_root_scale, ms.value
+        self._check(self.L.sv_get_params(self.h, C.byref(self.params)))  # the kept scale
+        return self.params.fmm_root_scale, ms.value
 
     def set_energy(self, init_steps, steps, interval, enable=True):
         """Integrator::toggleEnergy: records every `interval` steps of leapfrog()."""
