@@ -425,7 +425,7 @@ direct_batch_kernel(const DirectItem *__restrict__ items, int nitems, int *__res
                         const float dx = tx[k] - v.x, dy = ty[k] - v.y, dz = tz[k] - v.z;
                         float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
                         r2 = fmaxf(r2, kMinR2);
-                        const float inv = rsqrtf(r2);
+                        const float inv = rsqrt_ftz(r2);
                         const float wq = v.w * inv * inv * inv;
                         fx[k] = fmaf(dx, wq, fx[k]);
                         fy[k] = fmaf(dy, wq, fy[k]);

@@ -111,7 +111,7 @@ direct_mixed_kernel(const double *__restrict__ xs, const double *__restrict__ ys
                     const float dx = tx[k] - v.x, dy = ty[k] - v.y, dz = tz[k] - v.z;
                     float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
                     r2 = fmaxf(r2, kMinR2);  // self pair with eps = 0: d = 0 -> 0 * finite
-                    const float inv = rsqrtf(r2);
+                    const float inv = rsqrt_ftz(r2);
                     const float w = v.w * inv * inv * inv;
                     fx[k] = fmaf(dx, w, fx[k]);
                     fy[k] = fmaf(dy, w, fy[k]);

@@ -156,7 +156,7 @@ potential_kernel(const int *__restrict__ list, const int *__restrict__ cnt, cons
             const float dz = (th.z - a.z) + (tl.z - b.z);
             const float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
             const float w = __float_as_int(b.w) == i ? 0.f : a.w;
-            part = fmaf(w, rsqrtf(fmaxf(r2, kMinR2)), part);
+            part = fmaf(w, rsqrt_ftz(fmaxf(r2, kMinR2)), part);
         }
         kahan(s, c, part);
     }

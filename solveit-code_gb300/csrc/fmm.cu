@@ -1052,7 +1052,7 @@ p2p_body(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, co
                     const float dx = ta.x - u.x, dy = ta.y - u.y, dz = ta.z - u.z;
                     float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
                     if (CLAMP) r2 = fmaxf(r2, kMinR2);
-                    const float inv = rsqrtf(r2);
+                    const float inv = rsqrt_ftz(r2);
                     const float w = UQ ? inv * inv * inv : u.w * inv * inv * inv;
                     fax = fmaf(dx, w, fax);
                     fay = fmaf(dy, w, fay);
@@ -1062,7 +1062,7 @@ p2p_body(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, co
                     const float dx = tbv.x - u.x, dy = tbv.y - u.y, dz = tbv.z - u.z;
                     float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
                     if (CLAMP) r2 = fmaxf(r2, kMinR2);
-                    const float inv = rsqrtf(r2);
+                    const float inv = rsqrt_ftz(r2);
                     const float w = UQ ? inv * inv * inv : u.w * inv * inv * inv;
                     fbx = fmaf(dx, w, fbx);
                     fby = fmaf(dy, w, fby);
@@ -1127,7 +1127,7 @@ p2p_body(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, co
                     const float dx = tx - u.x, dy = ty - u.y, dz = tz - u.z;
                     float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
                     if (CLAMP) r2 = fmaxf(r2, kMinR2);
-                    const float inv = rsqrtf(r2);
+                    const float inv = rsqrt_ftz(r2);
                     const float w = UQ ? inv * inv * inv : u.w * inv * inv * inv;
                     fx = fmaf(dx, w, fx);
                     fy = fmaf(dy, w, fy);
@@ -1140,7 +1140,7 @@ p2p_body(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, co
                     const float dx = tx - u.x, dy = ty - u.y, dz = tz - u.z;
                     float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
                     if (CLAMP) r2 = fmaxf(r2, kMinR2);
-                    const float inv = rsqrtf(r2);
+                    const float inv = rsqrt_ftz(r2);
                     const float w = UQ ? inv * inv * inv : u.w * inv * inv * inv;
                     fx = fmaf(dx, w, fx);
                     fy = fmaf(dy, w, fy);

@@ -193,6 +193,16 @@ sv_status cuda_error(sv_ctx *c, cudaError_t e, const char *what, const char *fil
         if (_s != SV_OK) return _s;                                         \
     } while (0)
 
+// 1/sqrt(x) by the special-function unit's approximation with denormal
+// inputs and results flushed to zero: one instruction, where rsqrtf (built
+// without -ftz) adds a range test and rescaling for denormal inputs.  The
+// pair kernels' r^2 + eps^2 is never below kMinR2 (a normal float).
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 // 32-byte aligned quadruple of doubles (one shared-memory source record)
 struct alignas(32) dbl4_t {
     double x, y, z, w;
