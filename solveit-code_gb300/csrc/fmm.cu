@@ -958,7 +958,11 @@ __device__ __forceinline__ void kahan_add(float &s, float &e, float v) {
 // without per-box padding or per-box overhead.  CLAMP: floor r^2 at kMinR2,
 // needed only when eps^2 < kMinR2 (a zero-distance pair without softening).  Targets: one per lane; a
 // chunk of nt < 32 targets gives each target a group of g lanes (a power of
-// two, nt * g <= 32) that split the staged sources.  Each 32-source chunk's
+// two, nt * g <= 32) that split the staged sources.  Sources are staged as
+// negated coordinates in structure-of-arrays rows, so one 64-bit load gives
+// two consecutive sources and each pair operation is a packed FP32x2
+// instruction (FADD2 / FFMA2 / FMUL2) over two sources; the reciprocal square
+// roots stay scalar.  Each 32-source chunk's
 // FP32 partial sum is added with Kahan compensation.  The result is stored
 // (each particle of a box with targets once; boxes without targets are left
 // as they are).  UQ: every particle of
@@ -969,16 +973,36 @@ __device__ __forceinline__ void kahan_add(float &s, float &e, float v) {
 template <int WS>
 constexpr int p2p_nsp() { return ((2 * WS + 1) * (2 * WS + 1) * (2 * WS + 1) + 31) / 32 * 32; }
 
+// Two consecutive staged sources (negated coordinates X, Y, Z, charges Q)
+// against one target (T*, both halves the same), packed FP32x2: d = t + (-s),
+// r^-3 per half, partial sums of the even and odd sources in g*.
+template <bool CLAMP, bool UQ>
+__device__ __forceinline__ void pair2(float2 X, float2 Y, float2 Z, float2 Q, float2 TX, float2 TY, float2 TZ,
+                                      float2 E2, float2 &gx, float2 &gy, float2 &gz) {
+    const float2 dx = __fadd2_rn(TX, X), dy = __fadd2_rn(TY, Y), dz = __fadd2_rn(TZ, Z);
+    float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, E2)));
+    if (CLAMP) r2 = make_float2(fmaxf(r2.x, kMinR2), fmaxf(r2.y, kMinR2));
+    const float2 inv = make_float2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
+    float2 w = __fmul2_rn(__fmul2_rn(inv, inv), inv);
+    if (!UQ) w = __fmul2_rn(Q, w);
+    gx = __ffma2_rn(dx, w, gx);
+    gy = __ffma2_rn(dy, w, gy);
+    gz = __ffma2_rn(dz, w, gz);
+}
+
+__device__ __forceinline__ float2 ld2(const float *p, int k) { return *reinterpret_cast<const float2 *>(p + k); }
+
 template <int WS, bool CLAMP, bool UQ>
 __device__ __forceinline__ void
 p2p_body(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, const int *__restrict__ start,
          const int4 *__restrict__ coord, const int *__restrict__ nbr, const double *__restrict__ qm,
          const double *__restrict__ roots, int level, float eps2, double *__restrict__ ax, double *__restrict__ ay,
          double *__restrict__ az, unsigned long long *__restrict__ counts, const int *__restrict__ has_tgt,
-         const float4 *__restrict__ rel, float4 (*src)[32], int2 (*nb_rng)[p2p_nsp<WS>()],
+         const float4 *__restrict__ rel, float (*st)[4][32], int2 (*nb_rng)[p2p_nsp<WS>()],
          float4 (*nb_off)[p2p_nsp<WS>()]) {
     constexpr int NS1 = 2 * WS + 1, NS = NS1 * NS1 * NS1;
     const float4 pad = UQ ? make_float4(1e18f, 0.f, 0.f, 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float2 E2 = make_float2(eps2, eps2);
     unsigned long long pairs = 0;
     const unsigned lt_mask = (1u << (threadIdx.x & 31)) - 1u;
     SV_WARP_BOXES(kWarps) {
@@ -1026,6 +1050,8 @@ p2p_body(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, co
         const bool vb = ib < t1;
         const float4 ta = rel[ia], tbv = rel[vb ? ib : ia];
         if (lane == 0) pairs += (unsigned long long)total * (unsigned long long)min(64, t1 - tb);
+        const float2 AX = make_float2(ta.x, ta.x), AY = make_float2(ta.y, ta.y), AZ = make_float2(ta.z, ta.z);
+        const float2 BX = make_float2(tbv.x, tbv.x), BY = make_float2(tbv.y, tbv.y), BZ = make_float2(tbv.z, tbv.z);
         float sax = 0.f, say = 0.f, saz = 0.f, eax = 0.f, eay = 0.f, eaz = 0.f;
         float sbx = 0.f, sby = 0.f, sbz = 0.f, ebx = 0.f, eby = 0.f, ebz = 0.f;
         int kb = 0, kbeg = 0;
@@ -1042,33 +1068,21 @@ p2p_body(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, co
                 const float4 o = nb_off[wid][kb];
                 v = make_float4(r.x + o.x, r.y + o.y, r.z + o.z, r.w);
             }
-            src[wid][lane] = v;
+            st[wid][0][lane] = -v.x;
+            st[wid][1][lane] = -v.y;
+            st[wid][2][lane] = -v.z;
+            if (!UQ) st[wid][3][lane] = v.w;
             __syncwarp();
-            float fax = 0.f, fay = 0.f, faz = 0.f, fbx = 0.f, fby = 0.f, fbz = 0.f;
-#pragma unroll 8
-            for (int k = 0; k < 32; k++) {
-                const float4 u = src[wid][k];
-                {
-                    const float dx = ta.x - u.x, dy = ta.y - u.y, dz = ta.z - u.z;
-                    float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-                    if (CLAMP) r2 = fmaxf(r2, kMinR2);
-                    const float inv = rsqrt_ftz(r2);
-                    const float w = UQ ? inv * inv * inv : u.w * inv * inv * inv;
-                    fax = fmaf(dx, w, fax);
-                    fay = fmaf(dy, w, fay);
-                    faz = fmaf(dz, w, faz);
-                }
-                {
-                    const float dx = tbv.x - u.x, dy = tbv.y - u.y, dz = tbv.z - u.z;
-                    float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-                    if (CLAMP) r2 = fmaxf(r2, kMinR2);
-                    const float inv = rsqrt_ftz(r2);
-                    const float w = UQ ? inv * inv * inv : u.w * inv * inv * inv;
-                    fbx = fmaf(dx, w, fbx);
-                    fby = fmaf(dy, w, fby);
-                    fbz = fmaf(dz, w, fbz);
-                }
+            float2 gax = make_float2(0.f, 0.f), gay = gax, gaz = gax, gbx = gax, gby = gax, gbz = gax;
+#pragma unroll 4
+            for (int k = 0; k < 32; k += 2) {
+                const float2 X = ld2(st[wid][0], k), Y = ld2(st[wid][1], k), Z = ld2(st[wid][2], k);
+                const float2 Q = UQ ? make_float2(1.f, 1.f) : ld2(st[wid][3], k);
+                pair2<CLAMP, UQ>(X, Y, Z, Q, AX, AY, AZ, E2, gax, gay, gaz);
+                pair2<CLAMP, UQ>(X, Y, Z, Q, BX, BY, BZ, E2, gbx, gby, gbz);
             }
+            const float fax = gax.x + gax.y, fay = gay.x + gay.y, faz = gaz.x + gaz.y;
+            const float fbx = gbx.x + gbx.y, fby = gby.x + gby.y, fbz = gbz.x + gbz.y;
             __syncwarp();
             kahan_add(sax, eax, fax);
             kahan_add(say, eay, fay);
@@ -1099,7 +1113,7 @@ p2p_body(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, co
         const bool valid = tloc < nt;
         const int i = tb + (valid ? tloc : 0);
         const float4 ti = rel[i];
-        const float tx = ti.x, ty = ti.y, tz = ti.z;
+        const float2 TX = make_float2(ti.x, ti.x), TY = make_float2(ti.y, ti.y), TZ = make_float2(ti.z, ti.z);
         if (lane == 0) pairs += (unsigned long long)total * (unsigned long long)nt;
         float sx = 0.f, sy = 0.f, sz = 0.f, ex = 0.f, ey = 0.f, ez = 0.f;
         int kb = 0, kbeg = 0;  // this lane's current source box and its first running index
@@ -1116,37 +1130,21 @@ p2p_body(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, co
                 const float4 o = nb_off[wid][kb];
                 v = make_float4(r.x + o.x, r.y + o.y, r.z + o.z, r.w);
             }
-            src[wid][lane] = v;
+            st[wid][0][lane] = -v.x;
+            st[wid][1][lane] = -v.y;
+            st[wid][2][lane] = -v.z;
+            if (!UQ) st[wid][3][lane] = v.w;
             __syncwarp();
-            float fx = 0.f, fy = 0.f, fz = 0.f;
-            if (g == 1) {
-                // every lane a target, all 32 staged sources (padding adds nothing)
-#pragma unroll 8
-                for (int k = 0; k < 32; k++) {
-                    const float4 u = src[wid][k];
-                    const float dx = tx - u.x, dy = ty - u.y, dz = tz - u.z;
-                    float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-                    if (CLAMP) r2 = fmaxf(r2, kMinR2);
-                    const float inv = rsqrt_ftz(r2);
-                    const float w = UQ ? inv * inv * inv : u.w * inv * inv * inv;
-                    fx = fmaf(dx, w, fx);
-                    fy = fmaf(dy, w, fy);
-                    fz = fmaf(dz, w, fz);
-                }
-            } else {
+            // g lanes per target, each taking pairs of consecutive sources 2 sub + 2 g i
+            // (g = 1: every lane a target and all 32 staged sources; padding adds nothing)
+            float2 gx = make_float2(0.f, 0.f), gy = gx, gz = gx;
 #pragma unroll 4
-                for (int k = sub; k < 32; k += g) {
-                    const float4 u = src[wid][k];
-                    const float dx = tx - u.x, dy = ty - u.y, dz = tz - u.z;
-                    float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-                    if (CLAMP) r2 = fmaxf(r2, kMinR2);
-                    const float inv = rsqrt_ftz(r2);
-                    const float w = UQ ? inv * inv * inv : u.w * inv * inv * inv;
-                    fx = fmaf(dx, w, fx);
-                    fy = fmaf(dy, w, fy);
-                    fz = fmaf(dz, w, fz);
-                }
+            for (int k = 2 * sub; k < 32; k += 2 * g) {
+                const float2 X = ld2(st[wid][0], k), Y = ld2(st[wid][1], k), Z = ld2(st[wid][2], k);
+                const float2 Q = UQ ? make_float2(1.f, 1.f) : ld2(st[wid][3], k);
+                pair2<CLAMP, UQ>(X, Y, Z, Q, TX, TY, TZ, E2, gx, gy, gz);
             }
+            const float fx = gx.x + gx.y, fy = gy.x + gy.y, fz = gz.x + gz.y;
             __syncwarp();
             float y = fx - ex, t = sx + y;
             ex = (t - sx) - y;
@@ -1183,13 +1181,13 @@ p2p_body(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, co
 
 // counts[2] != 0: box_relative_kernel met two different charges
 template <int WS, bool CLAMP>
-__global__ void __launch_bounds__(kWarps * 32, 8)
+__global__ void __launch_bounds__(kWarps * 32, 6)
 p2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, const int *__restrict__ start,
            const int4 *__restrict__ coord, const int *__restrict__ nbr, const double *__restrict__ qm,
            const double *__restrict__ roots, int level, float eps2, double *__restrict__ ax, double *__restrict__ ay,
            double *__restrict__ az, unsigned long long *__restrict__ counts, const int *__restrict__ has_tgt,
            const float4 *__restrict__ rel) {
-    __shared__ float4 src[kWarps][32];
+    __shared__ __align__(16) float src[kWarps][4][32];  // staged sources: -x, -y, -z, charge
     __shared__ int2 nb_rng[kWarps][p2p_nsp<WS>()];    // (first source, running source count at the box's end)
     __shared__ float4 nb_off[kWarps][p2p_nsp<WS>()];  // source box centre - target box centre (exact in FP32)
     if (counts[2] == 0)
