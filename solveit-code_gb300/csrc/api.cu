@@ -423,7 +423,11 @@ sv_status sv_create(const sv_params *p, sv_ctx **out) {
     c->P = *p;
     c->device = p->device;
     cudaError_t e = cudaSetDevice(c->device);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    // the context's stream at the highest priority: the FMM's second stream
+    // (the near field, which fills every SM) yields to it as its blocks retire
+    int prio_lo = 0, prio_hi = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, prio_hi);
     if (e == cudaSuccess) e = cudaMalloc(&c->d_scalar, 64 * sizeof(double));
     if (e == cudaSuccess) e = cudaMallocHost(&c->h_scalar, 64 * sizeof(double));
     if (e == cudaSuccess) e = cudaEventCreate(&c->ev_begin);

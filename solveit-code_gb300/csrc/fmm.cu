@@ -79,6 +79,7 @@ struct Fmm {
     // the near field runs on its own stream beside the upward and downward passes
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_lists = nullptr, ev_join = nullptr, ev_near[2] = {};
+    cudaEvent_t ev_m2l_lists = nullptr;  // single plume: interaction lists built (second stream)
 };
 
 namespace {
@@ -137,22 +138,22 @@ __device__ __forceinline__ const double *box_root(const double *root, const int 
     for (int b = blockIdx.x * (W) + wid; b < nb_; b += gridDim.x * (W))
 
 // ---------------------------------------------------------------- lists --
+// Lists of one box b (coordinates cb, parent par) from its parent's near list
+// pnbr: the children of each of the parent's near boxes are classified round
+// by round (lanes take the parent's near slots) into the near list (|offset|
+// <= WS, written when write_near) and the interaction list (M2L entries
+// compacted by ballot).  Returns the box's M2L count.
 template <int WS>
-__global__ void __launch_bounds__(kWarps * 32)
-build_lists_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ parent,
-                   const int4 *__restrict__ coord, const int *__restrict__ pnbr, const int *__restrict__ pchild0,
-                   int *__restrict__ nbr, int2 *__restrict__ m2l, int *__restrict__ m2l_cnt, int cap,
-                   unsigned long long *__restrict__ counts) {
-    // one warp per box: lanes take the parent's near slots; the children of
-    // each are classified round by round, M2L entries compacted by ballot
+__device__ __forceinline__ int build_lists_box(int b, int4 cb, int par, const int4 *__restrict__ coord,
+                                               const int *__restrict__ pnbr, const int *__restrict__ pchild0,
+                                               int *__restrict__ nbr, int2 *__restrict__ m2l,
+                                               int *__restrict__ m2l_cnt, int cap, int write_near) {
     constexpr int NS1 = 2 * WS + 1, NS = NS1 * NS1 * NS1, R = 2 * WS + 1, SIDE = 2 * R + 1;
-    unsigned long long tot = 0;
-    const unsigned lt_mask = (1u << (threadIdx.x & 31)) - 1u;
-    SV_WARP_BOXES(kWarps) {
-    for (int s = lane; s < NS; s += 32) nbr[b * NS + s] = -1;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    if (write_near)
+        for (int s = lane; s < NS; s += 32) nbr[b * NS + s] = -1;
     __syncwarp();
-    const int4 cb = coord[b];
-    const int par = parent[b];
     int cnt = 0;
     for (int s0 = 0; s0 < NS; s0 += 32) {
         const int s = s0 + lane;
@@ -176,7 +177,7 @@ build_lists_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict_
                 // its capacity may not, and its result is discarded, but the class
                 // index must stay inside the tables
                 if (am <= WS) {
-                    nbr[b * NS + ((ox + WS) * NS1 + (oy + WS)) * NS1 + (oz + WS)] = ch;
+                    if (write_near) nbr[b * NS + ((ox + WS) * NS1 + (oy + WS)) * NS1 + (oz + WS)] = ch;
                 } else if (am <= R) {
                     far = true;
                     cls = ((ox + R) * SIDE + (oy + R)) * SIDE + (oz + R);
@@ -192,12 +193,114 @@ build_lists_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict_
         }
     }
     if (cnt > cap) cnt = cap;
-    if (lane == 0) {
-        m2l_cnt[b] = cnt;
-        tot += cnt;
-    }
+    if (lane == 0) m2l_cnt[b] = cnt;
+    return cnt;
+}
+
+// One level of a forest, one warp per box.
+template <int WS>
+__global__ void __launch_bounds__(kWarps * 32)
+build_lists_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ parent,
+                   const int4 *__restrict__ coord, const int *__restrict__ pnbr, const int *__restrict__ pchild0,
+                   int *__restrict__ nbr, int2 *__restrict__ m2l, int *__restrict__ m2l_cnt, int cap,
+                   unsigned long long *__restrict__ counts) {
+    unsigned long long tot = 0;
+    SV_WARP_BOXES(kWarps) {
+    const int cnt = build_lists_box<WS>(b, coord[b], parent[b], coord, pnbr, pchild0, nbr, m2l, m2l_cnt, cap, 1);
+    if (lane == 0) tot += cnt;
     }
     if ((threadIdx.x & 31) == 0 && tot) atomicAdd(&counts[0], tot);
+}
+
+// The levels of one tree for the list builders that take all levels in one
+// launch: level l's boxes are global indices [first, first + nbox).
+struct ListLevel {
+    int nbox, first;
+    const int4 *coord;
+    uint64_t *code;          // box Morton codes at this level (ascending)
+    int *nbr;                // near lists [nbox][NS]
+    const int *parent;       // box -> parent box at level - 1
+    const int *pchild0;      // the parent level's child ranges
+    const int *pnbr;         // the parent level's near lists
+    int2 *m2l;
+    int *m2l_cnt;
+};
+struct ListArgs {
+    int nlev, total;         // levels 0 .. nlev - 1; boxes of all of them
+    ListLevel lv[kMortonBits + 1];
+};
+
+__device__ __forceinline__ int list_level(const ListArgs &a, int g) {
+    int l = 0;
+    while (l + 1 < a.nlev && g >= a.lv[l + 1].first) l++;
+    return l;
+}
+
+__device__ __forceinline__ uint64_t box_code(int x, int y, int z) {
+    return morton_spread3((uint32_t)x) | (morton_spread3((uint32_t)y) << 1) | (morton_spread3((uint32_t)z) << 2);
+}
+
+// Morton code of every box of every level (a level's boxes are in ascending
+// code order)
+__global__ void box_codes_kernel(ListArgs a) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= a.total) return;
+    const ListLevel &L = a.lv[list_level(a, g)];
+    const int b = g - L.first;
+    const int4 c = L.coord[b];
+    L.code[b] = box_code(c.x, c.y, c.z);
+}
+
+// Near lists of every level straight from the boxes (one thread per box and
+// slot): the box at target - offset, found by binary search over the level's
+// codes, or -1; build_lists_box's layout, without a chain of coarser levels in
+// front of it.
+template <int WS>
+__global__ void near_lists_kernel(ListArgs a) {
+    constexpr int NS1 = 2 * WS + 1, NS = NS1 * NS1 * NS1;
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)a.total * NS) return;
+    const int g = (int)(t / NS), s = (int)(t - (int64_t)g * NS);
+    const int l = list_level(a, g);
+    const ListLevel &L = a.lv[l];
+    const int b = g - L.first;
+    const int ox = s / (NS1 * NS1) - WS, oy = (s / NS1) % NS1 - WS, oz = s % NS1 - WS;
+    const int4 cb = L.coord[b];
+    const int x = cb.x - ox, y = cb.y - oy, z = cb.z - oz, side = 1 << l;
+    int found = -1;
+    if (x >= 0 && y >= 0 && z >= 0 && x < side && y < side && z < side) {
+        const uint64_t key = box_code(x, y, z);
+        int lo = 0, hi = L.nbox - 1;
+        while (lo <= hi) {
+            const int mid = (lo + hi) >> 1;
+            const uint64_t cm = L.code[mid];
+            if (cm == key) {
+                found = mid;
+                break;
+            }
+            if (cm < key) lo = mid + 1;
+            else hi = mid - 1;
+        }
+    }
+    L.nbr[(size_t)b * NS + s] = found;
+}
+
+// Interaction lists of levels 1 .. nlev - 1, one warp per box, from the near
+// lists near_lists_kernel wrote
+template <int WS>
+__global__ void __launch_bounds__(kWarps * 32) m2l_lists_kernel(ListArgs a, int cap,
+                                                                unsigned long long *__restrict__ counts) {
+    unsigned long long tot = 0;
+    const int lane = threadIdx.x & 31;
+    const int first = a.nlev > 1 ? a.lv[1].first : a.total;
+    for (int g = first + blockIdx.x * kWarps + (int)(threadIdx.x >> 5); g < a.total; g += gridDim.x * kWarps) {
+        const ListLevel &L = a.lv[list_level(a, g)];
+        const int b = g - L.first;
+        const int cnt = build_lists_box<WS>(b, L.coord[b], L.parent[b], L.coord, L.pnbr, L.pchild0, L.nbr, L.m2l,
+                                            L.m2l_cnt, cap, 0);
+        if (lane == 0) tot += cnt;
+    }
+    if (lane == 0 && tot) atomicAdd(&counts[0], tot);
 }
 
 // Near list of every root: the root itself only (plumes never interact).
@@ -1235,6 +1338,7 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
                  rounded(nb * cap * sizeof(int2)) + rounded(nb * sizeof(int));
         if (chunks[l] > 1) bytes += rounded(nb * chunks[l] * NC * sizeof(float2));
     }
+    for (int l = 0; l <= L; l++) bytes += rounded((size_t)T.lv[l].nbox * sizeof(uint64_t));  // box codes
     if (F.arena_bytes < bytes) {
         cudaFree(F.arena);
         F.arena = nullptr;
@@ -1260,6 +1364,23 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         lst[l] = (int2 *)carve(nb * cap * sizeof(int2));
         cnt[l] = (int *)carve(nb * sizeof(int));
         part[l] = chunks[l] > 1 ? (float2 *)carve(nb * chunks[l] * NC * sizeof(float2)) : Lv[l];
+    }
+    // every level's lists in two launches (near lists, then interaction lists)
+    ListArgs la{};
+    la.nlev = L + 1;
+    for (int l = 0; l <= L; l++) {
+        ListLevel &q = la.lv[l];
+        q.nbox = T.lv[l].nbox;
+        q.first = la.total;
+        la.total += q.nbox;
+        q.coord = T.lv[l].coord;
+        q.code = (uint64_t *)carve((size_t)q.nbox * sizeof(uint64_t));
+        q.nbr = nbr[l];
+        q.parent = T.lv[l].parent;
+        q.pchild0 = l > 0 ? T.lv[l - 1].child0 : nullptr;
+        q.pnbr = l > 0 ? nbr[l - 1] : nullptr;
+        q.m2l = lst[l];
+        q.m2l_cnt = cnt[l];
     }
     phase_mark(c, 2);
     SV_CK(c, cudaMemsetAsync(F.d_counts, 0, 3 * sizeof(unsigned long long), c->stream));
@@ -1290,39 +1411,35 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         F.rel_cap = c->S.n;
     }
     double *fx = F.far, *fy = F.far + F.rel_cap, *fz = F.far + 2 * F.rel_cap;
-    // Two streams from here on.  The second builds the target flags and the
-    // interaction lists, then runs the near field (P2P), which needs only the
-    // sorted particles, the leaf boxes and their near lists, and writes the
-    // accelerations.  The main stream runs the upward pass beside the lists,
-    // waits for them, runs M2L / L2L and the far field (L2P or the treecode's
-    // M2P, into their own arrays) beside the near field, then waits for it;
-    // the scatter to the caller's order adds the two.
+    // Two streams from here on.  The second takes the leaf level's target
+    // flags, then the near and interaction lists of every level in two
+    // launches (boxes found by binary search over each level's Morton codes),
+    // then runs the near field (P2P), which needs only the sorted particles,
+    // the leaf boxes and their near lists, and writes the accelerations.  The
+    // main stream derives the coarser target flags and runs the upward pass,
+    // then M2L / L2L and the far field (L2P or the treecode's M2P, into their
+    // own arrays) beside the near field, then waits for it; the scatter to the
+    // caller's order adds the two.
     SV_CK(c, cudaEventRecord(F.ev_fork, c->stream));
     SV_CK(c, cudaStreamWaitEvent(F.side, F.ev_fork, 0));
-    root_nbr_kernel<<<1, 128, 0, F.side>>>(nbr[0], ns, 1, nullptr);
-    SV_LAUNCHED(c);
-    leaf_targets_kernel<<<div_up(T.lv[L].nbox, 256), 256, 0, F.side>>>(T.lv[L].nbox, nullptr, T.lv[L].start, S.qm,
-                                                                         tgt[L]);
-    SV_LAUNCHED(c);
-    for (int l = L - 1; l >= 0; l--) {
-        parent_targets_kernel<<<div_up(T.lv[l].nbox, 256), 256, 0, F.side>>>(T.lv[l].nbox, nullptr, T.lv[l].child0,
-                                                                              tgt[l + 1], tgt[l]);
-        SV_LAUNCHED(c);
-    }
-    for (int l = 1; l <= L; l++) {
-        const Level &V = T.lv[l];
-        const Level &U = T.lv[l - 1];
-        if (ws == 1)
-            build_lists_kernel<1><<<div_up(V.nbox, kWarps), kWarps * 32, 0, F.side>>>(
-                V.nbox, nullptr, V.parent, V.coord, nbr[l - 1], U.child0, nbr[l], lst[l], cnt[l], cap, F.d_counts);
-        else
-            build_lists_kernel<2><<<div_up(V.nbox, kWarps), kWarps * 32, 0, F.side>>>(
-                V.nbox, nullptr, V.parent, V.coord, nbr[l - 1], U.child0, nbr[l], lst[l], cnt[l], cap, F.d_counts);
-        SV_LAUNCHED(c);
-    }
-    SV_CK(c, cudaEventRecord(F.ev_lists, F.side));
     {
         const Level &V = T.lv[L];
+        leaf_targets_kernel<<<div_up(V.nbox, 256), 256, 0, F.side>>>(V.nbox, nullptr, V.start, S.qm, tgt[L]);
+        SV_LAUNCHED(c);
+        SV_CK(c, cudaEventRecord(F.ev_lists, F.side));
+        box_codes_kernel<<<div_up(la.total, 256), 256, 0, F.side>>>(la);
+        SV_LAUNCHED(c);
+        const int64_t slots = (int64_t)la.total * ns;
+        if (ws == 1) near_lists_kernel<1><<<div_up(slots, 256), 256, 0, F.side>>>(la);
+        else near_lists_kernel<2><<<div_up(slots, 256), 256, 0, F.side>>>(la);
+        SV_LAUNCHED(c);
+        if (L > 0) {
+            const int g = std::min(div_up(la.total - la.lv[1].first, kWarps), 16 * kNumSMs);
+            if (ws == 1) m2l_lists_kernel<1><<<g, kWarps * 32, 0, F.side>>>(la, cap, F.d_counts);
+            else m2l_lists_kernel<2><<<g, kWarps * 32, 0, F.side>>>(la, cap, F.d_counts);
+            SV_LAUNCHED(c);
+        }
+        SV_CK(c, cudaEventRecord(F.ev_m2l_lists, F.side));
         box_relative_kernel<<<div_up(V.nbox, kWarps), kWarps * 32, 0, F.side>>>(
             V.nbox, nullptr, nullptr, V.start, V.coord, S.x, S.y, S.z, S.q, S.root, L, F.rel, F.d_counts + 2);
         SV_LAUNCHED(c);
@@ -1336,6 +1453,13 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
             c->near_ev[1] = F.ev_near[1];
         }
         SV_CK(c, cudaEventRecord(F.ev_join, F.side));
+    }
+    // coarser target flags from the leaf flags
+    SV_CK(c, cudaStreamWaitEvent(c->stream, F.ev_lists, 0));
+    for (int l = L - 1; l >= 0; l--) {
+        parent_targets_kernel<<<div_up(T.lv[l].nbox, 256), 256, 0, c->stream>>>(T.lv[l].nbox, nullptr,
+                                                                                T.lv[l].child0, tgt[l + 1], tgt[l]);
+        SV_LAUNCHED(c);
     }
     phase_mark(c, 3);
     // upward pass
@@ -1351,8 +1475,8 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
             V.nbox, nullptr, V.child0, T.lv[l + 1].coord, Mv[l + 1], Mv[l], F.otab);
         SV_LAUNCHED(c);
     }
+    SV_CK(c, cudaStreamWaitEvent(c->stream, F.ev_m2l_lists, 0));
     phase_mark(c, 4);
-    SV_CK(c, cudaStreamWaitEvent(c->stream, F.ev_lists, 0));
     const bool treecode = c->P.fmm_type == SV_FMM_TREECODE || c->P.fmm_type == SV_FMM_TREECODE_OUTLIERS;
     // downward pass: M2L of all levels in one launch, then L2L level by level
     // (the treecode evaluates multipoles at the particles instead)
@@ -1644,6 +1768,7 @@ void fmm_free(sv_ctx *c) {
     if (F.ev_fork) cudaEventDestroy(F.ev_fork);
     if (F.ev_join) cudaEventDestroy(F.ev_join);
     if (F.ev_lists) cudaEventDestroy(F.ev_lists);
+    if (F.ev_m2l_lists) cudaEventDestroy(F.ev_m2l_lists);
     for (cudaEvent_t e : F.ev_near)
         if (e) cudaEventDestroy(e);
     c->near_ev[0] = c->near_ev[1] = nullptr;
@@ -1661,6 +1786,7 @@ static sv_status fmm_state(sv_ctx *c) {
         SV_CK(c, cudaEventCreateWithFlags(&F.ev_fork, cudaEventDisableTiming));
         SV_CK(c, cudaEventCreateWithFlags(&F.ev_join, cudaEventDisableTiming));
         SV_CK(c, cudaEventCreateWithFlags(&F.ev_lists, cudaEventDisableTiming));
+        SV_CK(c, cudaEventCreateWithFlags(&F.ev_m2l_lists, cudaEventDisableTiming));
         SV_CK(c, cudaEventCreate(&F.ev_near[0]));
         SV_CK(c, cudaEventCreate(&F.ev_near[1]));
     }

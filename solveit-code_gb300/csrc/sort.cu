@@ -116,15 +116,7 @@ __global__ void __launch_bounds__(kRedThreads) bbox_final(const double *__restri
     }
 }
 
-__device__ __forceinline__ uint64_t spread3(uint32_t v) {
-    uint64_t x = v & 0x1fffffull;
-    x = (x | (x << 32)) & 0x1f00000000ffffull;
-    x = (x | (x << 16)) & 0x1f0000ff0000ffull;
-    x = (x | (x << 8)) & 0x100f00f00f00f00full;
-    x = (x | (x << 4)) & 0x10c30c30c30c30c3ull;
-    x = (x | (x << 2)) & 0x1249249249249249ull;
-    return x;
-}
+__device__ __forceinline__ uint64_t spread3(uint32_t v) { return morton_spread3(v); }
 
 __global__ void morton_keys(const double *__restrict__ x, const double *__restrict__ y,
                             const double *__restrict__ z, const int32_t *__restrict__ st,

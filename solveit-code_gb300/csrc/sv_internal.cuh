@@ -203,6 +203,18 @@ __device__ __forceinline__ float rsqrt_ftz(float x) {
     return y;
 }
 
+// the low 21 bits of v spread to every third bit (Morton interleave: x at
+// bit 0, y at bit 1, z at bit 2 of each level's triple)
+__host__ __device__ __forceinline__ uint64_t morton_spread3(uint32_t v) {
+    uint64_t x = v & 0x1fffffull;
+    x = (x | (x << 32)) & 0x1f00000000ffffull;
+    x = (x | (x << 16)) & 0x1f0000ff0000ffull;
+    x = (x | (x << 8)) & 0x100f00f00f00f00full;
+    x = (x | (x << 4)) & 0x10c30c30c30c30c3ull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
+    return x;
+}
+
 // 32-byte aligned quadruple of doubles (one shared-memory source record)
 struct alignas(32) dbl4_t {
     double x, y, z, w;
