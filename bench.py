@@ -43,8 +43,9 @@ import plume  # noqa: E402
 
 METRIC = "particle-steps/s, mixed-prec vs plain FP64 path, same GB300, force err <=1e-5"
 # DRAM bytes (read + write) of one near-field launch of the fmm_n1m workload at
-# leaf level 11, from one ncu capture (profiles/p2p_kernel_fmm_n1m.md)
-P2P_TRAFFIC_BYTES = 53962240 + 430336
+# root scale 1.375 (leaf level 12), from one ncu capture
+# (profiles/p2p_kernel_fmm_n1m.md)
+P2P_TRAFFIC_BYTES = 30337280 + 143360
 EPS2 = 1e-20
 DT = 1e-13
 EZ = 1e8
@@ -616,13 +617,17 @@ def run_ours(args, wl, rank, world, local):
                                 "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                                 "frac": achieved / fp32_peak, "traffic": P2P_TRAFFIC_BYTES,
                                 "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one p2p_kernel "
-                                                  "launch at leaf level 11 (the 15th force evaluation of this "
-                                                  "workload), one ncu capture, profiles/p2p_kernel_fmm_n1m.md",
+                                                  "launch at root scale 1.375 (leaf level 12, the 4th force "
+                                                  "evaluation of this workload), one ncu capture, "
+                                                  "profiles/p2p_kernel_fmm_n1m.md",
+                                "solo": "the same launch alone under ncu: 1.059 ms, 42.5 TFLOP/s, 0.53 of the FP32 "
+                                        "FMA rate (profiles/p2p_kernel_fmm_n1m.md)",
                                 "peak_source": "FP32 FMA rate 152 SMs x 128 lanes x 2 flop x sm_max_mhz of "
                                                "MEASURED_PEAKS.json (no FP32 peak is measured there; the "
                                                "kernel runs on the FP32 pipe, not the tensor cores)",
                                 "timing": "CUDA events on the near field's own stream; the kernel shares the "
-                                          "GPU with the concurrent upward / downward passes",
+                                          "GPU with the concurrent upward / downward passes, whose stream has "
+                                          "the higher priority, so the span includes their work",
                                 "pairs_per_step": stats.pair_interactions,
                                 "m2l_per_step": stats.cell_interactions,
                                 "m2l_flop_per_step": m2l_flop}
