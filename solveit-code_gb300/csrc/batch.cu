@@ -380,8 +380,9 @@ direct_batch_kernel(const DirectItem *__restrict__ items, int nitems, int *__res
                     const double *__restrict__ xs, const double *__restrict__ ys, const double *__restrict__ zs,
                     const float *__restrict__ qs, const double *__restrict__ qm, float eps2,
                     double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az) {
-    __shared__ float4 tile[kDTile];
+    __shared__ __align__(16) float tile[4][kDTile];  // staged sources: -x, -y, -z, charge
     __shared__ int item_sh;
+    const float2 E2 = make_float2(eps2, eps2);
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) item_sh = atomicAdd(queue, 1);
@@ -390,14 +391,15 @@ direct_batch_kernel(const DirectItem *__restrict__ items, int nitems, int *__res
         if (it >= nitems) break;
         const DirectItem w = items[it];
         const double ox = xs[w.t0], oy = ys[w.t0], oz = zs[w.t0];
-        float tx[kDTPT], ty[kDTPT], tz[kDTPT];
+        float2 TX[kDTPT], TY[kDTPT], TZ[kDTPT];
         double sx[kDTPT], sy[kDTPT], sz[kDTPT];
 #pragma unroll
         for (int k = 0; k < kDTPT; k++) {
             const int ii = min(w.t0 + (int)threadIdx.x + k * kDTPB, w.t1 - 1);
-            tx[k] = (float)(xs[ii] - ox);
-            ty[k] = (float)(ys[ii] - oy);
-            tz[k] = (float)(zs[ii] - oz);
+            const float tx = (float)(xs[ii] - ox), ty = (float)(ys[ii] - oy), tz = (float)(zs[ii] - oz);
+            TX[k] = make_float2(tx, tx);
+            TY[k] = make_float2(ty, ty);
+            TZ[k] = make_float2(tz, tz);
             sx[k] = sy[k] = sz[k] = 0.0;
         }
         for (int g = 0; g < w.nimg; g++) {
@@ -411,32 +413,29 @@ direct_batch_kernel(const DirectItem *__restrict__ items, int nitems, int *__res
                         rot_image(g, px, py);
                         v = make_float4((float)(px - ox), (float)(py - oy), (float)(zs[j] - oz), qs[j]);
                     }
-                    tile[s] = v;
+                    tile[0][s] = -v.x;
+                    tile[1][s] = -v.y;
+                    tile[2][s] = -v.z;
+                    tile[3][s] = v.w;
                 }
                 __syncthreads();
-                float fx[kDTPT], fy[kDTPT], fz[kDTPT];
+                // two sources per packed FP32x2 operation, r^2 floored at kMinR2
+                float2 gx[kDTPT], gy[kDTPT], gz[kDTPT];
 #pragma unroll
-                for (int k = 0; k < kDTPT; k++) fx[k] = fy[k] = fz[k] = 0.f;
+                for (int k = 0; k < kDTPT; k++) gx[k] = gy[k] = gz[k] = make_float2(0.f, 0.f);
 #pragma unroll 4
-                for (int s = 0; s < kDTile; s++) {
-                    const float4 v = tile[s];
+                for (int s = 0; s < kDTile; s += 2) {
+                    const float2 X = ld2(tile[0], s), Y = ld2(tile[1], s), Z = ld2(tile[2], s),
+                                 Q = ld2(tile[3], s);
 #pragma unroll
-                    for (int k = 0; k < kDTPT; k++) {
-                        const float dx = tx[k] - v.x, dy = ty[k] - v.y, dz = tz[k] - v.z;
-                        float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-                        r2 = fmaxf(r2, kMinR2);
-                        const float inv = rsqrt_ftz(r2);
-                        const float wq = v.w * inv * inv * inv;
-                        fx[k] = fmaf(dx, wq, fx[k]);
-                        fy[k] = fmaf(dy, wq, fy[k]);
-                        fz[k] = fmaf(dz, wq, fz[k]);
-                    }
+                    for (int k = 0; k < kDTPT; k++)
+                        pair2<true, false>(X, Y, Z, Q, TX[k], TY[k], TZ[k], E2, gx[k], gy[k], gz[k]);
                 }
 #pragma unroll
                 for (int k = 0; k < kDTPT; k++) {
-                    sx[k] += fx[k];
-                    sy[k] += fy[k];
-                    sz[k] += fz[k];
+                    sx[k] += gx[k].x + gx[k].y;
+                    sy[k] += gy[k].x + gy[k].y;
+                    sz[k] += gz[k].x + gz[k].y;
                 }
             }
         }

@@ -67,7 +67,7 @@ direct_mixed_kernel(const double *__restrict__ xs, const double *__restrict__ ys
                     const double *__restrict__ qm, int n, int chunk, float eps2, Images im,
                     double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az,
                     int atomic_out) {
-    __shared__ float4 tile[kTile];
+    __shared__ __align__(16) float tile[4][kTile];  // staged sources: -x, -y, -z, charge
     const int t0 = blockIdx.x * (kTPB * kTPT);
     const int j_begin = blockIdx.y * chunk;
     const int j_end = min(n, j_begin + chunk);
@@ -75,15 +75,17 @@ direct_mixed_kernel(const double *__restrict__ xs, const double *__restrict__ ys
     const double ox = xs[o], oy = ys[o], oz = zs[o];
     if (!block_has_target(qm, t0, n)) return;  // whole CTA of non-targets (target subsets)
 
-    float tx[kTPT], ty[kTPT], tz[kTPT];
+    float2 TX[kTPT], TY[kTPT], TZ[kTPT];
+    const float2 E2 = make_float2(eps2, eps2);
     double sx[kTPT], sy[kTPT], sz[kTPT];
 #pragma unroll
     for (int k = 0; k < kTPT; k++) {
         const int i = t0 + threadIdx.x + k * kTPB;
         const int ii = min(i, n - 1);
-        tx[k] = (float)(xs[ii] - ox);
-        ty[k] = (float)(ys[ii] - oy);
-        tz[k] = (float)(zs[ii] - oz);
+        const float tx = (float)(xs[ii] - ox), ty = (float)(ys[ii] - oy), tz = (float)(zs[ii] - oz);
+        TX[k] = make_float2(tx, tx);
+        TY[k] = make_float2(ty, ty);
+        TZ[k] = make_float2(tz, tz);
         sx[k] = sy[k] = sz[k] = 0.0;
     }
     for (int g = 0; g < im.count; g++) {
@@ -97,32 +99,28 @@ direct_mixed_kernel(const double *__restrict__ xs, const double *__restrict__ ys
                     image_of(im, g, px, py, pz);
                     v = make_float4((float)(px - ox), (float)(py - oy), (float)(pz - oz), qs[j]);
                 }
-                tile[s] = v;
+                tile[0][s] = -v.x;
+                tile[1][s] = -v.y;
+                tile[2][s] = -v.z;
+                tile[3][s] = v.w;
             }
             __syncthreads();
-            float fx[kTPT], fy[kTPT], fz[kTPT];
+            // two sources per packed FP32x2 operation; r^2 floored at kMinR2
+            // (self pair with eps = 0: d = 0 -> 0 * finite)
+            float2 gx[kTPT], gy[kTPT], gz[kTPT];
 #pragma unroll
-            for (int k = 0; k < kTPT; k++) fx[k] = fy[k] = fz[k] = 0.f;
+            for (int k = 0; k < kTPT; k++) gx[k] = gy[k] = gz[k] = make_float2(0.f, 0.f);
 #pragma unroll 4
-            for (int s = 0; s < kTile; s++) {
-                const float4 v = tile[s];
+            for (int s = 0; s < kTile; s += 2) {
+                const float2 X = ld2(tile[0], s), Y = ld2(tile[1], s), Z = ld2(tile[2], s), Q = ld2(tile[3], s);
 #pragma unroll
-                for (int k = 0; k < kTPT; k++) {
-                    const float dx = tx[k] - v.x, dy = ty[k] - v.y, dz = tz[k] - v.z;
-                    float r2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-                    r2 = fmaxf(r2, kMinR2);  // self pair with eps = 0: d = 0 -> 0 * finite
-                    const float inv = rsqrt_ftz(r2);
-                    const float w = v.w * inv * inv * inv;
-                    fx[k] = fmaf(dx, w, fx[k]);
-                    fy[k] = fmaf(dy, w, fy[k]);
-                    fz[k] = fmaf(dz, w, fz[k]);
-                }
+                for (int k = 0; k < kTPT; k++) pair2<true, false>(X, Y, Z, Q, TX[k], TY[k], TZ[k], E2, gx[k], gy[k], gz[k]);
             }
 #pragma unroll
             for (int k = 0; k < kTPT; k++) {
-                sx[k] += fx[k];
-                sy[k] += fy[k];
-                sz[k] += fz[k];
+                sx[k] += gx[k].x + gx[k].y;
+                sy[k] += gy[k].x + gy[k].y;
+                sz[k] += gz[k].x + gz[k].y;
             }
         }
     }

@@ -203,6 +203,26 @@ __device__ __forceinline__ float rsqrt_ftz(float x) {
     return y;
 }
 
+// Two consecutive staged sources (negated coordinates X, Y, Z, charges Q)
+// against one target (T*, both halves the same), packed FP32x2: d = t + (-s),
+// r^-3 per half, partial sums of the even and odd sources in g*.
+template <bool CLAMP, bool UQ>
+__device__ __forceinline__ void pair2(float2 X, float2 Y, float2 Z, float2 Q, float2 TX, float2 TY, float2 TZ,
+                                      float2 E2, float2 &gx, float2 &gy, float2 &gz) {
+    const float2 dx = __fadd2_rn(TX, X), dy = __fadd2_rn(TY, Y), dz = __fadd2_rn(TZ, Z);
+    float2 r2 = __ffma2_rn(dx, dx, __ffma2_rn(dy, dy, __ffma2_rn(dz, dz, E2)));
+    if (CLAMP) r2 = make_float2(fmaxf(r2.x, kMinR2), fmaxf(r2.y, kMinR2));
+    const float2 inv = make_float2(rsqrt_ftz(r2.x), rsqrt_ftz(r2.y));
+    float2 w = __fmul2_rn(__fmul2_rn(inv, inv), inv);
+    if (!UQ) w = __fmul2_rn(Q, w);
+    gx = __ffma2_rn(dx, w, gx);
+    gy = __ffma2_rn(dy, w, gy);
+    gz = __ffma2_rn(dz, w, gz);
+}
+
+// two consecutive floats of a staged row
+__device__ __forceinline__ float2 ld2(const float *p, int k) { return *reinterpret_cast<const float2 *>(p + k); }
+
 // the low 21 bits of v spread to every third bit (Morton interleave: x at
 // bit 0, y at bit 1, z at bit 2 of each level's triple)
 __host__ __device__ __forceinline__ uint64_t morton_spread3(uint32_t v) {
