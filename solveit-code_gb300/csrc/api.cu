@@ -651,22 +651,30 @@ sv_status sv::compute_accel_device(sv_ctx *c, int64_t first, int64_t last) {
     if (n > 0) {
         phase_mark(c, 0);
         c->S.far = nullptr;
-        if (outliers) {
-            // outliers leave the tree; their interactions are summed directly below
-            const int32_t *st2 = nullptr;
-            SV_TRY(outliers_detect(c, &st2));
-            const ParticleView v{c->x, c->y, c->z, c->q, c->m, st2, c->n, c->n, c->qom};
-            SV_TRY(sort_view(c, v, first, last));
-        } else if (c->P.method == SV_METHOD_FMM && c->P.symmetry != SV_SYM_NONE) {
-            SV_TRY(fmm_sort_images(c, first, last));
-        } else {
-            SV_TRY(sort_state(c, first, last));
-        }
+        const int32_t *st2 = nullptr;
+        if (outliers) SV_TRY(outliers_detect(c, &st2));  // outliers leave the tree; summed directly below
+        auto sort_all = [&](int levels) -> sv_status {
+            c->S.want_levels = levels;
+            if (outliers) {
+                const ParticleView v{c->x, c->y, c->z, c->q, c->m, st2, c->n, c->n, c->qom};
+                return sort_view(c, v, first, last);
+            }
+            if (c->P.method == SV_METHOD_FMM && c->P.symmetry != SV_SYM_NONE) return fmm_sort_images(c, first, last);
+            return sort_state(c, first, last);
+        };
+        // the FMM orders its keys down to one level below its last leaf level
+        SV_TRY(sort_all(c->P.method == SV_METHOD_FMM ? fmm_sort_levels(c) : kMortonBits));
         phase_mark(c, 1);
         switch (c->P.method) {
         case SV_METHOD_DIRECT: SV_TRY(direct_accel(c)); break;
         case SV_METHOD_BARNES_HUT: SV_TRY(bh_accel(c)); break;
-        case SV_METHOD_FMM: SV_TRY(fmm_accel(c)); break;
+        case SV_METHOD_FMM:
+            SV_TRY(fmm_accel(c));
+            if (c->S.resort) {  // the leaf level moved down: the full order, then the FMM again
+                SV_TRY(sort_all(kMortonBits));
+                SV_TRY(fmm_accel(c));
+            }
+            break;
         default: return set_error(c, SV_ERR_INVALID, "unknown method");
         }
         phase_mark(c, 7);

@@ -66,6 +66,7 @@ struct Fmm {
     float4 *rel = nullptr;   // particle offset from its leaf box centre (FP32) + charge
     int64_t rel_cap = 0;
     double *far = nullptr;   // far-field acceleration (L2P / M2P), 3 x rel_cap, added in the scatter
+    int level_hint = -1;     // leaf level of the last evaluation (the next sort orders one level more)
     // forest (batched plumes): tree and per-level arrays carved at reserve time
     Tree *ftree = nullptr;
     void *farena = nullptr;
@@ -1831,6 +1832,11 @@ sv_status fmm_sort_images(sv_ctx *c, int64_t first, int64_t last) {
     return sort_view(c, v, first, last);
 }
 
+int fmm_sort_levels(const sv_ctx *c) {
+    const int h = c->fmm ? c->fmm->level_hint : -1;
+    return h >= 2 ? std::min(kMortonBits, h + 1) : kMortonBits;
+}
+
 sv_status fmm_accel(sv_ctx *c) {
     if (c->P.precision != SV_PREC_MIXED)
         return set_error(c, SV_ERR_UNSUPPORTED, "FMM runs in mixed precision only");
@@ -1841,7 +1847,15 @@ sv_status fmm_accel(sv_ctx *c) {
     Fmm &F = *c->fmm;
     SV_TRY(ensure_tables(c, F, p, c->P.fmm_ws));
     Tree *T = nullptr;
+    c->S.resort = false;
     SV_TRY(tree_build(c, kDepthMeanOccupancy, c->P.fmm_leaf_target, &T));
+    // the depth rule's box counts are exact down to the sorted levels only; a
+    // leaf level at or below them needs the full order
+    if (T->n_act > 0 && T->deepest >= c->S.key_levels && c->S.key_levels < kMortonBits) {
+        c->S.resort = true;
+        return SV_OK;
+    }
+    F.level_hint = T->deepest;
     if (T->n_act == 0) {
         SV_CK(c, cudaMemsetAsync(c->S.ax, 0, sizeof(double) * c->S.n, c->stream));
         SV_CK(c, cudaMemsetAsync(c->S.ay, 0, sizeof(double) * c->S.n, c->stream));

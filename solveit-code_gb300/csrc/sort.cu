@@ -242,9 +242,13 @@ sv_status sort_view(sv_ctx *c, const ParticleView &v, int64_t first, int64_t las
     cub::DoubleBuffer<uint64_t> kb(S.keys, S.keys_alt);
     cub::DoubleBuffer<uint32_t> vb(S.idx, S.idx_alt);
     size_t bytes = S.cub_bytes;
-    SV_CK(c, cub::DeviceRadixSort::SortPairs(S.cub_tmp, bytes, kb, vb, (int)n, 0, 3 * kMortonBits + 1,
-                                             c->stream));
-    c->launches += 2 * ((3 * kMortonBits + 1 + 7) / 8);  // CUB onesweep: histogram + passes
+    // levels 1 .. want_levels occupy bits >= 3 (kMortonBits - want_levels); bit 63 marks inactive keys
+    const int levels = std::max(1, std::min(kMortonBits, S.want_levels));
+    S.want_levels = kMortonBits;
+    S.key_levels = levels;
+    SV_CK(c, cub::DeviceRadixSort::SortPairs(S.cub_tmp, bytes, kb, vb, (int)n, 3 * (kMortonBits - levels),
+                                             3 * kMortonBits + 1, c->stream));
+    c->launches += 2 * ((3 * levels + 1 + 7) / 8);  // CUB onesweep: histogram + passes
     if (kb.Current() != S.keys) {
         std::swap(S.keys, S.keys_alt);
     }

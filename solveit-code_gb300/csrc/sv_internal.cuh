@@ -43,6 +43,11 @@ struct Sorted {
     double *red = nullptr;     // device reduction scratch
     int red_blocks = 0;
     int64_t cap = 0;
+    // Morton levels the next sort must order (a one-shot request, reset to all
+    // of them by the sort) and the levels the last sort ordered: an FMM tree
+    // needs its keys ordered down to its leaf level only
+    int want_levels = kMortonBits, key_levels = kMortonBits;
+    bool resort = false;  // the FMM found its leaf level below key_levels: sort again, fully
     int64_t n = 0;       // sorted entries (caller particles plus any image copies)
     int64_t n_orig = 0;  // caller particles; sorted idx >= n_orig are image copies
 };
@@ -269,6 +274,8 @@ cudaError_t launch_direct_mixed_sorted(const double *xs, const double *ys, const
 // tree.cu / bh.cu / fmm.cu
 sv_status bh_accel(sv_ctx *c);
 sv_status fmm_accel(sv_ctx *c);
+// Morton levels the FMM's next sort needs (its last leaf level + 1, or all)
+int fmm_sort_levels(const sv_ctx *c);
 // FMM with symmetry images: sorts the caller's particles plus their images
 sv_status fmm_sort_images(sv_ctx *c, int64_t first, int64_t last);
 void tree_free(sv_ctx *c);
