@@ -58,6 +58,17 @@ static std::map<std::string, std::string> parse_kv(int argc, char **argv, int fi
     return kv;
 }
 
+// a scratch file beside out.bin (the caller's directory), read back and removed
+static FILE *scratch_file(const char *out_path, const char *name) {
+    std::string dir(out_path);
+    const size_t slash = dir.find_last_of('/');
+    dir = slash == std::string::npos ? std::string() : dir.substr(0, slash + 1);
+    const std::string path = dir + name;
+    FILE *f = std::fopen(path.c_str(), "w+b");
+    if (f) std::remove(path.c_str());  // the open handle keeps it until closed
+    return f;
+}
+
 static double getd(std::map<std::string, std::string> &kv, const char *k, double d) {
     auto it = kv.find(k);
     return it == kv.end() ? d : std::atof(it->second.c_str());
@@ -199,8 +210,8 @@ int main(int argc, char **argv) {
         ps.params.interval = (int)getd(kv, "interval", steps);  // saveData every interval (constantRate)
         ps.params.timerInfo = TimerOptions::off;
         ps.params.saveDataToggle = SaveDataOptions::newOriginal;
-        snap = std::tmpfile();
-        events = std::tmpfile();
+        snap = scratch_file(argv[3], "snapshot.tmp");
+        events = scratch_file(argv[3], "events.tmp");
         if (!snap || !events) return 3;
         static FILE *files[1];
         files[0] = snap;
@@ -285,7 +296,7 @@ int main(int argc, char **argv) {
         bc.spatialBoundaryConditions = vec4<float>((float)getd(kv, "bx", 0.0), (float)getd(kv, "by", 0.0),
                                                    (float)getd(kv, "bz", 0.0), (float)getd(kv, "br", 0.0));
         bc.temporalBoundaryCondition = (float)getd(kv, "bt", 0.0);
-        events = std::tmpfile();
+        events = scratch_file(argv[3], "events.tmp");
         if (!events) return 3;
         ps.params.eventsFile = events;
         const float inbound = 1.0f;

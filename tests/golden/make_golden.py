@@ -55,11 +55,18 @@ sys.path.insert(0, os.path.join(ROOT, "solveit-code_gb300"))
 import plume  # noqa: E402
 
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "{}", "ref_harness")
+# scratch files of the harness runs stay inside the repository (oracle/_ref is git-ignored)
+SCRATCH = os.path.join(ROOT, "oracle", "_ref", "scratch")
+
+
+def scratch_dir():
+    os.makedirs(SCRATCH, exist_ok=True)
+    return tempfile.TemporaryDirectory(dir=SCRATCH)
 
 
 def run_ref(variant, mode, pos4, vel4, acc4, tinj, **kw):
     n = pos4.shape[0]
-    with tempfile.TemporaryDirectory() as td:
+    with scratch_dir() as td:
         fin = os.path.join(td, "in.bin")
         fout = os.path.join(td, "out.bin")
         with open(fin, "wb") as f:
@@ -221,7 +228,7 @@ def emitter_field():
     st["x"][9, 0] = 0.0       # on the y axis (phi = pi/2 whatever the sign of y)
     st["x"][9, 1] = -1e-8
     pos4, vel4, acc4, tinj = plume.to_ref32(st)
-    with tempfile.TemporaryDirectory() as td:
+    with scratch_dir() as td:
         with open(os.path.join(td, "fields.csv"), "w") as f:
             for k in range(len(er)):
                 f.write(f"{nodes[k, 0]:.17g},{nodes[k, 1]:.17g},{er[k]:.17g},{ez[k]:.17g}\n")
@@ -301,7 +308,7 @@ def energy():
     st = plume.make_plume(256, 1.2e-6, 9050)
     st["t_inj"][:] = np.floor(np.arange(256) / 64) * 2.03e-12
     st["status"][[11, 77]] = 2
-    with tempfile.TemporaryDirectory() as td:
+    with scratch_dir() as td:
         with open(os.path.join(td, "fields.csv"), "w") as f:
             for k in range(len(er)):
                 f.write(f"{nodes[k, 0]:.17g},{nodes[k, 1]:.17g},{er[k]:.17g},{ez[k]:.17g}\n")
