@@ -191,3 +191,20 @@ def test_fmm_tune_keeps_a_scale():
             fm.fmm_tune()
     with pytest.raises(sv.SolveitError):
         sv.ForceMethod(softening2=EPS20, method=sv.FMM, fmm_root_scale=2.5)
+
+
+@pytest.mark.parametrize("scale", [0.0, 1.625])
+def test_fmm_cube_of_mixed_charges(scale):
+    """A 3D geometry (uniform cube, charges 1 and 2, a few source-only
+    particles): every near box holds particles, the lists are full."""
+    n = 40000
+    rng = np.random.default_rng(91)
+    st = plume.make_plume(n, 1e-6, 92)
+    st["x"][:] = rng.random((n, 3)) * 2e-7
+    st["q"][:] = rng.choice([1.0, 2.0], n)
+    st["status"][::101] = 2
+    tg = np.arange(0, n, 20)
+    ref = O.direct_f64(st, EPS20, targets=tg)
+    a, s = run_accel(st, softening2=EPS20, method=sv.FMM, fmm_order=8, fmm_ws=2, fmm_root_scale=scale)
+    assert s.levels >= 3
+    assert rel_l2(a[tg], ref, st["status"][tg]) < 1e-5
