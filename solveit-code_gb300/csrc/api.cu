@@ -244,12 +244,6 @@ __global__ void range_status(const int32_t *__restrict__ st, int64_t first, int6
     if (i < n) out[i] = (i >= first && i < last) ? st[i] : 0;
 }
 
-__global__ void zero_nontargets(double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az,
-                                const int32_t *__restrict__ st, int64_t first, int64_t last, int64_t n) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    if (!(st[i] == 1 && i >= first && i < last)) ax[i] = ay[i] = az[i] = 0.0;
-}
 
 // Host <-> device copies split in pieces over the copy streams, so that
 // several copy engines share a large transfer: ordered after the work already
@@ -678,9 +672,7 @@ sv_status sv::compute_accel_device(sv_ctx *c, int64_t first, int64_t last) {
         default: return set_error(c, SV_ERR_INVALID, "unknown method");
         }
         phase_mark(c, 7);
-        SV_TRY(unsort_accel(c));
-        zero_nontargets<<<grid_of(n), 256, 0, c->stream>>>(c->ax, c->ay, c->az, force_status(c), first, last, n);
-        SV_LAUNCHED(c);
+        SV_TRY(unsort_accel(c));  // non-targets get zero
         if (outliers) SV_TRY(outliers_add(c, first, last));
         phase_mark(c, 8);
     }

@@ -167,12 +167,17 @@ __global__ void gather_sorted(const uint32_t *__restrict__ idx, int64_t n,
 __global__ void scatter_accel(const uint32_t *__restrict__ idx, int64_t n, int64_t n_orig,
                               const double *__restrict__ axs, const double *__restrict__ ays,
                               const double *__restrict__ azs, const double *__restrict__ far, int64_t fs,
-                              double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az) {
+                              const double *__restrict__ qm, double *__restrict__ ax, double *__restrict__ ay,
+                              double *__restrict__ az) {
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (s >= n) return;
     const uint32_t i = idx[s];
     if ((int64_t)i >= n_orig) return;
-    if (far) {
+    if (qm[s] == 0.0) {
+        // not a target of this evaluation (status, range or mass): zero, whatever the
+        // methods left in its sorted slot
+        ax[i] = ay[i] = az[i] = 0.0;
+    } else if (far) {
         ax[i] = axs[s] + far[s];
         ay[i] = ays[s] + far[fs + s];
         az[i] = azs[s] + far[2 * fs + s];
@@ -269,7 +274,7 @@ sv_status sort_state(sv_ctx *c, int64_t first, int64_t last) {
 sv_status unsort_accel(sv_ctx *c) {
     const int64_t n = c->S.n;
     scatter_accel<<<div_up(n, 256), 256, 0, c->stream>>>(c->S.idx, n, c->S.n_orig, c->S.ax, c->S.ay, c->S.az,
-                                                         c->S.far, c->S.far_stride, c->ax, c->ay, c->az);
+                                                         c->S.far, c->S.far_stride, c->S.qm, c->ax, c->ay, c->az);
     c->S.far = nullptr;
     SV_LAUNCHED(c);
     return SV_OK;

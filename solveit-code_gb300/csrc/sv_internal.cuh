@@ -258,7 +258,9 @@ sv_status ensure_sorted_capacity(sv_ctx *c, int64_t n);
 // Morton-sort the live plume into c->S (targets: inbound with index in [first,last)).
 sv_status sort_state(sv_ctx *c, int64_t first, int64_t last);
 sv_status sort_view(sv_ctx *c, const ParticleView &v, int64_t first, int64_t last);
-// Scatter c->S.a{x,y,z} back to caller order into c->a{x,y,z}.
+// Scatter c->S.a{x,y,z} (plus S.far when set) back to caller order into
+// c->a{x,y,z}; particles that are no target of the evaluation (K q/m of their
+// sorted slot = 0) get zero.
 sv_status unsort_accel(sv_ctx *c);
 // Read root box (origin, side) to the host (blocking).
 sv_status read_root(sv_ctx *c, double root[8]);
