@@ -47,6 +47,13 @@ public:
     // the FmmType the reference passes to MultipoleMethodForceCalculation's
     // constructor (multipole_method_force_calculation.cpp:9-104)
     void setFmmType(sv_fmm_type t) { params_.fmm_type = t; }
+    // the FMM root cube's scale (sv_params.fmm_root_scale), or sv_fmm_tune on
+    // the first evaluation's state when autoTune is set
+    void setRootScale(float s) { params_.fmm_root_scale = s; }
+    void setAutoTune(bool on) {
+        autoTune_ = on;
+        tuned_ = false;
+    }
 
     void updateAcceleration() override {
         if (particleSystem == nullptr) {
@@ -66,6 +73,11 @@ public:
         check(sv_upload_ref32(ctx_, n, &cp.position[f].x, &cp.velocity[f].x, &cp.acceleration[f].x,
                               cp.timeInjected ? &cp.timeInjected[f] : nullptr),
               "sv_upload_ref32");
+        if (autoTune_ && !tuned_ && params_.method == SV_METHOD_FMM) {
+            check(sv_fmm_tune(ctx_, nullptr), "sv_fmm_tune");
+            check(sv_get_params(ctx_, &params_), "sv_get_params");  // keeps the tuned scale
+            tuned_ = true;
+        }
         check(sv_compute_accel(ctx_, 0, n, nullptr), "sv_compute_accel");
         check(sv_add_accel_ref32(ctx_, &cp.acceleration[f].x), "sv_add_accel_ref32");
         if (timeInfoFile != nullptr) {
@@ -77,7 +89,10 @@ public:
         }
     }
 
-    void increaseLevel() override {}
+    // the reference's integrator calls this when a deeper FMM level measured
+    // faster (Integrator::compareAcceleration): tune the root scale again at
+    // the next evaluation
+    void increaseLevel() override { tuned_ = false; }
     void setSaveName() override {
         if (saveName[0] == '\0') saveName = "_gpu.bin";
     }
@@ -117,4 +132,5 @@ private:
 
     sv_params params_;
     sv_ctx *ctx_ = nullptr;
+    bool autoTune_ = false, tuned_ = false;
 };
