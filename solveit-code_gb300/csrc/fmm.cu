@@ -662,6 +662,10 @@ m2m_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ child0
 
 template <int P>
 constexpr int m2l_warps() { return P >= 10 ? 2 : 4; }
+// CTAs per SM the M2L is compiled for: the most that keep its registers
+// unspilled (the kernel waits on dependent loads, so resident warps hide it)
+template <int P>
+constexpr int m2l_min_ctas() { return P >= 10 ? 1 : (P >= 8 ? 6 : 8); }
 // list entries a warp carries through one pass of the M2L loop
 template <int P>
 constexpr int m2l_inflight() { return 2; }
@@ -670,7 +674,7 @@ constexpr int m2l_inflight() { return 2; }
 // in shared memory; the rotation rows of each entry's polar angle are read
 // from global memory (L1/L2), one 16-byte row segment per lane and group.
 template <int P>
-__global__ void __launch_bounds__(m2l_warps<P>() * 32) m2l_kernel(M2LArgs a) {
+__global__ void __launch_bounds__(m2l_warps<P>() * 32, m2l_min_ctas<P>()) m2l_kernel(M2LArgs a) {
     constexpr int NC = ncoef(P), RS = rot_rs<P>(), SR = sh_rs<P>(), ZK = z_ks<P>(), WP = m2l_warps<P>();
     constexpr int NU = m2l_inflight<P>();
     __shared__ __align__(16) float2 A[WP][NU][P * SR], B[WP][NU][P * SR];
