@@ -381,11 +381,26 @@ sv_status energy_first(sv_ctx *c, double t_end) {
     return SV_OK;
 }
 
+// one record (KE_inj, PE_inj, FE_inj, KE, PE, FE)
+static sv_status push_record(sv_ctx *c, const sv_energy_record &r) {
+    EnergyBook &E = c->en;
+    if (E.nrec == E.rec_cap) {
+        const int64_t cap = std::max<int64_t>(64, 2 * E.rec_cap);
+        sv_energy_record *m = (sv_energy_record *)std::realloc(E.recs, sizeof(sv_energy_record) * cap);
+        if (!m) return set_error(c, SV_ERR_CAPACITY, "no host memory for energy records");
+        E.recs = m;
+        E.rec_cap = cap;
+    }
+    E.recs[E.nrec++] = r;
+    return SV_OK;
+}
+
 sv_status energy_interval(sv_ctx *c, double ts, double dt) {
     EnergyBook &E = c->en;
-    if (!E.on || c->n == 0) return SV_OK;
+    if (!E.on) return SV_OK;
     const long long iter = std::llround(ts / dt) + 1;
     if (iter % E.interval != 0) return SV_OK;
+    if (c->n == 0) return push_record(c, sv_energy_record{0.f, 0.f, 0.f, 0.f, 0.f, 0.f});  // an empty window
     const double t_end = ts + dt;
     int cnt = 0;
     SV_TRY(select(c, WindowSel{c->t_inj, E.d_first, t_end}, &cnt));
@@ -409,16 +424,8 @@ sv_status energy_interval(sv_ctx *c, double ts, double dt) {
     SV_CK(c, cudaMemcpyAsync(acc, E.d_acc, sizeof(acc), cudaMemcpyDeviceToHost, c->stream));
     SV_CK(c, cudaStreamSynchronize(c->stream));
     const double pc = pe_coef();
-    if (E.nrec == E.rec_cap) {
-        const int64_t cap = std::max<int64_t>(64, 2 * E.rec_cap);
-        sv_energy_record *r = (sv_energy_record *)std::realloc(E.recs, sizeof(sv_energy_record) * cap);
-        if (!r) return set_error(c, SV_ERR_CAPACITY, "no host memory for energy records");
-        E.recs = r;
-        E.rec_cap = cap;
-    }
-    E.recs[E.nrec++] = sv_energy_record{(float)acc[0], (float)(acc[1] * pc), (float)acc[2],
-                                        (float)acc[3], (float)(0.5 * acc[4] * pc), (float)acc[5]};
-    return SV_OK;
+    return push_record(c, sv_energy_record{(float)acc[0], (float)(acc[1] * pc), (float)acc[2], (float)acc[3],
+                                           (float)(0.5 * acc[4] * pc), (float)acc[5]});
 }
 
 void energy_rearm(sv_ctx *c) {

@@ -154,3 +154,14 @@ def test_full_snapshot_holds_every_particle():
     ro = full_o.view(REC_ORIG)
     assert np.array_equal(ro["index"], np.arange(n)) and np.all(ro["last"] == last)
     assert np.array_equal(ro["f"], rec["f"]) and np.array_equal(ro["species"], rec["species"])
+
+
+def test_energy_records_of_an_empty_state():
+    st = {k: v[:0] for k, v in plume.make_plume(1, 1e-6, 9090).items()}
+    with sv.ForceMethod(softening2=1e-20, precision=sv.FP64) as fm:
+        fm.upload(st)
+        fm.set_energy(10, 10, 1)
+        fm.leapfrog(2, 1e-12)
+        rec = as_array(fm.energy_records())
+    # the reference writes a record per interval whatever the window holds
+    assert rec.shape == (2, 6) and np.all(rec == 0)

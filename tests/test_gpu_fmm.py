@@ -208,3 +208,21 @@ def test_fmm_cube_of_mixed_charges(scale):
     a, s = run_accel(st, softening2=EPS20, method=sv.FMM, fmm_order=8, fmm_ws=2, fmm_root_scale=scale)
     assert s.levels >= 3
     assert rel_l2(a[tg], ref, st["status"][tg]) < 1e-5
+
+
+@pytest.mark.parametrize("n", [0, 1, 37])
+def test_fmm_tune_small_and_empty(n):
+    st = plume.make_plume(max(n, 1), 1e-7, 95)
+    if n == 0:
+        st = {k: v[:0] for k, v in st.items()}
+    with sv.ForceMethod(softening2=EPS20, method=sv.FMM, fmm_order=8, fmm_ws=2) as fm:
+        fm.upload(st)
+        scale, _ = fm.fmm_tune()
+        assert 1.0 <= scale < 2.0
+        a = fm.accel()
+    assert a.shape == (n, 3)
+    if n == 37:
+        ref = O.direct_f64(st, EPS20)
+        assert rel_l2(a, ref, st["status"]) < 1e-5
+    elif n == 1:
+        assert np.all(a == 0)
