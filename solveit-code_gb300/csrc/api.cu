@@ -458,6 +458,7 @@ void sv_destroy(sv_ctx *c) {
     cudaFree(c->d_stage);
     cudaFree(c->d_scalar);
     if (c->h_scalar) cudaFreeHost(c->h_scalar);
+    if (c->h_accel) cudaFreeHost(c->h_accel);
     if (c->ev_begin) cudaEventDestroy(c->ev_begin);
     if (c->ev_end) cudaEventDestroy(c->ev_end);
     for (int k = 0; k < 9; k++)
@@ -707,12 +708,21 @@ sv_status sv_add_accel_ref32(sv_ctx *c, float *acc4) {
     if (!c || !acc4) return SV_ERR_INVALID;
     if (!c->have_accel) return set_error(c, SV_ERR_STATE, "no acceleration computed");
     const int64_t n = c->n;
-    std::vector<double> a(3 * n);
+    if (n == 0) return SV_OK;
+    // a page-locked copy kept by the context: no allocation or page faults per call
+    if (c->h_accel_cap < 3 * n) {
+        if (c->h_accel) cudaFreeHost(c->h_accel);
+        c->h_accel = nullptr;
+        c->h_accel_cap = 0;
+        SV_CK(c, cudaMallocHost(&c->h_accel, sizeof(double) * 3 * n));
+        c->h_accel_cap = 3 * n;
+    }
+    const double *a = c->h_accel;
     void *stg = nullptr;
     SV_TRY(stage_bytes(c, sizeof(double) * 3 * n, &stg));
     pack_accel<<<grid_of(n), 256, 0, c->stream>>>(c->ax, c->ay, c->az, c->status, 0, n, n, (double *)stg);
     SV_LAUNCHED(c);
-    SV_CK(c, cudaMemcpyAsync(a.data(), stg, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c->stream));
+    SV_CK(c, cudaMemcpyAsync(c->h_accel, stg, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c->stream));
     SV_CK(c, cudaStreamSynchronize(c->stream));
     for (int64_t i = 0; i < n; i++) {
         if (acc4[4 * i + 3] != 1.0f) continue;

@@ -160,6 +160,8 @@ struct sv_ctx {
     // their join events, the last one the fork from the context's stream
     cudaStream_t cps[4] = {};
     cudaEvent_t cpe[5] = {};
+    double *h_accel = nullptr;    // page-locked host copy of the acceleration (sv_add_accel_ref32)
+    int64_t h_accel_cap = 0;      // doubles
     double *d_scalar = nullptr;   // device scratch for small reductions
     double *h_scalar = nullptr;   // pinned mirror
     cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
