@@ -103,7 +103,11 @@ typedef struct {
                                 plume's extent, rounded down to a multiple of 1/8 in [1, 2)
                                 (0: 1): leaf boxes between two octree levels' sizes, so the
                                 box side can follow the plume (sv_fmm_tune picks it) */
-    int32_t reserved[4];
+    int32_t fmm_direct_pairs;  /* leaf-level interaction-list entries whose two boxes hold fewer
+                                particles multiplied than this are summed as direct pairs in the
+                                near field instead of an M2L translation (up to 128 per box; single
+                                plumes): 0 = 1024, < 0 = every entry by M2L */
+    int32_t reserved[3];
 } sv_params;
 
 /* Per-call statistics of the last force evaluation. */

@@ -144,18 +144,28 @@ __device__ __forceinline__ const double *box_root(const double *root, const int 
 // by round (lanes take the parent's near slots) into the near list (|offset|
 // <= WS, written when write_near) and the interaction list (M2L entries
 // compacted by ballot).  Returns the box's M2L count.
+//
+// Far-direct lists (fd non-null, the leaf level of a single tree): an
+// interaction-list entry whose two boxes hold fewer than fd_thresh particles
+// multiplied is cheaper as direct pairs than as an M2L translation; up to
+// fd_cap of them per box go to fd (summed by the near field), the rest stay
+// M2L entries.
 template <int WS>
 __device__ __forceinline__ int build_lists_box(int b, int4 cb, int par, const int4 *__restrict__ coord,
                                                const int *__restrict__ pnbr, const int *__restrict__ pchild0,
                                                int *__restrict__ nbr, int2 *__restrict__ m2l,
-                                               int *__restrict__ m2l_cnt, int cap, int write_near) {
+                                               int *__restrict__ m2l_cnt, int cap, int write_near,
+                                               const int *__restrict__ start = nullptr, int *__restrict__ fd = nullptr,
+                                               int *__restrict__ fd_cnt = nullptr, int fd_cap = 0,
+                                               int fd_thresh = 0) {
     constexpr int NS1 = 2 * WS + 1, NS = NS1 * NS1 * NS1, R = 2 * WS + 1, SIDE = 2 * R + 1;
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
     if (write_near)
         for (int s = lane; s < NS; s += 32) nbr[b * NS + s] = -1;
     __syncwarp();
-    int cnt = 0;
+    const long long nt = fd ? (long long)(start[b + 1] - start[b]) : 0;
+    int cnt = 0, dcnt = 0;
     for (int s0 = 0; s0 < NS; s0 += 32) {
         const int s = s0 + lane;
         int c0 = 0, c1 = 0;
@@ -184,6 +194,18 @@ __device__ __forceinline__ int build_lists_box(int b, int4 cb, int par, const in
                     cls = ((ox + R) * SIDE + (oy + R)) * SIDE + (oz + R);
                 }
             }
+            if (fd) {
+                const bool dir = far && (long long)(start[ch + 1] - start[ch]) * nt < (long long)fd_thresh;
+                const unsigned bd = __ballot_sync(0xffffffffu, dir);
+                if (dir) {
+                    const int pos = dcnt + __popc(bd & lt_mask);
+                    if (pos < fd_cap) {
+                        fd[(size_t)b * fd_cap + pos] = ch;
+                        far = false;
+                    }
+                }
+                dcnt += __popc(bd);
+            }
             const unsigned bal = __ballot_sync(0xffffffffu, far);
             if (far) {
                 const int pos = cnt + __popc(bal & lt_mask);
@@ -194,7 +216,10 @@ __device__ __forceinline__ int build_lists_box(int b, int4 cb, int par, const in
         }
     }
     if (cnt > cap) cnt = cap;
-    if (lane == 0) m2l_cnt[b] = cnt;
+    if (lane == 0) {
+        m2l_cnt[b] = cnt;
+        if (fd) fd_cnt[b] = dcnt < fd_cap ? dcnt : fd_cap;
+    }
     return cnt;
 }
 
@@ -225,9 +250,12 @@ struct ListLevel {
     const int *pnbr;         // the parent level's near lists
     int2 *m2l;
     int *m2l_cnt;
+    const int *start;        // particle ranges of this level's boxes
+    int *fd, *fd_cnt;        // far-direct lists (the leaf level only, else null)
 };
 struct ListArgs {
     int nlev, total;         // levels 0 .. nlev - 1; boxes of all of them
+    int fd_cap, fd_thresh;   // far-direct list capacity per box and pair threshold
     ListLevel lv[kMortonBits + 1];
 };
 
@@ -298,7 +326,7 @@ __global__ void __launch_bounds__(kWarps * 32) m2l_lists_kernel(ListArgs a, int 
         const ListLevel &L = a.lv[list_level(a, g)];
         const int b = g - L.first;
         const int cnt = build_lists_box<WS>(b, L.coord[b], L.parent[b], L.coord, L.pnbr, L.pchild0, L.nbr, L.m2l,
-                                            L.m2l_cnt, cap, 0);
+                                            L.m2l_cnt, cap, 0, L.start, L.fd, L.fd_cnt, a.fd_cap, a.fd_thresh);
         if (lane == 0) tot += cnt;
     }
     if (lane == 0 && tot) atomicAdd(&counts[0], tot);
@@ -1078,8 +1106,10 @@ __device__ __forceinline__ void kahan_add(float &s, float &e, float v) {
 // the pair weight is r^-3 alone, the sums are scaled by the target's own
 // charge (= Q) at the end, and padding sources sit far away (r^-3 underflows
 // to zero) instead of carrying zero charge.
+constexpr int kFarDirectCap = 128;  // far-direct source boxes per leaf box
+// source boxes a leaf box's near field can take: its near boxes and its far-direct ones
 template <int WS>
-constexpr int p2p_nsp() { return ((2 * WS + 1) * (2 * WS + 1) * (2 * WS + 1) + 31) / 32 * 32; }
+constexpr int p2p_nsp() { return ((2 * WS + 1) * (2 * WS + 1) * (2 * WS + 1) + 31) / 32 * 32 + kFarDirectCap; }
 
 
 template <int WS, bool CLAMP, bool UQ>
@@ -1088,8 +1118,8 @@ p2p_body(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, co
          const int4 *__restrict__ coord, const int *__restrict__ nbr, const double *__restrict__ qm,
          const double *__restrict__ roots, int level, float eps2, double *__restrict__ ax, double *__restrict__ ay,
          double *__restrict__ az, unsigned long long *__restrict__ counts, const int *__restrict__ has_tgt,
-         const float4 *__restrict__ rel, float (*st)[4][32], int2 (*nb_rng)[p2p_nsp<WS>()],
-         float4 (*nb_off)[p2p_nsp<WS>()]) {
+         const float4 *__restrict__ rel, const int *__restrict__ fd, const int *__restrict__ fd_cnt, int fd_cap,
+         float (*st)[4][32], int2 (*nb_rng)[p2p_nsp<WS>()], float4 (*nb_off)[p2p_nsp<WS>()]) {
     constexpr int NS1 = 2 * WS + 1, NS = NS1 * NS1 * NS1;
     const float4 pad = UQ ? make_float4(1e18f, 0.f, 0.f, 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
     const float2 E2 = make_float2(eps2, eps2);
@@ -1101,33 +1131,39 @@ p2p_body(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, co
     const float hf = (float)(box_root(roots, bpid, b)[3] / (double)(1 << level));
     const int4 cb = coord[b];
     int nnz = 0, total = 0;
-    for (int s0 = 0; s0 < NS; s0 += 32) {
-        const int s = s0 + lane;
-        int Q = -1, j0 = 0, cnt = 0;
-        if (s < NS) {
-            Q = nbr[b * NS + s];
-            if (Q >= 0) {
-                j0 = start[Q];
-                cnt = start[Q + 1] - j0;
+    // the non-empty boxes of a list (count warp-uniform; -1 entries skipped)
+    // appended with their running source count and their offset
+    auto add_boxes = [&](const int *list, int count) {
+        for (int s0 = 0; s0 < count; s0 += 32) {
+            const int s = s0 + lane;
+            int Q = -1, j0 = 0, cnt = 0;
+            if (s < count) {
+                Q = list[s];
+                if (Q >= 0) {
+                    j0 = start[Q];
+                    cnt = start[Q + 1] - j0;
+                }
             }
+            const bool f = cnt > 0;
+            const unsigned bal = __ballot_sync(0xffffffffu, f);
+            int inc = cnt;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += t;
+            }
+            if (f) {
+                const int pos = nnz + __popc(bal & lt_mask);
+                const int4 cq = coord[Q];
+                nb_rng[wid][pos] = make_int2(j0, total + inc);
+                nb_off[wid][pos] = make_float4((float)(cq.x - cb.x) * hf, (float)(cq.y - cb.y) * hf,
+                                               (float)(cq.z - cb.z) * hf, 0.f);
+            }
+            nnz += __popc(bal);
+            total += __shfl_sync(0xffffffffu, inc, 31);
         }
-        const bool f = cnt > 0;
-        const unsigned bal = __ballot_sync(0xffffffffu, f);
-        int inc = cnt;
-        for (int o = 1; o < 32; o <<= 1) {
-            const int t = __shfl_up_sync(0xffffffffu, inc, o);
-            if (lane >= o) inc += t;
-        }
-        if (f) {
-            const int pos = nnz + __popc(bal & lt_mask);
-            const int4 cq = coord[Q];
-            nb_rng[wid][pos] = make_int2(j0, total + inc);
-            nb_off[wid][pos] = make_float4((float)(cq.x - cb.x) * hf, (float)(cq.y - cb.y) * hf,
-                                           (float)(cq.z - cb.z) * hf, 0.f);
-        }
-        nnz += __popc(bal);
-        total += __shfl_sync(0xffffffffu, inc, 31);
-    }
+    };
+    add_boxes(nbr + (size_t)b * NS, NS);
+    if (fd) add_boxes(fd + (size_t)b * fd_cap, fd_cnt[b]);
     __syncwarp();
     const int t0 = start[b], t1 = start[b + 1];
     int tb = t0;
@@ -1276,26 +1312,28 @@ p2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, 
            const int4 *__restrict__ coord, const int *__restrict__ nbr, const double *__restrict__ qm,
            const double *__restrict__ roots, int level, float eps2, double *__restrict__ ax, double *__restrict__ ay,
            double *__restrict__ az, unsigned long long *__restrict__ counts, const int *__restrict__ has_tgt,
-           const float4 *__restrict__ rel) {
+           const float4 *__restrict__ rel, const int *__restrict__ fd, const int *__restrict__ fd_cnt, int fd_cap) {
     __shared__ __align__(16) float src[kWarps][4][32];  // staged sources: -x, -y, -z, charge
     __shared__ int2 nb_rng[kWarps][p2p_nsp<WS>()];    // (first source, running source count at the box's end)
     __shared__ float4 nb_off[kWarps][p2p_nsp<WS>()];  // source box centre - target box centre (exact in FP32)
     if (counts[2] == 0)
         p2p_body<WS, CLAMP, true>(nbox, nbd, bpid, start, coord, nbr, qm, roots, level, eps2, ax, ay, az, counts,
-                                  has_tgt, rel, src, nb_rng, nb_off);
+                                  has_tgt, rel, fd, fd_cnt, fd_cap, src, nb_rng, nb_off);
     else
         p2p_body<WS, CLAMP, false>(nbox, nbd, bpid, start, coord, nbr, qm, roots, level, eps2, ax, ay, az, counts,
-                                   has_tgt, rel, src, nb_rng, nb_off);
+                                   has_tgt, rel, fd, fd_cnt, fd_cap, src, nb_rng, nb_off);
 }
 
 // P2P launch: well-separation and whether r^2 needs the kMinR2 floor
 inline void launch_p2p(int ws, float eps2, int grid, cudaStream_t st, int nbox, const int *nbd, const int *bpid,
                        const int *start, const int4 *coord, const int *nbr, const double *qm, const double *roots,
                        int level, double *ax, double *ay, double *az, unsigned long long *counts,
-                       const int *has_tgt, const float4 *rel) {
+                       const int *has_tgt, const float4 *rel, const int *fd = nullptr,
+                       const int *fd_cnt = nullptr, int fd_cap = 0) {
     const bool clamp = !(eps2 >= kMinR2);
 #define SV_P2P(W, C) p2p_kernel<W, C><<<grid, kWarps * 32, 0, st>>>(nbox, nbd, bpid, start, coord, nbr, qm, roots, \
-                                                                   level, eps2, ax, ay, az, counts, has_tgt, rel)
+                                                                   level, eps2, ax, ay, az, counts, has_tgt, rel,  \
+                                                                   fd, fd_cnt, fd_cap)
     if (ws == 1) {
         if (clamp) SV_P2P(1, true);
         else SV_P2P(1, false);
@@ -1326,6 +1364,10 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         if (chunks[l] > 1) bytes += rounded(nb * chunks[l] * NC * sizeof(float2));
     }
     for (int l = 0; l <= L; l++) bytes += rounded((size_t)T.lv[l].nbox * sizeof(uint64_t));  // box codes
+    // far-direct lists of the leaf boxes (sv_params.fmm_direct_pairs; 0: 1024 pairs, < 0: none)
+    const int fd_thresh = c->P.fmm_direct_pairs == 0 ? 1024 : c->P.fmm_direct_pairs;
+    const bool use_fd = fd_thresh > 0 && L >= 2;
+    if (use_fd) bytes += rounded((size_t)T.lv[L].nbox * (kFarDirectCap + 1) * sizeof(int));
     if (F.arena_bytes < bytes) {
         cudaFree(F.arena);
         F.arena = nullptr;
@@ -1368,6 +1410,14 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         q.pnbr = l > 0 ? nbr[l - 1] : nullptr;
         q.m2l = lst[l];
         q.m2l_cnt = cnt[l];
+        q.start = T.lv[l].start;
+        q.fd = q.fd_cnt = nullptr;
+    }
+    la.fd_cap = kFarDirectCap;
+    la.fd_thresh = fd_thresh;
+    if (use_fd) {
+        la.lv[L].fd = (int *)carve((size_t)T.lv[L].nbox * kFarDirectCap * sizeof(int));
+        la.lv[L].fd_cnt = (int *)carve((size_t)T.lv[L].nbox * sizeof(int));
     }
     phase_mark(c, 2);
     SV_CK(c, cudaMemsetAsync(F.d_counts, 0, 3 * sizeof(unsigned long long), c->stream));
@@ -1432,7 +1482,8 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         SV_LAUNCHED(c);
         if (c->P.profile_phases) SV_CK(c, cudaEventRecord(F.ev_near[0], F.side));
         launch_p2p(ws, (float)c->P.softening2, div_up(V.nbox, kWarps), F.side, V.nbox, nullptr, nullptr, V.start,
-                   V.coord, nbr[L], S.qm, S.root, L, S.ax, S.ay, S.az, F.d_counts, tgt[L], F.rel);
+                   V.coord, nbr[L], S.qm, S.root, L, S.ax, S.ay, S.az, F.d_counts, tgt[L], F.rel, la.lv[L].fd,
+                   la.lv[L].fd_cnt, kFarDirectCap);
         SV_LAUNCHED(c);
         if (c->P.profile_phases) {
             SV_CK(c, cudaEventRecord(F.ev_near[1], F.side));
