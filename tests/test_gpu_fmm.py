@@ -226,3 +226,20 @@ def test_fmm_tune_small_and_empty(n):
         assert rel_l2(a, ref, st["status"]) < 1e-5
     elif n == 1:
         assert np.all(a == 0)
+
+
+def test_fmm_far_direct_lists():
+    """Sparse leaf interactions as direct pairs (fmm_direct_pairs): fewer M2L
+    translations, more pairs, the same accuracy bound; off (-1) and a large
+    threshold too."""
+    st = plume.make_plume(65536, 10e-6, 96)
+    st["x"][::7, :2] *= 3.0  # a sparse halo around the core
+    tg = np.arange(0, 65536, 32)
+    ref = O.direct_f64(st, EPS20, targets=tg)
+    out = {}
+    for th in (-1, 0, 20000):
+        a, s = run_accel(st, softening2=EPS20, method=sv.FMM, fmm_order=8, fmm_ws=2, fmm_direct_pairs=th)
+        assert rel_l2(a[tg], ref, st["status"][tg]) < 1e-5, th
+        out[th] = (s.cell_interactions, s.pair_interactions)
+    assert out[0][0] < out[-1][0] and out[0][1] > out[-1][1]
+    assert out[20000][0] <= out[0][0]
