@@ -75,6 +75,7 @@ struct Fmm {
     int fchunks[kMortonBits + 1] = {};
     int *fnbr[kMortonBits + 1] = {}, *fcnt[kMortonBits + 1] = {}, *ftgt[kMortonBits + 1] = {};
     int2 *flst[kMortonBits + 1] = {};
+    int *ffd = nullptr, *ffd_cnt = nullptr;  // far-direct lists of the forest's leaf boxes
     float4 *frel = nullptr;
     int64_t frel_cap = 0;
     // the near field runs on its own stream beside the upward and downward passes
@@ -229,10 +230,13 @@ __global__ void __launch_bounds__(kWarps * 32)
 build_lists_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ parent,
                    const int4 *__restrict__ coord, const int *__restrict__ pnbr, const int *__restrict__ pchild0,
                    int *__restrict__ nbr, int2 *__restrict__ m2l, int *__restrict__ m2l_cnt, int cap,
-                   unsigned long long *__restrict__ counts) {
+                   unsigned long long *__restrict__ counts, const int *__restrict__ start = nullptr,
+                   int *__restrict__ fd = nullptr, int *__restrict__ fd_cnt = nullptr, int fd_cap = 0,
+                   int fd_thresh = 0) {
     unsigned long long tot = 0;
     SV_WARP_BOXES(kWarps) {
-    const int cnt = build_lists_box<WS>(b, coord[b], parent[b], coord, pnbr, pchild0, nbr, m2l, m2l_cnt, cap, 1);
+    const int cnt = build_lists_box<WS>(b, coord[b], parent[b], coord, pnbr, pchild0, nbr, m2l, m2l_cnt, cap, 1,
+                                        start, fd, fd_cnt, fd_cap, fd_thresh);
     if (lane == 0) tot += cnt;
     }
     if ((threadIdx.x & 31) == 0 && tot) atomicAdd(&counts[0], tot);
@@ -1656,17 +1660,20 @@ sv_status run_fmm_forest(sv_ctx *c, Fmm &F, const ForestArgs &fa) {
                                                                         F.ftgt[l + 1], F.ftgt[l]);
         SV_LAUNCHED(c);
     }
+    // far-direct lists at the leaf level (sv_params.fmm_direct_pairs, as the single tree's)
+    const int fd_thresh = c->P.fmm_direct_pairs == 0 ? 1024 : c->P.fmm_direct_pairs;
     for (int l = 1; l <= L; l++) {
         const Level &V = T.lv[l];
         const Level &U = T.lv[l - 1];
+        const bool fdl = l == L && fd_thresh > 0;
         if (ws == 1)
             build_lists_kernel<1><<<forest_grid(f.cap[l], kWarps), kWarps * 32, 0, sd>>>(
                 f.cap[l], nbd + l, V.parent, V.coord, F.fnbr[l - 1], U.child0, F.fnbr[l], F.flst[l], F.fcnt[l], cap,
-                F.d_counts);
+                F.d_counts, V.start, fdl ? F.ffd : nullptr, F.ffd_cnt, kFarDirectCap, fd_thresh);
         else
             build_lists_kernel<2><<<forest_grid(f.cap[l], kWarps), kWarps * 32, 0, sd>>>(
                 f.cap[l], nbd + l, V.parent, V.coord, F.fnbr[l - 1], U.child0, F.fnbr[l], F.flst[l], F.fcnt[l], cap,
-                F.d_counts);
+                F.d_counts, V.start, fdl ? F.ffd : nullptr, F.ffd_cnt, kFarDirectCap, fd_thresh);
         SV_LAUNCHED(c);
     }
     SV_CK(c, cudaEventRecord(F.ev_lists, sd));
@@ -1680,7 +1687,8 @@ sv_status run_fmm_forest(sv_ctx *c, Fmm &F, const ForestArgs &fa) {
                                                        S.q, fa.roots, L, F.frel, F.d_counts + 2);
         SV_LAUNCHED(c);
         launch_p2p(ws, (float)c->P.softening2, g, sd, f.cap[L], nbd + L, V.pid, V.start, V.coord, F.fnbr[L], S.qm,
-                   fa.roots, L, S.ax, S.ay, S.az, F.d_counts, F.ftgt[L], F.frel);
+                   fa.roots, L, S.ax, S.ay, S.az, F.d_counts, F.ftgt[L], F.frel, fd_thresh > 0 ? F.ffd : nullptr,
+                   F.ffd_cnt, kFarDirectCap);
         SV_LAUNCHED(c);
         SV_CK(c, cudaEventRecord(F.ev_join, sd));
     }
@@ -1949,6 +1957,7 @@ sv_status fmm_forest_reserve(sv_ctx *c, const ForestArgs &fa) {
                  rounded(nb * cap * sizeof(int2)) + 2 * rounded(nb * sizeof(int));
         if (F.fchunks[l] > 1) bytes += rounded(nb * F.fchunks[l] * NC * sizeof(float2));
     }
+    bytes += rounded((size_t)f.cap[f.L] * kFarDirectCap * sizeof(int)) + rounded((size_t)f.cap[f.L] * sizeof(int));
     if (F.farena_bytes < bytes) {
         cudaFree(F.farena);
         F.farena = nullptr;
@@ -1977,6 +1986,8 @@ sv_status fmm_forest_reserve(sv_ctx *c, const ForestArgs &fa) {
         F.ftgt[l] = (int *)carve(nb * sizeof(int));
         F.fpart[l] = F.fchunks[l] > 1 ? (float2 *)carve(nb * F.fchunks[l] * NC * sizeof(float2)) : F.fL[l];
     }
+    F.ffd = (int *)carve((size_t)f.cap[f.L] * kFarDirectCap * sizeof(int));
+    F.ffd_cnt = (int *)carve((size_t)f.cap[f.L] * sizeof(int));
     if (F.frel_cap < f.n) {
         cudaFree(F.frel);
         F.frel = nullptr;
