@@ -81,7 +81,7 @@ struct Fmm {
     // the near field runs on its own stream beside the upward and downward passes
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_lists = nullptr, ev_join = nullptr, ev_near[2] = {};
-    cudaEvent_t ev_m2l_lists = nullptr;  // single plume: interaction lists built (second stream)
+    cudaEvent_t ev_m2l_lists = nullptr;  // single plume: near, interaction and far-direct lists built (second stream)
 };
 
 namespace {
