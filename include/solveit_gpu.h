@@ -106,7 +106,7 @@ typedef struct {
     int32_t fmm_direct_pairs;  /* leaf-level interaction-list entries whose two boxes hold fewer
                                 particles multiplied than this are summed as direct pairs in the
                                 near field instead of an M2L translation (up to 128 per box; single
-                                plumes): 0 = 1024, < 0 = every entry by M2L */
+                                plumes and a batch's FMM forest): 0 = 1024, < 0 = every entry by M2L */
     int32_t reserved[3];
 } sv_params;
 
