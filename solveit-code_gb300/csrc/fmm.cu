@@ -1091,23 +1091,24 @@ __device__ __forceinline__ void kahan_add(float &s, float &e, float v) {
     s = t;
 }
 
-// Near field of one leaf box per warp.  The box's non-empty near boxes are
-// first compacted into shared memory with a running count of their sources;
-// the sources are then streamed 32 at a time across box boundaries (each lane
-// walks forward to the box of its staged source), so the pair loop runs
-// without per-box padding or per-box overhead.  CLAMP: floor r^2 at kMinR2,
-// needed only when eps^2 < kMinR2 (a zero-distance pair without softening).  Targets: one per lane; a
-// chunk of nt < 32 targets gives each target a group of g lanes (a power of
-// two, nt * g <= 32) that split the staged sources.  Sources are staged as
-// negated coordinates in structure-of-arrays rows, so one 64-bit load gives
-// two consecutive sources and each pair operation is a packed FP32x2
-// instruction (FADD2 / FFMA2 / FMUL2) over two sources; the reciprocal square
-// roots stay scalar.  Each 32-source chunk's
-// FP32 partial sum is added with Kahan compensation.  The result is stored
-// (each particle of a box with targets once; boxes without targets are left
-// as they are).  UQ: every particle of
-// the tree carries the same charge Q (box_relative_kernel found no other), so
-// the pair weight is r^-3 alone, the sums are scaled by the target's own
+// Near field of one leaf box per warp.  The box's non-empty near boxes, then
+// its far-direct boxes (interaction-list entries cheaper as pairs, from
+// build_lists_box), are compacted into shared memory with a running count of
+// their sources; the sources are then streamed 32 at a time across box
+// boundaries (each lane walks forward to the box of its staged source), so the
+// pair loop runs without per-box padding or per-box overhead.  Sources are
+// staged as negated coordinates in structure-of-arrays rows, so one 64-bit
+// load gives two consecutive sources and each pair operation is a packed
+// FP32x2 instruction (FADD2 / FFMA2 / FMUL2) over two sources; the reciprocal
+// square roots stay scalar.  Targets: two per lane while more than 48 remain,
+// then one per lane; a chunk of nt < 32 targets gives each target a group of g
+// lanes (a power of two, nt * g <= 32) that split the staged sources.  Each
+// 32-source chunk's FP32 partial sum is added with Kahan compensation.  The
+// result is stored (each particle of a box with targets once; boxes without
+// targets are left as they are).  CLAMP: floor r^2 at kMinR2, needed only when
+// eps^2 < kMinR2 (a zero-distance pair without softening).  UQ: every particle
+// of the tree carries the same charge Q (box_relative_kernel found no other),
+// so the pair weight is r^-3 alone, the sums are scaled by the target's own
 // charge (= Q) at the end, and padding sources sit far away (r^-3 underflows
 // to zero) instead of carrying zero charge.
 constexpr int kFarDirectCap = 128;  // far-direct source boxes per leaf box
