@@ -20,27 +20,35 @@ constexpr int kRedThreads = 256;
 
 __device__ __forceinline__ bool is_source(int32_t s) { return s == 1 || s == 2; }
 
-// Per-block min/max of source positions (status 1 or 2).
+// A double's bits as a signed integer whose order is the double's order
+// (non-NaN values); the map is its own inverse.  Min / max on these run on
+// the integer pipe: GB300's FP64 pipe issues ~2 operations per clock per SM,
+// which made the FP64 fmin / fmax the bound of this reduction.
+__device__ __forceinline__ long long ordered_bits(long long b) { return b ^ ((b >> 63) & 0x7fffffffffffffffLL); }
+
+// Per-block min/max of source positions (status 1 or 2), exact.
 __global__ void bbox_partial(const double *__restrict__ x, const double *__restrict__ y,
                              const double *__restrict__ z, const int32_t *__restrict__ st,
                              int64_t n, double *__restrict__ out) {
-    double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+    const long long lo0 = ordered_bits(__double_as_longlong(1e300)), hi0 = ordered_bits(__double_as_longlong(-1e300));
+    long long mn[3] = {lo0, lo0, lo0}, mx[3] = {hi0, hi0, hi0};
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
          i += (int64_t)gridDim.x * blockDim.x) {
         if (!is_source(st[i])) continue;
-        double p[3] = {x[i], y[i], z[i]};
+        const long long p[3] = {ordered_bits(__double_as_longlong(x[i])), ordered_bits(__double_as_longlong(y[i])),
+                                ordered_bits(__double_as_longlong(z[i]))};
 #pragma unroll
         for (int d = 0; d < 3; d++) {
-            mn[d] = fmin(mn[d], p[d]);
-            mx[d] = fmax(mx[d], p[d]);
+            mn[d] = min(mn[d], p[d]);
+            mx[d] = max(mx[d], p[d]);
         }
     }
-    __shared__ double sh[6][kRedThreads / 32];
+    __shared__ long long sh[6][kRedThreads / 32];
 #pragma unroll
     for (int d = 0; d < 3; d++) {
         for (int o = 16; o > 0; o >>= 1) {
-            mn[d] = fmin(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
-            mx[d] = fmax(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
+            mn[d] = min(mn[d], __shfl_xor_sync(0xffffffffu, mn[d], o));
+            mx[d] = max(mx[d], __shfl_xor_sync(0xffffffffu, mx[d], o));
         }
     }
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -53,9 +61,9 @@ __global__ void bbox_partial(const double *__restrict__ x, const double *__restr
     __syncthreads();
     if (threadIdx.x < 6) {
         const int d = threadIdx.x;
-        double v = d < 3 ? 1e300 : -1e300;
-        for (int k = 0; k < (int)(blockDim.x >> 5); k++) v = d < 3 ? fmin(v, sh[d][k]) : fmax(v, sh[d][k]);
-        out[blockIdx.x * 6 + d] = v;
+        long long v = d < 3 ? lo0 : hi0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) v = d < 3 ? min(v, sh[d][k]) : max(v, sh[d][k]);
+        out[blockIdx.x * 6 + d] = __longlong_as_double(ordered_bits(v));
     }
 }
 
@@ -134,9 +142,12 @@ __global__ void morton_keys(const double *__restrict__ x, const double *__restri
     uint32_t c[3];
 #pragma unroll
     for (int d = 0; d < 3; d++) {
-        double f = floor(p[d] * inv);
-        f = fmin(fmax(f, 0.0), (double)((1u << kMortonBits) - 1));
-        c[d] = (uint32_t)f;
+        // floor(p * inv) clamped to [0, 2^21 - 1]: one round-down conversion
+        // (PTX float-to-integer conversions saturate) and an integer clamp give
+        // the same cell as floor, fmax and fmin in FP64, with half the FP64
+        // operations of the key
+        const int f = __double2int_rd(p[d] * inv);
+        c[d] = (uint32_t)min(max(f, 0), (int)((1u << kMortonBits) - 1));
     }
     // bit order within a level: x lowest, then y, then z
     keys[i] = spread3(c[0]) | (spread3(c[1]) << 1) | (spread3(c[2]) << 2);
