@@ -10,13 +10,14 @@ accumulation and integration).  A step = drift dt/2 + force evaluation + kick
   value          particle-steps/s with the plume resident in HBM (CUDA events
                  on the context stream around each step; L2 flushed between
                  steps by writing 512 MB)
-  e2e            same metric through the C ABI with host buffers: per step,
-                 upload of the state from pinned host memory, one step, and
-                 download of positions / velocities / status
+  e2e            same metric over the same steps from the same state, through
+                 the C ABI with host buffers: per step, upload of the current
+                 state from pinned host memory, one step, and download of
+                 positions / velocities / status (the next step's upload)
   fp64_direct    the plain FP64 GPU direct-sum path on the same GPU (measured
                  at N = 131072, scaled by N^2 to the workload's N)
   force_err      per-particle relative L2 of the FMM acceleration against the
-                 FP64 GPU direct sum on sampled targets
+                 FP64 GPU direct sum on 512 sampled targets
   cpu_baseline   the C oracle's FP64 direct sum (the reference's direct sum
                  restated; the reference's own FMM crashes at this N) on a
                  bounded sample of targets, all host threads
@@ -42,10 +43,10 @@ sys.path.insert(0, os.path.join(ROOT, "solveit-code_gb300"))
 import plume  # noqa: E402
 
 METRIC = "particle-steps/s, mixed-prec vs plain FP64 path, same GB300, force err <=1e-5"
-# DRAM bytes (read + write) of one near-field launch of the fmm_n1m workload at
-# root scale 1.375 (leaf level 12), from one ncu capture
-# (profiles/p2p_kernel_fmm_n1m.md)
-P2P_TRAFFIC_BYTES = 30337280 + 143360
+# DRAM bytes (read + write) of one near-field launch of the fmm_n1m workload,
+# from one ncu capture, with the root scale and leaf level it was taken at:
+# the roofline reports it only for a run at that same configuration
+P2P_TRAFFIC = {"bytes": 30337280 + 143360, "root_scale": 1.375, "leaf_level": 12}
 EPS2 = 1e-20
 DT = 1e-13
 EZ = 1e8
@@ -141,6 +142,32 @@ def sample_clocks_stop(p, f, gpu_index):
             "samples": len(sm)}
 
 
+def fp32_peak_tflops(local, sm_max_mhz):
+    """FP32 FMA rate of this device: SMs (queried) x 128 lanes x 2 flop x the
+    measured maximum SM clock."""
+    import torch
+
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    return sms * 128 * 2 * sm_max_mhz * 1e6 / 1e12, sms
+
+
+def fp64_sampled_accel(sv, local, cur, targets, sym=0):
+    """The plain FP64 GPU direct sum at the sampled targets of a plume (the
+    other particles act as sources only)."""
+    s2 = np.where(cur["status"] == 1, 2, cur["status"]).astype(np.int32)
+    s2[targets] = cur["status"][targets]
+    with sv.ForceMethod(softening2=EPS2, method=sv.DIRECT, precision=sv.FP64, device=local, symmetry=sym) as ref:
+        ref.upload(dict(cur, status=s2))
+        return ref.accel()[targets]
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
 def cpu_baseline(state, n_sample, threads):
     """The reference's direct sum, restated in C (bit-exact with the reference
     on its FP32 vec4 state), on n_sample targets against all sources, all host
@@ -188,7 +215,14 @@ def run_reference(args, wl, rank, world):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": {"workload": args.workload, "desc": wl["desc"], "n": wl["n"]},
             "cpu_baseline": cb, "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
-                                        "d2h_bytes_per_step": 0}}
+                                        "d2h_bytes_per_step": 0},
+            "extrapolated_from": {"targets_timed": n_sample, "targets_total": wl["n"],
+                                  "fraction": n_sample / wl["n"],
+                                  "how": "one force evaluation of the timed targets against all sources per "
+                                         "step; particle-steps/s = targets / time (the per-target cost does not "
+                                         "depend on how many targets are timed)"},
+            "comparison": "CPU O(N^2) direct sum (the reference's direct method; its FMM overflows its buffers "
+                          "at this plume size): a ratio against the GPU FMM is algorithmic as well as hardware"}
     print(json.dumps(line), flush=True)
 
 
@@ -200,7 +234,6 @@ def run_batch(args, wl, rank, world, local):
 
     import solveit_gpu as sv
 
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
     torch.cuda.set_device(local)
     dist = None
     if world > 1:
@@ -219,6 +252,8 @@ def run_batch(args, wl, rank, world, local):
     fm.leapfrog(args.warmup, DT, t)
     t += args.warmup * DT
     fm.sync()
+    t_start = t
+    snap = fm.download()  # the state at the start of the timed window (the e2e run repeats the window)
     clk_p, clk_f = sample_clocks_start()
     if dist:
         dist.barrier()
@@ -245,49 +280,55 @@ def run_batch(args, wl, rank, world, local):
         fm.close()
         return
 
-    # ---- end to end: upload of the batch state from pinned host memory (same
-    # shape: the plan and graphs are kept), one step, download
+    # ---- end to end: the same steps again from the same state, through the C
+    # ABI with host buffers: each step uploads the current batch state from
+    # pinned host memory (same shape: the plan and graphs are kept), runs one
+    # step and downloads positions, velocities and status into the buffers the
+    # next step uploads
     cat, _ = plume.concat(states)
     pin = {k: torch.empty(cat[k].shape, dtype=torch.float64 if cat[k].dtype == np.float64 else torch.int32,
                           pin_memory=True) for k in ("x", "v", "q", "m", "status", "t_inj")}
-    for k in pin:
-        pin[k].numpy()[...] = cat[k]
     cnt = np.ascontiguousarray(counts, np.int64)
     meth = np.ascontiguousarray(methods, np.int32)
     sym = np.ascontiguousarray(syms, np.int32)
-    xo = torch.empty((n, 3), dtype=torch.float64, pin_memory=True)
-    vo = torch.empty((n, 3), dtype=torch.float64, pin_memory=True)
-    so = torch.empty((n,), dtype=torch.int32, pin_memory=True)
     L = sv.load()
 
     def ptr(tn):
         return C.c_void_p(tn.data_ptr())
 
-    def e2e_step(t0):
-        rc = L.sv_upload_batch(fm.h, len(states), cnt.ctypes.data_as(C.c_void_p), meth.ctypes.data_as(C.c_void_p),
-                               sym.ctypes.data_as(C.c_void_p), ptr(pin["x"]), ptr(pin["v"]), ptr(pin["q"]),
-                               ptr(pin["m"]), ptr(pin["status"]), ptr(pin["t_inj"]))
-        rc = rc or L.sv_leapfrog(fm.h, 1, DT, t0)
-        rc = rc or L.sv_download(fm.h, ptr(xo), ptr(vo), ptr(so))
-        if rc != 0:
-            raise RuntimeError(L.sv_last_error(fm.h).decode())
+    def reset_pins():
+        for k in ("q", "m", "t_inj"):
+            pin[k].numpy()[...] = cat[k]
+        pin["x"].numpy()[...] = snap[0]
+        pin["v"].numpy()[...] = snap[1]
+        pin["status"].numpy()[...] = snap[2]
 
-    for _ in range(2):
-        e2e_step(0.0)
+    def e2e_step(t0):
+        for rc in (L.sv_upload_batch(fm.h, len(states), cnt.ctypes.data_as(C.c_void_p),
+                                     meth.ctypes.data_as(C.c_void_p), sym.ctypes.data_as(C.c_void_p),
+                                     ptr(pin["x"]), ptr(pin["v"]), ptr(pin["q"]), ptr(pin["m"]),
+                                     ptr(pin["status"]), ptr(pin["t_inj"])),
+                   L.sv_leapfrog(fm.h, 1, DT, t0),
+                   L.sv_download(fm.h, ptr(pin["x"]), ptr(pin["v"]), ptr(pin["status"]))):
+            if rc != 0:
+                raise RuntimeError(L.sv_last_error(fm.h).decode())
+
+    reset_pins()
+    e2e_step(t_start)  # warm-up of the host path, then back to the window's first state
+    reset_pins()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     w0 = time.perf_counter()
-    e2e_steps = max(3, args.steps // 4)
-    for k in range(e2e_steps):
-        e2e_step(k * DT)
+    for k in range(args.steps):
+        e2e_step(t_start + k * DT)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - w0
     if dist:
         e2e_s = max_over_ranks(e2e_s, dist, f"cuda:{local}")
-    e2e = {"value": world * n * e2e_steps / e2e_s, "unit": "particle-steps/s",
+    e2e = {"value": world * n * args.steps / e2e_s, "unit": "particle-steps/s",
            "h2d_bytes_per_step": n * (3 * 8 + 3 * 8 + 8 + 8 + 4 + 8), "d2h_bytes_per_step": n * (3 * 8 + 3 * 8 + 4),
-           "steps": e2e_steps}
+           "steps": args.steps, "window": "the timed steps of value, from the same state"}
     line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 pair/expansion arithmetic, f64 state and integration",
@@ -302,13 +343,8 @@ def run_batch(args, wl, rank, world, local):
                              "L2"},
             "clocks": clocks, "e2e": e2e, "gpu_launches": int(launches), "tuned_force_ms": tuned_ms}
     if rank == 0:
-        peaks = {}
-        try:
-            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-        except Exception:
-            pass
-        sm_max = peaks.get("sm_max_mhz", 2070.0)
-        fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+        sm_max = measured_peaks().get("sm_max_mhz", 2070.0)
+        fp32_peak, sms = fp32_peak_tflops(local, sm_max)
         p = wl["order"]
         m2l_flop = 8.0 * (2 * sum((k + 1) * (2 * k + 1) for k in range(p)) +
                           sum(p - k for j in range(p) for k in range(j + 1)))
@@ -318,10 +354,10 @@ def run_batch(args, wl, rank, world, local):
         line["roofline"] = {"kernel": "whole step (direct pairs + P2P pairs at 20 flop, M2L at its flop count, "
                                       "P2M + L2P)", "bound": "fp32", "achieved": achieved, "peak": fp32_peak,
                             "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
-                            "pairs_per_step": info.direct_pairs + info.fmm_pairs, "m2l_per_step": info.fmm_m2l}
-        # force error on sampled targets of a few plumes against the FP64 oracle
-        import oracle_py as O
-
+                            "pairs_per_step": info.direct_pairs + info.fmm_pairs, "m2l_per_step": info.fmm_m2l,
+                            "peak_source": f"FP32 FMA rate: {sms} SMs x 128 lanes x 2 flop x sm_max_mhz "
+                                           f"{sm_max:.0f} of MEASURED_PEAKS.json"}
+        # force error on sampled targets of a few plumes against the plain FP64 GPU direct sum
         x, v, stt = fm.download()
         a = fm.accel()
         offs = np.concatenate([[0], np.cumsum(counts)])
@@ -331,7 +367,7 @@ def run_batch(args, wl, rank, world, local):
             s0, s1 = offs[i], offs[i + 1]
             cur = dict(states[i], x=x[s0:s1], v=v[s0:s1], status=stt[s0:s1])
             tg = np.sort(rng.choice(s1 - s0, min(64, s1 - s0), replace=False))
-            ref = O.direct_f64(cur, EPS2, sym=syms[i], targets=tg, threads=os.cpu_count() or 1)
+            ref = fp64_sampled_accel(sv, local, cur, tg, sym=int(syms[i]))
             d = np.sum((a[s0:s1][tg] - ref) ** 2, axis=1) / np.sum(ref ** 2, axis=1)
             errs[f"plume{i}_n{s1 - s0}_{'fmm' if methods[i] == 2 else 'direct'}_{'rot4' if syms[i] else 'none'}"] = \
                 float(np.sqrt(np.mean(d)))
@@ -352,17 +388,17 @@ def run_batch(args, wl, rank, world, local):
         line["fp64_direct"] = {"value": n / t_all, "unit": "particle-steps/s",
                                "measured": f"FP64 direct force at N={counts[big]}: {t_big * 1e3:.1f} ms "
                                            f"({rate:.3g} pairs/s), applied to the batch's {pairs_all:.3g} "
-                                           f"pairs per step (x4 for the rotational plumes)"}
+                                           f"pairs per step (x4 for the rotational plumes)",
+                               "extrapolated_from": {"plume_measured": big, "n_measured": int(counts[big]),
+                                                     "pairs_measured": float(counts[big]) ** 2,
+                                                     "pairs_applied": pairs_all}}
         line["speedup_vs_fp64_direct"] = value / world / (n / t_all)
         # CPU baseline: the oracle's bit-exact restatement of the reference direct sum on a target sample,
         # as a pair rate applied to the whole batch
-        pos4, vel4, acc4, _ = plume.to_ref32(states[big])
         threads = os.cpu_count() or 1
-        O.direct_ref32(pos4, vel4, acc4, EPS2, i_range=(0, 64), threads=threads)
         ns = 2048
-        tc = time.perf_counter()
-        O.direct_ref32(pos4, vel4, acc4, EPS2, i_range=(0, ns), threads=threads)
-        tc = time.perf_counter() - tc
+        cb = cpu_baseline(states[big], ns, threads)
+        tc = ns / cb["value"]
         cpu_rate = ns * counts[big] / tc
         line["cpu_baseline"] = {"value": n / (pairs_all / cpu_rate), "unit": "particle-steps/s", "cores": threads,
                                 "kind": "port",
@@ -509,6 +545,8 @@ def run_ours(args, wl, rank, world, local):
         fm.leapfrog(1, DT, t)
         t += DT
     fm.sync()
+    t_start = t
+    snap = fm.download()  # the state at the start of the timed window (the e2e run repeats the window)
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     phase_ms = np.zeros(8)
     clk_p, clk_f = sample_clocks_start()
@@ -545,14 +583,12 @@ def run_ours(args, wl, rank, world, local):
                               "phases_ms": list(map(float, phase_ms)), "timed_only": True}), flush=True)
         fm.close()
         return
-    # ---- end to end through the C ABI with pinned host buffers
+    # ---- end to end through the C ABI with pinned host buffers: the same
+    # steps again from the same state; each step uploads the current state,
+    # runs one step and downloads positions, velocities and status into the
+    # buffers the next step uploads
     pin = {k: torch.empty(st[k].shape, dtype=torch.float64 if st[k].dtype == np.float64 else torch.int32,
                           pin_memory=True) for k in ("x", "v", "q", "m", "status", "t_inj")}
-    for k in pin:
-        pin[k].numpy()[...] = st[k]
-    xo = torch.empty((n, 3), dtype=torch.float64, pin_memory=True)
-    vo = torch.empty((n, 3), dtype=torch.float64, pin_memory=True)
-    so = torch.empty((n,), dtype=torch.int32, pin_memory=True)
     import ctypes as C
 
     L = sv.load()
@@ -560,22 +596,30 @@ def run_ours(args, wl, rank, world, local):
     def ptr(tn):
         return C.c_void_p(tn.data_ptr())
 
-    def e2e_step(t0):
-        L.sv_upload(fm.h, n, ptr(pin["x"]), ptr(pin["v"]), ptr(pin["q"]), ptr(pin["m"]), ptr(pin["status"]),
-                    ptr(pin["t_inj"]))
-        L.sv_leapfrog(fm.h, 1, DT, t0)
-        rc = L.sv_download(fm.h, ptr(xo), ptr(vo), ptr(so))
-        if rc != 0:
-            raise RuntimeError(L.sv_last_error(fm.h).decode())
+    def reset_pins():
+        for k in ("q", "m", "t_inj"):
+            pin[k].numpy()[...] = st[k]
+        pin["x"].numpy()[...] = snap[0]
+        pin["v"].numpy()[...] = snap[1]
+        pin["status"].numpy()[...] = snap[2]
 
-    for _ in range(max(1, args.warmup // 2)):
-        e2e_step(0.0)
+    def e2e_step(t0):
+        for rc in (L.sv_upload(fm.h, n, ptr(pin["x"]), ptr(pin["v"]), ptr(pin["q"]), ptr(pin["m"]),
+                               ptr(pin["status"]), ptr(pin["t_inj"])),
+                   L.sv_leapfrog(fm.h, 1, DT, t0),
+                   L.sv_download(fm.h, ptr(pin["x"]), ptr(pin["v"]), ptr(pin["status"]))):
+            if rc != 0:
+                raise RuntimeError(L.sv_last_error(fm.h).decode())
+
+    reset_pins()
+    e2e_step(t_start)  # warm-up of the host path, then back to the window's first state
+    reset_pins()
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     e0 = time.perf_counter()
     for k in range(args.steps):
-        e2e_step(k * DT)
+        e2e_step(t_start + k * DT)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - e0
     if dist:
@@ -583,7 +627,7 @@ def run_ours(args, wl, rank, world, local):
     h2d = n * (3 * 8 + 3 * 8 + 8 + 8 + 4 + 8)
     d2h = n * (3 * 8 + 3 * 8 + 4)
     e2e = {"value": world * n * args.steps / e2e_s, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": d2h}
+           "d2h_bytes_per_step": d2h, "window": "the timed steps of value, from the same state"}
 
     line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -603,30 +647,26 @@ def run_ours(args, wl, rank, world, local):
         # ---- phase breakdown and roofline of the dominant kernel
         names = ["sort", "tree", "lists", "upward_p2m_m2m", "downward_m2l_l2l", "l2p", "near_p2p", "scatter"]
         line["phases_ms"] = {nm: round(float(v), 4) for nm, v in zip(names, phase_ms)}
-        peaks = {}
-        try:
-            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-        except Exception:
-            pass
-        sm_max = peaks.get("sm_max_mhz", 2070.0)
-        fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+        sm_max = measured_peaks().get("sm_max_mhz", 2070.0)
+        fp32_peak, sms = fp32_peak_tflops(local, sm_max)
         if wl["method"] == "fmm":
             near_flop = 20.0 * stats.pair_interactions
             dom_ms = phase_ms[6]
             achieved = near_flop / (dom_ms * 1e-3) / 1e12
             m2l_flop = stats.flops_algorithmic - near_flop - n * 8.0 * (wl["order"] * (wl["order"] + 1) / 2) * 4
+            same_cfg = root_scale == P2P_TRAFFIC["root_scale"] and stats.levels == P2P_TRAFFIC["leaf_level"]
             line["roofline"] = {"kernel": "p2p_kernel (near field, 20 flop/pair)", "bound": "fp32",
                                 "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                                "frac": achieved / fp32_peak, "traffic": P2P_TRAFFIC_BYTES,
+                                "frac": achieved / fp32_peak,
+                                "traffic": P2P_TRAFFIC["bytes"] if same_cfg else None,
                                 "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum of one p2p_kernel "
-                                                  "launch at root scale 1.375 (leaf level 12, the 4th force "
-                                                  "evaluation of this workload), one ncu capture, "
-                                                  "profiles/p2p_kernel_fmm_n1m.md",
-                                "solo": "the same launch alone under ncu: 1.059 ms, 42.5 TFLOP/s, 0.53 of the FP32 "
-                                        "FMA rate (profiles/p2p_kernel_fmm_n1m.md)",
-                                "peak_source": "FP32 FMA rate 152 SMs x 128 lanes x 2 flop x sm_max_mhz of "
-                                               "MEASURED_PEAKS.json (no FP32 peak is measured there; the "
-                                               "kernel runs on the FP32 pipe, not the tensor cores)",
+                                                  f"launch at root scale {P2P_TRAFFIC['root_scale']} (leaf level "
+                                                  f"{P2P_TRAFFIC['leaf_level']}), one ncu capture of this "
+                                                  "workload; null when this run's root scale or leaf level differ "
+                                                  f"(this run: {root_scale}, level {stats.levels})",
+                                "peak_source": f"FP32 FMA rate {sms} SMs x 128 lanes x 2 flop x sm_max_mhz "
+                                               f"{sm_max:.0f} of MEASURED_PEAKS.json (no FP32 peak is measured "
+                                               "there; the kernel runs on the FP32 pipe, not the tensor cores)",
                                 "timing": "CUDA events on the near field's own stream; the kernel shares the "
                                           "GPU with the concurrent upward / downward passes, whose stream has "
                                           "the higher priority, so the span includes their work",
@@ -643,18 +683,13 @@ def run_ours(args, wl, rank, world, local):
             x, v, stt = fm.download()
             cur = dict(st, x=x, v=v, status=stt)
             a_fmm = fm.accel()
-            rng = np.random.default_rng(7)
-            tg = rng.choice(n, 64, replace=False)
-            cur2 = dict(cur)
-            s2 = np.where(cur["status"] == 1, 2, cur["status"]).astype(np.int32)
-            s2[tg] = cur["status"][tg]
-            cur2["status"] = s2
-            with sv.ForceMethod(softening2=EPS2, method=sv.DIRECT, precision=sv.FP64, device=local) as ref:
-                ref.upload(cur2)
-                a_ref = ref.accel()[tg]
+            tg = np.sort(np.random.default_rng(7).choice(n, 512, replace=False))
+            a_ref = fp64_sampled_accel(sv, local, cur, tg)
             d = np.sum((a_fmm[tg] - a_ref) ** 2, axis=1) / np.sum(a_ref ** 2, axis=1)
             line["force_err_rel_l2"] = float(np.sqrt(np.mean(d)))
             line["force_err_max"] = float(np.sqrt(np.max(d)))
+            line["force_err_sample"] = ("512 random targets of the state after the timed steps, against the "
+                                        "plain FP64 GPU direct sum (pinned to the CPU oracle by the GPU tests)")
             # ---- plain FP64 GPU direct path on the same GPU
             m = 131072
             sub = {k: (st[k][:m] if hasattr(st[k], "__len__") else st[k]) for k in st}
@@ -671,7 +706,10 @@ def run_ours(args, wl, rank, world, local):
             line["fp64_direct"] = {"value": n / t_n, "unit": "particle-steps/s",
                                    "measured": f"one FP64 direct leapfrog step at N={m}: {t_m * 1e3:.1f} ms, "
                                                f"scaled by (N/{m})^2 to N={n}",
-                                   "ms_per_step_at_n": t_n * 1e3}
+                                   "ms_per_step_at_n": t_n * 1e3,
+                                   "extrapolated_from": {"n_measured": m, "n": n, "scaled_by": f"(N/{m})^2",
+                                                         "timing": "one step, host wall clock around a "
+                                                                   "synchronised call"}}
             line["speedup_vs_fp64_direct"] = value / world / (n / t_n)
         # ---- CPU baseline (C oracle FP64 direct sum, bounded sample)
         threads = os.cpu_count() or 1

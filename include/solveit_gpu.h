@@ -391,8 +391,14 @@ SV_API sv_status sv_get_outliers(sv_ctx *ctx, int32_t *flags, int64_t *count);
  * (particles.cpp:535-578 with the halving of integration_schemes.cpp:815). */
 SV_API sv_status sv_energy(sv_ctx *ctx, double *ke, double *pe);
 
-/* Per-particle relative-L2 accuracy metric (integration_schemes.cpp:411-461)
- * of the device acceleration against a host reference (3n, m/s^2). */
+/* Per-particle relative-L2 accuracy metric of Integrator::compareAcceleration
+ * (integration_schemes.cpp:411-461) of the last evaluation's acceleration
+ * against a host reference ref3 (3n interleaved, m/s^2), computed on the
+ * device in FP64 over that evaluation's window [first, last) (the whole plume
+ * after sv_leapfrog or a batch): l2 = sqrt(mean over inbound k of
+ * |a_k - ref_k|^2 / |ref_k|^2), maxl2 = the largest per-particle term's square
+ * root, argmax = its index (the first of equal largest terms; 0 when none is
+ * positive).  maxl2 and argmax may be null. */
 SV_API sv_status sv_compare_accel(sv_ctx *ctx, const double *ref3, double *l2, double *maxl2,
                            int64_t *argmax);
 
@@ -477,9 +483,15 @@ SV_API sv_status sv_batch_get_info(const sv_ctx *ctx, sv_batch_info *out);
  * cudaStream_t (NULL = legacy default stream).  Working storage is one static
  * device array of SV_NOALLOC_SCRATCH_BYTES that each GPU loading the library
  * holds until exit; n above SV_NOALLOC_MAX_N returns SV_ERR_CAPACITY.  The
- * first call on a device looks the array up (cudaGetSymbolAddress) and must
- * come before any stream capture.  Calls whose work overlaps on the GPU race
- * on the shared array. */
+ * first call on a device is its set-up call: it looks the array up
+ * (cudaGetSymbolAddress) and, under lazy module loading (the CUDA default),
+ * loads the library's device code on that device, which commits the array's
+ * memory and can synchronise the device; make it during set-up, before any
+ * stream capture.  The looked-up address is kept for the life of the process,
+ * so after a cudaDeviceReset the entry point must not be called on that device
+ * again.  A CUDA error already pending on the calling thread makes the call
+ * return SV_ERR_CUDA without work and is left pending.  Calls whose work
+ * overlaps on the GPU race on the shared array. */
 #define SV_NOALLOC_MAX_N 262144
 #define SV_NOALLOC_SCRATCH_BYTES (40u << 20)
 SV_API sv_status sv_direct_accel_noalloc(int64_t n, const double *x3, const double *q, const double *m_amu,

@@ -36,10 +36,14 @@
 //          (dkd with events=1: then int32 count, count 40-byte event records
 //          as ChargedParticles::writeToEventsFile wrote them)
 //          (grid mode: int32 count, int32 points[3*count] in the Grid's order)
+// stderr : the single-evaluation modes (direct, bh, fmm) print
+//          update_s=<wall seconds of updateAcceleration()> threads=<t> n=<n>
 #include "force_calculation_methods.h"
 #include "integration_schemes.h"
 
 #include <dirent.h>
+
+#include <chrono>
 
 #include <cstdio>
 #include <cstdlib>
@@ -334,7 +338,10 @@ int main(int argc, char **argv) {
             drift_new(tpos, dt / 2);
         }
     } else {
+        const auto t0 = std::chrono::steady_clock::now();
         fm->updateAcceleration();
+        const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        std::fprintf(stderr, "update_s=%.6f threads=%d n=%d\n", sec, threads, n);
     }
 
     FILE *fo = std::fopen(argv[3], "wb");

@@ -367,7 +367,7 @@ __global__ void interleave(const double *__restrict__ x, const double *__restric
 int grid_of(int64_t n) { return (int)((n + 255) / 256 > 0 ? (n + 255) / 256 : 1); }
 int stream_grid(int64_t n) {
     const int64_t b = (n + 255) / 256;
-    return (int)(b < 1 ? 1 : (b > 16 * kNumSMs ? 16 * kNumSMs : b));
+    return (int)(b < 1 ? 1 : (b > 16 * device_sms() ? 16 * device_sms() : b));
 }
 
 sv_status copy_state(sv_ctx *c, double *dst) {
@@ -401,7 +401,7 @@ sv_status jtv_add(sv_ctx *c, const double *lax, const double *lay, const double 
     adj_gather_u<<<grid_of(n), 256, 0, c->stream>>>(S.idx, n, S.qm, lax, lay, laz, ux, uy, uz, umax);
     SV_LAUNCHED(c);
     const int tblocks = div_up(n, kTPB * kTPT);
-    int splits = div_up(8 * kNumSMs, tblocks);
+    int splits = div_up(8 * device_sms(), tblocks);
     const int max_splits = div_up(n, kTile);
     if (splits > max_splits) splits = max_splits;
     if (splits < 1) splits = 1;

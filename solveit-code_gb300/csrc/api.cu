@@ -4,10 +4,27 @@
 #include <cstdarg>
 #include <vector>
 #include <algorithm>
+#include <atomic>
 
 #include "sv_internal.cuh"
 
 namespace sv {
+
+int device_sms() {
+    constexpr int kMaxDevices = 64;
+    static std::atomic<int> cache[kMaxDevices];  // 0: not queried yet
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) dev = -1;
+    if (dev >= 0) {
+        const int v = cache[dev].load(std::memory_order_relaxed);
+        if (v > 0) return v;
+    }
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev < 0 ? 0 : dev) != cudaSuccess || sms < 1)
+        sms = 1;  // no device answers: launches stay valid, only smaller
+    if (dev >= 0) cache[dev].store(sms, std::memory_order_relaxed);
+    return sms;
+}
 
 sv_status set_error(sv_ctx *c, sv_status s, const char *fmt, ...) {
     if (c) {
@@ -320,6 +337,96 @@ sv_status check_params(sv_ctx *c, const sv_params *p) {
 
 int grid_of(int64_t n) { return (int)((n + 255) / 256 > 0 ? (n + 255) / 256 : 1); }
 
+// Accuracy metric of Integrator::compareAcceleration (integration_schemes.cpp:
+// 411-461) over the window [first, last) of the last evaluation: for every
+// inbound particle k, r_k = |a_k - ref_k|^2 / |ref_k|^2 (0 when both are 0);
+// the metric is sqrt(mean r_k), the largest sqrt(r_k) and its index (the
+// first index among equal largest terms, as the reference's strict > over
+// ascending k keeps it; index 0 when no term is positive).  Each term is
+// evaluated in FP64 without contraction, so terms, maximum and index equal a
+// sequential host loop's; the sum is taken per block, then over blocks in
+// block order.
+constexpr int kCmpThreads = 256;
+
+__global__ void __launch_bounds__(kCmpThreads)
+compare_partial(const double *__restrict__ ax, const double *__restrict__ ay, const double *__restrict__ az,
+                const double *__restrict__ ref3, const int32_t *__restrict__ status, int64_t first, int64_t last,
+                double *__restrict__ psum, double *__restrict__ pmax, long long *__restrict__ parg,
+                long long *__restrict__ pcnt) {
+    double sum = 0.0, mx = 0.0;
+    long long am = -1, cnt = 0;
+    for (int64_t k = first + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < last;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        if (status[k] != 1) continue;
+        cnt++;
+        const double a[3] = {ax[k], ay[k], az[k]};
+        double d = 0.0, nr = 0.0;
+#pragma unroll
+        for (int e = 0; e < 3; e++) {
+            const double r = ref3[3 * k + e];
+            const double df = __dadd_rn(a[e], -r);
+            d = __dadd_rn(d, __dmul_rn(df, df));
+            nr = __dadd_rn(nr, __dmul_rn(r, r));
+        }
+        const double t = (nr == 0.0 && d == 0.0) ? 0.0 : __ddiv_rn(d, nr);
+        sum = __dadd_rn(sum, t);
+        if (t > mx) {  // ascending k per thread: the first of equal terms stays
+            mx = t;
+            am = k;
+        }
+    }
+    __shared__ double s_sum[kCmpThreads], s_max[kCmpThreads];
+    __shared__ long long s_arg[kCmpThreads], s_cnt[kCmpThreads];
+    s_sum[threadIdx.x] = sum;
+    s_max[threadIdx.x] = mx;
+    s_arg[threadIdx.x] = am;
+    s_cnt[threadIdx.x] = cnt;
+    __syncthreads();
+    for (int w = kCmpThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            const int o = threadIdx.x + w;
+            s_sum[threadIdx.x] = __dadd_rn(s_sum[threadIdx.x], s_sum[o]);
+            s_cnt[threadIdx.x] += s_cnt[o];
+            const double m0 = s_max[threadIdx.x], m1 = s_max[o];
+            const long long a0 = s_arg[threadIdx.x], a1 = s_arg[o];
+            if (m1 > m0 || (m1 == m0 && a1 >= 0 && (a0 < 0 || a1 < a0))) {
+                s_max[threadIdx.x] = m1;
+                s_arg[threadIdx.x] = a1;
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        psum[blockIdx.x] = s_sum[0];
+        pmax[blockIdx.x] = s_max[0];
+        parg[blockIdx.x] = s_arg[0];
+        pcnt[blockIdx.x] = s_cnt[0];
+    }
+}
+
+// out[0] sum of the terms, out[1] largest term, out[2] its index, out[3] count
+// (the last two as 64-bit integers)
+__global__ void compare_final(int blocks, const double *__restrict__ psum, const double *__restrict__ pmax,
+                              const long long *__restrict__ parg, const long long *__restrict__ pcnt,
+                              double *__restrict__ out) {
+    if (threadIdx.x != 0) return;
+    double sum = 0.0, mx = 0.0;
+    long long am = -1, cnt = 0;
+    for (int b = 0; b < blocks; b++) {
+        sum = __dadd_rn(sum, psum[b]);
+        cnt += pcnt[b];
+        if (pmax[b] > mx || (pmax[b] == mx && parg[b] >= 0 && (am < 0 || parg[b] < am))) {
+            mx = pmax[b];
+            am = parg[b];
+        }
+    }
+    if (!(mx > 0.0)) am = 0;
+    out[0] = sum;
+    out[1] = mx;
+    reinterpret_cast<long long *>(out)[2] = am;
+    reinterpret_cast<long long *>(out)[3] = cnt;
+}
+
 }  // namespace
 }  // namespace sv
 
@@ -417,6 +524,7 @@ sv_status sv_create(const sv_params *p, sv_ctx **out) {
     c->P = *p;
     c->device = p->device;
     cudaError_t e = cudaSetDevice(c->device);
+    if (e == cudaSuccess) (void)device_sms();  // query the SM count once, outside any stream capture
     // the context's stream at the highest priority: the FMM's second stream
     // (the near field, which fills every SM) yields to it as its blocks retire
     int prio_lo = 0, prio_hi = 0;
@@ -627,6 +735,8 @@ sv_status sv::compute_accel_device(sv_ctx *c, int64_t first, int64_t last) {
         SV_TRY(batch_accel(c));
         SV_CK(c, cudaEventRecord(c->ev_end, c->stream));
         c->have_accel = true;
+        c->acc_first = 0;
+        c->acc_last = n;
         return SV_OK;
     }
     SV_CK(c, cudaEventRecord(c->ev_begin, c->stream));
@@ -683,6 +793,8 @@ sv_status sv::compute_accel_device(sv_ctx *c, int64_t first, int64_t last) {
     SV_TRY(st_run);
     SV_CK(c, cudaEventRecord(c->ev_end, c->stream));
     c->have_accel = true;
+    c->acc_first = first;
+    c->acc_last = last;
     return SV_OK;
 }
 
@@ -850,32 +962,33 @@ sv_status sv_fmm_tune(sv_ctx *c, double *best_ms) {
 sv_status sv_compare_accel(sv_ctx *c, const double *ref3, double *l2, double *maxl2, int64_t *argmax) {
     if (!c || !ref3 || !l2) return SV_ERR_INVALID;
     if (!c->have_accel) return set_error(c, SV_ERR_STATE, "no acceleration computed");
-    const int64_t n = c->n;
-    std::vector<double> a(3 * n);
-    std::vector<int32_t> st(n);
-    void *stg = nullptr;
-    SV_TRY(stage_bytes(c, sizeof(double) * 3 * n, &stg));
-    pack_accel<<<grid_of(n), 256, 0, c->stream>>>(c->ax, c->ay, c->az, c->status, 0, n, n, (double *)stg);
-    SV_LAUNCHED(c);
-    SV_CK(c, cudaMemcpyAsync(a.data(), stg, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c->stream));
-    SV_CK(c, cudaMemcpyAsync(st.data(), c->status, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, c->stream));
-    SV_CK(c, cudaStreamSynchronize(c->stream));
-    double s = 0, mx = 0;
-    int64_t cnt = 0, am = 0;
-    for (int64_t k = 0; k < n; k++) {
-        if (st[k] != 1) continue;
-        cnt++;
-        double d = 0, nr = 0;
-        for (int e = 0; e < 3; e++) {
-            const double df = a[3 * k + e] - ref3[3 * k + e];
-            d += df * df;
-            nr += ref3[3 * k + e] * ref3[3 * k + e];
-        }
-        const double r = (nr == 0 && d == 0) ? 0.0 : d / nr;
-        s += r;
-        if (r > mx) { mx = r; am = k; }
+    SV_CK(c, cudaSetDevice(c->device));
+    const int64_t n = c->n, first = c->acc_first, last = c->acc_last;
+    double sum = 0.0, mx = 0.0;
+    long long am = 0, cnt = 0;
+    if (last > first) {
+        const int blocks = std::max(1, std::min(div_up(last - first, kCmpThreads), 2 * device_sms()));
+        // staging: the reference (3n doubles), then per block sum, max, argmax and count
+        const size_t b3 = sizeof(double) * 3 * (size_t)n;
+        void *stg = nullptr;
+        SV_TRY(stage_bytes(c, b3 + (size_t)blocks * 32, &stg));
+        double *dref = (double *)stg;
+        double *psum = dref + 3 * n, *pmax = psum + blocks;
+        long long *parg = (long long *)(pmax + blocks), *pcnt = parg + blocks;
+        SV_CK(c, cudaMemcpyAsync(dref, ref3, b3, cudaMemcpyHostToDevice, c->stream));
+        compare_partial<<<blocks, kCmpThreads, 0, c->stream>>>(c->ax, c->ay, c->az, dref, c->status, first, last,
+                                                               psum, pmax, parg, pcnt);
+        SV_LAUNCHED(c);
+        compare_final<<<1, 32, 0, c->stream>>>(blocks, psum, pmax, parg, pcnt, c->d_scalar);
+        SV_LAUNCHED(c);
+        SV_CK(c, cudaMemcpyAsync(c->h_scalar, c->d_scalar, 4 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        SV_CK(c, cudaStreamSynchronize(c->stream));
+        sum = c->h_scalar[0];
+        mx = c->h_scalar[1];
+        memcpy(&am, &c->h_scalar[2], sizeof(am));
+        memcpy(&cnt, &c->h_scalar[3], sizeof(cnt));
     }
-    *l2 = cnt ? std::sqrt(s / cnt) : 0.0;
+    *l2 = cnt ? std::sqrt(sum / (double)cnt) : 0.0;
     if (maxl2) *maxl2 = std::sqrt(mx);
     if (argmax) *argmax = am;
     return SV_OK;

@@ -541,7 +541,7 @@ sv_status batch_force(sv_ctx *c, Batch &B) {
         SV_CK(c, cudaMemsetAsync(B.queue, 0, sizeof(int), c->stream));
         SV_CK(c, cudaEventRecord(B.fork, c->stream));
         SV_CK(c, cudaStreamWaitEvent(B.side, B.fork, 0));
-        int dev_sms = kNumSMs;
+        const int dev_sms = device_sms();
         direct_batch_kernel<<<std::min(B.nitems, 8 * dev_sms), kDTPB, 0, B.side>>>(
             B.items, B.nitems, B.queue, S.x, S.y, S.z, S.q, S.qm, (float)c->P.softening2, S.ax, S.ay, S.az);
         SV_LAUNCHED(c);

@@ -244,7 +244,7 @@ sv_status direct_accel(sv_ctx *c) {
     }
     const int tblocks = div_up(n, kTPB * kTPT);
     // split the source range so that the grid fills the GPU ~8 CTAs per SM deep
-    int splits = div_up(8 * kNumSMs, tblocks);
+    int splits = div_up(8 * device_sms(), tblocks);
     const int max_splits = div_up(n, kTile);
     if (splits > max_splits) splits = max_splits;
     if (splits < 1) splits = 1;
@@ -280,7 +280,7 @@ cudaError_t launch_direct_mixed_sorted(const double *xs, const double *ys, const
                                        cudaStream_t stream) {
     if (n <= 0) return cudaSuccess;
     const int tblocks = div_up(n, kTPB * kTPT);
-    int splits = div_up(8 * kNumSMs, tblocks);
+    int splits = div_up(8 * device_sms(), tblocks);
     const int max_splits = div_up(n, kTile);
     if (splits > max_splits) splits = max_splits;
     if (splits < 1) splits = 1;

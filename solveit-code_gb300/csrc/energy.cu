@@ -330,14 +330,14 @@ sv_status window_potential(sv_ctx *c, double t, int cnt) {
     SV_LAUNCHED(c);
     SV_CK(c, cudaMemsetAsync(E.pot, 0, sizeof(double) * cnt, c->stream));
     const int gx = div_up(cnt, kPotT);
-    const int gy = std::max(1, std::min(div_up(n, kPotT), div_up(4 * kNumSMs, gx)));
+    const int gy = std::max(1, std::min(div_up(n, kPotT), div_up(4 * device_sms(), gx)));
     potential_kernel<<<dim3(gx, gy), kPotT, 0, c->stream>>>(E.list, E.d_cnt, E.ph, E.pl, E.d_first, n,
                                                             (float)c->P.softening2, E.pot);
     SV_LAUNCHED(c);
     return SV_OK;
 }
 
-int sums_grid(int cnt) { return std::max(1, std::min(div_up(cnt, 256), 4 * kNumSMs)); }
+int sums_grid(int cnt) { return std::max(1, std::min(div_up(cnt, 256), 4 * device_sms())); }
 
 }  // namespace
 

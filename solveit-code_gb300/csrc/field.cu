@@ -27,7 +27,7 @@ __global__ void fill_minus_one(int *p, int64_t n) {
 
 int grid_for(int64_t n) {
     const int64_t b = (n + 255) / 256;
-    return (int)(b < 1 ? 1 : (b > 16 * kNumSMs ? 16 * kNumSMs : b));
+    return (int)(b < 1 ? 1 : (b > 16 * device_sms() ? 16 * device_sms() : b));
 }
 
 }  // namespace

@@ -846,7 +846,7 @@ __global__ void __launch_bounds__(kWarps * 32) l2l_kernel(L2LArgs a) {
 // warps per box for a level of nbox boxes: enough to give every SM a few
 // warps even at the coarse levels, at most 16
 inline int m2l_chunks(int nbox) {
-    const int want = 16 * kNumSMs;
+    const int want = 16 * device_sms();
     int c = nbox > 0 ? (want + nbox - 1) / nbox : 1;
     return c < 1 ? 1 : (c > 16 ? 16 : c);
 }
@@ -1476,7 +1476,7 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         else near_lists_kernel<2><<<div_up(slots, 256), 256, 0, F.side>>>(la);
         SV_LAUNCHED(c);
         if (L > 0) {
-            const int g = std::min(div_up(la.total - la.lv[1].first, kWarps), 16 * kNumSMs);
+            const int g = std::min(div_up(la.total - la.lv[1].first, kWarps), 16 * device_sms());
             if (ws == 1) m2l_lists_kernel<1><<<g, kWarps * 32, 0, F.side>>>(la, cap, F.d_counts);
             else m2l_lists_kernel<2><<<g, kWarps * 32, 0, F.side>>>(la, cap, F.d_counts);
             SV_LAUNCHED(c);
@@ -1626,11 +1626,10 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
 
 
 // ------------------------------------------------------------------ forest --
-constexpr int kMaxGrid = 16 * kNumSMs;  // grid-stride launches: at most 16 CTAs per SM
-
 inline int forest_grid(int cap, int per_cta) {
     const int g = div_up(cap > 0 ? cap : 1, per_cta);
-    return g < kMaxGrid ? g : kMaxGrid;
+    const int gmax = 16 * device_sms();  // grid-stride launches: at most 16 CTAs per SM
+    return g < gmax ? g : gmax;
 }
 
 template <int P>

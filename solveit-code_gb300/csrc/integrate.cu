@@ -328,7 +328,7 @@ __global__ void kinetic_kernel(const double *__restrict__ vx, const double *__re
 
 int stream_grid(int64_t n) {
     int64_t b = (n + 255) / 256;
-    const int64_t cap = 16LL * kNumSMs;
+    const int64_t cap = 16LL * device_sms();
     return (int)(b < 1 ? 1 : (b > cap ? cap : b));
 }
 

@@ -14,10 +14,18 @@
 //
 // The array's name is only a host-side stand-in in host code, so its device
 // address is fetched once per device with cudaGetSymbolAddress (with that
-// device current) on the first call made on that device; make that first call
-// before any stream capture.  All calls share the one array and it keeps the
-// previous call's contents: everything that has to start at zero is cleared
-// here, and two calls whose work overlaps on the GPU race on the array.
+// device current) on the first call made on that device.  That first call is
+// the set-up call: under lazy module loading (the CUDA default) it is also the
+// one that loads this library's device code on the device, which commits the
+// array's memory and can synchronise the device, so a caller that must not
+// allocate later makes it during its own set-up, before any stream capture.
+// The address is kept for the life of the process: after a cudaDeviceReset of
+// a device the entry point must not be called on that device again.  All
+// calls share the one array and it keeps the previous call's contents:
+// everything that has to start at zero is cleared here, and two calls whose
+// work overlaps on the GPU race on the array.  A CUDA error already pending on
+// the calling thread when a call starts is left pending (not consumed): the
+// call returns SV_ERR_CUDA without doing any work.
 #include <cub/device/device_radix_sort.cuh>
 
 #include <mutex>
@@ -30,7 +38,6 @@ namespace {
 static __device__ __align__(256) unsigned char g_noalloc_scratch[SV_NOALLOC_SCRATCH_BYTES];
 
 constexpr int kMaxDevices = 64;
-constexpr int kRedBlocks = 2 * kNumSMs;
 void *g_scratch_addr[kMaxDevices] = {nullptr};
 std::mutex g_scratch_mu;
 
@@ -183,6 +190,9 @@ extern "C" sv_status sv_direct_accel_noalloc(int64_t n, const double *x3, const 
     if (n > SV_NOALLOC_MAX_N) return SV_ERR_CAPACITY;
     if (n == 0) return SV_OK;
     if (!x3 || !q || !m_amu || !status || !a3) return SV_ERR_INVALID;
+    // the launch checks below read (and clear) the thread's last error: an
+    // error the caller's own work left pending is not this call's to consume
+    if (cudaPeekAtLastError() != cudaSuccess) return SV_ERR_CUDA;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return SV_ERR_CUDA;
     unsigned char *base = nullptr;
@@ -208,7 +218,8 @@ extern "C" sv_status sv_direct_accel_noalloc(int64_t n, const double *x3, const 
     double *ax = (double *)carve(sizeof(double) * ni);
     double *ay = (double *)carve(sizeof(double) * ni);
     double *az = (double *)carve(sizeof(double) * ni);
-    double *part = (double *)carve(sizeof(double) * 6 * kRedBlocks);
+    const int red_blocks = 2 * device_sms();
+    double *part = (double *)carve(sizeof(double) * 6 * red_blocks);
     double *root = (double *)carve(sizeof(double) * 8);
     cub::DoubleBuffer<uint64_t> kb(keys, keys_alt);
     cub::DoubleBuffer<uint32_t> vb(idx, idx_alt);
@@ -219,8 +230,8 @@ extern "C" sv_status sv_direct_accel_noalloc(int64_t n, const double *x3, const 
     if (off > (size_t)SV_NOALLOC_SCRATCH_BYTES) return SV_ERR_CAPACITY;
 
     const int nb = (ni + 255) / 256;
-    na_bbox_partial<<<kRedBlocks, 256, 0, s>>>(x3, status, ni, part);
-    na_bbox_final<<<1, 32, 0, s>>>(part, kRedBlocks, root);
+    na_bbox_partial<<<red_blocks, 256, 0, s>>>(x3, status, ni, part);
+    na_bbox_final<<<1, 32, 0, s>>>(part, red_blocks, root);
     na_keys<<<nb, 256, 0, s>>>(x3, status, ni, root, keys, idx);
     if (cudaGetLastError() != cudaSuccess) return SV_ERR_CUDA;
     if (cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, kb, vb, ni, 0, 3 * kMortonBits + 1, s) != cudaSuccess)

@@ -230,7 +230,7 @@ sv_status outliers_detect(sv_ctx *c, const int32_t **status_for_tree) {
     SV_TRY(reserve(c, O, n));
     const int g = div_up(n, 256);
     SV_CK(c, cudaMemsetAsync(O.count, 0, sizeof(int) * 2, c->stream));
-    count_sources_kernel<<<std::min(g, 16 * kNumSMs), 256, 0, c->stream>>>(force_status(c), n, O.count);
+    count_sources_kernel<<<std::min(g, 16 * device_sms()), 256, 0, c->stream>>>(force_status(c), n, O.count);
     SV_LAUNCHED(c);
     const double *axis[3] = {c->x, c->y, c->z};
     for (int pass = 0; pass < 2; pass++) {

@@ -228,7 +228,7 @@ sv_status ensure_sorted_capacity(sv_ctx *c, int64_t n) {
     SV_CK(c, cub::DeviceRadixSort::SortPairs(nullptr, bytes, kb, vb, (int)cap, 0, 64, c->stream));
     S.cub_bytes = bytes;
     SV_CK(c, cudaMalloc(&S.cub_tmp, bytes));
-    S.red_blocks = 2 * kNumSMs;
+    S.red_blocks = 2 * device_sms();
     SV_CK(c, cudaMalloc(&S.red, (size_t)S.red_blocks * 6 * sizeof(double)));
     SV_CK(c, cudaMalloc(&S.root, 16 * sizeof(double)));
     S.cap = cap;

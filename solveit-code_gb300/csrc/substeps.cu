@@ -180,7 +180,7 @@ __global__ void fill_levels(int8_t *p, int64_t n, int8_t v) {
 
 int grid_n(int64_t n) {
     const int64_t b = (n + 255) / 256;
-    return (int)(b < 1 ? 1 : (b > 16 * kNumSMs ? 16 * kNumSMs : b));
+    return (int)(b < 1 ? 1 : (b > 16 * device_sms() ? 16 * device_sms() : b));
 }
 
 struct Runner {

@@ -12,7 +12,6 @@
 
 namespace sv {
 
-constexpr int kNumSMs = 152;          // GB300: 2 dies x 76 SMs
 constexpr int kMortonBits = 21;       // bits per axis of the Morton key (63-bit keys)
 constexpr uint64_t kInactiveKey = ~0ull;
 // Floor of r^2 + eps^2 (m^2) in the FP32 pair kernels: 1e-24 keeps 1/r^3 below
@@ -146,6 +145,7 @@ struct sv_ctx {
     // last acceleration (force only), caller order, FP64
     double *ax = nullptr, *ay = nullptr, *az = nullptr;
     bool have_state = false, have_accel = false;
+    int64_t acc_first = 0, acc_last = 0;  // window [first, last) of the last evaluation
     sv::Sorted S;
     sv::Tree *tree = nullptr;
     sv::Fmm *fmm = nullptr;
@@ -254,6 +254,10 @@ inline void phase_mark(sv_ctx *c, int k) {
 }
 
 inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+// SM count of the current device (cudaDevAttrMultiProcessorCount), cached per
+// device: grid-stride and persistent launches are sized in multiples of it
+int device_sms();
 
 // sort.cu
 sv_status ensure_sorted_capacity(sv_ctx *c, int64_t n);

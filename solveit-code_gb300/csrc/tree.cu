@@ -497,7 +497,7 @@ sv_status tree_build_forest(sv_ctx *c, Tree &T, const ForestSpec &f, int *d_nbox
     SV_LAUNCHED(c);
     int maxcap = 1;
     for (int l = 0; l <= L; l++) maxcap = std::max(maxcap, f.cap[l]);
-    link_levels_forest<<<dim3(std::min(div_up(maxcap, 256), 4 * kNumSMs), L + 1), 256, 0, c->stream>>>(L, n, d_nbox, P);
+    link_levels_forest<<<dim3(std::min(div_up(maxcap, 256), 4 * device_sms()), L + 1), 256, 0, c->stream>>>(L, n, d_nbox, P);
     SV_LAUNCHED(c);
     return SV_OK;
 }

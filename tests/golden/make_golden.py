@@ -39,6 +39,13 @@ Fixtures (all FP32 vec4 arrays in the reference layout):
                     toggleEnergy over 6 steps: the energy file's records,
                     without and with the emitter field and with inactive
                     particles at the front (``... make_golden.py energy``).
+  bh_n65536_sampled.npz, fmm_n65536_z50_sampled.npz
+                    the reference's Barnes-Hut (theta 0.5) at the treecode
+                    workload's size and its FMM (p = 8) on the long 50 um
+                    plume at N = 65,536 (the largest size it runs cleanly),
+                    softening 1e-20 m^2: accelerations of every 64th particle
+                    and those particles' positions
+                    (``... make_golden.py sampled``).
 """
 from __future__ import annotations
 
@@ -141,7 +148,27 @@ def main():
     np.savez_compressed(os.path.join(HERE, "fmm_n4096.npz"), pos4=pos4, vel4=vel4, acc4=acc4,
                         tinj=tinj, acc_fmm=af, p=np.int32(8), eps=np.float64(6.4e-19))
     outliers()
+    sampled_configs()
     print("fixtures written to", HERE)
+
+
+def sampled_configs(ntarget=1024):
+    """The reference's Barnes-Hut at the treecode workload's size (N = 65,536,
+    z in [0, 10] um, theta 0.5, seed 1000) and its FMM at the largest size it
+    runs cleanly with the long plume (N = 65,536, z in [0, 50] um, p 8, seed
+    2000), softening 1e-10 m: accelerations of every 64th particle, with those
+    particles' FP32 positions to check that the plume generator reproduces the
+    same plume where the test runs."""
+    for name, mode, length, seed, kw in (("bh_n65536_sampled.npz", "bh", 10e-6, 1000, dict(theta=0.5)),
+                                         ("fmm_n65536_z50_sampled.npz", "fmm", 50e-6, 2000, dict(p=8))):
+        n = 65536
+        st = plume.make_plume(n, length, seed)
+        pos4, vel4, acc4, tinj = plume.to_ref32(st)
+        _, _, a = run_ref("eps20", mode, pos4, vel4, acc4, tinj, threads=os.cpu_count() or 4, **kw)
+        tg = np.arange(0, n, n // ntarget, dtype=np.int32)
+        np.savez_compressed(os.path.join(HERE, name), n=np.int32(n), length=np.float64(length),
+                            seed=np.int64(seed), eps=np.float64(1e-20), targets=tg, pos4_targets=pos4[tg],
+                            acc_ref=a[tg, :3].copy(), **{k: np.float64(v) for k, v in kw.items()})
 
 
 def outliers():
@@ -343,5 +370,7 @@ if __name__ == "__main__":
         substeps()
     elif sys.argv[1:] == ["energy"]:
         energy()
+    elif sys.argv[1:] == ["sampled"]:
+        sampled_configs()
     else:
         main()

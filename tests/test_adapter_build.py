@@ -7,7 +7,7 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REFERENCE = "/root/reference"
+REFERENCE = os.environ.get("SOLVEIT_REFERENCE", "/root/reference")
 
 
 @pytest.mark.skipif(not os.path.isdir(REFERENCE), reason="reference tree not present")

@@ -115,3 +115,20 @@ def test_energy_two_body():
     e = O.lib().orc_elem_charge()
     kc = O.lib().orc_coulomb_ke()
     assert abs(pe - e * e * kc / 1e-9) / pe < 1e-12
+
+
+@pytest.mark.parametrize("name", ["bh_n65536_sampled.npz", "fmm_n65536_z50_sampled.npz"])
+def test_sampled_fixture_plume_and_reference_error(golden_dir, name):
+    """The seeded plume generator reproduces the fixture's plume here (the
+    sampled particles' FP32 positions, bit for bit), and the reference's own
+    Barnes-Hut / FMM error on it against the oracle's FP64 direct sum is the
+    envelope the GPU tests hold the GPU methods to."""
+    g = load(golden_dir, name)
+    n, tg = int(g["n"]), g["targets"]
+    st = plume.make_plume(n, float(g["length"]), int(g["seed"]))
+    pos4 = plume.to_ref32(st)[0]
+    assert np.array_equal(pos4[tg], g["pos4_targets"])
+    ref = O.direct_f64(st, float(g["eps"]), targets=tg)
+    err = O.rel_l2(g["acc_ref"].astype(np.float64), ref, st["status"][tg])[0]
+    # the reference's monopole Barnes-Hut and uniform-depth ws-1 FMM
+    assert (3e-3 < err < 2e-2) if "bh" in name else (5e-5 < err < 1e-3), err

@@ -9,13 +9,20 @@ on different plumes, and checks each result against the regular entry point
 (sv_compute_accel, direct method, mixed precision) within 1e-12 relative per
 particle: both run the same sorted FP32 tile kernel and differ only in the
 order of FP64 atomic additions.  The second call must not change the amount
-of free device memory.
+of free device memory (the first call on a device is its set-up call: it
+loads the array).  Each result is also held to the oracle's FP64 direct sum
+on sampled targets within 2e-6 per-particle relative L2, the bound of the
+mixed-precision direct sum in tests/test_gpu_direct.py, and one call runs at
+the stated maximum size, where the array must hold the sort's temporary
+storage too.
 """
 import ctypes as C
+import os
 
 import numpy as np
 import pytest
 
+import oracle_py as O
 import plume
 import solveit_gpu as sv
 
@@ -56,6 +63,13 @@ def _assert_close(a, ref):
     assert np.all(a[~live] == 0.0)
 
 
+def _assert_oracle(a, state, k=512):
+    n = state["x"].shape[0]
+    tg = np.sort(np.random.default_rng(n).choice(n, min(n, k), replace=False))
+    ref = O.direct_f64(state, EPS20, targets=tg, threads=os.cpu_count() or 1)
+    assert O.rel_l2(a[tg], ref, state["status"][tg])[0] < 2e-6
+
+
 def test_noalloc_matches_regular_entry_point_twice():
     torch = pytest.importorskip("torch")
     L = sv.load()
@@ -70,12 +84,25 @@ def test_noalloc_matches_regular_entry_point_twice():
     rc, a1, _, _ = _noalloc(L, torch, s1, a3_dev)
     assert rc == 0
     _assert_close(a1, _regular(s1))
+    _assert_oracle(a1, s1)
 
     # second call: smaller plume, other statuses, same static array
     rc, a2, free_before, free_after = _noalloc(L, torch, s2, a3_dev)
     assert rc == 0
     _assert_close(a2, _regular(s2))
+    _assert_oracle(a2, s2)
     assert np.all(a2[300:400] == 0.0) and np.all(a2[:300] == 0.0)
+    assert free_after >= free_before
+
+    # the stated maximum size: keys, sorted copy and the sort's temporary
+    # storage all inside the static array
+    nmax = 262144
+    s3 = plume.make_plume(nmax, 20e-6, 503)
+    big = torch.empty((nmax, 3), dtype=torch.float64, device="cuda:0")
+    rc, a3, free_before, free_after = _noalloc(L, torch, s3, big)
+    assert rc == 0
+    _assert_close(a3, _regular(s3))
+    _assert_oracle(a3, s3)
     assert free_after >= free_before
 
     # sizes beyond the stated maximum are refused before any work
