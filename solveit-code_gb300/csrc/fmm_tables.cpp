@@ -284,4 +284,83 @@ bool build_fmm_tables(int p, int ws, FmmTables &T, std::string &err) {
     return true;
 }
 
+bool build_m2l_dense(int p, int ws, std::vector<double> &K, std::string &err) {
+    const int R = p * p, range = 2 * ws + 1, side = 2 * range + 1, ncls = side * side * side;
+    K.assign((size_t)ncls * R * R, 0.0);
+    auto N = [](int n, int m) { return std::sqrt(fact(n - m) * fact(n + m)); };
+    // z-translation constants C[k][j][n], as build_fmm_tables has them
+    std::vector<double> zc((size_t)p * p * p, 0.0);
+    for (int k = 0; k < p; k++)
+        for (int j = k; j < p; j++)
+            for (int n = k; n < p; n++)
+                zc[((size_t)k * p + j) * p + n] = ((j + k) & 1 ? -1.0 : 1.0) * fact(j + n) / (N(n, k) * N(j, k));
+    std::map<long long, std::pair<std::vector<std::vector<cd>>, std::vector<std::vector<cd>>>> rot;
+    // real index of (n, m, part): n^2 for Re(c_n^0); n^2 + 2m - 1 / n^2 + 2m for Re / Im(c_n^m)
+    auto ri = [](int n, int m, int im) { return m == 0 ? n * n : n * n + 2 * m - 1 + im; };
+    std::vector<cd> A(p * p), B(p * p), Cz(p * p), Rr(p * p);  // [n][m], m = 0..n
+    for (int dx = -range; dx <= range; dx++)
+        for (int dy = -range; dy <= range; dy++)
+            for (int dz = -range; dz <= range; dz++) {
+                if (std::max(std::abs(dx), std::max(std::abs(dy), std::abs(dz))) <= ws) continue;
+                const int id = ((dx + range) * side + (dy + range)) * side + (dz + range);
+                const double r = std::sqrt((double)(dx * dx + dy * dy + dz * dz));
+                const double th = std::acos(dz / r), ph = std::atan2((double)dy, (double)dx);
+                const long long key = std::llround(th * 1e12);
+                if (!rot.count(key)) {
+                    double mi1 = 0, mi2 = 0;
+                    auto gf = yrot(p, th, &mi1);
+                    auto gb = yrot(p, -th, &mi2);
+                    if (mi1 > 1e-9 || mi2 > 1e-9) {
+                        err = "y-rotation matrix is not real";
+                        return false;
+                    }
+                    rot[key] = {gf, gb};
+                }
+                const auto &Gf = rot[key].first, &Gb = rot[key].second;
+                // a real y-rotation of degree n on coefficients m = 0..n of a
+                // real-symmetric expansion (c_n^-m = conj c_n^m)
+                auto yrot_apply = [&](const std::vector<std::vector<cd>> &G, const std::vector<cd> &in,
+                                      std::vector<cd> &out) {
+                    for (int n = 0; n < p; n++) {
+                        const int w = 2 * n + 1;
+                        auto g = [&](int mp, int m) { return G[n][(mp + n) * w + (m + n)].real(); };
+                        for (int mp = 0; mp <= n; mp++) {
+                            double re = g(mp, 0) * in[n * p].real(), im = 0.0;
+                            for (int m = 1; m <= n; m++) {
+                                re += (g(mp, m) + g(mp, -m)) * in[n * p + m].real();
+                                if (mp > 0) im += (g(mp, m) - g(mp, -m)) * in[n * p + m].imag();
+                            }
+                            out[n * p + mp] = cd(re, im);
+                        }
+                    }
+                };
+                for (int n0 = 0; n0 < p; n0++)
+                    for (int m0 = 0; m0 <= n0; m0++)
+                        for (int part = 0; part < (m0 == 0 ? 1 : 2); part++) {
+                            std::fill(A.begin(), A.end(), cd(0, 0));
+                            // unit input, then the phase e^{i m phi}
+                            A[n0 * p + m0] = (part == 0 ? cd(1, 0) : cd(0, 1)) * std::polar(1.0, m0 * ph);
+                            yrot_apply(Gf, A, B);
+                            // translation along z: C_j^k = sum_n C[k][j][n] r^-(j+n+1) B_n^k
+                            std::fill(Cz.begin(), Cz.end(), cd(0, 0));
+                            for (int k = 0; k < p; k++)
+                                for (int j = k; j < p; j++) {
+                                    cd acc(0, 0);
+                                    for (int n = k; n < p; n++)
+                                        acc += zc[((size_t)k * p + j) * p + n] * std::pow(r, -(j + n + 1)) * B[n * p + k];
+                                    Cz[j * p + k] = acc;
+                                }
+                            yrot_apply(Gb, Cz, Rr);
+                            const int kin = ri(n0, m0, part);
+                            for (int j = 0; j < p; j++)
+                                for (int k = 0; k <= j; k++) {
+                                    const cd v = Rr[j * p + k] * std::polar(1.0, -k * ph);
+                                    K[((size_t)id * R + ri(j, k, 0)) * R + kin] = v.real();
+                                    if (k > 0) K[((size_t)id * R + ri(j, k, 1)) * R + kin] = v.imag();
+                                }
+                        }
+            }
+    return true;
+}
+
 }  // namespace sv

@@ -42,4 +42,14 @@ int dmat_offset_e(int n, int p);    // stride * sum_{k<n} (k+1): E block of degr
 int dmat_offset_o(int n, int p);    // stride * sum_{k<n} k: O block of degree n (rows mp = 1..n)
 bool build_fmm_tables(int p, int ws, FmmTables &T, std::string &err);
 
+// The M2L of every offset class as a dense real matrix, built in FP64 from
+// the same steps as the rotation-based M2L (phase, y-rotation, translation
+// along z, back-rotation, phase) without the softening of the distance.
+// Coefficients are taken as R = p^2 reals in degree order: for degree n,
+// Re(c_n^0), then Re(c_n^m), Im(c_n^m) for m = 1..n (the zero imaginary part
+// of c_n^0 is left out).  K[(cls * R + j) * R + k] maps input real k of the
+// source multipole to output real j of the target's local expansion (zero
+// for the near classes).
+bool build_m2l_dense(int p, int ws, std::vector<double> &K, std::string &err);
+
 }  // namespace sv
