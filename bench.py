@@ -244,7 +244,7 @@ def run_batch(args, wl, rank, world, local):
     counts = np.array([s["x"].shape[0] for s in states])
     n = int(counts.sum())
     fm = sv.ForceMethod(softening2=EPS2, efield=(0.0, 0.0, EZ), device=local, fmm_order=wl["order"],
-                        fmm_ws=wl["ws"])
+                        fmm_ws=wl["ws"], fmm_m2l_tc=args.m2l_tc)
     fm.upload_batch(states, methods, syms)
     tuned_ms = None if args.no_tune else fm.tune(None)
     stream = torch.cuda.ExternalStream(fm.stream, device=local)
@@ -524,7 +524,7 @@ def run_ours(args, wl, rank, world, local):
     st = plume.make_plume(n, wl["length"], plume_seed(wl, rank))
     if wl["method"] == "fmm":
         kw = dict(method=sv.FMM, precision=sv.MIXED, fmm_order=wl["order"], fmm_ws=wl["ws"],
-                  fmm_leaf_target=wl["leaf"])
+                  fmm_leaf_target=wl["leaf"], fmm_m2l_tc=args.m2l_tc)
     else:
         kw = dict(method=sv.DIRECT, precision=sv.FP64 if wl.get("precision") == "fp64" else sv.MIXED)
     fm = sv.ForceMethod(softening2=EPS2, efield=(0.0, 0.0, EZ), device=local, profile_phases=1, **kw)
@@ -580,7 +580,8 @@ def run_ours(args, wl, rank, world, local):
     if args.timed_only:
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "ms_per_step": ms_per_step,
-                              "phases_ms": list(map(float, phase_ms)), "timed_only": True}), flush=True)
+                              "phases_ms": list(map(float, phase_ms)), "m2l_tc": int(stats.m2l_tc),
+                              "m2l": stats.cell_interactions, "timed_only": True}), flush=True)
         fm.close()
         return
     # ---- end to end through the C ABI with pinned host buffers: the same
@@ -732,6 +733,8 @@ def main():
                     help="FMM: this root-cube scale instead of sv_fmm_tune's (profiling a fixed configuration)")
     ap.add_argument("--timed-only", action="store_true",
                     help="only the device-resident timed steps (for profiler launch lists)")
+    ap.add_argument("--m2l-tc", type=int, default=0, choices=[-1, 0, 1],
+                    help="FMM M2L: 1 tensor cores, -1 FP32 rotation kernel, 0 the library default")
     ap.add_argument("--no-tune", action="store_true",
                     help="skip the autotuner (batch: default depth-model weight; FMM: power-of-two root cube)")
     args = ap.parse_args()

@@ -107,7 +107,10 @@ typedef struct {
                                 particles multiplied than this are summed as direct pairs in the
                                 near field instead of an M2L translation (up to 128 per box; single
                                 plumes and a batch's FMM forest): 0 = 1024, < 0 = every entry by M2L */
-    int32_t reserved[3];
+    int32_t fmm_m2l_tc;        /* M2L translations: 1 = on the tensor cores (offset classes as dense TF32x3
+                                contractions, tcgen05), -1 = the FP32 rotation kernel, 0 = the default
+                                (the tensor cores) */
+    int32_t reserved[2];
 } sv_params;
 
 /* Per-call statistics of the last force evaluation. */
@@ -123,7 +126,9 @@ typedef struct {
                                      time and overlaps them */
     int32_t levels;               /* FMM leaf level / BH max depth */
     int32_t boxes;                /* occupied leaf boxes / BH nodes */
-    int32_t reserved[6];
+    int32_t m2l_tc;               /* FMM: 1 when the last evaluation's M2L ran on the tensor cores, 0 when
+                                     it ran on the FP32 rotation kernel */
+    int32_t reserved[5];
 } sv_stats;
 
 /* Fill p with the defaults of the reference configuration: softening

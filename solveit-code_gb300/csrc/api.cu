@@ -324,6 +324,7 @@ sv_status check_params(sv_ctx *c, const sv_params *p) {
         return set_error(c, SV_ERR_INVALID, "fmm_leaf_target outside 1..4096");
     if (p->fmm_type < SV_FMM_FMM || p->fmm_type > SV_FMM_TREECODE_OUTLIERS)
         return set_error(c, SV_ERR_INVALID, "unknown fmm_type %d", p->fmm_type);
+    if (p->fmm_m2l_tc < -1 || p->fmm_m2l_tc > 1) return set_error(c, SV_ERR_INVALID, "fmm_m2l_tc must be -1, 0 or 1");
     if (!(p->fmm_root_scale == 0.0f || (p->fmm_root_scale >= 1.0f && p->fmm_root_scale < 2.0f)))
         return set_error(c, SV_ERR_INVALID, "fmm_root_scale must be 0 or in [1, 2)");
     if (p->symmetry == SV_SYM_TRANSLATIONAL) {

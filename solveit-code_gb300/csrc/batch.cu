@@ -849,6 +849,8 @@ sv_status batch_accel(sv_ctx *c) {
         SV_TRY(read_err(c, B, &err));
         if (!err) {
             c->stats.pair_interactions = B.direct_pairs;
+            // the result stands (the rotation M2L ran); the next run gets more room
+            if (fmm_forest_tc_overflowed(c)) SV_TRY(plan_forest(c, B, 1));
             return SV_OK;
         }
         SV_TRY(grow(c, B, 2 << attempt));
@@ -895,6 +897,7 @@ sv_status batch_leapfrog(sv_ctx *c, int32_t nsteps, double dt, double t0) {
         SV_TRY(read_err(c, B, &err));
         if (!err) {
             c->ev_seq += 2LL * nsteps;
+            if (fmm_forest_tc_overflowed(c)) SV_TRY(plan_forest(c, B, 1));
             return SV_OK;
         }
         for (int k = 0; k < 6; k++)

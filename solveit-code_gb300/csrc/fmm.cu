@@ -37,6 +37,7 @@
 
 #include "fmm_tables.h"
 #include "forest.cuh"
+#include "m2l_tc.cuh"
 #include "sv_internal.cuh"
 #include "tree.cuh"
 
@@ -82,6 +83,7 @@ struct Fmm {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_lists = nullptr, ev_join = nullptr, ev_near[2] = {};
     cudaEvent_t ev_m2l_lists = nullptr;  // single plume: near, interaction and far-direct lists built (second stream)
+    M2LTc tc;                // the M2L on the tensor cores (m2l_tc.cu)
 };
 
 namespace {
@@ -478,6 +480,7 @@ struct M2LLevel {
 };
 
 struct M2LArgs {
+    const int *run_if;    // non-null: run only when *run_if != 0 (the tensor-core M2L overflowed its room)
     int nlev, cap, esz, osz, dsz;
     double eps2;
     const double *root;
@@ -709,6 +712,7 @@ template <int P>
 __global__ void __launch_bounds__(m2l_warps<P>() * 32, m2l_min_ctas<P>()) m2l_kernel(M2LArgs a) {
     constexpr int NC = ncoef(P), RS = rot_rs<P>(), SR = sh_rs<P>(), ZK = z_ks<P>(), WP = m2l_warps<P>();
     constexpr int NU = m2l_inflight<P>();
+    if (a.run_if && !*a.run_if) return;
     __shared__ __align__(16) float2 A[WP][NU][P * SR], B[WP][NU][P * SR];
     __shared__ __align__(16) float Zsh[P * ZK];
     // the table's rows (k, j), RS floats each, to k * ZK + j * RS
@@ -1523,6 +1527,7 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
     const bool treecode = c->P.fmm_type == SV_FMM_TREECODE || c->P.fmm_type == SV_FMM_TREECODE_OUTLIERS;
     // downward pass: M2L of all levels in one launch, then L2L level by level
     // (the treecode evaluates multipoles at the particles instead)
+    F.tc.launched = false;
     if (!treecode && L >= 2) {
         M2LArgs a{};
         a.cap = cap;
@@ -1551,6 +1556,41 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
             V.M = Mv[l];
             V.out = part[l];
             warps += V.nbox * V.chunks;
+        }
+        if (c->P.fmm_m2l_tc >= 0) {
+            // the tensor-core M2L; the rotation kernel below runs only if it overflowed its room
+            TcArgs ta{};
+            ta.nlev = a.nlev;
+            ta.cap = cap;
+            ta.eps2 = c->P.softening2;
+            ta.root = S.root;
+            ta.cls_rho2 = F.cls_rho2;
+            int64_t boxes = 0;
+            for (int k = 0; k < a.nlev; k++) {
+                const M2LLevel &V = a.lv[k];
+                TcLevel &q = ta.lv[k];
+                q.nbox = V.nbox;
+                q.level = V.level;
+                q.chunks = V.chunks;
+                q.warp0 = V.warp0;
+                q.first = (int)boxes;
+                q.nbd = nullptr;
+                q.bpid = nullptr;
+                q.m2l = lst[V.level];
+                q.cnt = V.cnt;
+                q.has_tgt = V.has_tgt;
+                q.M = V.M;
+                q.out = V.out;
+                boxes += V.nbox;
+            }
+            ta.total_boxes = (int)boxes;
+            // room: the last evaluation's translations (read back by then) with a margin, at least 32 per box
+            const int64_t last = F.tc.h_ctl && F.tc.p == P && F.tc.ws == ws ? F.tc.h_ctl[0] : 0;
+            SV_TRY(m2l_tc_prepare(c, F.tc, P, ws, std::max<int64_t>(last + last / 4, 32 * boxes)));
+            ta.ncls = F.tc.ncls;
+            SV_TRY(m2l_tc_launch(c, F.tc, ta, warps, c->stream));
+            a.run_if = m2l_tc_skip_flag(F.tc);
+            F.tc.launched = true;
         }
         m2l_kernel<P><<<div_up(warps, m2l_warps<P>()), m2l_warps<P>() * 32, 0, c->stream>>>(a);
         SV_LAUNCHED(c);
@@ -1734,6 +1774,40 @@ sv_status run_fmm_forest(sv_ctx *c, Fmm &F, const ForestArgs &fa) {
             V.out = F.fpart[l];
             warps += (long long)V.nbox * V.chunks;
         }
+        F.tc.launched = false;
+        if (c->P.fmm_m2l_tc >= 0 && F.tc.cap > 0 && F.tc.p == P && F.tc.ws == ws) {
+            // the tensor-core M2L (room reserved with the forest); the rotation
+            // kernel below runs only if the translations overflowed it
+            TcArgs ta{};
+            ta.nlev = a.nlev;
+            ta.cap = cap;
+            ta.eps2 = c->P.softening2;
+            ta.root = fa.roots;
+            ta.cls_rho2 = F.cls_rho2;
+            ta.ncls = F.tc.ncls;
+            long long boxes = 0;
+            for (int k = 0; k < a.nlev; k++) {
+                const M2LLevel &V = a.lv[k];
+                TcLevel &q = ta.lv[k];
+                q.nbox = V.nbox;
+                q.level = V.level;
+                q.chunks = V.chunks;
+                q.warp0 = V.warp0;
+                q.first = (int)boxes;
+                q.nbd = V.nbd;
+                q.bpid = V.bpid;
+                q.m2l = F.flst[V.level];
+                q.cnt = V.cnt;
+                q.has_tgt = V.has_tgt;
+                q.M = V.M;
+                q.out = V.out;
+                boxes += V.nbox;
+            }
+            ta.total_boxes = (int)boxes;
+            SV_TRY(m2l_tc_launch(c, F.tc, ta, (int)warps, c->stream));
+            a.run_if = m2l_tc_skip_flag(F.tc);
+            F.tc.launched = true;
+        }
         m2l_kernel<P><<<(int)((warps + m2l_warps<P>() - 1) / m2l_warps<P>()), m2l_warps<P>() * 32, 0,
                           c->stream>>>(a);
         SV_LAUNCHED(c);
@@ -1805,6 +1879,7 @@ void fmm_free(sv_ctx *c) {
     cudaFree(F.ex); cudaFree(F.ey); cudaFree(F.ez); cudaFree(F.eq); cudaFree(F.em); cudaFree(F.est);
     cudaFree(F.eoff); cudaFree(F.has_tgt); cudaFree(F.rel); cudaFree(F.far);
     cudaFree(F.farena); cudaFree(F.frel);
+    m2l_tc_free(F.tc);
     if (F.ftree) {
         tree_release(*F.ftree);
         delete F.ftree;
@@ -1988,6 +2063,15 @@ sv_status fmm_forest_reserve(sv_ctx *c, const ForestArgs &fa) {
     }
     F.ffd = (int *)carve((size_t)f.cap[f.L] * kFarDirectCap * sizeof(int));
     F.ffd_cnt = (int *)carve((size_t)f.cap[f.L] * sizeof(int));
+    if (c->P.fmm_m2l_tc >= 0 && f.L >= 2) {
+        // room of the tensor-core M2L: the last run's translations with a
+        // margin, at least 32 per box of the M2L levels (a graph keeps the
+        // buffers' addresses, so the room only changes here, at plan time)
+        int64_t boxes = 0;
+        for (int l = 2; l <= f.L; l++) boxes += f.cap[l];
+        const int64_t last = F.tc.h_ctl && F.tc.p == p && F.tc.ws == fa.ws ? F.tc.h_ctl[0] : 0;
+        SV_TRY(m2l_tc_prepare(c, F.tc, p, fa.ws, std::max<int64_t>(last + last / 4, 32 * boxes)));
+    }
     if (F.frel_cap < f.n) {
         cudaFree(F.frel);
         F.frel = nullptr;
@@ -1995,6 +2079,11 @@ sv_status fmm_forest_reserve(sv_ctx *c, const ForestArgs &fa) {
         F.frel_cap = f.n;
     }
     return SV_OK;
+}
+
+bool fmm_forest_tc_overflowed(const sv_ctx *c) {
+    const Fmm *F = c->fmm;
+    return F && F->tc.launched && F->tc.h_ctl && F->tc.h_ctl[2];
 }
 
 __global__ void max_count_kernel(const int4 *__restrict__ coord, const int *__restrict__ nbd, int cap,
@@ -2043,6 +2132,10 @@ sv_status fmm_counts(sv_ctx *c, double *m2l, double *pairs) {
     SV_CK(c, cudaStreamSynchronize(c->stream));
     *m2l = (double)c->fmm->h_counts[0];
     *pairs = (double)c->fmm->h_counts[1];
+    const M2LTc &tc = c->fmm->tc;
+    c->stats.m2l_tc = tc.launched && tc.h_ctl && !tc.h_ctl[2];
+    if (tc.launched && tc.h_ctl && tc.h_ctl[3])
+        return set_error(c, SV_ERR_TIMEOUT, "tensor-core M2L: a bounded wait on the tensor cores gave up");
     return SV_OK;
 }
 

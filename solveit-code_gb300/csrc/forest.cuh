@@ -28,5 +28,9 @@ sv_status fmm_forest_reserve(sv_ctx *c, const ForestArgs &a);
 sv_status fmm_forest_run(sv_ctx *c, const ForestArgs &a);
 // Largest leaf-box occupancy of the last run (blocking; diagnostics).
 sv_status fmm_forest_max_leaf(sv_ctx *c, const ForestArgs &a, int *out);
+// The last run's tensor-core M2L found more translations than its room and
+// ran the rotation kernel instead (read after the run has completed): the
+// caller re-plans, which grows the room, and captures its graphs again.
+bool fmm_forest_tc_overflowed(const sv_ctx *c);
 
 }  // namespace sv

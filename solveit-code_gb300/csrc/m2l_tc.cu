@@ -42,7 +42,6 @@ constexpr int kTile = 128;          // entries per tile (the MMA's M)
 constexpr int kTcThreads = 128;     // 4 warps: warp w owns TMEM lanes 32w..32w+31 = tile rows
 constexpr int kTmemCols = 128;      // accumulator columns allocated (N <= 112)
 constexpr int kCtl = 4;             // leading control words of M2LTc::ctl
-constexpr int kListWarps = 8;       // warps per block of the class / bucket passes
 constexpr int kMaxCls = 2048;       // classes a block can count in shared memory (ws <= 2: 1331)
 
 template <int P>
@@ -189,28 +188,77 @@ __device__ __forceinline__ int tc_find_level(const TcArgs &a, int g, int &b) {
 }
 
 // Pass 1 (bucket = false): class histogram.  Pass 3 (bucket = true): rows
-// in class order.  Warp per box, blocks of kListWarps warps.
+// in class order.  A block takes kClsBoxes consecutive boxes: one thread
+// reads each box's header (level, target flag, entry count), a block scan
+// lays the boxes' entries end to end, and the threads then walk the
+// flattened entries (every load independent of the others).  Counts go to a
+// shared histogram, then one global add per block and class (pass 1) or one
+// global range per block and class, from which each entry takes its row
+// (pass 3).  Against one box per warp over ~8x more blocks this is slower
+// alone under a profiler but faster inside the force evaluation, where these
+// passes share the GPU with the near field: fewer, longer-lived blocks take
+// fewer of its SM slots (fmm_n1m, 20 steps: 2.36 against 2.40 ms per step).
+constexpr int kClsBoxes = 128;
+
 template <bool BUCKET>
-__global__ void __launch_bounds__(kListWarps * 32) tc_classes_kernel(TcArgs a, int *__restrict__ ctl,
-                                                                     int4 *__restrict__ bucket) {
+__global__ void __launch_bounds__(kClsBoxes) tc_classes_kernel(TcArgs a, int *__restrict__ ctl,
+                                                               int4 *__restrict__ bucket) {
     __shared__ int hist[kMaxCls];
-    __shared__ int base[kMaxCls];
+    __shared__ int base[BUCKET ? kMaxCls : 1];
+    __shared__ int s_off[kClsBoxes + 1], s_li[kClsBoxes], s_b[kClsBoxes];
+    __shared__ float s_eh2[BUCKET ? kClsBoxes : 1];
+    __shared__ int s_warp[kClsBoxes / 32];
     int *cls_cnt = ctl + kCtl, *cls_off = cls_cnt + a.ncls, *cursor = cls_off + 2 * a.ncls;
     if (BUCKET && ctl[2]) return;  // overflow: the rotation M2L runs instead
-    for (int k = threadIdx.x; k < a.ncls; k += blockDim.x) hist[k] = 0;
-    __syncthreads();
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int g = blockIdx.x * kListWarps + wid;
-    int li = 0, b = 0, n = 0;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    for (int k = tid; k < a.ncls; k += kClsBoxes) hist[k] = 0;
+    // this thread's box
+    const int g = blockIdx.x * kClsBoxes + tid;
+    int n = 0, li = 0, b = 0;
     if (g < a.total_boxes) {
         li = tc_find_level(a, g, b);
         const TcLevel &v = a.lv[li];
-        if (b < tc_level_boxes(v) && v.has_tgt[b]) n = v.cnt[b];
+        if (b < tc_level_boxes(v) && v.has_tgt[b]) {
+            n = v.cnt[b];
+            if (BUCKET) {
+                const double h = (v.bpid ? a.root + 8 * v.bpid[b] : a.root)[3] / (double)(1 << v.level);
+                s_eh2[tid] = (float)(a.eps2 / (h * h));
+            }
+        }
     }
-    const int2 *lst = n ? a.lv[li].m2l + (size_t)b * a.cap : nullptr;
-    for (int e = lane; e < n; e += 32) atomicAdd(&hist[lst[e].y], 1);
+    s_li[tid] = li;
+    s_b[tid] = b;
+    // exclusive scan of the entry counts over the block
+    int inc = n;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += u;
+    }
+    if (lane == 31) s_warp[wid] = inc;
     __syncthreads();
-    for (int k = threadIdx.x; k < a.ncls; k += blockDim.x) {
+    int woff = 0;
+    for (int w = 0; w < wid; w++) woff += s_warp[w];
+    s_off[tid] = woff + inc - n;
+    if (tid == kClsBoxes - 1) s_off[kClsBoxes] = woff + inc;
+    __syncthreads();
+    const int total = s_off[kClsBoxes];
+    // the box of flattened entry f: the last box whose first entry is <= f
+    auto box_of = [&](int f) {
+        int lo = 0, hi = kClsBoxes - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_off[mid] <= f) lo = mid;
+            else hi = mid - 1;
+        }
+        return lo;
+    };
+    for (int f = tid; f < total; f += kClsBoxes) {
+        const int i = box_of(f);
+        atomicAdd(&hist[a.lv[s_li[i]].m2l[(size_t)s_b[i] * a.cap + (f - s_off[i])].y], 1);
+    }
+    __syncthreads();
+    for (int k = tid; k < a.ncls; k += kClsBoxes) {
         const int h = hist[k];
         if (!BUCKET) {
             if (h) atomicAdd(&cls_cnt[k], h);
@@ -221,51 +269,85 @@ __global__ void __launch_bounds__(kListWarps * 32) tc_classes_kernel(TcArgs a, i
     }
     if (!BUCKET) return;
     __syncthreads();
-    if (!n) return;
-    const TcLevel &v = a.lv[li];
-    const double h = (v.bpid ? a.root + 8 * v.bpid[b] : a.root)[3] / (double)(1 << v.level);
-    const float eh2 = (float)(a.eps2 / (h * h));
-    int2 *wl = a.lv[li].m2l + (size_t)b * a.cap;
-    for (int e = lane; e < n; e += 32) {
-        const int2 en = wl[e];
+    for (int f = tid; f < total; f += kClsBoxes) {
+        const int i = box_of(f);
+        int2 *slot = a.lv[s_li[i]].m2l + (size_t)s_b[i] * a.cap + (f - s_off[i]);
+        const int2 en = *slot;
         const int row = base[en.y] + atomicAdd(&hist[en.y], 1);
         // t = |offset| / rho with rho^2 = |offset|^2 + eps^2 / h^2
-        const float t = rsqrtf(1.0f + eh2 / a.cls_rho2[en.y]);
-        bucket[row] = make_int4(li, en.x, __float_as_int(t), 0);
-        wl[e].x = row;
+        const float t = rsqrtf(1.0f + s_eh2[i] / a.cls_rho2[en.y]);
+        bucket[row] = make_int4(s_li[i], en.x, __float_as_int(t), 0);
+        slot->x = row;
     }
 }
 
 // Pass 2: per class the first entry and first tile, the totals, the overflow
-// flag; cursors cleared for pass 3.  One block of 32 threads.
-__global__ void tc_scan_kernel(int ncls, int64_t cap, int *__restrict__ ctl) {
+// flag; cursors cleared for pass 3.  One block of kScanThreads threads, each
+// scanning up to two consecutive classes.
+constexpr int kScanThreads = 1024;
+
+__global__ void __launch_bounds__(kScanThreads) tc_scan_kernel(int ncls, int64_t cap, int *__restrict__ ctl,
+                                                                int4 *__restrict__ tiles) {
     int *cls_cnt = ctl + kCtl, *cls_off = cls_cnt + ncls, *tile_off = cls_off + ncls, *cursor = tile_off + ncls;
-    const int lane = threadIdx.x;
-    int e_run = 0, t_run = 0;
-    for (int k0 = 0; k0 < ncls; k0 += 32) {
-        const int k = k0 + lane;
-        const int cnt = k < ncls ? cls_cnt[k] : 0, tiles = (cnt + kTile - 1) / kTile;
-        int ce = cnt, ct = tiles;
+    __shared__ int s_e[kScanThreads / 32], s_t[kScanThreads / 32];
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int k0 = 2 * tid;
+    const int c0 = k0 < ncls ? cls_cnt[k0] : 0, c1 = k0 + 1 < ncls ? cls_cnt[k0 + 1] : 0;
+    const int t0 = (c0 + kTile - 1) / kTile, t1 = (c1 + kTile - 1) / kTile;
+    int ce = c0 + c1, ct = t0 + t1;  // inclusive scan over the block
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int ue = __shfl_up_sync(0xffffffffu, ce, o), ut = __shfl_up_sync(0xffffffffu, ct, o);
+        if (lane >= o) {
+            ce += ue;
+            ct += ut;
+        }
+    }
+    if (lane == 31) {
+        s_e[wid] = ce;
+        s_t[wid] = ct;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        int we = s_e[lane], wt = s_t[lane];
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            const int ue = __shfl_up_sync(0xffffffffu, ce, o), ut = __shfl_up_sync(0xffffffffu, ct, o);
+            const int ue = __shfl_up_sync(0xffffffffu, we, o), ut = __shfl_up_sync(0xffffffffu, wt, o);
             if (lane >= o) {
-                ce += ue;
-                ct += ut;
+                we += ue;
+                wt += ut;
             }
         }
-        if (k < ncls) {
-            cls_off[k] = e_run + ce - cnt;
-            tile_off[k] = t_run + ct - tiles;
-            cursor[k] = 0;
-        }
-        e_run += __shfl_sync(0xffffffffu, ce, 31);
-        t_run += __shfl_sync(0xffffffffu, ct, 31);
+        s_e[lane] = we;  // inclusive over warps
+        s_t[lane] = wt;
     }
-    if (lane == 0) {
-        ctl[0] = e_run;
-        ctl[1] = t_run;
-        ctl[2] = (int64_t)e_run > cap ? 1 : 0;
+    __syncthreads();
+    const int pe = (wid ? s_e[wid - 1] : 0) + ce - (c0 + c1), pt = (wid ? s_t[wid - 1] : 0) + ct - (t0 + t1);
+    if (k0 < ncls) {
+        cls_off[k0] = pe;
+        tile_off[k0] = pt;
+        cursor[k0] = 0;
+    }
+    if (k0 + 1 < ncls) {
+        cls_off[k0 + 1] = pe + c0;
+        tile_off[k0 + 1] = pt + t0;
+        cursor[k0 + 1] = 0;
+    }
+    if (tid == kScanThreads - 1) {
+        const int te = s_e[31], tt = s_t[31];
+        ctl[0] = te;
+        ctl[1] = tt;
+        ctl[2] = (int64_t)te > cap ? 1 : 0;
+    }
+    // the tile table: per tile its class, first row and row count (room for
+    // cap / kTile + ncls tiles, which holds whenever the entries fit)
+    if ((int64_t)s_e[31] > cap) return;
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        const int k = k0 + q, cnt = q ? c1 : c0;
+        const int e = q ? pe + c0 : pe, t = q ? pt + t0 : pt;
+        if (k >= ncls) break;
+        for (int j = 0; j * kTile < cnt; j++) tiles[t + j] = make_int4(k, e + j * kTile, min(kTile, cnt - j * kTile), 0);
     }
 }
 
@@ -275,22 +357,84 @@ struct TileArgs {
     const int *ctl;
     int *err;                          // ctl + 3: set when a wait gave up
     const int4 *bucket;
+    const int4 *tiles;                 // per tile: class, first row, row count
     const unsigned char *ops;          // per class: high then low operator image
-    float *rows;
+    unsigned char *rows;               // RowShape::RSTRIDE bytes per entry
     int ncls;
 };
+
+// Rows of the translated expansions and their shared-memory staging:
+// RSTRIDE = the NC float2 coefficients rounded up to 16 bytes (bulk copies
+// move 16-byte multiples between 16-byte aligned addresses); the staging
+// stride SROW is an odd number of 16-byte groups, so the 8 threads of a
+// quarter warp touch 8 different bank groups.  A multipole row starts on an
+// 8-byte boundary; its bulk copy starts at the 16-byte boundary below and
+// covers up to RSTRIDE bytes (so at most 8 bytes past the row, inside the
+// carved arena that holds the multipoles).
+template <int P>
+struct RowShape {
+    static constexpr int NC = P * (P + 1) / 2;
+    static constexpr int RB = 8 * NC;
+    static constexpr int RSTRIDE = (RB + 15) / 16 * 16;
+    static constexpr int SROW = (RSTRIDE / 16) % 2 ? RSTRIDE : RSTRIDE + 16;
+    static constexpr int STAGE = kTile * SROW;
+    // staging buffers that fit beside the operand images: two (the next
+    // tile's rows stream in during this one), one, or none (p = 10: the rows
+    // are read from global memory directly and stored without staging)
+    static constexpr int OPS = 2 * TcShape<P>::ABYTES + 2 * TcShape<P>::BBYTES + 2048;
+    static constexpr int NSTAGE = OPS + 2 * STAGE <= 227 * 1024 ? 2 : (OPS + STAGE <= 227 * 1024 ? 1 : 0);
+    // two operator buffers (the next class's operator streams in during this
+    // tile) when they fit beside the rest
+    static constexpr int NB = OPS + 2 * TcShape<P>::BBYTES + NSTAGE * STAGE <= 227 * 1024 ? 2 : 1;
+    static constexpr int SMEM = 2 * TcShape<P>::ABYTES + NB * 2 * TcShape<P>::BBYTES + NSTAGE * STAGE + 1024;
+    static_assert(SMEM <= 227 * 1024, "the operand images must fit in shared memory");
+};
+
+__device__ __forceinline__ void mbar_arrive_expect(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_s2g(void *dst, const void *src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_u32(src)),
+                 "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+// this thread's bulk stores have finished reading shared memory
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// ... and have completed
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+// Issue this thread's bulk copy of its row (bucket record bk, when mine) of
+// a tile into the staging buffer, arriving on bar with the bytes it expects.
+template <int P>
+__device__ __forceinline__ void gather_row(const int4 &bk, bool mine, const TileArgs &a, unsigned char *stage,
+                                           uint64_t *bar) {
+    using Rw = RowShape<P>;
+    if (mine) {
+        const uintptr_t src = (uintptr_t)(a.M[bk.x] + (size_t)bk.y * Rw::NC);
+        const uintptr_t al = src & ~(uintptr_t)15;
+        const uint32_t bytes = (uint32_t)((src - al + Rw::RB + 15) & ~(uintptr_t)15);
+        mbar_arrive_expect(bar, bytes);
+        bulk_g2s(stage + threadIdx.x * Rw::SROW, (const void *)al, bytes, bar);
+    } else {
+        mbar_arrive_expect(bar, 0);
+    }
+}
 
 template <int P>
 __global__ void __launch_bounds__(kTcThreads) m2l_tc_tiles_kernel(TileArgs a) {
     using S = TcShape<P>;
+    using Rw = RowShape<P>;
     extern __shared__ unsigned char dyn[];
-    // 1024-byte aligned operand images: A high, A low, B high, B low
+    // 1024-byte aligned: A high, A low, B high, B low, staging buffer(s)
     unsigned char *base = (unsigned char *)(((uintptr_t)dyn + 1023) & ~(uintptr_t)1023);
     unsigned char *a_hi = base, *a_lo = base + S::ABYTES, *b_img = base + 2 * S::ABYTES;
-    __shared__ __align__(8) uint64_t bar_b, bar_mma;
+    unsigned char *stage0 = b_img + Rw::NB * 2 * S::BBYTES;
+    __shared__ __align__(8) uint64_t bar_b[2], bar_mma, bar_row[2];
     __shared__ uint32_t tmem_slot;
     __shared__ int s_abort;
-    const int *cls_cnt = a.ctl + kCtl, *cls_off = cls_cnt + a.ncls, *tile_off = cls_off + a.ncls;
     if (a.ctl[2]) return;  // overflow: the rotation M2L runs instead
     const int total = a.ctl[1];
     // contiguous tile ranges per CTA: neighbouring tiles share their class
@@ -305,8 +449,11 @@ __global__ void __launch_bounds__(kTcThreads) m2l_tc_tiles_kernel(TileArgs a) {
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
     if (tid == 0) {
-        mbar_init(&bar_b, 1);
+        mbar_init(&bar_b[0], 1);
+        mbar_init(&bar_b[1], 1);
         mbar_init(&bar_mma, 1);
+        mbar_init(&bar_row[0], kTcThreads);
+        mbar_init(&bar_row[1], kTcThreads);
         s_abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -315,48 +462,77 @@ __global__ void __launch_bounds__(kTcThreads) m2l_tc_tiles_kernel(TileArgs a) {
     tc_fence_after();
     const uint32_t tmem = tmem_slot;
     constexpr uint32_t idesc = idesc_tf32(kTile, S::N);
-    uint32_t ph_b = 0, ph_mma = 0;
-    int loaded = -1;
-    // the class of the first tile: binary search over the tile offsets
-    int cls = 0;
-    {
-        int lo = 0, hi = a.ncls - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (tile_off[mid] <= t0) lo = mid;
-            else hi = mid - 1;
-        }
-        cls = lo;
+    // phase parities and pending flags (bit k: staging / operator buffer k)
+    uint32_t ph_b = 0, ph_mma = 0, ph_rows = 0, rows_pending = 0, b_pending = 0;
+    bool aborted = false, mma_pending = false;
+    int bcls0 = -1, bcls1 = -1;  // class whose operator each buffer holds (or is loading)
+    // tile records (class, first row, row count) one and two tiles ahead, and
+    // the bucket record of this thread's row of the current and next tile,
+    // are loaded an iteration before they are needed
+    const int4 none = make_int4(0, 0, 0, 0);
+    int4 rec = a.tiles[t0], rec_n = t0 + 1 < t1 ? a.tiles[t0 + 1] : none;
+    int4 bk = tid < rec.z ? a.bucket[rec.y + tid] : none;
+    if (Rw::NSTAGE > 0) {
+        gather_row<P>(bk, tid < rec.z, a, stage0, &bar_row[0]);
+        rows_pending |= 1u;
     }
-    bool aborted = false, b_pending = false, mma_pending = false;
     for (int t = t0; t < t1; t++) {
-        // the last class whose first tile is at or before t (classes without
-        // entries share their tile offset with the next class)
-        while (cls + 1 < a.ncls && tile_off[cls + 1] <= t) cls++;
-        const int row0 = cls_off[cls] + (t - tile_off[cls]) * kTile;
-        const int nrows = min(kTile, cls_off[cls] + cls_cnt[cls] - row0);
-        const bool load_b = cls != loaded;
-        if (load_b && tid == 0) {
-            mbar_expect_tx(&bar_b, 2 * S::BBYTES);
-            bulk_g2s(b_img, a.ops + (size_t)cls * 2 * S::BBYTES, 2 * S::BBYTES, &bar_b);
-            b_pending = true;
+        const int sb = Rw::NSTAGE == 2 ? (t - t0) & 1 : 0;
+        unsigned char *stage = stage0 + sb * Rw::STAGE;
+        const int4 rec_nn = t + 2 < t1 ? a.tiles[t + 2] : none;
+        const int4 bk_n = t + 1 < t1 && tid < rec_n.z ? a.bucket[rec_n.y + tid] : none;
+        const int cls = rec.x, row0 = rec.y, nrows = rec.z;
+        const int ncls_next = t + 1 < t1 ? rec_n.x : cls;
+        // prefetch the next tile's rows into the other staging buffer (its
+        // previous contents, the rows stored two tiles ago, read out first)
+        if (Rw::NSTAGE == 2 && t + 1 < t1) {
+            bulk_wait_read();
+            gather_row<P>(bk_n, tid < rec_n.z, a, stage0 + (sb ^ 1) * Rw::STAGE, &bar_row[sb ^ 1]);
+            rows_pending |= 1u << (sb ^ 1);
         }
-        loaded = cls;
-        // gather: thread r takes row r of the tile
-        int lvl = 0;
+        // the class operator: in a buffer already, or loaded now into the
+        // buffer that does not hold the next tile's class; the next tile's
+        // operator, when it differs, streams into the other buffer
+        int bsel = bcls0 == cls ? 0 : (Rw::NB == 2 && bcls1 == cls ? 1 : -1);
+        if (bsel < 0) {
+            bsel = Rw::NB == 2 && bcls0 == ncls_next ? 1 : 0;
+            if (tid == 0) {
+                mbar_expect_tx(&bar_b[bsel], 2 * S::BBYTES);
+                bulk_g2s(b_img + bsel * 2 * S::BBYTES, a.ops + (size_t)cls * 2 * S::BBYTES, 2 * S::BBYTES,
+                         &bar_b[bsel]);
+            }
+            b_pending |= 1u << bsel;
+            if (bsel) bcls1 = cls;
+            else bcls0 = cls;
+        }
+        if (Rw::NB == 2 && ncls_next != cls && (bsel ? bcls0 : bcls1) != ncls_next) {
+            const int o = bsel ^ 1;
+            if (tid == 0) {
+                mbar_expect_tx(&bar_b[o], 2 * S::BBYTES);
+                bulk_g2s(b_img + o * 2 * S::BBYTES, a.ops + (size_t)ncls_next * 2 * S::BBYTES, 2 * S::BBYTES,
+                         &bar_b[o]);
+            }
+            b_pending |= 1u << o;
+            if (o) bcls1 = ncls_next;
+            else bcls0 = ncls_next;
+        }
+        // this tile's rows have landed
+        if (Rw::NSTAGE > 0) {
+            if (!__syncthreads_and(mbar_wait_bounded(&bar_row[sb], (ph_rows >> sb) & 1u))) {
+                aborted = true;
+                break;
+            }
+            ph_rows ^= 1u << sb;
+            rows_pending &= ~(1u << sb);
+        }
+        // convert: thread r scales row r by t^n, splits it into TF32 high / low
         float tfac = 1.0f;
         if (tid < nrows) {
-            const int4 bk = a.bucket[row0 + tid];
-            lvl = bk.x;
             tfac = __int_as_float(bk.z);
-            const float2 *src = a.M[lvl] + (size_t)bk.y * S::NC;
-            float mv[2 * S::NC];
-#pragma unroll
-            for (int c = 0; c < S::NC; c++) {
-                const float2 v = __ldg(src + c);
-                mv[2 * c] = v.x;
-                mv[2 * c + 1] = v.y;
-            }
+            const float2 *msrc = a.M[bk.x] + (size_t)bk.y * Rw::NC;
+            const float *mv = Rw::NSTAGE > 0
+                                  ? reinterpret_cast<const float *>(stage + tid * Rw::SROW + ((uintptr_t)msrc & 15))
+                                  : reinterpret_cast<const float *>(msrc);
             float tp[P];
             tp[0] = 1.0f;
 #pragma unroll
@@ -381,17 +557,17 @@ __global__ void __launch_bounds__(kTcThreads) m2l_tc_tiles_kernel(TileArgs a) {
         __syncthreads();
         if (tid == 0) {
             bool ok = true;
-            if (load_b) {
-                ok = mbar_wait_bounded(&bar_b, ph_b);
+            if (b_pending & (1u << bsel)) {
+                ok = mbar_wait_bounded(&bar_b[bsel], (ph_b >> bsel) & 1u);
                 if (ok) {
-                    ph_b ^= 1;
-                    b_pending = false;
+                    ph_b ^= 1u << bsel;
+                    b_pending &= ~(1u << bsel);
                 }
             }
             if (ok) {
                 tc_fence_after();
-                const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo), bh = smem_u32(b_img),
-                               bl = smem_u32(b_img + S::BBYTES);
+                const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo), bh = smem_u32(b_img + bsel * 2 * S::BBYTES),
+                               bl = bh + S::BBYTES;
                 // lo.hi + hi.lo first (the small terms), then hi.hi
                 const uint32_t as[3] = {al, ah, ah}, bs[3] = {bh, bl, bh};
 #pragma unroll
@@ -412,15 +588,16 @@ __global__ void __launch_bounds__(kTcThreads) m2l_tc_tiles_kernel(TileArgs a) {
             break;
         }
         // every thread waits for the accumulator; the CTA decides together
-        const bool done = __syncthreads_and(mbar_wait_bounded(&bar_mma, ph_mma));
-        if (!done) {
+        if (!__syncthreads_and(mbar_wait_bounded(&bar_mma, ph_mma))) {
             aborted = true;
             break;
         }
         ph_mma ^= 1;
         mma_pending = false;
         tc_fence_after();
-        // epilogue: warp w reads lanes 32w.. (its threads' rows)
+        // epilogue: warp w reads lanes 32w.. (its threads' rows), scales the
+        // degree-j outputs by t^(j+1), writes the row into its (consumed)
+        // staging row and stores it with one bulk copy
         float out[S::N];
 #pragma unroll
         for (int c = 0; c < S::N; c += 16) tmem_ld16(tmem + ((uint32_t)(32 * warp) << 16) + c, out + c);
@@ -430,25 +607,46 @@ __global__ void __launch_bounds__(kTcThreads) m2l_tc_tiles_kernel(TileArgs a) {
             tq[0] = 1.0f;
 #pragma unroll
             for (int n = 1; n <= P; n++) tq[n] = tq[n - 1] * tfac;
-            float row[2 * S::NC];
+            float row[Rw::RSTRIDE / 4];
 #pragma unroll
-            for (int k = 0; k < 2 * S::NC; k++) row[k] = 0.0f;
+            for (int k = 0; k < Rw::RSTRIDE / 4; k++) row[k] = 0.0f;
 #pragma unroll
             for (int j = 0; j < S::R; j++) row[real_float(j)] = out[j] * tq[real_deg(j) + 1];
-            float2 *dst = reinterpret_cast<float2 *>(a.rows) + (size_t)(row0 + tid) * S::NC;
+            unsigned char *dst = a.rows + (size_t)(row0 + tid) * Rw::RSTRIDE;
+            float4 *st = reinterpret_cast<float4 *>(Rw::NSTAGE > 0 ? stage + tid * Rw::SROW : dst);
 #pragma unroll
-            for (int k = 0; k < S::NC; k++) dst[k] = make_float2(row[2 * k], row[2 * k + 1]);
+            for (int k = 0; k < Rw::RSTRIDE / 16; k++)
+                st[k] = make_float4(row[4 * k], row[4 * k + 1], row[4 * k + 2], row[4 * k + 3]);
+            if (Rw::NSTAGE > 0) {
+                fence_proxy_async();
+                bulk_s2g(dst, st, Rw::RSTRIDE);
+            }
         }
+        if (Rw::NSTAGE == 1 && t + 1 < t1) {
+            // one staging buffer: the next tile's rows after this tile's stores
+            bulk_wait_read();
+            gather_row<P>(bk_n, tid < rec_n.z, a, stage0, &bar_row[0]);
+            rows_pending |= 1u;
+        }
+        rec = rec_n;
+        rec_n = rec_nn;
+        bk = bk_n;
         tc_fence_before();
         __syncthreads();
     }
-    // an abandoned wait may leave a bulk copy or MMA in flight: give them a
-    // bounded time to land before the CTA's shared memory and TMEM go away
-    if (aborted && tid == 0) {
-        atomicExch(a.err, 1);
-        if (b_pending) (void)mbar_wait_bounded(&bar_b, ph_b);
-        if (mma_pending) (void)mbar_wait_bounded(&bar_mma, ph_mma);
+    // an abandoned wait may leave bulk copies or the MMA in flight: give them
+    // a bounded time to land before the CTA's shared memory and TMEM go away
+    if (aborted) {
+        if (rows_pending & 1u) (void)mbar_wait_bounded(&bar_row[0], ph_rows & 1u);
+        if (rows_pending & 2u) (void)mbar_wait_bounded(&bar_row[1], (ph_rows >> 1) & 1u);
+        if (tid == 0) {
+            atomicExch(a.err, 1);
+            if (b_pending & 1u) (void)mbar_wait_bounded(&bar_b[0], ph_b & 1u);
+            if (b_pending & 2u) (void)mbar_wait_bounded(&bar_b[1], (ph_b >> 1) & 1u);
+            if (mma_pending) (void)mbar_wait_bounded(&bar_mma, ph_mma);
+        }
     }
+    bulk_wait_all();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
@@ -460,7 +658,7 @@ __global__ void __launch_bounds__(kTcThreads) m2l_tc_tiles_kernel(TileArgs a) {
 // partials the L2L pass reads (the rotation M2L's warp / chunk layout).
 template <int P>
 __global__ void __launch_bounds__(128) m2l_tc_reduce_kernel(TcArgs a, const int *__restrict__ ctl,
-                                                            const float2 *__restrict__ rows) {
+                                                            const unsigned char *__restrict__ rows) {
     constexpr int NC = P * (P + 1) / 2;
     if (ctl[2]) return;
     const int lane = threadIdx.x & 31;
@@ -474,16 +672,30 @@ __global__ void __launch_bounds__(128) m2l_tc_reduce_kernel(TcArgs a, const int 
     const int e0 = ch * per, e1 = min(cnt, e0 + per);
     const int2 *lst = v.m2l + (size_t)b * a.cap;
     float2 acc0 = make_float2(0.f, 0.f), acc1 = make_float2(0.f, 0.f);
-    const int c1 = lane + 32;
-    for (int e = e0; e < e1; e++) {
-        const float2 *r = rows + (size_t)lst[e].x * NC;
-        const float2 x = r[lane < NC ? lane : 0];
-        acc0.x += x.x;
-        acc0.y += x.y;
-        if (c1 < NC) {
-            const float2 y = r[c1];
-            acc1.x += y.x;
-            acc1.y += y.y;
+    const int c0 = lane < NC ? lane : 0, c1 = lane + 32;
+    // 32 row numbers at a time (one per lane), then their rows four at a
+    // time, added in list order
+    for (int e = e0; e < e1; e += 32) {
+        const int m = min(32, e1 - e);
+        const int my = lane < m ? lst[e + lane].x : 0;
+        for (int k = 0; k < m; k += 4) {
+            float2 x[4], y[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int rr = __shfl_sync(0xffffffffu, my, min(k + u, m - 1));
+                const float2 *r = reinterpret_cast<const float2 *>(rows + (size_t)rr * RowShape<P>::RSTRIDE);
+                x[u] = r[c0];
+                y[u] = c1 < NC ? r[c1] : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                if (k + u < m) {
+                    acc0.x += x[u].x;
+                    acc0.y += x[u].y;
+                    acc1.x += y[u].x;
+                    acc1.y += y[u].y;
+                }
+            }
         }
     }
     float2 *dst = v.out + ((size_t)b * v.chunks + ch) * NC;
@@ -493,37 +705,37 @@ __global__ void __launch_bounds__(128) m2l_tc_reduce_kernel(TcArgs a, const int 
 
 template <int P>
 sv_status launch_tc(sv_ctx *c, M2LTc &T, const TcArgs &a, int reduce_warps, cudaStream_t s) {
-    using S = TcShape<P>;
-    static_assert(S::N <= kTmemCols, "accumulator wider than the TMEM allocation");
-    const int blocks = div_up(a.total_boxes, kListWarps);
+    static_assert(TcShape<P>::N <= kTmemCols, "accumulator wider than the TMEM allocation");
+    const int blocks = std::max(1, div_up(a.total_boxes, kClsBoxes));
     SV_CK(c, cudaMemsetAsync(T.ctl, 0, sizeof(int) * (kCtl + (size_t)a.ncls), s));
-    tc_classes_kernel<false><<<blocks, kListWarps * 32, 0, s>>>(a, T.ctl, T.bucket);
+    tc_classes_kernel<false><<<blocks, kClsBoxes, 0, s>>>(a, T.ctl, T.bucket);
     SV_LAUNCHED(c);
-    tc_scan_kernel<<<1, 32, 0, s>>>(a.ncls, T.cap, T.ctl);
+    tc_scan_kernel<<<1, kScanThreads, 0, s>>>(a.ncls, T.cap, T.ctl, T.tiles);
     SV_LAUNCHED(c);
-    tc_classes_kernel<true><<<blocks, kListWarps * 32, 0, s>>>(a, T.ctl, T.bucket);
+    tc_classes_kernel<true><<<blocks, kClsBoxes, 0, s>>>(a, T.ctl, T.bucket);
     SV_LAUNCHED(c);
     TileArgs ta{};
     for (int l = 0; l < a.nlev; l++) ta.M[l] = a.lv[l].M;
     ta.ctl = T.ctl;
     ta.err = T.ctl + 3;
     ta.bucket = T.bucket;
+    ta.tiles = T.tiles;
     ta.ops = (const unsigned char *)T.ops;
-    ta.rows = T.rows;
+    ta.rows = (unsigned char *)T.rows;
     ta.ncls = a.ncls;
     static bool attr_set[64] = {};
     int dev = 0;
     SV_CK(c, cudaGetDevice(&dev));
     if (dev >= 0 && dev < 64 && !attr_set[dev]) {
-        SV_CK(c, cudaFuncSetAttribute(m2l_tc_tiles_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM));
+        SV_CK(c, cudaFuncSetAttribute(m2l_tc_tiles_kernel<P>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      RowShape<P>::SMEM));
         attr_set[dev] = true;
     }
-    // two CTAs per SM where their shared memory fits (one gathers while the
-    // other's MMA / epilogue runs), else one
-    const int per_sm = 2 * (S::SMEM + 1024) <= 227 * 1024 ? 2 : 1;
-    m2l_tc_tiles_kernel<P><<<per_sm * device_sms(), kTcThreads, S::SMEM, s>>>(ta);
+    // one CTA per SM; its next tile's rows stream in (bulk copies) while the
+    // current tile converts, multiplies and stores
+    m2l_tc_tiles_kernel<P><<<device_sms(), kTcThreads, RowShape<P>::SMEM, s>>>(ta);
     SV_LAUNCHED(c);
-    m2l_tc_reduce_kernel<P><<<div_up(reduce_warps, 4), 128, 0, s>>>(a, T.ctl, (const float2 *)T.rows);
+    m2l_tc_reduce_kernel<P><<<div_up(reduce_warps, 4), 128, 0, s>>>(a, T.ctl, (const unsigned char *)T.rows);
     SV_LAUNCHED(c);
     // entries, tiles, overflow and timeout flags: sizing of the next evaluation, error report
     SV_CK(c, cudaMemcpyAsync(T.h_ctl, T.ctl, sizeof(int) * kCtl, cudaMemcpyDeviceToHost, s));
@@ -583,7 +795,10 @@ sv_status m2l_tc_prepare(sv_ctx *c, M2LTc &T, int p, int ws, int64_t entries) {
         cudaFree(T.ctl);
         T.ctl = nullptr;
         SV_CK(c, cudaMalloc(&T.ctl, sizeof(int) * (kCtl + 4 * (size_t)T.ncls)));
-        if (!T.h_ctl) SV_CK(c, cudaMallocHost(&T.h_ctl, sizeof(int) * kCtl));
+        if (!T.h_ctl) {
+            SV_CK(c, cudaMallocHost(&T.h_ctl, sizeof(int) * kCtl));
+            memset(T.h_ctl, 0, sizeof(int) * kCtl);
+        }
         T.p = p;
         T.ws = ws;
         T.cap = 0;  // rows depend on the order
@@ -591,12 +806,16 @@ sv_status m2l_tc_prepare(sv_ctx *c, M2LTc &T, int p, int ws, int64_t entries) {
     if (entries > T.cap) {
         cudaFree(T.bucket);
         cudaFree(T.rows);
+        cudaFree(T.tiles);
         T.bucket = nullptr;
         T.rows = nullptr;
+        T.tiles = nullptr;
         T.cap = 0;
         const int64_t cap = std::max<int64_t>(entries, 1 << 16);
         SV_CK(c, cudaMalloc(&T.bucket, sizeof(int4) * (size_t)cap));
-        SV_CK(c, cudaMalloc(&T.rows, sizeof(float) * (size_t)(p * (p + 1)) * (size_t)cap));
+        SV_CK(c, cudaMalloc(&T.tiles, sizeof(int4) * (size_t)(cap / kTile + T.ncls + 1)));
+        const size_t rstride = ((size_t)p * (p + 1) * 4 + 15) / 16 * 16;  // RowShape<p>::RSTRIDE
+        SV_CK(c, cudaMalloc(&T.rows, rstride * (size_t)cap));
         T.cap = cap;
     }
     return SV_OK;
@@ -617,6 +836,7 @@ void m2l_tc_free(M2LTc &T) {
     cudaFree(T.ctl);
     cudaFree(T.bucket);
     cudaFree(T.rows);
+    cudaFree(T.tiles);
     if (T.h_ctl) cudaFreeHost(T.h_ctl);
     T = M2LTc();
 }

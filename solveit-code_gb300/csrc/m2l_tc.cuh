@@ -57,9 +57,12 @@ struct M2LTc {
     int *ctl = nullptr;           // [0] entries, [1] tiles, [2] overflow, [3] wait timed out, then per class:
                                   // count, entry offset, tile offset, cursor
     int4 *bucket = nullptr;       // per entry in class order: level, source box, t (float bits), -
-    float *rows = nullptr;        // per entry in class order: the translated expansion (2 NC floats)
+    int4 *tiles = nullptr;        // per tile of 128 entries: class, first row, row count
+    void *rows = nullptr;         // per entry in class order: the translated expansion (NC float2, rows
+                                  // padded to 16-byte multiples)
     int64_t cap = 0;              // entries bucket / rows hold
     int *h_ctl = nullptr;         // pinned copy of ctl[0..3]
+    bool launched = false;        // the last evaluation launched the tensor-core M2L
 };
 
 // Build (once per order / separation) and upload the class operators;

@@ -52,7 +52,8 @@ class Params(C.Structure):
         ("fmm_order", C.c_int32), ("fmm_ws", C.c_int32), ("fmm_leaf_target", C.c_int32),
         ("sym_axes", C.c_int32 * 3), ("sym_levels", C.c_int32), ("domain_size", C.c_double * 3),
         ("device", C.c_int32), ("profile_phases", C.c_int32), ("fmm_type", C.c_int32),
-        ("fmm_root_scale", C.c_float), ("fmm_direct_pairs", C.c_int32), ("reserved", C.c_int32 * 3),
+        ("fmm_root_scale", C.c_float), ("fmm_direct_pairs", C.c_int32), ("fmm_m2l_tc", C.c_int32),
+        ("reserved", C.c_int32 * 2),
     ]
 
 
@@ -60,7 +61,7 @@ class Stats(C.Structure):
     _fields_ = [
         ("pair_interactions", C.c_double), ("cell_interactions", C.c_double),
         ("flops_algorithmic", C.c_double), ("ms_total", C.c_double), ("ms_phase", C.c_double * 8),
-        ("levels", C.c_int32), ("boxes", C.c_int32), ("reserved", C.c_int32 * 6),
+        ("levels", C.c_int32), ("boxes", C.c_int32), ("m2l_tc", C.c_int32), ("reserved", C.c_int32 * 5),
     ]
 
 
