@@ -55,6 +55,9 @@ WORKLOADS = {
     "fmm_n1m": dict(n=1 << 20, length=50e-6, method="fmm", order=8, ws=2, leaf=32, seed=2000,
                     desc="FMM p=8 ws=2, N=1048576 ions, plume r=20nm z=50um, eps=1e-10m, "
                          "leapfrog DKD dt=1e-13s, E_z=1e8V/m"),
+    "bh_n65536": dict(n=65536, length=10e-6, method="bh", theta=0.5, leaf=16, seed=1,
+                      desc="Barnes-Hut theta=0.5 leaf 16 (stackless warp walk, FP32 forces, FP64 integration), "
+                           "N=65536 ions, plume r=20nm z=10um, eps=1e-10m, leapfrog DKD dt=1e-13s, E_z=1e8V/m"),
     "direct_n4096": dict(n=4096, length=1e-6, method="direct", precision="fp64", seed=0,
                          desc="FP64 direct sum, N=4096 ions, plume r=20nm z=1um, eps=1e-10m, "
                               "leapfrog DKD dt=1e-13s, E_z=1e8V/m"),
@@ -525,6 +528,8 @@ def run_ours(args, wl, rank, world, local):
     if wl["method"] == "fmm":
         kw = dict(method=sv.FMM, precision=sv.MIXED, fmm_order=wl["order"], fmm_ws=wl["ws"],
                   fmm_leaf_target=wl["leaf"], fmm_m2l_tc=args.m2l_tc)
+    elif wl["method"] == "bh":
+        kw = dict(method=sv.BARNES_HUT, precision=sv.MIXED, theta=wl["theta"], leaf_size=wl["leaf"])
     else:
         kw = dict(method=sv.DIRECT, precision=sv.FP64 if wl.get("precision") == "fp64" else sv.MIXED)
     fm = sv.ForceMethod(softening2=EPS2, efield=(0.0, 0.0, EZ), device=local, profile_phases=1, **kw)
@@ -674,13 +679,24 @@ def run_ours(args, wl, rank, world, local):
                                 "pairs_per_step": stats.pair_interactions,
                                 "m2l_per_step": stats.cell_interactions,
                                 "m2l_flop_per_step": m2l_flop}
+        elif wl["method"] == "bh":
+            dom_ms = phase_ms[6]
+            achieved = stats.flops_algorithmic / (dom_ms * 1e-3) / 1e12
+            line["roofline"] = {"kernel": "bh_walk_kernel (accepted cells + leaf pairs, 20 flop each)",
+                                "bound": "fp32 (a divergent, latency-bound walk)", "achieved": achieved,
+                                "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
+                                "peak_source": f"FP32 FMA rate {sms} SMs x 128 lanes x 2 flop x sm_max_mhz "
+                                               f"{sm_max:.0f} of MEASURED_PEAKS.json",
+                                "timing": "CUDA events around the walk on the context stream, averaged over the "
+                                          "timed steps",
+                                "cells_per_step": stats.cell_interactions, "pairs_per_step": stats.pair_interactions}
         else:
             dom_ms = phase_ms[6]
             achieved = stats.flops_algorithmic / (dom_ms * 1e-3) / 1e12
             line["roofline"] = {"kernel": "direct kernel", "bound": "fp64", "achieved": achieved,
                                 "peak": None, "unit": "TFLOP/s", "frac": None, "traffic": None}
         # ---- force error against the FP64 GPU direct sum on sampled targets
-        if wl["method"] == "fmm":
+        if wl["method"] in ("fmm", "bh"):
             x, v, stt = fm.download()
             cur = dict(st, x=x, v=v, status=stt)
             a_fmm = fm.accel()
@@ -692,7 +708,7 @@ def run_ours(args, wl, rank, world, local):
             line["force_err_sample"] = ("512 random targets of the state after the timed steps, against the "
                                         "plain FP64 GPU direct sum (pinned to the CPU oracle by the GPU tests)")
             # ---- plain FP64 GPU direct path on the same GPU
-            m = 131072
+            m = min(n, 131072)
             sub = {k: (st[k][:m] if hasattr(st[k], "__len__") else st[k]) for k in st}
             with sv.ForceMethod(softening2=EPS2, method=sv.DIRECT, precision=sv.FP64, device=local,
                                 efield=(0.0, 0.0, EZ)) as f64:

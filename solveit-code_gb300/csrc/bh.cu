@@ -22,15 +22,20 @@
 //     relative to the root origin, so (target - centre) is formed as
 //     (t_hi - c_hi) + (t_lo - c_lo): FP64-like differences with FP32
 //     arithmetic only (the walk has no FP64 instruction);
-//   * the walk is warp-cooperative: a warp owns 32 Morton-consecutive targets
-//     and a shared-memory stack of (cell, lane mask) entries; a cell is
-//     visited once per warp, each lane applies its own acceptance test, lanes
-//     that accept add the monopole, the ballot of lanes that reject either
-//     pushes the children with that mask or, for a leaf, runs the direct sum
-//     over the leaf's particles.  Each target therefore gets exactly the
-//     cells its own stackless walk would accept, while the warp walks
-//     coherently.  The stack depth is bounded (8 per level); an overflow sets
-//     an error flag instead of running past the buffer.
+//   * the walk is warp-cooperative and stackless, over the tree threaded the
+//     way the reference threads its cells (nextSibling, cell.h:33-35,
+//     cell.cpp:171-172): every cell keeps a skip link to the next cell of
+//     the depth-first order outside its own subtree (its next sibling, else
+//     its parent's skip link).  A warp owns 32 Morton-consecutive targets
+//     and walks one cell at a time; each lane keeps one bit per level, set
+//     when it rejected the current ancestor at that level, so a lane takes
+//     part at a cell when it rejected the cell's parent.  Taking part, it
+//     applies its own acceptance test and adds the monopole when it
+//     accepts; when some lane rejects, the warp goes down to the first child
+//     (or, at a leaf, the rejecting lanes sum the leaf's particles
+//     directly), else it follows the skip link.  Each target gets exactly
+//     the cells its own walk would accept, the warp visits a cell at most
+//     once, and no stack bounds the depth.
 #include <cfloat>
 
 #include "sv_internal.cuh"
@@ -43,26 +48,58 @@ struct Bh {
     size_t arena_bytes = 0;
     float4 *ph = nullptr, *pl = nullptr;  // particle hi (xyz, q) and lo (xyz, 0)
     int64_t pcap = 0;
-    int *d_err = nullptr;
     unsigned long long *d_counts = nullptr;  // [0] accepted cells, [1] direct pairs
     unsigned long long *h_counts = nullptr;
-    int *h_err = nullptr;
 };
 
 namespace {
 
 constexpr int kBhWarps = 4;
-constexpr int kStack = 8 * (kMortonBits + 2);
 
 struct BhLevels {
     const float4 *nh[kMortonBits + 1];  // centre hi (xyz) + net charge
     const float4 *nl[kMortonBits + 1];  // centre lo (xyz) + delta
     const int *child0[kMortonBits + 1];
     const int *start[kMortonBits + 1];
+    const int *skip[kMortonBits + 1];   // next cell of the depth-first order outside the subtree, or kEnd
     float side[kMortonBits + 1];
     int deepest;
     int leaf_size;
 };
+
+// a cell as (level << 24) | box, and the end of the walk
+constexpr int kEnd = -1;
+__host__ __device__ __forceinline__ int cell_id(int l, int b) { return (l << 24) | b; }
+
+// Skip links of every cell of levels 0..D, one thread per cell: its next
+// sibling (same parent), else the first ancestor's next sibling, else kEnd.
+struct SkipArgs {
+    const int *parent[kMortonBits + 1];
+    int *skip[kMortonBits + 1];
+    int nbox[kMortonBits + 1];
+    int first[kMortonBits + 2];  // first global cell of each level; first[D + 1] = all cells
+    int D;
+};
+
+__global__ void skip_links_kernel(SkipArgs a) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= a.first[a.D + 1]) return;
+    int l = 0;
+    while (l < a.D && g >= a.first[l + 1]) l++;
+    const int b0 = g - a.first[l];
+    int lv = l, b = b0, out = kEnd;
+    for (;;) {
+        const bool sib = b + 1 < a.nbox[lv] && (lv == 0 || a.parent[lv][b + 1] == a.parent[lv][b]);
+        if (sib) {
+            out = cell_id(lv, b + 1);
+            break;
+        }
+        if (lv == 0) break;
+        b = a.parent[lv][b];
+        lv--;
+    }
+    a.skip[l][b0] = out;
+}
 
 struct BhImages {
     int kind;  // 0 none, 1 rotational, 2 translational offsets
@@ -172,8 +209,7 @@ bh_walk_kernel(BhLevels T, const float4 *__restrict__ ph, const float4 *__restri
                const double *__restrict__ xs, const double *__restrict__ ys, const double *__restrict__ zs,
                const double *__restrict__ qm, int n, const double *__restrict__ root, float theta, float eps2,
                BhImages im, double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az,
-               int *__restrict__ err, unsigned long long *__restrict__ counts) {
-    __shared__ int2 stack[kBhWarps][kStack];
+               unsigned long long *__restrict__ counts) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int i = (blockIdx.x * kBhWarps + wid) * 32 + lane;
     const bool live = i < n && qm[i] != 0.0;
@@ -208,60 +244,52 @@ bh_walk_kernel(BhLevels T, const float4 *__restrict__ ph, const float4 *__restri
         split_hilo(ty - root[1], thy, tly);
         split_hilo(tz - root[2], thz, tlz);
         float fx = 0.f, fy = 0.f, fz = 0.f;
-        int sp = 0;
-        if (lane == 0) stack[wid][0] = make_int2(0, (int)live_mask);
-        sp = 1;
-        __syncwarp();
-        while (sp > 0) {
-            sp--;
-            const int2 e = stack[wid][sp];
-            __syncwarp();
-            const int lvl = e.x >> 24, b = e.x & 0xffffff;
-            const unsigned mask = (unsigned)e.y;
-            const bool mine = (mask >> lane) & 1u;
-            const float4 h = T.nh[lvl][b], lo = T.nl[lvl][b];
-            const float dx = (thx - h.x) + (tlx - lo.x), dy = (thy - h.y) + (tly - lo.y),
-                        dz = (thz - h.z) + (tlz - lo.z);
-            const float d = sqrtf(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2))));
-            const bool acc = mine && theta * (d - lo.w) > T.side[lvl];
-            if (acc) {
-                const float f = h.w / (d * d * d);
-                fx = fmaf(f, dx, fx);
-                fy = fmaf(f, dy, fy);
-                fz = fmaf(f, dz, fz);
-                n_cells++;
-            }
-            const unsigned rej = __ballot_sync(0xffffffffu, mine && !acc);
-            if (rej == 0) continue;
-            const int s0 = T.start[lvl][b], s1 = T.start[lvl][b + 1];
-            const bool leaf = lvl == T.deepest || (s1 - s0) <= T.leaf_size;
-            if (leaf) {
-                const bool me = (rej >> lane) & 1u;
-                for (int j = s0; j < s1; j++) {
-                    const float4 qh = ph[j], ql = pl[j];
-                    if (me && !(self_excl && j == i)) {
-                        const float ex = (thx - qh.x) + (tlx - ql.x), ey = (thy - qh.y) + (tly - ql.y),
-                                    ez = (thz - qh.z) + (tlz - ql.z);
-                        const float dd = sqrtf(fmaf(ex, ex, fmaf(ey, ey, fmaf(ez, ez, eps2))));
-                        const float f = qh.w / (dd * dd * dd);
-                        fx = fmaf(f, ex, fx);
-                        fy = fmaf(f, ey, fy);
-                        fz = fmaf(f, ez, fz);
-                        n_pairs++;
+        unsigned want = 0;  // bit l: this lane rejected the current cell's ancestor at level l
+        int node = cell_id(0, 0);
+        while (node != kEnd) {
+            const int lvl = node >> 24, b = node & 0xffffff;
+            // taking part: the root for every live target, else the lanes that rejected the parent
+            const bool mine = lvl == 0 ? live : ((want >> (lvl - 1)) & 1u) != 0;
+            bool deeper = false, rej = false;
+            if (__any_sync(0xffffffffu, mine)) {
+                const float4 h = T.nh[lvl][b], lo = T.nl[lvl][b];
+                const float dx = (thx - h.x) + (tlx - lo.x), dy = (thy - h.y) + (tly - lo.y),
+                            dz = (thz - h.z) + (tlz - lo.z);
+                const float d = sqrtf(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2))));
+                const bool acc = mine && theta * (d - lo.w) > T.side[lvl];
+                if (acc) {
+                    const float f = h.w / (d * d * d);
+                    fx = fmaf(f, dx, fx);
+                    fy = fmaf(f, dy, fy);
+                    fz = fmaf(f, dz, fz);
+                    n_cells++;
+                }
+                rej = mine && !acc;
+                if (__any_sync(0xffffffffu, rej)) {
+                    const int s0 = T.start[lvl][b], s1 = T.start[lvl][b + 1];
+                    const bool leaf = lvl == T.deepest || (s1 - s0) <= T.leaf_size;
+                    if (leaf) {
+                        for (int j = s0; j < s1; j++) {
+                            const float4 qh = ph[j], ql = pl[j];
+                            if (rej && !(self_excl && j == i)) {
+                                const float ex = (thx - qh.x) + (tlx - ql.x), ey = (thy - qh.y) + (tly - ql.y),
+                                            ez = (thz - qh.z) + (tlz - ql.z);
+                                const float dd = sqrtf(fmaf(ex, ex, fmaf(ey, ey, fmaf(ez, ez, eps2))));
+                                const float f = qh.w / (dd * dd * dd);
+                                fx = fmaf(f, ex, fx);
+                                fy = fmaf(f, ey, fy);
+                                fz = fmaf(f, ez, fz);
+                                n_pairs++;
+                            }
+                        }
+                    } else {
+                        deeper = true;  // warp-uniform: the cell is internal and some lane rejected it
                     }
                 }
-            } else {
-                const int c0 = T.child0[lvl][b], c1 = T.child0[lvl][b + 1];
-                if (sp + (c1 - c0) > kStack) {
-                    if (lane == 0) atomicExch(err, 1);
-                    break;
-                }
-                // push in reverse so that the first child is visited first
-                if (lane == 0)
-                    for (int c = c1 - 1; c >= c0; c--) stack[wid][sp++] = make_int2(((lvl + 1) << 24) | c, (int)rej);
-                sp = __shfl_sync(0xffffffffu, sp, 0);
-                __syncwarp();
             }
+            // bit lvl: this lane goes below this cell (it rejected an internal cell)
+            want = (deeper && rej) ? (want | (1u << lvl)) : (want & ~(1u << lvl));
+            node = deeper ? cell_id(lvl + 1, T.child0[lvl][b]) : T.skip[lvl][b];
         }
         sx += (float)cb * fx - (float)sb * fy;
         sy += (float)sb * fx + (float)cb * fy;
@@ -292,10 +320,8 @@ sv_status bh_accel(sv_ctx *c) {
         return set_error(c, SV_ERR_UNSUPPORTED, "Barnes-Hut runs in mixed precision only");
     if (!c->bh) {
         c->bh = new Bh();
-        SV_CK(c, cudaMalloc(&c->bh->d_err, sizeof(int)));
         SV_CK(c, cudaMalloc(&c->bh->d_counts, 2 * sizeof(unsigned long long)));
         SV_CK(c, cudaMallocHost(&c->bh->h_counts, 2 * sizeof(unsigned long long)));
-        SV_CK(c, cudaMallocHost(&c->bh->h_err, sizeof(int)));
     }
     Bh &B = *c->bh;
     const int n = (int)c->S.n;
@@ -312,12 +338,13 @@ sv_status bh_accel(sv_ctx *c) {
         return SV_OK;
     }
     const int D = T.deepest;
-    // storage: per level Q, U (double), coc (double3), nh, nl (float4)
+    // storage: per level Q, U (double), coc (double3), nh, nl (float4), skip links (int)
     auto rounded = [](size_t sz) { return (sz + 255) & ~(size_t)255; };
     size_t bytes = 0;
     for (int l = 0; l <= D; l++) {
         const size_t nb = T.lv[l].nbox;
-        bytes += 2 * rounded(nb * sizeof(double)) + rounded(nb * sizeof(double3)) + 2 * rounded(nb * sizeof(float4));
+        bytes += 2 * rounded(nb * sizeof(double)) + rounded(nb * sizeof(double3)) + 2 * rounded(nb * sizeof(float4)) +
+                 rounded(nb * sizeof(int));
     }
     if (B.arena_bytes < bytes) {
         cudaFree(B.arena);
@@ -344,6 +371,8 @@ sv_status bh_accel(sv_ctx *c) {
     double *Q[kMortonBits + 1], *U[kMortonBits + 1];
     double3 *coc[kMortonBits + 1];
     BhLevels L{};
+    SkipArgs sk{};
+    sk.D = D;
     for (int l = 0; l <= D; l++) {
         const size_t nb = T.lv[l].nbox;
         Q[l] = (double *)carve(nb * sizeof(double));
@@ -353,7 +382,14 @@ sv_status bh_accel(sv_ctx *c) {
         L.nl[l] = (const float4 *)carve(nb * sizeof(float4));
         L.child0[l] = T.lv[l].child0;
         L.start[l] = T.lv[l].start;
+        sk.skip[l] = (int *)carve(nb * sizeof(int));
+        L.skip[l] = sk.skip[l];
+        sk.parent[l] = T.lv[l].parent;
+        sk.nbox[l] = (int)nb;
+        sk.first[l + 1] = sk.first[l] + (int)nb;
     }
+    skip_links_kernel<<<div_up(sk.first[D + 1], 256), 256, 0, c->stream>>>(sk);
+    SV_LAUNCHED(c);
     double root[8];
     SV_TRY(read_root(c, root));
     for (int l = 0; l <= D; l++) L.side[l] = (float)(root[3] / (double)(1ll << l));
@@ -392,12 +428,11 @@ sv_status bh_accel(sv_ctx *c) {
         im.count = cnt;
         im.off = d_off;
     }
-    SV_CK(c, cudaMemsetAsync(B.d_err, 0, sizeof(int), c->stream));
     SV_CK(c, cudaMemsetAsync(B.d_counts, 0, 2 * sizeof(unsigned long long), c->stream));
     // inactive sorted slots (beyond n_act) are never targets (qm = 0)
     bh_walk_kernel<<<div_up(n, 32 * kBhWarps), 32 * kBhWarps, 0, c->stream>>>(
         L, B.ph, B.pl, S.x, S.y, S.z, S.qm, T.n_act, S.root, c->P.theta, (float)c->P.softening2, im, S.ax, S.ay,
-        S.az, B.d_err, B.d_counts);
+        S.az, B.d_counts);
     SV_LAUNCHED(c);
     if (T.n_act < n) {
         SV_CK(c, cudaMemsetAsync(S.ax + T.n_act, 0, sizeof(double) * (n - T.n_act), c->stream));
@@ -408,9 +443,7 @@ sv_status bh_accel(sv_ctx *c) {
     if (d_off) SV_CK(c, cudaFreeAsync(d_off, c->stream));
     SV_CK(c, cudaMemcpyAsync(B.h_counts, B.d_counts, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                              c->stream));
-    SV_CK(c, cudaMemcpyAsync(B.h_err, B.d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     SV_CK(c, cudaStreamSynchronize(c->stream));
-    if (*B.h_err) return set_error(c, SV_ERR_CAPACITY, "Barnes-Hut walk stack overflow");
     c->stats.cell_interactions = (double)B.h_counts[0];
     c->stats.pair_interactions = (double)B.h_counts[1];
     c->stats.flops_algorithmic = 20.0 * (c->stats.cell_interactions + c->stats.pair_interactions);
@@ -426,10 +459,8 @@ void bh_free(sv_ctx *c) {
     cudaFree(B.arena);
     cudaFree(B.ph);
     cudaFree(B.pl);
-    cudaFree(B.d_err);
     cudaFree(B.d_counts);
     cudaFreeHost(B.h_counts);
-    cudaFreeHost(B.h_err);
     delete c->bh;
     c->bh = nullptr;
 }

@@ -156,3 +156,54 @@ def test_autograd_function_and_mixed_precision():
     assert np.linalg.norm(gxm - gx64) <= 1e-4 * np.linalg.norm(gx64)
     assert np.linalg.norm(gvm - gv64) <= 1e-4 * np.linalg.norm(gv64)
     assert abs(gem - ge64) <= 1e-4 * abs(ge64)
+
+
+def test_c4_adjoint_against_finite_differences():
+    """The adjoint workload's own configuration: N = 16,384, 50 steps,
+    checkpoint every 10.  The FP64 and the mixed-precision adjoint gradients
+    of the radius term (x0, v0) and of the momentum term (E_z) against
+    central finite differences of the FP64 rollout, to 1e-4.
+
+    Steps are h = 1e-6 of the perturbed vector's norm and h / 2, combined by
+    Richardson extrapolation (4 D(h/2) - D(h)) / 3: along positions the
+    rollout is stiff (pairs pass within a few softening lengths), and the
+    plain central difference at h = 1e-6 keeps an O(h^2) truncation error of
+    ~1e-3 that the extrapolation removes.  Directions: a seeded random one and
+    the radial one (x, y, 0)/r per particle.  The reference function is the
+    FP64 rollout; a finite difference of the mixed-precision rollout itself is
+    limited by its FP32 force rounding (the rollout is not smooth at the
+    1e-6 scale along random directions), and is checked along the radial
+    directions only."""
+    st = plume.make_plume(16384, 1e-6, 4000)
+    nsteps, ckpt = 50, 10
+    gx64, gv64, _ = adjoint(st, nsteps, EZ, sv.FP64, 0.0, 1.0, ckpt)
+    gxm, gvm, _ = adjoint(st, nsteps, EZ, sv.MIXED, 0.0, 1.0, ckpt)
+    r = np.sqrt(st["x"][:, 0] ** 2 + st["x"][:, 1] ** 2)
+    radial = np.stack([st["x"][:, 0] / r, st["x"][:, 1] / r, np.zeros_like(r)], axis=1)
+    rng = np.random.default_rng(16384)
+
+    def radius(s, prec):
+        return loss_terms(*rollout(s, nsteps, EZ, prec, ckpt), st["m"])[1]
+
+    def fd(key, d, rel, prec):
+        eps = rel * np.linalg.norm(st[key]) / np.linalg.norm(d)
+        return (radius(dict(st, **{key: st[key] + eps * d}), prec) -
+                radius(dict(st, **{key: st[key] - eps * d}), prec)) / (2 * eps)
+
+    for key, g64, gm in (("x", gx64, gxm), ("v", gv64, gvm)):
+        for name, d in (("random", rng.normal(size=st[key].shape)), ("radial", radial)):
+            ref = (4 * fd(key, d, 5e-7, sv.FP64) - fd(key, d, 1e-6, sv.FP64)) / 3
+            for g in (g64, gm):
+                ad = float(np.sum(g * d))
+                assert abs(ad - ref) <= 1e-4 * abs(ref), (key, name, ad, ref)
+            if name == "radial":
+                mix = (4 * fd(key, d, 5e-7, sv.MIXED) - fd(key, d, 1e-6, sv.MIXED)) / 3
+                assert abs(float(np.sum(gm * d)) - mix) <= 1e-4 * abs(mix), (key, mix)
+    # the field amplitude, through the momentum term
+    _, _, ge64 = adjoint(st, nsteps, EZ, sv.FP64, 1.0, 0.0, ckpt)
+    _, _, gem = adjoint(st, nsteps, EZ, sv.MIXED, 1.0, 0.0, ckpt)
+    h = 1e-6 * EZ
+    fde = (loss_terms(*rollout(st, nsteps, EZ + h, sv.FP64, ckpt), st["m"])[0] -
+           loss_terms(*rollout(st, nsteps, EZ - h, sv.FP64, ckpt), st["m"])[0]) / (2 * h)
+    for g in (ge64, gem):
+        assert abs(g[2] - fde) <= 1e-4 * abs(fde), (g[2], fde)

@@ -91,3 +91,25 @@ def test_bh_small_and_empty():
         assert a.shape == (n, 3) and np.all(np.isfinite(a))
         if n == 1:
             assert np.all(a == 0.0)
+
+
+def test_bh_deep_clusters_stackless():
+    """Tight clusters inside a long plume make the octree ~20 levels deep with
+    long single-child chains; the stackless walk has no depth bound.  theta =
+    0 still reproduces the direct sum: within 3e-5 here rather than 2e-6,
+    because 200 ions within a picometre sum their softened-core forces with
+    heavy cancellation in FP32 (a sequential FP32 sum of the same pair terms,
+    emulated on the host, is 7.7e-6 off the FP64 sum).  theta = 0.5 stays
+    within 1e-2."""
+    n = 6000
+    st = plume.make_plume(n, 5e-6, 65)
+    rng = np.random.default_rng(66)
+    for k in range(10):
+        c = st["x"][k * 300].copy()
+        st["x"][k * 300:k * 300 + 200] = c + rng.normal(scale=1e-12, size=(200, 3))
+    ref = O.direct_f64(st, EPS20)
+    a0, s0 = run_accel(st, softening2=EPS20, method=sv.BARNES_HUT, theta=0.0, leaf_size=1)
+    assert s0.levels >= 18
+    assert rel_l2(a0, ref, st["status"]) < 3e-5
+    a5, _ = run_accel(st, softening2=EPS20, method=sv.BARNES_HUT, theta=0.5, leaf_size=16)
+    assert rel_l2(a5, ref, st["status"]) < 1e-2
