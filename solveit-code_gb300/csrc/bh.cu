@@ -250,9 +250,13 @@ bh_walk_kernel(BhLevels T, const float4 *__restrict__ ph, const float4 *__restri
             const int lvl = node >> 24, b = node & 0xffffff;
             // taking part: the root for every live target, else the lanes that rejected the parent
             const bool mine = lvl == 0 ? live : ((want >> (lvl - 1)) & 1u) != 0;
+            // everything the cell's visit may need, loaded together: one memory
+            // latency per cell instead of a chain of three
+            const float4 h = T.nh[lvl][b], lo = T.nl[lvl][b];
+            const int s0 = T.start[lvl][b], s1 = T.start[lvl][b + 1];
+            const int child = lvl < T.deepest ? T.child0[lvl][b] : 0, skip = T.skip[lvl][b];
             bool deeper = false, rej = false;
             if (__any_sync(0xffffffffu, mine)) {
-                const float4 h = T.nh[lvl][b], lo = T.nl[lvl][b];
                 const float dx = (thx - h.x) + (tlx - lo.x), dy = (thy - h.y) + (tly - lo.y),
                             dz = (thz - h.z) + (tlz - lo.z);
                 const float d = sqrtf(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2))));
@@ -266,9 +270,9 @@ bh_walk_kernel(BhLevels T, const float4 *__restrict__ ph, const float4 *__restri
                 }
                 rej = mine && !acc;
                 if (__any_sync(0xffffffffu, rej)) {
-                    const int s0 = T.start[lvl][b], s1 = T.start[lvl][b + 1];
                     const bool leaf = lvl == T.deepest || (s1 - s0) <= T.leaf_size;
                     if (leaf) {
+#pragma unroll 4
                         for (int j = s0; j < s1; j++) {
                             const float4 qh = ph[j], ql = pl[j];
                             if (rej && !(self_excl && j == i)) {
@@ -289,7 +293,7 @@ bh_walk_kernel(BhLevels T, const float4 *__restrict__ ph, const float4 *__restri
             }
             // bit lvl: this lane goes below this cell (it rejected an internal cell)
             want = (deeper && rej) ? (want | (1u << lvl)) : (want & ~(1u << lvl));
-            node = deeper ? cell_id(lvl + 1, T.child0[lvl][b]) : T.skip[lvl][b];
+            node = deeper ? cell_id(lvl + 1, child) : skip;
         }
         sx += (float)cb * fx - (float)sb * fy;
         sy += (float)sb * fx + (float)cb * fy;
