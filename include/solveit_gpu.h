@@ -110,7 +110,10 @@ typedef struct {
     int32_t fmm_m2l_tc;        /* M2L translations: 1 = on the tensor cores (offset classes as dense TF32x3
                                 contractions, tcgen05), -1 = the FP32 rotation kernel, 0 = the default
                                 (the tensor cores) */
-    int32_t reserved[2];
+    float fmm_tune_err;        /* sv_fmm_tune's force-error bound: > 0 makes it choose the expansion order
+                                and separation as well (the fastest that meets the bound on sampled
+                                targets); 0 = it tunes the root scale only */
+    int32_t reserved[1];
 } sv_params;
 
 /* Per-call statistics of the last force evaluation. */
@@ -449,7 +452,15 @@ SV_API sv_status sv_batch_tune(sv_ctx *ctx, const char *cache_path, double *best
  * raising maxLevel from measured times, integration_schemes.cpp:470-570): times
  * force evaluations of the uploaded state at fmm_root_scale = 1, 1.125, ...,
  * 1.875 and keeps the fastest in the context's parameters (sv_get_params
- * shows it).  best_ms (nullable) receives its force-evaluation time. */
+ * shows it).  The root scale sets the leaf box side between two octree
+ * levels' sides, so it is also the leaf-size choice.  With fmm_tune_err > 0
+ * it also chooses the expansion order and separation, as the reference's
+ * test cases sweep the order (test_cases.cpp:217-295): for each of (p, ws) =
+ * (6, 2), (8, 1), (8, 2), (10, 1), (10, 2) it tunes the root scale, measures
+ * the per-particle relative-L2 force error on 256 evenly spaced targets
+ * against an FP64 direct sum, and keeps the fastest candidate whose error is
+ * at most fmm_tune_err (the most accurate one when none is).  best_ms
+ * (nullable) receives the kept force-evaluation time. */
 SV_API sv_status sv_fmm_tune(sv_ctx *ctx, double *best_ms);
 /* Sets the two tuned quantities directly (M2L weight >= 1, direct sources
  * per work item >= 256) and re-plans the batch. */

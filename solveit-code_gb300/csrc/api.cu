@@ -325,6 +325,8 @@ sv_status check_params(sv_ctx *c, const sv_params *p) {
     if (p->fmm_type < SV_FMM_FMM || p->fmm_type > SV_FMM_TREECODE_OUTLIERS)
         return set_error(c, SV_ERR_INVALID, "unknown fmm_type %d", p->fmm_type);
     if (p->fmm_m2l_tc < -1 || p->fmm_m2l_tc > 1) return set_error(c, SV_ERR_INVALID, "fmm_m2l_tc must be -1, 0 or 1");
+    if (!(p->fmm_tune_err >= 0.0f) || !std::isfinite(p->fmm_tune_err))
+        return set_error(c, SV_ERR_INVALID, "fmm_tune_err must be finite and >= 0");
     if (!(p->fmm_root_scale == 0.0f || (p->fmm_root_scale >= 1.0f && p->fmm_root_scale < 2.0f)))
         return set_error(c, SV_ERR_INVALID, "fmm_root_scale must be 0 or in [1, 2)");
     if (p->symmetry == SV_SYM_TRANSLATIONAL) {
@@ -348,6 +350,54 @@ int grid_of(int64_t n) { return (int)((n + 255) / 256 > 0 ? (n + 255) / 256 : 1)
 // sequential host loop's; the sum is taken per block, then over blocks in
 // block order.
 constexpr int kCmpThreads = 256;
+
+// The FP64 direct sum at sampled targets (one block per target, threads over
+// the sources, a fixed-order block reduction) beside the context's last
+// acceleration at those targets: out[6 k ..] = reference xyz, evaluated xyz.
+// Targets are the inbound particles, sources status 1 or 2, j != i
+// (direct_force_method.cpp:153-190 in FP64).
+constexpr int kSmpThreads = 256;
+
+__global__ void __launch_bounds__(kSmpThreads)
+sampled_direct_f64_kernel(const int64_t *__restrict__ tg, const double *__restrict__ x, const double *__restrict__ y,
+                          const double *__restrict__ z, const double *__restrict__ q, const double *__restrict__ qom,
+                          const int32_t *__restrict__ st, int64_t n, double eps2, double kconst,
+                          const double *__restrict__ ax, const double *__restrict__ ay,
+                          const double *__restrict__ az, double *__restrict__ out) {
+    const int64_t i = tg[blockIdx.x];
+    const double xi = x[i], yi = y[i], zi = z[i];
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    if (st[i] == 1)
+        for (int64_t j = threadIdx.x; j < n; j += kSmpThreads) {
+            if (j == i || (st[j] != 1 && st[j] != 2)) continue;
+            const double dx = xi - x[j], dy = yi - y[j], dz = zi - z[j];
+            const double r2 = dx * dx + dy * dy + dz * dz + eps2;
+            const double w = q[j] / (r2 * sqrt(r2));
+            sx += w * dx;
+            sy += w * dy;
+            sz += w * dz;
+        }
+    __shared__ double red[3][kSmpThreads];
+    red[0][threadIdx.x] = sx;
+    red[1][threadIdx.x] = sy;
+    red[2][threadIdx.x] = sz;
+    __syncthreads();
+    for (int w = kSmpThreads / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+            for (int d = 0; d < 3; d++) red[d][threadIdx.x] += red[d][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double c = st[i] == 1 ? kconst * qom[i] : 0.0;
+        double *o = out + 6 * blockIdx.x;
+        o[0] = red[0][0] * c;
+        o[1] = red[1][0] * c;
+        o[2] = red[2][0] * c;
+        o[3] = ax[i];
+        o[4] = ay[i];
+        o[5] = az[i];
+    }
+}
 
 __global__ void __launch_bounds__(kCmpThreads)
 compare_partial(const double *__restrict__ ax, const double *__restrict__ ay, const double *__restrict__ az,
@@ -931,14 +981,11 @@ sv_status sv_energy(sv_ctx *c, double *ke, double *pe) {
     return energy(c, ke, pe);
 }
 
-sv_status sv_fmm_tune(sv_ctx *c, double *best_ms) {
-    if (!c) return SV_ERR_INVALID;
-    if (!c->have_state) return set_error(c, SV_ERR_STATE, "no state uploaded");
-    if (c->batch) return set_error(c, SV_ERR_UNSUPPORTED, "batches tune with sv_batch_tune");
-    if (c->P.method != SV_METHOD_FMM) return set_error(c, SV_ERR_UNSUPPORTED, "sv_fmm_tune tunes the FMM");
-    SV_CK(c, cudaSetDevice(c->device));
+// Root-scale sweep of the context's current order and separation: the
+// fastest scale is left in the parameters, its time in *best.
+static sv_status tune_root_scale(sv_ctx *c, double *best) {
     float best_scale = 1.0f;
-    double best = 1e300;
+    *best = 1e300;
     for (int k = 0; k < 8; k++) {
         c->P.fmm_root_scale = 1.0f + 0.125f * (float)k;
         double t = 1e300;
@@ -949,13 +996,93 @@ sv_status sv_fmm_tune(sv_ctx *c, double *best_ms) {
             SV_CK(c, cudaEventElapsedTime(&ms, c->ev_begin, c->ev_end));
             if (r > 0) t = std::min(t, (double)ms);
         }
-        if (t < best) {
-            best = t;
+        if (t < *best) {
+            *best = t;
             best_scale = c->P.fmm_root_scale;
         }
     }
     c->P.fmm_root_scale = best_scale;
-    SV_TRY(compute_accel_device(c, 0, c->n));  // the last acceleration and statistics at the kept scale
+    return SV_OK;
+}
+
+// Per-particle relative-L2 error of the last acceleration on up to 256 evenly
+// spaced targets against the FP64 direct sum (compareAcceleration's metric).
+static sv_status sampled_error(sv_ctx *c, double *err) {
+    const int64_t n = c->n;
+    const int k = (int)std::min<int64_t>(n, 256);
+    *err = 0.0;
+    if (k == 0) return SV_OK;
+    std::vector<int64_t> tg(k);
+    for (int i = 0; i < k; i++) tg[i] = (int64_t)((double)i * (double)n / (double)k);
+    void *stg = nullptr;
+    SV_TRY(stage_bytes(c, sizeof(int64_t) * k + sizeof(double) * 6 * k, &stg));
+    int64_t *d_tg = (int64_t *)stg;
+    double *d_out = (double *)(d_tg + k);
+    SV_CK(c, cudaMemcpyAsync(d_tg, tg.data(), sizeof(int64_t) * k, cudaMemcpyHostToDevice, c->stream));
+    sampled_direct_f64_kernel<<<k, kSmpThreads, 0, c->stream>>>(d_tg, c->x, c->y, c->z, c->q, c->qom, c->status, n,
+                                                               c->P.softening2, c->P.k_const, c->ax, c->ay, c->az,
+                                                               d_out);
+    SV_LAUNCHED(c);
+    std::vector<double> h(6 * (size_t)k);
+    SV_CK(c, cudaMemcpyAsync(h.data(), d_out, sizeof(double) * 6 * k, cudaMemcpyDeviceToHost, c->stream));
+    SV_CK(c, cudaStreamSynchronize(c->stream));
+    double s = 0.0;
+    int cnt = 0;
+    for (int i = 0; i < k; i++) {
+        const double *o = &h[6 * (size_t)i];
+        double d = 0.0, nr = 0.0;
+        for (int e = 0; e < 3; e++) {
+            d += (o[3 + e] - o[e]) * (o[3 + e] - o[e]);
+            nr += o[e] * o[e];
+        }
+        if (nr == 0.0 && d == 0.0) continue;  // not a target (or no source)
+        s += nr > 0.0 ? d / nr : 1.0;
+        cnt++;
+    }
+    *err = cnt ? std::sqrt(s / cnt) : 0.0;
+    return SV_OK;
+}
+
+sv_status sv_fmm_tune(sv_ctx *c, double *best_ms) {
+    if (!c) return SV_ERR_INVALID;
+    if (!c->have_state) return set_error(c, SV_ERR_STATE, "no state uploaded");
+    if (c->batch) return set_error(c, SV_ERR_UNSUPPORTED, "batches tune with sv_batch_tune");
+    if (c->P.method != SV_METHOD_FMM) return set_error(c, SV_ERR_UNSUPPORTED, "sv_fmm_tune tunes the FMM");
+    SV_CK(c, cudaSetDevice(c->device));
+    double best = 1e300;
+    if (c->P.fmm_tune_err > 0.0f) {
+        // (order, separation) candidates, cheapest expected first
+        const int cand[5][2] = {{6, 2}, {8, 1}, {8, 2}, {10, 1}, {10, 2}};
+        int kept = -1, most_acc = 0;
+        double kept_t = 1e300, min_err = 1e300, times[5] = {};
+        float scales[5] = {};
+        for (int k = 0; k < 5; k++) {
+            c->P.fmm_order = cand[k][0];
+            c->P.fmm_ws = cand[k][1];
+            double t = 0.0, e = 0.0;
+            SV_TRY(tune_root_scale(c, &t));
+            scales[k] = c->P.fmm_root_scale;
+            times[k] = t;
+            SV_TRY(compute_accel_device(c, 0, c->n));
+            SV_TRY(sampled_error(c, &e));
+            if (e < min_err) {
+                min_err = e;
+                most_acc = k;
+            }
+            if (e <= (double)c->P.fmm_tune_err && t < kept_t) {
+                kept_t = t;
+                kept = k;
+            }
+        }
+        const int k = kept >= 0 ? kept : most_acc;
+        c->P.fmm_order = cand[k][0];
+        c->P.fmm_ws = cand[k][1];
+        c->P.fmm_root_scale = scales[k];
+        best = times[k];
+    } else {
+        SV_TRY(tune_root_scale(c, &best));
+    }
+    SV_TRY(compute_accel_device(c, 0, c->n));  // the last acceleration and statistics at the kept settings
     if (best_ms) *best_ms = best;
     return SV_OK;
 }

@@ -243,3 +243,27 @@ def test_fmm_far_direct_lists():
         out[th] = (s.cell_interactions, s.pair_interactions)
     assert out[0][0] < out[-1][0] and out[0][1] > out[-1][1]
     assert out[20000][0] <= out[0][0]
+
+
+def test_fmm_tune_chooses_order_under_error_bound():
+    """With fmm_tune_err set, sv_fmm_tune picks the expansion order and
+    separation as well: the kept one meets the bound on the oracle, and a
+    looser bound never keeps a slower-to-evaluate, more accurate choice than
+    a tighter one needs."""
+    n = 65536
+    st = plume.make_plume(n, 10e-6, 37)
+    tg = np.arange(0, n, 64)
+    ref = O.direct_f64(st, EPS20, targets=tg)
+    kept = {}
+    for bound in (1e-5, 3e-4):
+        with sv.ForceMethod(softening2=EPS20, method=sv.FMM, fmm_order=4, fmm_ws=1, fmm_tune_err=bound) as fm:
+            fm.upload(st)
+            scale, ms = fm.fmm_tune()
+            p = fm.params
+            a = fm.accel()
+        assert 1.0 <= scale < 2.0 and ms > 0
+        assert (p.fmm_order, p.fmm_ws) in ((6, 2), (8, 1), (8, 2), (10, 1), (10, 2))
+        assert rel_l2(a[tg], ref, st["status"][tg]) < bound * 1.5, (bound, p.fmm_order, p.fmm_ws)
+        kept[bound] = (p.fmm_order, p.fmm_ws, ms)
+    # the looser bound's choice is at least as fast as the tighter bound's (within timing noise)
+    assert kept[3e-4][2] <= kept[1e-5][2] * 1.15, kept
