@@ -378,14 +378,21 @@ struct RowShape {
     static constexpr int RSTRIDE = (RB + 15) / 16 * 16;
     static constexpr int SROW = (RSTRIDE / 16) % 2 ? RSTRIDE : RSTRIDE + 16;
     static constexpr int STAGE = kTile * SROW;
-    // staging buffers that fit beside the operand images: two (the next
-    // tile's rows stream in during this one), one, or none (p = 10: the rows
-    // are read from global memory directly and stored without staging)
+    // Shared-memory budget of the tile kernel: 100 KB, so that a tile CTA
+    // finds room on an SM beside the near field's blocks (which run at the
+    // same time, on the other stream).  With the whole 227 KB (two staging
+    // buffers of TMA-copied rows, two operator buffers) the kernel alone is
+    // faster (61 against 82 us per launch at fmm_n1m), but it waits for SMs
+    // that the near field holds: 2.366 against 2.339 ms per step.
+    // Staging buffers that fit beside the operand images: two (the next
+    // tile's rows stream in during this one), one, or none (the rows are
+    // read from global memory directly and stored without staging).
     static constexpr int OPS = 2 * TcShape<P>::ABYTES + 2 * TcShape<P>::BBYTES + 2048;
-    static constexpr int NSTAGE = OPS + 2 * STAGE <= 227 * 1024 ? 2 : (OPS + STAGE <= 227 * 1024 ? 1 : 0);
+    static constexpr int BUDGET = 100 * 1024;
+    static constexpr int NSTAGE = OPS + 2 * STAGE <= BUDGET ? 2 : (OPS + STAGE <= BUDGET ? 1 : 0);
     // two operator buffers (the next class's operator streams in during this
     // tile) when they fit beside the rest
-    static constexpr int NB = OPS + 2 * TcShape<P>::BBYTES + NSTAGE * STAGE <= 227 * 1024 ? 2 : 1;
+    static constexpr int NB = OPS + 2 * TcShape<P>::BBYTES + NSTAGE * STAGE <= BUDGET ? 2 : 1;
     static constexpr int SMEM = 2 * TcShape<P>::ABYTES + NB * 2 * TcShape<P>::BBYTES + NSTAGE * STAGE + 1024;
     static_assert(SMEM <= 227 * 1024, "the operand images must fit in shared memory");
 };
@@ -731,8 +738,8 @@ sv_status launch_tc(sv_ctx *c, M2LTc &T, const TcArgs &a, int reduce_warps, cuda
                                       RowShape<P>::SMEM));
         attr_set[dev] = true;
     }
-    // one CTA per SM; its next tile's rows stream in (bulk copies) while the
-    // current tile converts, multiplies and stores
+    // one CTA per SM (with staging, its next tile's rows stream in by bulk
+    // copies while the current tile converts, multiplies and stores)
     m2l_tc_tiles_kernel<P><<<device_sms(), kTcThreads, RowShape<P>::SMEM, s>>>(ta);
     SV_LAUNCHED(c);
     m2l_tc_reduce_kernel<P><<<div_up(reduce_warps, 4), 128, 0, s>>>(a, T.ctl, (const unsigned char *)T.rows);
