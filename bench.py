@@ -279,7 +279,7 @@ def run_batch(args, wl, rank, world, local):
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "ms_per_step": ms_per_step, "timed_only": True,
                               "m2l_weight": info.m2l_weight, "leaf_level": info.leaf_level,
-                              "regrows": info.regrows}), flush=True)
+                              "regrows": info.regrows, "m2l_tc": info.m2l_tc}), flush=True)
         fm.close()
         return
 
@@ -340,7 +340,7 @@ def run_batch(args, wl, rank, world, local):
                        "plumes": len(states), "fmm_plumes": info.fmm_plumes, "slots_with_images": info.slots,
                        "leaf_level": info.leaf_level, "tuned_m2l_weight": info.m2l_weight,
                        "tuned_direct_chunk": info.direct_chunk, "kernels_per_step_graph": info.graph_kernels_step,
-                       "capacity_regrows": info.regrows,
+                       "capacity_regrows": info.regrows, "m2l_on_tensor_cores": bool(info.m2l_tc),
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                        "l2": "no flush: the batch state (particles x 48 B plus sorted copies) is far larger than "
                              "L2"},

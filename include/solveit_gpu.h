@@ -441,10 +441,13 @@ SV_API sv_status sv_upload_batch(sv_ctx *ctx, int32_t nplumes, const int64_t *co
  * FMM plumes' depth model (the cost of one M2L translation in pair
  * interactions; each plume's depth is chosen on the device at every
  * evaluation to minimise P2P pairs + weight * M2L translations) and the direct
- * plumes' work-item size on the uploaded state and keeps the fastest.  Results are cached per batch shape (plume count, size
- * buckets, methods, symmetries, order) in the process and, when cache_path is
- * not null, in that text file (read first, appended to).  best_ms (nullable)
- * receives the tuned force-evaluation time. */
+ * plumes' work-item size on the uploaded state and keeps the fastest; among
+ * weights within 3 % of the fastest it keeps the largest (shallower trees, whose
+ * M2L work grows less as the plumes expand).  Results are cached per batch
+ * shape (plume count, size buckets, methods, symmetries, order, separation,
+ * M2L path) in the process and, when cache_path is not null, in that text
+ * file (read first, appended to).  best_ms (nullable) receives the tuned
+ * force-evaluation time. */
 SV_API sv_status sv_batch_tune(sv_ctx *ctx, const char *cache_path, double *best_ms);
 /* Autotuner of a single-plume FMM context, after the reference's timing-driven
  * choice of the FMM's level (MultipoleMethodForceCalculation::setOptimumLevel,
@@ -484,7 +487,9 @@ typedef struct {
     int32_t level_cap[22];          /* box capacity per level */
     int32_t level_max[22];          /* largest box count per level since the last plan */
     int32_t max_leaf;               /* most slots in one leaf box at the last evaluation */
-    int32_t reserved[5];
+    int32_t m2l_tc;                 /* 1: the last forest evaluation's M2L ran on the tensor cores, 0: on the
+                                       FP32 rotation kernel (selected, or its room was outgrown) */
+    int32_t reserved[4];
 } sv_batch_info;
 SV_API sv_status sv_batch_get_info(const sv_ctx *ctx, sv_batch_info *out);
 

@@ -25,7 +25,8 @@
 //  * every step (drift, force, kick, drift) is captured once in a CUDA graph
 //    and replayed; the step time lives on the device.  Box capacities are
 //    fixed per graph; an overflow sets a device flag, and the host restores
-//    the state, doubles the capacities and runs the steps again.
+//    the state saved before that step, doubles the capacities and runs the
+//    step again.
 #include <cub/device/device_radix_sort.cuh>
 
 #include <algorithm>
@@ -850,7 +851,10 @@ sv_status batch_accel(sv_ctx *c) {
         if (!err) {
             c->stats.pair_interactions = B.direct_pairs;
             // the result stands (the rotation M2L ran); the next run gets more room
-            if (fmm_forest_tc_overflowed(c)) SV_TRY(plan_forest(c, B, 1));
+            if (fmm_forest_tc_overflowed(c)) {
+                SV_TRY(fmm_forest_tc_grow(c));
+                drop_graphs(B);
+            }
             return SV_OK;
         }
         SV_TRY(grow(c, B, 2 << attempt));
@@ -870,46 +874,59 @@ sv_status batch_leapfrog(sv_ctx *c, int32_t nsteps, double dt, double t0) {
     if (c->B.crash != SV_CRASH_NONE || c->B.bc != SV_BC_NONE) SV_TRY(events_reserve(c));
     SV_TRY(field_prepare(c));  // before capture: the graph keeps the walk caches' address
     double *st[6] = {c->x, c->y, c->z, c->vx, c->vy, c->vz};
-    for (int k = 0; k < 6; k++)
-        SV_CK(c, cudaMemcpyAsync(B.backup + k * n, st[k], sizeof(double) * n, cudaMemcpyDeviceToDevice, c->stream));
-    SV_CK(c, cudaMemcpyAsync(B.backup_st, c->status, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, c->stream));
-    if (c->d_ev_count)
-        SV_CK(c, cudaMemcpyAsync(B.ev_count0, c->d_ev_count, sizeof(unsigned long long), cudaMemcpyDeviceToDevice,
-                                 c->stream));
-    for (int attempt = 0; attempt < 4; attempt++) {
-        // dt is baked into the step graph
-        if (B.g_step && B.step_dt != dt) {
-            cudaGraphExecDestroy(B.g_step);
-            B.g_step = nullptr;
-        }
-        B.step_dt = dt;
-        SV_TRY(ensure_step_graph(c, B));
-        B.h_time[0] = t0;
-        B.h_time[1] = dt;
-        B.h_time[2] = 0.0;
-        B.h_time[3] = (double)c->ev_seq;
-        SV_CK(c, cudaMemcpyAsync(B.d_time, B.h_time, sizeof(double) * 4, cudaMemcpyHostToDevice, c->stream));
-        for (int s = 0; s < nsteps; s++) {
+    const bool watch_tc = B.nf > 0 && B.nfp > 0 && c->P.fmm_m2l_tc >= 0;
+    // Step by step: each step's state is saved first (a device copy, ~0.1 ms
+    // for 8M ions), and the step's capacity flags are read after it (one
+    // host wait, small beside a batch step's device time).  A step that
+    // overflowed a forest level is undone and run again with larger
+    // capacities; only that step is repeated.  A step whose M2L translations
+    // outgrew the tensor-core room ran the rotation kernel (its result
+    // stands), and the room grows before the next step, so a run of steps
+    // whose plumes expand keeps the tensor cores.
+    for (int s = 0; s < nsteps; s++) {
+        for (int attempt = 0;; attempt++) {
+            if (attempt == 4) return set_error(c, SV_ERR_CAPACITY, "forest box capacity still exceeded after growing it");
+            for (int k = 0; k < 6; k++)
+                SV_CK(c, cudaMemcpyAsync(B.backup + k * n, st[k], sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                                         c->stream));
+            SV_CK(c, cudaMemcpyAsync(B.backup_st, c->status, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, c->stream));
+            if (c->d_ev_count)
+                SV_CK(c, cudaMemcpyAsync(B.ev_count0, c->d_ev_count, sizeof(unsigned long long),
+                                         cudaMemcpyDeviceToDevice, c->stream));
+            // dt is baked into the step graph
+            if (B.g_step && B.step_dt != dt) {
+                cudaGraphExecDestroy(B.g_step);
+                B.g_step = nullptr;
+            }
+            B.step_dt = dt;
+            SV_TRY(ensure_step_graph(c, B));
+            B.h_time[0] = t0;
+            B.h_time[1] = dt;
+            B.h_time[2] = (double)s;
+            B.h_time[3] = (double)c->ev_seq;
+            SV_CK(c, cudaMemcpyAsync(B.d_time, B.h_time, sizeof(double) * 4, cudaMemcpyHostToDevice, c->stream));
             SV_CK(c, cudaGraphLaunch(B.g_step, c->stream));
             c->launches += B.step_kernels;
-        }
-        int err = 0;
-        SV_TRY(read_err(c, B, &err));
-        if (!err) {
-            c->ev_seq += 2LL * nsteps;
-            if (fmm_forest_tc_overflowed(c)) SV_TRY(plan_forest(c, B, 1));
-            return SV_OK;
-        }
-        for (int k = 0; k < 6; k++)
-            SV_CK(c, cudaMemcpyAsync(st[k], B.backup + k * n, sizeof(double) * n, cudaMemcpyDeviceToDevice,
+            int err = 0;
+            SV_TRY(read_err(c, B, &err));
+            if (!err) break;
+            for (int k = 0; k < 6; k++)
+                SV_CK(c, cudaMemcpyAsync(st[k], B.backup + k * n, sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                                         c->stream));
+            SV_CK(c, cudaMemcpyAsync(c->status, B.backup_st, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice,
                                      c->stream));
-        SV_CK(c, cudaMemcpyAsync(c->status, B.backup_st, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, c->stream));
-        if (c->d_ev_count)
-            SV_CK(c, cudaMemcpyAsync(c->d_ev_count, B.ev_count0, sizeof(unsigned long long),
-                                     cudaMemcpyDeviceToDevice, c->stream));
-        SV_TRY(grow(c, B, 2 << attempt));
+            if (c->d_ev_count)
+                SV_CK(c, cudaMemcpyAsync(c->d_ev_count, B.ev_count0, sizeof(unsigned long long),
+                                         cudaMemcpyDeviceToDevice, c->stream));
+            SV_TRY(grow(c, B, 2 << attempt));
+        }
+        if (watch_tc && fmm_forest_tc_overflowed(c)) {
+            SV_TRY(fmm_forest_tc_grow(c));
+            drop_graphs(B);
+        }
     }
-    return set_error(c, SV_ERR_CAPACITY, "forest box capacity still exceeded after growing it");
+    c->ev_seq += 2LL * nsteps;
+    return SV_OK;
 }
 
 // ------------------------------------------------------------- autotuner --
@@ -928,7 +945,7 @@ std::string shape_key(const sv_ctx *c, const Batch &B) {
         hist["m" + std::to_string(B.method[p]) + "s" + std::to_string(B.sym[p]) + "b" + std::to_string(bucket)]++;
     }
     std::string k = "np" + std::to_string(B.np) + "_p" + std::to_string(c->P.fmm_order) + "_ws" +
-                    std::to_string(c->P.fmm_ws);
+                    std::to_string(c->P.fmm_ws) + (c->P.fmm_m2l_tc >= 0 ? "_tc" : "_rot");
     for (auto &kv : hist) k += "_" + kv.first + "x" + std::to_string(kv.second);
     return k;
 }
@@ -996,20 +1013,24 @@ sv_status batch_tune(sv_ctx *c, const char *cache_path, double *best_ms) {
         if (best_ms) *best_ms = ms;
         return SV_OK;
     }
-    // leaf occupancy first (FMM plumes), then the direct work-item size
+    // leaf occupancy first (FMM plumes), then the direct work-item size.
+    // Among the weights within 3 % of the fastest, the largest is kept: it
+    // chooses shallower trees, and as the plumes expand their M2L
+    // translations grow faster than their pairs (batch256 over 10 steps from
+    // a tie at the start: weight 400 95 ms per step, weight 200 107 ms).
     int best_lt = B.m2l_weight, best_dc = B.direct_chunk;
     double best = 1e30;
     if (B.nfp > 0) {
-        for (int lt : {100, 200, 400, 800, 1600, 3200}) {
-            B.m2l_weight = lt;
+        const int weights[6] = {100, 200, 400, 800, 1600, 3200};
+        double t[6];
+        for (int k = 0; k < 6; k++) {
+            B.m2l_weight = weights[k];
             SV_TRY(plan_forest(c, B, 1));
-            double ms = 0;
-            SV_TRY(time_accel(c, B, 5, &ms));
-            if (ms < best) {
-                best = ms;
-                best_lt = lt;
-            }
+            SV_TRY(time_accel(c, B, 5, &t[k]));
+            best = std::min(best, t[k]);
         }
+        for (int k = 0; k < 6; k++)
+            if (t[k] <= 1.03 * best) best_lt = weights[k];
     }
     B.m2l_weight = best_lt;
     SV_TRY(plan_forest(c, B, 1));
@@ -1079,6 +1100,7 @@ sv_status batch_info(const sv_ctx *c, sv_batch_info *out) {
         out->max_leaf = ml;
     }
     out->overflow_mask = B.overflow_mask;
+    out->m2l_tc = fmm_forest_tc_used(c) ? 1 : 0;
     if (B.planned && B.nfp > 0) {
         int h[3 * kBLevels];
         SV_CK(const_cast<sv_ctx *>(c), cudaMemcpy(h, B.d_nbox, sizeof(h), cudaMemcpyDeviceToHost));

@@ -2081,6 +2081,27 @@ sv_status fmm_forest_reserve(sv_ctx *c, const ForestArgs &fa) {
     return SV_OK;
 }
 
+sv_status fmm_forest_tc_grow(sv_ctx *c) {
+    Fmm &F = *c->fmm;
+    const int64_t need = F.tc.h_ctl ? F.tc.h_ctl[0] : 0;  // the true count of the run that overflowed
+    // expanding plumes add ~25 % translations per step: four times the count
+    // lasts ~6 steps; the room stays within 40 % of the device's memory
+    // (beyond it the rotation kernel takes the translations that do not fit)
+    size_t free_b = 0, total_b = 0;
+    SV_CK(c, cudaMemGetInfo(&free_b, &total_b));
+    const int p = F.tc.p;
+    const double per_entry = 16.0 + (double)(((size_t)p * (p + 1) * 4 + 15) / 16 * 16);
+    const int64_t limit = (int64_t)(0.4 * (double)total_b / per_entry);
+    const int64_t want = std::min<int64_t>(4 * need, limit);
+    if (want <= F.tc.cap) return SV_OK;
+    return m2l_tc_prepare(c, F.tc, p, F.tc.ws, want);
+}
+
+bool fmm_forest_tc_used(const sv_ctx *c) {
+    const Fmm *F = c->fmm;
+    return F && F->tc.launched && F->tc.h_ctl && !F->tc.h_ctl[2];
+}
+
 bool fmm_forest_tc_overflowed(const sv_ctx *c) {
     const Fmm *F = c->fmm;
     return F && F->tc.launched && F->tc.h_ctl && F->tc.h_ctl[2];

@@ -29,8 +29,13 @@ sv_status fmm_forest_run(sv_ctx *c, const ForestArgs &a);
 // Largest leaf-box occupancy of the last run (blocking; diagnostics).
 sv_status fmm_forest_max_leaf(sv_ctx *c, const ForestArgs &a, int *out);
 // The last run's tensor-core M2L found more translations than its room and
-// ran the rotation kernel instead (read after the run has completed): the
-// caller re-plans, which grows the room, and captures its graphs again.
+// ran the rotation kernel instead (read after the run has completed).
 bool fmm_forest_tc_overflowed(const sv_ctx *c);
+// Grows that room to four times the last run's translations, within 40 % of
+// the device's memory (host call, outside any capture; the buffers move, so
+// the caller captures its graphs again).
+sv_status fmm_forest_tc_grow(sv_ctx *c);
+// The last run's M2L ran on the tensor cores (read after the run has completed).
+bool fmm_forest_tc_used(const sv_ctx *c);
 
 }  // namespace sv

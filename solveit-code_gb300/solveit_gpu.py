@@ -73,7 +73,7 @@ class BatchInfo(C.Structure):
         ("tuned_ms", C.c_double), ("direct_pairs", C.c_double), ("fmm_m2l", C.c_double),
         ("fmm_pairs", C.c_double), ("regrows", C.c_int32), ("overflow_mask", C.c_int32),
         ("level_boxes", C.c_int32 * 22), ("level_cap", C.c_int32 * 22), ("level_max", C.c_int32 * 22),
-        ("max_leaf", C.c_int32), ("reserved", C.c_int32 * 5),
+        ("max_leaf", C.c_int32), ("m2l_tc", C.c_int32), ("reserved", C.c_int32 * 4),
     ]
 
 
