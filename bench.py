@@ -65,9 +65,10 @@ WORKLOADS = {
                            desc="adjoint of 50 leapfrog DKD steps (direct sum, mixed precision), N=16384 ions, "
                                 "plume r=20nm z=1um, eps=1e-10m, dt=1e-13s, E_z=1e8V/m, checkpoint every 10 steps; "
                                 "loss = mean z-momentum + 1e3 x mean transverse radius"),
-    "batch256": dict(n=None, nplumes=256, length=1e-6, method="batch", order=6, ws=2, seed=3,
+    "batch256": dict(n=None, nplumes=256, length=1e-6, method="batch", order=6, ws=2, near=2, seed=3,
                      desc="256 independent plumes, N_i uniform in [1024, 65536] (seed 3999), r=20nm z=1um, "
-                          "direct sum for N_i < 8192 and FMM p=6 ws=2 above, 4-fold rotational variant on the "
+                          "direct sum for N_i < 8192 and FMM p=6 ws=2 (trimmed near field) above, "
+                          "4-fold rotational variant on the "
                           "even plumes, eps=1e-10m, leapfrog DKD dt=1e-13s, E_z=1e8V/m, each step one CUDA "
                           "graph"),
 }
@@ -247,7 +248,7 @@ def run_batch(args, wl, rank, world, local):
     counts = np.array([s["x"].shape[0] for s in states])
     n = int(counts.sum())
     fm = sv.ForceMethod(softening2=EPS2, efield=(0.0, 0.0, EZ), device=local, fmm_order=wl["order"],
-                        fmm_ws=wl["ws"], fmm_m2l_tc=args.m2l_tc)
+                        fmm_ws=wl["ws"], fmm_m2l_tc=args.m2l_tc, fmm_near=args.fmm_near or wl.get("near", 0))
     fm.upload_batch(states, methods, syms)
     tuned_ms = None if args.no_tune else fm.tune(None)
     stream = torch.cuda.ExternalStream(fm.stream, device=local)
@@ -341,6 +342,7 @@ def run_batch(args, wl, rank, world, local):
                        "leaf_level": info.leaf_level, "tuned_m2l_weight": info.m2l_weight,
                        "tuned_direct_chunk": info.direct_chunk, "kernels_per_step_graph": info.graph_kernels_step,
                        "capacity_regrows": info.regrows, "m2l_on_tensor_cores": bool(info.m2l_tc),
+                       "fmm_near_field": "trimmed" if fm.params.fmm_near == 2 else "full 5^3 cube",
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                        "l2": "no flush: the batch state (particles x 48 B plus sorted copies) is far larger than "
                              "L2"},
@@ -527,7 +529,7 @@ def run_ours(args, wl, rank, world, local):
     st = plume.make_plume(n, wl["length"], plume_seed(wl, rank))
     if wl["method"] == "fmm":
         kw = dict(method=sv.FMM, precision=sv.MIXED, fmm_order=wl["order"], fmm_ws=wl["ws"],
-                  fmm_leaf_target=wl["leaf"], fmm_m2l_tc=args.m2l_tc)
+                  fmm_leaf_target=wl["leaf"], fmm_m2l_tc=args.m2l_tc, fmm_near=args.fmm_near or wl.get("near", 0))
     elif wl["method"] == "bh":
         kw = dict(method=sv.BARNES_HUT, precision=sv.MIXED, theta=wl["theta"], leaf_size=wl["leaf"])
     else:
@@ -751,6 +753,8 @@ def main():
                     help="FMM: this root-cube scale instead of sv_fmm_tune's (profiling a fixed configuration)")
     ap.add_argument("--timed-only", action="store_true",
                     help="only the device-resident timed steps (for profiler launch lists)")
+    ap.add_argument("--fmm-near", type=int, default=0, choices=[0, 1, 2],
+                    help="FMM near field at ws 2: 1 full cube, 2 trimmed, 0 the workload's choice")
     ap.add_argument("--m2l-tc", type=int, default=0, choices=[-1, 0, 1],
                     help="FMM M2L: 1 tensor cores, -1 FP32 rotation kernel, 0 the library default")
     ap.add_argument("--no-tune", action="store_true",

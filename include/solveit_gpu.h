@@ -113,7 +113,10 @@ typedef struct {
     float fmm_tune_err;        /* sv_fmm_tune's force-error bound: > 0 makes it choose the expansion order
                                 and separation as well (the fastest that meets the bound on sampled
                                 targets); 0 = it tunes the root scale only */
-    int32_t reserved[1];
+    int32_t fmm_near;          /* FMM near field at fmm_ws = 2: 1 = the full cube of 5^3 boxes, 2 = trimmed
+                                (the 32 boxes at (2,2,1)- and (2,2,2)-type offsets go to the M2L, whose
+                                worst separation ratio they do not raise), 0 = the default (the full
+                                cube); ignored at fmm_ws = 1 */
 } sv_params;
 
 /* Per-call statistics of the last force evaluation. */
@@ -457,9 +460,10 @@ SV_API sv_status sv_batch_tune(sv_ctx *ctx, const char *cache_path, double *best
  * 1.875 and keeps the fastest in the context's parameters (sv_get_params
  * shows it).  The root scale sets the leaf box side between two octree
  * levels' sides, so it is also the leaf-size choice.  With fmm_tune_err > 0
- * it also chooses the expansion order and separation, as the reference's
- * test cases sweep the order (test_cases.cpp:217-295): for each of (p, ws) =
- * (6, 2), (8, 1), (8, 2), (10, 1), (10, 2) it tunes the root scale, measures
+ * it also chooses the expansion order, separation and near-field shape, as
+ * the reference's test cases sweep the order (test_cases.cpp:217-295): for
+ * each of (p, ws) = (6, 2), (8, 1), (8, 2), (10, 1), (10, 2), with both
+ * fmm_near shapes at ws = 2 unless fmm_near is set, it tunes the root scale, measures
  * the per-particle relative-L2 force error on 256 evenly spaced targets
  * against an FP64 direct sum, and keeps the fastest candidate whose error is
  * at most fmm_tune_err (the most accurate one when none is).  best_ms

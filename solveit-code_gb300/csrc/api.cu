@@ -325,6 +325,7 @@ sv_status check_params(sv_ctx *c, const sv_params *p) {
     if (p->fmm_type < SV_FMM_FMM || p->fmm_type > SV_FMM_TREECODE_OUTLIERS)
         return set_error(c, SV_ERR_INVALID, "unknown fmm_type %d", p->fmm_type);
     if (p->fmm_m2l_tc < -1 || p->fmm_m2l_tc > 1) return set_error(c, SV_ERR_INVALID, "fmm_m2l_tc must be -1, 0 or 1");
+    if (p->fmm_near < 0 || p->fmm_near > 2) return set_error(c, SV_ERR_INVALID, "fmm_near must be 0, 1 or 2");
     if (!(p->fmm_tune_err >= 0.0f) || !std::isfinite(p->fmm_tune_err))
         return set_error(c, SV_ERR_INVALID, "fmm_tune_err must be finite and >= 0");
     if (!(p->fmm_root_scale == 0.0f || (p->fmm_root_scale >= 1.0f && p->fmm_root_scale < 2.0f)))
@@ -1051,14 +1052,31 @@ sv_status sv_fmm_tune(sv_ctx *c, double *best_ms) {
     SV_CK(c, cudaSetDevice(c->device));
     double best = 1e300;
     if (c->P.fmm_tune_err > 0.0f) {
-        // (order, separation) candidates, cheapest expected first
-        const int cand[5][2] = {{6, 2}, {8, 1}, {8, 2}, {10, 1}, {10, 2}};
+        // (order, separation, near field) candidates; both near-field shapes at
+        // separation 2 unless the caller fixed one
+        struct Cand {
+            int p, ws, near;
+        };
+        std::vector<Cand> cand;
+        const int fixed_near = c->P.fmm_near;
+        for (const int p : {6, 8, 10})
+            for (const int ws : {1, 2}) {
+                if (p == 6 && ws == 1) continue;  // the least accurate pair: not tried
+                if (ws == 1 || fixed_near != 0) cand.push_back({p, ws, ws == 1 ? 1 : fixed_near});
+                else {
+                    cand.push_back({p, ws, 2});
+                    cand.push_back({p, ws, 1});
+                }
+            }
+        const int nc = (int)cand.size();
         int kept = -1, most_acc = 0;
-        double kept_t = 1e300, min_err = 1e300, times[5] = {};
-        float scales[5] = {};
-        for (int k = 0; k < 5; k++) {
-            c->P.fmm_order = cand[k][0];
-            c->P.fmm_ws = cand[k][1];
+        double kept_t = 1e300, min_err = 1e300;
+        std::vector<double> times(nc);
+        std::vector<float> scales(nc);
+        for (int k = 0; k < nc; k++) {
+            c->P.fmm_order = cand[k].p;
+            c->P.fmm_ws = cand[k].ws;
+            c->P.fmm_near = cand[k].near;
             double t = 0.0, e = 0.0;
             SV_TRY(tune_root_scale(c, &t));
             scales[k] = c->P.fmm_root_scale;
@@ -1075,8 +1093,9 @@ sv_status sv_fmm_tune(sv_ctx *c, double *best_ms) {
             }
         }
         const int k = kept >= 0 ? kept : most_acc;
-        c->P.fmm_order = cand[k][0];
-        c->P.fmm_ws = cand[k][1];
+        c->P.fmm_order = cand[k].p;
+        c->P.fmm_ws = cand[k].ws;
+        c->P.fmm_near = cand[k].ws == 2 ? cand[k].near : fixed_near;
         c->P.fmm_root_scale = scales[k];
         best = times[k];
     } else {

@@ -45,6 +45,7 @@ namespace sv {
 
 struct Fmm {
     int p = 0, ws = 0;
+    int trim = 0;  // trimmed near field (sv_params.fmm_near = 2 at ws = 2) for the next evaluation
     FmmTables H;
     int *cls_theta = nullptr;
     float2 *cls_phase = nullptr;
@@ -146,7 +147,11 @@ __device__ __forceinline__ const double *box_root(const double *root, const int 
 // pnbr: the children of each of the parent's near boxes are classified round
 // by round (lanes take the parent's near slots) into the near list (|offset|
 // <= WS, written when write_near) and the interaction list (M2L entries
-// compacted by ballot).  Returns the box's M2L count.
+// compacted by ballot).  trim: the trimmed near field of WS = 2, whose
+// (2,2,1)- and (2,2,2)-type offsets are interaction-list entries instead
+// (fmm_trimmable); the near boxes of a box always have parents at offsets in
+// [-1, 1]^3 from its parent, which trimming never removes, so every pair is
+// still counted once.  Returns the box's M2L count.
 //
 // Far-direct lists (fd non-null, the leaf level of a single tree): an
 // interaction-list entry whose two boxes hold fewer than fd_thresh particles
@@ -157,7 +162,7 @@ template <int WS>
 __device__ __forceinline__ int build_lists_box(int b, int4 cb, int par, const int4 *__restrict__ coord,
                                                const int *__restrict__ pnbr, const int *__restrict__ pchild0,
                                                int *__restrict__ nbr, int2 *__restrict__ m2l,
-                                               int *__restrict__ m2l_cnt, int cap, int write_near,
+                                               int *__restrict__ m2l_cnt, int cap, int write_near, int trim,
                                                const int *__restrict__ start = nullptr, int *__restrict__ fd = nullptr,
                                                int *__restrict__ fd_cnt = nullptr, int fd_cap = 0,
                                                int fd_thresh = 0) {
@@ -190,7 +195,7 @@ __device__ __forceinline__ int build_lists_box(int b, int4 cb, int par, const in
                 // a consistent tree keeps |offset| <= R; a forest level clamped to
                 // its capacity may not, and its result is discarded, but the class
                 // index must stay inside the tables
-                if (am <= WS) {
+                if (am <= WS && !(trim && fmm_trimmable(ox, oy, oz, WS))) {
                     if (write_near) nbr[b * NS + ((ox + WS) * NS1 + (oy + WS)) * NS1 + (oz + WS)] = ch;
                 } else if (am <= R) {
                     far = true;
@@ -231,14 +236,14 @@ template <int WS>
 __global__ void __launch_bounds__(kWarps * 32)
 build_lists_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ parent,
                    const int4 *__restrict__ coord, const int *__restrict__ pnbr, const int *__restrict__ pchild0,
-                   int *__restrict__ nbr, int2 *__restrict__ m2l, int *__restrict__ m2l_cnt, int cap,
+                   int *__restrict__ nbr, int2 *__restrict__ m2l, int *__restrict__ m2l_cnt, int cap, int trim,
                    unsigned long long *__restrict__ counts, const int *__restrict__ start = nullptr,
                    int *__restrict__ fd = nullptr, int *__restrict__ fd_cnt = nullptr, int fd_cap = 0,
                    int fd_thresh = 0) {
     unsigned long long tot = 0;
     SV_WARP_BOXES(kWarps) {
     const int cnt = build_lists_box<WS>(b, coord[b], parent[b], coord, pnbr, pchild0, nbr, m2l, m2l_cnt, cap, 1,
-                                        start, fd, fd_cnt, fd_cap, fd_thresh);
+                                        trim, start, fd, fd_cnt, fd_cap, fd_thresh);
     if (lane == 0) tot += cnt;
     }
     if ((threadIdx.x & 31) == 0 && tot) atomicAdd(&counts[0], tot);
@@ -262,6 +267,7 @@ struct ListLevel {
 struct ListArgs {
     int nlev, total;         // levels 0 .. nlev - 1; boxes of all of them
     int fd_cap, fd_thresh;   // far-direct list capacity per box and pair threshold
+    int trim;                // trimmed near field (build_lists_box)
     ListLevel lv[kMortonBits + 1];
 };
 
@@ -303,7 +309,7 @@ __global__ void near_lists_kernel(ListArgs a) {
     const int4 cb = L.coord[b];
     const int x = cb.x - ox, y = cb.y - oy, z = cb.z - oz, side = 1 << l;
     int found = -1;
-    if (x >= 0 && y >= 0 && z >= 0 && x < side && y < side && z < side) {
+    if (x >= 0 && y >= 0 && z >= 0 && x < side && y < side && z < side && !(a.trim && fmm_trimmable(ox, oy, oz, WS))) {
         const uint64_t key = box_code(x, y, z);
         int lo = 0, hi = L.nbox - 1;
         while (lo <= hi) {
@@ -332,7 +338,8 @@ __global__ void __launch_bounds__(kWarps * 32) m2l_lists_kernel(ListArgs a, int 
         const ListLevel &L = a.lv[list_level(a, g)];
         const int b = g - L.first;
         const int cnt = build_lists_box<WS>(b, L.coord[b], L.parent[b], L.coord, L.pnbr, L.pchild0, L.nbr, L.m2l,
-                                            L.m2l_cnt, cap, 0, L.start, L.fd, L.fd_cnt, a.fd_cap, a.fd_thresh);
+                                            L.m2l_cnt, cap, 0, a.trim, L.start, L.fd, L.fd_cnt, a.fd_cap,
+                                            a.fd_thresh);
         if (lane == 0) tot += cnt;
     }
     if (lane == 0 && tot) atomicAdd(&counts[0], tot);
@@ -1088,6 +1095,15 @@ box_relative_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict
     if (__any_sync(0xffffffffu, diff) && (threadIdx.x & 31) == 0) *mixed = 1ull;
 }
 
+// 16-byte asynchronous copy global -> shared (LDGSTS): the data lands without
+// passing through registers; the issuing thread sees it after cp_async_wait_all.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
 // s += v with Kahan compensation e (the running sum is s - e)
 __device__ __forceinline__ void kahan_add(float &s, float &e, float v) {
     const float y = v - e, t = s + y;
@@ -1128,7 +1144,8 @@ p2p_body(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, co
          const double *__restrict__ roots, int level, float eps2, double *__restrict__ ax, double *__restrict__ ay,
          double *__restrict__ az, unsigned long long *__restrict__ counts, const int *__restrict__ has_tgt,
          const float4 *__restrict__ rel, const int *__restrict__ fd, const int *__restrict__ fd_cnt, int fd_cap,
-         float (*st)[4][32], int2 (*nb_rng)[p2p_nsp<WS>()], float4 (*nb_off)[p2p_nsp<WS>()]) {
+         float (*st)[4][32], float4 (*raw)[2][32], int2 (*nb_rng)[p2p_nsp<WS>()],
+         float4 (*nb_off)[p2p_nsp<WS>()]) {
     constexpr int NS1 = 2 * WS + 1, NS = NS1 * NS1 * NS1;
     const float4 pad = UQ ? make_float4(1e18f, 0.f, 0.f, 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
     const float2 E2 = make_float2(eps2, eps2);
@@ -1175,6 +1192,40 @@ p2p_body(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, co
     if (fd) add_boxes(fd + (size_t)b * fd_cap, fd_cnt[b]);
     __syncwarp();
     const int t0 = start[b], t1 = start[b + 1];
+    // Sources are staged one 32-source chunk ahead: the lane's source of the
+    // next chunk is copied into raw[buf] (cp.async) while the current chunk's
+    // pairs run.  kb / kbeg: the lane's current source box and its first
+    // running index (lanes walk forward through the compacted boxes); kn: the
+    // box slot of the copied source, -1 past the end.
+    int kb = 0, kbeg = 0, kn = -1;
+    auto prefetch = [&](int c0, int buf) {
+        const int j = c0 + lane;
+        kn = -1;
+        if (j < total) {
+            int2 rg = nb_rng[wid][kb];
+            while (rg.y <= j) {
+                kbeg = rg.y;
+                rg = nb_rng[wid][++kb];
+            }
+            cp_async16(&raw[wid][buf][lane], rel + rg.x + (j - kbeg));
+            kn = kb;
+        }
+        cp_async_commit();
+    };
+    // the copied chunk, moved to its target-box offset, into the staging rows
+    auto stage = [&](int buf) {
+        cp_async_wait_all();
+        float4 v = pad;
+        if (kn >= 0) {
+            const float4 r = raw[wid][buf][lane];
+            const float4 o = nb_off[wid][kn];
+            v = make_float4(r.x + o.x, r.y + o.y, r.z + o.z, r.w);
+        }
+        st[wid][0][lane] = -v.x;
+        st[wid][1][lane] = -v.y;
+        st[wid][2][lane] = -v.z;
+        if (!UQ) st[wid][3][lane] = v.w;
+    };
     int tb = t0;
     // two targets per lane while more than 48 remain: each staged source
     // (one shared-memory load) then feeds two pairs.  33-48 targets cost less
@@ -1189,24 +1240,11 @@ p2p_body(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, co
         const float2 BX = make_float2(tbv.x, tbv.x), BY = make_float2(tbv.y, tbv.y), BZ = make_float2(tbv.z, tbv.z);
         float sax = 0.f, say = 0.f, saz = 0.f, eax = 0.f, eay = 0.f, eaz = 0.f;
         float sbx = 0.f, sby = 0.f, sbz = 0.f, ebx = 0.f, eby = 0.f, ebz = 0.f;
-        int kb = 0, kbeg = 0;
-        for (int c0 = 0; c0 < total; c0 += 32) {
-            const int j = c0 + lane;
-            float4 v = pad;
-            if (j < total) {
-                int2 rg = nb_rng[wid][kb];
-                while (rg.y <= j) {
-                    kbeg = rg.y;
-                    rg = nb_rng[wid][++kb];
-                }
-                const float4 r = rel[rg.x + (j - kbeg)];
-                const float4 o = nb_off[wid][kb];
-                v = make_float4(r.x + o.x, r.y + o.y, r.z + o.z, r.w);
-            }
-            st[wid][0][lane] = -v.x;
-            st[wid][1][lane] = -v.y;
-            st[wid][2][lane] = -v.z;
-            if (!UQ) st[wid][3][lane] = v.w;
+        kb = kbeg = 0;
+        prefetch(0, 0);
+        for (int c0 = 0, buf = 0; c0 < total; c0 += 32, buf ^= 1) {
+            stage(buf);
+            if (c0 + 32 < total) prefetch(c0 + 32, buf ^ 1);
             __syncwarp();
             float2 gax = make_float2(0.f, 0.f), gay = gax, gaz = gax, gbx = gax, gby = gax, gbz = gax;
 #pragma unroll 4
@@ -1251,24 +1289,11 @@ p2p_body(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, co
         const float2 TX = make_float2(ti.x, ti.x), TY = make_float2(ti.y, ti.y), TZ = make_float2(ti.z, ti.z);
         if (lane == 0) pairs += (unsigned long long)total * (unsigned long long)nt;
         float sx = 0.f, sy = 0.f, sz = 0.f, ex = 0.f, ey = 0.f, ez = 0.f;
-        int kb = 0, kbeg = 0;  // this lane's current source box and its first running index
-        for (int c0 = 0; c0 < total; c0 += 32) {
-            const int j = c0 + lane;
-            float4 v = pad;
-            if (j < total) {
-                int2 rg = nb_rng[wid][kb];
-                while (rg.y <= j) {
-                    kbeg = rg.y;
-                    rg = nb_rng[wid][++kb];
-                }
-                const float4 r = rel[rg.x + (j - kbeg)];
-                const float4 o = nb_off[wid][kb];
-                v = make_float4(r.x + o.x, r.y + o.y, r.z + o.z, r.w);
-            }
-            st[wid][0][lane] = -v.x;
-            st[wid][1][lane] = -v.y;
-            st[wid][2][lane] = -v.z;
-            if (!UQ) st[wid][3][lane] = v.w;
+        kb = kbeg = 0;
+        prefetch(0, 0);
+        for (int c0 = 0, buf = 0; c0 < total; c0 += 32, buf ^= 1) {
+            stage(buf);
+            if (c0 + 32 < total) prefetch(c0 + 32, buf ^ 1);
             __syncwarp();
             // g lanes per target, each taking pairs of consecutive sources 2 sub + 2 g i
             // (g = 1: every lane a target and all 32 staged sources; padding adds nothing)
@@ -1325,12 +1350,13 @@ p2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, 
     __shared__ __align__(16) float src[kWarps][4][32];  // staged sources: -x, -y, -z, charge
     __shared__ int2 nb_rng[kWarps][p2p_nsp<WS>()];    // (first source, running source count at the box's end)
     __shared__ float4 nb_off[kWarps][p2p_nsp<WS>()];  // source box centre - target box centre (exact in FP32)
+    __shared__ float4 raw[kWarps][2][32];             // next chunk's sources as copied (double buffer)
     if (counts[2] == 0)
         p2p_body<WS, CLAMP, true>(nbox, nbd, bpid, start, coord, nbr, qm, roots, level, eps2, ax, ay, az, counts,
-                                  has_tgt, rel, fd, fd_cnt, fd_cap, src, nb_rng, nb_off);
+                                  has_tgt, rel, fd, fd_cnt, fd_cap, src, raw, nb_rng, nb_off);
     else
         p2p_body<WS, CLAMP, false>(nbox, nbd, bpid, start, coord, nbr, qm, roots, level, eps2, ax, ay, az, counts,
-                                   has_tgt, rel, fd, fd_cnt, fd_cap, src, nb_rng, nb_off);
+                                   has_tgt, rel, fd, fd_cnt, fd_cap, src, raw, nb_rng, nb_off);
 }
 
 // P2P launch: well-separation and whether r^2 needs the kMinR2 floor
@@ -1424,6 +1450,7 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
     }
     la.fd_cap = kFarDirectCap;
     la.fd_thresh = fd_thresh;
+    la.trim = F.trim;
     if (use_fd) {
         la.lv[L].fd = (int *)carve((size_t)T.lv[L].nbox * kFarDirectCap * sizeof(int));
         la.lv[L].fd_cnt = (int *)carve((size_t)T.lv[L].nbox * sizeof(int));
@@ -1709,11 +1736,11 @@ sv_status run_fmm_forest(sv_ctx *c, Fmm &F, const ForestArgs &fa) {
         if (ws == 1)
             build_lists_kernel<1><<<forest_grid(f.cap[l], kWarps), kWarps * 32, 0, sd>>>(
                 f.cap[l], nbd + l, V.parent, V.coord, F.fnbr[l - 1], U.child0, F.fnbr[l], F.flst[l], F.fcnt[l], cap,
-                F.d_counts, V.start, fdl ? F.ffd : nullptr, F.ffd_cnt, kFarDirectCap, fd_thresh);
+                F.trim, F.d_counts, V.start, fdl ? F.ffd : nullptr, F.ffd_cnt, kFarDirectCap, fd_thresh);
         else
             build_lists_kernel<2><<<forest_grid(f.cap[l], kWarps), kWarps * 32, 0, sd>>>(
                 f.cap[l], nbd + l, V.parent, V.coord, F.fnbr[l - 1], U.child0, F.fnbr[l], F.flst[l], F.fcnt[l], cap,
-                F.d_counts, V.start, fdl ? F.ffd : nullptr, F.ffd_cnt, kFarDirectCap, fd_thresh);
+                F.trim, F.d_counts, V.start, fdl ? F.ffd : nullptr, F.ffd_cnt, kFarDirectCap, fd_thresh);
         SV_LAUNCHED(c);
     }
     SV_CK(c, cudaEventRecord(F.ev_lists, sd));
@@ -1984,6 +2011,7 @@ sv_status fmm_accel(sv_ctx *c) {
     SV_TRY(fmm_state(c));
     Fmm &F = *c->fmm;
     SV_TRY(ensure_tables(c, F, p, c->P.fmm_ws));
+    F.trim = c->P.fmm_near == 2 && c->P.fmm_ws == 2;
     Tree *T = nullptr;
     c->S.resort = false;
     SV_TRY(tree_build(c, kDepthMeanOccupancy, c->P.fmm_leaf_target, &T));
@@ -2019,6 +2047,7 @@ sv_status fmm_forest_reserve(sv_ctx *c, const ForestArgs &fa) {
     SV_TRY(fmm_state(c));
     Fmm &F = *c->fmm;
     SV_TRY(ensure_tables(c, F, p, fa.ws));
+    F.trim = c->P.fmm_near == 2 && fa.ws == 2;
     if (!F.ftree) F.ftree = new Tree();
     SV_TRY(tree_forest_reserve(c, *F.ftree, f));
     const int NC = p * (p + 1) / 2;

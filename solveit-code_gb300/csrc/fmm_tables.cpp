@@ -179,7 +179,7 @@ bool build_fmm_tables(int p, int ws, FmmTables &T, std::string &err) {
         for (int dy = -R; dy <= R; dy++)
             for (int dz = -R; dz <= R; dz++) {
                 const int id = ((dx + R) * T.side + (dy + R)) * T.side + (dz + R);
-                if (std::max(std::abs(dx), std::max(std::abs(dy), std::abs(dz))) <= ws) continue;
+                if (!fmm_m2l_class(dx, dy, dz, ws)) continue;
                 const double r = std::sqrt((double)(dx * dx + dy * dy + dz * dz));
                 const double th = std::acos(dz / r);
                 const double ph = std::atan2((double)dy, (double)dx);
@@ -301,7 +301,7 @@ bool build_m2l_dense(int p, int ws, std::vector<double> &K, std::string &err) {
     for (int dx = -range; dx <= range; dx++)
         for (int dy = -range; dy <= range; dy++)
             for (int dz = -range; dz <= range; dz++) {
-                if (std::max(std::abs(dx), std::max(std::abs(dy), std::abs(dz))) <= ws) continue;
+                if (!fmm_m2l_class(dx, dy, dz, ws)) continue;
                 const int id = ((dx + range) * side + (dy + range)) * side + (dz + range);
                 const double r = std::sqrt((double)(dx * dx + dy * dy + dz * dz));
                 const double th = std::acos(dz / r), ph = std::atan2((double)dy, (double)dx);

@@ -4,6 +4,12 @@
 #include <string>
 #include <vector>
 
+#ifdef __CUDACC__
+#define SV_HD __host__ __device__
+#else
+#define SV_HD
+#endif
+
 namespace sv {
 
 struct FmmTables {
@@ -14,7 +20,7 @@ struct FmmTables {
     int ntheta = 0;  // distinct polar angles among the M2L offsets
     int stride = 0;  // floats per rotation / translation row: p rounded up to 4 (16-byte rows)
     int esz = 0, osz = 0, dsz = 0;
-    std::vector<int> cls_theta;    // [ncls] polar-angle index, -1 for near offsets
+    std::vector<int> cls_theta;    // [ncls] polar-angle index, -1 for offsets never translated (fmm_m2l_class)
     std::vector<float> cls_phase;  // [ncls][p][2] cos(m phi), sin(m phi)
     std::vector<float> cls_rho2;   // [ncls] |offset|^2
     std::vector<float> dmat;       // [ntheta][Ef | Of | Eb | Ob] folded y-rotations, group-major rows of `stride`
@@ -37,6 +43,24 @@ struct OctLayout {
 };
 OctLayout oct_layout(int p);
 
+// Near-field offsets that the trimmed near field of ws = 2 hands to the M2L:
+// the (2,2,1) and (2,2,2) types (32 of the 125 boxes).  Their worst-case
+// separation ratio (sum of the two boxes' circumradii over the centre distance)
+// is sqrt(3)/3 for (2,2,1) and 1/2 for (2,2,2), no larger than that of the
+// closest M2L offsets of the full cube, (3,0,0).
+SV_HD inline bool fmm_trimmable(int dx, int dy, int dz, int ws) {
+    if (ws != 2) return false;
+    const int a = dx < 0 ? -dx : dx, b = dy < 0 ? -dy : dy, c = dz < 0 ? -dz : dz;
+    const int n2 = (a == 2) + (b == 2) + (c == 2);
+    return n2 == 3 || (n2 == 2 && a + b + c == 5);
+}
+// An offset class the M2L tables carry: outside the near cube, or trimmable.
+SV_HD inline bool fmm_m2l_class(int dx, int dy, int dz, int ws) {
+    const int a = dx < 0 ? -dx : dx, b = dy < 0 ? -dy : dy, c = dz < 0 ? -dz : dz;
+    const int am = a > b ? (a > c ? a : c) : (b > c ? b : c);
+    return am > ws || fmm_trimmable(dx, dy, dz, ws);
+}
+
 int rot_stride(int p);              // p rounded up to a multiple of 4
 int dmat_offset_e(int n, int p);    // stride * sum_{k<n} (k+1): E block of degree n
 int dmat_offset_o(int n, int p);    // stride * sum_{k<n} k: O block of degree n (rows mp = 1..n)
@@ -49,7 +73,7 @@ bool build_fmm_tables(int p, int ws, FmmTables &T, std::string &err);
 // Re(c_n^0), then Re(c_n^m), Im(c_n^m) for m = 1..n (the zero imaginary part
 // of c_n^0 is left out).  K[(cls * R + j) * R + k] maps input real k of the
 // source multipole to output real j of the target's local expansion (zero
-// for the near classes).
+// for the classes fmm_m2l_class leaves out).
 bool build_m2l_dense(int p, int ws, std::vector<double> &K, std::string &err);
 
 }  // namespace sv

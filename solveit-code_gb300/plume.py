@@ -55,6 +55,19 @@ def make_plume(n: int, length: float, seed: int, radius: float = 20e-9,
     }
 
 
+def make_ball(n: int, radius: float, seed: int):
+    """make_plume's ions (species, velocities) placed uniformly in a ball of
+    the given radius about the origin: a plume resolved in all three
+    dimensions, as a batch's plumes become once they expand."""
+    st = make_plume(n, 1e-6, seed)
+    rng = np.random.Generator(np.random.PCG64(seed + 7919))
+    u = rng.normal(size=(n, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    r = radius * rng.random(n) ** (1.0 / 3.0)
+    st["x"] = np.ascontiguousarray(u * r[:, None])
+    return st
+
+
 def make_batch(nplumes: int = 256, config: int = 3, nmin: int = 1024, nmax: int = 65536,
                length: float = 1e-6, direct_below: int = 8192):
     """The batched-plume workload: nplumes independent realisations.

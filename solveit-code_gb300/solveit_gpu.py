@@ -53,7 +53,7 @@ class Params(C.Structure):
         ("sym_axes", C.c_int32 * 3), ("sym_levels", C.c_int32), ("domain_size", C.c_double * 3),
         ("device", C.c_int32), ("profile_phases", C.c_int32), ("fmm_type", C.c_int32),
         ("fmm_root_scale", C.c_float), ("fmm_direct_pairs", C.c_int32), ("fmm_m2l_tc", C.c_int32),
-        ("fmm_tune_err", C.c_float), ("reserved", C.c_int32 * 1),
+        ("fmm_tune_err", C.c_float), ("fmm_near", C.c_int32),
     ]
 
 

@@ -263,6 +263,7 @@ def test_fmm_tune_chooses_order_under_error_bound():
             a = fm.accel()
         assert 1.0 <= scale < 2.0 and ms > 0
         assert (p.fmm_order, p.fmm_ws) in ((6, 2), (8, 1), (8, 2), (10, 1), (10, 2))
+        assert p.fmm_ws == 1 or p.fmm_near in (1, 2)
         assert rel_l2(a[tg], ref, st["status"][tg]) < bound * 1.5, (bound, p.fmm_order, p.fmm_ws)
         kept[bound] = (p.fmm_order, p.fmm_ws, ms)
     # the looser bound's choice is at least as fast as the tighter bound's (within timing noise)
