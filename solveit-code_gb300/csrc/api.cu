@@ -1159,6 +1159,13 @@ sv_status sv_get_stats(const sv_ctx *cc, sv_stats *out) {
         c->stats.flops_algorithmic = 20.0 * pairs + m2l * 8.0 * (2.0 * rot + zt) +
                                      (double)c->n * 8.0 * (p * (p + 1) / 2) * 4.0;
     }
+    if (c->have_accel && c->P.method == SV_METHOD_BARNES_HUT) {
+        double cells = 0, pairs = 0;
+        SV_TRY(bh_counts(c, &cells, &pairs));
+        c->stats.cell_interactions = cells;
+        c->stats.pair_interactions = pairs;
+        c->stats.flops_algorithmic = 20.0 * (cells + pairs);
+    }
     if (c->have_accel && c->P.profile_phases && cudaEventQuery(c->ph_ev[8]) == cudaSuccess) {
         for (int k = 0; k < 8; k++) {
             float t = 0.f;

@@ -62,7 +62,6 @@ struct BhLevels {
     const int *child0[kMortonBits + 1];
     const int *start[kMortonBits + 1];
     const int *skip[kMortonBits + 1];   // next cell of the depth-first order outside the subtree, or kEnd
-    float side[kMortonBits + 1];
     int deepest;
     int leaf_size;
 };
@@ -129,11 +128,12 @@ __global__ void particles_hilo(const double *__restrict__ xs, const double *__re
 __global__ void props_from_particles(int nbox, const int *__restrict__ start, const int4 *__restrict__ coord,
                                      const double *__restrict__ xs, const double *__restrict__ ys,
                                      const double *__restrict__ zs, const float *__restrict__ qs,
-                                     const double *__restrict__ root, double side, double *__restrict__ Q,
+                                     const double *__restrict__ root, int level, double *__restrict__ Q,
                                      double *__restrict__ U, double3 *__restrict__ coc, float4 *__restrict__ nh,
                                      float4 *__restrict__ nl) {
     const int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= nbox) return;
+    const double side = root[3] / (double)(1ll << level);
     double q = 0, u = 0, cx = 0, cy = 0, cz = 0;
     for (int j = start[b]; j < start[b + 1]; j++) {
         const double qj = qs[j], aq = fabs(qj);
@@ -168,23 +168,29 @@ __global__ void props_from_particles(int nbox, const int *__restrict__ start, co
 
 // coarser levels from their children (computeCellProperties :358-388):
 // centre = sum_c coc_c |Q_c| / sum_c U_c, geometric centre when U = 0
-__global__ void props_from_children(int nbox, const int *__restrict__ child0, const int4 *__restrict__ coord,
-                                    double side, const double *__restrict__ Qc, const double *__restrict__ Uc,
-                                    const double3 *__restrict__ cocc, double *__restrict__ Q, double *__restrict__ U,
-                                    double3 *__restrict__ coc, float4 *__restrict__ nh, float4 *__restrict__ nl) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nbox) return;
+struct PropLevel {
+    int nbox;
+    const int *child0;
+    const int4 *coord;
+    double *Q, *U;
+    double3 *coc;
+    float4 *nh, *nl;
+};
+
+__device__ __forceinline__ void props_box(int b, int level, const double *__restrict__ root, const PropLevel &C,
+                                          const PropLevel &V) {
+    const double side = root[3] / (double)(1ll << level);
     double q = 0, u = 0, tx = 0, ty = 0, tz = 0;
-    for (int c = child0[b]; c < child0[b + 1]; c++) {
-        const double qc = Qc[c], w = fabs(qc);
+    for (int c = V.child0[b]; c < V.child0[b + 1]; c++) {
+        const double qc = C.Q[c], w = fabs(qc);
         q += qc;
-        u += Uc[c];
-        const double3 p = cocc[c];
+        u += C.U[c];
+        const double3 p = C.coc[c];
         tx += p.x * w;
         ty += p.y * w;
         tz += p.z * w;
     }
-    const int4 cb = coord[b];
+    const int4 cb = V.coord[b];
     const double gx = (cb.x + 0.5) * side, gy = (cb.y + 0.5) * side, gz = (cb.z + 0.5) * side;
     double cx = gx, cy = gy, cz = gz;
     if (u != 0.0) {
@@ -192,16 +198,34 @@ __global__ void props_from_children(int nbox, const int *__restrict__ child0, co
         cy = ty / u;
         cz = tz / u;
     }
-    Q[b] = q;
-    U[b] = u;
-    coc[b] = make_double3(cx, cy, cz);
+    V.Q[b] = q;
+    V.U[b] = u;
+    V.coc[b] = make_double3(cx, cy, cz);
     const double dx = cx - gx, dy = cy - gy, dz = cz - gz;
     float hx, lx, hy, ly, hz, lz;
     split_hilo(cx, hx, lx);
     split_hilo(cy, hy, ly);
     split_hilo(cz, hz, lz);
-    nh[b] = make_float4(hx, hy, hz, (float)q);
-    nl[b] = make_float4(lx, ly, lz, (float)sqrt(dx * dx + dy * dy + dz * dz));
+    V.nh[b] = make_float4(hx, hy, hz, (float)q);
+    V.nl[b] = make_float4(lx, ly, lz, (float)sqrt(dx * dx + dy * dy + dz * dz));
+}
+
+// one level from the level below it, one thread per box
+__global__ void props_from_children(int level, const double *__restrict__ root, PropLevel C, PropLevel V) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < V.nbox) props_box(b, level, root, C, V);
+}
+
+// Levels top .. 0 in one CTA, level by level (coarse levels have few boxes,
+// and one launch per level made each of them a launch's latency).
+struct PropLevels {
+    PropLevel lv[kMortonBits + 1];
+};
+__global__ void props_coarse_levels(int top, const double *__restrict__ root, PropLevels P) {
+    for (int l = top; l >= 0; l--) {
+        for (int b = threadIdx.x; b < P.lv[l].nbox; b += blockDim.x) props_box(b, l, root, P.lv[l + 1], P.lv[l]);
+        __syncthreads();
+    }
 }
 
 __global__ void __launch_bounds__(kBhWarps * 32)
@@ -210,6 +234,10 @@ bh_walk_kernel(BhLevels T, const float4 *__restrict__ ph, const float4 *__restri
                const double *__restrict__ qm, int n, const double *__restrict__ root, float theta, float eps2,
                BhImages im, double *__restrict__ ax, double *__restrict__ ay, double *__restrict__ az,
                unsigned long long *__restrict__ counts) {
+    // cell side of every level, from the root cube on the device
+    __shared__ float side[kMortonBits + 1];
+    if (threadIdx.x <= T.deepest) side[threadIdx.x] = (float)(root[3] / (double)(1ll << threadIdx.x));
+    __syncthreads();
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int i = (blockIdx.x * kBhWarps + wid) * 32 + lane;
     const bool live = i < n && qm[i] != 0.0;
@@ -260,7 +288,7 @@ bh_walk_kernel(BhLevels T, const float4 *__restrict__ ph, const float4 *__restri
                 const float dx = (thx - h.x) + (tlx - lo.x), dy = (thy - h.y) + (tly - lo.y),
                             dz = (thz - h.z) + (tlz - lo.z);
                 const float d = sqrtf(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2))));
-                const bool acc = mine && theta * (d - lo.w) > T.side[lvl];
+                const bool acc = mine && theta * (d - lo.w) > side[lvl];
                 if (acc) {
                     const float f = h.w / (d * d * d);
                     fx = fmaf(f, dx, fx);
@@ -394,9 +422,6 @@ sv_status bh_accel(sv_ctx *c) {
     }
     skip_links_kernel<<<div_up(sk.first[D + 1], 256), 256, 0, c->stream>>>(sk);
     SV_LAUNCHED(c);
-    double root[8];
-    SV_TRY(read_root(c, root));
-    for (int l = 0; l <= D; l++) L.side[l] = (float)(root[3] / (double)(1ll << l));
     L.deepest = D;
     L.leaf_size = c->P.leaf_size;
     particles_hilo<<<div_up(T.n_act, 256), 256, 0, c->stream>>>(S.x, S.y, S.z, S.q, T.n_act, S.root, B.ph, B.pl);
@@ -404,16 +429,27 @@ sv_status bh_accel(sv_ctx *c) {
     {
         const Level &V = T.lv[D];
         props_from_particles<<<div_up(V.nbox, 128), 128, 0, c->stream>>>(
-            V.nbox, V.start, V.coord, S.x, S.y, S.z, S.q, S.root, root[3] / (double)(1ll << D), Q[D], U[D], coc[D],
-            (float4 *)L.nh[D], (float4 *)L.nl[D]);
+            V.nbox, V.start, V.coord, S.x, S.y, S.z, S.q, S.root, D, Q[D], U[D], coc[D], (float4 *)L.nh[D],
+            (float4 *)L.nl[D]);
         SV_LAUNCHED(c);
     }
-    for (int l = D - 1; l >= 0; l--) {
-        const Level &V = T.lv[l];
-        props_from_children<<<div_up(V.nbox, 128), 128, 0, c->stream>>>(
-            V.nbox, V.child0, V.coord, root[3] / (double)(1ll << l), Q[l + 1], U[l + 1], coc[l + 1], Q[l], U[l],
-            coc[l], (float4 *)L.nh[l], (float4 *)L.nl[l]);
-        SV_LAUNCHED(c);
+    {
+        PropLevels pl{};
+        for (int l = 0; l <= D; l++)
+            pl.lv[l] = PropLevel{T.lv[l].nbox, T.lv[l].child0, T.lv[l].coord, Q[l], U[l], coc[l],
+                                 (float4 *)L.nh[l], (float4 *)L.nl[l]};
+        // the coarse levels (every level above holding at most kCoarseBoxes boxes) in one launch
+        constexpr int kCoarseBoxes = 1024;
+        int top = -1;
+        while (top + 1 < D && T.lv[top + 1].nbox <= kCoarseBoxes) top++;
+        for (int l = D - 1; l > top; l--) {
+            props_from_children<<<div_up(T.lv[l].nbox, 128), 128, 0, c->stream>>>(l, S.root, pl.lv[l + 1], pl.lv[l]);
+            SV_LAUNCHED(c);
+        }
+        if (top >= 0) {
+            props_coarse_levels<<<1, kCoarseBoxes, 0, c->stream>>>(top, S.root, pl);
+            SV_LAUNCHED(c);
+        }
     }
     phase_mark(c, 4);
     phase_mark(c, 5);
@@ -445,15 +481,23 @@ sv_status bh_accel(sv_ctx *c) {
     }
     phase_mark(c, 6);
     if (d_off) SV_CK(c, cudaFreeAsync(d_off, c->stream));
+    // the counts reach the host with the stream; bh_counts reads them
     SV_CK(c, cudaMemcpyAsync(B.h_counts, B.d_counts, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                              c->stream));
-    SV_CK(c, cudaStreamSynchronize(c->stream));
-    c->stats.cell_interactions = (double)B.h_counts[0];
-    c->stats.pair_interactions = (double)B.h_counts[1];
-    c->stats.flops_algorithmic = 20.0 * (c->stats.cell_interactions + c->stats.pair_interactions);
     c->stats.levels = D;
     c->stats.boxes = 0;
     for (int l = 0; l <= D; l++) c->stats.boxes += T.lv[l].nbox;
+    return SV_OK;
+}
+
+sv_status bh_counts(sv_ctx *c, double *cells, double *pairs) {
+    if (!c->bh) {
+        *cells = *pairs = 0;
+        return SV_OK;
+    }
+    SV_CK(c, cudaStreamSynchronize(c->stream));
+    *cells = (double)c->bh->h_counts[0];
+    *pairs = (double)c->bh->h_counts[1];
     return SV_OK;
 }
 

@@ -291,11 +291,4 @@ sv_status unsort_accel(sv_ctx *c) {
     return SV_OK;
 }
 
-sv_status read_root(sv_ctx *c, double root[8]) {
-    SV_CK(c, cudaMemcpyAsync(c->h_scalar, c->S.root, 8 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    SV_CK(c, cudaStreamSynchronize(c->stream));
-    memcpy(root, c->h_scalar, 8 * sizeof(double));
-    return SV_OK;
-}
-
 }  // namespace sv

@@ -268,8 +268,6 @@ sv_status sort_view(sv_ctx *c, const ParticleView &v, int64_t first, int64_t las
 // c->a{x,y,z}; particles that are no target of the evaluation (K q/m of their
 // sorted slot = 0) get zero.
 sv_status unsort_accel(sv_ctx *c);
-// Read root box (origin, side) to the host (blocking).
-sv_status read_root(sv_ctx *c, double root[8]);
 
 // direct.cu
 sv_status direct_accel(sv_ctx *c);  // sorted -> c->S.a*
@@ -281,6 +279,8 @@ cudaError_t launch_direct_mixed_sorted(const double *xs, const double *ys, const
 
 // tree.cu / bh.cu / fmm.cu
 sv_status bh_accel(sv_ctx *c);
+// the last Barnes-Hut evaluation's cell and pair interaction counts (waits for the stream)
+sv_status bh_counts(sv_ctx *c, double *cells, double *pairs);
 sv_status fmm_accel(sv_ctx *c);
 // Morton levels the FMM's next sort needs (its last leaf level + 1, or all)
 int fmm_sort_levels(const sv_ctx *c);
