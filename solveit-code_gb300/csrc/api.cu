@@ -819,12 +819,21 @@ sv_status sv::compute_accel_device(sv_ctx *c, int64_t first, int64_t last) {
             if (c->P.method == SV_METHOD_FMM && c->P.symmetry != SV_SYM_NONE) return fmm_sort_images(c, first, last);
             return sort_state(c, first, last);
         };
-        // the FMM orders its keys down to one level below its last leaf level
-        SV_TRY(sort_all(c->P.method == SV_METHOD_FMM ? fmm_sort_levels(c) : kMortonBits));
+        // the FMM orders its keys down to one level below its last leaf level,
+        // the Barnes-Hut two levels below its last tree's deepest
+        SV_TRY(sort_all(c->P.method == SV_METHOD_FMM          ? fmm_sort_levels(c)
+                        : c->P.method == SV_METHOD_BARNES_HUT ? bh_sort_levels(c)
+                                                              : kMortonBits));
         phase_mark(c, 1);
         switch (c->P.method) {
         case SV_METHOD_DIRECT: SV_TRY(direct_accel(c)); break;
-        case SV_METHOD_BARNES_HUT: SV_TRY(bh_accel(c)); break;
+        case SV_METHOD_BARNES_HUT:
+            SV_TRY(bh_accel(c));
+            if (c->S.resort) {  // the tree reached the sorted levels: the full order, then again
+                SV_TRY(sort_all(kMortonBits));
+                SV_TRY(bh_accel(c));
+            }
+            break;
         case SV_METHOD_FMM:
             SV_TRY(fmm_accel(c));
             if (c->S.resort) {  // the leaf level moved down: the full order, then the FMM again

@@ -50,6 +50,7 @@ struct Bh {
     int64_t pcap = 0;
     unsigned long long *d_counts = nullptr;  // [0] accepted cells, [1] direct pairs
     unsigned long long *h_counts = nullptr;
+    int level_hint = -1;  // deepest level of the last tree
 };
 
 namespace {
@@ -359,8 +360,15 @@ sv_status bh_accel(sv_ctx *c) {
     const int n = (int)c->S.n;
     Sorted &S = c->S;
     Tree *Tp = nullptr;
+    c->S.resort = false;
     SV_TRY(tree_build(c, kDepthAllSplit, c->P.leaf_size, &Tp));
     Tree &T = *Tp;
+    // the splits are exact down to the sorted levels only; a tree reaching
+    // them needs the full order
+    if (T.n_act > 0 && T.deepest >= S.key_levels && S.key_levels < kMortonBits) {
+        c->S.resort = true;
+        return SV_OK;
+    }
     phase_mark(c, 2);
     phase_mark(c, 3);
     if (T.n_act == 0) {
@@ -370,6 +378,7 @@ sv_status bh_accel(sv_ctx *c) {
         return SV_OK;
     }
     const int D = T.deepest;
+    B.level_hint = D;
     // storage: per level Q, U (double), coc (double3), nh, nl (float4), skip links (int)
     auto rounded = [](size_t sz) { return (sz + 255) & ~(size_t)255; };
     size_t bytes = 0;
@@ -488,6 +497,11 @@ sv_status bh_accel(sv_ctx *c) {
     c->stats.boxes = 0;
     for (int l = 0; l <= D; l++) c->stats.boxes += T.lv[l].nbox;
     return SV_OK;
+}
+
+int bh_sort_levels(const sv_ctx *c) {
+    const int h = c->bh ? c->bh->level_hint : -1;
+    return h >= 1 ? std::min(kMortonBits, h + 2) : kMortonBits;
 }
 
 sv_status bh_counts(sv_ctx *c, double *cells, double *pairs) {

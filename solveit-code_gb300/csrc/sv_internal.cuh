@@ -279,6 +279,8 @@ cudaError_t launch_direct_mixed_sorted(const double *xs, const double *ys, const
 
 // tree.cu / bh.cu / fmm.cu
 sv_status bh_accel(sv_ctx *c);
+// Morton levels the Barnes-Hut's next sort needs (its last tree's depth + 2, or all)
+int bh_sort_levels(const sv_ctx *c);
 // the last Barnes-Hut evaluation's cell and pair interaction counts (waits for the stream)
 sv_status bh_counts(sv_ctx *c, double *cells, double *pairs);
 sv_status fmm_accel(sv_ctx *c);

@@ -35,6 +35,31 @@ def test_bh_theta0_is_direct(sym):
     assert s.cell_interactions == 0 and s.pair_interactions > 0
 
 
+def test_bh_sort_levels_follow_the_tree():
+    """The sort orders the keys down to two levels below the last tree's
+    depth; a tree that reaches them is sorted again in full.  One context
+    evaluates a shallow plume, then one with a tight cluster (a much deeper
+    tree), twice, then the shallow plume again.  Each result equals a fresh
+    context's (full order) to FP32 summation-order rounding, and theta = 0
+    equals the direct sum: 2e-6 on the shallow plume, 3e-5 on the cluster
+    (test_bh_deep_clusters_stackless gives the FP32 reason)."""
+    shallow = plume.make_plume(3000, 1e-6, 71)
+    deep = plume.make_plume(3000, 1e-6, 72)
+    deep["x"][:1000] = deep["x"][:1000] * 1e-4 + 3e-7
+    kw = dict(softening2=EPS20, method=sv.BARNES_HUT, theta=0.0, leaf_size=4)
+    fresh = {}
+    for name, st in (("shallow", shallow), ("deep", deep)):
+        fresh[name] = run_accel(st, **kw)
+    assert fresh["deep"][1].levels >= fresh["shallow"][1].levels + 3
+    with sv.ForceMethod(**kw) as fm:
+        for name, st, bound in (("shallow", shallow, 2e-6), ("deep", deep, 3e-5), ("deep", deep, 3e-5),
+                                ("shallow", shallow, 2e-6)):
+            fm.upload(st)
+            a = fm.accel()
+            assert rel_l2(a, fresh[name][0], st["status"]) < 1e-6, name
+            assert rel_l2(a, O.direct_f64(st, EPS20), st["status"]) < bound, name
+
+
 def test_bh_theta05_within_reference_envelope(golden_dir):
     g = dict(np.load(os.path.join(golden_dir, "bh_n4096.npz")))
     st = plume.from_ref32(g["pos4"], g["vel4"], g["acc4"], g["tinj"])
