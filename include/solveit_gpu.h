@@ -446,11 +446,16 @@ SV_API sv_status sv_upload_batch(sv_ctx *ctx, int32_t nplumes, const int64_t *co
  * evaluation to minimise P2P pairs + weight * M2L translations) and the direct
  * plumes' work-item size on the uploaded state and keeps the fastest; among
  * weights within 3 % of the fastest it keeps the largest (shallower trees, whose
- * M2L work grows less as the plumes expand).  Results are cached per batch
- * shape (plume count, size buckets, methods, symmetries, order, separation,
- * M2L path) in the process and, when cache_path is not null, in that text
- * file (read first, appended to).  best_ms (nullable) receives the tuned
- * force-evaluation time. */
+ * M2L work grows less as the plumes expand).  With fmm_tune_err > 0 it also
+ * chooses the forest's expansion order (4, 6, 8) and, at fmm_ws = 2 with
+ * fmm_near = 0, the near-field shape: the fastest whose force error (the
+ * largest over up to four FMM plumes without symmetry images, 64 sampled
+ * targets each, against an FP64 direct sum) is at most fmm_tune_err, else the
+ * most accurate; sv_get_params and sv_batch_get_info show the choice.  Results
+ * are cached per batch shape (plume count, size buckets, methods, symmetries,
+ * order, separation, near field, M2L path, error bound) in the process and,
+ * when cache_path is not null, in that text file (read first, appended to).
+ * best_ms (nullable) receives the tuned force-evaluation time. */
 SV_API sv_status sv_batch_tune(sv_ctx *ctx, const char *cache_path, double *best_ms);
 /* Autotuner of a single-plume FMM context, after the reference's timing-driven
  * choice of the FMM's level (MultipoleMethodForceCalculation::setOptimumLevel,
@@ -493,7 +498,9 @@ typedef struct {
     int32_t max_leaf;               /* most slots in one leaf box at the last evaluation */
     int32_t m2l_tc;                 /* 1: the last forest evaluation's M2L ran on the tensor cores, 0: on the
                                        FP32 rotation kernel (selected, or its room was outgrown) */
-    int32_t reserved[4];
+    int32_t fmm_order;              /* the forest's expansion order (sv_batch_tune may choose it) */
+    int32_t fmm_near;               /* the forest's near field (sv_params.fmm_near) */
+    int32_t reserved[2];
 } sv_batch_info;
 SV_API sv_status sv_batch_get_info(const sv_ctx *ctx, sv_batch_info *out);
 

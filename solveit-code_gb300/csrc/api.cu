@@ -1015,23 +1015,26 @@ static sv_status tune_root_scale(sv_ctx *c, double *best) {
     return SV_OK;
 }
 
-// Per-particle relative-L2 error of the last acceleration on up to 256 evenly
-// spaced targets against the FP64 direct sum (compareAcceleration's metric).
-static sv_status sampled_error(sv_ctx *c, double *err) {
-    const int64_t n = c->n;
-    const int k = (int)std::min<int64_t>(n, 256);
+}  // extern "C"
+
+// Per-particle relative-L2 error of the last acceleration on up to k evenly
+// spaced targets of [first, first + count) against the FP64 direct sum over
+// the sources of that range (compareAcceleration's metric; a batch's plume
+// is such a range).
+sv_status sv::sampled_error_range(sv_ctx *c, int64_t first, int64_t count, int k_max, double *err) {
+    const int k = (int)std::min<int64_t>(count, k_max);
     *err = 0.0;
     if (k == 0) return SV_OK;
     std::vector<int64_t> tg(k);
-    for (int i = 0; i < k; i++) tg[i] = (int64_t)((double)i * (double)n / (double)k);
+    for (int i = 0; i < k; i++) tg[i] = (int64_t)((double)i * (double)count / (double)k);
     void *stg = nullptr;
     SV_TRY(stage_bytes(c, sizeof(int64_t) * k + sizeof(double) * 6 * k, &stg));
     int64_t *d_tg = (int64_t *)stg;
     double *d_out = (double *)(d_tg + k);
     SV_CK(c, cudaMemcpyAsync(d_tg, tg.data(), sizeof(int64_t) * k, cudaMemcpyHostToDevice, c->stream));
-    sampled_direct_f64_kernel<<<k, kSmpThreads, 0, c->stream>>>(d_tg, c->x, c->y, c->z, c->q, c->qom, c->status, n,
-                                                               c->P.softening2, c->P.k_const, c->ax, c->ay, c->az,
-                                                               d_out);
+    sampled_direct_f64_kernel<<<k, kSmpThreads, 0, c->stream>>>(
+        d_tg, c->x + first, c->y + first, c->z + first, c->q + first, c->qom + first, c->status + first, count,
+        c->P.softening2, c->P.k_const, c->ax + first, c->ay + first, c->az + first, d_out);
     SV_LAUNCHED(c);
     std::vector<double> h(6 * (size_t)k);
     SV_CK(c, cudaMemcpyAsync(h.data(), d_out, sizeof(double) * 6 * k, cudaMemcpyDeviceToHost, c->stream));
@@ -1052,6 +1055,10 @@ static sv_status sampled_error(sv_ctx *c, double *err) {
     *err = cnt ? std::sqrt(s / cnt) : 0.0;
     return SV_OK;
 }
+
+static sv_status sampled_error(sv_ctx *c, double *err) { return sv::sampled_error_range(c, 0, c->n, 256, err); }
+
+extern "C" {
 
 sv_status sv_fmm_tune(sv_ctx *c, double *best_ms) {
     if (!c) return SV_ERR_INVALID;

@@ -933,10 +933,15 @@ sv_status batch_leapfrog(sv_ctx *c, int32_t nsteps, double dt, double t0) {
 namespace {
 
 std::mutex g_tune_mu;
-std::map<std::string, std::pair<int, int>> g_tune_cache;  // shape -> (leaf target, direct chunk)
+// shape -> the tuned choice: leaf target (M2L weight), direct chunk, FMM order and near field
+struct Tuned {
+    int lt, dc, p, near;
+};
+std::map<std::string, Tuned> g_tune_cache;
 
 // The batch's shape: plume count, per method / symmetry the plume count and
-// the log2 buckets of plume sizes, FMM order and well-separation.
+// the log2 buckets of plume sizes, FMM order and well-separation (and the
+// error bound when the order is tuned too).
 std::string shape_key(const sv_ctx *c, const Batch &B) {
     std::map<std::string, int> hist;
     for (int p = 0; p < B.np; p++) {
@@ -945,27 +950,38 @@ std::string shape_key(const sv_ctx *c, const Batch &B) {
         hist["m" + std::to_string(B.method[p]) + "s" + std::to_string(B.sym[p]) + "b" + std::to_string(bucket)]++;
     }
     std::string k = "np" + std::to_string(B.np) + "_p" + std::to_string(c->P.fmm_order) + "_ws" +
-                    std::to_string(c->P.fmm_ws) + (c->P.fmm_m2l_tc >= 0 ? "_tc" : "_rot");
+                    std::to_string(c->P.fmm_ws) + "_n" + std::to_string(c->P.fmm_near) +
+                    (c->P.fmm_m2l_tc >= 0 ? "_tc" : "_rot");
+    if (c->P.fmm_tune_err > 0.0f) {
+        char e[32];
+        snprintf(e, sizeof(e), "_err%.3g", (double)c->P.fmm_tune_err);
+        k += e;
+    }
     for (auto &kv : hist) k += "_" + kv.first + "x" + std::to_string(kv.second);
     return k;
 }
 
+// Cache file lines: key, leaf target, direct chunk, ms, then (optional) FMM
+// order and near field.
 void load_cache(const char *path) {
     if (!path) return;
     FILE *f = fopen(path, "r");
     if (!f) return;
-    char key[4096];
-    int lt, dc;
-    double ms;
-    while (fscanf(f, "%4095s %d %d %lf", key, &lt, &dc, &ms) == 4) g_tune_cache[key] = {lt, dc};
+    char line[8192], key[4096];
+    while (fgets(line, sizeof(line), f)) {
+        int lt, dc, po = 0, nr = 0;
+        double ms;
+        const int got = sscanf(line, "%4095s %d %d %lf %d %d", key, &lt, &dc, &ms, &po, &nr);
+        if (got == 4 || got == 6) g_tune_cache[key] = Tuned{lt, dc, got == 6 ? po : 0, got == 6 ? nr : 0};
+    }
     fclose(f);
 }
 
-void append_cache(const char *path, const std::string &key, int lt, int dc, double ms) {
+void append_cache(const char *path, const std::string &key, const Tuned &t, double ms) {
     if (!path) return;
     FILE *f = fopen(path, "a");
     if (!f) return;
-    fprintf(f, "%s %d %d %.6f\n", key.c_str(), lt, dc, ms);
+    fprintf(f, "%s %d %d %.6f %d %d\n", key.c_str(), t.lt, t.dc, ms, t.p, t.near);
     fclose(f);
 }
 
@@ -990,6 +1006,44 @@ sv_status time_accel(sv_ctx *c, Batch &B, int reps, double *ms) {
     return SV_OK;
 }
 
+// Leaf occupancy of the FMM plumes: the M2L weight of the depth model.
+// Among the weights within 3 % of the fastest, the largest is kept: it
+// chooses shallower trees, and as the plumes expand their M2L translations
+// grow faster than their pairs (batch256 over 10 steps from a tie at the
+// start: weight 400 95 ms per step, weight 200 107 ms).
+sv_status sweep_weights(sv_ctx *c, Batch &B, int *best_lt, double *best_ms) {
+    const int weights[6] = {100, 200, 400, 800, 1600, 3200};
+    double t[6], best = 1e30;
+    for (int k = 0; k < 6; k++) {
+        B.m2l_weight = weights[k];
+        SV_TRY(plan_forest(c, B, 1));
+        SV_TRY(time_accel(c, B, 5, &t[k]));
+        best = std::min(best, t[k]);
+    }
+    for (int k = 0; k < 6; k++)
+        if (t[k] <= 1.03 * best) *best_lt = weights[k];
+    *best_ms = best;
+    return SV_OK;
+}
+
+// The force error of the current plan: the largest over up to four FMM
+// plumes without symmetry images (the biggest), 64 sampled targets each,
+// against the FP64 direct sum of the plume.
+sv_status batch_sampled_error(sv_ctx *c, Batch &B, double *err) {
+    std::vector<int> cand;
+    for (int p = 0; p < B.np; p++)
+        if (B.method[p] == SV_METHOD_FMM && B.sym[p] == SV_SYM_NONE) cand.push_back(p);
+    std::sort(cand.begin(), cand.end(), [&](int a, int b) { return B.count[a] > B.count[b]; });
+    if (cand.size() > 4) cand.resize(4);
+    *err = 0.0;
+    for (int p : cand) {
+        double e = 0.0;
+        SV_TRY(sampled_error_range(c, B.off[p], B.count[p], 64, &e));
+        *err = std::max(*err, e);
+    }
+    return SV_OK;
+}
+
 }  // namespace
 
 sv_status batch_tune(sv_ctx *c, const char *cache_path, double *best_ms) {
@@ -1003,9 +1057,16 @@ sv_status batch_tune(sv_ctx *c, const char *cache_path, double *best_ms) {
     const std::string key = shape_key(c, B);
     auto it = g_tune_cache.find(key);
     if (it != g_tune_cache.end()) {
-        B.m2l_weight = it->second.first;
-        B.direct_chunk = it->second.second;
+        const Tuned &t = it->second;
+        if (t.p > 0 && (t.p != c->P.fmm_order || t.near != c->P.fmm_near)) {
+            c->P.fmm_order = t.p;
+            c->P.fmm_near = t.near;
+            batch_invalidate(c);
+        }
+        B.m2l_weight = t.lt;
+        B.direct_chunk = t.dc;
         SV_TRY(build_items(c, B));
+        drop_graphs(B);
         SV_TRY(plan_forest(c, B, 1));
         double ms = 0;
         SV_TRY(time_accel(c, B, 3, &ms));
@@ -1013,24 +1074,53 @@ sv_status batch_tune(sv_ctx *c, const char *cache_path, double *best_ms) {
         if (best_ms) *best_ms = ms;
         return SV_OK;
     }
-    // leaf occupancy first (FMM plumes), then the direct work-item size.
-    // Among the weights within 3 % of the fastest, the largest is kept: it
-    // chooses shallower trees, and as the plumes expand their M2L
-    // translations grow faster than their pairs (batch256 over 10 steps from
-    // a tie at the start: weight 400 95 ms per step, weight 200 107 ms).
     int best_lt = B.m2l_weight, best_dc = B.direct_chunk;
     double best = 1e30;
-    if (B.nfp > 0) {
-        const int weights[6] = {100, 200, 400, 800, 1600, 3200};
-        double t[6];
-        for (int k = 0; k < 6; k++) {
-            B.m2l_weight = weights[k];
-            SV_TRY(plan_forest(c, B, 1));
-            SV_TRY(time_accel(c, B, 5, &t[k]));
-            best = std::min(best, t[k]);
+    if (B.nfp > 0 && c->P.fmm_tune_err > 0.0f) {
+        // the expansion order and near field too: the fastest (order, shape)
+        // whose sampled force error meets fmm_tune_err (else the most accurate)
+        struct Cand {
+            int p, near;
+        };
+        std::vector<Cand> cands;
+        const int fixed_near = c->P.fmm_near;
+        for (const int p : {4, 6, 8}) {
+            if (c->P.fmm_ws == 2 && fixed_near == 0) {
+                cands.push_back({p, 2});
+                cands.push_back({p, 1});
+            } else {
+                cands.push_back({p, fixed_near});
+            }
         }
-        for (int k = 0; k < 6; k++)
-            if (t[k] <= 1.03 * best) best_lt = weights[k];
+        int kept = -1, most_acc = 0;
+        double kept_t = 1e30, min_err = 1e300;
+        std::vector<int> lts(cands.size());
+        for (size_t k = 0; k < cands.size(); k++) {
+            c->P.fmm_order = cands[k].p;
+            c->P.fmm_near = cands[k].near;
+            batch_invalidate(c);
+            double t = 0.0, e = 0.0;
+            SV_TRY(sweep_weights(c, B, &lts[k], &t));
+            B.m2l_weight = lts[k];
+            SV_TRY(plan_forest(c, B, 1));
+            SV_TRY(time_accel(c, B, 3, &t));
+            SV_TRY(batch_sampled_error(c, B, &e));
+            if (e < min_err) {
+                min_err = e;
+                most_acc = (int)k;
+            }
+            if (e <= (double)c->P.fmm_tune_err && t < kept_t) {
+                kept_t = t;
+                kept = (int)k;
+            }
+        }
+        const int k = kept >= 0 ? kept : most_acc;
+        c->P.fmm_order = cands[k].p;
+        c->P.fmm_near = cands[k].near;
+        batch_invalidate(c);
+        best_lt = lts[k];
+    } else if (B.nfp > 0) {
+        SV_TRY(sweep_weights(c, B, &best_lt, &best));
     }
     B.m2l_weight = best_lt;
     SV_TRY(plan_forest(c, B, 1));
@@ -1054,8 +1144,10 @@ sv_status batch_tune(sv_ctx *c, const char *cache_path, double *best_ms) {
     double ms = 0;
     SV_TRY(time_accel(c, B, 5, &ms));
     B.tuned_ms = ms;
-    g_tune_cache[key] = {best_lt, best_dc};
-    append_cache(cache_path, key, best_lt, best_dc, ms);
+    const Tuned t{best_lt, best_dc, c->P.fmm_tune_err > 0.0f ? c->P.fmm_order : 0,
+                  c->P.fmm_tune_err > 0.0f ? c->P.fmm_near : 0};
+    g_tune_cache[key] = t;
+    append_cache(cache_path, key, t, ms);
     if (best_ms) *best_ms = ms;
     return SV_OK;
 }
@@ -1101,6 +1193,8 @@ sv_status batch_info(const sv_ctx *c, sv_batch_info *out) {
     }
     out->overflow_mask = B.overflow_mask;
     out->m2l_tc = fmm_forest_tc_used(c) ? 1 : 0;
+    out->fmm_order = c->P.fmm_order;
+    out->fmm_near = c->P.fmm_near;
     if (B.planned && B.nfp > 0) {
         int h[3 * kBLevels];
         SV_CK(const_cast<sv_ctx *>(c), cudaMemcpy(h, B.d_nbox, sizeof(h), cudaMemcpyDeviceToHost));

@@ -279,6 +279,9 @@ cudaError_t launch_direct_mixed_sorted(const double *xs, const double *ys, const
 
 // tree.cu / bh.cu / fmm.cu
 sv_status bh_accel(sv_ctx *c);
+// Relative-L2 error of the last acceleration on up to k_max evenly spaced
+// targets of [first, first + count) against the FP64 direct sum over that range
+sv_status sampled_error_range(sv_ctx *c, int64_t first, int64_t count, int k_max, double *err);
 // Morton levels the Barnes-Hut's next sort needs (its last tree's depth + 2, or all)
 int bh_sort_levels(const sv_ctx *c);
 // the last Barnes-Hut evaluation's cell and pair interaction counts (waits for the stream)

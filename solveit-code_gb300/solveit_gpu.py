@@ -73,7 +73,8 @@ class BatchInfo(C.Structure):
         ("tuned_ms", C.c_double), ("direct_pairs", C.c_double), ("fmm_m2l", C.c_double),
         ("fmm_pairs", C.c_double), ("regrows", C.c_int32), ("overflow_mask", C.c_int32),
         ("level_boxes", C.c_int32 * 22), ("level_cap", C.c_int32 * 22), ("level_max", C.c_int32 * 22),
-        ("max_leaf", C.c_int32), ("m2l_tc", C.c_int32), ("reserved", C.c_int32 * 4),
+        ("max_leaf", C.c_int32), ("m2l_tc", C.c_int32), ("fmm_order", C.c_int32),
+        ("fmm_near", C.c_int32), ("reserved", C.c_int32 * 2),
     ]
 
 
@@ -268,6 +269,7 @@ class ForceMethod:
         ms = C.c_double()
         path = None if cache_path is None else str(cache_path).encode()
         self._check(self.L.sv_batch_tune(self.h, path, C.byref(ms)))
+        self._check(self.L.sv_get_params(self.h, C.byref(self.params)))  # an order the tuner chose
         return ms.value
 
     def set_tuning(self, m2l_weight, direct_chunk):

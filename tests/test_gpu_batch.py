@@ -118,17 +118,51 @@ def test_batch_tune_and_cache(tmp_path):
     assert info.m2l_weight in (100, 200, 400, 800, 1600, 3200)
     assert info.direct_chunk in (1024, 2048, 4096, 8192)
     lines = cache.read_text().split()
-    assert len(lines) == 4 and int(lines[1]) == info.m2l_weight
+    # key, leaf target, direct chunk, ms, order and near field (0: not tuned)
+    assert len(lines) == 6 and int(lines[1]) == info.m2l_weight and lines[4:] == ["0", "0"]
     # a new context with the same shape reads the cached choice
     with batch_ctx() as fm2:
         fm2.upload_batch(states, methods, syms)
         fm2.tune(cache)
         i2 = fm2.batch_info()
     assert (i2.m2l_weight, i2.direct_chunk) == (info.m2l_weight, info.direct_chunk)
-    assert len(cache.read_text().split()) == 4
+    assert len(cache.read_text().split()) == 6
     for s, ap, meth, sym in zip(states, a, methods, syms):
         ref = O.direct_f64(s, EPS20, sym=sym)
         assert O.rel_l2(ap, ref, s["status"])[0] <= (TOL_DIRECT if meth == sv.DIRECT else TOL_FMM_P6)
+
+
+def test_batch_tune_chooses_order_under_error_bound(tmp_path):
+    """With fmm_tune_err the batch tuner also picks the forest's order and
+    near field: the kept choice meets the bound on every FMM plume against
+    the oracle (1.5x margin: the tuner samples 64 targets on up to four
+    plumes), a looser bound keeps a choice at least as fast, and a cached
+    choice is restored in a new context."""
+    sizes = [9000, 14000, 20000, 3000]
+    states = [plume.make_ball(n, 100e-9, 3500 + i) for i, n in enumerate(sizes)]
+    methods = [sv.FMM, sv.FMM, sv.FMM, sv.DIRECT]
+    syms = [sv.SYM_NONE, sv.SYM_ROTATIONAL, sv.SYM_NONE, sv.SYM_NONE]
+    cache = tmp_path / "tune.txt"
+    kept = {}
+    for bound in (1e-5, 3e-4):
+        with sv.ForceMethod(softening2=EPS20, fmm_order=6, fmm_ws=2, fmm_tune_err=bound) as fm:
+            fm.upload_batch(states, methods, syms)
+            fm.tune(cache)
+            info = fm.batch_info()
+            a = split(fm.accel(), states)
+        assert info.fmm_order in (4, 6, 8) and info.fmm_near in (1, 2)
+        for s, ap, meth, sym in zip(states, a, methods, syms):
+            if meth == sv.FMM:
+                e = O.rel_l2(ap, O.direct_f64(s, EPS20, sym=sym), s["status"])[0]
+                assert e <= 1.5 * bound, (bound, info.fmm_order, info.fmm_near, sym, e)
+        kept[bound] = (info.fmm_order, info.fmm_near, info.tuned_ms)
+    # the looser bound's choice is at least as fast (within timing noise)
+    assert kept[3e-4][2] <= 1.15 * kept[1e-5][2], kept
+    with sv.ForceMethod(softening2=EPS20, fmm_order=6, fmm_ws=2, fmm_tune_err=1e-5) as fm:
+        fm.upload_batch(states, methods, syms)
+        fm.tune(cache)
+        i2 = fm.batch_info()
+    assert (i2.fmm_order, i2.fmm_near) == kept[1e-5][:2]
 
 
 def test_batch_edge_cases():
