@@ -202,6 +202,32 @@ __global__ void unpack_fp64(const double *__restrict__ x3, const double *__restr
     to[i] = has_t ? tinj[i] : 0.0;
 }
 
+// The same unpacking, reading the caller's arrays in place in mapped host
+// memory (over NVLink-C2C on a Grace-Blackwell node): each thread takes
+// consecutive doubles of the interleaved x3 / v3 arrays, so a warp's loads are
+// one contiguous run across the link.
+__global__ void unpack_mapped(const double *__restrict__ x3, const double *__restrict__ v3,
+                              const double *__restrict__ q, const double *__restrict__ m,
+                              const int32_t *__restrict__ st, const double *__restrict__ tinj, int64_t n,
+                              int has_v, int has_t, double *__restrict__ x, double *__restrict__ y,
+                              double *__restrict__ z, double *__restrict__ vx, double *__restrict__ vy,
+                              double *__restrict__ vz, double *__restrict__ qo, double *__restrict__ mo,
+                              int32_t *__restrict__ so, double *__restrict__ to) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < 3 * n; t += stride) {
+        const int64_t i = t / 3;
+        const int d = (int)(t - 3 * i);
+        (d == 0 ? x : (d == 1 ? y : z))[i] = x3[t];
+        (d == 0 ? vx : (d == 1 ? vy : vz))[i] = has_v ? v3[t] : 0.0;
+        if (t < n) {
+            qo[t] = q[t];
+            mo[t] = m[t];
+            so[t] = st[t];
+            to[t] = has_t ? tinj[t] : 0.0;
+        }
+    }
+}
+
 // ParticleSpeciesFunction::getMass (particles.h:65-87): EMI 111, BF4 87 amu
 __device__ double species_mass(int s) {
     switch (s) {
@@ -242,6 +268,36 @@ __global__ void pack_fp64(const double *__restrict__ x, const double *__restrict
     v3[3 * i] = vx[i]; v3[3 * i + 1] = vy[i]; v3[3 * i + 2] = vz[i];
 }
 
+// pack_fp64 writing the caller's arrays in place in mapped host memory,
+// consecutive doubles per thread (v3 and st optional)
+__global__ void pack_mapped(const double *__restrict__ x, const double *__restrict__ y,
+                            const double *__restrict__ z, const double *__restrict__ vx,
+                            const double *__restrict__ vy, const double *__restrict__ vz,
+                            const int32_t *__restrict__ st, int64_t n, double *__restrict__ x3,
+                            double *__restrict__ v3, int32_t *__restrict__ st_out) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < 3 * n; t += stride) {
+        const int64_t i = t / 3;
+        const int d = (int)(t - 3 * i);
+        if (x3) x3[t] = (d == 0 ? x : (d == 1 ? y : z))[i];
+        if (v3) v3[t] = (d == 0 ? vx : (d == 1 ? vy : vz))[i];
+        if (st_out && t < n) st_out[t] = st[t];
+    }
+}
+
+// pack_accel over all particles, writing mapped host memory in place,
+// consecutive doubles per thread
+__global__ void pack_accel_mapped(const double *__restrict__ ax, const double *__restrict__ ay,
+                                  const double *__restrict__ az, const int32_t *__restrict__ st, int64_t n,
+                                  double *__restrict__ a3) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < 3 * n; t += stride) {
+        const int64_t i = t / 3;
+        const int d = (int)(t - 3 * i);
+        a3[t] = st[i] == 1 ? (d == 0 ? ax : (d == 1 ? ay : az))[i] : 0.0;
+    }
+}
+
 __global__ void pack_accel(const double *__restrict__ ax, const double *__restrict__ ay,
                            const double *__restrict__ az, const int32_t *__restrict__ st,
                            int64_t first, int64_t last, int64_t n, double *__restrict__ a3) {
@@ -265,6 +321,27 @@ __global__ void range_status(const int32_t *__restrict__ st, int64_t first, int6
 // Host <-> device copies split in pieces over the copy streams, so that
 // several copy engines share a large transfer: ordered after the work already
 // on c->stream and joined back into it.
+// Device address of a caller's host array that kernels may read and write in
+// place: memory pinned by cudaHostAlloc / cudaHostRegister and mapped into
+// the device's address space.  Null for anything else (pageable memory goes
+// by copies).
+static void *mapped_host(const void *h) {
+    if (!h) return nullptr;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// grid of a grid-stride pass over the host link: enough loads in flight
+static int link_grid(int64_t items) {
+    const int64_t g = (items + 255) / 256;
+    const int64_t cap = 8 * (int64_t)device_sms();
+    return (int)std::max<int64_t>(1, std::min(g, cap));
+}
+
 struct HostCopy {
     void *dst;
     const void *src;
@@ -665,6 +742,22 @@ static sv_status upload_state(sv_ctx *c, int64_t n, const double *x3, const doub
     if (n == 0) return SV_OK;
     SV_CK(c, cudaMemsetAsync(c->e2, 0, sizeof(float) * 3 * (size_t)n, c->stream));
     SV_CK(c, cudaMemsetAsync(c->e1, 0, sizeof(float) * 3 * (size_t)n, c->stream));
+    {
+        // pinned, mapped arrays: read in place, no staging copy
+        const double *mx = (const double *)mapped_host(x3), *mv = (const double *)mapped_host(v3);
+        const double *mq = (const double *)mapped_host(q), *mm = (const double *)mapped_host(m_amu);
+        const double *mt = (const double *)mapped_host(t_inj);
+        const int32_t *ms = (const int32_t *)mapped_host(status);
+        if (mx && mq && mm && ms && (!v3 || mv) && (!t_inj || mt)) {
+            unpack_mapped<<<link_grid(3 * n), 256, 0, c->stream>>>(
+                mx, mv, mq, mm, ms, mt, n, v3 != nullptr, t_inj != nullptr, c->x, c->y, c->z, c->vx, c->vy, c->vz,
+                c->q, c->m, c->status, c->t_inj);
+            SV_LAUNCHED(c);
+            charge_over_mass<<<grid_of(n), 256, 0, c->stream>>>(c->q, c->m, n, c->qom, c->species);
+            SV_LAUNCHED(c);
+            return SV_OK;
+        }
+    }
     const size_t b3 = sizeof(double) * 3 * (size_t)n, b1 = sizeof(double) * (size_t)n;
     void *stg = nullptr;
     SV_TRY(stage_bytes(c, 2 * b3 + 3 * b1 + sizeof(int32_t) * (size_t)n, &stg));
@@ -745,6 +838,18 @@ sv_status sv_download(sv_ctx *c, double *x3, double *v3, int32_t *status) {
     const int64_t n = c->n;
     if (n == 0) return SV_OK;
     SV_CK(c, cudaSetDevice(c->device));
+    {
+        // pinned, mapped arrays: written in place, no staging copy
+        double *mx = (double *)mapped_host(x3), *mv = (double *)mapped_host(v3);
+        int32_t *ms = (int32_t *)mapped_host(status);
+        if ((!x3 || mx) && (!v3 || mv) && (!status || ms)) {
+            pack_mapped<<<link_grid(3 * n), 256, 0, c->stream>>>(c->x, c->y, c->z, c->vx, c->vy, c->vz, c->status, n,
+                                                                 mx, mv, ms);
+            SV_LAUNCHED(c);
+            SV_CK(c, cudaStreamSynchronize(c->stream));
+            return SV_OK;
+        }
+    }
     const size_t b3 = sizeof(double) * 3 * (size_t)n;
     void *stg = nullptr;
     SV_TRY(stage_bytes(c, 2 * b3, &stg));
@@ -867,6 +972,12 @@ sv_status sv_compute_accel(sv_ctx *c, int64_t first, int64_t last, double *a3_ou
     SV_TRY(compute_accel_device(c, first, last));
     if (a3_out && c->n > 0) {
         const int64_t n = c->n;
+        if (double *ma = (double *)mapped_host(a3_out)) {  // pinned and mapped: written in place
+            pack_accel_mapped<<<link_grid(3 * n), 256, 0, c->stream>>>(c->ax, c->ay, c->az, c->status, n, ma);
+            SV_LAUNCHED(c);
+            SV_CK(c, cudaStreamSynchronize(c->stream));
+            return SV_OK;
+        }
         void *stg = nullptr;
         SV_TRY(stage_bytes(c, sizeof(double) * 3 * n, &stg));
         pack_accel<<<grid_of(n), 256, 0, c->stream>>>(c->ax, c->ay, c->az, c->status, 0, n, n, (double *)stg);
@@ -891,11 +1002,16 @@ sv_status sv_add_accel_ref32(sv_ctx *c, float *acc4) {
         c->h_accel_cap = 3 * n;
     }
     const double *a = c->h_accel;
-    void *stg = nullptr;
-    SV_TRY(stage_bytes(c, sizeof(double) * 3 * n, &stg));
-    pack_accel<<<grid_of(n), 256, 0, c->stream>>>(c->ax, c->ay, c->az, c->status, 0, n, n, (double *)stg);
-    SV_LAUNCHED(c);
-    SV_CK(c, cudaMemcpyAsync(c->h_accel, stg, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c->stream));
+    if (double *ma = (double *)mapped_host(c->h_accel)) {  // mapped: written in place
+        pack_accel_mapped<<<link_grid(3 * n), 256, 0, c->stream>>>(c->ax, c->ay, c->az, c->status, n, ma);
+        SV_LAUNCHED(c);
+    } else {
+        void *stg = nullptr;
+        SV_TRY(stage_bytes(c, sizeof(double) * 3 * n, &stg));
+        pack_accel<<<grid_of(n), 256, 0, c->stream>>>(c->ax, c->ay, c->az, c->status, 0, n, n, (double *)stg);
+        SV_LAUNCHED(c);
+        SV_CK(c, cudaMemcpyAsync(c->h_accel, stg, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, c->stream));
+    }
     SV_CK(c, cudaStreamSynchronize(c->stream));
     for (int64_t i = 0; i < n; i++) {
         if (acc4[4 * i + 3] != 1.0f) continue;
