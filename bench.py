@@ -655,7 +655,7 @@ def run_ours(args, wl, rank, world, local):
         # ---- phase breakdown and roofline of the dominant kernel
         names = ["sort", "tree", "lists", "upward_p2m_m2m", "downward_m2l_l2l", "l2p", "near_p2p", "scatter"]
         if wl["method"] == "bh":
-            names = ["sort", "tree", "-", "cell_properties", "-", "walk", "counts_readback", "scatter"]
+            names = ["sort", "tree", "-", "cell_properties", "-", "walk", "walk_tail", "scatter"]
         line["phases_ms"] = {nm: round(float(v), 4) for nm, v in zip(names, phase_ms)}
         sm_max = measured_peaks().get("sm_max_mhz", 2070.0)
         fp32_peak, sms = fp32_peak_tflops(local, sm_max)

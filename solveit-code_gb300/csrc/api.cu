@@ -1115,7 +1115,7 @@ static sv_status tune_root_scale(sv_ctx *c, double *best) {
     for (int k = 0; k < 8; k++) {
         c->P.fmm_root_scale = 1.0f + 0.125f * (float)k;
         double t = 1e300;
-        for (int r = 0; r < 3; r++) {  // the first evaluation warms the scale's buffers
+        for (int r = 0; r < 5; r++) {  // the first evaluation warms the scale's buffers; min of the other four
             SV_TRY(compute_accel_device(c, 0, c->n));
             SV_CK(c, cudaEventSynchronize(c->ev_end));
             float ms = 0.f;
