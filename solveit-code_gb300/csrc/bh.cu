@@ -56,6 +56,7 @@ struct Bh {
 namespace {
 
 constexpr int kBhWarps = 4;
+constexpr int kBhHalfWarps = 32;  // warps per SM below which the walk takes 16 targets per warp
 
 struct BhLevels {
     const float4 *nh[kMortonBits + 1];  // centre hi (xyz) + net charge
@@ -229,6 +230,12 @@ __global__ void props_coarse_levels(int top, const double *__restrict__ root, Pr
     }
 }
 
+// TPW targets per warp: 32, or 16 with the two half-warps sharing each
+// target (both take the same acceptance decisions, the lower half adds the
+// accepted cells, the halves split each opened leaf's particles and add their
+// sums at the end): twice the warps for a small plume, each walking the union
+// of fewer targets' cells.
+template <int TPW>
 __global__ void __launch_bounds__(kBhWarps * 32)
 bh_walk_kernel(BhLevels T, const float4 *__restrict__ ph, const float4 *__restrict__ pl,
                const double *__restrict__ xs, const double *__restrict__ ys, const double *__restrict__ zs,
@@ -240,7 +247,8 @@ bh_walk_kernel(BhLevels T, const float4 *__restrict__ ph, const float4 *__restri
     if (threadIdx.x <= T.deepest) side[threadIdx.x] = (float)(root[3] / (double)(1ll << threadIdx.x));
     __syncthreads();
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int i = (blockIdx.x * kBhWarps + wid) * 32 + lane;
+    const int half = lane / TPW;  // 0, or 1 for the upper half-warp when TPW = 16
+    const int i = (blockIdx.x * kBhWarps + wid) * TPW + lane % TPW;
     const bool live = i < n && qm[i] != 0.0;
     const unsigned live_mask = __ballot_sync(0xffffffffu, live);
     if (live_mask == 0) return;
@@ -290,7 +298,7 @@ bh_walk_kernel(BhLevels T, const float4 *__restrict__ ph, const float4 *__restri
                             dz = (thz - h.z) + (tlz - lo.z);
                 const float d = sqrtf(fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2))));
                 const bool acc = mine && theta * (d - lo.w) > side[lvl];
-                if (acc) {
+                if (acc && half == 0) {
                     const float f = h.w / (d * d * d);
                     fx = fmaf(f, dx, fx);
                     fy = fmaf(f, dy, fy);
@@ -302,7 +310,7 @@ bh_walk_kernel(BhLevels T, const float4 *__restrict__ ph, const float4 *__restri
                     const bool leaf = lvl == T.deepest || (s1 - s0) <= T.leaf_size;
                     if (leaf) {
 #pragma unroll 4
-                        for (int j = s0; j < s1; j++) {
+                        for (int j = s0 + half; j < s1; j += 32 / TPW) {
                             const float4 qh = ph[j], ql = pl[j];
                             if (rej && !(self_excl && j == i)) {
                                 const float ex = (thx - qh.x) + (tlx - ql.x), ey = (thy - qh.y) + (tly - ql.y),
@@ -328,12 +336,17 @@ bh_walk_kernel(BhLevels T, const float4 *__restrict__ ph, const float4 *__restri
         sy += (float)sb * fx + (float)cb * fy;
         sz += fz;
     }
-    if (live) {
+    if (TPW == 16) {
+        sx += __shfl_xor_sync(0xffffffffu, sx, 16);
+        sy += __shfl_xor_sync(0xffffffffu, sy, 16);
+        sz += __shfl_xor_sync(0xffffffffu, sz, 16);
+    }
+    if (half == 0 && live) {
         const double c = qm[i];
         ax[i] = (double)sx * c;
         ay[i] = (double)sy * c;
         az[i] = (double)sz * c;
-    } else if (i < n) {
+    } else if (half == 0 && i < n) {
         ax[i] = ay[i] = az[i] = 0.0;
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -479,9 +492,15 @@ sv_status bh_accel(sv_ctx *c) {
     }
     SV_CK(c, cudaMemsetAsync(B.d_counts, 0, 2 * sizeof(unsigned long long), c->stream));
     // inactive sorted slots (beyond n_act) are never targets (qm = 0)
-    bh_walk_kernel<<<div_up(n, 32 * kBhWarps), 32 * kBhWarps, 0, c->stream>>>(
-        L, B.ph, B.pl, S.x, S.y, S.z, S.qm, T.n_act, S.root, c->P.theta, (float)c->P.softening2, im, S.ax, S.ay,
-        S.az, B.d_counts);
+    // half-warp targets while 32 per warp would leave fewer than kBhHalfWarps warps per SM
+    if (div_up(n, 32) < kBhHalfWarps * device_sms())
+        bh_walk_kernel<16><<<div_up(n, 16 * kBhWarps), 32 * kBhWarps, 0, c->stream>>>(
+            L, B.ph, B.pl, S.x, S.y, S.z, S.qm, T.n_act, S.root, c->P.theta, (float)c->P.softening2, im, S.ax, S.ay,
+            S.az, B.d_counts);
+    else
+        bh_walk_kernel<32><<<div_up(n, 32 * kBhWarps), 32 * kBhWarps, 0, c->stream>>>(
+            L, B.ph, B.pl, S.x, S.y, S.z, S.qm, T.n_act, S.root, c->P.theta, (float)c->P.softening2, im, S.ax, S.ay,
+            S.az, B.d_counts);
     SV_LAUNCHED(c);
     if (T.n_act < n) {
         SV_CK(c, cudaMemsetAsync(S.ax + T.n_act, 0, sizeof(double) * (n - T.n_act), c->stream));

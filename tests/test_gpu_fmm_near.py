@@ -89,6 +89,34 @@ def test_trimmed_leapfrog_tracks_direct():
     assert np.sqrt(np.mean(dv ** 2)) < 1e-5
 
 
+@pytest.mark.parametrize("sym", [1, 2])
+def test_trimmed_symmetry_images(sym):
+    """Rotational (4 quadrant images) and translational (81 images) variants
+    with the trimmed near field: the image copies join the tree as sources,
+    so their boxes at trimmed offsets are M2L sources too."""
+    st = plume.make_ball(4096, 150e-9, 9600 + sym)
+    st["x"][:, 0] += 3e-7
+    img = O.trans_images(2, (1, 1, 0)) * np.array([1e-6, 1e-6, 0.0]) if sym == 2 else None
+    ref = O.direct_f64(st, EPS20, sym=sym, img_off=img)
+    kw = dict(fmm_order=8, fmm_ws=2, symmetry=sym, sym_axes=(1, 1, 0), sym_levels=2, domain_size=(1e-6, 1e-6, 0.0))
+    a2, s2 = _eval(st, fmm_near=2, **kw)
+    a1, s1 = _eval(st, fmm_near=1, **kw)
+    assert rel_l2(a2, ref, st["status"]) < 1e-5
+    assert s2.pair_interactions < s1.pair_interactions
+
+
+@pytest.mark.parametrize("ftype", [sv.TREECODE, sv.FMM_OUTLIERS])
+def test_trimmed_treecode_and_outlier_types(ftype):
+    """The treecode evaluates interaction-list entries by M2P, the outlier
+    variant leaves outliers out of the tree: both take the trimmed lists."""
+    st = plume.make_ball(16384, 120e-9, 9700)
+    if ftype == sv.FMM_OUTLIERS:
+        st["x"][:16] *= 40.0  # a few ions far outside the ball
+    ref = O.direct_f64(st, EPS20)
+    a, _ = _eval(st, fmm_order=8, fmm_ws=2, fmm_near=2, fmm_type=ftype)
+    assert rel_l2(a, ref, st["status"]) < 2e-5
+
+
 def test_near_option_ignored_at_separation_1():
     st = plume.make_ball(16384, 100e-9, 9500)
     a1, _ = _eval(st, fmm_order=8, fmm_ws=1, fmm_near=1)
