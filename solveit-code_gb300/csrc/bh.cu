@@ -404,7 +404,7 @@ sv_status bh_accel(sv_ctx *c) {
         cudaFree(B.arena);
         B.arena = nullptr;
         B.arena_bytes = 0;
-        const size_t want = bytes + bytes / 4;
+        const size_t want = bytes + bytes / 2;  // headroom: a growing tree reallocates rarely
         SV_CK(c, cudaMalloc(&B.arena, want));
         B.arena_bytes = want;
     }

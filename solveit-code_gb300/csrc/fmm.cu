@@ -1407,7 +1407,7 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         cudaFree(F.arena);
         F.arena = nullptr;
         F.arena_bytes = 0;
-        const size_t want = bytes + bytes / 4;
+        const size_t want = bytes + bytes / 2;  // headroom: a growing tree reallocates rarely
         SV_CK(c, cudaMalloc(&F.arena, want));
         F.arena_bytes = want;
     }
@@ -1465,8 +1465,9 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         if (F.tgt_cap < tot) {
             cudaFree(F.has_tgt);
             F.has_tgt = nullptr;
-            SV_CK(c, cudaMalloc(&F.has_tgt, sizeof(int) * tot));
-            F.tgt_cap = tot;
+            const int64_t want = tot + tot / 2;  // headroom: a growing tree reallocates rarely
+            SV_CK(c, cudaMalloc(&F.has_tgt, sizeof(int) * want));
+            F.tgt_cap = want;
         }
         int64_t o = 0;
         for (int l = 0; l <= L; l++) {
@@ -2123,7 +2124,7 @@ sv_status fmm_forest_tc_grow(sv_ctx *c) {
     const int64_t limit = (int64_t)(0.4 * (double)total_b / per_entry);
     const int64_t want = std::min<int64_t>(4 * need, limit);
     if (want <= F.tc.cap) return SV_OK;
-    return m2l_tc_prepare(c, F.tc, p, F.tc.ws, want);
+    return m2l_tc_prepare(c, F.tc, p, F.tc.ws, want, true);
 }
 
 bool fmm_forest_tc_used(const sv_ctx *c) {

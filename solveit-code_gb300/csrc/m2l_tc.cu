@@ -789,7 +789,7 @@ sv_status build_ops(sv_ctx *c, M2LTc &T, int ws) {
 
 }  // namespace
 
-sv_status m2l_tc_prepare(sv_ctx *c, M2LTc &T, int p, int ws, int64_t entries) {
+sv_status m2l_tc_prepare(sv_ctx *c, M2LTc &T, int p, int ws, int64_t entries, bool exact) {
     if (T.p != p || T.ws != ws || !T.ops) {
         switch (p) {
         case 4: SV_TRY(build_ops<4>(c, T, ws)); break;
@@ -818,7 +818,10 @@ sv_status m2l_tc_prepare(sv_ctx *c, M2LTc &T, int p, int ws, int64_t entries) {
         T.rows = nullptr;
         T.tiles = nullptr;
         T.cap = 0;
-        const int64_t cap = std::max<int64_t>(entries, 1 << 16);
+        // half as much again: a growing plume's count then reallocates (a
+        // device-wide synchronisation in the middle of an evaluation) a few
+        // times in a run, not at every step
+        const int64_t cap = std::max<int64_t>(exact ? entries : entries + entries / 2, 1 << 16);
         SV_CK(c, cudaMalloc(&T.bucket, sizeof(int4) * (size_t)cap));
         SV_CK(c, cudaMalloc(&T.tiles, sizeof(int4) * (size_t)(cap / kTile + T.ncls + 1)));
         const size_t rstride = ((size_t)p * (p + 1) * 4 + 15) / 16 * 16;  // RowShape<p>::RSTRIDE

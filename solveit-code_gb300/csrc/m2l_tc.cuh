@@ -66,8 +66,9 @@ struct M2LTc {
 };
 
 // Build (once per order / separation) and upload the class operators;
-// reserve room for `entries` translations.
-sv_status m2l_tc_prepare(sv_ctx *c, M2LTc &T, int p, int ws, int64_t entries);
+// reserve room for `entries` translations (half as much again when it has to
+// grow, unless exact).
+sv_status m2l_tc_prepare(sv_ctx *c, M2LTc &T, int p, int ws, int64_t entries, bool exact = false);
 // The class pass, the bucket pass, the tensor-core tiles and the reduction,
 // all on stream s.  When the translations exceed the reserved room, nothing
 // is computed and ctl[2] is set: the caller's rotation M2L launch then runs

@@ -284,7 +284,7 @@ sv_status arena_reserve(sv_ctx *c, Tree &T, size_t bytes) {
     cudaFree(T.arena);
     T.arena = nullptr;
     T.arena_bytes = 0;
-    const size_t want = bytes + bytes / 4;
+    const size_t want = bytes + bytes / 2;  // headroom: a growing tree reallocates rarely
     SV_CK(c, cudaMalloc(&T.arena, want));
     T.arena_bytes = want;
     return SV_OK;
