@@ -68,6 +68,19 @@ constexpr int kBuildThreads = 1024;  // particles per CTA of the level builder
 // max_i min(lvl[i+1 .. i+leaf]): a window of leaf+1 consecutive particles
 // without a box boundary at level <= l means a box of level l with more than
 // `leaf` particles.  Slots past the active particles count as boundaries.
+// the histogram's counters zeroed and the active count at n (no inactive particle)
+__global__ void hist_init(int *__restrict__ hist, int n) {
+    const int t = threadIdx.x;
+    if (t <= kLevels) hist[t] = 0;
+    if (t == kLevels + 1) hist[t] = n;
+}
+
+// the histogram into the host's mapped copy (the host waits on the stream, then reads it)
+__global__ void hist_publish(const int *__restrict__ hist, int *__restrict__ out) {
+    const int t = threadIdx.x;
+    if (t < kLevels + 2) out[t] = hist[t];
+}
+
 __global__ void window_depth(const uint8_t *__restrict__ lvl, int n, int leaf, int *__restrict__ out) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     int m = 0;
@@ -317,11 +330,8 @@ static sv_status tree_levels(sv_ctx *c, Tree &T, int leaf_window) {
         SV_CK(c, cudaMalloc(&T.scratch, sizeof(int) * (size_t)kLevels * (cap / kBuildThreads + 1)));
         T.cap = cap;
     }
-    SV_CK(c, cudaMemsetAsync(T.hist, 0, sizeof(int) * (kLevels + 2), c->stream));
-    // n_act defaults to n (no inactive particle)
-    T.h_hist[kLevels + 1] = n;
-    SV_CK(c, cudaMemcpyAsync(T.hist + kLevels + 1, T.h_hist + kLevels + 1, sizeof(int), cudaMemcpyHostToDevice,
-                             c->stream));
+    hist_init<<<1, 32, 0, c->stream>>>(T.hist, n);
+    SV_LAUNCHED(c);
     split_levels<<<div_up(n, 256), 256, 0, c->stream>>>(c->S.keys, n, T.lvl, T.hist, T.hist + kLevels + 1);
     SV_LAUNCHED(c);
     if (leaf_window > 0) {
@@ -329,7 +339,13 @@ static sv_status tree_levels(sv_ctx *c, Tree &T, int leaf_window) {
         window_depth<<<div_up(n, 256), 256, 0, c->stream>>>(T.lvl, n, leaf_window, T.hist + kLevels);
         SV_LAUNCHED(c);
     }
-    SV_CK(c, cudaMemcpyAsync(T.h_hist, T.hist, sizeof(int) * (kLevels + 2), cudaMemcpyDeviceToHost, c->stream));
+    // the pinned host copy is mapped: a kernel writes it, no copy engine in the round trip
+    if (T.d_h_hist) {
+        hist_publish<<<1, 32, 0, c->stream>>>(T.hist, T.d_h_hist);
+        SV_LAUNCHED(c);
+    } else {
+        SV_CK(c, cudaMemcpyAsync(T.h_hist, T.hist, sizeof(int) * (kLevels + 2), cudaMemcpyDeviceToHost, c->stream));
+    }
     SV_CK(c, cudaStreamSynchronize(c->stream));
     T.n_act = T.h_hist[kLevels + 1];
     int acc = T.n_act > 0 ? 1 : 0;
@@ -345,6 +361,9 @@ sv_status tree_build(sv_ctx *c, int depth_rule, int param, Tree **out) {
         c->tree = new Tree();
         SV_CK(c, cudaMalloc(&c->tree->hist, sizeof(int) * (kLevels + 2)));
         SV_CK(c, cudaMallocHost(&c->tree->h_hist, sizeof(int) * (kLevels + 2)));
+        void *dp = nullptr;
+        if (cudaHostGetDevicePointer(&dp, c->tree->h_hist, 0) == cudaSuccess) c->tree->d_h_hist = (int *)dp;
+        else (void)cudaGetLastError();
     }
     Tree &T = *c->tree;
     *out = &T;

@@ -27,6 +27,7 @@ struct Tree {
     uint8_t *lvl = nullptr; // per particle: coarsest level at which it starts a box
     int *hist = nullptr;    // device histogram [levels] + n_act
     int *h_hist = nullptr;  // pinned mirror
+    int *d_h_hist = nullptr;  // its device address (mapped), null where it has none
     int *scratch = nullptr; // per-CTA, per-level box-start counts of the level builder
     void *arena = nullptr;
     size_t arena_bytes = 0;
