@@ -83,6 +83,7 @@ struct Fmm {
     // the near field runs on its own stream beside the upward and downward passes
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_lists = nullptr, ev_join = nullptr, ev_near[2] = {};
+    cudaEvent_t ev_rel = nullptr;  // the second stream's leaf offsets (F.rel) are written
     cudaEvent_t ev_m2l_lists = nullptr;  // single plume: near, interaction and far-direct lists built (second stream)
     M2LTc tc;                // the M2L on the tensor cores (m2l_tc.cu)
 };
@@ -429,14 +430,16 @@ p2m_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, 
     const double h = root[3] / (double)(1 << level);
     const int4 cb = coord[b];
     const double cx = root[0] + (cb.x + 0.5) * h, cy = root[1] + (cb.y + 0.5) * h, cz = root[2] + (cb.z + 0.5) * h;
-    const double ih = 1.0 / h;
+    // the offset in FP64 (positions are large), its scaling in FP32: the FP64
+    // pipe runs at 1/64 of the FP32 rate on this GPU
+    const float ihf = (float)(1.0 / h);
     float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
     const int s0 = start[b], s1 = start[b + 1];
     for (int base = s0; base < s1; base += 32) {
         const int i = base + lane;
         float2 R[NC];
         if (i < s1) {
-            solid_harmonics<P>((float)((xs[i] - cx) * ih), (float)((ys[i] - cy) * ih), (float)((zs[i] - cz) * ih), R);
+            solid_harmonics<P>((float)(xs[i] - cx) * ihf, (float)(ys[i] - cy) * ihf, (float)(zs[i] - cz) * ihf, R);
             const float q = qs[i];
 #pragma unroll
             for (int c = 0; c < NC; c++) buf[wid][lane][c] = make_float2(q * R[c].x, -q * R[c].y);
@@ -866,8 +869,7 @@ inline int m2l_chunks(int nbox) {
 template <int P>
 __global__ void __launch_bounds__(kWarps * 32)
 l2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, const int *__restrict__ start,
-           const int4 *__restrict__ coord, const double *__restrict__ xs, const double *__restrict__ ys,
-           const double *__restrict__ zs, const double *__restrict__ qm, const double *__restrict__ roots, int level,
+           const float4 *__restrict__ rel, const double *__restrict__ qm, const double *__restrict__ roots, int level,
            const float *__restrict__ nrm, const float2 *__restrict__ Lc, double *__restrict__ ax,
            double *__restrict__ ay, double *__restrict__ az, const int *__restrict__ has_tgt, int accumulate) {
     constexpr int NC = ncoef(P);
@@ -886,14 +888,16 @@ l2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, 
         lam[wid][c] = cscale(Lc[(size_t)b * NC + c], nrm[n * P + m]);
     }
     __syncwarp();
+    // Positions relative to the leaf box centre come from box_relative_kernel
+    // (FP32, metres); the per-particle work stays on the FP32 pipe, the FP64
+    // pipe (1/64 of its rate on this GPU) sees only the stores' conversions.
     const double h = root[3] / (double)(1 << level);
-    const int4 cb = coord[b];
-    const double cx = root[0] + (cb.x + 0.5) * h, cy = root[1] + (cb.y + 0.5) * h, cz = root[2] + (cb.z + 0.5) * h;
-    const double ih = 1.0 / h;
+    const float ihf = (float)(1.0 / h), mih2 = (float)(-1.0 / (h * h));
     const int s1 = start[b + 1];
     for (int i = start[b] + lane; i < s1; i += 32) {
         float2 R[ncoef(P - 1) > 0 ? ncoef(P - 1) : 1];
-        solid_harmonics<P - 1>((float)((xs[i] - cx) * ih), (float)((ys[i] - cy) * ih), (float)((zs[i] - cz) * ih), R);
+        const float4 r = rel[i];
+        solid_harmonics<P - 1>(r.x * ihf, r.y * ihf, r.z * ihf, R);
         float gz = 0.f;
         float2 gm = make_float2(0.f, 0.f);
 #pragma unroll
@@ -912,15 +916,16 @@ l2p_kernel(int nbox, const int *__restrict__ nbd, const int *__restrict__ bpid, 
         }
         // a = -grad(phi) * K q / m, grad in box units / h^2 (added to the
         // near field when that ran first)
-        const double f = -qm[i] * ih * ih;
+        const float f = (float)qm[i] * mih2;
+        const float vx = f * gm.x, vy = -f * gm.y, vz = f * gz;
         if (accumulate) {
-            ax[i] += f * (double)gm.x;
-            ay[i] += f * (double)(-gm.y);
-            az[i] += f * (double)gz;
+            ax[i] += (double)vx;
+            ay[i] += (double)vy;
+            az[i] += (double)vz;
         } else {
-            ax[i] = f * (double)gm.x;
-            ay[i] = f * (double)(-gm.y);
-            az[i] = f * (double)gz;
+            ax[i] = (double)vx;
+            ay[i] = (double)vy;
+            az[i] = (double)vz;
         }
     }
     __syncwarp();
@@ -1517,6 +1522,7 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
         box_relative_kernel<<<div_up(V.nbox, kWarps), kWarps * 32, 0, F.side>>>(
             V.nbox, nullptr, nullptr, V.start, V.coord, S.x, S.y, S.z, S.q, S.root, L, F.rel, F.d_counts + 2);
         SV_LAUNCHED(c);
+        SV_CK(c, cudaEventRecord(F.ev_rel, F.side));
         if (c->P.profile_phases) SV_CK(c, cudaEventRecord(F.ev_near[0], F.side));
         launch_p2p(ws, (float)c->P.softening2, div_up(V.nbox, kWarps), F.side, V.nbox, nullptr, nullptr, V.start,
                    V.coord, nbr[L], S.qm, S.root, L, S.ax, S.ay, S.az, F.d_counts, tgt[L], F.rel, la.lv[L].fd,
@@ -1675,9 +1681,9 @@ sv_status run_fmm(sv_ctx *c, Fmm &F, Tree &T) {
             SV_LAUNCHED(c);
             S.far = F.far;
         } else if (L >= 2) {
+            SV_CK(c, cudaStreamWaitEvent(c->stream, F.ev_rel, 0));  // the leaf offsets of the second stream
             l2p_kernel<P><<<div_up(V.nbox, kWarps), kWarps * 32, 0, c->stream>>>(
-                V.nbox, nullptr, nullptr, V.start, V.coord, S.x, S.y, S.z, S.qm, S.root, L, F.nrm, Lv[L], fx, fy, fz,
-                tgt[L], 0);
+                V.nbox, nullptr, nullptr, V.start, F.rel, S.qm, S.root, L, F.nrm, Lv[L], fx, fy, fz, tgt[L], 0);
             SV_LAUNCHED(c);
             S.far = F.far;
         }
@@ -1861,9 +1867,8 @@ sv_status run_fmm_forest(sv_ctx *c, Fmm &F, const ForestArgs &fa) {
     {
         const Level &V = T.lv[L];
         const int g = forest_grid(f.cap[L], kWarps);
-        l2p_kernel<P><<<g, kWarps * 32, 0, c->stream>>>(f.cap[L], nbd + L, V.pid, V.start, V.coord, S.x, S.y, S.z,
-                                                        S.qm, fa.roots, L, F.nrm, F.fL[L], S.ax, S.ay, S.az,
-                                                        F.ftgt[L], 1);
+        l2p_kernel<P><<<g, kWarps * 32, 0, c->stream>>>(f.cap[L], nbd + L, V.pid, V.start, F.frel, S.qm, fa.roots,
+                                                        L, F.nrm, F.fL[L], S.ax, S.ay, S.az, F.ftgt[L], 1);
         SV_LAUNCHED(c);
     }
     SV_CK(c, cudaMemcpyAsync(F.h_counts, F.d_counts, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
@@ -1918,6 +1923,7 @@ void fmm_free(sv_ctx *c) {
     if (F.ev_join) cudaEventDestroy(F.ev_join);
     if (F.ev_lists) cudaEventDestroy(F.ev_lists);
     if (F.ev_m2l_lists) cudaEventDestroy(F.ev_m2l_lists);
+    if (F.ev_rel) cudaEventDestroy(F.ev_rel);
     for (cudaEvent_t e : F.ev_near)
         if (e) cudaEventDestroy(e);
     c->near_ev[0] = c->near_ev[1] = nullptr;
@@ -1936,6 +1942,7 @@ static sv_status fmm_state(sv_ctx *c) {
         SV_CK(c, cudaEventCreateWithFlags(&F.ev_join, cudaEventDisableTiming));
         SV_CK(c, cudaEventCreateWithFlags(&F.ev_lists, cudaEventDisableTiming));
         SV_CK(c, cudaEventCreateWithFlags(&F.ev_m2l_lists, cudaEventDisableTiming));
+        SV_CK(c, cudaEventCreateWithFlags(&F.ev_rel, cudaEventDisableTiming));
         SV_CK(c, cudaEventCreate(&F.ev_near[0]));
         SV_CK(c, cudaEventCreate(&F.ev_near[1]));
     }
