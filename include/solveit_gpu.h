@@ -163,6 +163,14 @@ SV_API sv_status sv_upload_ref32(sv_ctx *ctx, int64_t n, const float *pos4,
                           const float *vel4, const float *acc4,
                           const float *t_inj);
 SV_API sv_status sv_download(sv_ctx *ctx, double *x3, double *v3, int32_t *status);
+/* Replace the uploaded plume's positions, velocities and statuses (the arrays
+ * the reference's integrator advances, particles.h:99-105: position,
+ * velocity, acceleration.w) and keep its charges, masses, injection times and
+ * run state (events, energy records, snapshot fields, substep levels).  n must
+ * be the uploaded count; v3 and status may be null to keep them.  The same
+ * transfers as sv_upload: pinned, mapped arrays are read in place. */
+SV_API sv_status sv_update_state(sv_ctx *ctx, int64_t n, const double *x3, const double *v3,
+                                 const int32_t *status);
 SV_API sv_status sv_download_ref32(sv_ctx *ctx, float *pos4, float *vel4);
 
 /* One force evaluation with the context's method: the body of

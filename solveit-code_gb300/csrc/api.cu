@@ -228,6 +228,23 @@ __global__ void unpack_mapped(const double *__restrict__ x3, const double *__res
     }
 }
 
+// sv_update_state's unpacking: positions, velocities (optional) and statuses
+// (optional), from device staging or in place from mapped host memory, each
+// thread taking consecutive doubles of the interleaved arrays
+__global__ void unpack_state(const double *__restrict__ x3, const double *__restrict__ v3,
+                             const int32_t *__restrict__ st, int64_t n, double *__restrict__ x,
+                             double *__restrict__ y, double *__restrict__ z, double *__restrict__ vx,
+                             double *__restrict__ vy, double *__restrict__ vz, int32_t *__restrict__ so) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < 3 * n; t += stride) {
+        const int64_t i = t / 3;
+        const int d = (int)(t - 3 * i);
+        (d == 0 ? x : (d == 1 ? y : z))[i] = x3[t];
+        if (v3) (d == 0 ? vx : (d == 1 ? vy : vz))[i] = v3[t];
+        if (st && t < n) so[t] = st[t];
+    }
+}
+
 // ParticleSpeciesFunction::getMass (particles.h:65-87): EMI 111, BF4 87 amu
 __device__ double species_mass(int s) {
     switch (s) {
@@ -828,6 +845,36 @@ sv_status sv_upload_ref32(sv_ctx *c, int64_t n, const float *pos4, const float *
                                                     c->vx, c->vy, c->vz, c->q, c->m, c->status, c->t_inj);
     SV_LAUNCHED(c);
     charge_over_mass<<<grid_of(n), 256, 0, c->stream>>>(c->q, c->m, n, c->qom, c->species);
+    SV_LAUNCHED(c);
+    return SV_OK;
+}
+
+sv_status sv_update_state(sv_ctx *c, int64_t n, const double *x3, const double *v3, const int32_t *status) {
+    if (!c || !x3) return SV_ERR_INVALID;
+    if (!c->have_state) return set_error(c, SV_ERR_STATE, "no state uploaded");
+    if (c->batch) return set_error(c, SV_ERR_UNSUPPORTED, "a batch's state is replaced by sv_upload_batch");
+    if (n != c->n) return set_error(c, SV_ERR_INVALID, "n=%lld, the uploaded plume has %lld", (long long)n,
+                                    (long long)c->n);
+    SV_CK(c, cudaSetDevice(c->device));
+    c->have_accel = false;
+    if (n == 0) return SV_OK;
+    const double *mx = (const double *)mapped_host(x3), *mv = (const double *)mapped_host(v3);
+    const int32_t *ms = (const int32_t *)mapped_host(status);
+    if (mx && (!v3 || mv) && (!status || ms)) {  // pinned, mapped arrays: read in place
+        unpack_state<<<link_grid(3 * n), 256, 0, c->stream>>>(mx, mv, ms, n, c->x, c->y, c->z, c->vx, c->vy, c->vz,
+                                                             c->status);
+        SV_LAUNCHED(c);
+        return SV_OK;
+    }
+    const size_t b3 = sizeof(double) * 3 * (size_t)n;
+    void *stg = nullptr;
+    SV_TRY(stage_bytes(c, 2 * b3 + sizeof(int32_t) * (size_t)n, &stg));
+    double *dx3 = (double *)stg, *dv3 = dx3 + 3 * n;
+    int32_t *ds = (int32_t *)(dv3 + 3 * n);
+    const HostCopy cp[3] = {{dx3, x3, b3}, {dv3, v3, v3 ? b3 : 0}, {ds, status, status ? sizeof(int32_t) * (size_t)n : 0}};
+    SV_TRY(copy_split(c, cp, 3, cudaMemcpyHostToDevice));
+    unpack_state<<<link_grid(3 * n), 256, 0, c->stream>>>(dx3, v3 ? dv3 : nullptr, status ? ds : nullptr, n, c->x,
+                                                         c->y, c->z, c->vx, c->vy, c->vz, c->status);
     SV_LAUNCHED(c);
     return SV_OK;
 }

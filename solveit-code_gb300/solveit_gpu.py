@@ -123,6 +123,7 @@ def load(path: str = LIB_PATH):
     L.sv_upload.argtypes = [vp, C.c_int64, vp, vp, vp, vp, vp, vp]
     L.sv_upload_ref32.argtypes = [vp, C.c_int64, vp, vp, vp, vp]
     L.sv_download.argtypes = [vp, vp, vp, vp]
+    L.sv_update_state.argtypes = [vp, C.c_int64, vp, vp, vp]
     L.sv_download_ref32.argtypes = [vp, vp, vp]
     L.sv_compute_accel.argtypes = [vp, C.c_int64, C.c_int64, vp]
     L.sv_add_accel_ref32.argtypes = [vp, vp]
@@ -279,6 +280,13 @@ class ForceMethod:
         b = BatchInfo()
         self._check(self.L.sv_batch_get_info(self.h, C.byref(b)))
         return b
+
+    def update_state(self, x, v=None, status=None):
+        """sv_update_state: new positions (and velocities, statuses) for the uploaded plume."""
+        x = np.ascontiguousarray(x, np.float64)
+        v = None if v is None else np.ascontiguousarray(v, np.float64)
+        st = None if status is None else np.ascontiguousarray(status, np.int32)
+        self._check(self.L.sv_update_state(self.h, x.shape[0], _p(x), _p(v), _p(st)))
 
     def download(self):
         x = np.zeros((self.n, 3), np.float64)

@@ -71,6 +71,43 @@ def test_pinned_and_pageable_paths_agree():
         assert np.array_equal(xb.numpy(), fa.download()[0])
 
 
+def test_update_state_continues_a_run():
+    """sv_update_state with the downloaded state (pinned or pageable arrays)
+    changes nothing: one step, update, two steps equals three steps, bit for
+    bit (the FMM is deterministic); the wrong count and a state-less context
+    are refused."""
+    st = plume.make_plume(N, 1e-6, 13)
+    kw = dict(softening2=EPS20, method=sv.FMM, efield=(0.0, 0.0, 1e8))
+    L = sv.load()
+    with sv.ForceMethod(**kw) as fa:
+        fa.upload(st)
+        fa.leapfrog(3, 1e-13, 0.0)
+        xa, va, sa = fa.download()
+    for pinned in (False, True):
+        with sv.ForceMethod(**kw) as fb:
+            fb.upload(st)
+            fb.leapfrog(1, 1e-13, 0.0)
+            x, v, s = fb.download()
+            if pinned:
+                px, pv, ps = _pinned(x), _pinned(v), _pinned(s)
+                assert L.sv_update_state(fb.h, N, _p(px), _p(pv), _p(ps)) == 0
+            else:
+                fb.update_state(x, v, s)
+            fb.leapfrog(2, 1e-13, 1e-13)
+            xb, vb, sb = fb.download()
+        assert np.array_equal(xb, xa) and np.array_equal(vb, va) and np.array_equal(sb, sa)
+    with sv.ForceMethod(**kw) as fc:
+        with pytest.raises(sv.SolveitError):
+            fc.update_state(st["x"])
+        fc.upload(st)
+        with pytest.raises(sv.SolveitError):
+            fc.update_state(st["x"][:10])
+        # positions only: velocities and statuses stay
+        fc.update_state(st["x"] + 1e-9)
+        x, v, s = fc.download()
+        assert np.array_equal(x, st["x"] + 1e-9) and np.array_equal(v, st["v"]) and np.array_equal(s, st["status"])
+
+
 def test_adapter_add_accel_uses_the_context_buffer():
     """sv_add_accel_ref32 adds the last acceleration into the reference's
     float4 array through the context's own pinned buffer."""
